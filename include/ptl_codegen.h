@@ -1,0 +1,119 @@
+/*
+ * ptilopsis_gb300 -- GB300 (sm_103a) implementation of Ptilopsis's data-parallel RISC-V
+ * code generator, behind a plain C ABI.
+ *
+ * The reference's interface is the C++ class rv_generator_avx
+ * (include/codegen/rv_generator_avx.hpp:58, src/codegen/rv_generator_avx.cpp:21-120 of
+ * the reference): construct it from a DepthTree (the flattened post-order AST of
+ * pareas-ast, subprojects/pareas-ast/include/codegen/depthtree.hpp:12-59), call
+ * process(profile) (include/codegen/rv_generator.hpp:67), read get_instructions()
+ * (src/codegen/rv_generator_avx.cpp:82-84) and, through the protected members
+ * func_starts/func_ends/function_sizes/function_ids (include/codegen/rv_generator.hpp:
+ * 46-51), the function table.  Each entry point below names the call it replaces.
+ *
+ * Output is bit-identical to the reference's one-worker-thread run of that class.
+ * Errors are status codes; no C++ exception crosses this boundary.  A generator is not
+ * thread-safe; distinct generators may be used from distinct threads.
+ */
+#ifndef PTL_CODEGEN_H
+#define PTL_CODEGEN_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    PTL_OK = 0,
+    PTL_INVALID_AST = 1,        /* the arrays violate the DepthTree contract */
+    PTL_UNSUPPORTED = 2,        /* input reaches behaviour the reference leaves undefined */
+    PTL_OOM = 3,                /* device memory exhausted */
+    PTL_ADMISSION_DENIED = 4,   /* a compile server refused the request (memory budget) */
+    PTL_DEVICE_TIMEOUT = 5,     /* a bounded device-side wait gave up */
+    PTL_CUDA_ERROR = 6,
+    PTL_BAD_ARGUMENT = 7
+} ptl_status;
+
+/* A DepthTree: six parallel arrays of n nodes in post-order (children before parents,
+ * the root last with parent -1 and child index -1).  type is the Pareas NodeType
+ * (astnode.hpp:11-56), rtype the Pareas DataType (datatype.hpp:7-14).  With on_device
+ * != 0 the pointers are CUDA device pointers on the generator's device. */
+typedef struct {
+    size_t n;
+    size_t max_depth;
+    const uint8_t* type;
+    const uint8_t* rtype;
+    const int32_t* parent;
+    const int32_t* depth;
+    const int32_t* child_idx;
+    const uint32_t* data;
+    int on_device;
+} ptl_ast_view;
+
+typedef struct ptl_generator ptl_generator;
+
+/* Replaces rv_generator_avx(const DepthTree&, concurrency, sync, altblock, mininstr)
+ * (rv_generator_avx.hpp:58): copies the tree to the device.  The scheduling arguments
+ * of the CPU constructor have no GPU meaning and are not taken. */
+ptl_status ptl_generator_create(const ptl_ast_view* tree, int device, ptl_generator** out);
+
+/* Replaces rv_generator_avx::process(bool profile) (rv_generator_avx.cpp:104-120): runs
+ * the seven stages.  Unlike the reference, which mutates its arrays and cannot be run
+ * twice, process may be called again and recompiles from the copied tree. */
+ptl_status ptl_generator_process(ptl_generator* gen, int profile);
+
+/* Replaces get_instructions() (rv_generator_avx.cpp:82-84): the encoded RV words, in a
+ * host buffer owned by the generator, valid until the next process or destroy. */
+ptl_status ptl_generator_instructions(ptl_generator* gen, const uint32_t** words, size_t* count);
+
+/* The same words as a device pointer (no copy). */
+ptl_status ptl_generator_device_instructions(ptl_generator* gen, const uint32_t** words, size_t* count);
+
+/* The function table the reference keeps in func_starts, func_ends, function_sizes and
+ * function_ids (rv_generator.hpp:46-51), after its final fix_func_tab
+ * (rv_generator_avx.cpp:1992).  Host buffers owned by the generator. */
+ptl_status ptl_generator_function_table(ptl_generator* gen, const uint32_t** starts,
+                                        const uint32_t** ends, const uint32_t** sizes,
+                                        const uint32_t** ids, size_t* count);
+
+/* Per-stage device time of the last process(profile != 0), in the order of the
+ * reference's -p CSV (rv_generator.cpp:142-162): preprocess, isn_cnt, isn_gen,
+ * optimize, regalloc, fix_jumps, postprocess (the last is fused into fix_jumps and
+ * reported as 0). */
+ptl_status ptl_generator_stage_ns(ptl_generator* gen, uint64_t ns[7]);
+
+/* Human-readable detail of the last non-OK status. */
+const char* ptl_generator_last_error(const ptl_generator* gen);
+
+void ptl_generator_destroy(ptl_generator* gen);
+
+/* One-shot compile of a host tree into a caller buffer.  With words == NULL or a too
+ * small capacity, *count receives the required size and PTL_BAD_ARGUMENT is returned
+ * when words was given. */
+ptl_status ptl_compile(const ptl_ast_view* tree, int device, uint32_t* words, size_t capacity,
+                       size_t* count);
+
+/* Intermediate arrays of the last process, for stage-by-stage parity checks.  which
+ * selects the same arrays, in the same order, as the reference generator's members
+ * after each stage (see ptilopsis_gb300/codegen.py SNAPSHOTS). */
+ptl_status ptl_generator_snapshot(ptl_generator* gen, int which, uint32_t* out, size_t capacity,
+                                  size_t* count);
+
+/* The code tables in the reference's flat layouts (rv_nodetype.hpp:197-1134):
+ * which = 0 node_size[256][6], 1 has_instr[256][4][6], 2 has_output[256][4][6],
+ * 3 parent_arg_idx[256][4][6], 4 get_output[256][4][6], 5 instr[256][4][6],
+ * 6 instr_constant[256][4], 7 operand[256][4][6][2], 8 instr_jt[256][4],
+ * 9 pareas_to_rv[44].  Returns the element count; out may be NULL. */
+size_t ptl_code_table(int which, uint32_t* out);
+
+/* Library and device facts: CUDA runtime/driver versions, device name. */
+ptl_status ptl_device_info(int device, char* name, size_t name_len, int* sm_count,
+                           int* cc_major, int* cc_minor);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,685 @@
+// C ABI of the GB300 code generator (include/ptl_codegen.h): generator objects, the
+// device arena and the stage sequence.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/ptl_codegen.h"
+#include "ptl_kernels.cuh"
+
+namespace ptl {
+namespace {
+
+constexpr size_t kFrontPad = 16;  // elements before index 0 (the reference reads [-1])
+constexpr size_t kBackPad = 80;   // elements after the last 8-lane block
+
+// A device buffer with the reference's padding around it.
+struct DevBuf {
+    void* base = nullptr;
+    size_t bytes = 0;
+    size_t elem = 4;
+    size_t count = 0;  // logical capacity in elements (without pads)
+
+    template <typename T>
+    T* at() const { return base ? reinterpret_cast<T*>(static_cast<char*>(base) + kFrontPad * elem) : nullptr; }
+
+    cudaError_t ensure(size_t n, size_t esize) {
+        const size_t need = (n + kFrontPad + kBackPad) * esize;
+        if (base && bytes >= need && elem == esize) {
+            count = n;
+            return cudaSuccess;
+        }
+        if (base) cudaFree(base);
+        base = nullptr;
+        bytes = 0;
+        const size_t grow = need + need / 4;  // room to grow without reallocating
+        cudaError_t e = cudaMalloc(&base, grow);
+        if (e != cudaSuccess) { base = nullptr; return e; }
+        bytes = grow;
+        elem = esize;
+        count = n;
+        return cudaSuccess;
+    }
+    cudaError_t zero(cudaStream_t s) const { return base ? cudaMemsetAsync(base, 0, (count + kFrontPad + kBackPad) * elem, s) : cudaSuccess; }
+    cudaError_t fill(cudaStream_t s, int byte) const { return base ? cudaMemsetAsync(base, byte, (count + kFrontPad + kBackPad) * elem, s) : cudaSuccess; }
+    void release() { if (base) cudaFree(base); base = nullptr; bytes = 0; }
+};
+
+const CodeTables& host_tables() {
+    static CodeTables t;
+    static std::once_flag once;
+    std::call_once(once, [] { build_code_tables(&t); });
+    return t;
+}
+
+inline size_t r8(size_t n) { return (n + 7) & ~size_t(7); }
+
+}  // namespace
+
+// Input checks: the DepthTree contract (post-order, one root, consistent depths).
+__global__ void k_validate(const uint8_t* type, const uint8_t* rtype, const int32_t* parent,
+                           const int32_t* depth, const int32_t* child, uint32_t n, uint32_t max_depth,
+                           ErrorWord* err) {
+    for (uint64_t k = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x; k < n;
+         k += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+        const uint32_t i = static_cast<uint32_t>(k);
+        bool bad = type[i] >= kNumPareasTypes || rtype[i] > 5;
+        const int32_t p = parent[i];
+        if (i == n - 1) {
+            bad |= p != -1 || depth[i] != 0;
+        } else {
+            bad |= p <= static_cast<int32_t>(i) || p >= static_cast<int32_t>(n) || child[i] < 0;
+            if (!bad) bad |= depth[i] != depth[p] + 1;
+        }
+        bad |= depth[i] < 0 || static_cast<uint32_t>(depth[i]) > max_depth;
+        if (bad) record_error(err, ST_INVALID_AST, 0, i);
+    }
+}
+
+__global__ void k_init_lifetime(unsigned long long* lt, uint32_t F) {
+    for (uint64_t k = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x; k < F;
+         k += static_cast<uint64_t>(gridDim.x) * blockDim.x)
+        lt[k] = 0x1Full;
+}
+
+__global__ void k_depth_seen(const int32_t* depth, uint32_t n, uint32_t* seen) {
+    for (uint64_t k = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x; k < n;
+         k += static_cast<uint64_t>(gridDim.x) * blockDim.x)
+        seen[depth[k]] = 1;
+}
+
+}  // namespace ptl
+
+using namespace ptl;
+
+struct ptl_generator {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::string last_error;
+
+    // input (device copy)
+    size_t n = 0, max_depth = 0;
+    DevBuf in_type, in_rtype, in_parent, in_depth, in_child, in_data;
+    // node arrays
+    DevBuf nt, rt, nd1, nd, par, ci, dep, fflag, sizes, loc0, loc, pos, regs;
+    DevBuf decl, fn_id, fn_start, fn_size, fn_end, fn_start0, fn_size0, fn_end0;
+    DevBuf fn_ra_start, fn_ra_end, fn_ra_size;
+    DevBuf instr, rd, rs1, rs2, jt, owner, used, smark, used_instrs;
+    DevBuf symreg, symswp, stamp, lifetime, trig_min, trig_max, spill, roffs;
+    DevBuf ni, nrd, nr1, nr2, njt, fsz, joffs, out;
+    DevBuf sort_a, sort_apos, sort_bpos, sort_seg0, sort_seg1, sort_tile_seg, sort_tile_l, sort_tile_r,
+        sort_leaf, sort_heap, sort_counters;
+    DevBuf scan_status, scan_counter, meta, flags, errw, tables, depth_seen;
+
+    // results
+    uint32_t F = 0, W = 0, W2 = 0, W3 = 0, S = 0;
+    std::vector<uint32_t> words, fn_start_h, fn_end_h, fn_size_h, fn_id_h;
+    bool host_valid = false;
+    uint64_t stage_ns[7] = {0, 0, 0, 0, 0, 0, 0};
+    uint32_t sort_rounds = 0, opt_sweeps = 0;
+    bool ra_serial = false;
+
+    ~ptl_generator() {
+        for (DevBuf* b : all()) b->release();
+        if (stream) cudaStreamDestroy(stream);
+    }
+    std::vector<DevBuf*> all() {
+        return {&in_type, &in_rtype, &in_parent, &in_depth, &in_child, &in_data, &nt, &rt, &nd1, &nd,
+                &par, &ci, &dep, &fflag, &sizes, &loc0, &loc, &pos, &regs, &decl, &fn_id, &fn_start,
+                &fn_size, &fn_end, &fn_start0, &fn_size0, &fn_end0, &fn_ra_start, &fn_ra_end, &fn_ra_size,
+                &instr, &rd, &rs1, &rs2, &jt, &owner, &used, &smark, &used_instrs, &symreg, &symswp,
+                &stamp, &lifetime, &trig_min, &trig_max, &spill, &roffs, &ni, &nrd, &nr1, &nr2, &njt,
+                &fsz, &joffs, &out, &sort_a, &sort_apos, &sort_bpos, &sort_seg0, &sort_seg1,
+                &sort_tile_seg, &sort_tile_l, &sort_tile_r, &sort_leaf, &sort_heap, &sort_counters,
+                &scan_status, &scan_counter, &meta, &flags, &errw, &tables, &depth_seen};
+    }
+};
+
+namespace {
+
+ptl_status fail(ptl_generator* g, ptl_status st, const std::string& msg) {
+    if (g) g->last_error = msg;
+    return st;
+}
+
+ptl_status cuda_fail(ptl_generator* g, cudaError_t e, const char* what) {
+    const ptl_status st = (e == cudaErrorMemoryAllocation) ? PTL_OOM : PTL_CUDA_ERROR;
+    return fail(g, st, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define PTL_CU(expr)                                          \
+    do {                                                      \
+        const cudaError_t e_ = (expr);                        \
+        if (e_ != cudaSuccess) return cuda_fail(g, e_, #expr); \
+    } while (0)
+
+Prog make_prog(ptl_generator* g) {
+    Prog P{};
+    P.n = static_cast<uint32_t>(g->n);
+    P.nb8 = static_cast<uint32_t>(r8(g->n));
+    P.max_depth = static_cast<uint32_t>(g->max_depth);
+    P.F = g->F;
+    P.fb8 = static_cast<uint32_t>(r8(g->F));
+    P.W = g->W;
+    P.wb8 = static_cast<uint32_t>(r8(g->W));
+    P.W2 = g->W2;
+    P.w2b8 = static_cast<uint32_t>(r8(g->W2));
+    P.W3 = g->W3;
+    P.S = g->S;
+    P.in_type = g->in_type.at<uint8_t>();
+    P.in_rtype = g->in_rtype.at<uint8_t>();
+    P.in_parent = g->in_parent.at<int32_t>();
+    P.in_depth = g->in_depth.at<int32_t>();
+    P.in_child = g->in_child.at<int32_t>();
+    P.in_data = g->in_data.at<uint32_t>();
+    P.nt = g->nt.at<uint32_t>();
+    P.rt = g->rt.at<uint32_t>();
+    P.nd1 = g->nd1.at<uint32_t>();
+    P.nd = g->nd.at<uint32_t>();
+    P.par = g->par.at<int32_t>();
+    P.ci = g->ci.at<int32_t>();
+    P.dep = g->dep.at<int32_t>();
+    P.fflag = g->fflag.at<uint8_t>();
+    P.sizes = g->sizes.at<uint32_t>();
+    P.loc0 = g->loc0.at<uint32_t>();
+    P.loc = g->loc.at<uint32_t>();
+    P.regs = g->regs.at<uint32_t>();
+    P.pos = g->pos.at<uint32_t>();
+    P.owner = g->owner.at<unsigned long long>();
+    P.decl = g->decl.at<uint32_t>();
+    P.fn_id = g->fn_id.at<uint32_t>();
+    P.fn_start = g->fn_start.at<uint32_t>();
+    P.fn_size = g->fn_size.at<uint32_t>();
+    P.fn_end = g->fn_end.at<uint32_t>();
+    P.fn_start0 = g->fn_start0.at<uint32_t>();
+    P.fn_size0 = g->fn_size0.at<uint32_t>();
+    P.instr = g->instr.at<uint32_t>();
+    P.rd = g->rd.at<uint32_t>();
+    P.rs1 = g->rs1.at<uint32_t>();
+    P.rs2 = g->rs2.at<uint32_t>();
+    P.jt = g->jt.at<uint32_t>();
+    P.used = g->used.at<uint8_t>();
+    P.smark = g->smark.at<uint8_t>();
+    P.used_instrs = g->used_instrs.at<uint32_t>();
+    P.symreg = g->symreg.at<uint32_t>();
+    P.symswp = g->symswp.at<uint32_t>();
+    P.stamp = g->stamp.at<uint32_t>();
+    P.lifetime = g->lifetime.at<unsigned long long>();
+    P.trig_min = g->trig_min.at<uint32_t>();
+    P.trig_max = g->trig_max.at<uint32_t>();
+    P.spill = g->spill.at<uint32_t>();
+    P.roffs = g->roffs.at<uint32_t>();
+    P.ni = g->ni.at<uint32_t>();
+    P.nrd = g->nrd.at<uint32_t>();
+    P.nr1 = g->nr1.at<uint32_t>();
+    P.nr2 = g->nr2.at<uint32_t>();
+    P.njt = g->njt.at<uint32_t>();
+    P.fsz = g->fsz.at<uint32_t>();
+    P.joffs = g->joffs.at<uint32_t>();
+    P.out = g->out.at<uint32_t>();
+    P.tab.t = g->tables.at<CodeTables>();
+    P.err = g->errw.at<ErrorWord>();
+    P.flags = g->flags.at<uint32_t>();
+    return P;
+}
+
+ptl_status check_error_word(ptl_generator* g) {
+    ErrorWord e{};
+    cudaError_t ce = cudaMemcpyAsync(&e, g->errw.at<ErrorWord>(), sizeof(e), cudaMemcpyDeviceToHost, g->stream);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(g->stream);
+    if (ce != cudaSuccess) return cuda_fail(g, ce, "error word");
+    if (e.code == ST_OK) return PTL_OK;
+    static const char* stages[] = {"input", "preprocess", "isn_cnt", "depth sort", "isn_gen", "optimize",
+                                   "regalloc", "regalloc (lane 0)", "regalloc scatter", "fix_jumps", "scan"};
+    char buf[256];
+    std::snprintf(buf, sizeof buf, "%s: %s at index %u",
+                  e.where < sizeof(stages) / sizeof(stages[0]) ? stages[e.where] : "?",
+                  e.code == ST_INVALID_AST ? "input violates the DepthTree contract"
+                  : e.code == ST_DEVICE_TIMEOUT ? "bounded device wait gave up"
+                                                : "input reaches behaviour the reference leaves undefined",
+                  e.detail);
+    return fail(g, static_cast<ptl_status>(e.code), buf);
+}
+
+template <typename T>
+cudaError_t read1(ptl_generator* g, const T* dptr, T* out) {
+    cudaError_t e = cudaMemcpyAsync(out, dptr, sizeof(T), cudaMemcpyDeviceToHost, g->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+    return e;
+}
+
+struct StageTimer {
+    ptl_generator* g;
+    bool on;
+    cudaEvent_t ev[8] = {};
+    int k = 0;
+    StageTimer(ptl_generator* gen, bool enable) : g(gen), on(enable) {
+        if (!on) return;
+        for (auto& e : ev) cudaEventCreate(&e);
+        cudaEventRecord(ev[0], g->stream);
+    }
+    void mark() {
+        if (on && k < 7) cudaEventRecord(ev[++k], g->stream);
+    }
+    void finish() {
+        if (!on) return;
+        cudaEventSynchronize(ev[k]);
+        for (int s = 0; s < 7; ++s) {
+            float ms = 0;
+            if (s < k) cudaEventElapsedTime(&ms, ev[s], ev[s + 1]);
+            g->stage_ns[s] = static_cast<uint64_t>(ms * 1e6);
+        }
+    }
+    ~StageTimer() {
+        if (on) for (auto& e : ev) cudaEventDestroy(e);
+    }
+};
+
+ptl_status run_pipeline(ptl_generator* g, bool profile, bool to_host) {
+    cudaStream_t s = g->stream;
+    const size_t n = g->n;
+    const size_t nb8 = r8(n);
+    g->host_valid = false;
+    StageTimer timer(g, profile);
+
+    PTL_CU(g->errw.zero(s));
+    PTL_CU(g->meta.zero(s));
+    // node arrays
+    for (DevBuf* b : {&g->nt, &g->rt, &g->nd1, &g->nd, &g->par, &g->ci, &g->dep, &g->sizes, &g->loc0, &g->loc, &g->pos}) {
+        PTL_CU(b->ensure(nb8, 4));
+        PTL_CU(b->zero(s));
+    }
+    PTL_CU(g->fflag.ensure(nb8, 1));
+    PTL_CU(g->fflag.zero(s));
+    PTL_CU(g->decl.ensure(nb8, 4));
+    PTL_CU(g->decl.zero(s));
+    PTL_CU(g->regs.ensure(3 * n, 4));
+    PTL_CU(g->regs.zero(s));
+    PTL_CU(g->depth_seen.ensure(g->max_depth + 1, 4));
+    PTL_CU(g->depth_seen.zero(s));
+    const size_t scan_tiles = (std::max(nb8, size_t(1)) + 4095) / 4096 + 8;
+    PTL_CU(g->scan_status.ensure(scan_tiles, 8));
+    PTL_CU(g->scan_counter.ensure(1, 4));
+
+    g->F = g->W = g->W2 = g->W3 = g->S = 0;
+    Prog P = make_prog(g);
+    ScanScratch sc{g->scan_status.at<unsigned long long>(), g->scan_counter.at<uint32_t>(),
+                   static_cast<uint32_t>(scan_tiles)};
+
+    // ---- input checks
+    k_validate<<<std::min<size_t>((n + 255) / 256, 152 * 16), 256, 0, s>>>(
+        P.in_type, P.in_rtype, P.in_parent, P.in_depth, P.in_child, P.n, P.max_depth, P.err);
+    k_depth_seen<<<std::min<size_t>((n + 255) / 256, 152 * 16), 256, 0, s>>>(P.in_depth, P.n,
+                                                                             g->depth_seen.at<uint32_t>());
+    if (ptl_status st = check_error_word(g); st != PTL_OK) return st;
+    {
+        std::vector<uint32_t> seen(g->max_depth + 1);
+        PTL_CU(cudaMemcpyAsync(seen.data(), g->depth_seen.at<uint32_t>(), seen.size() * 4, cudaMemcpyDeviceToHost, s));
+        PTL_CU(cudaStreamSynchronize(s));
+        for (uint32_t v : seen) {
+            if (!v) return fail(g, PTL_INVALID_AST, "input: depths 0..max_depth are not all populated");
+        }
+    }
+
+    // ---- preprocess
+    launch_translate(P, s);
+    launch_preprocess(P, s);
+    timer.mark();
+
+    // ---- isn_cnt: count + scan, fixes, function table
+    launch_count_scan(P, sc, s);
+    launch_fix(P, s);
+    launch_decl_scan(P, g->meta.at<uint32_t>(), sc, s);
+    uint32_t meta[3] = {0, 0, 0};
+    PTL_CU(cudaMemcpyAsync(meta, g->meta.at<uint32_t>(), sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    PTL_CU(cudaStreamSynchronize(s));
+    if (ptl_status st = check_error_word(g); st != PTL_OK) return st;
+    g->F = meta[0];
+    if (g->F == 0) return fail(g, PTL_UNSUPPORTED, "isn_cnt: program has no function (the reference takes the max of an empty range)");
+    const size_t fb8 = r8(g->F);
+    for (DevBuf* b : {&g->fn_id, &g->fn_start, &g->fn_size, &g->fn_end, &g->fn_start0, &g->fn_size0, &g->fn_end0,
+                      &g->fn_ra_start, &g->fn_ra_end, &g->fn_ra_size}) {
+        PTL_CU(b->ensure(fb8 + 8, 4));
+        PTL_CU(b->zero(s));
+    }
+    P = make_prog(g);
+    launch_functab(P, g->meta.at<uint32_t>(), s);
+    PTL_CU(cudaMemcpyAsync(meta, g->meta.at<uint32_t>(), sizeof(meta), cudaMemcpyDeviceToHost, s));
+    PTL_CU(cudaStreamSynchronize(s));
+    g->W = meta[1];
+    g->S = meta[2];
+    PTL_CU(cudaMemcpyAsync(g->fn_end0.at<uint32_t>(), g->fn_end.at<uint32_t>(), g->F * 4, cudaMemcpyDeviceToDevice, s));
+    timer.mark();
+
+    // ---- isn_gen: depth order, register propagation, instruction writes
+    const size_t seg_cap = n / 17 + 16, tile_cap = n / kSortTile + seg_cap + 16, leaf_cap = n / 2 + 16;
+    PTL_CU(g->sort_a.ensure(n, 8));
+    PTL_CU(g->sort_apos.ensure(n, 4));
+    PTL_CU(g->sort_bpos.ensure(n, 4));
+    PTL_CU(g->sort_seg0.ensure(seg_cap, sizeof(SortSeg)));
+    PTL_CU(g->sort_seg1.ensure(seg_cap, sizeof(SortSeg)));
+    PTL_CU(g->sort_tile_seg.ensure(tile_cap, 4));
+    PTL_CU(g->sort_tile_l.ensure(tile_cap, 4));
+    PTL_CU(g->sort_tile_r.ensure(tile_cap, 4));
+    PTL_CU(g->sort_leaf.ensure(2 * leaf_cap, 4));
+    PTL_CU(g->sort_heap.ensure(2 * leaf_cap, 4));
+    PTL_CU(g->sort_counters.ensure(4, 4));
+    SortScratch ss{};
+    ss.a = g->sort_a.at<unsigned long long>();
+    ss.apos = g->sort_apos.at<uint32_t>();
+    ss.bpos = g->sort_bpos.at<uint32_t>();
+    ss.seg[0] = g->sort_seg0.at<SortSeg>();
+    ss.seg[1] = g->sort_seg1.at<SortSeg>();
+    ss.seg_cap = static_cast<uint32_t>(seg_cap);
+    ss.tile_seg = g->sort_tile_seg.at<uint32_t>();
+    ss.tile_l = g->sort_tile_l.at<uint32_t>();
+    ss.tile_r = g->sort_tile_r.at<uint32_t>();
+    ss.tile_cap = static_cast<uint32_t>(tile_cap);
+    ss.leaf = g->sort_leaf.at<uint32_t>();
+    ss.heap = g->sort_heap.at<uint32_t>();
+    ss.leaf_cap = static_cast<uint32_t>(leaf_cap);
+    ss.counters = g->sort_counters.at<uint32_t>();
+
+    const size_t wb8 = r8(g->W);
+    for (DevBuf* b : {&g->instr, &g->rd, &g->rs1, &g->rs2, &g->jt, &g->used_instrs, &g->symreg, &g->symswp,
+                      &g->stamp, &g->spill, &g->roffs}) {
+        PTL_CU(b->ensure(wb8, 4));
+        PTL_CU(b->zero(s));
+    }
+    PTL_CU(g->owner.ensure(wb8, 8));
+    PTL_CU(g->owner.zero(s));
+    PTL_CU(g->used.ensure(wb8, 1));
+    PTL_CU(g->used.zero(s));
+    PTL_CU(g->smark.ensure(wb8, 1));
+    PTL_CU(g->smark.zero(s));
+    P = make_prog(g);
+    PTL_CU(run_depth_sort(P, ss, s, &g->sort_rounds));
+    launch_gen(P, s);
+    if (ptl_status st = check_error_word(g); st != PTL_OK) return st;
+    timer.mark();
+
+    // ---- optimize
+    PTL_CU(g->flags.ensure(4, 4));
+    PTL_CU(g->flags.zero(s));
+    PTL_CU(run_optimize(P, s, &g->opt_sweeps));
+    if (ptl_status st = check_error_word(g); st != PTL_OK) return st;
+    timer.mark();
+
+    // ---- regalloc
+    PTL_CU(g->lifetime.ensure(fb8, 8));
+    PTL_CU(g->lifetime.zero(s));
+    k_init_lifetime<<<std::min<size_t>((g->F + 255) / 256, 1024), 256, 0, s>>>(g->lifetime.at<unsigned long long>(), g->F);
+    const size_t trig = static_cast<size_t>(std::max<uint32_t>(g->S, 1)) * 64;
+    PTL_CU(g->trig_min.ensure(trig, 4));
+    PTL_CU(g->trig_min.fill(s, 0xFF));
+    PTL_CU(g->trig_max.ensure(trig, 4));
+    PTL_CU(g->trig_max.zero(s));
+    P = make_prog(g);
+    PTL_CU(run_regalloc_steps(P, s, &g->ra_serial));
+    launch_regalloc_count_scan(P, sc, s);
+    uint32_t last_off = 0;
+    PTL_CU(read1(g, P.roffs + (g->W - 1), &last_off));
+    if (ptl_status st = check_error_word(g); st != PTL_OK) return st;
+    g->W2 = last_off + 1;
+    const size_t w2b8 = r8(g->W2);
+    for (DevBuf* b : {&g->ni, &g->nrd, &g->nr1, &g->nr2, &g->njt, &g->fsz, &g->joffs}) {
+        PTL_CU(b->ensure(w2b8 + 16, 4));
+        PTL_CU(b->zero(s));
+    }
+    P = make_prog(g);
+    launch_regalloc_emit(P, s);
+    for (int k = 0; k < 3; ++k) {
+        DevBuf* src[3] = {&g->fn_start, &g->fn_end, &g->fn_size};
+        DevBuf* dst[3] = {&g->fn_ra_start, &g->fn_ra_end, &g->fn_ra_size};
+        PTL_CU(cudaMemcpyAsync(dst[k]->at<uint32_t>(), src[k]->at<uint32_t>(), g->F * 4, cudaMemcpyDeviceToDevice, s));
+    }
+    timer.mark();
+
+    // ---- fix_jumps (+ postprocess)
+    launch_fixjumps_scan(P, sc, s);
+    uint32_t last_size = 0, last_joff = 0;
+    PTL_CU(read1(g, P.fsz + (g->W2 - 1), &last_size));
+    PTL_CU(read1(g, P.joffs + (g->W2 - 1), &last_joff));
+    if (ptl_status st = check_error_word(g); st != PTL_OK) return st;
+    g->W3 = last_size + last_joff;
+    PTL_CU(g->out.ensure(r8(g->W3) + 8, 4));
+    PTL_CU(g->out.zero(s));
+    P = make_prog(g);
+    launch_fixjumps_emit(P, s);
+    timer.mark();
+    timer.mark();  // postprocess is fused into fix_jumps
+    if (ptl_status st = check_error_word(g); st != PTL_OK) return st;
+    timer.finish();
+
+    if (to_host) {
+        g->words.resize(g->W3);
+        g->fn_start_h.resize(g->F);
+        g->fn_end_h.resize(g->F);
+        g->fn_size_h.resize(g->F);
+        g->fn_id_h.resize(g->F);
+        if (g->W3) PTL_CU(cudaMemcpyAsync(g->words.data(), P.out, g->W3 * 4ull, cudaMemcpyDeviceToHost, s));
+        PTL_CU(cudaMemcpyAsync(g->fn_start_h.data(), P.fn_start, g->F * 4ull, cudaMemcpyDeviceToHost, s));
+        PTL_CU(cudaMemcpyAsync(g->fn_end_h.data(), P.fn_end, g->F * 4ull, cudaMemcpyDeviceToHost, s));
+        PTL_CU(cudaMemcpyAsync(g->fn_size_h.data(), P.fn_size, g->F * 4ull, cudaMemcpyDeviceToHost, s));
+        PTL_CU(cudaMemcpyAsync(g->fn_id_h.data(), P.fn_id, g->F * 4ull, cudaMemcpyDeviceToHost, s));
+        PTL_CU(cudaStreamSynchronize(s));
+        g->host_valid = true;
+    }
+    return PTL_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+ptl_status ptl_generator_create(const ptl_ast_view* tree, int device, ptl_generator** out) {
+    if (!tree || !out) return PTL_BAD_ARGUMENT;
+    *out = nullptr;
+    if (tree->n == 0 || tree->n >= (1ull << 31) || !tree->type || !tree->rtype || !tree->parent ||
+        !tree->depth || !tree->child_idx || !tree->data) {
+        return PTL_BAD_ARGUMENT;
+    }
+    if (tree->max_depth == 0) return PTL_INVALID_AST;  // the reference divides by it (rv_generator_avx.cpp:583)
+    ptl_generator* g = new (std::nothrow) ptl_generator();
+    if (!g) return PTL_OOM;
+    g->device = device;
+    g->n = tree->n;
+    g->max_depth = tree->max_depth;
+    cudaError_t e = cudaSetDevice(device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking);
+    const cudaMemcpyKind kind = tree->on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    const size_t n = tree->n;
+    struct { DevBuf* b; const void* src; size_t es; } in[] = {
+        {&g->in_type, tree->type, 1}, {&g->in_rtype, tree->rtype, 1}, {&g->in_parent, tree->parent, 4},
+        {&g->in_depth, tree->depth, 4}, {&g->in_child, tree->child_idx, 4}, {&g->in_data, tree->data, 4}};
+    for (auto& x : in) {
+        if (e != cudaSuccess) break;
+        e = x.b->ensure(n, x.es);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(x.b->at<char>(), x.src, n * x.es, kind, g->stream);
+    }
+    if (e == cudaSuccess) e = g->tables.ensure(sizeof(CodeTables), 1);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(g->tables.at<char>(), &host_tables(), sizeof(CodeTables), cudaMemcpyHostToDevice, g->stream);
+    if (e == cudaSuccess) e = g->errw.ensure(1, sizeof(ErrorWord));
+    if (e == cudaSuccess) e = g->meta.ensure(4, 4);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+    if (e != cudaSuccess) {
+        const ptl_status st = e == cudaErrorMemoryAllocation ? PTL_OOM : PTL_CUDA_ERROR;
+        delete g;
+        return st;
+    }
+    *out = g;
+    return PTL_OK;
+}
+
+ptl_status ptl_generator_process(ptl_generator* g, int profile) {
+    if (!g) return PTL_BAD_ARGUMENT;
+    if (cudaSetDevice(g->device) != cudaSuccess) return fail(g, PTL_CUDA_ERROR, "cudaSetDevice");
+    const ptl_status st = run_pipeline(g, (profile & 1) != 0, (profile & 2) == 0);
+    if (st == PTL_OK) g->last_error.clear();
+    return st;
+}
+
+ptl_status ptl_generator_instructions(ptl_generator* g, const uint32_t** words, size_t* count) {
+    if (!g || !words || !count) return PTL_BAD_ARGUMENT;
+    if (!g->host_valid) {
+        g->words.resize(g->W3);
+        if (g->W3) {
+            cudaError_t e = cudaMemcpyAsync(g->words.data(), g->out.at<uint32_t>(), g->W3 * 4ull, cudaMemcpyDeviceToHost, g->stream);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+            if (e != cudaSuccess) return cuda_fail(g, e, "instructions");
+        }
+    }
+    *words = g->words.data();
+    *count = g->W3;
+    return PTL_OK;
+}
+
+ptl_status ptl_generator_device_instructions(ptl_generator* g, const uint32_t** words, size_t* count) {
+    if (!g || !words || !count) return PTL_BAD_ARGUMENT;
+    *words = g->out.at<uint32_t>();
+    *count = g->W3;
+    return PTL_OK;
+}
+
+ptl_status ptl_generator_function_table(ptl_generator* g, const uint32_t** starts, const uint32_t** ends,
+                                        const uint32_t** sizes, const uint32_t** ids, size_t* count) {
+    if (!g || !count) return PTL_BAD_ARGUMENT;
+    if (!g->host_valid) {
+        const uint32_t* w;
+        size_t c;
+        if (ptl_status st = ptl_generator_instructions(g, &w, &c); st != PTL_OK) return st;
+        g->fn_start_h.resize(g->F);
+        g->fn_end_h.resize(g->F);
+        g->fn_size_h.resize(g->F);
+        g->fn_id_h.resize(g->F);
+        cudaMemcpyAsync(g->fn_start_h.data(), g->fn_start.at<uint32_t>(), g->F * 4ull, cudaMemcpyDeviceToHost, g->stream);
+        cudaMemcpyAsync(g->fn_end_h.data(), g->fn_end.at<uint32_t>(), g->F * 4ull, cudaMemcpyDeviceToHost, g->stream);
+        cudaMemcpyAsync(g->fn_size_h.data(), g->fn_size.at<uint32_t>(), g->F * 4ull, cudaMemcpyDeviceToHost, g->stream);
+        cudaMemcpyAsync(g->fn_id_h.data(), g->fn_id.at<uint32_t>(), g->F * 4ull, cudaMemcpyDeviceToHost, g->stream);
+        const cudaError_t e = cudaStreamSynchronize(g->stream);
+        if (e != cudaSuccess) return cuda_fail(g, e, "function table");
+        g->host_valid = true;
+    }
+    if (starts) *starts = g->fn_start_h.data();
+    if (ends) *ends = g->fn_end_h.data();
+    if (sizes) *sizes = g->fn_size_h.data();
+    if (ids) *ids = g->fn_id_h.data();
+    *count = g->F;
+    return PTL_OK;
+}
+
+ptl_status ptl_generator_stage_ns(ptl_generator* g, uint64_t ns[7]) {
+    if (!g || !ns) return PTL_BAD_ARGUMENT;
+    std::memcpy(ns, g->stage_ns, sizeof(g->stage_ns));
+    return PTL_OK;
+}
+
+const char* ptl_generator_last_error(const ptl_generator* g) { return g ? g->last_error.c_str() : "null generator"; }
+
+void ptl_generator_destroy(ptl_generator* g) { delete g; }
+
+ptl_status ptl_compile(const ptl_ast_view* tree, int device, uint32_t* words, size_t capacity, size_t* count) {
+    if (!count) return PTL_BAD_ARGUMENT;
+    ptl_generator* g = nullptr;
+    ptl_status st = ptl_generator_create(tree, device, &g);
+    if (st != PTL_OK) return st;
+    st = ptl_generator_process(g, 0);
+    if (st == PTL_OK) {
+        *count = g->W3;
+        if (words) {
+            if (capacity < g->W3) st = PTL_BAD_ARGUMENT;
+            else std::memcpy(words, g->words.data(), g->W3 * 4ull);
+        }
+    }
+    ptl_generator_destroy(g);
+    return st;
+}
+
+ptl_status ptl_generator_snapshot(ptl_generator* g, int which, uint32_t* out, size_t capacity, size_t* count) {
+    if (!g || !count) return PTL_BAD_ARGUMENT;
+    const DevBuf* b = nullptr;
+    size_t len = 0;
+    switch (which) {
+        case 0: b = &g->out; len = g->W3; break;
+        case 1: b = &g->fn_start; len = g->F; break;
+        case 2: b = &g->fn_end; len = g->F; break;
+        case 3: b = &g->fn_size; len = g->F; break;
+        case 4: b = &g->fn_id; len = g->F; break;
+        case 5: b = &g->nt; len = g->n; break;
+        case 6: b = &g->rt; len = g->n; break;
+        case 7: b = &g->nd; len = g->n; break;
+        case 8: b = &g->sizes; len = g->n; break;
+        case 9: b = &g->loc; len = g->n; break;
+        case 10: b = &g->fn_id; len = g->F; break;
+        case 11: b = &g->fn_start0; len = g->F; break;
+        case 12: b = &g->fn_end0; len = g->F; break;
+        case 13: b = &g->fn_size0; len = g->F; break;
+        case 14: b = &g->instr; len = g->W; break;
+        case 15: b = &g->rd; len = g->W; break;
+        case 16: b = &g->rs1; len = g->W; break;
+        case 17: b = &g->rs2; len = g->W; break;
+        case 18: b = &g->jt; len = g->W; break;
+        case 19: b = &g->used_instrs; len = g->W; break;
+        case 20: b = &g->ni; len = g->W2; break;
+        case 21: b = &g->nrd; len = g->W2; break;
+        case 22: b = &g->nr1; len = g->W2; break;
+        case 23: b = &g->nr2; len = g->W2; break;
+        case 24: b = &g->njt; len = g->W2; break;
+        case 25: b = &g->fn_ra_start; len = g->F; break;
+        case 26: b = &g->fn_ra_end; len = g->F; break;
+        case 27: b = &g->fn_ra_size; len = g->F; break;
+        case 40: b = &g->pos; len = g->n; break;
+        case 41: b = &g->regs; len = 3 * g->n; break;
+        case 42: b = &g->symreg; len = g->W; break;
+        case 43: b = &g->symswp; len = g->W; break;
+        default: return fail(g, PTL_BAD_ARGUMENT, "snapshot not kept by the GPU pipeline");
+    }
+    *count = len;
+    if (!out) return PTL_OK;
+    if (capacity < len) return PTL_BAD_ARGUMENT;
+    if (len) {
+        cudaError_t e = cudaMemcpyAsync(out, b->at<uint32_t>(), len * 4, cudaMemcpyDeviceToHost, g->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+        if (e != cudaSuccess) return cuda_fail(g, e, "snapshot");
+    }
+    return PTL_OK;
+}
+
+size_t ptl_code_table(int which, uint32_t* out) {
+    const CodeTables& t = host_tables();
+    auto flat = [&](size_t count, auto value) {
+        if (out) for (size_t k = 0; k < count; ++k) out[k] = value(k);
+        return count;
+    };
+    switch (which) {
+        case 0: return flat(256 * 6, [&](size_t k) { return static_cast<uint32_t>(t.size[t.row_of[k / 6]][k % 6]); });
+        case 1: return flat(256 * 24, [&](size_t k) { return ((t.has_instr[t.row_of[k / 24]][(k / 6) % 4] >> (k % 6)) & 1u) ? 0xFFFFFFFFu : 0u; });
+        case 2: return flat(256 * 24, [&](size_t k) { return ((t.has_output[t.row_of[k / 24]][(k / 6) % 4] >> (k % 6)) & 1u) ? 0xFFFFFFFFu : 0u; });
+        case 3: return flat(256 * 24, [&](size_t k) { return static_cast<uint32_t>(t.pai[t.row_of[k / 24]][(k / 6) % 4][k % 6]); });
+        case 4: return flat(256 * 24, [&](size_t k) { return static_cast<uint32_t>(t.out[t.row_of[k / 24]][(k / 6) % 4][k % 6]); });
+        case 5: return flat(256 * 24, [&](size_t k) { return t.instr[t.row_of[k / 24]][(k / 6) % 4][k % 6]; });
+        case 6: return flat(256 * 4, [&](size_t k) { return static_cast<uint32_t>(t.cnst[t.row_of[k / 4]][k % 4]); });
+        case 7: return flat(256 * 48, [&](size_t k) { return static_cast<uint32_t>(t.opd[t.row_of[k / 48]][(k / 12) % 4][(k / 2) % 6][k % 2]); });
+        case 8: return flat(256 * 4, [&](size_t k) { return static_cast<uint32_t>(t.jt[t.row_of[k / 4]][k % 4]); });
+        case 9: return flat(kNumPareasTypes, [&](size_t k) { return static_cast<uint32_t>(t.pareas_to_rv[k]); });
+        default: return 0;
+    }
+}
+
+ptl_status ptl_device_info(int device, char* name, size_t name_len, int* sm_count, int* cc_major, int* cc_minor) {
+    cudaDeviceProp prop{};
+    if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) return PTL_CUDA_ERROR;
+    if (name && name_len) std::snprintf(name, name_len, "%s", prop.name);
+    if (sm_count) *sm_count = prop.multiProcessorCount;
+    if (cc_major) *cc_major = prop.major;
+    if (cc_minor) *cc_minor = prop.minor;
+    return PTL_OK;
+}
+
+}  // extern "C"

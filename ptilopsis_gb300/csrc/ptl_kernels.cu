@@ -1,0 +1,682 @@
+// CUDA kernels of the GB300 code generator.  Per-thread logic lives in ptl_stages.cuh and
+// ptl_sort.cuh; this file holds the launch shapes, the cross-thread primitives (scans,
+// the depth-order rounds, the lock-step register allocator of lane-0 functions) and
+// their bounded waits.
+#include <cuda_runtime.h>
+
+#include "ptl_kernels.cuh"
+
+namespace ptl {
+
+namespace {
+
+constexpr int kThreads = 256;
+
+inline unsigned grid_for(uint64_t n, int threads = kThreads) {
+    uint64_t g = (n + threads - 1) / threads;
+    if (g < 1) g = 1;
+    if (g > 152ull * 64ull) g = 152ull * 64ull;  // grid-stride beyond 64 CTAs per SM
+    return static_cast<unsigned>(g);
+}
+
+#define PTL_FOR(i, count)                                                                \
+    for (uint64_t i##_ = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;   \
+         i##_ < (count); i##_ += static_cast<uint64_t>(gridDim.x) * blockDim.x)          \
+        if (const uint32_t i = static_cast<uint32_t>(i##_); true)
+
+// ------------------------------------------------------------------ element-wise stages
+__global__ void k_translate(Prog P) { PTL_FOR(i, P.nb8) st_translate(P, i); }
+__global__ void k_pre_args(Prog P) { PTL_FOR(i, P.nb8) st_pre_args(P, i); }
+__global__ void k_pre_lists(Prog P) { PTL_FOR(i, P.nb8) st_pre_lists(P, i); }
+__global__ void k_pre_float(Prog P) { PTL_FOR(i, P.nb8) st_pre_float(P, i); }
+__global__ void k_pre_float_apply(Prog P) { PTL_FOR(i, P.nb8) st_pre_float_apply(P, i); }
+__global__ void k_fix_own(Prog P) { PTL_FOR(i, P.nb8) st_fix_own(P, i); }
+__global__ void k_fix_cond(Prog P) { PTL_FOR(i, P.nb8) st_fix_cond(P, i); }
+
+// ------------------------------------------------------------------ decoupled look-back scan
+// Exclusive scan (mod 2^32) of load(i) over [0, count), single pass: tiles take tickets
+// in order, publish their aggregate, look back over predecessors until one has published
+// its inclusive prefix, then publish their own.  A look-back that waits too long gives
+// up and records ST_DEVICE_TIMEOUT instead of spinning forever.
+constexpr int kScanThreads = 256;
+constexpr int kScanItems = 16;
+constexpr uint32_t kScanTile = kScanThreads * kScanItems;
+constexpr uint32_t kSpinLimit = 1u << 26;
+
+__device__ __forceinline__ uint32_t warp_incl_scan(uint32_t x) {
+    const uint32_t lane = threadIdx.x & 31u;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, d);
+        if (lane >= static_cast<uint32_t>(d)) x += y;
+    }
+    return x;
+}
+
+template <class Load, class Store>
+__global__ void __launch_bounds__(kScanThreads) k_scan(Load load, Store store, uint32_t count, ScanScratch sc, ErrorWord* err) {
+    constexpr int kWarps = kScanThreads / 32;
+    __shared__ uint32_t s_tile, s_prefix;
+    __shared__ uint32_t s_warp[kWarps];
+    if (threadIdx.x == 0) s_tile = atomicAdd(sc.counter, 1u);
+    __syncthreads();
+    const uint32_t tile = s_tile;
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    const uint64_t wbase = static_cast<uint64_t>(tile) * kScanTile + static_cast<uint64_t>(warp) * 32u * kScanItems;
+    uint32_t v[kScanItems];
+    uint32_t carry = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        const uint64_t idx = wbase + static_cast<uint64_t>(k) * 32u + lane;
+        const uint32_t x = idx < count ? load(static_cast<uint32_t>(idx)) : 0u;
+        const uint32_t incl = warp_incl_scan(x);
+        v[k] = carry + incl - x;
+        carry += __shfl_sync(0xFFFFFFFFu, incl, 31);
+    }
+    if (lane == 0) s_warp[warp] = carry;
+    __syncthreads();
+    if (warp == 0) {
+        const uint32_t t = lane < kWarps ? s_warp[lane] : 0u;
+        const uint32_t incl = warp_incl_scan(t);
+        if (lane < kWarps) s_warp[lane] = incl - t;
+        const uint32_t aggregate = __shfl_sync(0xFFFFFFFFu, incl, kWarps - 1);
+        if (lane == 0) {
+            uint32_t prefix = 0;
+            if (tile == 0) {
+                atomicExch(&sc.status[0], (2ull << 32) | aggregate);
+            } else {
+                atomicExch(&sc.status[tile], (1ull << 32) | aggregate);
+                int64_t j = static_cast<int64_t>(tile) - 1;
+                uint32_t spins = 0;
+                while (j >= 0) {
+                    const unsigned long long st = *reinterpret_cast<volatile unsigned long long*>(&sc.status[j]);
+                    const uint32_t flag = static_cast<uint32_t>(st >> 32);
+                    if (flag == 0) {
+                        if (++spins > kSpinLimit) {
+                            record_error(err, ST_DEVICE_TIMEOUT, W_SCAN, tile);
+                            break;
+                        }
+                        continue;
+                    }
+                    prefix += static_cast<uint32_t>(st);
+                    if (flag == 2) break;
+                    --j;
+                }
+                atomicExch(&sc.status[tile], (2ull << 32) | (prefix + aggregate));
+            }
+            s_prefix = prefix;
+        }
+    }
+    __syncthreads();
+    const uint32_t base = s_prefix + s_warp[warp];
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        const uint64_t idx = wbase + static_cast<uint64_t>(k) * 32u + lane;
+        if (idx < count) store(static_cast<uint32_t>(idx), base + v[k]);
+    }
+}
+
+template <class Load, class Store>
+void run_scan(Load load, Store store, uint32_t count, const ScanScratch& sc, ErrorWord* err, cudaStream_t s) {
+    const uint32_t tiles = (count + kScanTile - 1) / kScanTile;
+    if (tiles == 0) return;
+    cudaMemsetAsync(sc.status, 0, sizeof(unsigned long long) * tiles, s);
+    cudaMemsetAsync(sc.counter, 0, sizeof(uint32_t), s);
+    k_scan<<<tiles, kScanThreads, 0, s>>>(load, store, count, sc, err);
+}
+
+struct CountLoad {
+    Prog P;
+    __device__ uint32_t operator()(uint32_t i) const {
+        const uint32_t v = st_count(P, i);
+        P.sizes[i] = v;
+        return v;
+    }
+};
+struct StoreTo {
+    uint32_t* out;
+    __device__ void operator()(uint32_t i, uint32_t v) const { out[i] = v; }
+};
+struct DeclLoad {
+    Prog P;
+    __device__ uint32_t operator()(uint32_t i) const { return P.nt[i] == RV_FUNC_DECL ? 1u : 0u; }
+};
+struct DeclStore {
+    Prog P;
+    uint32_t* meta;
+    uint32_t count;
+    __device__ void operator()(uint32_t i, uint32_t v) const {
+        const bool is_decl = P.nt[i] == RV_FUNC_DECL;
+        if (is_decl) P.decl[v] = i;
+        if (i == count - 1) meta[0] = v + (is_decl ? 1u : 0u);
+    }
+};
+struct RaCountLoad {
+    Prog P;
+    __device__ uint32_t operator()(uint32_t i) const { return st_ra_count(P, i); }
+};
+struct FjSizeLoad {
+    Prog P;
+    __device__ uint32_t operator()(uint32_t i) const {
+        const uint32_t v = i < P.W2 ? st_fj_size(P, i) : 0u;
+        P.fsz[i] = v;
+        return v;
+    }
+};
+
+// ------------------------------------------------------------------ function table
+__global__ void k_functab(Prog P, const uint32_t* meta) {
+    const uint32_t F = meta[0];
+    const uint32_t fb8 = (F + 7u) & ~7u;
+    PTL_FOR(f, fb8) st_functab(P, f);
+}
+__global__ void k_functab_end(Prog P, uint32_t* meta) {
+    const uint32_t F = meta[0];
+    const uint32_t fb8 = (F + 7u) & ~7u;
+    PTL_FOR(f, fb8) {
+        st_functab_end(P, f);
+        if (f < F) atomicMax(&meta[2], P.fn_size[f]);  // longest function, in steps
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) meta[1] = P.loc[P.n - 1];  // word count
+}
+
+// ------------------------------------------------------------------ depth order
+__global__ void k_sort_init(Prog P, SortScratch ss) {
+    PTL_FOR(i, P.n) ss.a[i] = (static_cast<unsigned long long>(u32(P.dep[i])) << 32) | i;
+}
+
+__global__ void k_sort_tiles(SortScratch ss, const SortSeg* cur, SortSeg* curw, uint32_t nseg) {
+    PTL_FOR(s, nseg) {
+        SortSeg g = cur[s];
+        median_to_first(ss.a, g.first, g.last);
+        g.pivot = skey(ss.a[g.first]);
+        const uint32_t m1 = g.last - g.first - 1;
+        g.tcount = (m1 + kSortTile - 1) / kSortTile;
+        g.tbase = atomicAdd(&ss.counters[0], g.tcount);
+        curw[s] = g;
+        for (uint32_t k = 0; k < g.tcount; ++k) ss.tile_seg[g.tbase + k] = s;
+    }
+}
+
+__device__ __forceinline__ uint32_t block_reduce_add(uint32_t v, uint32_t* sm) {
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) v += __shfl_down_sync(0xFFFFFFFFu, v, d);
+    if (lane == 0) sm[warp] = v;
+    __syncthreads();
+    uint32_t t = 0;
+    if (threadIdx.x == 0) {
+        for (uint32_t w = 0; w < blockDim.x / 32; ++w) t += sm[w];
+    }
+    __syncthreads();
+    return t;  // valid in thread 0
+}
+
+constexpr uint32_t kSortItems = kSortTile / kThreads;  // 8 per thread
+
+__global__ void __launch_bounds__(kThreads) k_sort_count(SortScratch ss, const SortSeg* cur) {
+    __shared__ uint32_t sm[kThreads / 32];
+    const uint32_t t = blockIdx.x;
+    const SortSeg g = cur[ss.tile_seg[t]];
+    const uint32_t lo = g.first + 1 + (t - g.tbase) * kSortTile;
+    const uint32_t hi = min(g.last, lo + kSortTile);
+    uint32_t cl = 0, cr = 0;
+    for (uint32_t p = lo + threadIdx.x; p < hi; p += kThreads) {
+        const int32_t k = skey(ss.a[p]);
+        cl += is_lstop(k, g.pivot);
+        cr += is_rstop(k, g.pivot);
+    }
+    const uint32_t tl = block_reduce_add(cl, sm);
+    const uint32_t tr = block_reduce_add(cr, sm);
+    if (threadIdx.x == 0) {
+        ss.tile_l[t] = tl;
+        ss.tile_r[t] = tr;
+    }
+}
+
+// Exclusive offsets of the tile counts of each segment (one CTA per segment).
+__global__ void __launch_bounds__(kThreads) k_sort_segscan(SortScratch ss, SortSeg* cur) {
+    __shared__ uint32_t sl[kThreads], sr[kThreads];
+    __shared__ uint32_t carry_l, carry_r;
+    SortSeg& g = cur[blockIdx.x];
+    if (threadIdx.x == 0) { carry_l = 0; carry_r = 0; }
+    __syncthreads();
+    for (uint32_t c = 0; c < g.tcount; c += kThreads) {
+        const uint32_t k = c + threadIdx.x;
+        const uint32_t vl = k < g.tcount ? ss.tile_l[g.tbase + k] : 0u;
+        const uint32_t vr = k < g.tcount ? ss.tile_r[g.tbase + k] : 0u;
+        sl[threadIdx.x] = vl;
+        sr[threadIdx.x] = vr;
+        __syncthreads();
+        for (uint32_t d = 1; d < kThreads; d <<= 1) {
+            const uint32_t al = threadIdx.x >= d ? sl[threadIdx.x - d] : 0u;
+            const uint32_t ar = threadIdx.x >= d ? sr[threadIdx.x - d] : 0u;
+            __syncthreads();
+            sl[threadIdx.x] += al;
+            sr[threadIdx.x] += ar;
+            __syncthreads();
+        }
+        if (k < g.tcount) {
+            ss.tile_l[g.tbase + k] = carry_l + sl[threadIdx.x] - vl;
+            ss.tile_r[g.tbase + k] = carry_r + sr[threadIdx.x] - vr;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            carry_l += sl[kThreads - 1];
+            carry_r += sr[kThreads - 1];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        g.nL = carry_l;
+        g.nR = carry_r;
+    }
+}
+
+// Stop positions by rank: A[rank] for L-stops, B[rank from the right] for R-stops.
+__global__ void __launch_bounds__(kThreads) k_sort_pos(SortScratch ss, const SortSeg* cur) {
+    __shared__ uint32_t sl[kThreads], sr[kThreads];
+    const uint32_t t = blockIdx.x;
+    const SortSeg g = cur[ss.tile_seg[t]];
+    const uint32_t lo = g.first + 1 + (t - g.tbase) * kSortTile;
+    const uint32_t hi = min(g.last, lo + kSortTile);
+    const uint32_t p0 = lo + threadIdx.x * kSortItems;
+    uint32_t fl = 0, fr = 0, cl = 0, cr = 0;
+#pragma unroll
+    for (uint32_t k = 0; k < kSortItems; ++k) {
+        const uint32_t p = p0 + k;
+        if (p < hi) {
+            const int32_t key = skey(ss.a[p]);
+            if (is_lstop(key, g.pivot)) { fl |= 1u << k; ++cl; }
+            if (is_rstop(key, g.pivot)) { fr |= 1u << k; ++cr; }
+        }
+    }
+    sl[threadIdx.x] = cl;
+    sr[threadIdx.x] = cr;
+    __syncthreads();
+    for (uint32_t d = 1; d < kThreads; d <<= 1) {
+        const uint32_t al = threadIdx.x >= d ? sl[threadIdx.x - d] : 0u;
+        const uint32_t ar = threadIdx.x >= d ? sr[threadIdx.x - d] : 0u;
+        __syncthreads();
+        sl[threadIdx.x] += al;
+        sr[threadIdx.x] += ar;
+        __syncthreads();
+    }
+    uint32_t rl = ss.tile_l[t] + sl[threadIdx.x] - cl;
+    uint32_t rr = ss.tile_r[t] + sr[threadIdx.x] - cr;
+#pragma unroll
+    for (uint32_t k = 0; k < kSortItems; ++k) {
+        const uint32_t p = p0 + k;
+        if ((fl >> k) & 1u) ss.apos[g.first + rl++] = p;
+        if ((fr >> k) & 1u) ss.bpos[g.first + (g.nR - 1u - rr++)] = p;
+    }
+}
+
+__device__ void sort_emit(SortScratch ss, SortSeg* next, uint32_t first, uint32_t last, uint32_t dl) {
+    if (last - first <= kSortThreshold) {
+        if (last - first > 1) {
+            const uint32_t k = atomicAdd(&ss.counters[2], 1u);
+            if (k < ss.leaf_cap) { ss.leaf[2 * k] = first; ss.leaf[2 * k + 1] = last; }
+        }
+        return;
+    }
+    if (dl == 0) {
+        const uint32_t k = atomicAdd(&ss.counters[3], 1u);
+        if (k < ss.leaf_cap) { ss.heap[2 * k] = first; ss.heap[2 * k + 1] = last; }
+        return;
+    }
+    const uint32_t k = atomicAdd(&ss.counters[1], 1u);
+    if (k < ss.seg_cap) {
+        SortSeg c{};
+        c.first = first;
+        c.last = last;
+        c.dl = dl;
+        next[k] = c;
+    }
+}
+
+__global__ void k_sort_cut(SortScratch ss, SortSeg* cur, uint32_t nseg, SortSeg* next) {
+    PTL_FOR(s, nseg) {
+        SortSeg& g = cur[s];
+        g.K = partition_k(ss.apos + g.first, ss.bpos + g.first, g.nL, g.nR);
+        g.cut = partition_cut(ss.apos + g.first, ss.bpos + g.first, g.nL, g.K);
+        sort_emit(ss, next, g.first, g.cut, g.dl - 1);
+        sort_emit(ss, next, g.cut, g.last, g.dl - 1);
+    }
+}
+
+__global__ void __launch_bounds__(kThreads) k_sort_swap(SortScratch ss, const SortSeg* cur) {
+    const uint32_t t = blockIdx.x;
+    const SortSeg g = cur[ss.tile_seg[t]];
+    const uint32_t k0 = (t - g.tbase) * kSortTile;
+    const uint32_t k1 = min(g.K, k0 + kSortTile);
+    for (uint32_t k = k0 + threadIdx.x; k < k1; k += kThreads) {
+        sswap(ss.a, ss.apos[g.first + k], ss.bpos[g.first + k]);
+    }
+}
+
+__global__ void k_sort_leaves(SortScratch ss, uint32_t count) {
+    PTL_FOR(k, count) leaf_sort(ss.a, ss.leaf[2 * k], ss.leaf[2 * k + 1]);
+}
+__global__ void k_sort_heaps(SortScratch ss, uint32_t count) {
+    PTL_FOR(k, count) heap_sort_range(ss.a + ss.heap[2 * k], ss.heap[2 * k + 1] - ss.heap[2 * k]);
+}
+__global__ void k_sort_out(Prog P, SortScratch ss) { PTL_FOR(p, P.n) P.pos[sidx(ss.a[p])] = p; }
+
+// ------------------------------------------------------------------ isn_gen / optimize
+__global__ void k_gen_prop(Prog P) { PTL_FOR(x, P.n) st_gen_prop(P, x); }
+__global__ void k_gen_claim(Prog P) { PTL_FOR(x, P.n) st_gen_claim(P, x); }
+__global__ void k_gen_write(Prog P) { PTL_FOR(x, P.n) st_gen_write(P, x); }
+
+__global__ void k_opt_mark(Prog P) { PTL_FOR(i, P.wb8) st_opt_mark(P, i); }
+__global__ void k_opt_sweep(Prog P) {
+    bool any = false;
+    PTL_FOR(i, P.wb8) any |= st_opt_sweep(P, i);
+    if (__syncthreads_or(any) && threadIdx.x == 0) P.flags[0] = 1;
+}
+__global__ void k_opt_final(Prog P) { PTL_FOR(i, P.wb8) st_opt_final(P, i); }
+
+// ------------------------------------------------------------------ regalloc
+__global__ void k_ra_free(Prog P) {
+    PTL_FOR(f, P.F) {
+        if ((f & 7u) != 0) st_ra_free_function(P, f);
+    }
+}
+
+// Lane-0 functions (f % 8 == 0) in lock-step, one CTA.  Within a step the reference
+// visits groups of 8 functions in order; a lane-0 function's symbols are marked
+// swapped through row 0 of the register state by any function whose register operand
+// was live.  Per step:
+//   1. snapshot row 0 (the reference copies the register state at each step);
+//   2. each active function computes its step; a symbol reads as swapped if a function
+//      of an earlier group triggered the physical register holding it.  Earlier
+//      lane-0 triggers depend on the same computation, so the CTA iterates until the
+//      per-register minimum trigger group stops changing (a DAG in group order);
+//   3. symbol updates: a symbol updated by its owner ends swapped only if a later
+//      group also triggered it; other triggered symbols end swapped;
+//   4. row 0 takes, per physical register, the write of the highest group.
+constexpr int kRaThreads = 512;
+constexpr int kRaPerThread = 16;
+
+__device__ __forceinline__ bool ra_marked(const uint32_t* snap, const uint32_t* fmin, uint32_t v, uint32_t limit) {
+    for (int p = 0; p < 64; ++p) {
+        if (snap[p] == v && fmin[p] <= limit) return true;
+    }
+    return false;
+}
+
+__global__ void __launch_bounds__(kRaThreads) k_ra_lane0(Prog P, uint32_t S0) {
+    __shared__ uint32_t R0[64], snap[64], fmin[64], fnext[64], fmax[64], omin[64], omax[64];
+    __shared__ unsigned long long r0key[64];
+    __shared__ int s_changed;
+    const uint32_t G0 = (P.F + 7u) / 8u;
+    const uint32_t tid = threadIdx.x;
+    if (G0 > static_cast<uint32_t>(kRaThreads) * kRaPerThread) {
+        if (tid == 0) record_error(P.err, ST_UNSUPPORTED, W_RA2, G0);
+        return;
+    }
+    if (tid < 64) R0[tid] = 0xFFFFFFFFu;
+    __syncthreads();
+    for (uint32_t i = 0; i < S0; ++i) {
+        if (tid < 64) {
+            snap[tid] = R0[tid];
+            omin[tid] = P.trig_min[static_cast<size_t>(i) * 64u + tid];
+            omax[tid] = P.trig_max[static_cast<size_t>(i) * 64u + tid];
+            fmin[tid] = omin[tid];
+            r0key[tid] = 0;
+        }
+        RaStep st[kRaPerThread];
+        bool act[kRaPerThread];
+#pragma unroll
+        for (int q = 0; q < kRaPerThread; ++q) {
+            const uint32_t j = tid + static_cast<uint32_t>(q) * kRaThreads;
+            act[q] = j < G0 && ra_load(P, 8u * j, i, st[q]);
+            if (act[q] && (st[q].ins == 0x000000EFu || !ra_own(P, 8u * j, st[q].r1) ||
+                           !ra_own(P, 8u * j, st[q].r2) || !ra_own(P, 8u * j, st[q].ord))) {
+                record_error(P.err, ST_UNSUPPORTED, W_RA2, P.fn_start0[8u * j] + i);
+                act[q] = false;
+            }
+        }
+        __syncthreads();
+        for (uint32_t round = 0;; ++round) {
+            if (tid < 64) { fnext[tid] = omin[tid]; fmax[tid] = omax[tid]; }
+            if (tid == 0) s_changed = 0;
+            __syncthreads();
+#pragma unroll
+            for (int q = 0; q < kRaPerThread; ++q) {
+                if (!act[q]) continue;
+                const uint32_t j = tid + static_cast<uint32_t>(q) * kRaThreads;
+                RaStep& S = st[q];
+                uint32_t r1reg = 0, r2reg = 0;
+                bool r1s = false, r2s = false;
+                if (s32(S.r1) > 63) {
+                    r1reg = P.symreg[S.r1 - 64u];
+                    r1s = P.symswp[S.r1 - 64u] != 0 || ra_marked(snap, fmin, S.r1, j);
+                }
+                if (s32(S.r2) > 63) {
+                    r2reg = P.symreg[S.r2 - 64u];
+                    r2s = P.symswp[S.r2 - 64u] != 0 || ra_marked(snap, fmin, S.r2, j);
+                }
+                ra_compute(S, P.lifetime[8u * j], r1reg, r1s, r2reg, r2s);
+                uint64_t t = S.trig;
+                while (t) {
+                    const uint32_t p = static_cast<uint32_t>(__ffsll(static_cast<long long>(t)) - 1);
+                    t &= t - 1;
+                    atomicMin(&fnext[p], j + 1u);
+                    atomicMax(&fmax[p], j + 1u);
+                }
+            }
+            __syncthreads();
+            if (tid < 64) {
+                if (fnext[tid] != fmin[tid]) s_changed = 1;
+                fmin[tid] = fnext[tid];
+            }
+            __syncthreads();
+            if (!s_changed) break;
+            if (round > G0 + 2u) {
+                if (tid == 0) record_error(P.err, ST_DEVICE_TIMEOUT, W_RA2, i);
+                break;
+            }
+        }
+        // symbol updates of each function's own registers
+#pragma unroll
+        for (int q = 0; q < kRaPerThread; ++q) {
+            if (!act[q]) continue;
+            const uint32_t j = tid + static_cast<uint32_t>(q) * kRaThreads;
+            const RaStep& S = st[q];
+            P.lifetime[8u * j] = S.cleared | S.rdm;
+            auto upd = [&](uint32_t v, uint32_t reg) {
+                bool later = false;
+                for (int p = 0; p < 64; ++p) later |= snap[p] == v && fmax[p] > j + 1u;
+                P.symreg[v - 64u] = reg;
+                P.symswp[v - 64u] = later ? 0xFFFFFFFFu : 0u;
+                P.stamp[v - 64u] = i + 1u;
+            };
+            if (s32(S.ord) > 63) upd(S.ord, S.rdr);
+            if (s32(S.r1) > 63) upd(S.r1, S.r1r);
+            if (s32(S.r2) > 63) upd(S.r2, S.r2r);
+            if (S.ord != 0) atomicMax(&r0key[S.rdr & 63u], (static_cast<unsigned long long>(j + 1u) << 32) | S.ord);
+            if (S.r1r != S.rdr && s32(S.r1r) >= 0 && S.r1r < 64u)
+                atomicMax(&r0key[S.r1r], (static_cast<unsigned long long>(j + 1u) << 32) | 0xFFFFFFFFull);
+            if (S.r2r != S.rdr && s32(S.r2r) >= 0 && S.r2r < 64u)
+                atomicMax(&r0key[S.r2r], (static_cast<unsigned long long>(j + 1u) << 32) | 0xFFFFFFFFull);
+        }
+        __syncthreads();
+        if (tid < 64) {
+            if (fmin[tid] != 0xFFFFFFFFu) {
+                const uint32_t v = snap[tid];
+                if (s32(v - 64u) >= 0 && P.stamp[v - 64u] != i + 1u) P.symswp[v - 64u] = 0xFFFFFFFFu;
+            }
+            if (r0key[tid] != 0) R0[tid] = static_cast<uint32_t>(r0key[tid]);
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void k_ra_cross(Prog P) {
+    bool any = false;
+    PTL_FOR(i, P.W) any |= st_ra_cross(P, i);
+    if (__syncthreads_or(any) && threadIdx.x == 0) P.flags[1] = 1;
+}
+__global__ void k_ra_serial(Prog P) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) st_ra_serial(P, P.stamp);
+}
+__global__ void k_ra_spill(Prog P) { PTL_FOR(v, P.W) st_ra_spill(P, v); }
+__global__ void k_ra_scatter(Prog P) { PTL_FOR(i, P.wb8) st_ra_scatter(P, i); }
+__global__ void k_ra_functab(Prog P) { PTL_FOR(f, P.F) st_fix_functab(P, f, P.roffs, P.W); }
+__global__ void k_ra_frame(Prog P) { PTL_FOR(f, P.F) st_ra_frame(P, f); }
+__global__ void k_fj_emit(Prog P) { PTL_FOR(i, P.W2) st_fj_emit(P, i); }
+__global__ void k_fj_functab(Prog P) { PTL_FOR(f, P.F) st_fix_functab(P, f, P.joffs, P.W2); }
+
+}  // namespace
+
+// ====================================================================== launchers
+void launch_translate(const Prog& P, cudaStream_t s) {
+    k_translate<<<grid_for(P.nb8), kThreads, 0, s>>>(P);
+}
+
+void launch_preprocess(const Prog& P, cudaStream_t s) {
+    k_pre_args<<<grid_for(P.nb8), kThreads, 0, s>>>(P);
+    k_pre_lists<<<grid_for(P.nb8), kThreads, 0, s>>>(P);
+    k_pre_float<<<grid_for(P.nb8), kThreads, 0, s>>>(P);
+    k_pre_float_apply<<<grid_for(P.nb8), kThreads, 0, s>>>(P);
+}
+
+void launch_count_scan(const Prog& P, const ScanScratch& sc, cudaStream_t s) {
+    run_scan(CountLoad{P}, StoreTo{P.loc0}, P.nb8, sc, P.err, s);
+}
+
+void launch_fix(const Prog& P, cudaStream_t s) {
+    k_fix_own<<<grid_for(P.nb8), kThreads, 0, s>>>(P);
+    k_fix_cond<<<grid_for(P.nb8), kThreads, 0, s>>>(P);
+}
+
+void launch_decl_scan(const Prog& P, uint32_t* meta, const ScanScratch& sc, cudaStream_t s) {
+    run_scan(DeclLoad{P}, DeclStore{P, meta, P.nb8}, P.nb8, sc, P.err, s);
+}
+
+void launch_functab(const Prog& P, uint32_t* meta, cudaStream_t s) {
+    // F is known on the device only; launch for the node count's upper bound.
+    const uint64_t bound = P.nb8 / 8u + 8u;
+    k_functab<<<grid_for(bound), kThreads, 0, s>>>(P, meta);
+    k_functab_end<<<grid_for(bound), kThreads, 0, s>>>(P, meta);
+}
+
+cudaError_t run_depth_sort(const Prog& P, const SortScratch& ss, cudaStream_t s, uint32_t* rounds_out) {
+    const uint32_t n = P.n;
+    k_sort_init<<<grid_for(n), kThreads, 0, s>>>(P, ss);
+    cudaMemsetAsync(ss.counters, 0, sizeof(uint32_t) * 4, s);
+    uint32_t nseg = 0;
+    if (n > kSortThreshold) {
+        SortSeg g{};
+        g.first = 0;
+        g.last = n;
+        g.dl = 2u * floor_log2(n);
+        cudaMemcpyAsync(ss.seg[0], &g, sizeof(g), cudaMemcpyHostToDevice, s);
+        nseg = 1;
+    } else if (n > 1) {
+        const uint32_t leaf[2] = {0, n};
+        cudaMemcpyAsync(ss.leaf, leaf, sizeof(leaf), cudaMemcpyHostToDevice, s);
+        const uint32_t one = 1;
+        cudaMemcpyAsync(ss.counters + 2, &one, sizeof(one), cudaMemcpyHostToDevice, s);
+    }
+    uint32_t rounds = 0;
+    int cur = 0;
+    while (nseg > 0) {
+        SortSeg* segs = ss.seg[cur];
+        SortSeg* next = ss.seg[cur ^ 1];
+        cudaMemsetAsync(ss.counters, 0, sizeof(uint32_t) * 2, s);
+        k_sort_tiles<<<grid_for(nseg), kThreads, 0, s>>>(ss, segs, segs, nseg);
+        uint32_t ntiles = 0;
+        cudaMemcpyAsync(&ntiles, ss.counters, sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
+        cudaError_t e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) return e;
+        if (ntiles > ss.tile_cap) return cudaErrorMemoryAllocation;
+        k_sort_count<<<ntiles, kThreads, 0, s>>>(ss, segs);
+        k_sort_segscan<<<nseg, kThreads, 0, s>>>(ss, segs);
+        k_sort_pos<<<ntiles, kThreads, 0, s>>>(ss, segs);
+        k_sort_cut<<<grid_for(nseg), kThreads, 0, s>>>(ss, segs, nseg, next);
+        k_sort_swap<<<ntiles, kThreads, 0, s>>>(ss, segs);
+        cudaMemcpyAsync(&nseg, ss.counters + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
+        e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) return e;
+        if (nseg > ss.seg_cap) return cudaErrorMemoryAllocation;
+        cur ^= 1;
+        ++rounds;
+    }
+    uint32_t lh[2] = {0, 0};
+    cudaMemcpyAsync(lh, ss.counters + 2, sizeof(lh), cudaMemcpyDeviceToHost, s);
+    cudaError_t e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return e;
+    if (lh[0] > ss.leaf_cap || lh[1] > ss.leaf_cap) return cudaErrorMemoryAllocation;
+    if (lh[1]) k_sort_heaps<<<grid_for(lh[1]), kThreads, 0, s>>>(ss, lh[1]);
+    if (lh[0]) k_sort_leaves<<<grid_for(lh[0]), kThreads, 0, s>>>(ss, lh[0]);
+    k_sort_out<<<grid_for(n), kThreads, 0, s>>>(P, ss);
+    if (rounds_out) *rounds_out = rounds;
+    return cudaGetLastError();
+}
+
+void launch_gen(const Prog& P, cudaStream_t s) {
+    k_gen_prop<<<grid_for(P.n), kThreads, 0, s>>>(P);
+    k_gen_claim<<<grid_for(P.n), kThreads, 0, s>>>(P);
+    k_gen_write<<<grid_for(P.n), kThreads, 0, s>>>(P);
+}
+
+cudaError_t run_optimize(const Prog& P, cudaStream_t s, uint32_t* sweeps_out) {
+    k_opt_mark<<<grid_for(P.wb8), kThreads, 0, s>>>(P);
+    uint32_t sweeps = 0;
+    for (;;) {
+        cudaMemsetAsync(P.flags, 0, sizeof(uint32_t), s);
+        for (int k = 0; k < 4; ++k) k_opt_sweep<<<grid_for(P.wb8), kThreads, 0, s>>>(P);
+        sweeps += 4;
+        uint32_t changed = 0;
+        cudaMemcpyAsync(&changed, P.flags, sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
+        const cudaError_t e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) return e;
+        if (!changed) break;
+        if (sweeps > P.W + 8u) break;  // cannot happen: every sweep clears a mark
+    }
+    k_opt_final<<<grid_for(P.wb8), kThreads, 0, s>>>(P);
+    if (sweeps_out) *sweeps_out = sweeps;
+    return cudaGetLastError();
+}
+
+cudaError_t run_regalloc_steps(const Prog& P, cudaStream_t s, bool* serial_out) {
+    // Programs whose functions share symbols need the reference's serial order.
+    cudaMemsetAsync(P.flags + 1, 0, sizeof(uint32_t), s);
+    k_ra_cross<<<grid_for(P.W), kThreads, 0, s>>>(P);
+    uint32_t cross = 0;
+    cudaMemcpyAsync(&cross, P.flags + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
+    const cudaError_t e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return e;
+    if (cross) {
+        k_ra_serial<<<1, 1, 0, s>>>(P);
+    } else {
+        k_ra_free<<<grid_for(P.F, 64), 64, 0, s>>>(P);
+        k_ra_lane0<<<1, kRaThreads, 0, s>>>(P, P.S);
+    }
+    k_ra_spill<<<grid_for(P.W), kThreads, 0, s>>>(P);
+    if (serial_out) *serial_out = cross != 0;
+    return cudaGetLastError();
+}
+
+void launch_regalloc_count_scan(const Prog& P, const ScanScratch& sc, cudaStream_t s) {
+    run_scan(RaCountLoad{P}, StoreTo{P.roffs}, P.wb8, sc, P.err, s);
+}
+
+void launch_regalloc_emit(const Prog& P, cudaStream_t s) {
+    k_ra_scatter<<<grid_for(P.wb8), kThreads, 0, s>>>(P);
+    k_ra_functab<<<grid_for(P.F), kThreads, 0, s>>>(P);
+    k_ra_frame<<<grid_for(P.F), kThreads, 0, s>>>(P);
+}
+
+void launch_fixjumps_scan(const Prog& P, const ScanScratch& sc, cudaStream_t s) {
+    run_scan(FjSizeLoad{P}, StoreTo{P.joffs}, P.w2b8, sc, P.err, s);
+}
+
+void launch_fixjumps_emit(const Prog& P, cudaStream_t s) {
+    k_fj_emit<<<grid_for(P.W2), kThreads, 0, s>>>(P);
+    k_fj_functab<<<grid_for(P.F), kThreads, 0, s>>>(P);
+}
+
+}  // namespace ptl

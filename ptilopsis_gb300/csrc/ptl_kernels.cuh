@@ -1,0 +1,53 @@
+// Kernel launch interface of the GB300 code generator (ptl_kernels.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "ptl_stages.cuh"
+#include "ptl_sort.cuh"
+
+namespace ptl {
+
+// Device scratch that a compile needs besides the Prog arrays; sized by the arena.
+struct SortScratch {
+    unsigned long long* a;     // (key, index) pairs, n
+    uint32_t* apos;            // L-stop positions by rank, n
+    uint32_t* bpos;            // R-stop positions by rank from the right, n
+    SortSeg* seg[2];           // segment lists of this and the next round
+    uint32_t seg_cap;
+    uint32_t* tile_seg;        // tile -> segment
+    uint32_t* tile_l;          // L-stop count per tile, then its exclusive offset
+    uint32_t* tile_r;
+    uint32_t tile_cap;
+    uint32_t* leaf;            // leaf ranges (first, last)
+    uint32_t* heap;            // heap-sorted ranges
+    uint32_t leaf_cap;
+    uint32_t* counters;        // [0] tiles [1] next segments [2] leaves [3] heaps
+};
+
+struct ScanScratch {
+    unsigned long long* status;  // per tile: (flag << 32) | value
+    uint32_t* counter;           // dynamic tile ticket
+    uint32_t tile_cap;
+};
+
+// Element-wise stages (grid-stride launches of the per-thread functions).
+void launch_translate(const Prog& P, cudaStream_t s);
+void launch_preprocess(const Prog& P, cudaStream_t s);
+void launch_count_scan(const Prog& P, const ScanScratch& sc, cudaStream_t s);
+void launch_fix(const Prog& P, cudaStream_t s);
+void launch_decl_scan(const Prog& P, uint32_t* flags_tmp, const ScanScratch& sc, cudaStream_t s);
+void launch_functab(const Prog& P, uint32_t* meta, cudaStream_t s);
+
+// Depth-order emulation; returns a CUDA error and needs the host for its round loop.
+cudaError_t run_depth_sort(const Prog& P, const SortScratch& ss, cudaStream_t s, uint32_t* rounds_out);
+
+void launch_gen(const Prog& P, cudaStream_t s);
+cudaError_t run_optimize(const Prog& P, cudaStream_t s, uint32_t* sweeps_out);
+cudaError_t run_regalloc_steps(const Prog& P, cudaStream_t s, bool* serial_out);
+void launch_regalloc_count_scan(const Prog& P, const ScanScratch& sc, cudaStream_t s);
+void launch_regalloc_emit(const Prog& P, cudaStream_t s);
+void launch_fixjumps_scan(const Prog& P, const ScanScratch& sc, cudaStream_t s);
+void launch_fixjumps_emit(const Prog& P, cudaStream_t s);
+
+}  // namespace ptl

@@ -1,0 +1,148 @@
+// Emulation of the order libstdc++'s std::sort leaves when it sorts iota(n) by depth --
+// the reference's isn_gen sort, src/codegen/rv_generator_avx.cpp:539-541.  That order
+// decides which of two same-depth nodes writes a shared instruction slot last, so the
+// GPU must reproduce it exactly, not merely sort.
+//
+// std::sort is introsort (the published algorithm, Musser 1997, as libstdc++ writes
+// it): while a range holds more than 16 elements, move the median of (first+1, mid,
+// last-1) to first, partition [first+1, last) around it with the unguarded Hoare scan,
+// and recurse; a range whose depth budget (2*floor(log2 n)) runs out is heap-sorted;
+// a final insertion sort finishes the small ranges.
+//
+// The Hoare scan is sequential, but its result has a closed form that parallelises:
+// call an element an L-stop when its key >= pivot and an R-stop when key <= pivot.  Let
+// A[k] be the k-th L-stop from the left and B[k] the k-th R-stop from the right.  The
+// scan swaps A[k] with B[k] exactly for k < K, where K counts the k with A[k] < B[k],
+// and returns cut = A[0] when K == 0, else min(A[K], B[K-1]).  (An element equal to the
+// pivot is both kinds of stop but is swapped at most once.)  The insertion sort is
+// stable and never moves an element across a partition boundary, so it amounts to a
+// stable sort of each final range of <= 16 elements.
+#pragma once
+
+#include "ptl_common.cuh"
+
+namespace ptl {
+
+struct SortSeg {
+    uint32_t first, last;  // [first, last) in the array
+    uint32_t dl;           // remaining depth budget
+    int32_t pivot;         // pivot key after the median move
+    uint32_t tbase, tcount;  // tiles of [first+1, last)
+    uint32_t nL, nR;       // stop counts
+    uint32_t K, cut;
+};
+
+constexpr uint32_t kSortThreshold = 16;   // libstdc++ _S_threshold
+constexpr uint32_t kSortTile = 2048;      // elements per partition tile
+
+PTL_HD int32_t skey(unsigned long long e) { return static_cast<int32_t>(static_cast<uint32_t>(e >> 32)); }
+PTL_HD uint32_t sidx(unsigned long long e) { return static_cast<uint32_t>(e); }
+
+PTL_HD uint32_t floor_log2(uint32_t n) {
+    uint32_t r = 0;
+    while (n > 1) { n >>= 1; ++r; }
+    return r;
+}
+
+PTL_HD void sswap(unsigned long long* a, uint32_t i, uint32_t j) {
+    const unsigned long long t = a[i];
+    a[i] = a[j];
+    a[j] = t;
+}
+
+// std::__move_median_to_first(result = first, a = first+1, b = mid, c = last-1)
+PTL_HD void median_to_first(unsigned long long* a, uint32_t first, uint32_t last) {
+    const uint32_t ia = first + 1, ib = first + (last - first) / 2, ic = last - 1;
+    const int32_t ka = skey(a[ia]), kb = skey(a[ib]), kc = skey(a[ic]);
+    uint32_t pick;
+    if (ka < kb) {
+        if (kb < kc) pick = ib;
+        else if (ka < kc) pick = ic;
+        else pick = ia;
+    } else if (ka < kc) {
+        pick = ia;
+    } else if (kb < kc) {
+        pick = ic;
+    } else {
+        pick = ib;
+    }
+    sswap(a, first, pick);
+}
+
+PTL_HD bool is_lstop(int32_t key, int32_t pivot) { return !(key < pivot); }
+PTL_HD bool is_rstop(int32_t key, int32_t pivot) { return !(pivot < key); }
+
+// K = #{k : A[k] < B[k]}; the predicate is true for a prefix of k.
+PTL_HD uint32_t partition_k(const uint32_t* apos, const uint32_t* bpos, uint32_t nL, uint32_t nR) {
+    uint32_t lo = 0, hi = nL < nR ? nL : nR;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) / 2;
+        if (apos[mid] < bpos[mid]) lo = mid + 1; else hi = mid;
+    }
+    return lo;
+}
+
+PTL_HD uint32_t partition_cut(const uint32_t* apos, const uint32_t* bpos, uint32_t nL, uint32_t K) {
+    if (K == 0) return apos[0];
+    const uint32_t b = bpos[K - 1];
+    if (K < nL && apos[K] < b) return apos[K];
+    return b;
+}
+
+// libstdc++ __adjust_heap / __push_heap / make_heap / sort_heap on a[first, first+len).
+PTL_HD void heap_push(unsigned long long* a, int64_t hole, int64_t top, unsigned long long v) {
+    int64_t parent = (hole - 1) / 2;
+    while (hole > top && skey(a[parent]) < skey(v)) {
+        a[hole] = a[parent];
+        hole = parent;
+        parent = (hole - 1) / 2;
+    }
+    a[hole] = v;
+}
+
+PTL_HD void heap_adjust(unsigned long long* a, int64_t hole, int64_t len, unsigned long long v) {
+    const int64_t top = hole;
+    int64_t second = hole;
+    while (second < (len - 1) / 2) {
+        second = 2 * (second + 1);
+        if (skey(a[second]) < skey(a[second - 1])) second--;
+        a[hole] = a[second];
+        hole = second;
+    }
+    if ((len & 1) == 0 && second == (len - 2) / 2) {
+        second = 2 * (second + 1);
+        a[hole] = a[second - 1];
+        hole = second - 1;
+    }
+    heap_push(a, hole, top, v);
+}
+
+PTL_HD void heap_sort_range(unsigned long long* base, uint32_t len) {
+    if (len < 2) return;
+    const int64_t n = len;
+    for (int64_t parent = (n - 2) / 2;; --parent) {
+        heap_adjust(base, parent, n, base[parent]);
+        if (parent == 0) break;
+    }
+    for (int64_t last = n; last > 1;) {
+        --last;
+        const unsigned long long v = base[last];
+        base[last] = base[0];
+        heap_adjust(base, 0, last, v);
+    }
+}
+
+// Stable insertion sort by key (what the final insertion sort does to one small range).
+PTL_HD void leaf_sort(unsigned long long* a, uint32_t first, uint32_t last) {
+    for (uint32_t i = first + 1; i < last; ++i) {
+        const unsigned long long v = a[i];
+        uint32_t j = i;
+        while (j > first && skey(v) < skey(a[j - 1])) {
+            a[j] = a[j - 1];
+            --j;
+        }
+        a[j] = v;
+    }
+}
+
+}  // namespace ptl
