@@ -1,0 +1,308 @@
+"""Benchmark: AST nodes/s of the GB300 code generator.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--config c1] [--impl gb300|reference]
+
+A step is one full compile (all seven stages) of one synthetic program.  The default
+workload is the large single program (config c1: ~4M nodes, 2,048 functions); the
+other configurations are parity-test cases.  Prints one JSON line (rank 0).
+
+  value       nodes/s with the tree already resident in HBM; device time of the
+              pipeline from CUDA events the library records on its own stream
+  e2e         the same through the public API with host buffers: host->device copy
+              of the six arrays, the compile, device->host copy of the words and the
+              function table, per step
+  roofline    the dominant kernel: algorithmic bytes per launch / its event-timed
+              duration, against the measured HBM copy bandwidth
+  cpu_baseline  the oracle's CPU restatement of the reference on the same program,
+              one thread, one compile
+
+--impl reference times the oracle restatement on the host cores, on the same workload
+(the reference itself is AVX2-only and cannot run on the aarch64 GPU hosts).
+Multi-GPU: every rank compiles its own replica (programs do not shard below the
+program level); value aggregates nodes over ranks, timed to the slowest rank.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = "AST nodes/s codegen, batched vs plain GPU (bit-exact); serving p50/p99 latency"
+UNIT = "nodes/s"
+
+# Algorithmic bytes per unit (node n, word w) of each stage: the minimum single-pass
+# traffic of the reference's arrays.
+STAGE_BYTES = {
+    "preprocess": lambda n, w, w2, w3: 20 * n,
+    "isn_cnt": lambda n, w, w2, w3: 14 * n,
+    "isn_gen": lambda n, w, w2, w3: 22 * n + 16 * n + 20 * w,
+    "optimize": lambda n, w, w2, w3: 16 * w + 8 * w,
+    "regalloc": lambda n, w, w2, w3: 24 * w + 20 * w2,
+    "fix_jumps": lambda n, w, w2, w3: 20 * w2 + 4 * w3,
+}
+
+
+def env_rank():
+    return (int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)),
+            int(os.environ.get("LOCAL_RANK", 0)))
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.path or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    sm.append(float(parts[1]))
+                    smax.append(float(parts[2]))
+                except ValueError:
+                    continue
+                for name, val in zip(names, parts[5:9]):
+                    if val.lower() == "active":
+                        reasons.add(name)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def l2_flush(buf):
+    buf.fill_(1)  # 256 MB > the 129 MB L2
+
+
+def cpu_baseline(tree, sample: str):
+    from oracle import portbind
+    from oracle.refbind import Ast
+    ast = Ast(tree.type, tree.rtype, tree.parent, tree.depth, tree.child_idx, tree.data, tree.max_depth)
+    t0 = time.perf_counter()
+    res = portbind.compile_ast(ast)
+    dt = time.perf_counter() - t0
+    return {"value": tree.n / dt, "unit": UNIT, "cores": 1, "kind": "port", "sample": sample,
+            "seconds": round(dt, 3), "words": int(len(res.words))}, res
+
+
+def run_reference(args):
+    rank, world, _ = env_rank()
+    if rank != 0:
+        return
+    from ptilopsis_gb300 import build as b
+    from ptilopsis_gb300.synth import config_tree
+    from oracle import portbind
+    b.build_synth()
+    portbind.build()
+    tree = config_tree(args.config, args.scale)
+    sample = f"one full compile of config {args.config} ({tree.n} nodes) per step, one thread"
+    for _ in range(args.warmup):
+        cpu_baseline(tree, sample)
+    times = []
+    for _ in range(args.steps):
+        base, _ = cpu_baseline(tree, sample)
+        times.append(base["seconds"])
+    ms = 1000.0 * sum(times) / len(times)
+    value = tree.n / (ms / 1000.0)
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u32", "data": "synthetic (seeded grammar)", "impl": "reference",
+            "config": {"workload": f"{args.config}: one synthetic program, {tree.n} nodes", "nodes": tree.n},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_gb300(args):
+    import torch
+    rank, world, local = env_rank()
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    from ptilopsis_gb300 import RvGenerator, STAGES
+    from ptilopsis_gb300 import build as b
+    from ptilopsis_gb300.codegen import kernel_launches
+    from ptilopsis_gb300.synth import config_tree
+    b.build_all()
+    tree = config_tree(args.config, args.scale)
+    n = tree.n
+    dev = torch.device("cuda", local)
+    dtree = tree.to(dev)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    gen = RvGenerator(dtree, device=local)
+    for _ in range(args.warmup):
+        gen.process(profile=True, to_host=False)
+    barrier()
+    stage_sum = np.zeros(7)
+    step_ms = []
+    launches0 = kernel_launches()
+    t_wall0 = time.perf_counter()
+    with ClockSampler(local) as clocks:
+        for _ in range(args.steps):
+            l2_flush(flush)
+            torch.cuda.synchronize()
+            gen.process(profile=True, to_host=False)
+            ns = np.array(gen.stage_ns(), dtype=np.float64)
+            stage_sum += ns
+            step_ms.append(ns.sum() / 1e6)
+        barrier()
+    wall_s = time.perf_counter() - t_wall0
+    launches = kernel_launches() - launches0
+    ms = float(np.mean(step_ms))
+    ms_all = ms
+    if dist is not None:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_all = float(t.item())
+    value = world * n / (ms_all / 1000.0)
+    words_dev, n_words = gen.device_instructions()
+    W3 = n_words
+
+    # ---- e2e: host buffers through the public API
+    pinned = {k: torch.from_numpy(np.ascontiguousarray(getattr(tree, k).view(np.int32) if k == "data" else getattr(tree, k))).pin_memory()
+              for k in ("type", "rtype", "parent", "depth", "child_idx", "data")}
+    from ptilopsis_gb300 import DepthTree
+    htree = DepthTree(max_depth=tree.max_depth, **pinned)
+    ftab_entries = 0
+    e2e_s = []
+    for k in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        gen.upload(htree)
+        gen.process(profile=False, to_host=True)
+        words = gen.get_instructions()
+        ftab = gen.function_table()
+        dt = time.perf_counter() - t0
+        if k >= args.warmup:
+            e2e_s.append(dt)
+        ftab_entries = len(ftab["starts"])
+    e2e_ms = 1000.0 * float(np.mean(e2e_s))
+    if dist is not None:
+        t = torch.tensor([e2e_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    e2e = {"value": world * n / (e2e_ms / 1000.0), "unit": UNIT, "h2d_bytes_per_step": int(18 * n),
+           "d2h_bytes_per_step": int(4 * len(words) + 16 * ftab_entries), "ms_per_step": e2e_ms}
+
+    # ---- roofline of the dominant stage (event-timed on the library's stream)
+    stage_ms = stage_sum / 1e6 / args.steps
+    sizes = gen_sizes(gen)
+    dom = int(np.argmax(stage_ms[:6]))
+    name = STAGES[dom]
+    alg = STAGE_BYTES[name](n, sizes["W"], sizes["W2"], W3)
+    achieved = alg / (stage_ms[dom] / 1000.0) / 1e9
+    peak, peak_kind = peaks()
+    roofline = {"bound": "hbm", "kernel": f"{name} stage", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "peak_source": peak_kind, "traffic": None,
+                "algorithmic_bytes_per_launch": int(alg),
+                "stage_ms": {s: round(float(v), 4) for s, v in zip(STAGES, stage_ms)}}
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_all, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u32", "data": "synthetic (seeded grammar, no datasets)",
+            "config": {"workload": f"{args.config}: one synthetic program per GPU, {n} nodes, "
+                                   f"{sizes['F']} functions, {W3} output words",
+                       "nodes": n, "functions": sizes["F"], "words": W3,
+                       "l2": "flushed between steps (256 MB write); working set > L2",
+                       "parallelism": f"replicas x{world}"},
+            "e2e": e2e, "roofline": roofline, "gpu_launches": int(launches),
+            "wall_s_timed": round(wall_s, 3)}
+    if rank == 0:
+        line["clocks"] = clocks.summary()
+        if not args.no_cpu_baseline:
+            base, ref = cpu_baseline(tree, f"one full compile of {args.config} ({n} nodes), one thread")
+            line["cpu_baseline"] = base
+            gen.process(profile=False, to_host=True)
+            line["bit_exact_vs_oracle"] = bool(np.array_equal(gen.get_instructions(), ref.words))
+        print(json.dumps(line), flush=True)
+    gen.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def gen_sizes(gen):
+    import ctypes
+    from ptilopsis_gb300.codegen import SNAPSHOTS
+    out = {}
+    for key, snap in (("W", "gen_instr"), ("W2", "ra_instr"), ("F", "fn_start")):
+        n = ctypes.c_size_t()
+        gen._lib.ptl_generator_snapshot(gen._h, SNAPSHOTS[snap], None, 0, ctypes.byref(n))
+        out[key] = int(n.value)
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--config", default="c1")
+    ap.add_argument("--scale", type=float, default=1.0)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -59,6 +59,11 @@ typedef struct ptl_generator ptl_generator;
  * of the CPU constructor have no GPU meaning and are not taken. */
 ptl_status ptl_generator_create(const ptl_ast_view* tree, int device, ptl_generator** out);
 
+/* Replaces the generator's input with another tree of any size, reusing the device
+ * memory of earlier compiles (the reference builds a new generator per tree).  Host
+ * trees are copied on the generator's stream. */
+ptl_status ptl_generator_upload(ptl_generator* gen, const ptl_ast_view* tree);
+
 /* Replaces rv_generator_avx::process(bool profile) (rv_generator_avx.cpp:104-120): runs
  * the seven stages.  Unlike the reference, which mutates its arrays and cannot be run
  * twice, process may be called again and recompiles from the copied tree. */
@@ -107,6 +112,9 @@ ptl_status ptl_generator_snapshot(ptl_generator* gen, int which, uint32_t* out, 
  * 6 instr_constant[256][4], 7 operand[256][4][6][2], 8 instr_jt[256][4],
  * 9 pareas_to_rv[44].  Returns the element count; out may be NULL. */
 size_t ptl_code_table(int which, uint32_t* out);
+
+/* Kernel launches the library has issued so far (all generators of the process). */
+uint64_t ptl_kernel_launches(void);
 
 /* Library and device facts: CUDA runtime/driver versions, device name. */
 ptl_status ptl_device_info(int device, char* name, size_t name_len, int* sm_count,

@@ -1,0 +1,299 @@
+"""Python mirror of the reference code generator's interface, over the C ABI of
+include/ptl_codegen.h (libptl_gb300.so).
+
+The reference (TypeA2/Ptilopsis) is driven as
+
+    DepthTree tree(ast);                                   // pareas-ast flattening
+    rv_generator_avx gen(tree, threads, sync, altblock, mininstr);
+    gen.process(profile);
+    gen.get_instructions();  gen.to_binary(os);
+
+(src/main.cpp:119-157).  Here:
+
+    gen = RvGenerator(tree)          # tree: DepthTree of numpy arrays or CUDA tensors
+    gen.process(profile=True)
+    gen.get_instructions()           # np.uint32 words, identical to the reference's
+    gen.to_binary(stream)
+
+There is no CPU fallback: if the CUDA library is missing or no GPU is visible,
+constructing a generator raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from dataclasses import dataclass
+from typing import BinaryIO, Optional
+
+import numpy as np
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_PKG, "_lib", "libptl_gb300.so")
+
+# ptl_status (include/ptl_codegen.h)
+STATUS = {0: "OK", 1: "INVALID_AST", 2: "UNSUPPORTED", 3: "OOM", 4: "ADMISSION_DENIED",
+          5: "DEVICE_TIMEOUT", 6: "CUDA_ERROR", 7: "BAD_ARGUMENT"}
+
+STAGES = ["preprocess", "isn_cnt", "isn_gen", "optimize", "regalloc", "fix_jumps", "postprocess"]
+
+# Snapshot slots of ptl_generator_snapshot: the reference generator's arrays after each
+# stage (same order as the oracle harness).  Slots the GPU pipeline does not keep
+# (the intermediate fix_jumps arrays, fused with postprocess) are absent.
+SNAPSHOTS = {
+    "out_words": 0, "fn_start": 1, "fn_end": 2, "fn_size": 3, "fn_id": 4,
+    "pre_type": 5, "pre_rtype": 6, "pre_data": 7,
+    "cnt_size": 8, "cnt_loc": 9, "cnt_fn_id": 10, "cnt_fn_start": 11, "cnt_fn_end": 12, "cnt_fn_size": 13,
+    "gen_instr": 14, "gen_rd": 15, "gen_rs1": 16, "gen_rs2": 17, "gen_jt": 18,
+    "opt_used": 19,
+    "ra_instr": 20, "ra_rd": 21, "ra_rs1": 22, "ra_rs2": 23, "ra_jt": 24,
+    "ra_fn_start": 25, "ra_fn_end": 26, "ra_fn_size": 27,
+    "depth_order_pos": 40, "registers": 41,
+}
+
+
+class PtlError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{STATUS.get(status, status)}: {message}")
+        self.status = status
+
+
+@dataclass
+class DepthTree:
+    """The flattened AST of pareas-ast (subprojects/pareas-ast/include/codegen/
+    depthtree.hpp:12-59): six parallel arrays in post-order, root last."""
+    type: object        # u8 Pareas NodeType
+    rtype: object       # u8 Pareas DataType
+    parent: object      # i32
+    depth: object       # i32
+    child_idx: object   # i32
+    data: object        # u32
+    max_depth: int
+
+    @property
+    def n(self) -> int:
+        return int(self.type.shape[0])
+
+    @property
+    def on_device(self) -> bool:
+        return bool(getattr(self.type, "is_cuda", False))
+
+    def to(self, device) -> "DepthTree":
+        """Copy the arrays to a torch device (for device-resident compiles)."""
+        import torch
+        conv = {"type": torch.uint8, "rtype": torch.uint8, "parent": torch.int32,
+                "depth": torch.int32, "child_idx": torch.int32, "data": torch.int32}
+        out = {}
+        for k, dt in conv.items():
+            a = getattr(self, k)
+            if isinstance(a, np.ndarray):
+                a = torch.from_numpy(a.view(np.int32) if k == "data" else a)
+            out[k] = a.to(device=device, dtype=dt).contiguous()
+        return DepthTree(max_depth=self.max_depth, **out)
+
+    def numpy(self) -> "DepthTree":
+        def host(a, dt):
+            if isinstance(a, np.ndarray):
+                return np.ascontiguousarray(a, dt)
+            return np.ascontiguousarray(a.cpu().numpy()).view(dt) if dt == np.uint32 else np.ascontiguousarray(a.cpu().numpy(), dt)
+        return DepthTree(host(self.type, np.uint8), host(self.rtype, np.uint8), host(self.parent, np.int32),
+                         host(self.depth, np.int32), host(self.child_idx, np.int32), host(self.data, np.uint32),
+                         self.max_depth)
+
+    def nbytes(self) -> int:
+        return self.n * 18
+
+
+class _AstView(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_size_t), ("max_depth", ctypes.c_size_t),
+                ("type", ctypes.c_void_p), ("rtype", ctypes.c_void_p), ("parent", ctypes.c_void_p),
+                ("depth", ctypes.c_void_p), ("child_idx", ctypes.c_void_p), ("data", ctypes.c_void_p),
+                ("on_device", ctypes.c_int)]
+
+
+_lib = None
+
+
+def library_path() -> str:
+    return LIB_PATH
+
+
+def lib():
+    """Load libptl_gb300.so; raises when it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"GB300 code generator library missing ({LIB_PATH}); run "
+                               "ptilopsis_gb300.build.build_all() -- there is no CPU fallback")
+        L = ctypes.CDLL(LIB_PATH)
+        vp, sz, u32p = ctypes.c_void_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_uint32)
+        L.ptl_generator_create.argtypes = [ctypes.POINTER(_AstView), ctypes.c_int, ctypes.POINTER(vp)]
+        L.ptl_generator_process.argtypes = [vp, ctypes.c_int]
+        L.ptl_generator_upload.argtypes = [vp, ctypes.POINTER(_AstView)]
+        L.ptl_kernel_launches.argtypes = []
+        L.ptl_kernel_launches.restype = ctypes.c_uint64
+        L.ptl_generator_instructions.argtypes = [vp, ctypes.POINTER(u32p), ctypes.POINTER(sz)]
+        L.ptl_generator_device_instructions.argtypes = [vp, ctypes.POINTER(vp), ctypes.POINTER(sz)]
+        L.ptl_generator_function_table.argtypes = [vp, ctypes.POINTER(u32p), ctypes.POINTER(u32p),
+                                                   ctypes.POINTER(u32p), ctypes.POINTER(u32p), ctypes.POINTER(sz)]
+        L.ptl_generator_stage_ns.argtypes = [vp, ctypes.POINTER(ctypes.c_uint64)]
+        L.ptl_generator_last_error.argtypes = [vp]
+        L.ptl_generator_last_error.restype = ctypes.c_char_p
+        L.ptl_generator_destroy.argtypes = [vp]
+        L.ptl_generator_destroy.restype = None
+        L.ptl_generator_snapshot.argtypes = [vp, ctypes.c_int, u32p, sz, ctypes.POINTER(sz)]
+        L.ptl_compile.argtypes = [ctypes.POINTER(_AstView), ctypes.c_int, u32p, sz, ctypes.POINTER(sz)]
+        L.ptl_code_table.argtypes = [ctypes.c_int, u32p]
+        L.ptl_code_table.restype = ctypes.c_size_t
+        L.ptl_device_info.argtypes = [ctypes.c_int, ctypes.c_char_p, sz, ctypes.POINTER(ctypes.c_int),
+                                      ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
+        for fn in ("ptl_generator_create", "ptl_generator_process", "ptl_generator_upload", "ptl_generator_instructions",
+                   "ptl_generator_device_instructions", "ptl_generator_function_table",
+                   "ptl_generator_stage_ns", "ptl_generator_snapshot", "ptl_compile", "ptl_device_info"):
+            getattr(L, fn).restype = ctypes.c_int
+        _lib = L
+    return _lib
+
+
+def _ptr(a) -> int:
+    if isinstance(a, np.ndarray):
+        return a.ctypes.data
+    return a.data_ptr()
+
+
+def _view(tree: DepthTree, keep: list) -> _AstView:
+    v = _AstView()
+    v.n = tree.n
+    v.max_depth = int(tree.max_depth)
+    on_dev = tree.on_device
+    arrays = []
+    for name, dt in (("type", np.uint8), ("rtype", np.uint8), ("parent", np.int32), ("depth", np.int32),
+                     ("child_idx", np.int32), ("data", np.uint32)):
+        a = getattr(tree, name)
+        if not on_dev:
+            a = np.ascontiguousarray(a, dt)
+        keep.append(a)
+        arrays.append(_ptr(a))
+    v.type, v.rtype, v.parent, v.depth, v.child_idx, v.data = arrays
+    v.on_device = 1 if on_dev else 0
+    return v
+
+
+def code_table(which: int) -> np.ndarray:
+    """The generator's code tables in the reference's flat layouts (ptl_code_table)."""
+    L = lib()
+    n = L.ptl_code_table(which, None)
+    out = np.empty(n, np.uint32)
+    L.ptl_code_table(which, out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)))
+    return out
+
+
+class RvGenerator:
+    """GPU counterpart of rv_generator_avx (include/codegen/rv_generator_avx.hpp:26-148)."""
+
+    def __init__(self, tree: DepthTree, device: int = 0):
+        self._lib = lib()
+        self._h = ctypes.c_void_p()
+        keep: list = []
+        view = _view(tree, keep)
+        st = self._lib.ptl_generator_create(ctypes.byref(view), device, ctypes.byref(self._h))
+        if st != 0:
+            raise PtlError(st, "ptl_generator_create")
+        self.n = tree.n
+
+    def _check(self, st: int, what: str) -> None:
+        if st != 0:
+            msg = self._lib.ptl_generator_last_error(self._h)
+            raise PtlError(st, f"{what}: {msg.decode() if msg else ''}")
+
+    def upload(self, tree: DepthTree) -> None:
+        """Rebinds the generator to another tree, reusing its device memory."""
+        keep: list = []
+        view = _view(tree, keep)
+        self._check(self._lib.ptl_generator_upload(self._h, ctypes.byref(view)), "upload")
+        self.n = tree.n
+
+    def process(self, profile: bool = False, to_host: bool = True) -> None:
+        """rv_generator_avx::process.  to_host=False leaves the words on the device."""
+        flags = (1 if profile else 0) | (0 if to_host else 2)
+        self._check(self._lib.ptl_generator_process(self._h, flags), "process")
+
+    def get_instructions(self) -> np.ndarray:
+        p = ctypes.POINTER(ctypes.c_uint32)()
+        n = ctypes.c_size_t()
+        self._check(self._lib.ptl_generator_instructions(self._h, ctypes.byref(p), ctypes.byref(n)), "instructions")
+        if n.value == 0:
+            return np.zeros(0, np.uint32)
+        return np.ctypeslib.as_array(p, shape=(n.value,)).copy()
+
+    def device_instructions(self):
+        """(device pointer, count) of the output words."""
+        p = ctypes.c_void_p()
+        n = ctypes.c_size_t()
+        self._check(self._lib.ptl_generator_device_instructions(self._h, ctypes.byref(p), ctypes.byref(n)), "device words")
+        return p.value, n.value
+
+    def function_table(self) -> dict:
+        ptrs = [ctypes.POINTER(ctypes.c_uint32)() for _ in range(4)]
+        n = ctypes.c_size_t()
+        self._check(self._lib.ptl_generator_function_table(self._h, *[ctypes.byref(p) for p in ptrs], ctypes.byref(n)),
+                    "function table")
+        names = ["starts", "ends", "sizes", "ids"]
+        return {k: (np.ctypeslib.as_array(p, shape=(n.value,)).copy() if n.value else np.zeros(0, np.uint32))
+                for k, p in zip(names, ptrs)}
+
+    def stage_ns(self) -> list:
+        ns = (ctypes.c_uint64 * 7)()
+        self._check(self._lib.ptl_generator_stage_ns(self._h, ns), "stage_ns")
+        return list(ns)
+
+    def snapshot(self, name: str) -> np.ndarray:
+        which = SNAPSHOTS[name]
+        n = ctypes.c_size_t()
+        self._check(self._lib.ptl_generator_snapshot(self._h, which, None, 0, ctypes.byref(n)), "snapshot size")
+        out = np.empty(n.value, np.uint32)
+        if n.value:
+            self._check(self._lib.ptl_generator_snapshot(self._h, which, out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)),
+                                                         n.value, ctypes.byref(n)), "snapshot")
+        return out
+
+    def to_binary(self, stream: BinaryIO) -> None:
+        """rv_generator::to_binary (src/codegen/rv_generator.cpp:116-119): raw
+        little-endian 32-bit words."""
+        stream.write(self.get_instructions().astype("<u4").tobytes())
+
+    def close(self) -> None:
+        if self._h:
+            self._lib.ptl_generator_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+def compile_tree(tree: DepthTree, device: int = 0, profile: bool = False) -> np.ndarray:
+    with RvGenerator(tree, device) as gen:
+        gen.process(profile=profile)
+        return gen.get_instructions()
+
+
+def kernel_launches() -> int:
+    """Kernel launches issued by the library so far in this process."""
+    return int(lib().ptl_kernel_launches())
+
+
+def device_info(device: int = 0) -> Optional[dict]:
+    L = lib()
+    name = ctypes.create_string_buffer(256)
+    sm, ma, mi = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    if L.ptl_device_info(device, name, 256, ctypes.byref(sm), ctypes.byref(ma), ctypes.byref(mi)) != 0:
+        return None
+    return {"name": name.value.decode(), "sm_count": sm.value, "cc": (ma.value, mi.value)}

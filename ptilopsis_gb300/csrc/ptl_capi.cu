@@ -313,8 +313,10 @@ ptl_status run_pipeline(ptl_generator* g, bool profile, bool to_host) {
                    static_cast<uint32_t>(scan_tiles)};
 
     // ---- input checks
+    note_launch();
     k_validate<<<std::min<size_t>((n + 255) / 256, 152 * 16), 256, 0, s>>>(
         P.in_type, P.in_rtype, P.in_parent, P.in_depth, P.in_child, P.n, P.max_depth, P.err);
+    note_launch();
     k_depth_seen<<<std::min<size_t>((n + 255) / 256, 152 * 16), 256, 0, s>>>(P.in_depth, P.n,
                                                                              g->depth_seen.at<uint32_t>());
     if (ptl_status st = check_error_word(g); st != PTL_OK) return st;
@@ -414,6 +416,7 @@ ptl_status run_pipeline(ptl_generator* g, bool profile, bool to_host) {
     // ---- regalloc
     PTL_CU(g->lifetime.ensure(fb8, 8));
     PTL_CU(g->lifetime.zero(s));
+    note_launch();
     k_init_lifetime<<<std::min<size_t>((g->F + 255) / 256, 1024), 256, 0, s>>>(g->lifetime.at<unsigned long long>(), g->F);
     const size_t trig = static_cast<size_t>(std::max<uint32_t>(g->S, 1)) * 64;
     PTL_CU(g->trig_min.ensure(trig, 4));
@@ -478,13 +481,48 @@ ptl_status run_pipeline(ptl_generator* g, bool profile, bool to_host) {
 
 extern "C" {
 
-ptl_status ptl_generator_create(const ptl_ast_view* tree, int device, ptl_generator** out) {
-    if (!tree || !out) return PTL_BAD_ARGUMENT;
-    *out = nullptr;
-    if (tree->n == 0 || tree->n >= (1ull << 31) || !tree->type || !tree->rtype || !tree->parent ||
-        !tree->depth || !tree->child_idx || !tree->data) {
-        return PTL_BAD_ARGUMENT;
+namespace {
+
+cudaError_t upload_inputs(ptl_generator* g, const ptl_ast_view* tree) {
+    const cudaMemcpyKind kind = tree->on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    const size_t n = tree->n;
+    struct { DevBuf* b; const void* src; size_t es; } in[] = {
+        {&g->in_type, tree->type, 1}, {&g->in_rtype, tree->rtype, 1}, {&g->in_parent, tree->parent, 4},
+        {&g->in_depth, tree->depth, 4}, {&g->in_child, tree->child_idx, 4}, {&g->in_data, tree->data, 4}};
+    cudaError_t e = cudaSuccess;
+    for (auto& x : in) {
+        e = x.b->ensure(n, x.es);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(x.b->at<char>(), x.src, n * x.es, kind, g->stream);
+        if (e != cudaSuccess) return e;
     }
+    g->n = tree->n;
+    g->max_depth = tree->max_depth;
+    g->host_valid = false;
+    return cudaSuccess;
+}
+
+bool view_ok(const ptl_ast_view* tree) {
+    return tree && tree->n > 0 && tree->n < (1ull << 31) && tree->type && tree->rtype && tree->parent &&
+           tree->depth && tree->child_idx && tree->data;
+}
+
+}  // namespace
+
+ptl_status ptl_generator_upload(ptl_generator* g, const ptl_ast_view* tree) {
+    if (!g || !view_ok(tree)) return PTL_BAD_ARGUMENT;
+    if (tree->max_depth == 0) return PTL_INVALID_AST;
+    if (cudaSetDevice(g->device) != cudaSuccess) return fail(g, PTL_CUDA_ERROR, "cudaSetDevice");
+    const cudaError_t e = upload_inputs(g, tree);
+    if (e != cudaSuccess) return cuda_fail(g, e, "upload");
+    return PTL_OK;
+}
+
+uint64_t ptl_kernel_launches(void) { return ptl::launch_count(); }
+
+ptl_status ptl_generator_create(const ptl_ast_view* tree, int device, ptl_generator** out) {
+    if (!out) return PTL_BAD_ARGUMENT;
+    *out = nullptr;
+    if (!view_ok(tree)) return PTL_BAD_ARGUMENT;
     if (tree->max_depth == 0) return PTL_INVALID_AST;  // the reference divides by it (rv_generator_avx.cpp:583)
     ptl_generator* g = new (std::nothrow) ptl_generator();
     if (!g) return PTL_OOM;
@@ -493,16 +531,7 @@ ptl_status ptl_generator_create(const ptl_ast_view* tree, int device, ptl_genera
     g->max_depth = tree->max_depth;
     cudaError_t e = cudaSetDevice(device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking);
-    const cudaMemcpyKind kind = tree->on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
-    const size_t n = tree->n;
-    struct { DevBuf* b; const void* src; size_t es; } in[] = {
-        {&g->in_type, tree->type, 1}, {&g->in_rtype, tree->rtype, 1}, {&g->in_parent, tree->parent, 4},
-        {&g->in_depth, tree->depth, 4}, {&g->in_child, tree->child_idx, 4}, {&g->in_data, tree->data, 4}};
-    for (auto& x : in) {
-        if (e != cudaSuccess) break;
-        e = x.b->ensure(n, x.es);
-        if (e == cudaSuccess) e = cudaMemcpyAsync(x.b->at<char>(), x.src, n * x.es, kind, g->stream);
-    }
+    if (e == cudaSuccess) e = upload_inputs(g, tree);
     if (e == cudaSuccess) e = g->tables.ensure(sizeof(CodeTables), 1);
     if (e == cudaSuccess) e = cudaMemcpyAsync(g->tables.at<char>(), &host_tables(), sizeof(CodeTables), cudaMemcpyHostToDevice, g->stream);
     if (e == cudaSuccess) e = g->errw.ensure(1, sizeof(ErrorWord));

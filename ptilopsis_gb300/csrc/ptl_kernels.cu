@@ -4,11 +4,15 @@
 // their bounded waits.
 #include <cuda_runtime.h>
 
+#include <atomic>
+
 #include "ptl_kernels.cuh"
 
 namespace ptl {
 
 namespace {
+
+std::atomic<uint64_t> g_launches{0};
 
 constexpr int kThreads = 256;
 
@@ -122,6 +126,7 @@ void run_scan(Load load, Store store, uint32_t count, const ScanScratch& sc, Err
     if (tiles == 0) return;
     cudaMemsetAsync(sc.status, 0, sizeof(unsigned long long) * tiles, s);
     cudaMemsetAsync(sc.counter, 0, sizeof(uint32_t), s);
+    g_launches++;
     k_scan<<<tiles, kScanThreads, 0, s>>>(load, store, count, sc, err);
 }
 
@@ -194,6 +199,7 @@ __global__ void k_sort_tiles(SortScratch ss, const SortSeg* cur, SortSeg* curw, 
         g.tcount = (m1 + kSortTile - 1) / kSortTile;
         g.tbase = atomicAdd(&ss.counters[0], g.tcount);
         curw[s] = g;
+        if (g.tbase + g.tcount > ss.tile_cap) continue;  // the host sees the count and stops
         for (uint32_t k = 0; k < g.tcount; ++k) ss.tile_seg[g.tbase + k] = s;
     }
 }
@@ -335,11 +341,21 @@ __device__ void sort_emit(SortScratch ss, SortSeg* next, uint32_t first, uint32_
     }
 }
 
-__global__ void k_sort_cut(SortScratch ss, SortSeg* cur, uint32_t nseg, SortSeg* next) {
+__global__ void k_sort_cut(SortScratch ss, SortSeg* cur, uint32_t nseg, SortSeg* next, ErrorWord* err) {
     PTL_FOR(s, nseg) {
         SortSeg& g = cur[s];
+        if (g.nL == 0 || g.nR == 0) {  // the median move guarantees both kinds of stop
+            record_error(err, ST_UNSUPPORTED, W_SORT, g.first);
+            g.K = 0;
+            continue;
+        }
         g.K = partition_k(ss.apos + g.first, ss.bpos + g.first, g.nL, g.nR);
         g.cut = partition_cut(ss.apos + g.first, ss.bpos + g.first, g.nL, g.K);
+        if (g.cut <= g.first || g.cut >= g.last) {
+            record_error(err, ST_UNSUPPORTED, W_SORT, g.first);
+            g.K = 0;
+            continue;
+        }
         sort_emit(ss, next, g.first, g.cut, g.dl - 1);
         sort_emit(ss, next, g.cut, g.last, g.dl - 1);
     }
@@ -530,15 +546,23 @@ __global__ void k_fj_functab(Prog P) { PTL_FOR(f, P.F) st_fix_functab(P, f, P.jo
 
 }  // namespace
 
+uint64_t launch_count() { return g_launches.load(); }
+void note_launch() { g_launches++; }
+
 // ====================================================================== launchers
 void launch_translate(const Prog& P, cudaStream_t s) {
+    g_launches++;
     k_translate<<<grid_for(P.nb8), kThreads, 0, s>>>(P);
 }
 
 void launch_preprocess(const Prog& P, cudaStream_t s) {
+    g_launches++;
     k_pre_args<<<grid_for(P.nb8), kThreads, 0, s>>>(P);
+    g_launches++;
     k_pre_lists<<<grid_for(P.nb8), kThreads, 0, s>>>(P);
+    g_launches++;
     k_pre_float<<<grid_for(P.nb8), kThreads, 0, s>>>(P);
+    g_launches++;
     k_pre_float_apply<<<grid_for(P.nb8), kThreads, 0, s>>>(P);
 }
 
@@ -547,7 +571,9 @@ void launch_count_scan(const Prog& P, const ScanScratch& sc, cudaStream_t s) {
 }
 
 void launch_fix(const Prog& P, cudaStream_t s) {
+    g_launches++;
     k_fix_own<<<grid_for(P.nb8), kThreads, 0, s>>>(P);
+    g_launches++;
     k_fix_cond<<<grid_for(P.nb8), kThreads, 0, s>>>(P);
 }
 
@@ -558,12 +584,15 @@ void launch_decl_scan(const Prog& P, uint32_t* meta, const ScanScratch& sc, cuda
 void launch_functab(const Prog& P, uint32_t* meta, cudaStream_t s) {
     // F is known on the device only; launch for the node count's upper bound.
     const uint64_t bound = P.nb8 / 8u + 8u;
+    g_launches++;
     k_functab<<<grid_for(bound), kThreads, 0, s>>>(P, meta);
+    g_launches++;
     k_functab_end<<<grid_for(bound), kThreads, 0, s>>>(P, meta);
 }
 
 cudaError_t run_depth_sort(const Prog& P, const SortScratch& ss, cudaStream_t s, uint32_t* rounds_out) {
     const uint32_t n = P.n;
+    g_launches++;
     k_sort_init<<<grid_for(n), kThreads, 0, s>>>(P, ss);
     cudaMemsetAsync(ss.counters, 0, sizeof(uint32_t) * 4, s);
     uint32_t nseg = 0;
@@ -586,16 +615,22 @@ cudaError_t run_depth_sort(const Prog& P, const SortScratch& ss, cudaStream_t s,
         SortSeg* segs = ss.seg[cur];
         SortSeg* next = ss.seg[cur ^ 1];
         cudaMemsetAsync(ss.counters, 0, sizeof(uint32_t) * 2, s);
+        g_launches++;
         k_sort_tiles<<<grid_for(nseg), kThreads, 0, s>>>(ss, segs, segs, nseg);
         uint32_t ntiles = 0;
         cudaMemcpyAsync(&ntiles, ss.counters, sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
         cudaError_t e = cudaStreamSynchronize(s);
         if (e != cudaSuccess) return e;
         if (ntiles > ss.tile_cap) return cudaErrorMemoryAllocation;
+        g_launches++;
         k_sort_count<<<ntiles, kThreads, 0, s>>>(ss, segs);
+        g_launches++;
         k_sort_segscan<<<nseg, kThreads, 0, s>>>(ss, segs);
+        g_launches++;
         k_sort_pos<<<ntiles, kThreads, 0, s>>>(ss, segs);
-        k_sort_cut<<<grid_for(nseg), kThreads, 0, s>>>(ss, segs, nseg, next);
+        g_launches++;
+        k_sort_cut<<<grid_for(nseg), kThreads, 0, s>>>(ss, segs, nseg, next, P.err);
+        g_launches++;
         k_sort_swap<<<ntiles, kThreads, 0, s>>>(ss, segs);
         cudaMemcpyAsync(&nseg, ss.counters + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
         e = cudaStreamSynchronize(s);
@@ -603,31 +638,42 @@ cudaError_t run_depth_sort(const Prog& P, const SortScratch& ss, cudaStream_t s,
         if (nseg > ss.seg_cap) return cudaErrorMemoryAllocation;
         cur ^= 1;
         ++rounds;
+        // every round shortens each segment and the depth budget ends partitioning
+        // after 2*floor(log2 n) levels
+        if (rounds > 2u * floor_log2(n) + 4u) return cudaErrorLaunchFailure;
     }
     uint32_t lh[2] = {0, 0};
     cudaMemcpyAsync(lh, ss.counters + 2, sizeof(lh), cudaMemcpyDeviceToHost, s);
     cudaError_t e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return e;
     if (lh[0] > ss.leaf_cap || lh[1] > ss.leaf_cap) return cudaErrorMemoryAllocation;
-    if (lh[1]) k_sort_heaps<<<grid_for(lh[1]), kThreads, 0, s>>>(ss, lh[1]);
-    if (lh[0]) k_sort_leaves<<<grid_for(lh[0]), kThreads, 0, s>>>(ss, lh[0]);
+    if (lh[1]) { g_launches++; k_sort_heaps<<<grid_for(lh[1]), kThreads, 0, s>>>(ss, lh[1]); }
+    if (lh[0]) { g_launches++; k_sort_leaves<<<grid_for(lh[0]), kThreads, 0, s>>>(ss, lh[0]); }
+    g_launches++;
     k_sort_out<<<grid_for(n), kThreads, 0, s>>>(P, ss);
     if (rounds_out) *rounds_out = rounds;
     return cudaGetLastError();
 }
 
 void launch_gen(const Prog& P, cudaStream_t s) {
+    g_launches++;
     k_gen_prop<<<grid_for(P.n), kThreads, 0, s>>>(P);
+    g_launches++;
     k_gen_claim<<<grid_for(P.n), kThreads, 0, s>>>(P);
+    g_launches++;
     k_gen_write<<<grid_for(P.n), kThreads, 0, s>>>(P);
 }
 
 cudaError_t run_optimize(const Prog& P, cudaStream_t s, uint32_t* sweeps_out) {
+    g_launches++;
     k_opt_mark<<<grid_for(P.wb8), kThreads, 0, s>>>(P);
     uint32_t sweeps = 0;
     for (;;) {
         cudaMemsetAsync(P.flags, 0, sizeof(uint32_t), s);
-        for (int k = 0; k < 4; ++k) k_opt_sweep<<<grid_for(P.wb8), kThreads, 0, s>>>(P);
+        for (int k = 0; k < 4; ++k) {
+            g_launches++;
+            k_opt_sweep<<<grid_for(P.wb8), kThreads, 0, s>>>(P);
+        }
         sweeps += 4;
         uint32_t changed = 0;
         cudaMemcpyAsync(&changed, P.flags, sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
@@ -636,6 +682,7 @@ cudaError_t run_optimize(const Prog& P, cudaStream_t s, uint32_t* sweeps_out) {
         if (!changed) break;
         if (sweeps > P.W + 8u) break;  // cannot happen: every sweep clears a mark
     }
+    g_launches++;
     k_opt_final<<<grid_for(P.wb8), kThreads, 0, s>>>(P);
     if (sweeps_out) *sweeps_out = sweeps;
     return cudaGetLastError();
@@ -644,17 +691,22 @@ cudaError_t run_optimize(const Prog& P, cudaStream_t s, uint32_t* sweeps_out) {
 cudaError_t run_regalloc_steps(const Prog& P, cudaStream_t s, bool* serial_out) {
     // Programs whose functions share symbols need the reference's serial order.
     cudaMemsetAsync(P.flags + 1, 0, sizeof(uint32_t), s);
+    g_launches++;
     k_ra_cross<<<grid_for(P.W), kThreads, 0, s>>>(P);
     uint32_t cross = 0;
     cudaMemcpyAsync(&cross, P.flags + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
     const cudaError_t e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return e;
     if (cross) {
+        g_launches++;
         k_ra_serial<<<1, 1, 0, s>>>(P);
     } else {
+        g_launches++;
         k_ra_free<<<grid_for(P.F, 64), 64, 0, s>>>(P);
+        g_launches++;
         k_ra_lane0<<<1, kRaThreads, 0, s>>>(P, P.S);
     }
+    g_launches++;
     k_ra_spill<<<grid_for(P.W), kThreads, 0, s>>>(P);
     if (serial_out) *serial_out = cross != 0;
     return cudaGetLastError();
@@ -665,8 +717,11 @@ void launch_regalloc_count_scan(const Prog& P, const ScanScratch& sc, cudaStream
 }
 
 void launch_regalloc_emit(const Prog& P, cudaStream_t s) {
+    g_launches++;
     k_ra_scatter<<<grid_for(P.wb8), kThreads, 0, s>>>(P);
+    g_launches++;
     k_ra_functab<<<grid_for(P.F), kThreads, 0, s>>>(P);
+    g_launches++;
     k_ra_frame<<<grid_for(P.F), kThreads, 0, s>>>(P);
 }
 
@@ -675,7 +730,9 @@ void launch_fixjumps_scan(const Prog& P, const ScanScratch& sc, cudaStream_t s) 
 }
 
 void launch_fixjumps_emit(const Prog& P, cudaStream_t s) {
+    g_launches++;
     k_fj_emit<<<grid_for(P.W2), kThreads, 0, s>>>(P);
+    g_launches++;
     k_fj_functab<<<grid_for(P.F), kThreads, 0, s>>>(P);
 }
 

@@ -31,6 +31,10 @@ struct ScanScratch {
     uint32_t tile_cap;
 };
 
+// Kernel launches issued by this library since load (counted at each launch site).
+uint64_t launch_count();
+void note_launch();
+
 // Element-wise stages (grid-stride launches of the per-thread functions).
 void launch_translate(const Prog& P, cudaStream_t s);
 void launch_preprocess(const Prog& P, cudaStream_t s);

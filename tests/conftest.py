@@ -1,0 +1,71 @@
+"""Shared test setup: the gpu marker, library builds and fixture loading."""
+from __future__ import annotations
+
+import json
+import os
+import sys
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300); run with -m gpu")
+
+
+@pytest.fixture(scope="session")
+def built():
+    """Builds the native libraries in-tree (no-op when up to date)."""
+    from ptilopsis_gb300 import build as b
+    from oracle import portbind
+    b.build_synth()
+    b.build_hostmodel()
+    assert portbind.build(), "oracle restatement failed to build"
+    return True
+
+
+@pytest.fixture(scope="session")
+def built_cuda(built):
+    from ptilopsis_gb300 import build as b
+    b.build_cuda()
+    return True
+
+
+def manifest() -> dict:
+    with open(os.path.join(GOLDEN, "manifest.json")) as f:
+        return json.load(f)
+
+
+def load_fixture(name: str):
+    """(Ast, golden dict) of a committed fixture."""
+    from oracle.refbind import Ast
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    ast = Ast(type=z["type"], rtype=z["rtype"], parent=z["parent"], depth=z["depth"], child_idx=z["child_idx"],
+              data=z["data"], max_depth=int(z["max_depth"]))
+    return ast, {k: z[k] for k in ("words", "fn_start", "fn_end", "fn_size", "fn_id")}
+
+
+def load_synth_golden(name: str) -> dict:
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    return {k: z[k] for k in z.files}
+
+
+def tree_to_ast(tree):
+    from oracle.refbind import Ast
+    return Ast(type=tree.type, rtype=tree.rtype, parent=tree.parent, depth=tree.depth, child_idx=tree.child_idx,
+               data=tree.data, max_depth=tree.max_depth)
+
+
+def ast_to_tree(ast):
+    from ptilopsis_gb300 import DepthTree
+    return DepthTree(ast.type, ast.rtype, ast.parent, ast.depth, ast.child_idx, ast.data, ast.max_depth)
+
+
+def reference_available() -> bool:
+    from oracle import refbind
+    return refbind.build()

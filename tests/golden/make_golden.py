@@ -1,0 +1,101 @@
+"""Regenerates the golden fixtures of tests/golden from the reference itself.
+
+Run in the x86-64 build container, where the reference tree is mounted and
+oracle/ref/Makefile has built it into oracle/_ref:
+
+    python tests/golden/make_golden.py
+
+For each fixture it stores the DepthTree the reference front end (pareas-ast) builds
+from one of the reference's own Pareas test inputs, and what the reference generator
+(rv_generator_avx with one worker thread) produces from it: the output words, the
+function table, and a CRC32 of every intermediate array.  Seeded synthetic programs
+store only the outputs (their trees are regenerated from the seed).  The code tables
+are stored as CRC32s of the reference's constexpr arrays.
+"""
+from __future__ import annotations
+
+import json
+import os
+import sys
+import zlib
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from oracle import refbind  # noqa: E402
+
+REF = refbind.REF_ROOT_DEFAULT
+FIXTURES = [
+    "testfiles/pareas/basic/1.in",
+    "testfiles/pareas/basic/2.in",
+    "testfiles/pareas/basic/3.in",
+    "testfiles/arith1.ptl",
+    "testfiles/basic1.ptl",
+    "testfiles/comp0.ptl",
+    "testfiles/comp1.ptl",
+    "testfiles/comp_all.ptl",
+    "testfiles/many_args.in",
+]
+SYNTH_SEEDS = [0x50544C00, 0x50544C00 + 1, 0x50544C00 + 2]
+
+
+def crc(a: np.ndarray) -> int:
+    return zlib.crc32(np.ascontiguousarray(a, np.uint32).tobytes())
+
+
+def table_crcs() -> dict:
+    import ctypes
+    L = refbind.lib()
+    L.ptlref_table.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_uint32)]
+    L.ptlref_table.restype = ctypes.c_size_t
+    out = {}
+    for w in range(10):
+        n = L.ptlref_table(w, None)
+        a = np.empty(n, np.uint32)
+        L.ptlref_table(w, a.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)))
+        out[str(w)] = [int(n), crc(a)]
+    return out
+
+
+def main() -> None:
+    if not refbind.build(REF):
+        raise SystemExit("the reference could not be built here (needs the reference tree on x86-64)")
+    manifest = {"fixtures": [], "synthetic": [], "tables": table_crcs()}
+    for rel in FIXTURES:
+        ast = refbind.parse_file(os.path.join(REF, rel))
+        res = refbind.compile_ast(ast, snapshots=True)
+        name = rel.replace("testfiles/", "").replace("/", "_").replace(".", "_")
+        np.savez_compressed(os.path.join(HERE, name + ".npz"),
+                            type=ast.type, rtype=ast.rtype, parent=ast.parent, depth=ast.depth,
+                            child_idx=ast.child_idx, data=ast.data, max_depth=np.int64(ast.max_depth),
+                            words=res.bufs["out_words"], fn_start=res.bufs["fn_start"], fn_end=res.bufs["fn_end"],
+                            fn_size=res.bufs["fn_size"], fn_id=res.bufs["fn_id"])
+        snaps = {k: [int(len(v)), crc(v)] for k, v in res.bufs.items()}
+        manifest["fixtures"].append({"name": name, "source": rel, "n": int(ast.n), "words": int(len(res.words)),
+                                     "snapshots": snaps})
+        print(f"{rel}: {ast.n} nodes -> {len(res.words)} words")
+
+    from ptilopsis_gb300.synth import SynthParams, generate
+    for seed in SYNTH_SEEDS:
+        tree = generate(SynthParams(seed=seed))
+        ast = refbind.Ast(tree.type, tree.rtype, tree.parent, tree.depth, tree.child_idx, tree.data, tree.max_depth)
+        res = refbind.compile_ast(ast, snapshots=True)
+        name = f"synth_c0_{seed:08x}"
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), words=res.bufs["out_words"],
+                            fn_start=res.bufs["fn_start"], fn_end=res.bufs["fn_end"], fn_size=res.bufs["fn_size"],
+                            fn_id=res.bufs["fn_id"])
+        manifest["synthetic"].append({"name": name, "seed": seed, "n": int(ast.n),
+                                      "tree_crc": [crc(tree.type.astype(np.uint32)), crc(tree.parent.view(np.uint32)),
+                                                   crc(tree.data)],
+                                      "words": int(len(res.words)),
+                                      "snapshots": {k: [int(len(v)), crc(v)] for k, v in res.bufs.items()}})
+        print(f"synthetic seed {seed:#x}: {ast.n} nodes -> {len(res.words)} words")
+    with open(os.path.join(HERE, "manifest.json"), "w") as f:
+        json.dump(manifest, f, indent=1, sort_keys=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,132 @@
+"""GPU parity through the C ABI: the CUDA pipeline against the reference's golden
+outputs and against the oracle, stage by stage, on the same inputs.  Integer work:
+the bar is bit-exact."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import ast_to_tree, load_fixture, load_synth_golden, manifest, tree_to_ast
+
+pytestmark = pytest.mark.gpu
+
+STAGE_SNAPSHOTS = ["pre_type", "pre_rtype", "pre_data", "cnt_size", "cnt_loc", "cnt_fn_id", "cnt_fn_start",
+                   "cnt_fn_end", "cnt_fn_size", "gen_instr", "gen_rd", "gen_rs1", "gen_rs2", "gen_jt", "opt_used",
+                   "ra_instr", "ra_rd", "ra_rs1", "ra_rs2", "ra_jt", "ra_fn_start", "ra_fn_end", "ra_fn_size",
+                   "out_words", "fn_start", "fn_end", "fn_size", "fn_id"]
+
+
+def gpu_compile(tree, snapshots=False):
+    from ptilopsis_gb300 import RvGenerator
+    with RvGenerator(tree) as gen:
+        gen.process(profile=True)
+        words = gen.get_instructions()
+        table = gen.function_table()
+        snaps = {k: gen.snapshot(k) for k in STAGE_SNAPSHOTS} if snapshots else {}
+    return words, table, snaps
+
+
+def assert_matches_oracle(tree):
+    from oracle import portbind
+    ref = portbind.compile_ast(tree_to_ast(tree), snapshots=True)
+    words, table, snaps = gpu_compile(tree, snapshots=True)
+    for name in STAGE_SNAPSHOTS:
+        np.testing.assert_array_equal(snaps[name], ref.bufs[name], err_msg=name)
+    np.testing.assert_array_equal(words, ref.words)
+    return words
+
+
+@pytest.mark.parametrize("fx", [f["name"] for f in manifest()["fixtures"]])
+def test_gpu_matches_reference_golden(built_cuda, fx):
+    ast, gold = load_fixture(fx)
+    words, table, _ = gpu_compile(ast_to_tree(ast))
+    np.testing.assert_array_equal(words, gold["words"])
+    for k, g in (("starts", "fn_start"), ("ends", "fn_end"), ("sizes", "fn_size"), ("ids", "fn_id")):
+        np.testing.assert_array_equal(table[k], gold[g], err_msg=k)
+
+
+@pytest.mark.parametrize("entry", manifest()["synthetic"], ids=lambda e: e["name"])
+def test_gpu_matches_reference_golden_synthetic(built_cuda, entry):
+    from ptilopsis_gb300.synth import SynthParams, generate
+    words, _, _ = gpu_compile(generate(SynthParams(seed=entry["seed"])))
+    np.testing.assert_array_equal(words, load_synth_golden(entry["name"])["words"])
+
+
+@pytest.mark.parametrize("fx", [f["name"] for f in manifest()["fixtures"]])
+def test_gpu_stages_match_oracle_fixture(built_cuda, fx):
+    ast, _ = load_fixture(fx)
+    assert_matches_oracle(ast_to_tree(ast))
+
+
+@pytest.mark.parametrize("seed", [0x50544C00, 0x50544C40, 0x50544C41])
+def test_gpu_stages_match_oracle_synthetic(built_cuda, seed):
+    from ptilopsis_gb300.synth import SynthParams, generate
+    assert_matches_oracle(generate(SynthParams(seed=seed)))
+
+
+def test_gpu_spilling_program(built_cuda):
+    from ptilopsis_gb300.synth import config_params, generate
+    assert_matches_oracle(generate(config_params("c1", scale=96 / 2048)))
+
+
+def test_gpu_many_functions(built_cuda):
+    from ptilopsis_gb300.synth import SynthParams, generate
+    assert_matches_oracle(generate(SynthParams(seed=0x50544C42, n_functions=2000, median_fn_nodes=80.0,
+                                               sigma=1.0, max_nesting=8)))
+
+
+def test_gpu_float_heavy_deep_expressions(built_cuda):
+    from ptilopsis_gb300.synth import config_params, generate
+    assert_matches_oracle(generate(config_params("c2", scale=64 / 32768)))
+
+
+def test_gpu_device_resident_input_equals_host_input(built_cuda):
+    import torch
+    from ptilopsis_gb300.synth import SynthParams, generate
+    tree = generate(SynthParams(seed=0x50544C43))
+    host_words, _, _ = gpu_compile(tree)
+    dev_words, _, _ = gpu_compile(tree.to(torch.device("cuda", 0)))
+    np.testing.assert_array_equal(host_words, dev_words)
+
+
+def test_gpu_process_is_repeatable_and_upload_rebinds(built_cuda):
+    from oracle import portbind
+    from ptilopsis_gb300 import RvGenerator
+    from ptilopsis_gb300.synth import SynthParams, generate
+    a = generate(SynthParams(seed=0x50544C44))
+    b = generate(SynthParams(seed=0x50544C45, n_functions=40, median_fn_nodes=900.0, sigma=1.0))
+    with RvGenerator(a) as gen:
+        gen.process()
+        w1 = gen.get_instructions()
+        gen.process()
+        np.testing.assert_array_equal(gen.get_instructions(), w1)
+        gen.upload(b)
+        gen.process()
+        np.testing.assert_array_equal(gen.get_instructions(), portbind.compile_ast(tree_to_ast(b)).words)
+        gen.upload(a)
+        gen.process()
+        np.testing.assert_array_equal(gen.get_instructions(), w1)
+
+
+def test_gpu_rejects_malformed_tree(built_cuda):
+    from ptilopsis_gb300 import PtlError, RvGenerator
+    from ptilopsis_gb300.synth import SynthParams, generate
+    tree = generate(SynthParams(seed=0x50544C46, n_functions=2, median_fn_nodes=50.0))
+    bad = ast_to_tree(tree_to_ast(tree))
+    bad.parent = bad.parent.copy()
+    bad.parent[3] = 1  # a parent before its child breaks post-order
+    with RvGenerator(bad) as gen:
+        with pytest.raises(PtlError) as e:
+            gen.process()
+    assert e.value.status == 1
+
+
+def test_gpu_large_program_against_oracle(built_cuda):
+    """A quarter of the large-program workload (~1M nodes), words and function table."""
+    from oracle import portbind
+    from ptilopsis_gb300.synth import config_params, generate
+    tree = generate(config_params("c1", scale=0.25))
+    ref = portbind.compile_ast(tree_to_ast(tree))
+    words, table, _ = gpu_compile(tree)
+    np.testing.assert_array_equal(words, ref.words)
+    np.testing.assert_array_equal(table["starts"], ref.bufs["fn_start"])

@@ -1,0 +1,99 @@
+"""Pins the oracle (the CPU restatement in oracle/port) to the reference.
+
+Where the reference is built here (x86-64 with the reference tree), the restatement is
+compared stage by stage with the reference itself; everywhere, it is compared with the
+golden outputs the reference produced (tests/golden, made by make_golden.py)."""
+from __future__ import annotations
+
+import glob
+import os
+import zlib
+
+import numpy as np
+import pytest
+
+from conftest import load_fixture, load_synth_golden, manifest, reference_available, tree_to_ast
+
+STAGE_BUFS = ["pre_type", "pre_rtype", "pre_data", "cnt_size", "cnt_loc", "cnt_fn_id", "cnt_fn_start",
+              "cnt_fn_end", "cnt_fn_size", "gen_instr", "gen_rd", "gen_rs1", "gen_rs2", "gen_jt", "opt_used",
+              "ra_instr", "ra_rd", "ra_rs1", "ra_rs2", "ra_jt", "ra_fn_start", "ra_fn_end", "ra_fn_size",
+              "fj_instr", "fj_rd", "fj_rs1", "fj_rs2", "fj_jt", "fj_fn_start", "fj_fn_end", "fj_fn_size",
+              "out_words", "fn_start", "fn_end", "fn_size", "fn_id"]
+
+
+def crc(a):
+    return zlib.crc32(np.ascontiguousarray(a, np.uint32).tobytes())
+
+
+@pytest.mark.parametrize("fx", [f["name"] for f in manifest()["fixtures"]])
+def test_port_matches_golden_fixture(built, fx):
+    from oracle import portbind
+    ast, gold = load_fixture(fx)
+    res = portbind.compile_ast(ast, snapshots=True)
+    np.testing.assert_array_equal(res.words, gold["words"])
+    for k in ("fn_start", "fn_end", "fn_size", "fn_id"):
+        np.testing.assert_array_equal(res.bufs[k], gold[k])
+    # every intermediate array, through the CRCs of the reference's snapshots
+    snaps = next(f for f in manifest()["fixtures"] if f["name"] == fx)["snapshots"]
+    for name, (length, c) in snaps.items():
+        assert len(res.bufs[name]) == length, name
+        assert crc(res.bufs[name]) == c, name
+
+
+@pytest.mark.parametrize("entry", manifest()["synthetic"], ids=lambda e: e["name"])
+def test_port_matches_golden_synthetic(built, entry):
+    from oracle import portbind
+    from ptilopsis_gb300.synth import SynthParams, generate
+    tree = generate(SynthParams(seed=entry["seed"]))
+    assert tree.n == entry["n"]
+    res = portbind.compile_ast(tree_to_ast(tree), snapshots=True)
+    gold = load_synth_golden(entry["name"])
+    np.testing.assert_array_equal(res.words, gold["words"])
+    for name, (length, c) in entry["snapshots"].items():
+        assert len(res.bufs[name]) == length and crc(res.bufs[name]) == c, name
+
+
+def test_port_tables_match_reference_tables(built):
+    from oracle import portbind
+    for w, (n, c) in manifest()["tables"].items():
+        t = portbind.table(int(w))
+        assert len(t) == n and crc(t) == c, portbind.TABLE_NAMES[int(w)]
+
+
+REF_INPUTS = ["basic/1.in", "basic/3.in", "basic/5.in", "funclen/1.in", "funclen/8.in"]
+
+
+@pytest.mark.parametrize("rel", REF_INPUTS)
+def test_port_matches_reference_stage_by_stage(built, rel):
+    if not reference_available():
+        pytest.skip("reference not buildable on this host")
+    from oracle import portbind, refbind
+    ast = refbind.parse_file(os.path.join(refbind.REF_ROOT_DEFAULT, "testfiles/pareas", rel))
+    ref = refbind.compile_ast(ast, snapshots=True)
+    port = portbind.compile_ast(ast, snapshots=True)
+    for name in STAGE_BUFS:
+        np.testing.assert_array_equal(port.bufs[name], ref.bufs[name], err_msg=name)
+
+
+@pytest.mark.parametrize("seed", [0x50544C10 + k for k in range(4)])
+def test_port_matches_reference_on_synthetic(built, seed):
+    if not reference_available():
+        pytest.skip("reference not buildable on this host")
+    from oracle import portbind, refbind
+    from ptilopsis_gb300.synth import SynthParams, generate
+    tree = generate(SynthParams(seed=seed, n_functions=24, median_fn_nodes=600.0, sigma=1.0, spill_frac=0.3,
+                                max_nesting=24))
+    ast = tree_to_ast(tree)
+    ref = refbind.compile_ast(ast, snapshots=True)
+    port = portbind.compile_ast(ast, snapshots=True)
+    for name in STAGE_BUFS:
+        np.testing.assert_array_equal(port.bufs[name], ref.bufs[name], err_msg=name)
+
+
+def test_depth_sort_is_libstdcxx_sort(built):
+    """The oracle's depth order is std::sort's; the golden words depend on it."""
+    from oracle import portbind
+    keys = np.array([3, 1, 2, 1, 3, 0, 2, 1, 1, 2, 0, 3, 1, 2, 2, 1, 0, 3, 1, 1, 2, 2], np.int32)
+    perm = portbind.depth_sort(keys)
+    assert np.all(np.diff(keys[perm]) >= 0)
+    assert sorted(perm.tolist()) == list(range(len(keys)))
