@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <initializer_list>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -159,6 +160,13 @@ ptl_status cuda_fail(ptl_generator* g, cudaError_t e, const char* what) {
         if (e_ != cudaSuccess) return cuda_fail(g, e_, #expr); \
     } while (0)
 
+// A kernel must never see a pointer to a buffer that is not allocated yet; the views
+// are rebuilt after each allocation and checked here before use.
+bool prog_ready(const Prog& P, std::initializer_list<const void*> need) {
+    for (const void* p : need) if (!p) return false;
+    return P.err && P.flags && P.tab.t;
+}
+
 Prog make_prog(ptl_generator* g) {
     Prog P{};
     P.n = static_cast<uint32_t>(g->n);
@@ -288,6 +296,9 @@ ptl_status run_pipeline(ptl_generator* g, bool profile, bool to_host) {
     g->host_valid = false;
     StageTimer timer(g, profile);
 
+    // fixed-size scratch first, so every Prog view below sees it
+    PTL_CU(g->flags.ensure(4, 4));
+    PTL_CU(g->flags.zero(s));
     PTL_CU(g->errw.zero(s));
     PTL_CU(g->meta.zero(s));
     // node arrays
@@ -303,14 +314,21 @@ ptl_status run_pipeline(ptl_generator* g, bool profile, bool to_host) {
     PTL_CU(g->regs.zero(s));
     PTL_CU(g->depth_seen.ensure(g->max_depth + 1, 4));
     PTL_CU(g->depth_seen.zero(s));
-    const size_t scan_tiles = (std::max(nb8, size_t(1)) + 4095) / 4096 + 8;
-    PTL_CU(g->scan_status.ensure(scan_tiles, 8));
     PTL_CU(g->scan_counter.ensure(1, 4));
+    // Tile-status scratch for a scan over `count` elements (grows with the word counts).
+    auto scan_for = [&](size_t count, ScanScratch* sc) -> cudaError_t {
+        const size_t tiles = (std::max(count, size_t(1)) + kScanTileElems - 1) / kScanTileElems + 8;
+        const cudaError_t e = g->scan_status.ensure(tiles, 8);
+        if (e != cudaSuccess) return e;
+        *sc = ScanScratch{g->scan_status.at<unsigned long long>(), g->scan_counter.at<uint32_t>(),
+                          static_cast<uint32_t>(tiles)};
+        return cudaSuccess;
+    };
+    ScanScratch sc{};
+    PTL_CU(scan_for(nb8, &sc));
 
     g->F = g->W = g->W2 = g->W3 = g->S = 0;
     Prog P = make_prog(g);
-    ScanScratch sc{g->scan_status.at<unsigned long long>(), g->scan_counter.at<uint32_t>(),
-                   static_cast<uint32_t>(scan_tiles)};
 
     // ---- input checks
     note_launch();
@@ -330,6 +348,8 @@ ptl_status run_pipeline(ptl_generator* g, bool profile, bool to_host) {
     }
 
     // ---- preprocess
+    if (!prog_ready(P, {P.nt, P.rt, P.nd1, P.nd, P.par, P.ci, P.dep, P.fflag, P.sizes, P.loc0, P.loc, P.decl}))
+        return fail(g, PTL_CUDA_ERROR, "internal: unallocated node arrays");
     launch_translate(P, s);
     launch_preprocess(P, s);
     timer.mark();
@@ -351,6 +371,8 @@ ptl_status run_pipeline(ptl_generator* g, bool profile, bool to_host) {
         PTL_CU(b->zero(s));
     }
     P = make_prog(g);
+    if (!prog_ready(P, {P.fn_id, P.fn_start, P.fn_size, P.fn_end, P.fn_start0, P.fn_size0}))
+        return fail(g, PTL_CUDA_ERROR, "internal: unallocated function table");
     launch_functab(P, g->meta.at<uint32_t>(), s);
     PTL_CU(cudaMemcpyAsync(meta, g->meta.at<uint32_t>(), sizeof(meta), cudaMemcpyDeviceToHost, s));
     PTL_CU(cudaStreamSynchronize(s));
@@ -401,14 +423,15 @@ ptl_status run_pipeline(ptl_generator* g, bool profile, bool to_host) {
     PTL_CU(g->smark.ensure(wb8, 1));
     PTL_CU(g->smark.zero(s));
     P = make_prog(g);
+    if (!prog_ready(P, {P.instr, P.rd, P.rs1, P.rs2, P.jt, P.used_instrs, P.symreg, P.symswp, P.stamp, P.spill,
+                        P.roffs, P.owner, P.used, P.smark, P.pos, P.regs}))
+        return fail(g, PTL_CUDA_ERROR, "internal: unallocated word arrays");
     PTL_CU(run_depth_sort(P, ss, s, &g->sort_rounds));
     launch_gen(P, s);
     if (ptl_status st = check_error_word(g); st != PTL_OK) return st;
     timer.mark();
 
     // ---- optimize
-    PTL_CU(g->flags.ensure(4, 4));
-    PTL_CU(g->flags.zero(s));
     PTL_CU(run_optimize(P, s, &g->opt_sweeps));
     if (ptl_status st = check_error_word(g); st != PTL_OK) return st;
     timer.mark();
@@ -424,7 +447,10 @@ ptl_status run_pipeline(ptl_generator* g, bool profile, bool to_host) {
     PTL_CU(g->trig_max.ensure(trig, 4));
     PTL_CU(g->trig_max.zero(s));
     P = make_prog(g);
+    if (!prog_ready(P, {P.lifetime, P.trig_min, P.trig_max}))
+        return fail(g, PTL_CUDA_ERROR, "internal: unallocated regalloc state");
     PTL_CU(run_regalloc_steps(P, s, &g->ra_serial));
+    PTL_CU(scan_for(wb8, &sc));
     launch_regalloc_count_scan(P, sc, s);
     uint32_t last_off = 0;
     PTL_CU(read1(g, P.roffs + (g->W - 1), &last_off));
@@ -436,6 +462,8 @@ ptl_status run_pipeline(ptl_generator* g, bool profile, bool to_host) {
         PTL_CU(b->zero(s));
     }
     P = make_prog(g);
+    if (!prog_ready(P, {P.ni, P.nrd, P.nr1, P.nr2, P.njt, P.fsz, P.joffs}))
+        return fail(g, PTL_CUDA_ERROR, "internal: unallocated regalloc output");
     launch_regalloc_emit(P, s);
     for (int k = 0; k < 3; ++k) {
         DevBuf* src[3] = {&g->fn_start, &g->fn_end, &g->fn_size};
@@ -445,6 +473,7 @@ ptl_status run_pipeline(ptl_generator* g, bool profile, bool to_host) {
     timer.mark();
 
     // ---- fix_jumps (+ postprocess)
+    PTL_CU(scan_for(w2b8, &sc));
     launch_fixjumps_scan(P, sc, s);
     uint32_t last_size = 0, last_joff = 0;
     PTL_CU(read1(g, P.fsz + (g->W2 - 1), &last_size));
@@ -454,6 +483,7 @@ ptl_status run_pipeline(ptl_generator* g, bool profile, bool to_host) {
     PTL_CU(g->out.ensure(r8(g->W3) + 8, 4));
     PTL_CU(g->out.zero(s));
     P = make_prog(g);
+    if (!prog_ready(P, {P.out})) return fail(g, PTL_CUDA_ERROR, "internal: unallocated output");
     launch_fixjumps_emit(P, s);
     timer.mark();
     timer.mark();  // postprocess is fused into fix_jumps

@@ -120,10 +120,18 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(Load load, Store store, u
     }
 }
 
+static_assert(kScanTile == kScanTileElems, "scan tile size shared with the host");
+
 template <class Load, class Store>
 void run_scan(Load load, Store store, uint32_t count, const ScanScratch& sc, ErrorWord* err, cudaStream_t s) {
     const uint32_t tiles = (count + kScanTile - 1) / kScanTile;
     if (tiles == 0) return;
+    if (tiles > sc.tile_cap) {  // the caller sizes the scratch; never write past it
+        ErrorWord e{ST_UNSUPPORTED, W_SCAN, tiles, 0};
+        cudaMemcpyAsync(err, &e, sizeof(e), cudaMemcpyHostToDevice, s);
+        cudaStreamSynchronize(s);
+        return;
+    }
     cudaMemsetAsync(sc.status, 0, sizeof(unsigned long long) * tiles, s);
     cudaMemsetAsync(sc.counter, 0, sizeof(uint32_t), s);
     g_launches++;

@@ -25,6 +25,8 @@ struct SortScratch {
     uint32_t* counters;        // [0] tiles [1] next segments [2] leaves [3] heaps
 };
 
+constexpr size_t kScanTileElems = 4096;  // elements per scan tile (ptl_kernels.cu)
+
 struct ScanScratch {
     unsigned long long* status;  // per tile: (flag << 32) | value
     uint32_t* counter;           // dynamic tile ticket

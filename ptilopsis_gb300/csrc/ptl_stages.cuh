@@ -537,8 +537,8 @@ PTL_HD bool st_opt_sweep(const Prog& P, uint32_t i) {
     bool changed = false;
     const int32_t a = s32(P.rs1[i] - 64u);
     const int32_t b = s32(P.rs2[i] - 64u);
-    if (a >= 0 && !P.smark[a] && P.used[a]) { P.used[a] = 0; changed = true; }
-    if (b >= 0 && !P.smark[b] && P.used[b]) { P.used[b] = 0; changed = true; }
+    if (a >= 0 && u32(a) < P.W && !P.smark[a] && P.used[a]) { P.used[a] = 0; changed = true; }
+    if (b >= 0 && u32(b) < P.W && !P.smark[b] && P.used[b]) { P.used[b] = 0; changed = true; }
     return changed;
 }
 
