@@ -15,10 +15,13 @@
 #include "ptl_common.cuh"
 #include "ptl_sort.cuh"
 #include "ptl_stages.cuh"
+#include "ptl_ra.cuh"
 
 using namespace ptl;
 
 namespace {
+
+uint32_t g_cache_k = 4;  // entries per function of the lane-0 symbol cache
 
 template <typename T>
 struct HBuf {
@@ -202,6 +205,41 @@ struct Model {
         }
     }
 
+    uint32_t hm_cache_k = g_cache_k;
+
+    // The lane-0 pass with the same phase functions as k_ra_lane0_cached.
+    void lane0_cached(uint32_t S, uint32_t K) {
+        const uint32_t G0 = (P.F + 7) / 8;
+        Ra2Shared sh{};
+        std::vector<uint32_t> cur(3 * G0), tag(static_cast<size_t>(G0) * K);
+        std::vector<uint16_t> val(static_cast<size_t>(G0) * K);
+        const SymCache c{tag.data(), val.data(), K};
+        std::vector<Ra2Slot> L(G0);
+        for (uint32_t j = 0; j < G0; ++j) {
+            L[j].act = false;
+            L[j].have_next = false;
+            ra2_slot_init(P, c, L[j], j, j);
+        }
+        for (int p = 0; p < 64; ++p) { sh.R0[p] = 0xFFFFFFFFu; sh.R0own[p] = 0xFFFFFFFFu; }
+        for (uint32_t i = 0; i < S; ++i) {
+            for (uint32_t p = 0; p < 64; ++p) ra2_begin_p(P, sh, i, p);
+            for (uint32_t j = 0; j < G0; ++j) ra2_load(P, L[j], i, cur.data() + 3 * j);
+            for (uint32_t j = 0; j < G0; ++j) ra2_compute0(P, c, sh, L[j], j);
+            for (uint32_t j = 0; j < G0; ++j) ra2_check(sh, L[j]);
+            if (sh.flag) {
+                for (uint32_t round = 0;; ++round) {
+                    for (uint32_t j = 0; j < G0; ++j) ra2_round(sh, L[j]);
+                    bool changed = false;
+                    for (uint32_t p = 0; p < 64; ++p) changed |= ra2_round_p(sh, p);
+                    if (!changed) break;
+                    if (round > G0 + 2) { record_error(P.err, ST_DEVICE_TIMEOUT, W_RA2, i); break; }
+                }
+            }
+            for (uint32_t j = 0; j < G0; ++j) ra2_apply(P, c, sh, L[j], j);
+            for (uint32_t p = 0; p < 64; ++p) ra2_end_p(P, c, sh, p, cur.data());
+        }
+    }
+
     int run(const uint8_t* type, const uint8_t* rtype, const int32_t* parent, const int32_t* depth,
             const int32_t* child, const uint32_t* data, size_t n_, size_t max_depth) {
         build_code_tables(&tab);
@@ -270,11 +308,15 @@ struct Model {
         bind();
         bool cross = false;
         for (uint32_t i = 0; i < W; ++i) cross |= st_ra_cross(P, i);
-        if (cross) {
+        const uint32_t G0 = (F + 7) / 8;
+        if (cross || G0 > 8192u) {
             st_ra_serial(P, stamp.p);
         } else {
-            for (uint32_t f = 0; f < F; ++f) if (f & 7u) st_ra_free_function(P, f);
-            lane0(S);
+            std::vector<uint32_t> tag(64), dummy;
+            std::vector<uint16_t> val(64);
+            const SymCache c1{tag.data(), val.data(), 64};
+            for (uint32_t f = 0; f < F; ++f) if (f & 7u) ra_free_function_cached(P, c1, 0, f);
+            lane0_cached(S, hm_cache_k);
         }
         for (uint32_t v = 0; v < W; ++v) st_ra_spill(P, v);
         exclusive_scan(wb8, [&](uint32_t i) { return st_ra_count(P, i); }, roffs.p);
@@ -343,6 +385,8 @@ int ptlhm_compile(const uint8_t* type, const uint8_t* rtype, const int32_t* pare
     delete m;
     return rc;
 }
+
+void ptlhm_set_cache_entries(uint32_t k) { g_cache_k = k; }
 
 void ptlhm_free(ptlhm_buf* bufs, int nbufs) {
     for (int k = 0; k < nbufs; ++k) { std::free(bufs[k].p); bufs[k].p = nullptr; bufs[k].n = 0; }

@@ -7,6 +7,7 @@
 #include <atomic>
 
 #include "ptl_kernels.cuh"
+#include "ptl_ra.cuh"
 
 namespace ptl {
 
@@ -537,6 +538,92 @@ __global__ void __launch_bounds__(kRaThreads) k_ra_lane0(Prog P, uint32_t S0) {
     }
 }
 
+// Independent functions with an on-chip symbol cache per thread.
+constexpr int kRaFreeThreads = 64;
+constexpr uint32_t kRaFreeK = 64;
+
+__global__ void __launch_bounds__(kRaFreeThreads) k_ra_free_cached(Prog P) {
+    __shared__ uint32_t tag[kRaFreeThreads * kRaFreeK];
+    __shared__ uint16_t val[kRaFreeThreads * kRaFreeK];
+    const SymCache c{tag, val, kRaFreeK};
+    // non-lane-0 functions only: function index skips multiples of 8
+    const uint32_t k = blockIdx.x * kRaFreeThreads + threadIdx.x;
+    const uint32_t f = (k / 7u) * 8u + (k % 7u) + 1u;
+    if (f < P.F) ra_free_function_cached(P, c, threadIdx.x, f);
+}
+
+// Lane-0 functions in lock-step (see ptl_ra.cuh).  One CTA; thread t runs slots
+// t, t+T, ... (Q per thread); slot = group index.
+template <int Q>
+__global__ void __launch_bounds__(1024) k_ra_lane0_cached(Prog P, uint32_t S, uint32_t K) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    Ra2Shared& sh = *reinterpret_cast<Ra2Shared*>(smem);
+    const uint32_t G0 = (P.F + 7u) / 8u;
+    uint32_t* cur = reinterpret_cast<uint32_t*>(smem + sizeof(Ra2Shared));
+    uint32_t* ctag = cur + 3u * G0;
+    uint16_t* cval = reinterpret_cast<uint16_t*>(ctag + G0 * K);
+    const SymCache c{ctag, cval, K};
+    const uint32_t tid = threadIdx.x, T = blockDim.x;
+    Ra2Slot L[Q];
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        const uint32_t j = tid + static_cast<uint32_t>(q) * T;
+        L[q].act = false;
+        L[q].have_next = false;
+        if (j < G0) ra2_slot_init(P, c, L[q], j, j);
+    }
+    if (tid < 64) {
+        sh.R0[tid] = 0xFFFFFFFFu;
+        sh.R0own[tid] = 0xFFFFFFFFu;
+    }
+    __syncthreads();
+    for (uint32_t i = 0; i < S; ++i) {
+        if (tid < 64) ra2_begin_p(P, sh, i, tid);
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+            const uint32_t j = tid + static_cast<uint32_t>(q) * T;
+            if (j < G0) ra2_load(P, L[q], i, cur + 3u * j);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+            const uint32_t j = tid + static_cast<uint32_t>(q) * T;
+            if (j < G0) ra2_compute0(P, c, sh, L[q], j);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+            const uint32_t j = tid + static_cast<uint32_t>(q) * T;
+            if (j < G0) ra2_check(sh, L[q]);
+        }
+        __syncthreads();
+        if (sh.flag) {
+            for (uint32_t round = 0;; ++round) {
+#pragma unroll
+                for (int q = 0; q < Q; ++q) {
+                    const uint32_t j = tid + static_cast<uint32_t>(q) * T;
+                    if (j < G0) ra2_round(sh, L[q]);
+                }
+                __syncthreads();
+                const bool changed = tid < 64 ? ra2_round_p(sh, tid) : false;
+                if (!__syncthreads_or(changed)) break;
+                if (round > G0 + 2u) {
+                    if (tid == 0) record_error(P.err, ST_DEVICE_TIMEOUT, W_RA2, i);
+                    break;
+                }
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+            const uint32_t j = tid + static_cast<uint32_t>(q) * T;
+            if (j < G0) ra2_apply(P, c, sh, L[q], j);
+        }
+        __syncthreads();
+        if (tid < 64) ra2_end_p(P, c, sh, tid, cur);
+        __syncthreads();
+    }
+}
+
 __global__ void k_ra_cross(Prog P) {
     bool any = false;
     PTL_FOR(i, P.W) any |= st_ra_cross(P, i);
@@ -705,14 +792,46 @@ cudaError_t run_regalloc_steps(const Prog& P, cudaStream_t s, bool* serial_out) 
     cudaMemcpyAsync(&cross, P.flags + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
     const cudaError_t e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return e;
-    if (cross) {
+    const uint32_t G0 = (P.F + 7u) / 8u;
+    if (cross || G0 > 8192u) {
+        // functions share symbols (or too many lane-0 functions for one CTA): serial path
         g_launches++;
         k_ra_serial<<<1, 1, 0, s>>>(P);
     } else {
+        const uint32_t free_fns = P.F - G0;
+        if (free_fns) {
+            g_launches++;
+            k_ra_free_cached<<<(free_fns + kRaFreeThreads - 1) / kRaFreeThreads, kRaFreeThreads, 0, s>>>(P);
+        }
+        const uint32_t T = G0 <= 1024u ? ((G0 + 31u) & ~31u) : 1024u;
+        const uint32_t Q = (G0 + T - 1u) / T;
+        // symbol cache entries per function: the largest power of two within ~160 KB
+        uint32_t K = 64;
+        const size_t fixed = sizeof(Ra2Shared) + 12ull * G0;
+        while (K > 1 && fixed + static_cast<size_t>(G0) * K * 6u > 160u * 1024u) K >>= 1;
+        const size_t smem = fixed + static_cast<size_t>(G0) * K * 6u + 16;
         g_launches++;
-        k_ra_free<<<grid_for(P.F, 64), 64, 0, s>>>(P);
-        g_launches++;
-        k_ra_lane0<<<1, kRaThreads, 0, s>>>(P, P.S);
+        cudaError_t ce = cudaSuccess;
+        switch (Q) {
+            case 1:
+                ce = cudaFuncSetAttribute(k_ra_lane0_cached<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+                k_ra_lane0_cached<1><<<1, T, smem, s>>>(P, P.S, K);
+                break;
+            case 2:
+                ce = cudaFuncSetAttribute(k_ra_lane0_cached<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+                k_ra_lane0_cached<2><<<1, T, smem, s>>>(P, P.S, K);
+                break;
+            case 3:
+            case 4:
+                ce = cudaFuncSetAttribute(k_ra_lane0_cached<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+                k_ra_lane0_cached<4><<<1, T, smem, s>>>(P, P.S, K);
+                break;
+            default:
+                ce = cudaFuncSetAttribute(k_ra_lane0_cached<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+                k_ra_lane0_cached<8><<<1, T, smem, s>>>(P, P.S, K);
+                break;
+        }
+        if (ce != cudaSuccess) return ce;
     }
     g_launches++;
     k_ra_spill<<<grid_for(P.W), kThreads, 0, s>>>(P);

@@ -1,0 +1,290 @@
+// Register allocation step loops (rv_generator_avx.cpp:1018-1420) with on-chip symbol
+// caches.  The phases below are shared by the CUDA kernels (one thread per function
+// slot, barriers between phases) and the host model (the same phases in loops).
+//
+// Symbol state (physical register, swapped flag) lives in global memory, which always
+// holds the truth; each function keeps a direct-mapped copy of recently used symbols
+// in shared memory.  A symbol is written only by the function that owns it (its own
+// instruction range) and by swap marks, and a mark can only hit a symbol that sits in
+// row 0 of the register state -- row 0 also records which function wrote each entry,
+// so a mark updates that function's cached copy together with global memory.
+#pragma once
+
+#include "ptl_stages.cuh"
+
+namespace ptl {
+
+// ---------------------------------------------------------------- symbol caches
+struct SymCache {
+    uint32_t* tag;   // [slots * K] virtual register held, 0 = empty
+    uint16_t* val;   // (swapped << 8) | physical register
+    uint32_t K;      // entries per function (power of two)
+};
+
+PTL_HD void cache_reset(const SymCache& c, uint32_t slot) {
+    for (uint32_t k = 0; k < c.K; ++k) c.tag[slot * c.K + k] = 0;
+}
+
+// Looks up v (> 63); returns physical register and swapped flag.
+PTL_HD void sym_read(const Prog& P, const SymCache& c, uint32_t slot, uint32_t v, uint32_t* reg, bool* swp) {
+    const uint32_t e = slot * c.K + ((v - 64u) & (c.K - 1u));
+    if (c.tag[e] == v) {
+        const uint16_t x = c.val[e];
+        *reg = x & 0xFFu;
+        *swp = (x >> 8) != 0;
+        return;
+    }
+    *reg = P.symreg[v - 64u];
+    *swp = P.symswp[v - 64u] != 0;
+    c.tag[e] = v;
+    c.val[e] = static_cast<uint16_t>((*reg & 0xFFu) | (*swp ? 0x100u : 0u));
+}
+
+PTL_HD void sym_write(const Prog& P, const SymCache& c, uint32_t slot, uint32_t v, uint32_t reg, bool swp) {
+    P.symreg[v - 64u] = reg;
+    P.symswp[v - 64u] = swp ? 0xFFFFFFFFu : 0u;
+    const uint32_t e = slot * c.K + ((v - 64u) & (c.K - 1u));
+    c.tag[e] = v;
+    c.val[e] = static_cast<uint16_t>((reg & 0xFFu) | (swp ? 0x100u : 0u));
+}
+
+// A swap mark: global memory, plus the owner's cached copy if it holds v.
+PTL_HD void sym_mark(const Prog& P, const SymCache& c, uint32_t owner_slot, uint32_t v) {
+    P.symswp[v - 64u] = 0xFFFFFFFFu;
+    if (owner_slot == 0xFFFFFFFFu) return;
+    const uint32_t e = owner_slot * c.K + ((v - 64u) & (c.K - 1u));
+    if (c.tag[e] == v) c.val[e] = static_cast<uint16_t>(c.val[e] | 0x100u);
+}
+
+// ---------------------------------------------------------------- independent functions
+// Functions outside lane 0: no marks reach their symbols, so the loop needs only the
+// physical registers (kept in the cache) and emits trigger records for the lane-0 pass.
+PTL_HD void ra_free_function_cached(const Prog& P, const SymCache& c, uint32_t slot, uint32_t f) {
+    cache_reset(c, slot);
+    unsigned long long lifetime = 0x1Full;
+    const uint32_t g1 = f / 8u + 1u;
+    RaStep next;
+    bool have = ra_load(P, f, 0, next);
+    for (uint32_t i = 0; have; ++i) {
+        RaStep S = next;
+        have = ra_load(P, f, i + 1, next);  // issue the next step's loads early
+        if (S.ins == 0x000000EFu || !ra_own(P, f, S.r1) || !ra_own(P, f, S.r2) || !ra_own(P, f, S.ord)) {
+            record_error(P.err, ST_UNSUPPORTED, W_RA1, P.fn_start0[f] + i);
+            return;
+        }
+        uint32_t r1reg = 0, r2reg = 0;
+        bool s1 = false, s2 = false;
+        if (s32(S.r1) > 63) sym_read(P, c, slot, S.r1, &r1reg, &s1);
+        if (s32(S.r2) > 63) sym_read(P, c, slot, S.r2, &r2reg, &s2);
+        ra_compute(S, lifetime, r1reg, false, r2reg, false);
+        lifetime = S.cleared | S.rdm;
+        if (s32(S.ord) > 63) sym_write(P, c, slot, S.ord, S.rdr, false);
+        if (s32(S.r1) > 63) sym_write(P, c, slot, S.r1, S.r1r, false);
+        if (s32(S.r2) > 63) sym_write(P, c, slot, S.r2, S.r2r, false);
+        for (uint64_t t = S.trig; t; t &= t - 1) {
+            const uint32_t p = ctz64(t);
+            at_min_u32(&P.trig_min[static_cast<size_t>(i) * 64u + p], g1);
+            at_max_u32(&P.trig_max[static_cast<size_t>(i) * 64u + p], g1);
+        }
+    }
+}
+
+// ---------------------------------------------------------------- lane-0 lock-step
+// Shared (on-chip) state of the lane-0 pass.  Groups are stored as group+1 ("g1"); 0 and
+// 0xFFFFFFFF mean none for the max / min arrays.
+struct Ra2Shared {
+    uint32_t R0[64];       // row 0 of the register state
+    uint32_t R0own[64];    // slot of the function that wrote the entry
+    uint32_t snap[64];     // row 0 at the start of the step
+    uint32_t snapown[64];
+    uint32_t omin[64], omax[64];   // trigger groups of the other functions this step
+    uint32_t lcur[64], lmax[64];   // lane-0 triggers of the current round
+    uint32_t lnew[64], lmaxnew[64];
+    unsigned long long r0key[64];
+    uint32_t flag;
+};
+
+// Per function slot (registers on the device).
+struct Ra2Slot {
+    uint32_t j;            // group index (function 8j)
+    bool act;
+    unsigned long long lifetime;
+    RaStep S, next;
+    bool have_next;
+    uint32_t r1reg, r2reg;
+    bool r1stored, r2stored;   // swapped flag as stored before the step
+    bool r1m, r2m;             // marked by an earlier group this step (as used)
+    uint64_t m1, m2;           // row-0 positions holding r1 / r2
+};
+
+PTL_HD uint64_t snap_positions(const Ra2Shared& sh, uint32_t v) {
+    uint64_t m = 0;
+    for (int p = 0; p < 64; ++p) if (sh.snap[p] == v) m |= 1ull << p;
+    return m;
+}
+
+// Whether a symbol at row-0 positions m is marked by a group before j (g1 <= j).
+PTL_HD bool marked_before(const Ra2Shared& sh, uint64_t m, uint32_t j, bool with_lane0) {
+    for (; m; m &= m - 1) {
+        const uint32_t p = ctz64(m);
+        uint32_t g = sh.omin[p];
+        if (with_lane0 && sh.lcur[p] < g) g = sh.lcur[p];
+        if (g <= j) return true;
+    }
+    return false;
+}
+
+PTL_HD void ra2_slot_init(const Prog& P, const SymCache& c, Ra2Slot& L, uint32_t slot, uint32_t j) {
+    L.j = j;
+    L.lifetime = 0x1Full;
+    L.have_next = 8u * j < P.F && ra_load(P, 8u * j, 0, L.next);
+    cache_reset(c, slot);
+}
+
+// Step start for row-0 position p (64 threads).
+PTL_HD void ra2_begin_p(const Prog& P, Ra2Shared& sh, uint32_t i, uint32_t p) {
+    sh.snap[p] = sh.R0[p];
+    sh.snapown[p] = sh.R0own[p];
+    sh.omin[p] = P.trig_min[static_cast<size_t>(i) * 64u + p];
+    sh.omax[p] = P.trig_max[static_cast<size_t>(i) * 64u + p];
+    sh.lcur[p] = 0xFFFFFFFFu;
+    sh.lmax[p] = 0;
+    sh.lnew[p] = 0xFFFFFFFFu;
+    sh.lmaxnew[p] = 0;
+    sh.r0key[p] = 0;
+    if (p == 0) sh.flag = 0;
+}
+
+// Loads the slot's instruction of step i (prefetched in the previous step).
+PTL_HD void ra2_load(const Prog& P, Ra2Slot& L, uint32_t i, uint32_t* cur) {
+    L.act = L.have_next;
+    if (L.act) {
+        L.S = L.next;
+        L.have_next = ra_load(P, 8u * L.j, i + 1, L.next);
+        if (L.S.ins == 0x000000EFu || !ra_own(P, 8u * L.j, L.S.r1) || !ra_own(P, 8u * L.j, L.S.r2) ||
+            !ra_own(P, 8u * L.j, L.S.ord)) {
+            record_error(P.err, ST_UNSUPPORTED, W_RA2, P.fn_start0[8u * L.j] + i);
+            L.act = false;
+            L.have_next = false;
+        }
+    }
+    // what this function updates this step (for the mark phase)
+    cur[0] = L.act ? L.S.ord : 0u;
+    cur[1] = L.act ? L.S.r1 : 0u;
+    cur[2] = L.act ? L.S.r2 : 0u;
+}
+
+PTL_HD void ra2_add_triggers(Ra2Shared& sh, uint64_t trig, uint32_t g1, bool into_new) {
+    for (uint64_t t = trig; t; t &= t - 1) {
+        const uint32_t p = ctz64(t);
+        if (into_new) {
+            at_min_u32(&sh.lnew[p], g1);
+            at_max_u32(&sh.lmaxnew[p], g1);
+        } else {
+            at_min_u32(&sh.lcur[p], g1);
+            at_max_u32(&sh.lmax[p], g1);
+        }
+    }
+}
+
+// Round 0: lookups through the cache, marks of earlier groups among the other functions
+// only, the allocation, and this slot's triggers into lcur/lmax.
+PTL_HD void ra2_compute0(const Prog& P, const SymCache& c, Ra2Shared& sh, Ra2Slot& L, uint32_t slot) {
+    if (!L.act) return;
+    RaStep& S = L.S;
+    L.r1reg = L.r2reg = 0;
+    L.r1stored = L.r2stored = false;
+    L.m1 = L.m2 = 0;
+    if (s32(S.r1) > 63) {
+        sym_read(P, c, slot, S.r1, &L.r1reg, &L.r1stored);
+        L.m1 = snap_positions(sh, S.r1);
+    }
+    if (s32(S.r2) > 63) {
+        sym_read(P, c, slot, S.r2, &L.r2reg, &L.r2stored);
+        L.m2 = snap_positions(sh, S.r2);
+    }
+    L.r1m = marked_before(sh, L.m1, L.j, false);
+    L.r2m = marked_before(sh, L.m2, L.j, false);
+    ra_compute(S, L.lifetime, L.r1reg, L.r1stored || L.r1m, L.r2reg, L.r2stored || L.r2m);
+    ra2_add_triggers(sh, S.trig, L.j + 1u, false);
+}
+
+// After round 0: does an earlier lane-0 trigger change what this slot read?
+PTL_HD void ra2_check(Ra2Shared& sh, const Ra2Slot& L) {
+    if (!L.act || (L.m1 | L.m2) == 0) return;
+    if (marked_before(sh, L.m1, L.j, true) != L.r1m || marked_before(sh, L.m2, L.j, true) != L.r2m) sh.flag = 1;
+}
+
+// Jacobi round (only when the check fired): recompute with the current lane-0 triggers
+// and accumulate the next round's triggers.
+PTL_HD void ra2_round(Ra2Shared& sh, Ra2Slot& L) {
+    if (!L.act) return;
+    if (L.m1 | L.m2) {
+        L.r1m = marked_before(sh, L.m1, L.j, true);
+        L.r2m = marked_before(sh, L.m2, L.j, true);
+        ra_compute(L.S, L.lifetime, L.r1reg, L.r1stored || L.r1m, L.r2reg, L.r2stored || L.r2m);
+    }
+    ra2_add_triggers(sh, L.S.trig, L.j + 1u, true);
+}
+
+// Row-0 thread p after a Jacobi round: adopt the new triggers; report change.
+PTL_HD bool ra2_round_p(Ra2Shared& sh, uint32_t p) {
+    const bool changed = sh.lnew[p] != sh.lcur[p];
+    sh.lcur[p] = sh.lnew[p];
+    sh.lmax[p] = sh.lmaxnew[p];
+    sh.lnew[p] = 0xFFFFFFFFu;
+    sh.lmaxnew[p] = 0;
+    return changed;
+}
+
+// Apply the step: lifetime, own symbol updates (swapped only when a later group marks
+// the symbol in this step), row-0 writes as (group, value) keys.
+PTL_HD void ra2_apply(const Prog& P, const SymCache& c, Ra2Shared& sh, Ra2Slot& L, uint32_t slot) {
+    if (!L.act) return;
+    const RaStep& S = L.S;
+    L.lifetime = S.cleared | S.rdm;
+    const uint32_t g1 = L.j + 1u;
+    auto later = [&](uint32_t v) {
+        for (uint64_t m = snap_positions(sh, v); m; m &= m - 1) {
+            const uint32_t p = ctz64(m);
+            const uint32_t g = sh.omax[p] > sh.lmax[p] ? sh.omax[p] : sh.lmax[p];
+            if (g > g1) return true;
+        }
+        return false;
+    };
+    // the reference's order: rd, rs1, rs2 (a later write of the same symbol wins)
+    if (s32(S.ord) > 63) sym_write(P, c, slot, S.ord, S.rdr, false);
+    if (s32(S.r1) > 63) sym_write(P, c, slot, S.r1, S.r1r, false);
+    if (s32(S.r2) > 63) sym_write(P, c, slot, S.r2, S.r2r, false);
+    if (s32(S.ord) > 63 && later(S.ord)) sym_write(P, c, slot, S.ord, P.symreg[S.ord - 64u], true);
+    if (s32(S.r1) > 63 && later(S.r1)) sym_write(P, c, slot, S.r1, P.symreg[S.r1 - 64u], true);
+    if (s32(S.r2) > 63 && later(S.r2)) sym_write(P, c, slot, S.r2, P.symreg[S.r2 - 64u], true);
+    const unsigned long long key = static_cast<unsigned long long>(g1) << 32;
+    if (S.ord != 0) at_max_u64(&sh.r0key[S.rdr & 63u], key | S.ord);
+    if (S.r1r != S.rdr && s32(S.r1r) >= 0 && S.r1r < 64u) at_max_u64(&sh.r0key[S.r1r], key | 0xFFFFFFFFull);
+    if (S.r2r != S.rdr && s32(S.r2r) >= 0 && S.r2r < 64u) at_max_u64(&sh.r0key[S.r2r], key | 0xFFFFFFFFull);
+}
+
+// Step end for row-0 position p: marks on symbols their owner did not update this step,
+// then row 0 takes the highest group's write.  cur[3*slot..] are the slots' updates;
+// slot_of_group maps a group to its slot.
+PTL_HD void ra2_end_p(const Prog& P, const SymCache& c, Ra2Shared& sh, uint32_t p, const uint32_t* cur) {
+    const bool triggered = sh.omin[p] != 0xFFFFFFFFu || sh.lcur[p] != 0xFFFFFFFFu;
+    const uint32_t v = sh.snap[p];
+    if (triggered && s32(v - 64u) >= 0) {
+        const uint32_t own = sh.snapown[p];
+        bool updated = false;
+        if (own != 0xFFFFFFFFu) {
+            const uint32_t* u = cur + 3u * own;
+            updated = (s32(u[0]) > 63 && u[0] == v) || (s32(u[1]) > 63 && u[1] == v) || (s32(u[2]) > 63 && u[2] == v);
+        }
+        if (!updated) sym_mark(P, c, own, v);
+    }
+    const unsigned long long k = sh.r0key[p];
+    if (k != 0) {
+        sh.R0[p] = static_cast<uint32_t>(k);
+        sh.R0own[p] = static_cast<uint32_t>(k >> 32) - 1u;  // group index == slot index
+    }
+}
+
+}  // namespace ptl

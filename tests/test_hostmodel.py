@@ -119,3 +119,17 @@ def test_depth_order_emulation_equals_std_sort(built, mode):
         got = np.empty(n, np.uint32)
         L.ptlhm_depth_sort(keys.ctypes.data, n, got.ctypes.data)
         np.testing.assert_array_equal(got, want)
+
+
+@pytest.mark.parametrize("k", [1, 64])
+def test_hostmodel_symbol_cache_sizes(built, k):
+    """The lane-0 symbol cache gives the same result with one entry and with many."""
+    from ptilopsis_gb300.synth import config_params, generate
+    L = hostmodel()
+    L.ptlhm_set_cache_entries(ctypes.c_uint32(k))
+    try:
+        assert_stages_equal(tree_to_ast(generate(config_params("c1", scale=40 / 2048))))
+        ast, _ = load_fixture("pareas_basic_3_in")
+        assert_stages_equal(ast)
+    finally:
+        L.ptlhm_set_cache_entries(ctypes.c_uint32(4))
