@@ -4,6 +4,7 @@
 // their bounded waits.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <atomic>
 
 #include "ptl_kernels.cuh"
@@ -564,6 +565,10 @@ __global__ void __launch_bounds__(1024) k_ra_lane0_cached(Prog P, uint32_t S, ui
     uint16_t* cval = reinterpret_cast<uint16_t*>(ctag + G0 * K);
     const SymCache c{ctag, cval, K};
     const uint32_t tid = threadIdx.x, T = blockDim.x;
+    if (T < 64u) {  // the row-0 phases need a thread per physical register
+        if (tid == 0) record_error(P.err, ST_UNSUPPORTED, W_RA2, T);
+        return;
+    }
     Ra2Slot L[Q];
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
@@ -803,7 +808,8 @@ cudaError_t run_regalloc_steps(const Prog& P, cudaStream_t s, bool* serial_out) 
             g_launches++;
             k_ra_free_cached<<<(free_fns + kRaFreeThreads - 1) / kRaFreeThreads, kRaFreeThreads, 0, s>>>(P);
         }
-        const uint32_t T = G0 <= 1024u ? ((G0 + 31u) & ~31u) : 1024u;
+        // at least 64 threads: one per physical register in the row-0 phases
+        const uint32_t T = G0 <= 1024u ? std::max(64u, (G0 + 31u) & ~31u) : 1024u;
         const uint32_t Q = (G0 + T - 1u) / T;
         // symbol cache entries per function: the largest power of two within ~160 KB
         uint32_t K = 64;
