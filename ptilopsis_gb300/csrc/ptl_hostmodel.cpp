@@ -221,22 +221,37 @@ struct Model {
             ra2_slot_init(P, c, L[j], j, j);
         }
         for (int p = 0; p < 64; ++p) { sh.R0[p] = 0xFFFFFFFFu; sh.R0own[p] = 0xFFFFFFFFu; }
+        if (S > 0) for (uint32_t p = 0; p < 64; ++p) ra2_begin_p(sh, 0, p, P.trig_min[p], P.trig_max[p]);
         for (uint32_t i = 0; i < S; ++i) {
-            for (uint32_t p = 0; p < 64; ++p) ra2_begin_p(P, sh, i, p);
-            for (uint32_t j = 0; j < G0; ++j) ra2_load(P, L[j], i, cur.data() + 3 * j);
-            for (uint32_t j = 0; j < G0; ++j) ra2_compute0(P, c, sh, L[j], j);
-            for (uint32_t j = 0; j < G0; ++j) ra2_check(sh, L[j]);
-            if (sh.flag) {
-                for (uint32_t round = 0;; ++round) {
-                    for (uint32_t j = 0; j < G0; ++j) ra2_round(sh, L[j]);
-                    bool changed = false;
-                    for (uint32_t p = 0; p < 64; ++p) changed |= ra2_round_p(sh, p);
-                    if (!changed) break;
-                    if (round > G0 + 2) { record_error(P.err, ST_DEVICE_TIMEOUT, W_RA2, i); break; }
+            bool in_row0 = false;
+            for (uint32_t j = 0; j < G0; ++j) {
+                ra2_load(P, L[j], i, cur.data() + 3 * j);
+                in_row0 |= ra2_compute0(P, c, sh, L[j], j, i);
+            }
+            if (in_row0) {
+                bool flag = false;
+                for (uint32_t j = 0; j < G0; ++j) flag |= ra2_check(sh, L[j]);
+                if (flag) {
+                    for (uint32_t round = 0;; ++round) {
+                        for (uint32_t j = 0; j < G0; ++j) ra2_round(sh, L[j]);
+                        bool changed = false;
+                        for (uint32_t p = 0; p < 64; ++p) changed |= ra2_round_p(sh, p);
+                        if (!changed) break;
+                        if (round > G0 + 2) { record_error(P.err, ST_DEVICE_TIMEOUT, W_RA2, i); break; }
+                    }
                 }
             }
-            for (uint32_t j = 0; j < G0; ++j) ra2_apply(P, c, sh, L[j], j);
-            for (uint32_t p = 0; p < 64; ++p) ra2_end_p(P, c, sh, p, cur.data());
+            for (uint32_t j = 0; j < G0; ++j) ra2_apply(P, c, sh, L[j], j, i);
+            for (uint32_t p = 0; p < 64; ++p) snap_clear_next(sh, i, p);
+            for (uint32_t p = 0; p < 64; ++p) {
+                ra2_end_p(P, c, sh, p, cur.data());
+            }
+            if (i + 1 < S) {
+                for (uint32_t p = 0; p < 64; ++p) {
+                    ra2_begin_p(sh, i + 1, p, P.trig_min[static_cast<size_t>(i + 1) * 64 + p],
+                                P.trig_max[static_cast<size_t>(i + 1) * 64 + p]);
+                }
+            }
         }
     }
 

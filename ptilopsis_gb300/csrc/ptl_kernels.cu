@@ -577,54 +577,74 @@ __global__ void __launch_bounds__(1024) k_ra_lane0_cached(Prog P, uint32_t S, ui
         L[q].have_next = false;
         if (j < G0) ra2_slot_init(P, c, L[q], j, j);
     }
+    uint32_t tmin = 0xFFFFFFFFu, tmax = 0;  // trigger records, one step ahead
     if (tid < 64) {
         sh.R0[tid] = 0xFFFFFFFFu;
         sh.R0own[tid] = 0xFFFFFFFFu;
+        for (uint32_t k = tid; k < kSnapHash; k += 64) {
+            sh.hkey[0][k] = sh.hkey[1][k] = 0;
+            sh.hmask[0][k] = sh.hmask[1][k] = 0;
+        }
     }
     __syncthreads();
+    if (tid < 64 && S > 0) {
+        ra2_begin_p(sh, 0, tid, P.trig_min[tid], P.trig_max[tid]);
+        if (S > 1) { tmin = P.trig_min[64u + tid]; tmax = P.trig_max[64u + tid]; }
+    }
+    __syncthreads();
+    // Per step, three barriers unless an operand sits in row 0: (load+compute) |
+    // (apply + clear next hash) | (marks, row 0, next step's snapshot).
     for (uint32_t i = 0; i < S; ++i) {
-        if (tid < 64) ra2_begin_p(P, sh, i, tid);
+        bool in_row0 = false;
 #pragma unroll
         for (int q = 0; q < Q; ++q) {
             const uint32_t j = tid + static_cast<uint32_t>(q) * T;
-            if (j < G0) ra2_load(P, L[q], i, cur + 3u * j);
+            if (j < G0) {
+                ra2_load(P, L[q], i, cur + 3u * j);
+                in_row0 |= ra2_compute0(P, c, sh, L[q], j, i);
+            }
         }
-        __syncthreads();
+        if (__syncthreads_or(in_row0)) {
+            bool flag = false;
 #pragma unroll
-        for (int q = 0; q < Q; ++q) {
-            const uint32_t j = tid + static_cast<uint32_t>(q) * T;
-            if (j < G0) ra2_compute0(P, c, sh, L[q], j);
-        }
-        __syncthreads();
+            for (int q = 0; q < Q; ++q) {
+                const uint32_t j = tid + static_cast<uint32_t>(q) * T;
+                if (j < G0) flag |= ra2_check(sh, L[q]);
+            }
+            if (__syncthreads_or(flag)) {
+                for (uint32_t round = 0;; ++round) {
 #pragma unroll
-        for (int q = 0; q < Q; ++q) {
-            const uint32_t j = tid + static_cast<uint32_t>(q) * T;
-            if (j < G0) ra2_check(sh, L[q]);
-        }
-        __syncthreads();
-        if (sh.flag) {
-            for (uint32_t round = 0;; ++round) {
-#pragma unroll
-                for (int q = 0; q < Q; ++q) {
-                    const uint32_t j = tid + static_cast<uint32_t>(q) * T;
-                    if (j < G0) ra2_round(sh, L[q]);
-                }
-                __syncthreads();
-                const bool changed = tid < 64 ? ra2_round_p(sh, tid) : false;
-                if (!__syncthreads_or(changed)) break;
-                if (round > G0 + 2u) {
-                    if (tid == 0) record_error(P.err, ST_DEVICE_TIMEOUT, W_RA2, i);
-                    break;
+                    for (int q = 0; q < Q; ++q) {
+                        const uint32_t j = tid + static_cast<uint32_t>(q) * T;
+                        if (j < G0) ra2_round(sh, L[q]);
+                    }
+                    __syncthreads();
+                    const bool changed = tid < 64 ? ra2_round_p(sh, tid) : false;
+                    if (!__syncthreads_or(changed)) break;
+                    if (round > G0 + 2u) {
+                        if (tid == 0) record_error(P.err, ST_DEVICE_TIMEOUT, W_RA2, i);
+                        break;
+                    }
                 }
             }
         }
 #pragma unroll
         for (int q = 0; q < Q; ++q) {
             const uint32_t j = tid + static_cast<uint32_t>(q) * T;
-            if (j < G0) ra2_apply(P, c, sh, L[q], j);
+            if (j < G0) ra2_apply(P, c, sh, L[q], j, i);
         }
+        if (tid < 64) snap_clear_next(sh, i, tid);
         __syncthreads();
-        if (tid < 64) ra2_end_p(P, c, sh, tid, cur);
+        if (tid < 64) {
+            ra2_end_p(P, c, sh, tid, cur);
+            if (i + 1 < S) {
+                ra2_begin_p(sh, i + 1, tid, tmin, tmax);
+                if (i + 2 < S) {
+                    tmin = P.trig_min[static_cast<size_t>(i + 2) * 64u + tid];
+                    tmax = P.trig_max[static_cast<size_t>(i + 2) * 64u + tid];
+                }
+            }
+        }
         __syncthreads();
     }
 }

@@ -92,7 +92,11 @@ PTL_HD void ra_free_function_cached(const Prog& P, const SymCache& c, uint32_t s
 // ---------------------------------------------------------------- lane-0 lock-step
 // Shared (on-chip) state of the lane-0 pass.  Groups are stored as group+1 ("g1"); 0 and
 // 0xFFFFFFFF mean none for the max / min arrays.
+constexpr uint32_t kSnapHash = 128;  // open-addressing table: virtual register -> row-0 positions
+
 struct Ra2Shared {
+    uint32_t hkey[2][kSnapHash];            // double-buffered by step parity; 0 = empty
+    unsigned long long hmask[2][kSnapHash];
     uint32_t R0[64];       // row 0 of the register state
     uint32_t R0own[64];    // slot of the function that wrote the entry
     uint32_t snap[64];     // row 0 at the start of the step
@@ -101,7 +105,6 @@ struct Ra2Shared {
     uint32_t lcur[64], lmax[64];   // lane-0 triggers of the current round
     uint32_t lnew[64], lmaxnew[64];
     unsigned long long r0key[64];
-    uint32_t flag;
 };
 
 // Per function slot (registers on the device).
@@ -117,10 +120,50 @@ struct Ra2Slot {
     uint64_t m1, m2;           // row-0 positions holding r1 / r2
 };
 
-PTL_HD uint64_t snap_positions(const Ra2Shared& sh, uint32_t v) {
-    uint64_t m = 0;
-    for (int p = 0; p < 64; ++p) if (sh.snap[p] == v) m |= 1ull << p;
-    return m;
+PTL_HD uint32_t snap_hash(uint32_t v) { return (v * 2654435761u) >> 25; }
+
+// Row-0 positions holding v at the start of step i (v > 63).
+PTL_HD uint64_t snap_positions(const Ra2Shared& sh, uint32_t i, uint32_t v) {
+    const uint32_t t = i & 1u;
+    uint32_t h = snap_hash(v);
+    for (uint32_t probe = 0; probe < kSnapHash; ++probe) {
+        const uint32_t k = sh.hkey[t][h];
+        if (k == v) return sh.hmask[t][h];
+        if (k == 0) return 0;
+        h = (h + 1u) & (kSnapHash - 1u);
+    }
+    return 0;
+}
+
+PTL_HD void snap_insert(Ra2Shared& sh, uint32_t i, uint32_t v, uint32_t p) {
+    const uint32_t t = i & 1u;
+    uint32_t h = snap_hash(v);
+    for (uint32_t probe = 0; probe < kSnapHash; ++probe) {
+#if defined(__CUDA_ARCH__)
+        const uint32_t prev = atomicCAS(&sh.hkey[t][h], 0u, v);
+#else
+        const uint32_t prev = sh.hkey[t][h];
+        if (prev == 0) sh.hkey[t][h] = v;
+#endif
+        if (prev == 0 || prev == v) {
+#if defined(__CUDA_ARCH__)
+            atomicOr(&sh.hmask[t][h], 1ull << p);
+#else
+            sh.hmask[t][h] |= 1ull << p;
+#endif
+            return;
+        }
+        h = (h + 1u) & (kSnapHash - 1u);
+    }
+}
+
+// Empties the table step i+1 will use (called during step i, before its last barrier).
+PTL_HD void snap_clear_next(Ra2Shared& sh, uint32_t i, uint32_t p) {
+    const uint32_t t = (i + 1u) & 1u;
+    for (uint32_t k = p; k < kSnapHash; k += 64u) {
+        sh.hkey[t][k] = 0;
+        sh.hmask[t][k] = 0;
+    }
 }
 
 // Whether a symbol at row-0 positions m is marked by a group before j (g1 <= j).
@@ -141,18 +184,19 @@ PTL_HD void ra2_slot_init(const Prog& P, const SymCache& c, Ra2Slot& L, uint32_t
     cache_reset(c, slot);
 }
 
-// Step start for row-0 position p (64 threads).
-PTL_HD void ra2_begin_p(const Prog& P, Ra2Shared& sh, uint32_t i, uint32_t p) {
+// Step start for row-0 position p (64 threads); tmin/tmax are the step's trigger
+// records of the other functions (loaded a step ahead).
+PTL_HD void ra2_begin_p(Ra2Shared& sh, uint32_t i, uint32_t p, uint32_t tmin, uint32_t tmax) {
     sh.snap[p] = sh.R0[p];
     sh.snapown[p] = sh.R0own[p];
-    sh.omin[p] = P.trig_min[static_cast<size_t>(i) * 64u + p];
-    sh.omax[p] = P.trig_max[static_cast<size_t>(i) * 64u + p];
+    if (s32(sh.R0[p] - 64u) >= 0) snap_insert(sh, i, sh.R0[p], p);
+    sh.omin[p] = tmin;
+    sh.omax[p] = tmax;
     sh.lcur[p] = 0xFFFFFFFFu;
     sh.lmax[p] = 0;
     sh.lnew[p] = 0xFFFFFFFFu;
     sh.lmaxnew[p] = 0;
     sh.r0key[p] = 0;
-    if (p == 0) sh.flag = 0;
 }
 
 // Loads the slot's instruction of step i (prefetched in the previous step).
@@ -189,30 +233,32 @@ PTL_HD void ra2_add_triggers(Ra2Shared& sh, uint64_t trig, uint32_t g1, bool int
 
 // Round 0: lookups through the cache, marks of earlier groups among the other functions
 // only, the allocation, and this slot's triggers into lcur/lmax.
-PTL_HD void ra2_compute0(const Prog& P, const SymCache& c, Ra2Shared& sh, Ra2Slot& L, uint32_t slot) {
-    if (!L.act) return;
+// Returns whether the slot read a symbol that sits in row 0 (then the check phase runs).
+PTL_HD bool ra2_compute0(const Prog& P, const SymCache& c, Ra2Shared& sh, Ra2Slot& L, uint32_t slot, uint32_t i) {
+    if (!L.act) return false;
     RaStep& S = L.S;
     L.r1reg = L.r2reg = 0;
     L.r1stored = L.r2stored = false;
     L.m1 = L.m2 = 0;
     if (s32(S.r1) > 63) {
         sym_read(P, c, slot, S.r1, &L.r1reg, &L.r1stored);
-        L.m1 = snap_positions(sh, S.r1);
+        L.m1 = snap_positions(sh, i, S.r1);
     }
     if (s32(S.r2) > 63) {
         sym_read(P, c, slot, S.r2, &L.r2reg, &L.r2stored);
-        L.m2 = snap_positions(sh, S.r2);
+        L.m2 = snap_positions(sh, i, S.r2);
     }
     L.r1m = marked_before(sh, L.m1, L.j, false);
     L.r2m = marked_before(sh, L.m2, L.j, false);
     ra_compute(S, L.lifetime, L.r1reg, L.r1stored || L.r1m, L.r2reg, L.r2stored || L.r2m);
     ra2_add_triggers(sh, S.trig, L.j + 1u, false);
+    return (L.m1 | L.m2) != 0;
 }
 
 // After round 0: does an earlier lane-0 trigger change what this slot read?
-PTL_HD void ra2_check(Ra2Shared& sh, const Ra2Slot& L) {
-    if (!L.act || (L.m1 | L.m2) == 0) return;
-    if (marked_before(sh, L.m1, L.j, true) != L.r1m || marked_before(sh, L.m2, L.j, true) != L.r2m) sh.flag = 1;
+PTL_HD bool ra2_check(const Ra2Shared& sh, const Ra2Slot& L) {
+    if (!L.act || (L.m1 | L.m2) == 0) return false;
+    return marked_before(sh, L.m1, L.j, true) != L.r1m || marked_before(sh, L.m2, L.j, true) != L.r2m;
 }
 
 // Jacobi round (only when the check fired): recompute with the current lane-0 triggers
@@ -239,13 +285,13 @@ PTL_HD bool ra2_round_p(Ra2Shared& sh, uint32_t p) {
 
 // Apply the step: lifetime, own symbol updates (swapped only when a later group marks
 // the symbol in this step), row-0 writes as (group, value) keys.
-PTL_HD void ra2_apply(const Prog& P, const SymCache& c, Ra2Shared& sh, Ra2Slot& L, uint32_t slot) {
+PTL_HD void ra2_apply(const Prog& P, const SymCache& c, Ra2Shared& sh, Ra2Slot& L, uint32_t slot, uint32_t i) {
     if (!L.act) return;
     const RaStep& S = L.S;
     L.lifetime = S.cleared | S.rdm;
     const uint32_t g1 = L.j + 1u;
     auto later = [&](uint32_t v) {
-        for (uint64_t m = snap_positions(sh, v); m; m &= m - 1) {
+        for (uint64_t m = snap_positions(sh, i, v); m; m &= m - 1) {
             const uint32_t p = ctz64(m);
             const uint32_t g = sh.omax[p] > sh.lmax[p] ? sh.omax[p] : sh.lmax[p];
             if (g > g1) return true;
