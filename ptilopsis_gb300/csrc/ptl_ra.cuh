@@ -63,11 +63,12 @@ PTL_HD void ra_free_function_cached(const Prog& P, const SymCache& c, uint32_t s
     cache_reset(c, slot);
     unsigned long long lifetime = 0x1Full;
     const uint32_t g1 = f / 8u + 1u;
+    const uint32_t start = P.fn_start0[f], size = P.fn_size0[f];
     RaStep next;
-    bool have = ra_load(P, f, 0, next);
+    bool have = ra_load_at(P, start, size, 0, next);
     for (uint32_t i = 0; have; ++i) {
         RaStep S = next;
-        have = ra_load(P, f, i + 1, next);  // issue the next step's loads early
+        have = ra_load_at(P, start, size, i + 1, next);  // issue the next step's loads early
         if (S.ins == 0x000000EFu || !ra_own(P, f, S.r1) || !ra_own(P, f, S.r2) || !ra_own(P, f, S.ord)) {
             record_error(P.err, ST_UNSUPPORTED, W_RA1, P.fn_start0[f] + i);
             return;
@@ -110,6 +111,7 @@ struct Ra2Shared {
 // Per function slot (registers on the device).
 struct Ra2Slot {
     uint32_t j;            // group index (function 8j)
+    uint32_t start, size;  // the function's isn_cnt instruction range
     bool act;
     unsigned long long lifetime;
     RaStep S, next;
@@ -180,7 +182,9 @@ PTL_HD bool marked_before(const Ra2Shared& sh, uint64_t m, uint32_t j, bool with
 PTL_HD void ra2_slot_init(const Prog& P, const SymCache& c, Ra2Slot& L, uint32_t slot, uint32_t j) {
     L.j = j;
     L.lifetime = 0x1Full;
-    L.have_next = 8u * j < P.F && ra_load(P, 8u * j, 0, L.next);
+    L.start = 8u * j < P.F ? P.fn_start0[8u * j] : 0u;
+    L.size = 8u * j < P.F ? P.fn_size0[8u * j] : 0u;
+    L.have_next = 8u * j < P.F && ra_load_at(P, L.start, L.size, 0, L.next);
     cache_reset(c, slot);
 }
 
@@ -204,7 +208,7 @@ PTL_HD void ra2_load(const Prog& P, Ra2Slot& L, uint32_t i, uint32_t* cur) {
     L.act = L.have_next;
     if (L.act) {
         L.S = L.next;
-        L.have_next = ra_load(P, 8u * L.j, i + 1, L.next);
+        L.have_next = ra_load_at(P, L.start, L.size, i + 1, L.next);
         if (L.S.ins == 0x000000EFu || !ra_own(P, 8u * L.j, L.S.r1) || !ra_own(P, 8u * L.j, L.S.r2) ||
             !ra_own(P, 8u * L.j, L.S.ord)) {
             record_error(P.err, ST_UNSUPPORTED, W_RA2, P.fn_start0[8u * L.j] + i);

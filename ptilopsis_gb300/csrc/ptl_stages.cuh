@@ -603,7 +603,17 @@ PTL_HD void ra_compute(RaStep& S, unsigned long long lifetime, uint32_t r1reg, b
     S.trig = trig;
 }
 
-// Loads the step's instruction of the function with isn_cnt range [start, start+size).
+// Loads step i's instruction of a function with isn_cnt range [start, start+size).
+PTL_HD bool ra_load_at(const Prog& P, uint32_t start, uint32_t size, uint32_t i, RaStep& S) {
+    if (s32(i) >= s32(size)) return false;
+    const uint32_t off = start + i;
+    S.ins = P.instr[off];
+    S.r1 = P.rs1[off];
+    S.r2 = P.rs2[off];
+    S.ord = P.rd[off];
+    return true;
+}
+
 PTL_HD bool ra_load(const Prog& P, uint32_t f, uint32_t i, RaStep& S) {
     const uint32_t sz = P.fn_size0[f];
     if (s32(i) >= s32(sz)) return false;
