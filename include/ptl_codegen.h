@@ -66,7 +66,11 @@ ptl_status ptl_generator_upload(ptl_generator* gen, const ptl_ast_view* tree);
 
 /* Replaces rv_generator_avx::process(bool profile) (rv_generator_avx.cpp:104-120): runs
  * the seven stages.  Unlike the reference, which mutates its arrays and cannot be run
- * twice, process may be called again and recompiles from the copied tree. */
+ * twice, process may be called again and recompiles from the copied tree.
+ * profile bits: 1 = per-stage device times (ptl_generator_stage_ns); 2 = leave the words
+ * on the device (ptl_generator_device_instructions); 4 = the register allocator finds
+ * row-0 values through its hash table even when every virtual register has one
+ * definition (the general path, normally taken only when one has two; same output). */
 ptl_status ptl_generator_process(ptl_generator* gen, int profile);
 
 /* Replaces get_instructions() (rv_generator_avx.cpp:82-84): the encoded RV words, in a

@@ -112,7 +112,7 @@ struct ptl_generator {
     DevBuf decl, fn_id, fn_start, fn_size, fn_end, fn_start0, fn_size0, fn_end0;
     DevBuf fn_ra_start, fn_ra_end, fn_ra_size;
     DevBuf instr, rd, rs1, rs2, jt, owner, used, smark, used_instrs;
-    DevBuf symreg, symswp, stamp, lifetime, trig_min, trig_max, spill, roffs;
+    DevBuf symreg, symswp, stamp, defpos, lifetime, trig_min, trig_max, spill, roffs;
     DevBuf ni, nrd, nr1, nr2, njt, fsz, joffs, out;
     DevBuf sort_a, sort_apos, sort_bpos, sort_seg0, sort_seg1, sort_tile_seg, sort_tile_l, sort_tile_r,
         sort_leaf, sort_heap, sort_counters;
@@ -135,7 +135,7 @@ struct ptl_generator {
                 &par, &ci, &dep, &fflag, &sizes, &loc0, &loc, &pos, &regs, &decl, &fn_id, &fn_start,
                 &fn_size, &fn_end, &fn_start0, &fn_size0, &fn_end0, &fn_ra_start, &fn_ra_end, &fn_ra_size,
                 &instr, &rd, &rs1, &rs2, &jt, &owner, &used, &smark, &used_instrs, &symreg, &symswp,
-                &stamp, &lifetime, &trig_min, &trig_max, &spill, &roffs, &ni, &nrd, &nr1, &nr2, &njt,
+                &stamp, &defpos, &lifetime, &trig_min, &trig_max, &spill, &roffs, &ni, &nrd, &nr1, &nr2, &njt,
                 &fsz, &joffs, &out, &sort_a, &sort_apos, &sort_bpos, &sort_seg0, &sort_seg1,
                 &sort_tile_seg, &sort_tile_l, &sort_tile_r, &sort_leaf, &sort_heap, &sort_counters,
                 &scan_status, &scan_counter, &meta, &flags, &errw, &tables, &depth_seen};
@@ -218,6 +218,7 @@ Prog make_prog(ptl_generator* g) {
     P.symreg = g->symreg.at<uint32_t>();
     P.symswp = g->symswp.at<uint32_t>();
     P.stamp = g->stamp.at<uint32_t>();
+    P.defpos = g->defpos.at<uint8_t>();
     P.lifetime = g->lifetime.at<unsigned long long>();
     P.trig_min = g->trig_min.at<uint32_t>();
     P.trig_max = g->trig_max.at<uint32_t>();
@@ -289,7 +290,7 @@ struct StageTimer {
     }
 };
 
-ptl_status run_pipeline(ptl_generator* g, bool profile, bool to_host) {
+ptl_status run_pipeline(ptl_generator* g, bool profile, bool to_host, bool row0_hash) {
     cudaStream_t s = g->stream;
     const size_t n = g->n;
     const size_t nb8 = r8(n);
@@ -422,9 +423,10 @@ ptl_status run_pipeline(ptl_generator* g, bool profile, bool to_host) {
     PTL_CU(g->used.zero(s));
     PTL_CU(g->smark.ensure(wb8, 1));
     PTL_CU(g->smark.zero(s));
+    PTL_CU(g->defpos.ensure(wb8, 1));
     P = make_prog(g);
     if (!prog_ready(P, {P.instr, P.rd, P.rs1, P.rs2, P.jt, P.used_instrs, P.symreg, P.symswp, P.stamp, P.spill,
-                        P.roffs, P.owner, P.used, P.smark, P.pos, P.regs}))
+                        P.defpos, P.roffs, P.owner, P.used, P.smark, P.pos, P.regs}))
         return fail(g, PTL_CUDA_ERROR, "internal: unallocated word arrays");
     PTL_CU(run_depth_sort(P, ss, s, &g->sort_rounds));
     launch_gen(P, s);
@@ -449,7 +451,7 @@ ptl_status run_pipeline(ptl_generator* g, bool profile, bool to_host) {
     P = make_prog(g);
     if (!prog_ready(P, {P.lifetime, P.trig_min, P.trig_max}))
         return fail(g, PTL_CUDA_ERROR, "internal: unallocated regalloc state");
-    PTL_CU(run_regalloc_steps(P, s, &g->ra_serial));
+    PTL_CU(run_regalloc_steps(P, s, &g->ra_serial, row0_hash));
     PTL_CU(scan_for(wb8, &sc));
     launch_regalloc_count_scan(P, sc, s);
     uint32_t last_off = 0;
@@ -579,7 +581,7 @@ ptl_status ptl_generator_create(const ptl_ast_view* tree, int device, ptl_genera
 ptl_status ptl_generator_process(ptl_generator* g, int profile) {
     if (!g) return PTL_BAD_ARGUMENT;
     if (cudaSetDevice(g->device) != cudaSuccess) return fail(g, PTL_CUDA_ERROR, "cudaSetDevice");
-    const ptl_status st = run_pipeline(g, (profile & 1) != 0, (profile & 2) == 0);
+    const ptl_status st = run_pipeline(g, (profile & 1) != 0, (profile & 2) == 0, (profile & 4) != 0);
     if (st == PTL_OK) g->last_error.clear();
     return st;
 }

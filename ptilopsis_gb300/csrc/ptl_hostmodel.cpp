@@ -22,6 +22,8 @@ using namespace ptl;
 namespace {
 
 uint32_t g_cache_k = 4;  // entries per function of the lane-0 symbol cache
+bool g_force_hashed = false;  // lane-0 pass finds row-0 values by hashing even when definitions are unique
+bool g_last_hashed = false;   // the last compile had a lane-0 virtual register with two definitions
 
 template <typename T>
 struct HBuf {
@@ -41,7 +43,7 @@ struct Model {
     CodeTables tab;
     ErrorWord err{};
     uint32_t flags[4] = {0, 0, 0, 0};
-    HBuf<uint8_t> in_type, in_rtype, fflag, used, smark;
+    HBuf<uint8_t> in_type, in_rtype, fflag, used, smark, defpos;
     HBuf<int32_t> in_parent, in_depth, in_child, par, ci, dep;
     HBuf<uint32_t> in_data, nt, rt, nd1, nd, sizes, loc0, loc, regs, pos, decl, fn_id, fn_start, fn_size,
         fn_end, fn_start0, fn_size0, fn_end0, fn_ra_start, fn_ra_end, fn_ra_size, instr, rd, rs1, rs2, jt,
@@ -59,6 +61,7 @@ struct Model {
         P.fn_end = fn_end.p; P.fn_start0 = fn_start0.p; P.fn_size0 = fn_size0.p; P.instr = instr.p;
         P.rd = rd.p; P.rs1 = rs1.p; P.rs2 = rs2.p; P.jt = jt.p; P.used = used.p; P.smark = smark.p;
         P.used_instrs = used_instrs.p; P.symreg = symreg.p; P.symswp = symswp.p; P.stamp = stamp.p;
+        P.defpos = defpos.p;
         P.lifetime = lifetime.p; P.trig_min = trig_min.p; P.trig_max = trig_max.p; P.spill = spill.p;
         P.roffs = roffs.p; P.ni = ni.p; P.nrd = nrd.p; P.nr1 = nr1.p; P.nr2 = nr2.p; P.njt = njt.p;
         P.fsz = fsz.p; P.joffs = joffs.p; P.out = out.p;
@@ -127,92 +130,16 @@ struct Model {
         for (uint32_t p = 0; p < n; ++p) pos.p[sidx(a[p])] = p;
     }
 
-    // Lane-0 functions in lock-step (k_ra_lane0).
-    void lane0(uint32_t S) {
-        const uint32_t G0 = (P.F + 7) / 8;
-        uint32_t R0[64], snap[64], fmin[64], fnext[64], fmax[64], omin[64], omax[64];
-        unsigned long long r0key[64];
-        std::fill(R0, R0 + 64, 0xFFFFFFFFu);
-        std::vector<RaStep> st(G0);
-        std::vector<char> act(G0);
-        auto marked = [&](uint32_t v, uint32_t limit) {
-            for (int p = 0; p < 64; ++p) if (snap[p] == v && fmin[p] <= limit) return true;
-            return false;
-        };
-        for (uint32_t i = 0; i < S; ++i) {
-            for (int p = 0; p < 64; ++p) {
-                snap[p] = R0[p];
-                omin[p] = P.trig_min[static_cast<size_t>(i) * 64 + p];
-                omax[p] = P.trig_max[static_cast<size_t>(i) * 64 + p];
-                fmin[p] = omin[p];
-                r0key[p] = 0;
-            }
-            for (uint32_t j = 0; j < G0; ++j) {
-                act[j] = ra_load(P, 8 * j, i, st[j]);
-                if (act[j] && (st[j].ins == 0xEFu || !ra_own(P, 8 * j, st[j].r1) || !ra_own(P, 8 * j, st[j].r2) ||
-                               !ra_own(P, 8 * j, st[j].ord))) {
-                    record_error(P.err, ST_UNSUPPORTED, W_RA2, P.fn_start0[8 * j] + i);
-                    act[j] = 0;
-                }
-            }
-            for (uint32_t round = 0;; ++round) {
-                for (int p = 0; p < 64; ++p) { fnext[p] = omin[p]; fmax[p] = omax[p]; }
-                for (uint32_t j = 0; j < G0; ++j) {
-                    if (!act[j]) continue;
-                    RaStep& S1 = st[j];
-                    uint32_t r1reg = 0, r2reg = 0;
-                    bool r1s = false, r2s = false;
-                    if (s32(S1.r1) > 63) { r1reg = P.symreg[S1.r1 - 64]; r1s = P.symswp[S1.r1 - 64] != 0 || marked(S1.r1, j); }
-                    if (s32(S1.r2) > 63) { r2reg = P.symreg[S1.r2 - 64]; r2s = P.symswp[S1.r2 - 64] != 0 || marked(S1.r2, j); }
-                    ra_compute(S1, P.lifetime[8 * j], r1reg, r1s, r2reg, r2s);
-                    for (uint64_t t = S1.trig; t; t &= t - 1) {
-                        const uint32_t p = ctz64(t);
-                        fnext[p] = std::min(fnext[p], j + 1);
-                        fmax[p] = std::max(fmax[p], j + 1);
-                    }
-                }
-                bool changed = false;
-                for (int p = 0; p < 64; ++p) { changed |= fnext[p] != fmin[p]; fmin[p] = fnext[p]; }
-                if (!changed) break;
-                if (round > G0 + 2) { record_error(P.err, ST_DEVICE_TIMEOUT, W_RA2, i); break; }
-            }
-            for (uint32_t j = 0; j < G0; ++j) {
-                if (!act[j]) continue;
-                const RaStep& S1 = st[j];
-                P.lifetime[8 * j] = S1.cleared | S1.rdm;
-                auto upd = [&](uint32_t v, uint32_t reg) {
-                    bool later = false;
-                    for (int p = 0; p < 64; ++p) later |= snap[p] == v && fmax[p] > j + 1;
-                    P.symreg[v - 64] = reg;
-                    P.symswp[v - 64] = later ? 0xFFFFFFFFu : 0u;
-                    P.stamp[v - 64] = i + 1;
-                };
-                if (s32(S1.ord) > 63) upd(S1.ord, S1.rdr);
-                if (s32(S1.r1) > 63) upd(S1.r1, S1.r1r);
-                if (s32(S1.r2) > 63) upd(S1.r2, S1.r2r);
-                auto kmax = [&](uint32_t p, unsigned long long k) { if (k > r0key[p]) r0key[p] = k; };
-                if (S1.ord != 0) kmax(S1.rdr & 63, (static_cast<unsigned long long>(j + 1) << 32) | S1.ord);
-                if (S1.r1r != S1.rdr && s32(S1.r1r) >= 0 && S1.r1r < 64) kmax(S1.r1r, (static_cast<unsigned long long>(j + 1) << 32) | 0xFFFFFFFFull);
-                if (S1.r2r != S1.rdr && s32(S1.r2r) >= 0 && S1.r2r < 64) kmax(S1.r2r, (static_cast<unsigned long long>(j + 1) << 32) | 0xFFFFFFFFull);
-            }
-            for (int p = 0; p < 64; ++p) {
-                if (fmin[p] != 0xFFFFFFFFu) {
-                    const uint32_t v = snap[p];
-                    if (s32(v - 64) >= 0 && P.stamp[v - 64] != i + 1) P.symswp[v - 64] = 0xFFFFFFFFu;
-                }
-                if (r0key[p] != 0) R0[p] = static_cast<uint32_t>(r0key[p]);
-            }
-        }
-    }
-
     uint32_t hm_cache_k = g_cache_k;
 
     // The lane-0 pass with the same phase functions as k_ra_lane0_cached.
-    void lane0_cached(uint32_t S, uint32_t K) {
+    void lane0_cached(uint32_t S, uint32_t K, bool hashed) {
         const uint32_t G0 = (P.F + 7) / 8;
+        const Prog Psave = P;
+        if (hashed) P.defpos = nullptr;
         Ra2Shared sh{};
         std::vector<uint32_t> cur(3 * G0), tag(static_cast<size_t>(G0) * K);
-        std::vector<uint16_t> val(static_cast<size_t>(G0) * K);
+        std::vector<uint32_t> val(static_cast<size_t>(G0) * K);
         const SymCache c{tag.data(), val.data(), K};
         std::vector<Ra2Slot> L(G0);
         for (uint32_t j = 0; j < G0; ++j) {
@@ -221,7 +148,7 @@ struct Model {
             ra2_slot_init(P, c, L[j], j, j);
         }
         for (int p = 0; p < 64; ++p) { sh.R0[p] = 0xFFFFFFFFu; sh.R0own[p] = 0xFFFFFFFFu; }
-        if (S > 0) for (uint32_t p = 0; p < 64; ++p) ra2_begin_p(sh, 0, p, P.trig_min[p], P.trig_max[p]);
+        if (S > 0) for (uint32_t p = 0; p < 64; ++p) ra2_begin_p(sh, 0, p, P.trig_min[p], P.trig_max[p], hashed);
         for (uint32_t i = 0; i < S; ++i) {
             bool in_row0 = false;
             for (uint32_t j = 0; j < G0; ++j) {
@@ -242,17 +169,18 @@ struct Model {
                 }
             }
             for (uint32_t j = 0; j < G0; ++j) ra2_apply(P, c, sh, L[j], j, i);
-            for (uint32_t p = 0; p < 64; ++p) snap_clear_next(sh, i, p);
+            if (hashed) for (uint32_t p = 0; p < 64; ++p) snap_clear_next(sh, i, p);
             for (uint32_t p = 0; p < 64; ++p) {
                 ra2_end_p(P, c, sh, p, cur.data());
             }
             if (i + 1 < S) {
                 for (uint32_t p = 0; p < 64; ++p) {
                     ra2_begin_p(sh, i + 1, p, P.trig_min[static_cast<size_t>(i + 1) * 64 + p],
-                                P.trig_max[static_cast<size_t>(i + 1) * 64 + p]);
+                                P.trig_max[static_cast<size_t>(i + 1) * 64 + p], hashed);
                 }
             }
         }
+        P = Psave;
     }
 
     int run(const uint8_t* type, const uint8_t* rtype, const int32_t* parent, const int32_t* depth,
@@ -321,17 +249,21 @@ struct Model {
         trig_min.ensure(static_cast<size_t>(std::max<uint32_t>(S, 1)) * 64, 0xFFFFFFFFu);
         trig_max.ensure(static_cast<size_t>(std::max<uint32_t>(S, 1)) * 64, 0u);
         bind();
-        bool cross = false;
-        for (uint32_t i = 0; i < W; ++i) cross |= st_ra_cross(P, i);
+        defpos.ensure(wb8);
+        bind();
+        uint32_t flagbits = 0;
+        for (uint32_t i = 0; i < W; ++i) flagbits |= st_ra_cross(P, i, stamp.p);
         const uint32_t G0 = (F + 7) / 8;
-        if (cross || G0 > 8192u) {
+        if ((flagbits & 1u) || G0 > 8192u) {
             st_ra_serial(P, stamp.p);
         } else {
-            std::vector<uint32_t> tag(64), dummy;
-            std::vector<uint16_t> val(64);
+            std::vector<uint32_t> tag(64), val(64);
             const SymCache c1{tag.data(), val.data(), 64};
-            for (uint32_t f = 0; f < F; ++f) if (f & 7u) ra_free_function_cached(P, c1, 0, f);
-            lane0_cached(S, hm_cache_k);
+            Prog Pfree = P;
+            Pfree.defpos = nullptr;
+            for (uint32_t f = 0; f < F; ++f) if (f & 7u) ra_free_function_cached(Pfree, c1, 0, f);
+            lane0_cached(S, hm_cache_k, (flagbits & 2u) != 0 || g_force_hashed);
+            g_last_hashed = (flagbits & 2u) != 0;
         }
         for (uint32_t v = 0; v < W; ++v) st_ra_spill(P, v);
         exclusive_scan(wb8, [&](uint32_t i) { return st_ra_count(P, i); }, roffs.p);
@@ -402,6 +334,8 @@ int ptlhm_compile(const uint8_t* type, const uint8_t* rtype, const int32_t* pare
 }
 
 void ptlhm_set_cache_entries(uint32_t k) { g_cache_k = k; }
+void ptlhm_set_hashed(int on) { g_force_hashed = on != 0; }
+int ptlhm_last_hashed(void) { return g_last_hashed ? 1 : 0; }
 
 void ptlhm_free(ptlhm_buf* bufs, int nbufs) {
     for (int k = 0; k < nbufs; ++k) { std::free(bufs[k].p); bufs[k].p = nullptr; bufs[k].n = 0; }

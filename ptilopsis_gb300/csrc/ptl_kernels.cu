@@ -403,149 +403,13 @@ __global__ void k_opt_sweep(Prog P) {
 __global__ void k_opt_final(Prog P) { PTL_FOR(i, P.wb8) st_opt_final(P, i); }
 
 // ------------------------------------------------------------------ regalloc
-__global__ void k_ra_free(Prog P) {
-    PTL_FOR(f, P.F) {
-        if ((f & 7u) != 0) st_ra_free_function(P, f);
-    }
-}
-
-// Lane-0 functions (f % 8 == 0) in lock-step, one CTA.  Within a step the reference
-// visits groups of 8 functions in order; a lane-0 function's symbols are marked
-// swapped through row 0 of the register state by any function whose register operand
-// was live.  Per step:
-//   1. snapshot row 0 (the reference copies the register state at each step);
-//   2. each active function computes its step; a symbol reads as swapped if a function
-//      of an earlier group triggered the physical register holding it.  Earlier
-//      lane-0 triggers depend on the same computation, so the CTA iterates until the
-//      per-register minimum trigger group stops changing (a DAG in group order);
-//   3. symbol updates: a symbol updated by its owner ends swapped only if a later
-//      group also triggered it; other triggered symbols end swapped;
-//   4. row 0 takes, per physical register, the write of the highest group.
-constexpr int kRaThreads = 512;
-constexpr int kRaPerThread = 16;
-
-__device__ __forceinline__ bool ra_marked(const uint32_t* snap, const uint32_t* fmin, uint32_t v, uint32_t limit) {
-    for (int p = 0; p < 64; ++p) {
-        if (snap[p] == v && fmin[p] <= limit) return true;
-    }
-    return false;
-}
-
-__global__ void __launch_bounds__(kRaThreads) k_ra_lane0(Prog P, uint32_t S0) {
-    __shared__ uint32_t R0[64], snap[64], fmin[64], fnext[64], fmax[64], omin[64], omax[64];
-    __shared__ unsigned long long r0key[64];
-    __shared__ int s_changed;
-    const uint32_t G0 = (P.F + 7u) / 8u;
-    const uint32_t tid = threadIdx.x;
-    if (G0 > static_cast<uint32_t>(kRaThreads) * kRaPerThread) {
-        if (tid == 0) record_error(P.err, ST_UNSUPPORTED, W_RA2, G0);
-        return;
-    }
-    if (tid < 64) R0[tid] = 0xFFFFFFFFu;
-    __syncthreads();
-    for (uint32_t i = 0; i < S0; ++i) {
-        if (tid < 64) {
-            snap[tid] = R0[tid];
-            omin[tid] = P.trig_min[static_cast<size_t>(i) * 64u + tid];
-            omax[tid] = P.trig_max[static_cast<size_t>(i) * 64u + tid];
-            fmin[tid] = omin[tid];
-            r0key[tid] = 0;
-        }
-        RaStep st[kRaPerThread];
-        bool act[kRaPerThread];
-#pragma unroll
-        for (int q = 0; q < kRaPerThread; ++q) {
-            const uint32_t j = tid + static_cast<uint32_t>(q) * kRaThreads;
-            act[q] = j < G0 && ra_load(P, 8u * j, i, st[q]);
-            if (act[q] && (st[q].ins == 0x000000EFu || !ra_own(P, 8u * j, st[q].r1) ||
-                           !ra_own(P, 8u * j, st[q].r2) || !ra_own(P, 8u * j, st[q].ord))) {
-                record_error(P.err, ST_UNSUPPORTED, W_RA2, P.fn_start0[8u * j] + i);
-                act[q] = false;
-            }
-        }
-        __syncthreads();
-        for (uint32_t round = 0;; ++round) {
-            if (tid < 64) { fnext[tid] = omin[tid]; fmax[tid] = omax[tid]; }
-            if (tid == 0) s_changed = 0;
-            __syncthreads();
-#pragma unroll
-            for (int q = 0; q < kRaPerThread; ++q) {
-                if (!act[q]) continue;
-                const uint32_t j = tid + static_cast<uint32_t>(q) * kRaThreads;
-                RaStep& S = st[q];
-                uint32_t r1reg = 0, r2reg = 0;
-                bool r1s = false, r2s = false;
-                if (s32(S.r1) > 63) {
-                    r1reg = P.symreg[S.r1 - 64u];
-                    r1s = P.symswp[S.r1 - 64u] != 0 || ra_marked(snap, fmin, S.r1, j);
-                }
-                if (s32(S.r2) > 63) {
-                    r2reg = P.symreg[S.r2 - 64u];
-                    r2s = P.symswp[S.r2 - 64u] != 0 || ra_marked(snap, fmin, S.r2, j);
-                }
-                ra_compute(S, P.lifetime[8u * j], r1reg, r1s, r2reg, r2s);
-                uint64_t t = S.trig;
-                while (t) {
-                    const uint32_t p = static_cast<uint32_t>(__ffsll(static_cast<long long>(t)) - 1);
-                    t &= t - 1;
-                    atomicMin(&fnext[p], j + 1u);
-                    atomicMax(&fmax[p], j + 1u);
-                }
-            }
-            __syncthreads();
-            if (tid < 64) {
-                if (fnext[tid] != fmin[tid]) s_changed = 1;
-                fmin[tid] = fnext[tid];
-            }
-            __syncthreads();
-            if (!s_changed) break;
-            if (round > G0 + 2u) {
-                if (tid == 0) record_error(P.err, ST_DEVICE_TIMEOUT, W_RA2, i);
-                break;
-            }
-        }
-        // symbol updates of each function's own registers
-#pragma unroll
-        for (int q = 0; q < kRaPerThread; ++q) {
-            if (!act[q]) continue;
-            const uint32_t j = tid + static_cast<uint32_t>(q) * kRaThreads;
-            const RaStep& S = st[q];
-            P.lifetime[8u * j] = S.cleared | S.rdm;
-            auto upd = [&](uint32_t v, uint32_t reg) {
-                bool later = false;
-                for (int p = 0; p < 64; ++p) later |= snap[p] == v && fmax[p] > j + 1u;
-                P.symreg[v - 64u] = reg;
-                P.symswp[v - 64u] = later ? 0xFFFFFFFFu : 0u;
-                P.stamp[v - 64u] = i + 1u;
-            };
-            if (s32(S.ord) > 63) upd(S.ord, S.rdr);
-            if (s32(S.r1) > 63) upd(S.r1, S.r1r);
-            if (s32(S.r2) > 63) upd(S.r2, S.r2r);
-            if (S.ord != 0) atomicMax(&r0key[S.rdr & 63u], (static_cast<unsigned long long>(j + 1u) << 32) | S.ord);
-            if (S.r1r != S.rdr && s32(S.r1r) >= 0 && S.r1r < 64u)
-                atomicMax(&r0key[S.r1r], (static_cast<unsigned long long>(j + 1u) << 32) | 0xFFFFFFFFull);
-            if (S.r2r != S.rdr && s32(S.r2r) >= 0 && S.r2r < 64u)
-                atomicMax(&r0key[S.r2r], (static_cast<unsigned long long>(j + 1u) << 32) | 0xFFFFFFFFull);
-        }
-        __syncthreads();
-        if (tid < 64) {
-            if (fmin[tid] != 0xFFFFFFFFu) {
-                const uint32_t v = snap[tid];
-                if (s32(v - 64u) >= 0 && P.stamp[v - 64u] != i + 1u) P.symswp[v - 64u] = 0xFFFFFFFFu;
-            }
-            if (r0key[tid] != 0) R0[tid] = static_cast<uint32_t>(r0key[tid]);
-        }
-        __syncthreads();
-    }
-}
-
 // Independent functions with an on-chip symbol cache per thread.
 constexpr int kRaFreeThreads = 64;
 constexpr uint32_t kRaFreeK = 64;
 
 __global__ void __launch_bounds__(kRaFreeThreads) k_ra_free_cached(Prog P) {
     __shared__ uint32_t tag[kRaFreeThreads * kRaFreeK];
-    __shared__ uint16_t val[kRaFreeThreads * kRaFreeK];
+    __shared__ uint32_t val[kRaFreeThreads * kRaFreeK];
     const SymCache c{tag, val, kRaFreeK};
     // non-lane-0 functions only: function index skips multiples of 8
     const uint32_t k = blockIdx.x * kRaFreeThreads + threadIdx.x;
@@ -553,8 +417,17 @@ __global__ void __launch_bounds__(kRaFreeThreads) k_ra_free_cached(Prog P) {
     if (f < P.F) ra_free_function_cached(P, c, threadIdx.x, f);
 }
 
-// Lane-0 functions in lock-step (see ptl_ra.cuh).  One CTA; thread t runs slots
-// t, t+T, ... (Q per thread); slot = group index.
+// Lane-0 functions (f % 8 == 0) in lock-step, one CTA; thread t runs slots t, t+T, ...
+// (Q per thread); slot = group index.  Per step:
+//   1. each active function computes its step; a symbol reads as swapped if a function
+//      of an earlier group triggered the physical register holding it in row 0.  The
+//      other functions' triggers are known (trig_min/trig_max); earlier lane-0 triggers
+//      depend on the same computation, so when an operand sits in row 0 the CTA
+//      iterates until the per-register minimum trigger group stops changing (a DAG in
+//      group order);
+//   2. symbol updates: a symbol updated by its owner ends swapped only if a later group
+//      also triggered it; other triggered symbols end swapped;
+//   3. row 0 takes, per physical register, the write of the highest group.
 template <int Q>
 __global__ void __launch_bounds__(1024) k_ra_lane0_cached(Prog P, uint32_t S, uint32_t K) {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -562,9 +435,10 @@ __global__ void __launch_bounds__(1024) k_ra_lane0_cached(Prog P, uint32_t S, ui
     const uint32_t G0 = (P.F + 7u) / 8u;
     uint32_t* cur = reinterpret_cast<uint32_t*>(smem + sizeof(Ra2Shared));
     uint32_t* ctag = cur + 3u * G0;
-    uint16_t* cval = reinterpret_cast<uint16_t*>(ctag + G0 * K);
+    uint32_t* cval = ctag + G0 * K;
     const SymCache c{ctag, cval, K};
     const uint32_t tid = threadIdx.x, T = blockDim.x;
+    const bool hashed = P.defpos == nullptr;
     if (T < 64u) {  // the row-0 phases need a thread per physical register
         if (tid == 0) record_error(P.err, ST_UNSUPPORTED, W_RA2, T);
         return;
@@ -588,7 +462,7 @@ __global__ void __launch_bounds__(1024) k_ra_lane0_cached(Prog P, uint32_t S, ui
     }
     __syncthreads();
     if (tid < 64 && S > 0) {
-        ra2_begin_p(sh, 0, tid, P.trig_min[tid], P.trig_max[tid]);
+        ra2_begin_p(sh, 0, tid, P.trig_min[tid], P.trig_max[tid], hashed);
         if (S > 1) { tmin = P.trig_min[64u + tid]; tmax = P.trig_max[64u + tid]; }
     }
     __syncthreads();
@@ -633,12 +507,12 @@ __global__ void __launch_bounds__(1024) k_ra_lane0_cached(Prog P, uint32_t S, ui
             const uint32_t j = tid + static_cast<uint32_t>(q) * T;
             if (j < G0) ra2_apply(P, c, sh, L[q], j, i);
         }
-        if (tid < 64) snap_clear_next(sh, i, tid);
+        if (hashed && tid < 64) snap_clear_next(sh, i, tid);
         __syncthreads();
         if (tid < 64) {
             ra2_end_p(P, c, sh, tid, cur);
             if (i + 1 < S) {
-                ra2_begin_p(sh, i + 1, tid, tmin, tmax);
+                ra2_begin_p(sh, i + 1, tid, tmin, tmax, hashed);
                 if (i + 2 < S) {
                     tmin = P.trig_min[static_cast<size_t>(i + 2) * 64u + tid];
                     tmax = P.trig_max[static_cast<size_t>(i + 2) * 64u + tid];
@@ -649,10 +523,13 @@ __global__ void __launch_bounds__(1024) k_ra_lane0_cached(Prog P, uint32_t S, ui
     }
 }
 
+// flags[1]: functions share symbols; flags[2]: a lane-0 virtual register has two
+// definitions.  stamp counts the definitions (zeroed before).
 __global__ void k_ra_cross(Prog P) {
-    bool any = false;
-    PTL_FOR(i, P.W) any |= st_ra_cross(P, i);
-    if (__syncthreads_or(any) && threadIdx.x == 0) P.flags[1] = 1;
+    uint32_t any = 0;
+    PTL_FOR(i, P.W) any |= st_ra_cross(P, i, P.stamp);
+    if (__syncthreads_or(any & 1u) && threadIdx.x == 0) P.flags[1] = 1;
+    if (__syncthreads_or(any & 2u) && threadIdx.x == 0) P.flags[2] = 1;
 }
 __global__ void k_ra_serial(Prog P) {
     if (blockIdx.x == 0 && threadIdx.x == 0) st_ra_serial(P, P.stamp);
@@ -808,15 +685,23 @@ cudaError_t run_optimize(const Prog& P, cudaStream_t s, uint32_t* sweeps_out) {
     return cudaGetLastError();
 }
 
-cudaError_t run_regalloc_steps(const Prog& P, cudaStream_t s, bool* serial_out) {
+cudaError_t run_regalloc_steps(const Prog& P, cudaStream_t s, bool* serial_out, bool row0_hash) {
     // Programs whose functions share symbols need the reference's serial order.
-    cudaMemsetAsync(P.flags + 1, 0, sizeof(uint32_t), s);
+    cudaMemsetAsync(P.flags + 1, 0, 2 * sizeof(uint32_t), s);
+    cudaMemsetAsync(P.stamp, 0, sizeof(uint32_t) * P.W, s);
+    cudaMemsetAsync(P.defpos, 0, P.W, s);
     g_launches++;
     k_ra_cross<<<grid_for(P.W), kThreads, 0, s>>>(P);
-    uint32_t cross = 0;
-    cudaMemcpyAsync(&cross, P.flags + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
+    uint32_t fl[2] = {0, 0};
+    cudaMemcpyAsync(fl, P.flags + 1, sizeof(fl), cudaMemcpyDeviceToHost, s);
     const cudaError_t e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return e;
+    const uint32_t cross = fl[0];
+    // independent functions never need the definition positions; the lane-0 pass hashes
+    // row 0 when a virtual register has two definitions
+    Prog Pfree = P, P0 = P;
+    Pfree.defpos = nullptr;
+    if (fl[1] || row0_hash) P0.defpos = nullptr;
     const uint32_t G0 = (P.F + 7u) / 8u;
     if (cross || G0 > 8192u) {
         // functions share symbols (or too many lane-0 functions for one CTA): serial path
@@ -826,7 +711,7 @@ cudaError_t run_regalloc_steps(const Prog& P, cudaStream_t s, bool* serial_out) 
         const uint32_t free_fns = P.F - G0;
         if (free_fns) {
             g_launches++;
-            k_ra_free_cached<<<(free_fns + kRaFreeThreads - 1) / kRaFreeThreads, kRaFreeThreads, 0, s>>>(P);
+            k_ra_free_cached<<<(free_fns + kRaFreeThreads - 1) / kRaFreeThreads, kRaFreeThreads, 0, s>>>(Pfree);
         }
         // at least 64 threads: one per physical register in the row-0 phases
         const uint32_t T = G0 <= 1024u ? std::max(64u, (G0 + 31u) & ~31u) : 1024u;
@@ -834,27 +719,27 @@ cudaError_t run_regalloc_steps(const Prog& P, cudaStream_t s, bool* serial_out) 
         // symbol cache entries per function: the largest power of two within ~160 KB
         uint32_t K = 64;
         const size_t fixed = sizeof(Ra2Shared) + 12ull * G0;
-        while (K > 1 && fixed + static_cast<size_t>(G0) * K * 6u > 160u * 1024u) K >>= 1;
-        const size_t smem = fixed + static_cast<size_t>(G0) * K * 6u + 16;
+        while (K > 1 && fixed + static_cast<size_t>(G0) * K * 8u > 160u * 1024u) K >>= 1;
+        const size_t smem = fixed + static_cast<size_t>(G0) * K * 8u + 16;
         g_launches++;
         cudaError_t ce = cudaSuccess;
         switch (Q) {
             case 1:
                 ce = cudaFuncSetAttribute(k_ra_lane0_cached<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-                k_ra_lane0_cached<1><<<1, T, smem, s>>>(P, P.S, K);
+                k_ra_lane0_cached<1><<<1, T, smem, s>>>(P0, P.S, K);
                 break;
             case 2:
                 ce = cudaFuncSetAttribute(k_ra_lane0_cached<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-                k_ra_lane0_cached<2><<<1, T, smem, s>>>(P, P.S, K);
+                k_ra_lane0_cached<2><<<1, T, smem, s>>>(P0, P.S, K);
                 break;
             case 3:
             case 4:
                 ce = cudaFuncSetAttribute(k_ra_lane0_cached<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-                k_ra_lane0_cached<4><<<1, T, smem, s>>>(P, P.S, K);
+                k_ra_lane0_cached<4><<<1, T, smem, s>>>(P0, P.S, K);
                 break;
             default:
                 ce = cudaFuncSetAttribute(k_ra_lane0_cached<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-                k_ra_lane0_cached<8><<<1, T, smem, s>>>(P, P.S, K);
+                k_ra_lane0_cached<8><<<1, T, smem, s>>>(P0, P.S, K);
                 break;
         }
         if (ce != cudaSuccess) return ce;

@@ -50,7 +50,7 @@ cudaError_t run_depth_sort(const Prog& P, const SortScratch& ss, cudaStream_t s,
 
 void launch_gen(const Prog& P, cudaStream_t s);
 cudaError_t run_optimize(const Prog& P, cudaStream_t s, uint32_t* sweeps_out);
-cudaError_t run_regalloc_steps(const Prog& P, cudaStream_t s, bool* serial_out);
+cudaError_t run_regalloc_steps(const Prog& P, cudaStream_t s, bool* serial_out, bool row0_hash);
 void launch_regalloc_count_scan(const Prog& P, const ScanScratch& sc, cudaStream_t s);
 void launch_regalloc_emit(const Prog& P, cudaStream_t s);
 void launch_fixjumps_scan(const Prog& P, const ScanScratch& sc, cudaStream_t s);

@@ -17,7 +17,7 @@ namespace ptl {
 // ---------------------------------------------------------------- symbol caches
 struct SymCache {
     uint32_t* tag;   // [slots * K] virtual register held, 0 = empty
-    uint16_t* val;   // (swapped << 8) | physical register
+    uint32_t* val;   // physical register | swapped << 8 | (row-0 position + 1) << 16
     uint32_t K;      // entries per function (power of two)
 };
 
@@ -29,23 +29,41 @@ PTL_HD void cache_reset(const SymCache& c, uint32_t slot) {
 PTL_HD void sym_read(const Prog& P, const SymCache& c, uint32_t slot, uint32_t v, uint32_t* reg, bool* swp) {
     const uint32_t e = slot * c.K + ((v - 64u) & (c.K - 1u));
     if (c.tag[e] == v) {
-        const uint16_t x = c.val[e];
+        const uint32_t x = c.val[e];
         *reg = x & 0xFFu;
-        *swp = (x >> 8) != 0;
+        *swp = ((x >> 8) & 1u) != 0;
         return;
     }
     *reg = P.symreg[v - 64u];
     *swp = P.symswp[v - 64u] != 0;
     c.tag[e] = v;
-    c.val[e] = static_cast<uint16_t>((*reg & 0xFFu) | (*swp ? 0x100u : 0u));
+    c.val[e] = (*reg & 0xFFu) | (*swp ? 0x100u : 0u) | (P.defpos ? static_cast<uint32_t>(P.defpos[v - 64u]) << 16 : 0u);
 }
 
-PTL_HD void sym_write(const Prog& P, const SymCache& c, uint32_t slot, uint32_t v, uint32_t reg, bool swp) {
+// Row-0 position (+1, 0 = none) where v's definition wrote it (lane-0 functions).
+PTL_HD uint32_t sym_defpos(const Prog& P, const SymCache& c, uint32_t slot, uint32_t v) {
+    const uint32_t e = slot * c.K + ((v - 64u) & (c.K - 1u));
+    if (c.tag[e] == v) return c.val[e] >> 16;
+    return P.defpos[v - 64u];
+}
+
+// Owner update of v.  defp = row-0 position + 1 of a definition, 0 for a use (kept).
+PTL_HD void sym_write(const Prog& P, const SymCache& c, uint32_t slot, uint32_t v, uint32_t reg, bool swp,
+                      uint32_t defp = 0) {
     P.symreg[v - 64u] = reg;
     P.symswp[v - 64u] = swp ? 0xFFFFFFFFu : 0u;
     const uint32_t e = slot * c.K + ((v - 64u) & (c.K - 1u));
+    uint32_t keep = 0;
+    if (defp) {
+        if (P.defpos) P.defpos[v - 64u] = static_cast<uint8_t>(defp);
+        keep = defp << 16;
+    } else if (c.tag[e] == v) {
+        keep = c.val[e] & 0xFFFF0000u;
+    } else if (P.defpos) {
+        keep = static_cast<uint32_t>(P.defpos[v - 64u]) << 16;
+    }
     c.tag[e] = v;
-    c.val[e] = static_cast<uint16_t>((reg & 0xFFu) | (swp ? 0x100u : 0u));
+    c.val[e] = (reg & 0xFFu) | (swp ? 0x100u : 0u) | keep;
 }
 
 // A swap mark: global memory, plus the owner's cached copy if it holds v.
@@ -53,7 +71,7 @@ PTL_HD void sym_mark(const Prog& P, const SymCache& c, uint32_t owner_slot, uint
     P.symswp[v - 64u] = 0xFFFFFFFFu;
     if (owner_slot == 0xFFFFFFFFu) return;
     const uint32_t e = owner_slot * c.K + ((v - 64u) & (c.K - 1u));
-    if (c.tag[e] == v) c.val[e] = static_cast<uint16_t>(c.val[e] | 0x100u);
+    if (c.tag[e] == v) c.val[e] |= 0x100u;
 }
 
 // ---------------------------------------------------------------- independent functions
@@ -124,8 +142,8 @@ struct Ra2Slot {
 
 PTL_HD uint32_t snap_hash(uint32_t v) { return (v * 2654435761u) >> 25; }
 
-// Row-0 positions holding v at the start of step i (v > 63).
-PTL_HD uint64_t snap_positions(const Ra2Shared& sh, uint32_t i, uint32_t v) {
+// Row-0 positions holding v at the start of step i (v > 63), from the hash of row 0.
+PTL_HD uint64_t snap_positions_hashed(const Ra2Shared& sh, uint32_t i, uint32_t v) {
     const uint32_t t = i & 1u;
     uint32_t h = snap_hash(v);
     for (uint32_t probe = 0; probe < kSnapHash; ++probe) {
@@ -168,6 +186,17 @@ PTL_HD void snap_clear_next(Ra2Shared& sh, uint32_t i, uint32_t p) {
     }
 }
 
+// Row-0 positions holding v: a lane-0 value enters row 0 only where its definition put
+// it, so one compare answers the question -- unless two instructions define the same
+// virtual register, for which the row-0 hash is built instead (P.defpos == null).
+PTL_HD uint64_t snap_positions(const Prog& P, const SymCache& c, const Ra2Shared& sh, uint32_t slot, uint32_t i,
+                               uint32_t v) {
+    if (!P.defpos) return snap_positions_hashed(sh, i, v);
+    const uint32_t d = sym_defpos(P, c, slot, v);
+    if (d == 0) return 0;
+    return sh.snap[d - 1u] == v ? (1ull << (d - 1u)) : 0ull;
+}
+
 // Whether a symbol at row-0 positions m is marked by a group before j (g1 <= j).
 PTL_HD bool marked_before(const Ra2Shared& sh, uint64_t m, uint32_t j, bool with_lane0) {
     for (; m; m &= m - 1) {
@@ -190,10 +219,10 @@ PTL_HD void ra2_slot_init(const Prog& P, const SymCache& c, Ra2Slot& L, uint32_t
 
 // Step start for row-0 position p (64 threads); tmin/tmax are the step's trigger
 // records of the other functions (loaded a step ahead).
-PTL_HD void ra2_begin_p(Ra2Shared& sh, uint32_t i, uint32_t p, uint32_t tmin, uint32_t tmax) {
+PTL_HD void ra2_begin_p(Ra2Shared& sh, uint32_t i, uint32_t p, uint32_t tmin, uint32_t tmax, bool hashed) {
     sh.snap[p] = sh.R0[p];
     sh.snapown[p] = sh.R0own[p];
-    if (s32(sh.R0[p] - 64u) >= 0) snap_insert(sh, i, sh.R0[p], p);
+    if (hashed && s32(sh.R0[p] - 64u) >= 0) snap_insert(sh, i, sh.R0[p], p);
     sh.omin[p] = tmin;
     sh.omax[p] = tmax;
     sh.lcur[p] = 0xFFFFFFFFu;
@@ -246,11 +275,11 @@ PTL_HD bool ra2_compute0(const Prog& P, const SymCache& c, Ra2Shared& sh, Ra2Slo
     L.m1 = L.m2 = 0;
     if (s32(S.r1) > 63) {
         sym_read(P, c, slot, S.r1, &L.r1reg, &L.r1stored);
-        L.m1 = snap_positions(sh, i, S.r1);
+        L.m1 = snap_positions(P, c, sh, slot, i, S.r1);
     }
     if (s32(S.r2) > 63) {
         sym_read(P, c, slot, S.r2, &L.r2reg, &L.r2stored);
-        L.m2 = snap_positions(sh, i, S.r2);
+        L.m2 = snap_positions(P, c, sh, slot, i, S.r2);
     }
     L.r1m = marked_before(sh, L.m1, L.j, false);
     L.r2m = marked_before(sh, L.m2, L.j, false);
@@ -295,20 +324,25 @@ PTL_HD void ra2_apply(const Prog& P, const SymCache& c, Ra2Shared& sh, Ra2Slot& 
     L.lifetime = S.cleared | S.rdm;
     const uint32_t g1 = L.j + 1u;
     auto later = [&](uint32_t v) {
-        for (uint64_t m = snap_positions(sh, i, v); m; m &= m - 1) {
+        for (uint64_t m = snap_positions(P, c, sh, slot, i, v); m; m &= m - 1) {
             const uint32_t p = ctz64(m);
             const uint32_t g = sh.omax[p] > sh.lmax[p] ? sh.omax[p] : sh.lmax[p];
             if (g > g1) return true;
         }
         return false;
     };
-    // the reference's order: rd, rs1, rs2 (a later write of the same symbol wins)
-    if (s32(S.ord) > 63) sym_write(P, c, slot, S.ord, S.rdr, false);
+    // the swap flags need the row-0 positions before this step's updates
+    const bool l_ord = s32(S.ord) > 63 && later(S.ord);
+    const bool l_r1 = s32(S.r1) > 63 && later(S.r1);
+    const bool l_r2 = s32(S.r2) > 63 && later(S.r2);
+    // the reference's order: rd, rs1, rs2 (a later write of the same symbol wins); a
+    // definition records the row-0 position it writes (when it writes row 0 at all)
+    if (s32(S.ord) > 63) sym_write(P, c, slot, S.ord, S.rdr, false, (S.rdr & 63u) + 1u);
     if (s32(S.r1) > 63) sym_write(P, c, slot, S.r1, S.r1r, false);
     if (s32(S.r2) > 63) sym_write(P, c, slot, S.r2, S.r2r, false);
-    if (s32(S.ord) > 63 && later(S.ord)) sym_write(P, c, slot, S.ord, P.symreg[S.ord - 64u], true);
-    if (s32(S.r1) > 63 && later(S.r1)) sym_write(P, c, slot, S.r1, P.symreg[S.r1 - 64u], true);
-    if (s32(S.r2) > 63 && later(S.r2)) sym_write(P, c, slot, S.r2, P.symreg[S.r2 - 64u], true);
+    if (l_ord) sym_write(P, c, slot, S.ord, P.symreg[S.ord - 64u], true);
+    if (l_r1) sym_write(P, c, slot, S.r1, P.symreg[S.r1 - 64u], true);
+    if (l_r2) sym_write(P, c, slot, S.r2, P.symreg[S.r2 - 64u], true);
     const unsigned long long key = static_cast<unsigned long long>(g1) << 32;
     if (S.ord != 0) at_max_u64(&sh.r0key[S.rdr & 63u], key | S.ord);
     if (S.r1r != S.rdr && s32(S.r1r) >= 0 && S.r1r < 64u) at_max_u64(&sh.r0key[S.r1r], key | 0xFFFFFFFFull);

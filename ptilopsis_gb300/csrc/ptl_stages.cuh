@@ -126,6 +126,7 @@ struct Prog {
     uint32_t* symreg;
     uint32_t* symswp;
     uint32_t* stamp;
+    uint8_t* defpos;      // row-0 position + 1 of each lane-0 definition; null: use the row-0 hash
     unsigned long long* lifetime;
     uint32_t* trig_min;   // [S][64] min group+1 of non-lane-0 triggers, 0xFFFFFFFF = none
     uint32_t* trig_max;   // [S][64] max group+1, 0 = none
@@ -634,51 +635,31 @@ PTL_HD bool ra_own(const Prog& P, uint32_t f, uint32_t r) {
     return v >= st && v - st < P.fn_size0[f];
 }
 
-// Functions outside lane 0 (f % 8 != 0): their symbols are never marked swapped (marks
-// go to the virtual registers held in lane 0's row of the register state), so each is
-// a sequential loop over its own instructions.  Trigger records feed the lane-0 pass.
-PTL_HD void st_ra_free_function(const Prog& P, uint32_t f) {
-    unsigned long long lifetime = 0x1Full;
-    const uint32_t g1 = f / 8u + 1u;
-    for (uint32_t i = 0;; ++i) {
-        RaStep S;
-        if (!ra_load(P, f, i, S)) break;
-        if (S.ins == 0x000000EFu || !ra_own(P, f, S.r1) || !ra_own(P, f, S.r2) || !ra_own(P, f, S.ord)) {
-            record_error(P.err, ST_UNSUPPORTED, W_RA1, P.fn_start0[f] + i);
-            return;
-        }
-        const uint32_t r1reg = s32(S.r1) > 63 ? P.symreg[S.r1 - 64u] : 0u;
-        const uint32_t r2reg = s32(S.r2) > 63 ? P.symreg[S.r2 - 64u] : 0u;
-        ra_compute(S, lifetime, r1reg, false, r2reg, false);
-        lifetime = S.cleared | S.rdm;
-        if (s32(S.ord) > 63) { P.symreg[S.ord - 64u] = S.rdr; P.symswp[S.ord - 64u] = 0; }
-        if (s32(S.r1) > 63) { P.symreg[S.r1 - 64u] = S.r1r; P.symswp[S.r1 - 64u] = 0; }
-        if (s32(S.r2) > 63) { P.symreg[S.r2 - 64u] = S.r2r; P.symswp[S.r2 - 64u] = 0; }
-        uint64_t t = S.trig;
-        while (t) {
-            const uint32_t p = ctz64(t);
-            t &= t - 1;
-            at_min_u32(&P.trig_min[static_cast<size_t>(i) * 64u + p], g1);
-            at_max_u32(&P.trig_max[static_cast<size_t>(i) * 64u + p], g1);
-        }
-    }
-}
-
 // A virtual register names an instruction of the program (checked where it is read).
 PTL_HD bool ra_in_range(const Prog& P, uint32_t r) { return !(s32(r) > 63) || r - 64u < P.W; }
 
-// Whether instruction i names a virtual register outside its own function.  The
+// Whether instruction i names a virtual register outside its own function (bit 0).  The
 // reference lets that happen when an instruction number lands in a register operand
 // (a child of a float-as-int call argument propagates its instruction count, which
 // reads as virtual register count-64); such programs couple functions through the
-// symbol table and take the serial path below.
-PTL_HD bool st_ra_cross(const Prog& P, uint32_t i) {
+// symbol table and take the serial path below.  Bit 1: a lane-0 instruction defines a
+// virtual register that an earlier-counted instruction also defines (defcnt counts the
+// definitions, zeroed beforehand); the lane-0 pass then finds row-0 values by hashing.
+PTL_HD uint32_t st_ra_cross(const Prog& P, uint32_t i, uint32_t* defcnt) {
     uint32_t lo = 0, hi = P.F;
     while (hi - lo > 1) {
         const uint32_t mid = (lo + hi) / 2;
         if (P.fn_start0[mid] <= i) lo = mid; else hi = mid;
     }
-    return !ra_own(P, lo, P.rs1[i]) || !ra_own(P, lo, P.rs2[i]) || !ra_own(P, lo, P.rd[i]);
+    const uint32_t rd = P.rd[i];
+    if (!ra_own(P, lo, P.rs1[i]) || !ra_own(P, lo, P.rs2[i]) || !ra_own(P, lo, rd)) return 1u;
+    if ((lo & 7u) != 0 || !(s32(rd) > 63)) return 0u;
+#if defined(__CUDA_ARCH__)
+    const uint32_t before = atomicAdd(&defcnt[rd - 64u], 1u);
+#else
+    const uint32_t before = defcnt[rd - 64u]++;
+#endif
+    return before != 0 ? 2u : 0u;
 }
 
 // The reference's step loop as written (rv_generator_avx.cpp:1400-1413 with one worker):

@@ -69,6 +69,20 @@ def test_gpu_spilling_program(built_cuda):
     assert_matches_oracle(generate(config_params("c1", scale=96 / 2048)))
 
 
+@pytest.mark.parametrize("scale", [96 / 2048, 0.1])
+def test_gpu_row0_hash_path_equals_definition_path(built_cuda, scale):
+    """The register allocator's two row-0 lookups (recorded definition position, and
+    the hash of row 0 taken when a virtual register has two definitions) agree."""
+    from ptilopsis_gb300 import RvGenerator
+    from ptilopsis_gb300.synth import config_params, generate
+    tree = generate(config_params("c1", scale=scale))
+    with RvGenerator(tree) as gen:
+        gen.process()
+        fast = gen.get_instructions()
+        gen.process(row0_hash=True)
+        np.testing.assert_array_equal(gen.get_instructions(), fast)
+
+
 def test_gpu_many_functions(built_cuda):
     from ptilopsis_gb300.synth import SynthParams, generate
     assert_matches_oracle(generate(SynthParams(seed=0x50544C42, n_functions=2000, median_fn_nodes=80.0,

@@ -133,3 +133,18 @@ def test_hostmodel_symbol_cache_sizes(built, k):
         assert_stages_equal(ast)
     finally:
         L.ptlhm_set_cache_entries(ctypes.c_uint32(4))
+
+
+@pytest.mark.parametrize("hashed", [False, True])
+def test_hostmodel_row0_lookup_modes(built, hashed):
+    """Row-0 membership by recorded definition position and by hashing row 0 agree."""
+    from ptilopsis_gb300.synth import config_params, generate
+    L = hostmodel()
+    L.ptlhm_set_hashed(ctypes.c_int(1 if hashed else 0))
+    try:
+        assert_stages_equal(tree_to_ast(generate(config_params("c1", scale=40 / 2048))))
+        for name in ("pareas_basic_3_in", "comp_all_ptl", "arith1_ptl"):
+            ast, _ = load_fixture(name)
+            assert_stages_equal(ast)
+    finally:
+        L.ptlhm_set_hashed(ctypes.c_int(0))
