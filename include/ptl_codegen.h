@@ -117,6 +117,29 @@ ptl_status ptl_generator_snapshot(ptl_generator* gen, int which, uint32_t* out, 
  * 9 pareas_to_rv[44].  Returns the element count; out may be NULL. */
 size_t ptl_code_table(int which, uint32_t* out);
 
+/* No counterpart in the reference: its optimize pass (rv_generator_avx.cpp:891-1016) runs
+ * only inside process().  This is the same pass over caller-owned device buffers that
+ * allocates no device memory, for callers that cannot have a library call cudaMalloc:
+ * one that reserves the device's memory budget in its own pool and admits work against
+ * it, or one that cannot take the device-wide synchronisation of a cudaMalloc/cudaFree
+ * in the middle of its stream.  Its scratch is a fixed 8 MiB + 256 B array in device
+ * memory that every GPU loading this library holds until the process exits.
+ *
+ * instr, rd, rs1, rs2: the count words of an isn_gen instruction stream and their
+ * registers (the arrays ptl_generator_snapshot returns for which = 14..17), device
+ * pointers on the current device.  used_instrs receives count words: 0xFFFFFFFF for a
+ * word that stays, 0 for one the pass removes (ptl_generator_snapshot's which = 19).
+ * stream is a cudaStream_t (NULL = the legacy default stream); the call returns when
+ * the result is written.  count > PTL_OPTIMIZE_NOALLOC_MAX_WORDS returns
+ * PTL_BAD_ARGUMENT before touching anything, as do null or non-device pointers.
+ * The first call on each device looks up the scratch array's address with that
+ * device current (cudaGetSymbolAddress); make that first call before any stream
+ * capture begins.  Calls on one device are serialised by a lock because they share
+ * the scratch; device work that used the same scratch concurrently would race. */
+#define PTL_OPTIMIZE_NOALLOC_MAX_WORDS (1u << 22)
+ptl_status ptl_optimize_noalloc(const uint32_t* instr, const uint32_t* rd, const uint32_t* rs1,
+                                const uint32_t* rs2, size_t count, uint32_t* used_instrs, void* stream);
+
 /* Kernel launches the library has issued so far (all generators of the process). */
 uint64_t ptl_kernel_launches(void);
 

@@ -1,0 +1,122 @@
+"""ptl_optimize_noalloc through the C ABI against the generator's own optimize stage.
+
+The generator (ptl_generator_process) exposes its isn_gen instruction stream
+(snapshots 14..17) and the optimize stage's used_instrs (snapshot 19); the
+allocation-free entry point must give the same words from the same inputs, call after
+call, without growing device memory use.  Collected last on purpose, and
+self-contained so that it also passes alone in a fresh process.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+MAX_WORDS = 1 << 22  # PTL_OPTIMIZE_NOALLOC_MAX_WORDS
+
+
+def _entry():
+    from ptilopsis_gb300.codegen import lib
+    f = lib().ptl_optimize_noalloc
+    vp = ctypes.c_void_p
+    f.argtypes = [vp, vp, vp, vp, ctypes.c_size_t, vp, vp]
+    f.restype = ctypes.c_int
+    return f
+
+
+def _generator_stream(tree):
+    """(instr, rd, rs1, rs2, used_instrs) of the generator's optimize stage."""
+    from ptilopsis_gb300 import RvGenerator
+    with RvGenerator(tree) as gen:
+        gen.process()
+        return tuple(gen.snapshot(k) for k in ("gen_instr", "gen_rd", "gen_rs1", "gen_rs2", "opt_used"))
+
+
+def _run(f, dev_arrays, count, out, stream=None):
+    import torch
+    s = stream.cuda_stream if stream is not None else torch.cuda.current_stream().cuda_stream
+    return f(*[ctypes.c_void_p(a.data_ptr()) for a in dev_arrays], count, ctypes.c_void_p(out.data_ptr()),
+             ctypes.c_void_p(s))
+
+
+def _programs():
+    from conftest import ast_to_tree, load_fixture
+    from ptilopsis_gb300.synth import SynthParams, config_params, generate
+    ast, _ = load_fixture("comp_all_ptl")
+    return [("comp_all_ptl", ast_to_tree(ast)),
+            ("synthetic_c0", generate(SynthParams(seed=0x50544C00))),
+            ("c1_spilling", generate(config_params("c1", scale=96 / 2048))),
+            ("c1_quarter", generate(config_params("c1", scale=0.25)))]
+
+
+def test_no_alloc_optimize_matches_generator(built_cuda):
+    import torch
+    f = _entry()
+    dev = torch.device("cuda", 0)
+    cases = []
+    for name, tree in _programs():
+        instr, rd, rs1, rs2, used = _generator_stream(tree)
+        assert 0 < len(instr) <= MAX_WORDS, name
+        cases.append((name, [torch.from_numpy(a.astype(np.uint32).view(np.int32)).to(dev)
+                             for a in (instr, rd, rs1, rs2)], used))
+    # outputs come from torch's pool up front, and torch's own fill and copy paths run
+    # once, so that the measured region holds only this library's calls
+    outs = [torch.empty(len(used), dtype=torch.int32, device=dev) for _, _, used in cases]
+    for o in outs:
+        o.fill_(0x5A5A5A5A)
+        o[:1].cpu()
+    # the first call on the device does the one-time set-up
+    name, arrs, used = cases[0]
+    assert _run(f, arrs, len(used), outs[0]) == 0
+    torch.cuda.synchronize()
+    free_before = torch.cuda.mem_get_info(0)[0]
+    # two calls in a row per program, largest program between small ones: stale scratch
+    # from a bigger call must not leak into a smaller one
+    order = list(range(len(cases)))
+    for k in order + order[::-1]:
+        name, arrs, used = cases[k]
+        for call in range(2):
+            outs[k].fill_(0x5A5A5A5A)
+            assert _run(f, arrs, len(used), outs[k]) == 0, (name, call)
+            got = outs[k].cpu().numpy().view(np.uint32)
+            np.testing.assert_array_equal(got, used, err_msg=f"{name} call {call}")
+    torch.cuda.synchronize()
+    assert free_before - torch.cuda.mem_get_info(0)[0] < (1 << 20)
+
+
+def test_no_alloc_optimize_on_a_side_stream(built_cuda):
+    import torch
+    f = _entry()
+    dev = torch.device("cuda", 0)
+    from ptilopsis_gb300.synth import SynthParams, generate
+    instr, rd, rs1, rs2, used = _generator_stream(generate(SynthParams(seed=0x50544C47, n_functions=64)))
+    arrs = [torch.from_numpy(a.astype(np.uint32).view(np.int32)).to(dev) for a in (instr, rd, rs1, rs2)]
+    side = torch.cuda.Stream(device=dev)
+    side.wait_stream(torch.cuda.current_stream())
+    for _ in range(2):
+        with torch.cuda.stream(side):
+            out = torch.zeros(len(used), dtype=torch.int32, device=dev)
+            assert _run(f, arrs, len(used), out, stream=side) == 0
+        side.synchronize()
+        np.testing.assert_array_equal(out.cpu().numpy().view(np.uint32), used)
+
+
+def test_no_alloc_optimize_rejects_oversize_and_bad_pointers(built_cuda):
+    import torch
+    f = _entry()
+    dev = torch.device("cuda", 0)
+    small = [torch.zeros(8, dtype=torch.int32, device=dev) for _ in range(4)]
+    out = torch.zeros(8, dtype=torch.int32, device=dev)
+    # the size check comes before any pointer is used
+    assert _run(f, small, MAX_WORDS + 1, out) == 7  # PTL_BAD_ARGUMENT
+    host = np.zeros(8, np.uint32)
+    vp = ctypes.c_void_p
+    s = vp(torch.cuda.current_stream().cuda_stream)
+    assert f(vp(host.ctypes.data), vp(small[1].data_ptr()), vp(small[2].data_ptr()), vp(small[3].data_ptr()), 8,
+             vp(out.data_ptr()), s) == 7
+    assert f(None, vp(small[1].data_ptr()), vp(small[2].data_ptr()), vp(small[3].data_ptr()), 8,
+             vp(out.data_ptr()), s) == 7
+    assert _run(f, small, 0, out) == 0
