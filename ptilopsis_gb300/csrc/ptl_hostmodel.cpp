@@ -138,7 +138,7 @@ struct Model {
         const Prog Psave = P;
         if (hashed) P.defpos = nullptr;
         Ra2Shared sh{};
-        std::vector<uint32_t> cur(3 * G0), tag(static_cast<size_t>(G0) * K);
+        std::vector<uint32_t> cur(4 * G0), tag(static_cast<size_t>(G0) * K);
         std::vector<uint32_t> val(static_cast<size_t>(G0) * K);
         const SymCache c{tag.data(), val.data(), K};
         std::vector<Ra2Slot> L(G0);
@@ -152,7 +152,7 @@ struct Model {
         for (uint32_t i = 0; i < S; ++i) {
             bool in_row0 = false;
             for (uint32_t j = 0; j < G0; ++j) {
-                ra2_load(P, L[j], i, cur.data() + 3 * j);
+                ra2_load(P, L[j], i, cur.data() + 4 * j);
                 in_row0 |= ra2_compute0(P, c, sh, L[j], j, i);
             }
             if (in_row0) {
@@ -168,7 +168,7 @@ struct Model {
                     }
                 }
             }
-            for (uint32_t j = 0; j < G0; ++j) ra2_apply(P, c, sh, L[j], j, i);
+            for (uint32_t j = 0; j < G0; ++j) ra2_apply(P, c, sh, L[j], j, i, cur.data() + 4 * j);
             if (hashed) for (uint32_t p = 0; p < 64; ++p) snap_clear_next(sh, i, p);
             for (uint32_t p = 0; p < 64; ++p) {
                 ra2_end_p(P, c, sh, p, cur.data());

@@ -434,7 +434,7 @@ __global__ void __launch_bounds__(1024) k_ra_lane0_cached(Prog P, uint32_t S, ui
     Ra2Shared& sh = *reinterpret_cast<Ra2Shared*>(smem);
     const uint32_t G0 = (P.F + 7u) / 8u;
     uint32_t* cur = reinterpret_cast<uint32_t*>(smem + sizeof(Ra2Shared));
-    uint32_t* ctag = cur + 3u * G0;
+    uint32_t* ctag = cur + 4u * G0;
     uint32_t* cval = ctag + G0 * K;
     const SymCache c{ctag, cval, K};
     const uint32_t tid = threadIdx.x, T = blockDim.x;
@@ -474,7 +474,7 @@ __global__ void __launch_bounds__(1024) k_ra_lane0_cached(Prog P, uint32_t S, ui
         for (int q = 0; q < Q; ++q) {
             const uint32_t j = tid + static_cast<uint32_t>(q) * T;
             if (j < G0) {
-                ra2_load(P, L[q], i, cur + 3u * j);
+                ra2_load(P, L[q], i, cur + 4u * j);
                 in_row0 |= ra2_compute0(P, c, sh, L[q], j, i);
             }
         }
@@ -505,7 +505,7 @@ __global__ void __launch_bounds__(1024) k_ra_lane0_cached(Prog P, uint32_t S, ui
 #pragma unroll
         for (int q = 0; q < Q; ++q) {
             const uint32_t j = tid + static_cast<uint32_t>(q) * T;
-            if (j < G0) ra2_apply(P, c, sh, L[q], j, i);
+            if (j < G0) ra2_apply(P, c, sh, L[q], j, i, cur + 4u * j);
         }
         if (hashed && tid < 64) snap_clear_next(sh, i, tid);
         __syncthreads();
@@ -718,7 +718,7 @@ cudaError_t run_regalloc_steps(const Prog& P, cudaStream_t s, bool* serial_out, 
         const uint32_t Q = (G0 + T - 1u) / T;
         // symbol cache entries per function: the largest power of two within ~160 KB
         uint32_t K = 64;
-        const size_t fixed = sizeof(Ra2Shared) + 12ull * G0;
+        const size_t fixed = sizeof(Ra2Shared) + 16ull * G0;
         while (K > 1 && fixed + static_cast<size_t>(G0) * K * 8u > 160u * 1024u) K >>= 1;
         const size_t smem = fixed + static_cast<size_t>(G0) * K * 8u + 16;
         g_launches++;

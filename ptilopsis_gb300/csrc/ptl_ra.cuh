@@ -25,26 +25,23 @@ PTL_HD void cache_reset(const SymCache& c, uint32_t slot) {
     for (uint32_t k = 0; k < c.K; ++k) c.tag[slot * c.K + k] = 0;
 }
 
-// Looks up v (> 63); returns physical register and swapped flag.
-PTL_HD void sym_read(const Prog& P, const SymCache& c, uint32_t slot, uint32_t v, uint32_t* reg, bool* swp) {
+// Looks up v (> 63); returns physical register, swapped flag and (through defp, when
+// given) the row-0 position + 1 of v's definition.
+PTL_HD void sym_read(const Prog& P, const SymCache& c, uint32_t slot, uint32_t v, uint32_t* reg, bool* swp,
+                     uint32_t* defp = nullptr) {
     const uint32_t e = slot * c.K + ((v - 64u) & (c.K - 1u));
+    uint32_t x;
     if (c.tag[e] == v) {
-        const uint32_t x = c.val[e];
-        *reg = x & 0xFFu;
-        *swp = ((x >> 8) & 1u) != 0;
-        return;
+        x = c.val[e];
+    } else {
+        x = (P.symreg[v - 64u] & 0xFFu) | (P.symswp[v - 64u] != 0 ? 0x100u : 0u) |
+            (P.defpos ? static_cast<uint32_t>(P.defpos[v - 64u]) << 16 : 0u);
+        c.tag[e] = v;
+        c.val[e] = x;
     }
-    *reg = P.symreg[v - 64u];
-    *swp = P.symswp[v - 64u] != 0;
-    c.tag[e] = v;
-    c.val[e] = (*reg & 0xFFu) | (*swp ? 0x100u : 0u) | (P.defpos ? static_cast<uint32_t>(P.defpos[v - 64u]) << 16 : 0u);
-}
-
-// Row-0 position (+1, 0 = none) where v's definition wrote it (lane-0 functions).
-PTL_HD uint32_t sym_defpos(const Prog& P, const SymCache& c, uint32_t slot, uint32_t v) {
-    const uint32_t e = slot * c.K + ((v - 64u) & (c.K - 1u));
-    if (c.tag[e] == v) return c.val[e] >> 16;
-    return P.defpos[v - 64u];
+    *reg = x & 0xFFu;
+    *swp = ((x >> 8) & 1u) != 0;
+    if (defp) *defp = x >> 16;
 }
 
 // Owner update of v.  defp = row-0 position + 1 of a definition, 0 for a use (kept).
@@ -74,6 +71,12 @@ PTL_HD void sym_mark(const Prog& P, const SymCache& c, uint32_t owner_slot, uint
     if (c.tag[e] == v) c.val[e] |= 0x100u;
 }
 
+// Whether r is a physical register or a virtual register of the instruction range
+// [start, start+size) (ra_own with the range in registers).
+PTL_HD bool ra_own_in(uint32_t start, uint32_t size, uint32_t r) {
+    return !(s32(r) > 63) || r - 64u - start < size;
+}
+
 // ---------------------------------------------------------------- independent functions
 // Functions outside lane 0: no marks reach their symbols, so the loop needs only the
 // physical registers (kept in the cache) and emits trigger records for the lane-0 pass.
@@ -87,8 +90,9 @@ PTL_HD void ra_free_function_cached(const Prog& P, const SymCache& c, uint32_t s
     for (uint32_t i = 0; have; ++i) {
         RaStep S = next;
         have = ra_load_at(P, start, size, i + 1, next);  // issue the next step's loads early
-        if (S.ins == 0x000000EFu || !ra_own(P, f, S.r1) || !ra_own(P, f, S.r2) || !ra_own(P, f, S.ord)) {
-            record_error(P.err, ST_UNSUPPORTED, W_RA1, P.fn_start0[f] + i);
+        if (S.ins == 0x000000EFu || !ra_own_in(start, size, S.r1) || !ra_own_in(start, size, S.r2) ||
+            !ra_own_in(start, size, S.ord)) {
+            record_error(P.err, ST_UNSUPPORTED, W_RA1, start + i);
             return;
         }
         uint32_t r1reg = 0, r2reg = 0;
@@ -123,7 +127,7 @@ struct Ra2Shared {
     uint32_t omin[64], omax[64];   // trigger groups of the other functions this step
     uint32_t lcur[64], lmax[64];   // lane-0 triggers of the current round
     uint32_t lnew[64], lmaxnew[64];
-    unsigned long long r0key[64];
+    uint32_t r0grp[64];    // highest group (+1) writing each position this step
 };
 
 // Per function slot (registers on the device).
@@ -189,10 +193,8 @@ PTL_HD void snap_clear_next(Ra2Shared& sh, uint32_t i, uint32_t p) {
 // Row-0 positions holding v: a lane-0 value enters row 0 only where its definition put
 // it, so one compare answers the question -- unless two instructions define the same
 // virtual register, for which the row-0 hash is built instead (P.defpos == null).
-PTL_HD uint64_t snap_positions(const Prog& P, const SymCache& c, const Ra2Shared& sh, uint32_t slot, uint32_t i,
-                               uint32_t v) {
+PTL_HD uint64_t snap_positions(const Prog& P, const Ra2Shared& sh, uint32_t i, uint32_t v, uint32_t d) {
     if (!P.defpos) return snap_positions_hashed(sh, i, v);
-    const uint32_t d = sym_defpos(P, c, slot, v);
     if (d == 0) return 0;
     return sh.snap[d - 1u] == v ? (1ull << (d - 1u)) : 0ull;
 }
@@ -229,23 +231,23 @@ PTL_HD void ra2_begin_p(Ra2Shared& sh, uint32_t i, uint32_t p, uint32_t tmin, ui
     sh.lmax[p] = 0;
     sh.lnew[p] = 0xFFFFFFFFu;
     sh.lmaxnew[p] = 0;
-    sh.r0key[p] = 0;
+    sh.r0grp[p] = 0;
 }
 
-// Loads the slot's instruction of step i (prefetched in the previous step).
+// Loads the slot's instruction of step i (prefetched in the previous step).  cur[0..2]:
+// what the slot updates this step (for the mark phase); cur[3] is set by ra2_apply.
 PTL_HD void ra2_load(const Prog& P, Ra2Slot& L, uint32_t i, uint32_t* cur) {
     L.act = L.have_next;
     if (L.act) {
         L.S = L.next;
         L.have_next = ra_load_at(P, L.start, L.size, i + 1, L.next);
-        if (L.S.ins == 0x000000EFu || !ra_own(P, 8u * L.j, L.S.r1) || !ra_own(P, 8u * L.j, L.S.r2) ||
-            !ra_own(P, 8u * L.j, L.S.ord)) {
+        if (L.S.ins == 0x000000EFu || !ra_own_in(L.start, L.size, L.S.r1) || !ra_own_in(L.start, L.size, L.S.r2) ||
+            !ra_own_in(L.start, L.size, L.S.ord)) {
             record_error(P.err, ST_UNSUPPORTED, W_RA2, P.fn_start0[8u * L.j] + i);
             L.act = false;
             L.have_next = false;
         }
     }
-    // what this function updates this step (for the mark phase)
     cur[0] = L.act ? L.S.ord : 0u;
     cur[1] = L.act ? L.S.r1 : 0u;
     cur[2] = L.act ? L.S.r2 : 0u;
@@ -274,12 +276,14 @@ PTL_HD bool ra2_compute0(const Prog& P, const SymCache& c, Ra2Shared& sh, Ra2Slo
     L.r1stored = L.r2stored = false;
     L.m1 = L.m2 = 0;
     if (s32(S.r1) > 63) {
-        sym_read(P, c, slot, S.r1, &L.r1reg, &L.r1stored);
-        L.m1 = snap_positions(P, c, sh, slot, i, S.r1);
+        uint32_t d;
+        sym_read(P, c, slot, S.r1, &L.r1reg, &L.r1stored, &d);
+        L.m1 = snap_positions(P, sh, i, S.r1, d);
     }
     if (s32(S.r2) > 63) {
-        sym_read(P, c, slot, S.r2, &L.r2reg, &L.r2stored);
-        L.m2 = snap_positions(P, c, sh, slot, i, S.r2);
+        uint32_t d;
+        sym_read(P, c, slot, S.r2, &L.r2reg, &L.r2stored, &d);
+        L.m2 = snap_positions(P, sh, i, S.r2, d);
     }
     L.r1m = marked_before(sh, L.m1, L.j, false);
     L.r2m = marked_before(sh, L.m2, L.j, false);
@@ -317,24 +321,29 @@ PTL_HD bool ra2_round_p(Ra2Shared& sh, uint32_t p) {
 }
 
 // Apply the step: lifetime, own symbol updates (swapped only when a later group marks
-// the symbol in this step), row-0 writes as (group, value) keys.
-PTL_HD void ra2_apply(const Prog& P, const SymCache& c, Ra2Shared& sh, Ra2Slot& L, uint32_t slot, uint32_t i) {
+// the symbol in this step), row-0 writes as the highest writing group per position.
+// The winner's value follows from its record: its defined register at its rd position
+// (cur[3]), a cleared entry (0xFFFFFFFF) at its rs1/rs2 positions.
+PTL_HD void ra2_apply(const Prog& P, const SymCache& c, Ra2Shared& sh, Ra2Slot& L, uint32_t slot, uint32_t i,
+                      uint32_t* cur) {
     if (!L.act) return;
     const RaStep& S = L.S;
     L.lifetime = S.cleared | S.rdm;
     const uint32_t g1 = L.j + 1u;
-    auto later = [&](uint32_t v) {
-        for (uint64_t m = snap_positions(P, c, sh, slot, i, v); m; m &= m - 1) {
+    auto later = [&](uint64_t m) {
+        for (; m; m &= m - 1) {
             const uint32_t p = ctz64(m);
             const uint32_t g = sh.omax[p] > sh.lmax[p] ? sh.omax[p] : sh.lmax[p];
             if (g > g1) return true;
         }
         return false;
     };
-    // the swap flags need the row-0 positions before this step's updates
-    const bool l_ord = s32(S.ord) > 63 && later(S.ord);
-    const bool l_r1 = s32(S.r1) > 63 && later(S.r1);
-    const bool l_r2 = s32(S.r2) > 63 && later(S.r2);
+    // The swap flags need the row-0 positions at the step start: m1/m2 from the round-0
+    // lookups.  The defined register sits in row 0 before its definition only when it
+    // has two definitions, i.e. in hashed mode.
+    const bool l_ord = !P.defpos && s32(S.ord) > 63 && later(snap_positions_hashed(sh, i, S.ord));
+    const bool l_r1 = s32(S.r1) > 63 && later(L.m1);
+    const bool l_r2 = s32(S.r2) > 63 && later(L.m2);
     // the reference's order: rd, rs1, rs2 (a later write of the same symbol wins); a
     // definition records the row-0 position it writes (when it writes row 0 at all)
     if (s32(S.ord) > 63) sym_write(P, c, slot, S.ord, S.rdr, false, (S.rdr & 63u) + 1u);
@@ -343,15 +352,17 @@ PTL_HD void ra2_apply(const Prog& P, const SymCache& c, Ra2Shared& sh, Ra2Slot& 
     if (l_ord) sym_write(P, c, slot, S.ord, P.symreg[S.ord - 64u], true);
     if (l_r1) sym_write(P, c, slot, S.r1, P.symreg[S.r1 - 64u], true);
     if (l_r2) sym_write(P, c, slot, S.r2, P.symreg[S.r2 - 64u], true);
-    const unsigned long long key = static_cast<unsigned long long>(g1) << 32;
-    if (S.ord != 0) at_max_u64(&sh.r0key[S.rdr & 63u], key | S.ord);
-    if (S.r1r != S.rdr && s32(S.r1r) >= 0 && S.r1r < 64u) at_max_u64(&sh.r0key[S.r1r], key | 0xFFFFFFFFull);
-    if (S.r2r != S.rdr && s32(S.r2r) >= 0 && S.r2r < 64u) at_max_u64(&sh.r0key[S.r2r], key | 0xFFFFFFFFull);
+    // rdr < 64 always, and a clear never lands on the rd position, so each group writes
+    // one value per position
+    cur[3] = S.rdr & 63u;
+    if (S.ord != 0) at_max_u32(&sh.r0grp[S.rdr & 63u], g1);
+    if (S.r1r != S.rdr && s32(S.r1r) >= 0 && S.r1r < 64u) at_max_u32(&sh.r0grp[S.r1r], g1);
+    if (S.r2r != S.rdr && s32(S.r2r) >= 0 && S.r2r < 64u) at_max_u32(&sh.r0grp[S.r2r], g1);
 }
 
 // Step end for row-0 position p: marks on symbols their owner did not update this step,
-// then row 0 takes the highest group's write.  cur[3*slot..] are the slots' updates;
-// slot_of_group maps a group to its slot.
+// then row 0 takes the highest group's write.  cur[4*slot..] are the slots' records
+// (slot index == group index).
 PTL_HD void ra2_end_p(const Prog& P, const SymCache& c, Ra2Shared& sh, uint32_t p, const uint32_t* cur) {
     const bool triggered = sh.omin[p] != 0xFFFFFFFFu || sh.lcur[p] != 0xFFFFFFFFu;
     const uint32_t v = sh.snap[p];
@@ -359,15 +370,16 @@ PTL_HD void ra2_end_p(const Prog& P, const SymCache& c, Ra2Shared& sh, uint32_t 
         const uint32_t own = sh.snapown[p];
         bool updated = false;
         if (own != 0xFFFFFFFFu) {
-            const uint32_t* u = cur + 3u * own;
+            const uint32_t* u = cur + 4u * own;
             updated = (s32(u[0]) > 63 && u[0] == v) || (s32(u[1]) > 63 && u[1] == v) || (s32(u[2]) > 63 && u[2] == v);
         }
         if (!updated) sym_mark(P, c, own, v);
     }
-    const unsigned long long k = sh.r0key[p];
-    if (k != 0) {
-        sh.R0[p] = static_cast<uint32_t>(k);
-        sh.R0own[p] = static_cast<uint32_t>(k >> 32) - 1u;  // group index == slot index
+    const uint32_t g = sh.r0grp[p];
+    if (g != 0) {
+        const uint32_t* w = cur + 4u * (g - 1u);
+        sh.R0[p] = (w[0] != 0 && w[3] == p) ? w[0] : 0xFFFFFFFFu;
+        sh.R0own[p] = g - 1u;
     }
 }
 
