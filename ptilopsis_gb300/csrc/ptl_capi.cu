@@ -112,7 +112,7 @@ struct ptl_generator {
     DevBuf decl, fn_id, fn_start, fn_size, fn_end, fn_start0, fn_size0, fn_end0;
     DevBuf fn_ra_start, fn_ra_end, fn_ra_size;
     DevBuf instr, rd, rs1, rs2, jt, owner, used, smark, used_instrs;
-    DevBuf symreg, symswp, stamp, defpos, lifetime, trig_min, trig_max, spill, roffs;
+    DevBuf symreg, symswp, stamp, defpos, lifetime, trig_min, trig_max, ra_chunks, spill, roffs;
     DevBuf ni, nrd, nr1, nr2, njt, fsz, joffs, out;
     DevBuf sort_a, sort_apos, sort_bpos, sort_seg0, sort_seg1, sort_tile_seg, sort_tile_l, sort_tile_r,
         sort_leaf, sort_heap, sort_counters;
@@ -135,7 +135,7 @@ struct ptl_generator {
                 &par, &ci, &dep, &fflag, &sizes, &loc0, &loc, &pos, &regs, &decl, &fn_id, &fn_start,
                 &fn_size, &fn_end, &fn_start0, &fn_size0, &fn_end0, &fn_ra_start, &fn_ra_end, &fn_ra_size,
                 &instr, &rd, &rs1, &rs2, &jt, &owner, &used, &smark, &used_instrs, &symreg, &symswp,
-                &stamp, &defpos, &lifetime, &trig_min, &trig_max, &spill, &roffs, &ni, &nrd, &nr1, &nr2, &njt,
+                &stamp, &defpos, &lifetime, &trig_min, &trig_max, &ra_chunks, &spill, &roffs, &ni, &nrd, &nr1, &nr2, &njt,
                 &fsz, &joffs, &out, &sort_a, &sort_apos, &sort_bpos, &sort_seg0, &sort_seg1,
                 &sort_tile_seg, &sort_tile_l, &sort_tile_r, &sort_leaf, &sort_heap, &sort_counters,
                 &scan_status, &scan_counter, &meta, &flags, &errw, &tables, &depth_seen};
@@ -222,6 +222,7 @@ Prog make_prog(ptl_generator* g) {
     P.lifetime = g->lifetime.at<unsigned long long>();
     P.trig_min = g->trig_min.at<uint32_t>();
     P.trig_max = g->trig_max.at<uint32_t>();
+    P.ra_chunks = g->ra_chunks.at<uint32_t>();
     P.spill = g->spill.at<uint32_t>();
     P.roffs = g->roffs.at<uint32_t>();
     P.ni = g->ni.at<uint32_t>();
@@ -448,8 +449,9 @@ ptl_status run_pipeline(ptl_generator* g, bool profile, bool to_host, bool row0_
     PTL_CU(g->trig_min.fill(s, 0xFF));
     PTL_CU(g->trig_max.ensure(trig, 4));
     PTL_CU(g->trig_max.zero(s));
+    PTL_CU(g->ra_chunks.ensure(2 * (static_cast<size_t>(g->S) / 32 + 2), 4));
     P = make_prog(g);
-    if (!prog_ready(P, {P.lifetime, P.trig_min, P.trig_max}))
+    if (!prog_ready(P, {P.lifetime, P.trig_min, P.trig_max, P.ra_chunks}))
         return fail(g, PTL_CUDA_ERROR, "internal: unallocated regalloc state");
     PTL_CU(run_regalloc_steps(P, s, &g->ra_serial, row0_hash));
     PTL_CU(scan_for(wb8, &sc));

@@ -403,22 +403,58 @@ __global__ void k_opt_sweep(Prog P) {
 __global__ void k_opt_final(Prog P) { PTL_FOR(i, P.wb8) st_opt_final(P, i); }
 
 // ------------------------------------------------------------------ regalloc
-// Independent functions with an on-chip symbol cache per thread.
+// Independent functions with an on-chip symbol cache per thread (used when the fused
+// launch below cannot be made co-resident).
 constexpr int kRaFreeThreads = 64;
 constexpr uint32_t kRaFreeK = 64;
+
+__device__ __forceinline__ uint32_t free_function_of(uint32_t k) {
+    return (k / 7u) * 8u + (k % 7u) + 1u;  // the k-th function index that is not a multiple of 8
+}
 
 __global__ void __launch_bounds__(kRaFreeThreads) k_ra_free_cached(Prog P) {
     __shared__ uint32_t tag[kRaFreeThreads * kRaFreeK];
     __shared__ uint32_t val[kRaFreeThreads * kRaFreeK];
     const SymCache c{tag, val, kRaFreeK};
-    // non-lane-0 functions only: function index skips multiples of 8
-    const uint32_t k = blockIdx.x * kRaFreeThreads + threadIdx.x;
-    const uint32_t f = (k / 7u) * 8u + (k % 7u) + 1u;
+    const uint32_t f = free_function_of(blockIdx.x * kRaFreeThreads + threadIdx.x);
     if (f < P.F) ra_free_function_cached(P, c, threadIdx.x, f);
 }
 
-// Lane-0 functions (f % 8 == 0) in lock-step, one CTA; thread t runs slots t, t+T, ...
-// (Q per thread); slot = group index.  Per step:
+// Progress chunks: hist[x] = independent functions whose last step falls in chunk x.
+__global__ void k_ra_chunk_hist(Prog P, uint32_t nfree) {
+    PTL_FOR(k, nfree) {
+        const uint32_t f = free_function_of(k);
+        if (f >= P.F) continue;
+        const uint32_t size = P.fn_size0[f];
+        if (s32(size) > 0) atomicAdd(&P.ra_chunks[(size - 1u) / kRaChunk], 1u);
+    }
+}
+
+constexpr uint32_t kRaWaitLimit = 1u << 23;  // polls of 128 ns or more: about a second
+
+// Lane-0 block: waits until every independent function has finished chunk c, i.e. until
+// done[c] reaches need.  Gives up (false) on an error word or after the poll limit.
+__device__ bool ra_wait_chunk(const uint32_t* done, uint32_t c, uint32_t need, ErrorWord* err) {
+    for (uint32_t polls = 0;; ++polls) {
+        if (*reinterpret_cast<const volatile uint32_t*>(&done[c]) >= need) {
+            __threadfence();
+            return true;
+        }
+        if (*reinterpret_cast<const volatile uint32_t*>(&err->code) != 0) return false;
+        if (polls > kRaWaitLimit) {
+            record_error(err, ST_DEVICE_TIMEOUT, W_RA2, c);
+            return false;
+        }
+        __nanosleep(128);
+    }
+}
+
+// Register allocation steps in one launch.  Block 0 runs the lane-0 functions (f % 8 ==
+// 0) in lock-step; thread t runs slots t, t+T, ... (Q per thread), slot = group index.
+// Blocks 1.. run the independent functions, one per thread, and count finished chunks
+// of trigger records; block 0 waits for a chunk before it loads that chunk's records.
+// With chunks == 0 there are no other blocks: the independent functions ran before.
+// Per step of block 0:
 //   1. each active function computes its step; a symbol reads as swapped if a function
 //      of an earlier group triggered the physical register holding it in row 0.  The
 //      other functions' triggers are known (trig_min/trig_max); earlier lane-0 triggers
@@ -429,19 +465,43 @@ __global__ void __launch_bounds__(kRaFreeThreads) k_ra_free_cached(Prog P) {
 //      also triggered it; other triggered symbols end swapped;
 //   3. row 0 takes, per physical register, the write of the highest group.
 template <int Q>
-__global__ void __launch_bounds__(1024) k_ra_lane0_cached(Prog P, uint32_t S, uint32_t K) {
+__global__ void __launch_bounds__(1024) k_ra_steps(Prog P, uint32_t S, uint32_t K, uint32_t Kf, uint32_t chunks) {
     extern __shared__ __align__(16) unsigned char smem[];
+    const uint32_t tid = threadIdx.x, T = blockDim.x;
+    if (blockIdx.x > 0) {
+        uint32_t* tag = reinterpret_cast<uint32_t*>(smem);
+        const SymCache cf{tag, tag + T * Kf, Kf};
+        // the independent functions never need definition positions
+        Prog Pf = P;
+        Pf.defpos = nullptr;
+        const uint32_t f = free_function_of((blockIdx.x - 1u) * T + tid);
+        if (f < P.F) ra_free_function_cached(Pf, cf, tid, f, P.ra_chunks + chunks);
+        return;
+    }
+    __shared__ uint32_t s_abort;
+    const uint32_t* hist = P.ra_chunks;
+    const uint32_t* done = P.ra_chunks + chunks;
     Ra2Shared& sh = *reinterpret_cast<Ra2Shared*>(smem);
     const uint32_t G0 = (P.F + 7u) / 8u;
     uint32_t* cur = reinterpret_cast<uint32_t*>(smem + sizeof(Ra2Shared));
     uint32_t* ctag = cur + 4u * G0;
     uint32_t* cval = ctag + G0 * K;
     const SymCache c{ctag, cval, K};
-    const uint32_t tid = threadIdx.x, T = blockDim.x;
     const bool hashed = P.defpos == nullptr;
     if (T < 64u) {  // the row-0 phases need a thread per physical register
         if (tid == 0) record_error(P.err, ST_UNSUPPORTED, W_RA2, T);
         return;
+    }
+    // thread 0: independent functions still running in chunk wc (need)
+    uint32_t need = 0, wc = 0;
+    auto wait_for = [&](uint32_t chunk) {
+        while (wc < chunk) need -= hist[wc++];
+        if (!ra_wait_chunk(done, chunk, need, P.err)) s_abort = 1;
+    };
+    if (tid == 0) {
+        s_abort = 0;
+        for (uint32_t x = 0; x < chunks; ++x) need += hist[x];
+        if (chunks > 0 && S > 0) wait_for(0);
     }
     Ra2Slot L[Q];
 #pragma unroll
@@ -461,14 +521,17 @@ __global__ void __launch_bounds__(1024) k_ra_lane0_cached(Prog P, uint32_t S, ui
         }
     }
     __syncthreads();
+    if (s_abort) return;
+    // trigger records are read from L2: lines of a chunk may sit in L1 from the chunk before
     if (tid < 64 && S > 0) {
-        ra2_begin_p(sh, 0, tid, P.trig_min[tid], P.trig_max[tid], hashed);
-        if (S > 1) { tmin = P.trig_min[64u + tid]; tmax = P.trig_max[64u + tid]; }
+        ra2_begin_p(sh, 0, tid, __ldcg(&P.trig_min[tid]), __ldcg(&P.trig_max[tid]), hashed);
+        if (S > 1) { tmin = __ldcg(&P.trig_min[64u + tid]); tmax = __ldcg(&P.trig_max[64u + tid]); }
     }
     __syncthreads();
     // Per step, three barriers unless an operand sits in row 0: (load+compute) |
     // (apply + clear next hash) | (marks, row 0, next step's snapshot).
     for (uint32_t i = 0; i < S; ++i) {
+        if (tid == 0 && chunks > 0 && i + 2 < S && (i + 2) % kRaChunk == 0) wait_for((i + 2) / kRaChunk);
         bool in_row0 = false;
 #pragma unroll
         for (int q = 0; q < Q; ++q) {
@@ -478,7 +541,9 @@ __global__ void __launch_bounds__(1024) k_ra_lane0_cached(Prog P, uint32_t S, ui
                 in_row0 |= ra2_compute0(P, c, sh, L[q], j, i);
             }
         }
-        if (__syncthreads_or(in_row0)) {
+        const bool any_row0 = __syncthreads_or(in_row0);
+        if (s_abort) break;  // set before the barrier: every thread leaves together
+        if (any_row0) {
             bool flag = false;
 #pragma unroll
             for (int q = 0; q < Q; ++q) {
@@ -514,8 +579,8 @@ __global__ void __launch_bounds__(1024) k_ra_lane0_cached(Prog P, uint32_t S, ui
             if (i + 1 < S) {
                 ra2_begin_p(sh, i + 1, tid, tmin, tmax, hashed);
                 if (i + 2 < S) {
-                    tmin = P.trig_min[static_cast<size_t>(i + 2) * 64u + tid];
-                    tmax = P.trig_max[static_cast<size_t>(i + 2) * 64u + tid];
+                    tmin = __ldcg(&P.trig_min[static_cast<size_t>(i + 2) * 64u + tid]);
+                    tmax = __ldcg(&P.trig_max[static_cast<size_t>(i + 2) * 64u + tid]);
                 }
             }
         }
@@ -685,6 +750,67 @@ cudaError_t run_optimize(const Prog& P, cudaStream_t s, uint32_t* sweeps_out) {
     return cudaGetLastError();
 }
 
+// Shape of the register allocation launch: T threads (at least 64, one per physical
+// register in the row-0 phases), Q lane-0 slots per thread, K symbol-cache entries per
+// lane-0 function and Kf per independent function, within about 160 KB of shared memory.
+template <int Q>
+cudaError_t launch_ra_steps_q(const Prog& P0, const Prog& Pfree, uint32_t G0, uint32_t T, cudaStream_t s) {
+    const uint32_t free_fns = P0.F - G0;
+    constexpr size_t kBudget = 160u * 1024u;
+    uint32_t K = 64;
+    const size_t fixed = sizeof(Ra2Shared) + 16ull * G0;
+    while (K > 1 && fixed + static_cast<size_t>(G0) * K * 8u > kBudget) K >>= 1;
+    uint32_t Kf = 64;
+    while (Kf > 1 && static_cast<size_t>(T) * Kf * 8u > kBudget) Kf >>= 1;
+    const size_t smem = std::max(fixed + static_cast<size_t>(G0) * K * 8u, static_cast<size_t>(T) * Kf * 8u) + 16;
+    cudaError_t ce = cudaFuncSetAttribute(k_ra_steps<Q>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+    if (ce != cudaSuccess) return ce;
+    uint32_t S = P0.S;
+    // One launch when its blocks can all be resident: the independent functions run
+    // beside the lane-0 block, which waits on their progress (so the launch must be
+    // cooperative).  Otherwise the independent functions run first.
+    bool fused = false;
+    const uint32_t free_blocks = (free_fns + T - 1u) / T;
+    if (free_fns > 0) {
+        int dev = 0, coop = 0, sms = 0, per_sm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_ra_steps<Q>, static_cast<int>(T), smem);
+        fused = coop != 0 && static_cast<long long>(per_sm) * sms >= 1ll + free_blocks;
+    }
+    if (fused) {
+        uint32_t chunks = (S + kRaChunk - 1u) / kRaChunk;
+        cudaMemsetAsync(P0.ra_chunks, 0, 2ull * chunks * sizeof(uint32_t), s);
+        g_launches++;
+        k_ra_chunk_hist<<<grid_for(free_fns), kThreads, 0, s>>>(P0, free_fns);
+        Prog Pl = P0;
+        void* args[] = {&Pl, &S, &K, &Kf, &chunks};
+        g_launches++;
+        return cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(k_ra_steps<Q>), dim3(1 + free_blocks),
+                                           dim3(T), args, smem, s);
+    }
+    if (free_fns) {
+        g_launches++;
+        k_ra_free_cached<<<(free_fns + kRaFreeThreads - 1) / kRaFreeThreads, kRaFreeThreads, 0, s>>>(Pfree);
+    }
+    g_launches++;
+    k_ra_steps<Q><<<1, T, smem, s>>>(P0, S, K, Kf, 0u);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_ra_steps(const Prog& P0, const Prog& Pfree, uint32_t G0, cudaStream_t s) {
+    const uint32_t T = G0 <= 1024u ? std::max(64u, (G0 + 31u) & ~31u) : 1024u;
+    const uint32_t Q = (G0 + T - 1u) / T;
+    switch (Q) {
+        case 1: return launch_ra_steps_q<1>(P0, Pfree, G0, T, s);
+        case 2: return launch_ra_steps_q<2>(P0, Pfree, G0, T, s);
+        case 3:
+        case 4: return launch_ra_steps_q<4>(P0, Pfree, G0, T, s);
+        default: return launch_ra_steps_q<8>(P0, Pfree, G0, T, s);
+    }
+}
+
 cudaError_t run_regalloc_steps(const Prog& P, cudaStream_t s, bool* serial_out, bool row0_hash) {
     // Programs whose functions share symbols need the reference's serial order.
     cudaMemsetAsync(P.flags + 1, 0, 2 * sizeof(uint32_t), s);
@@ -708,40 +834,7 @@ cudaError_t run_regalloc_steps(const Prog& P, cudaStream_t s, bool* serial_out, 
         g_launches++;
         k_ra_serial<<<1, 1, 0, s>>>(P);
     } else {
-        const uint32_t free_fns = P.F - G0;
-        if (free_fns) {
-            g_launches++;
-            k_ra_free_cached<<<(free_fns + kRaFreeThreads - 1) / kRaFreeThreads, kRaFreeThreads, 0, s>>>(Pfree);
-        }
-        // at least 64 threads: one per physical register in the row-0 phases
-        const uint32_t T = G0 <= 1024u ? std::max(64u, (G0 + 31u) & ~31u) : 1024u;
-        const uint32_t Q = (G0 + T - 1u) / T;
-        // symbol cache entries per function: the largest power of two within ~160 KB
-        uint32_t K = 64;
-        const size_t fixed = sizeof(Ra2Shared) + 16ull * G0;
-        while (K > 1 && fixed + static_cast<size_t>(G0) * K * 8u > 160u * 1024u) K >>= 1;
-        const size_t smem = fixed + static_cast<size_t>(G0) * K * 8u + 16;
-        g_launches++;
-        cudaError_t ce = cudaSuccess;
-        switch (Q) {
-            case 1:
-                ce = cudaFuncSetAttribute(k_ra_lane0_cached<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-                k_ra_lane0_cached<1><<<1, T, smem, s>>>(P0, P.S, K);
-                break;
-            case 2:
-                ce = cudaFuncSetAttribute(k_ra_lane0_cached<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-                k_ra_lane0_cached<2><<<1, T, smem, s>>>(P0, P.S, K);
-                break;
-            case 3:
-            case 4:
-                ce = cudaFuncSetAttribute(k_ra_lane0_cached<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-                k_ra_lane0_cached<4><<<1, T, smem, s>>>(P0, P.S, K);
-                break;
-            default:
-                ce = cudaFuncSetAttribute(k_ra_lane0_cached<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-                k_ra_lane0_cached<8><<<1, T, smem, s>>>(P0, P.S, K);
-                break;
-        }
+        const cudaError_t ce = launch_ra_steps(P0, Pfree, G0, s);
         if (ce != cudaSuccess) return ce;
     }
     g_launches++;

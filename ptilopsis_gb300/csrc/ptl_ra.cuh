@@ -78,9 +78,16 @@ PTL_HD bool ra_own_in(uint32_t start, uint32_t size, uint32_t r) {
 }
 
 // ---------------------------------------------------------------- independent functions
+// Steps per progress chunk: when the lane-0 pass runs beside the independent functions,
+// each function counts the chunks whose trigger records it has finished.
+constexpr uint32_t kRaChunk = 32;
+
 // Functions outside lane 0: no marks reach their symbols, so the loop needs only the
 // physical registers (kept in the cache) and emits trigger records for the lane-0 pass.
-PTL_HD void ra_free_function_cached(const Prog& P, const SymCache& c, uint32_t slot, uint32_t f) {
+// done (device only, may be null): per-chunk count of functions whose records for that
+// chunk are complete; the fence orders the records before the count.
+PTL_HD void ra_free_function_cached(const Prog& P, const SymCache& c, uint32_t slot, uint32_t f,
+                                    uint32_t* done = nullptr) {
     cache_reset(c, slot);
     unsigned long long lifetime = 0x1Full;
     const uint32_t g1 = f / 8u + 1u;
@@ -109,6 +116,12 @@ PTL_HD void ra_free_function_cached(const Prog& P, const SymCache& c, uint32_t s
             at_min_u32(&P.trig_min[static_cast<size_t>(i) * 64u + p], g1);
             at_max_u32(&P.trig_max[static_cast<size_t>(i) * 64u + p], g1);
         }
+#if defined(__CUDA_ARCH__)
+        if (done && (!have || (i + 1u) % kRaChunk == 0)) {
+            __threadfence();
+            atomicAdd(&done[i / kRaChunk], 1u);
+        }
+#endif
     }
 }
 
