@@ -155,20 +155,20 @@ struct Model {
                 ra2_load(P, L[j], i, cur.data() + 4 * j);
                 in_row0 |= ra2_compute0(P, c, sh, L[j], j, i);
             }
-            if (in_row0) {
-                bool flag = false;
-                for (uint32_t j = 0; j < G0; ++j) flag |= ra2_check(sh, L[j]);
-                if (flag) {
-                    for (uint32_t round = 0;; ++round) {
-                        for (uint32_t j = 0; j < G0; ++j) ra2_round(sh, L[j]);
-                        bool changed = false;
-                        for (uint32_t p = 0; p < 64; ++p) changed |= ra2_round_p(sh, p);
-                        if (!changed) break;
-                        if (round > G0 + 2) { record_error(P.err, ST_DEVICE_TIMEOUT, W_RA2, i); break; }
-                    }
-                }
-            }
+            bool flag = false;
+            if (in_row0) for (uint32_t j = 0; j < G0; ++j) flag |= ra2_check(sh, L[j]);
             for (uint32_t j = 0; j < G0; ++j) ra2_apply(P, c, sh, L[j], j, i, cur.data() + 4 * j);
+            if (flag) {
+                for (uint32_t p = 0; p < 64; ++p) sh.r0grp[p] = 0;
+                for (uint32_t round = 0;; ++round) {
+                    for (uint32_t j = 0; j < G0; ++j) ra2_round(sh, L[j]);
+                    bool changed = false;
+                    for (uint32_t p = 0; p < 64; ++p) changed |= ra2_round_p(sh, p);
+                    if (!changed) break;
+                    if (round > G0 + 2) { record_error(P.err, ST_DEVICE_TIMEOUT, W_RA2, i); break; }
+                }
+                for (uint32_t j = 0; j < G0; ++j) ra2_apply(P, c, sh, L[j], j, i, cur.data() + 4 * j);
+            }
             if (hashed) for (uint32_t p = 0; p < 64; ++p) snap_clear_next(sh, i, p);
             for (uint32_t p = 0; p < 64; ++p) {
                 ra2_end_p(P, c, sh, p, cur.data());

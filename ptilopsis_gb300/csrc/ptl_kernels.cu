@@ -528,8 +528,8 @@ __global__ void __launch_bounds__(1024) k_ra_steps(Prog P, uint32_t S, uint32_t 
         if (S > 1) { tmin = __ldcg(&P.trig_min[64u + tid]); tmax = __ldcg(&P.trig_max[64u + tid]); }
     }
     __syncthreads();
-    // Per step, three barriers unless an operand sits in row 0: (load+compute) |
-    // (apply + clear next hash) | (marks, row 0, next step's snapshot).
+    // Per step, three barriers: (load+compute) | (check + speculative apply + clear next
+    // hash) | (marks, row 0, next step's snapshot).
     for (uint32_t i = 0; i < S; ++i) {
         if (tid == 0 && chunks > 0 && i + 2 < S && (i + 2) % kRaChunk == 0) wait_for((i + 2) / kRaChunk);
         bool in_row0 = false;
@@ -543,28 +543,14 @@ __global__ void __launch_bounds__(1024) k_ra_steps(Prog P, uint32_t S, uint32_t 
         }
         const bool any_row0 = __syncthreads_or(in_row0);
         if (s_abort) break;  // set before the barrier: every thread leaves together
+        // Apply speculatively; if an earlier lane-0 trigger changes what some slot read
+        // (rare), undo the row-0 writes, iterate to the fixed point and apply again.
+        bool flag = false;
         if (any_row0) {
-            bool flag = false;
 #pragma unroll
             for (int q = 0; q < Q; ++q) {
                 const uint32_t j = tid + static_cast<uint32_t>(q) * T;
                 if (j < G0) flag |= ra2_check(sh, L[q]);
-            }
-            if (__syncthreads_or(flag)) {
-                for (uint32_t round = 0;; ++round) {
-#pragma unroll
-                    for (int q = 0; q < Q; ++q) {
-                        const uint32_t j = tid + static_cast<uint32_t>(q) * T;
-                        if (j < G0) ra2_round(sh, L[q]);
-                    }
-                    __syncthreads();
-                    const bool changed = tid < 64 ? ra2_round_p(sh, tid) : false;
-                    if (!__syncthreads_or(changed)) break;
-                    if (round > G0 + 2u) {
-                        if (tid == 0) record_error(P.err, ST_DEVICE_TIMEOUT, W_RA2, i);
-                        break;
-                    }
-                }
             }
         }
 #pragma unroll
@@ -573,7 +559,29 @@ __global__ void __launch_bounds__(1024) k_ra_steps(Prog P, uint32_t S, uint32_t 
             if (j < G0) ra2_apply(P, c, sh, L[q], j, i, cur + 4u * j);
         }
         if (hashed && tid < 64) snap_clear_next(sh, i, tid);
-        __syncthreads();
+        if (__syncthreads_or(flag)) {
+            if (tid < 64) sh.r0grp[tid] = 0;
+            for (uint32_t round = 0;; ++round) {
+#pragma unroll
+                for (int q = 0; q < Q; ++q) {
+                    const uint32_t j = tid + static_cast<uint32_t>(q) * T;
+                    if (j < G0) ra2_round(sh, L[q]);
+                }
+                __syncthreads();
+                const bool changed = tid < 64 ? ra2_round_p(sh, tid) : false;
+                if (!__syncthreads_or(changed)) break;
+                if (round > G0 + 2u) {
+                    if (tid == 0) record_error(P.err, ST_DEVICE_TIMEOUT, W_RA2, i);
+                    break;
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < Q; ++q) {
+                const uint32_t j = tid + static_cast<uint32_t>(q) * T;
+                if (j < G0) ra2_apply(P, c, sh, L[q], j, i, cur + 4u * j);
+            }
+            __syncthreads();
+        }
         if (tid < 64) {
             ra2_end_p(P, c, sh, tid, cur);
             if (i + 1 < S) {

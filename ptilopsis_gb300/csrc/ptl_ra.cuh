@@ -148,7 +148,7 @@ struct Ra2Slot {
     uint32_t j;            // group index (function 8j)
     uint32_t start, size;  // the function's isn_cnt instruction range
     bool act;
-    unsigned long long lifetime;
+    unsigned long long lifetime, lt_new;  // live mask before the step; after it (set by ra2_apply)
     RaStep S, next;
     bool have_next;
     uint32_t r1reg, r2reg;
@@ -225,7 +225,7 @@ PTL_HD bool marked_before(const Ra2Shared& sh, uint64_t m, uint32_t j, bool with
 
 PTL_HD void ra2_slot_init(const Prog& P, const SymCache& c, Ra2Slot& L, uint32_t slot, uint32_t j) {
     L.j = j;
-    L.lifetime = 0x1Full;
+    L.lifetime = L.lt_new = 0x1Full;
     L.start = 8u * j < P.F ? P.fn_start0[8u * j] : 0u;
     L.size = 8u * j < P.F ? P.fn_size0[8u * j] : 0u;
     L.have_next = 8u * j < P.F && ra_load_at(P, L.start, L.size, 0, L.next);
@@ -250,6 +250,7 @@ PTL_HD void ra2_begin_p(Ra2Shared& sh, uint32_t i, uint32_t p, uint32_t tmin, ui
 // Loads the slot's instruction of step i (prefetched in the previous step).  cur[0..2]:
 // what the slot updates this step (for the mark phase); cur[3] is set by ra2_apply.
 PTL_HD void ra2_load(const Prog& P, Ra2Slot& L, uint32_t i, uint32_t* cur) {
+    L.lifetime = L.lt_new;
     L.act = L.have_next;
     if (L.act) {
         L.S = L.next;
@@ -335,13 +336,15 @@ PTL_HD bool ra2_round_p(Ra2Shared& sh, uint32_t p) {
 
 // Apply the step: lifetime, own symbol updates (swapped only when a later group marks
 // the symbol in this step), row-0 writes as the highest writing group per position.
+// Applying again after Jacobi rounds rewrites the same symbols and records (row-0
+// group maxima are reset in between), so a step may be applied speculatively.
 // The winner's value follows from its record: its defined register at its rd position
 // (cur[3]), a cleared entry (0xFFFFFFFF) at its rs1/rs2 positions.
 PTL_HD void ra2_apply(const Prog& P, const SymCache& c, Ra2Shared& sh, Ra2Slot& L, uint32_t slot, uint32_t i,
                       uint32_t* cur) {
     if (!L.act) return;
     const RaStep& S = L.S;
-    L.lifetime = S.cleared | S.rdm;
+    L.lt_new = S.cleared | S.rdm;
     const uint32_t g1 = L.j + 1u;
     auto later = [&](uint64_t m) {
         for (; m; m &= m - 1) {
