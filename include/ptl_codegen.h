@@ -140,6 +140,51 @@ size_t ptl_code_table(int which, uint32_t* out);
 ptl_status ptl_optimize_noalloc(const uint32_t* instr, const uint32_t* rd, const uint32_t* rs1,
                                 const uint32_t* rs2, size_t count, uint32_t* used_instrs, void* stream);
 
+/* ---- Batched compilation.  No counterpart in the reference, which compiles one tree per
+ * process (src/main.cpp:121-157).  A batch keeps `workers` host threads, each with its own
+ * generator (resident device arena, own stream), so that the compiles of a call overlap
+ * on the GPU; programs are taken largest first.  Each program's output is identical to
+ * compiling it alone. */
+typedef struct ptl_batch ptl_batch;
+ptl_status ptl_batch_create(int device, int workers, ptl_batch** out);
+/* Compiles count host trees; blocks until all are done.  Returns the first non-OK status
+ * (per-program status: ptl_batch_status).  Results stay valid until the next compile. */
+ptl_status ptl_batch_compile(ptl_batch* batch, const ptl_ast_view* trees, size_t count);
+ptl_status ptl_batch_status(const ptl_batch* batch, size_t k);
+ptl_status ptl_batch_words(const ptl_batch* batch, size_t k, const uint32_t** words, size_t* count);
+ptl_status ptl_batch_function_table(const ptl_batch* batch, size_t k, const uint32_t** starts,
+                                    const uint32_t** ends, const uint32_t** sizes, const uint32_t** ids,
+                                    size_t* count);
+/* Wall time of the last ptl_batch_compile, in ns. */
+uint64_t ptl_batch_elapsed_ns(const ptl_batch* batch);
+void ptl_batch_destroy(ptl_batch* batch);
+
+/* ---- Compile server.  No counterpart in the reference.  `slots` worker threads, each
+ * with a resident generator, take queued requests in arrival order as soon as a slot is
+ * free and the request's device-memory estimate fits in what is left of memory_budget
+ * (a later request that fits may pass one that does not); compiles of different slots
+ * overlap on the GPU.  Results are identical to compiling each tree alone. */
+typedef struct ptl_server ptl_server;
+ptl_status ptl_server_create(int device, int slots, uint64_t memory_budget, ptl_server** out);
+/* Copies a host tree into a request and queues it; PTL_ADMISSION_DENIED when the request
+ * alone exceeds the budget. */
+ptl_status ptl_server_submit(ptl_server* server, const ptl_ast_view* tree, uint64_t* ticket);
+/* *done = 1 once the request finished (wait != 0 blocks until then); returns its status. */
+ptl_status ptl_server_poll(ptl_server* server, uint64_t ticket, int wait, int* done);
+/* Output of a finished request (the table pointers may be NULL); valid until release. */
+ptl_status ptl_server_result(ptl_server* server, uint64_t ticket, const uint32_t** words, size_t* count,
+                             const uint32_t** starts, const uint32_t** ends, const uint32_t** sizes,
+                             const uint32_t** ids, size_t* functions);
+/* Submit, start and completion times of a finished request (ptl_clock_ns clock). */
+ptl_status ptl_server_times(ptl_server* server, uint64_t ticket, uint64_t times[3]);
+ptl_status ptl_server_release(ptl_server* server, uint64_t ticket);
+/* stats[0..3]: requests completed, nodes compiled, requests queued, admitted bytes in flight. */
+ptl_status ptl_server_stats(ptl_server* server, uint64_t stats[4]);
+/* Destroys the server after the compiles in flight; queued requests are dropped. */
+void ptl_server_destroy(ptl_server* server);
+/* The monotonic clock of the server's times, in ns. */
+uint64_t ptl_clock_ns(void);
+
 /* Kernel launches the library has issued so far (all generators of the process). */
 uint64_t ptl_kernel_launches(void);
 

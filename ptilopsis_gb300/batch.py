@@ -1,0 +1,206 @@
+"""Batched compilation and the compile server (ptl_batch_* / ptl_server_* of
+include/ptl_codegen.h).
+
+Neither exists in the reference, which compiles one tree per process.  Both run a pool of
+worker threads in libptl_gb300.so, each owning a generator with a resident device arena
+and its own stream, so compiles overlap on the GPU; every program's output is identical to
+compiling it alone.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+from typing import List, Optional, Sequence
+
+import numpy as np
+
+from .codegen import DepthTree, PtlError, _AstView, _view, lib
+
+_u32p = ctypes.POINTER(ctypes.c_uint32)
+
+
+def _bind(L):
+    if getattr(L, "_ptl_batch_bound", False):
+        return L
+    vp, sz, u64 = ctypes.c_void_p, ctypes.c_size_t, ctypes.c_uint64
+    L.ptl_batch_create.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.POINTER(vp)]
+    L.ptl_batch_compile.argtypes = [vp, ctypes.POINTER(_AstView), sz]
+    L.ptl_batch_status.argtypes = [vp, sz]
+    L.ptl_batch_words.argtypes = [vp, sz, ctypes.POINTER(_u32p), ctypes.POINTER(sz)]
+    L.ptl_batch_function_table.argtypes = [vp, sz] + [ctypes.POINTER(_u32p)] * 4 + [ctypes.POINTER(sz)]
+    L.ptl_batch_elapsed_ns.argtypes = [vp]
+    L.ptl_batch_elapsed_ns.restype = u64
+    L.ptl_batch_destroy.argtypes = [vp]
+    L.ptl_batch_destroy.restype = None
+    L.ptl_server_create.argtypes = [ctypes.c_int, ctypes.c_int, u64, ctypes.POINTER(vp)]
+    L.ptl_server_submit.argtypes = [vp, ctypes.POINTER(_AstView), ctypes.POINTER(u64)]
+    L.ptl_server_poll.argtypes = [vp, u64, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
+    L.ptl_server_result.argtypes = [vp, u64, ctypes.POINTER(_u32p), ctypes.POINTER(sz)] + \
+        [ctypes.POINTER(_u32p)] * 4 + [ctypes.POINTER(sz)]
+    L.ptl_server_times.argtypes = [vp, u64, ctypes.POINTER(u64)]
+    L.ptl_server_release.argtypes = [vp, u64]
+    L.ptl_server_stats.argtypes = [vp, ctypes.POINTER(u64)]
+    L.ptl_server_destroy.argtypes = [vp]
+    L.ptl_server_destroy.restype = None
+    L.ptl_clock_ns.argtypes = []
+    L.ptl_clock_ns.restype = u64
+    for fn in ("ptl_batch_create", "ptl_batch_compile", "ptl_batch_status", "ptl_batch_words",
+               "ptl_batch_function_table", "ptl_server_create", "ptl_server_submit", "ptl_server_poll",
+               "ptl_server_result", "ptl_server_times", "ptl_server_release", "ptl_server_stats"):
+        getattr(L, fn).restype = ctypes.c_int
+    L._ptl_batch_bound = True
+    return L
+
+
+def _arr(p, n) -> np.ndarray:
+    if n == 0:
+        return np.zeros(0, np.uint32)
+    return np.ctypeslib.as_array(p, shape=(n,)).copy()
+
+
+@dataclass
+class Compiled:
+    words: np.ndarray
+    table: dict  # starts, ends, sizes, ids
+
+
+def clock_ns() -> int:
+    """The monotonic clock of the server's request times."""
+    return int(_bind(lib()).ptl_clock_ns())
+
+
+class BatchCompiler:
+    """Compiles many programs per call on `workers` concurrent generators."""
+
+    def __init__(self, device: int = 0, workers: int = 8):
+        self._lib = _bind(lib())
+        self._h = ctypes.c_void_p()
+        st = self._lib.ptl_batch_create(device, workers, ctypes.byref(self._h))
+        if st != 0:
+            raise PtlError(st, "ptl_batch_create")
+
+    def compile(self, trees: Sequence[DepthTree]) -> None:
+        """Compiles the trees (host arrays); results via result(k)."""
+        keep: list = []
+        views = (_AstView * len(trees))(*[_view(t, keep) for t in trees])
+        self._n = len(trees)
+        st = self._lib.ptl_batch_compile(self._h, views, len(trees))
+        if st != 0:
+            raise PtlError(st, "ptl_batch_compile")
+
+    def elapsed_ns(self) -> int:
+        return int(self._lib.ptl_batch_elapsed_ns(self._h))
+
+    def words(self, k: int) -> np.ndarray:
+        p, n = _u32p(), ctypes.c_size_t()
+        st = self._lib.ptl_batch_words(self._h, k, ctypes.byref(p), ctypes.byref(n))
+        if st != 0:
+            raise PtlError(st, f"ptl_batch_words({k})")
+        return _arr(p, n.value)
+
+    def function_table(self, k: int) -> dict:
+        ptrs = [_u32p() for _ in range(4)]
+        n = ctypes.c_size_t()
+        st = self._lib.ptl_batch_function_table(self._h, k, *[ctypes.byref(p) for p in ptrs], ctypes.byref(n))
+        if st != 0:
+            raise PtlError(st, f"ptl_batch_function_table({k})")
+        return {name: _arr(p, n.value) for name, p in zip(("starts", "ends", "sizes", "ids"), ptrs)}
+
+    def result(self, k: int) -> Compiled:
+        return Compiled(self.words(k), self.function_table(k))
+
+    def close(self) -> None:
+        if self._h:
+            self._lib.ptl_batch_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class CompileServer:
+    """Continuous-batching compile server: `slots` concurrent compiles, admission against a
+    device-memory budget (bytes)."""
+
+    def __init__(self, device: int = 0, slots: int = 8, memory_budget: int = 120 << 30):
+        self._lib = _bind(lib())
+        self._h = ctypes.c_void_p()
+        st = self._lib.ptl_server_create(device, slots, memory_budget, ctypes.byref(self._h))
+        if st != 0:
+            raise PtlError(st, "ptl_server_create")
+
+    def submit(self, tree: DepthTree) -> int:
+        keep: list = []
+        view = _view(tree, keep)
+        t = ctypes.c_uint64()
+        st = self._lib.ptl_server_submit(self._h, ctypes.byref(view), ctypes.byref(t))
+        if st != 0:
+            raise PtlError(st, "ptl_server_submit")
+        return int(t.value)
+
+    def poll(self, ticket: int, wait: bool = False) -> bool:
+        done = ctypes.c_int()
+        st = self._lib.ptl_server_poll(self._h, ticket, 1 if wait else 0, ctypes.byref(done))
+        if st != 0:
+            raise PtlError(st, f"request {ticket}")
+        return bool(done.value)
+
+    def result(self, ticket: int) -> Compiled:
+        self.poll(ticket, wait=True)
+        p, n = _u32p(), ctypes.c_size_t()
+        ptrs = [_u32p() for _ in range(4)]
+        f = ctypes.c_size_t()
+        st = self._lib.ptl_server_result(self._h, ticket, ctypes.byref(p), ctypes.byref(n),
+                                         *[ctypes.byref(q) for q in ptrs], ctypes.byref(f))
+        if st != 0:
+            raise PtlError(st, f"request {ticket}")
+        return Compiled(_arr(p, n.value), {name: _arr(q, f.value)
+                                           for name, q in zip(("starts", "ends", "sizes", "ids"), ptrs)})
+
+    def times(self, ticket: int) -> tuple:
+        """(submitted, started, finished) in clock_ns() time."""
+        t = (ctypes.c_uint64 * 3)()
+        st = self._lib.ptl_server_times(self._h, ticket, t)
+        if st != 0:
+            raise PtlError(st, f"request {ticket}")
+        return int(t[0]), int(t[1]), int(t[2])
+
+    def release(self, ticket: int) -> None:
+        self._lib.ptl_server_release(self._h, ticket)
+
+    def stats(self) -> dict:
+        s = (ctypes.c_uint64 * 4)()
+        self._lib.ptl_server_stats(self._h, s)
+        return {"completed": int(s[0]), "nodes": int(s[1]), "queued": int(s[2]), "bytes_in_flight": int(s[3])}
+
+    def close(self) -> None:
+        if self._h:
+            self._lib.ptl_server_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def compile_many(trees: Sequence[DepthTree], device: int = 0, workers: int = 8) -> List[Compiled]:
+    with BatchCompiler(device, workers) as b:
+        b.compile(trees)
+        return [b.result(k) for k in range(len(trees))]

@@ -58,7 +58,8 @@ def _src(*names: str) -> list[str]:
 
 def build_cuda(force: bool = False) -> str:
     hdrs = _src(*HEADERS) + [os.path.join(ROOT, "include", "ptl_codegen.h")]
-    units = [("ptl_kernels.cu", "nvcc"), ("ptl_capi.cu", "nvcc"), ("ptl_noalloc.cu", "nvcc"), ("ptl_tables.cpp", "cxx")]
+    units = [("ptl_kernels.cu", "nvcc"), ("ptl_capi.cu", "nvcc"), ("ptl_noalloc.cu", "nvcc"), ("ptl_tables.cpp", "cxx"),
+             ("ptl_batch.cpp", "cxx")]
     all_src = _src(*(u for u, _ in units)) + hdrs
     if not force and _newer(CUDA_LIB, all_src):
         return CUDA_LIB
@@ -75,7 +76,7 @@ def build_cuda(force: bool = False) -> str:
     with cf.ThreadPoolExecutor(max_workers=len(jobs)) as ex:
         for f in [ex.submit(_run, cmd) for cmd, _ in jobs]:
             f.result()
-    _run([nvcc, *ARCH, "-shared", "-o", CUDA_LIB, *[o for _, o in jobs], "-lcudart"])
+    _run([nvcc, *ARCH, "-shared", "-o", CUDA_LIB, *[o for _, o in jobs], "-lcudart", "-lpthread"])
     return CUDA_LIB
 
 

@@ -1,0 +1,347 @@
+// Batched compilation and the compile server (include/ptl_codegen.h: ptl_batch_*,
+// ptl_server_*), built on the generator entry points.
+//
+// Neither has a counterpart in the reference, which compiles one tree per process
+// (src/main.cpp:121-157).  Both keep a pool of worker threads, each owning one generator:
+// its device arena stays resident and grows to the largest program it has compiled,
+// and its stream lets the compiles of different workers overlap on the GPU (the
+// register allocation chains of different programs then run on different SMs).
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <memory>
+#include <mutex>
+#include <new>
+#include <numeric>
+#include <string>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/ptl_codegen.h"
+
+namespace {
+
+uint64_t now_ns() {
+    return static_cast<uint64_t>(
+        std::chrono::duration_cast<std::chrono::nanoseconds>(std::chrono::steady_clock::now().time_since_epoch())
+            .count());
+}
+
+// One compiled program, copied out of the generator that made it.
+struct Result {
+    ptl_status status = PTL_OK;
+    std::vector<uint32_t> words, starts, ends, sizes, ids;
+};
+
+// Compiles tree on gen (created on first use) and copies the output into r.
+void compile_into(ptl_generator*& gen, int device, const ptl_ast_view& tree, Result& r) {
+    ptl_status st = gen ? ptl_generator_upload(gen, &tree) : ptl_generator_create(&tree, device, &gen);
+    if (st == PTL_OK) st = ptl_generator_process(gen, 0);
+    if (st == PTL_OK) {
+        const uint32_t* w = nullptr;
+        size_t n = 0;
+        st = ptl_generator_instructions(gen, &w, &n);
+        if (st == PTL_OK) r.words.assign(w, w + n);
+    }
+    if (st == PTL_OK) {
+        const uint32_t *s = nullptr, *e = nullptr, *z = nullptr, *id = nullptr;
+        size_t f = 0;
+        st = ptl_generator_function_table(gen, &s, &e, &z, &id, &f);
+        if (st == PTL_OK) {
+            r.starts.assign(s, s + f);
+            r.ends.assign(e, e + f);
+            r.sizes.assign(z, z + f);
+            r.ids.assign(id, id + f);
+        }
+    }
+    r.status = st;
+}
+
+// Device footprint of a compile, for admission: the generator's arrays for n nodes (about
+// 190 bytes per node with the word arrays at ~1.3 words per node and the scratch, plus
+// the arena's growth margin) and fixed scratch.
+uint64_t footprint(size_t n) { return 64ull * 1024 * 1024 + 256ull * n; }
+
+}  // namespace
+
+// ===================================================================== batch
+struct ptl_batch {
+    int device = 0;
+    int workers = 1;
+    std::vector<ptl_generator*> gens;
+    std::vector<Result> results;
+    uint64_t last_ns = 0;
+};
+
+extern "C" ptl_status ptl_batch_create(int device, int workers, ptl_batch** out) {
+    if (!out || workers < 1 || workers > 256) return PTL_BAD_ARGUMENT;
+    ptl_batch* b = new (std::nothrow) ptl_batch;
+    if (!b) return PTL_OOM;
+    b->device = device;
+    b->workers = workers;
+    b->gens.assign(static_cast<size_t>(workers), nullptr);
+    *out = b;
+    return PTL_OK;
+}
+
+extern "C" ptl_status ptl_batch_compile(ptl_batch* b, const ptl_ast_view* trees, size_t count) {
+    if (!b || (!trees && count)) return PTL_BAD_ARGUMENT;
+    b->results.assign(count, Result{});
+    // largest first, so that the long compiles do not trail at the end
+    std::vector<size_t> order(count);
+    std::iota(order.begin(), order.end(), size_t{0});
+    std::stable_sort(order.begin(), order.end(), [&](size_t x, size_t y) { return trees[x].n > trees[y].n; });
+    std::atomic<size_t> next{0};
+    const uint64_t t0 = now_ns();
+    auto work = [&](int w) {
+        for (;;) {
+            const size_t i = next.fetch_add(1);
+            if (i >= count) break;
+            const size_t k = order[i];
+            compile_into(b->gens[static_cast<size_t>(w)], b->device, trees[k], b->results[k]);
+        }
+    };
+    const int nw = static_cast<int>(std::min<size_t>(static_cast<size_t>(b->workers), std::max<size_t>(count, 1)));
+    std::vector<std::thread> pool;
+    for (int w = 1; w < nw; ++w) pool.emplace_back(work, w);
+    work(0);
+    for (auto& t : pool) t.join();
+    b->last_ns = now_ns() - t0;
+    for (const Result& r : b->results)
+        if (r.status != PTL_OK) return r.status;
+    return PTL_OK;
+}
+
+extern "C" ptl_status ptl_batch_status(const ptl_batch* b, size_t k) {
+    if (!b || k >= b->results.size()) return PTL_BAD_ARGUMENT;
+    return b->results[k].status;
+}
+
+extern "C" ptl_status ptl_batch_words(const ptl_batch* b, size_t k, const uint32_t** words, size_t* count) {
+    if (!b || !words || !count || k >= b->results.size()) return PTL_BAD_ARGUMENT;
+    const Result& r = b->results[k];
+    if (r.status != PTL_OK) return r.status;
+    *words = r.words.data();
+    *count = r.words.size();
+    return PTL_OK;
+}
+
+extern "C" ptl_status ptl_batch_function_table(const ptl_batch* b, size_t k, const uint32_t** starts,
+                                               const uint32_t** ends, const uint32_t** sizes, const uint32_t** ids,
+                                               size_t* count) {
+    if (!b || !starts || !ends || !sizes || !ids || !count || k >= b->results.size()) return PTL_BAD_ARGUMENT;
+    const Result& r = b->results[k];
+    if (r.status != PTL_OK) return r.status;
+    *starts = r.starts.data();
+    *ends = r.ends.data();
+    *sizes = r.sizes.data();
+    *ids = r.ids.data();
+    *count = r.starts.size();
+    return PTL_OK;
+}
+
+extern "C" uint64_t ptl_batch_elapsed_ns(const ptl_batch* b) { return b ? b->last_ns : 0; }
+
+extern "C" void ptl_batch_destroy(ptl_batch* b) {
+    if (!b) return;
+    for (ptl_generator* g : b->gens) ptl_generator_destroy(g);
+    delete b;
+}
+
+// ===================================================================== server
+namespace {
+
+// A request owns a copy of its tree (the caller's arrays may go away after submit).
+struct Request {
+    uint64_t ticket = 0;
+    size_t n = 0, max_depth = 0;
+    std::vector<uint8_t> type, rtype;
+    std::vector<int32_t> parent, depth, child;
+    std::vector<uint32_t> data;
+    uint64_t bytes = 0;        // admission estimate
+    uint64_t t_submit = 0, t_start = 0, t_done = 0;
+    bool done = false;
+    Result result;
+
+    ptl_ast_view view() const {
+        return ptl_ast_view{n,           max_depth,    type.data(),  rtype.data(), parent.data(),
+                            depth.data(), child.data(), data.data(), 0};
+    }
+};
+
+}  // namespace
+
+struct ptl_server {
+    int device = 0;
+    uint64_t budget = 0;
+    uint64_t in_use = 0;       // admission estimates of the compiles in flight
+    std::mutex mu;
+    std::condition_variable cv_work, cv_done;
+    std::deque<std::shared_ptr<Request>> queue;
+    std::unordered_map<uint64_t, std::shared_ptr<Request>> all;
+    std::vector<std::thread> workers;
+    std::vector<ptl_generator*> gens;
+    uint64_t next_ticket = 1;
+    bool stopping = false;
+    uint64_t completed = 0, nodes_done = 0, busy_ns = 0;
+
+    void run(size_t w) {
+        for (;;) {
+            std::shared_ptr<Request> req;
+            {
+                std::unique_lock<std::mutex> lk(mu);
+                for (;;) {
+                    if (stopping) return;
+                    // first queued request that fits the free budget: requests that
+                    // arrive while others compile are admitted as memory frees up
+                    auto it = std::find_if(queue.begin(), queue.end(),
+                                           [&](const std::shared_ptr<Request>& r) { return in_use + r->bytes <= budget; });
+                    if (it != queue.end()) {
+                        req = *it;
+                        queue.erase(it);
+                        in_use += req->bytes;
+                        break;
+                    }
+                    cv_work.wait(lk);
+                }
+            }
+            req->t_start = now_ns();
+            const ptl_ast_view v = req->view();
+            compile_into(gens[w], device, v, req->result);
+            {
+                std::lock_guard<std::mutex> lk(mu);
+                req->t_done = now_ns();
+                req->done = true;
+                in_use -= req->bytes;
+                ++completed;
+                nodes_done += req->n;
+                busy_ns += req->t_done - req->t_start;
+            }
+            cv_done.notify_all();
+            cv_work.notify_all();
+        }
+    }
+};
+
+extern "C" ptl_status ptl_server_create(int device, int slots, uint64_t memory_budget, ptl_server** out) {
+    if (!out || slots < 1 || slots > 256 || memory_budget == 0) return PTL_BAD_ARGUMENT;
+    ptl_server* s = new (std::nothrow) ptl_server;
+    if (!s) return PTL_OOM;
+    s->device = device;
+    s->budget = memory_budget;
+    s->gens.assign(static_cast<size_t>(slots), nullptr);
+    for (int w = 0; w < slots; ++w) s->workers.emplace_back([s, w] { s->run(static_cast<size_t>(w)); });
+    *out = s;
+    return PTL_OK;
+}
+
+extern "C" ptl_status ptl_server_submit(ptl_server* s, const ptl_ast_view* tree, uint64_t* ticket) {
+    if (!s || !tree || !ticket || tree->on_device) return PTL_BAD_ARGUMENT;
+    auto req = std::make_shared<Request>();
+    const size_t n = tree->n;
+    req->n = n;
+    req->max_depth = tree->max_depth;
+    req->bytes = footprint(n);
+    if (req->bytes > s->budget) return PTL_ADMISSION_DENIED;  // could never be admitted
+    if (n && (!tree->type || !tree->rtype || !tree->parent || !tree->depth || !tree->child_idx || !tree->data))
+        return PTL_BAD_ARGUMENT;
+    req->type.assign(tree->type, tree->type + n);
+    req->rtype.assign(tree->rtype, tree->rtype + n);
+    req->parent.assign(tree->parent, tree->parent + n);
+    req->depth.assign(tree->depth, tree->depth + n);
+    req->child.assign(tree->child_idx, tree->child_idx + n);
+    req->data.assign(tree->data, tree->data + n);
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        req->ticket = s->next_ticket++;
+        req->t_submit = now_ns();
+        s->all[req->ticket] = req;
+        s->queue.push_back(req);
+        *ticket = req->ticket;
+    }
+    s->cv_work.notify_one();
+    return PTL_OK;
+}
+
+// Waits (wait != 0) or checks whether the ticket is done; *done receives the state.
+extern "C" ptl_status ptl_server_poll(ptl_server* s, uint64_t ticket, int wait, int* done) {
+    if (!s || !done) return PTL_BAD_ARGUMENT;
+    std::unique_lock<std::mutex> lk(s->mu);
+    auto it = s->all.find(ticket);
+    if (it == s->all.end()) return PTL_BAD_ARGUMENT;
+    std::shared_ptr<Request> req = it->second;
+    if (wait) s->cv_done.wait(lk, [&] { return req->done; });
+    *done = req->done ? 1 : 0;
+    return req->done ? req->result.status : PTL_OK;
+}
+
+extern "C" ptl_status ptl_server_result(ptl_server* s, uint64_t ticket, const uint32_t** words, size_t* count,
+                                        const uint32_t** starts, const uint32_t** ends, const uint32_t** sizes,
+                                        const uint32_t** ids, size_t* functions) {
+    if (!s || !words || !count) return PTL_BAD_ARGUMENT;
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->all.find(ticket);
+    if (it == s->all.end() || !it->second->done) return PTL_BAD_ARGUMENT;
+    const Result& r = it->second->result;
+    if (r.status != PTL_OK) return r.status;
+    *words = r.words.data();
+    *count = r.words.size();
+    if (starts && ends && sizes && ids && functions) {
+        *starts = r.starts.data();
+        *ends = r.ends.data();
+        *sizes = r.sizes.data();
+        *ids = r.ids.data();
+        *functions = r.starts.size();
+    }
+    return PTL_OK;
+}
+
+// Submit, start and completion times (steady clock, ns) of a finished ticket.
+extern "C" ptl_status ptl_server_times(ptl_server* s, uint64_t ticket, uint64_t times[3]) {
+    if (!s || !times) return PTL_BAD_ARGUMENT;
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->all.find(ticket);
+    if (it == s->all.end() || !it->second->done) return PTL_BAD_ARGUMENT;
+    times[0] = it->second->t_submit;
+    times[1] = it->second->t_start;
+    times[2] = it->second->t_done;
+    return PTL_OK;
+}
+
+extern "C" ptl_status ptl_server_release(ptl_server* s, uint64_t ticket) {
+    if (!s) return PTL_BAD_ARGUMENT;
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->all.find(ticket);
+    if (it == s->all.end() || !it->second->done) return PTL_BAD_ARGUMENT;
+    s->all.erase(it);
+    return PTL_OK;
+}
+
+// stats: completed, nodes compiled, queued, in flight (admission bytes)
+extern "C" ptl_status ptl_server_stats(ptl_server* s, uint64_t stats[4]) {
+    if (!s || !stats) return PTL_BAD_ARGUMENT;
+    std::lock_guard<std::mutex> lk(s->mu);
+    stats[0] = s->completed;
+    stats[1] = s->nodes_done;
+    stats[2] = s->queue.size();
+    stats[3] = s->in_use;
+    return PTL_OK;
+}
+
+extern "C" uint64_t ptl_clock_ns(void) { return now_ns(); }
+
+extern "C" void ptl_server_destroy(ptl_server* s) {
+    if (!s) return;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->stopping = true;
+    }
+    s->cv_work.notify_all();
+    for (auto& t : s->workers) t.join();
+    for (ptl_generator* g : s->gens) ptl_generator_destroy(g);
+    delete s;
+}

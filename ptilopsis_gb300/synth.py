@@ -8,7 +8,8 @@ Workload presets follow the benchmark configurations of this project:
       functions holding more than 31 live values at once
   c2  one huge program: 32,768 functions, lognormal (median 1.5k, sigma 1.2) clipped
       to ~64M nodes, expression depth <= 12, 50% float
-  c3  4,096 independent programs, 1k..500k nodes each (lognormal), 4..512 functions
+  c3  4,096 independent programs, 1k..500k nodes each (lognormal, about 258M nodes in
+      total), 4..512 functions
   c4  compile requests for the server: 80% U[1k, 10k] nodes, 20% lognormal in
       [100k, 2M]
 
@@ -118,12 +119,14 @@ def config_params(name: str, scale: float = 1.0, program: int = 0) -> SynthParam
         return SynthParams(seed=seed, n_functions=max(8, int(32768 * scale)), median_fn_nodes=1500.0, sigma=1.2,
                            max_fn_nodes=4000, max_expr_depth=12, float_frac=0.5, max_nesting=64)
     if name == "c3":
-        # program k: total size lognormal clipped to [1k, 500k], 4..512 functions
+        # program k: total size lognormal (median 22k nodes, sigma 1.6) clipped to [1k, 500k]
+        # -- a mean of about 63k, 258M nodes over 4,096 programs -- in 4..512 functions whose
+        # sizes are lognormal (sigma 0.5) with that mean
         rng = np.random.default_rng(seed ^ program)
-        total = float(np.clip(np.exp(math.log(20000.0) + 1.6 * rng.standard_normal()), 1000, 500000))
+        total = float(np.clip(np.exp(math.log(22000.0) + 1.6 * rng.standard_normal()), 1000, 500000))
         nf = int(np.clip(total / 600.0, 4, 512))
-        return SynthParams(seed=seed ^ program, n_functions=nf, median_fn_nodes=total / nf, sigma=0.8,
-                           max_nesting=32)
+        return SynthParams(seed=seed ^ program, n_functions=nf, median_fn_nodes=total / nf / math.exp(0.125),
+                           sigma=0.5, max_nesting=32)
     if name == "c4":
         rng = np.random.default_rng(seed ^ program)
         if rng.random() < 0.8:

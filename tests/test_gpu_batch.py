@@ -1,0 +1,101 @@
+"""Batched compilation and the compile server through the C ABI: every program's output
+equals compiling it alone with a plain generator, and the oracle for the small ones."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import tree_to_ast
+
+pytestmark = pytest.mark.gpu
+
+
+def _programs(count, seed0=0x50544C60, max_fns=24):
+    from ptilopsis_gb300.synth import SynthParams, generate
+    rng = np.random.default_rng(seed0)
+    out = []
+    for k in range(count):
+        out.append(generate(SynthParams(seed=seed0 + k, n_functions=int(rng.integers(1, max_fns)),
+                                        median_fn_nodes=float(rng.integers(40, 900)), sigma=0.8,
+                                        max_nesting=int(rng.integers(2, 12)), spill_frac=0.2 if k % 3 == 0 else 0.0)))
+    return out
+
+
+def _alone(tree):
+    from ptilopsis_gb300 import RvGenerator
+    with RvGenerator(tree) as g:
+        g.process()
+        return g.get_instructions(), g.function_table()
+
+
+def _assert_same(res, words, table, msg):
+    np.testing.assert_array_equal(res.words, words, err_msg=msg)
+    for k in ("starts", "ends", "sizes", "ids"):
+        np.testing.assert_array_equal(res.table[k], table[k], err_msg=f"{msg} {k}")
+
+
+def test_batch_equals_alone_and_oracle(built_cuda):
+    from oracle import portbind
+    from ptilopsis_gb300.batch import BatchCompiler
+    trees = _programs(48)
+    with BatchCompiler(workers=6) as b:
+        b.compile(trees)
+        for k, t in enumerate(trees):
+            res = b.result(k)
+            w, tab = _alone(t)
+            _assert_same(res, w, tab, f"program {k}")
+            if k % 4 == 0:
+                np.testing.assert_array_equal(res.words, portbind.compile_ast(tree_to_ast(t)).words, err_msg=f"oracle {k}")
+        # a second call on the same workers (arenas reused, other sizes)
+        trees2 = _programs(17, seed0=0x50544C90, max_fns=60)
+        b.compile(trees2)
+        for k, t in enumerate(trees2):
+            w, tab = _alone(t)
+            _assert_same(b.result(k), w, tab, f"second call, program {k}")
+
+
+def test_batch_uneven_sizes(built_cuda):
+    """Large and tiny programs in one call (largest-first scheduling)."""
+    from ptilopsis_gb300.batch import BatchCompiler
+    from ptilopsis_gb300.synth import config_params, generate
+    trees = [generate(config_params("c3", program=k)) for k in (1, 5)] + _programs(12, seed0=0x50544CA0)
+    trees = [t for t in trees if t.n <= 400_000]
+    with BatchCompiler(workers=4) as b:
+        b.compile(trees)
+        for k, t in enumerate(trees):
+            w, tab = _alone(t)
+            _assert_same(b.result(k), w, tab, f"program {k} ({t.n} nodes)")
+
+
+def test_server_results_same_alone_and_in_the_mix(built_cuda):
+    from ptilopsis_gb300.batch import CompileServer
+    trees = _programs(40, seed0=0x50544CB0)
+    alone = [_alone(t) for t in trees]
+    with CompileServer(slots=6, memory_budget=8 << 30) as srv:
+        tickets = [srv.submit(t) for t in trees]
+        for k, tk in enumerate(tickets):
+            _assert_same(srv.result(tk), *alone[k], f"request {k}")
+            s, st, d = srv.times(tk)
+            assert s <= st <= d
+            srv.release(tk)
+        assert srv.stats()["completed"] == len(trees)
+
+
+def test_server_budget_admission(built_cuda):
+    """A budget that fits one request at a time still completes every request correctly;
+    a request larger than the whole budget is refused at submit."""
+    from ptilopsis_gb300 import PtlError
+    from ptilopsis_gb300.batch import CompileServer
+    trees = _programs(10, seed0=0x50544CC0)
+    alone = [_alone(t) for t in trees]
+    budget = (64 << 20) + 256 * max(t.n for t in trees)  # one compile in flight at a time
+    with CompileServer(slots=4, memory_budget=budget) as srv:
+        tickets = [srv.submit(t) for t in trees]
+        for k, tk in enumerate(tickets):
+            _assert_same(srv.result(tk), *alone[k], f"request {k}")
+        from ptilopsis_gb300.synth import SynthParams, generate
+        big = generate(SynthParams(seed=0x50544CD0, n_functions=100, median_fn_nodes=900.0))
+        assert 256 * big.n + (64 << 20) > budget
+        with pytest.raises(PtlError) as e:
+            srv.submit(big)
+        assert e.value.status == 4  # PTL_ADMISSION_DENIED
