@@ -141,14 +141,16 @@ ptl_status ptl_optimize_noalloc(const uint32_t* instr, const uint32_t* rd, const
                                 const uint32_t* rs2, size_t count, uint32_t* used_instrs, void* stream);
 
 /* ---- Batched compilation.  No counterpart in the reference, which compiles one tree per
- * process (src/main.cpp:121-157).  A batch keeps `workers` host threads, each with its own
- * generator (resident device arena, own stream), so that the compiles of a call overlap
- * on the GPU; programs are taken largest first.  Each program's output is identical to
- * compiling it alone. */
+ * process (src/main.cpp:121-157).  All programs of a call go through the seven stages
+ * together: one launch per stage step for the whole batch, per-program arrays in shared
+ * device arenas kept between calls, sizes read back once per batch.  `workers` host
+ * threads gather the inputs.  Each program's output is identical to compiling it alone;
+ * a program that fails a check fails alone. */
 typedef struct ptl_batch ptl_batch;
 ptl_status ptl_batch_create(int device, int workers, ptl_batch** out);
-/* Compiles count host trees; blocks until all are done.  Returns the first non-OK status
- * (per-program status: ptl_batch_status).  Results stay valid until the next compile. */
+/* Compiles count host trees; blocks until all are done.  Returns a batch-wide failure
+ * (ptl_batch_last_error says which) or else the first program's non-OK status; each
+ * program's own status is ptl_batch_status.  Results stay valid until the next compile. */
 ptl_status ptl_batch_compile(ptl_batch* batch, const ptl_ast_view* trees, size_t count);
 ptl_status ptl_batch_status(const ptl_batch* batch, size_t k);
 ptl_status ptl_batch_words(const ptl_batch* batch, size_t k, const uint32_t** words, size_t* count);
@@ -157,6 +159,12 @@ ptl_status ptl_batch_function_table(const ptl_batch* batch, size_t k, const uint
                                     size_t* count);
 /* Wall time of the last ptl_batch_compile, in ns. */
 uint64_t ptl_batch_elapsed_ns(const ptl_batch* batch);
+/* Device time per stage of the last compile (ptl_generator_stage_ns's seven columns). */
+ptl_status ptl_batch_stage_ns(const ptl_batch* batch, uint64_t ns[7]);
+/* Bytes copied host-to-device and device-to-host by the last compile. */
+ptl_status ptl_batch_copied_bytes(const ptl_batch* batch, uint64_t* h2d, uint64_t* d2h);
+/* Detail of the last batch-wide failure. */
+const char* ptl_batch_last_error(const ptl_batch* batch);
 void ptl_batch_destroy(ptl_batch* batch);
 
 /* ---- Compile server.  No counterpart in the reference.  `slots` worker threads, each

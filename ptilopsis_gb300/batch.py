@@ -1,10 +1,11 @@
 """Batched compilation and the compile server (ptl_batch_* / ptl_server_* of
 include/ptl_codegen.h).
 
-Neither exists in the reference, which compiles one tree per process.  Both run a pool of
-worker threads in libptl_gb300.so, each owning a generator with a resident device arena
-and its own stream, so compiles overlap on the GPU; every program's output is identical to
-compiling it alone.
+Neither exists in the reference, which compiles one tree per process.  A batch goes
+through the batched pipeline (one launch per stage step for all its programs); the server
+runs a pool of worker threads in libptl_gb300.so, each owning a generator with a resident
+device arena and its own stream, so compiles overlap on the GPU.  Every program's output is
+identical to compiling it alone.
 """
 from __future__ import annotations
 
@@ -30,6 +31,10 @@ def _bind(L):
     L.ptl_batch_function_table.argtypes = [vp, sz] + [ctypes.POINTER(_u32p)] * 4 + [ctypes.POINTER(sz)]
     L.ptl_batch_elapsed_ns.argtypes = [vp]
     L.ptl_batch_elapsed_ns.restype = u64
+    L.ptl_batch_stage_ns.argtypes = [vp, ctypes.POINTER(u64)]
+    L.ptl_batch_copied_bytes.argtypes = [vp, ctypes.POINTER(u64), ctypes.POINTER(u64)]
+    L.ptl_batch_last_error.argtypes = [vp]
+    L.ptl_batch_last_error.restype = ctypes.c_char_p
     L.ptl_batch_destroy.argtypes = [vp]
     L.ptl_batch_destroy.restype = None
     L.ptl_server_create.argtypes = [ctypes.c_int, ctypes.c_int, u64, ctypes.POINTER(vp)]
@@ -44,7 +49,8 @@ def _bind(L):
     L.ptl_server_destroy.restype = None
     L.ptl_clock_ns.argtypes = []
     L.ptl_clock_ns.restype = u64
-    for fn in ("ptl_batch_create", "ptl_batch_compile", "ptl_batch_status", "ptl_batch_words",
+    for fn in ("ptl_batch_create", "ptl_batch_compile", "ptl_batch_status", "ptl_batch_words", "ptl_batch_stage_ns",
+               "ptl_batch_copied_bytes",
                "ptl_batch_function_table", "ptl_server_create", "ptl_server_submit", "ptl_server_poll",
                "ptl_server_result", "ptl_server_times", "ptl_server_release", "ptl_server_stats"):
         getattr(L, fn).restype = ctypes.c_int
@@ -70,7 +76,8 @@ def clock_ns() -> int:
 
 
 class BatchCompiler:
-    """Compiles many programs per call on `workers` concurrent generators."""
+    """Compiles many programs per call through the batched pipeline (one launch per stage
+    step for the whole batch); `workers` host threads gather the inputs."""
 
     def __init__(self, device: int = 0, workers: int = 8):
         self._lib = _bind(lib())
@@ -79,14 +86,31 @@ class BatchCompiler:
         if st != 0:
             raise PtlError(st, "ptl_batch_create")
 
-    def compile(self, trees: Sequence[DepthTree]) -> None:
-        """Compiles the trees (host arrays); results via result(k)."""
+    def compile(self, trees: Sequence[DepthTree], check: bool = True) -> None:
+        """Compiles the trees (host arrays); results via result(k).  With check=False a
+        program's own failure is left to status(k)."""
         keep: list = []
         views = (_AstView * len(trees))(*[_view(t, keep) for t in trees])
         self._n = len(trees)
         st = self._lib.ptl_batch_compile(self._h, views, len(trees))
-        if st != 0:
-            raise PtlError(st, "ptl_batch_compile")
+        if st != 0 and (check or self._batch_failed()):
+            raise PtlError(st, "ptl_batch_compile: " + (self._lib.ptl_batch_last_error(self._h) or b"").decode())
+
+    def _batch_failed(self) -> bool:
+        return bool(self._lib.ptl_batch_last_error(self._h))
+
+    def status(self, k: int) -> int:
+        return int(self._lib.ptl_batch_status(self._h, k))
+
+    def stage_ns(self) -> list:
+        ns = (ctypes.c_uint64 * 7)()
+        self._lib.ptl_batch_stage_ns(self._h, ns)
+        return list(ns)
+
+    def copied_bytes(self) -> tuple:
+        a, b = ctypes.c_uint64(), ctypes.c_uint64()
+        self._lib.ptl_batch_copied_bytes(self._h, ctypes.byref(a), ctypes.byref(b))
+        return int(a.value), int(b.value)
 
     def elapsed_ns(self) -> int:
         return int(self._lib.ptl_batch_elapsed_ns(self._h))

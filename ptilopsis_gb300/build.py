@@ -29,7 +29,7 @@ CUDA_LIB = os.path.join(LIBDIR, "libptl_gb300.so")
 SYNTH_LIB = os.path.join(LIBDIR, "libptlsynth.so")
 HOSTMODEL_LIB = os.path.join(LIBDIR, "libptl_hostmodel.so")
 
-HEADERS = ["ptl_common.cuh", "ptl_stages.cuh", "ptl_sort.cuh", "ptl_ra.cuh", "ptl_kernels.cuh"]
+HEADERS = ["ptl_common.cuh", "ptl_stages.cuh", "ptl_sort.cuh", "ptl_ra.cuh", "ptl_kernels.cuh", "ptl_bpipe.h"]
 
 
 def _nvcc() -> str:
@@ -58,8 +58,8 @@ def _src(*names: str) -> list[str]:
 
 def build_cuda(force: bool = False) -> str:
     hdrs = _src(*HEADERS) + [os.path.join(ROOT, "include", "ptl_codegen.h")]
-    units = [("ptl_kernels.cu", "nvcc"), ("ptl_capi.cu", "nvcc"), ("ptl_noalloc.cu", "nvcc"), ("ptl_tables.cpp", "cxx"),
-             ("ptl_batch.cpp", "cxx")]
+    units = [("ptl_kernels.cu", "nvcc"), ("ptl_capi.cu", "nvcc"), ("ptl_noalloc.cu", "nvcc"), ("ptl_bpipe.cu", "nvcc"),
+             ("ptl_tables.cpp", "cxx"), ("ptl_batch.cpp", "cxx")]
     all_src = _src(*(u for u, _ in units)) + hdrs
     if not force and _newer(CUDA_LIB, all_src):
         return CUDA_LIB

@@ -1,11 +1,12 @@
 // Batched compilation and the compile server (include/ptl_codegen.h: ptl_batch_*,
-// ptl_server_*), built on the generator entry points.
+// ptl_server_*).
 //
 // Neither has a counterpart in the reference, which compiles one tree per process
-// (src/main.cpp:121-157).  Both keep a pool of worker threads, each owning one generator:
-// its device arena stays resident and grows to the largest program it has compiled,
-// and its stream lets the compiles of different workers overlap on the GPU (the
-// register allocation chains of different programs then run on different SMs).
+// (src/main.cpp:121-157).  A batch runs all its programs through the batched pipeline
+// (one launch per stage step for the whole batch).  The server keeps a pool of worker
+// threads, each owning one generator: its device arena stays resident and grows to the
+// largest program it has compiled, and its stream lets the compiles of different workers
+// overlap on the GPU.
 #include <algorithm>
 #include <atomic>
 #include <chrono>
@@ -22,6 +23,7 @@
 #include <vector>
 
 #include "../../include/ptl_codegen.h"
+#include "ptl_bpipe.h"
 
 namespace {
 
@@ -69,11 +71,10 @@ uint64_t footprint(size_t n) { return 64ull * 1024 * 1024 + 256ull * n; }
 }  // namespace
 
 // ===================================================================== batch
+// One batched pipeline (ptl_bpipe.cu): every stage step is one launch for all programs.
 struct ptl_batch {
-    int device = 0;
-    int workers = 1;
-    std::vector<ptl_generator*> gens;
-    std::vector<Result> results;
+    std::unique_ptr<ptl::BatchPipeline> pipe;
+    std::vector<ptl::BatchResult> results;
     uint64_t last_ns = 0;
 };
 
@@ -81,37 +82,23 @@ extern "C" ptl_status ptl_batch_create(int device, int workers, ptl_batch** out)
     if (!out || workers < 1 || workers > 256) return PTL_BAD_ARGUMENT;
     ptl_batch* b = new (std::nothrow) ptl_batch;
     if (!b) return PTL_OOM;
-    b->device = device;
-    b->workers = workers;
-    b->gens.assign(static_cast<size_t>(workers), nullptr);
+    ptl_status st = PTL_OK;
+    b->pipe.reset(ptl::BatchPipeline::create(device, workers, &st));
+    if (!b->pipe) {
+        delete b;
+        return st;
+    }
     *out = b;
     return PTL_OK;
 }
 
 extern "C" ptl_status ptl_batch_compile(ptl_batch* b, const ptl_ast_view* trees, size_t count) {
     if (!b || (!trees && count)) return PTL_BAD_ARGUMENT;
-    b->results.assign(count, Result{});
-    // largest first, so that the long compiles do not trail at the end
-    std::vector<size_t> order(count);
-    std::iota(order.begin(), order.end(), size_t{0});
-    std::stable_sort(order.begin(), order.end(), [&](size_t x, size_t y) { return trees[x].n > trees[y].n; });
-    std::atomic<size_t> next{0};
     const uint64_t t0 = now_ns();
-    auto work = [&](int w) {
-        for (;;) {
-            const size_t i = next.fetch_add(1);
-            if (i >= count) break;
-            const size_t k = order[i];
-            compile_into(b->gens[static_cast<size_t>(w)], b->device, trees[k], b->results[k]);
-        }
-    };
-    const int nw = static_cast<int>(std::min<size_t>(static_cast<size_t>(b->workers), std::max<size_t>(count, 1)));
-    std::vector<std::thread> pool;
-    for (int w = 1; w < nw; ++w) pool.emplace_back(work, w);
-    work(0);
-    for (auto& t : pool) t.join();
+    const ptl_status st = b->pipe->compile(trees, count, b->results);
     b->last_ns = now_ns() - t0;
-    for (const Result& r : b->results)
+    if (st != PTL_OK) return st;
+    for (const ptl::BatchResult& r : b->results)
         if (r.status != PTL_OK) return r.status;
     return PTL_OK;
 }
@@ -123,10 +110,10 @@ extern "C" ptl_status ptl_batch_status(const ptl_batch* b, size_t k) {
 
 extern "C" ptl_status ptl_batch_words(const ptl_batch* b, size_t k, const uint32_t** words, size_t* count) {
     if (!b || !words || !count || k >= b->results.size()) return PTL_BAD_ARGUMENT;
-    const Result& r = b->results[k];
+    const ptl::BatchResult& r = b->results[k];
     if (r.status != PTL_OK) return r.status;
-    *words = r.words.data();
-    *count = r.words.size();
+    *words = r.words;
+    *count = r.count;
     return PTL_OK;
 }
 
@@ -134,23 +121,33 @@ extern "C" ptl_status ptl_batch_function_table(const ptl_batch* b, size_t k, con
                                                const uint32_t** ends, const uint32_t** sizes, const uint32_t** ids,
                                                size_t* count) {
     if (!b || !starts || !ends || !sizes || !ids || !count || k >= b->results.size()) return PTL_BAD_ARGUMENT;
-    const Result& r = b->results[k];
+    const ptl::BatchResult& r = b->results[k];
     if (r.status != PTL_OK) return r.status;
-    *starts = r.starts.data();
-    *ends = r.ends.data();
-    *sizes = r.sizes.data();
-    *ids = r.ids.data();
-    *count = r.starts.size();
+    *starts = r.starts;
+    *ends = r.ends;
+    *sizes = r.sizes;
+    *ids = r.ids;
+    *count = r.functions;
     return PTL_OK;
 }
 
 extern "C" uint64_t ptl_batch_elapsed_ns(const ptl_batch* b) { return b ? b->last_ns : 0; }
 
-extern "C" void ptl_batch_destroy(ptl_batch* b) {
-    if (!b) return;
-    for (ptl_generator* g : b->gens) ptl_generator_destroy(g);
-    delete b;
+extern "C" ptl_status ptl_batch_stage_ns(const ptl_batch* b, uint64_t ns[7]) {
+    if (!b || !ns) return PTL_BAD_ARGUMENT;
+    b->pipe->stage_ns(ns);
+    return PTL_OK;
 }
+
+extern "C" ptl_status ptl_batch_copied_bytes(const ptl_batch* b, uint64_t* h2d, uint64_t* d2h) {
+    if (!b) return PTL_BAD_ARGUMENT;
+    b->pipe->copied_bytes(h2d, d2h);
+    return PTL_OK;
+}
+
+extern "C" const char* ptl_batch_last_error(const ptl_batch* b) { return b ? b->pipe->last_error() : ""; }
+
+extern "C" void ptl_batch_destroy(ptl_batch* b) { delete b; }
 
 // ===================================================================== server
 namespace {

@@ -1,0 +1,787 @@
+// Batched pipeline (ptl_bpipe.h): the seven stages of rv_generator_avx::process
+// (rv_generator_avx.cpp:104-120) for many programs at once, one launch per stage step for
+// the whole batch.
+//
+// Every per-program array lives in an arena shared by the batch: program p's array of a
+// family starts at element off[p] + 16 of the family's buffers and is followed by at
+// least 80 zero elements, the same pads a single generator gives its arrays, so the
+// stage functions see exactly what they see for that program alone.  Each program has
+// its own Prog view (device memory); kernels cut their work into tiles that never
+// straddle programs.  The host reads sizes between stages (function counts, word counts,
+// steps) once per batch, and a program that fails a check drops out of the later stages
+// without affecting the others.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "ptl_bpipe.h"
+#include "ptl_kernels.cuh"
+
+namespace ptl {
+namespace {
+
+constexpr uint64_t kFront = 16, kBack = 80;
+inline uint64_t r8(uint64_t n) { return (n + 7) & ~uint64_t(7); }
+inline uint64_t region(uint64_t count) { return (count + kFront + kBack + 31) & ~uint64_t(31); }
+
+struct DBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    cudaError_t ensure(size_t need) {
+        if (need <= bytes && p) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+        const size_t grow = need + need / 4 + 4096;
+        const cudaError_t e = cudaMalloc(&p, grow);
+        if (e != cudaSuccess) {
+            p = nullptr;
+            return e;
+        }
+        bytes = grow;
+        return cudaSuccess;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    template <class T>
+    T* at(uint64_t elem = 0) const { return static_cast<T*>(p) + elem; }
+};
+
+struct PBuf {  // pinned host memory
+    void* p = nullptr;
+    size_t bytes = 0;
+    cudaError_t ensure(size_t need) {
+        if (need <= bytes && p) return cudaSuccess;
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        bytes = 0;
+        const size_t grow = need + need / 4 + 4096;
+        const cudaError_t e = cudaHostAlloc(&p, grow, cudaHostAllocDefault);
+        if (e != cudaSuccess) {
+            p = nullptr;
+            return e;
+        }
+        bytes = grow;
+        return cudaSuccess;
+    }
+    void release() {
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    template <class T>
+    T* at(uint64_t elem = 0) const { return static_cast<T*>(p) + elem; }
+};
+
+// Per-program regions of one array family.
+struct Layout {
+    std::vector<uint64_t> off;
+    uint64_t total = 0;
+    void build(const std::vector<uint64_t>& counts, const std::vector<uint8_t>& active) {
+        off.assign(counts.size(), 0);
+        total = 0;
+        for (size_t p = 0; p < counts.size(); ++p) {
+            off[p] = total;
+            if (active[p]) total += region(counts[p]);
+        }
+        total += kFront + kBack;
+    }
+    uint64_t elem(size_t p) const { return off[p] + kFront; }
+};
+
+const CodeTables& tables() {
+    static CodeTables t;
+    static std::once_flag once;
+    std::call_once(once, [] { build_code_tables(&t); });
+    return t;
+}
+
+#define BP_CU(x)                                                     \
+    do {                                                             \
+        const cudaError_t e_ = (x);                                  \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #x);             \
+    } while (0)
+
+class Pipeline final : public BatchPipeline {
+public:
+    int device = 0;
+    int threads = 8;
+    cudaStream_t s = nullptr;
+    cudaEvent_t ev[8] = {};
+    uint64_t ns[7] = {0, 0, 0, 0, 0, 0, 0};
+    uint64_t h2d = 0, d2h = 0;
+    std::string err_text;
+
+    DBuf tab;  // CodeTables
+    DBuf in_type, in_rtype, in_parent, in_depth, in_child, in_data;
+    DBuf nt, rt, nd1, nd, par, ci, dep, sizes, loc0, loc, pos, decl, fflag, regs, seen;
+    DBuf fn_id, fn_start, fn_size, fn_end, fn_start0, fn_size0, lifetime;
+    DBuf instr, rd, rs1, rs2, jt, used_instrs, symreg, symswp, stamp, spill, roffs, owner, used, smark, defpos;
+    DBuf trig_min, trig_max;
+    DBuf ni, nrd, nr1, nr2, njt, fsz, joffs, out;
+    DBuf errw, flags, meta, progs, tabs, lists, changed, sort_err, seen_off, a_off;
+    DBuf sa, sapos, sbpos, seg0, seg1, tile_seg, tile_l, tile_r, leaf, heap, counters, scan_status, scan_counter;
+    PBuf h_in, h_out, h_fn, h_small;
+
+    std::vector<uint8_t> active;
+    std::vector<ptl_status> status;
+
+    ~Pipeline() override {
+        for (DBuf* b : all()) b->release();
+        h_in.release();
+        h_out.release();
+        h_fn.release();
+        h_small.release();
+        for (auto& e : ev)
+            if (e) cudaEventDestroy(e);
+        if (s) cudaStreamDestroy(s);
+    }
+    std::vector<DBuf*> all() {
+        return {&tab, &in_type, &in_rtype, &in_parent, &in_depth, &in_child, &in_data, &nt, &rt, &nd1, &nd, &par,
+                &ci, &dep, &sizes, &loc0, &loc, &pos, &decl, &fflag, &regs, &seen, &fn_id, &fn_start, &fn_size,
+                &fn_end, &fn_start0, &fn_size0, &lifetime, &instr, &rd, &rs1, &rs2, &jt, &used_instrs, &symreg,
+                &symswp, &stamp, &spill, &roffs, &owner, &used, &smark, &defpos, &trig_min, &trig_max, &ni, &nrd,
+                &nr1, &nr2, &njt, &fsz, &joffs, &out, &errw, &flags, &meta, &progs, &tabs, &lists, &changed,
+                &sort_err, &seen_off, &a_off, &sa, &sapos, &sbpos, &seg0, &seg1, &tile_seg, &tile_l, &tile_r,
+                &leaf, &heap, &counters, &scan_status, &scan_counter};
+    }
+
+    ptl_status cuda_fail(cudaError_t e, const char* what) {
+        err_text = std::string(what) + ": " + cudaGetErrorString(e);
+        return e == cudaErrorMemoryAllocation ? PTL_OOM : PTL_CUDA_ERROR;
+    }
+
+    void stage_ns(uint64_t out_ns[7]) const override {
+        for (int k = 0; k < 7; ++k) out_ns[k] = ns[k];
+    }
+    void copied_bytes(uint64_t* a, uint64_t* b) const override {
+        if (a) *a = h2d;
+        if (b) *b = d2h;
+    }
+    const char* last_error() const override { return err_text.c_str(); }
+
+    // Zeroed family of per-program arrays.
+    cudaError_t family(const Layout& L, std::initializer_list<DBuf*> bufs, size_t es) {
+        for (DBuf* b : bufs) {
+            cudaError_t e = b->ensure(L.total * es);
+            if (e == cudaSuccess) e = cudaMemsetAsync(b->p, 0, L.total * es, s);
+            if (e != cudaSuccess) return e;
+        }
+        return cudaSuccess;
+    }
+
+    // Pinned small-area slots: tile tables, lists, host copies of per-program words.
+    size_t B = 0;
+    uint32_t* table_slot(int k) { return h_small.at<uint32_t>(static_cast<uint64_t>(k) * (B + 1)); }
+    uint32_t* dtable_slot(int k) { return tabs.at<uint32_t>(static_cast<uint64_t>(k) * (B + 1)); }
+
+    // Tile table for per-program counts (inactive programs get none); uploads to slot k
+    // and returns the total tile count.
+    uint32_t tiles(int k, const std::vector<uint64_t>& counts, uint64_t tile, const std::vector<uint8_t>* only = nullptr) {
+        uint32_t* h = table_slot(k);
+        uint64_t t = 0;
+        for (size_t p = 0; p < B; ++p) {
+            h[p] = static_cast<uint32_t>(t);
+            const bool on = active[p] && (!only || (*only)[p]);
+            if (on) t += (counts[p] + tile - 1) / tile;
+        }
+        h[B] = static_cast<uint32_t>(t);
+        cudaMemcpyAsync(dtable_slot(k), h, (B + 1) * sizeof(uint32_t), cudaMemcpyHostToDevice, s);
+        return static_cast<uint32_t>(t);
+    }
+    BatchLaunch bl(int k) { return BatchLaunch{progs.at<Prog>(), dtable_slot(k), static_cast<uint32_t>(B), s}; }
+
+    std::vector<Prog> hp;  // host copies of the views
+    Prog* h_progs() { return reinterpret_cast<Prog*>(h_small.at<uint8_t>(small_progs_off)); }
+    size_t small_progs_off = 0, small_meta_off = 0, small_err_off = 0, small_list_off = 0, small_up_off = 0;
+
+    void upload_progs() {
+        std::memcpy(h_progs(), hp.data(), B * sizeof(Prog));
+        cudaMemcpyAsync(progs.p, h_progs(), B * sizeof(Prog), cudaMemcpyHostToDevice, s);
+    }
+
+    // Per-program error words: marks failed programs.  Syncs the stream.
+    cudaError_t collect_errors() {
+        ErrorWord* he = reinterpret_cast<ErrorWord*>(h_small.at<uint8_t>(small_err_off));
+        cudaError_t e = cudaMemcpyAsync(he, errw.p, B * sizeof(ErrorWord), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) return e;
+        for (size_t p = 0; p < B; ++p) {
+            if (active[p] && he[p].code != ST_OK) {
+                active[p] = 0;
+                status[p] = static_cast<ptl_status>(he[p].code);
+            }
+        }
+        return cudaSuccess;
+    }
+    uint32_t* read_meta() {
+        uint32_t* hm = reinterpret_cast<uint32_t*>(h_small.at<uint8_t>(small_meta_off));
+        cudaMemcpyAsync(hm, meta.p, B * 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
+        return hm;
+    }
+    uint32_t* upload_list(int k, const std::vector<uint32_t>& v) {
+        uint32_t* h = reinterpret_cast<uint32_t*>(h_small.at<uint8_t>(small_list_off)) + static_cast<uint64_t>(k) * (B + 1);
+        std::copy(v.begin(), v.end(), h);
+        uint32_t* d = lists.at<uint32_t>(static_cast<uint64_t>(k) * (B + 1));
+        if (!v.empty()) cudaMemcpyAsync(d, h, v.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, s);
+        return d;
+    }
+
+    ptl_status compile(const ptl_ast_view* trees, size_t count, std::vector<BatchResult>& res) override;
+};
+
+ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vector<BatchResult>& res) {
+    res.assign(count, BatchResult{});
+    err_text.clear();
+    h2d = d2h = 0;
+    for (auto& x : ns) x = 0;
+    if (count == 0) return PTL_OK;
+    if (!trees) return PTL_BAD_ARGUMENT;
+    if (count > (1u << 24)) return PTL_BAD_ARGUMENT;
+    BP_CU(cudaSetDevice(device));
+    B = count;
+    active.assign(B, 1);
+    status.assign(B, PTL_OK);
+    std::vector<uint64_t> n(B), nb8(B), n3(B), md1(B);
+    uint64_t ntot = 0;
+    for (size_t p = 0; p < B; ++p) {
+        const ptl_ast_view& t = trees[p];
+        const bool ok = t.n > 0 && t.n < (1ull << 31) && t.type && t.rtype && t.parent && t.depth && t.child_idx &&
+                        t.data && !t.on_device;
+        if (!ok || t.max_depth == 0 || t.max_depth >= t.n) {
+            active[p] = 0;
+            status[p] = ok ? PTL_INVALID_AST : PTL_BAD_ARGUMENT;
+            continue;
+        }
+        n[p] = t.n;
+        nb8[p] = r8(t.n);
+        n3[p] = 3 * t.n;
+        md1[p] = t.max_depth + 1;
+        ntot += t.n;
+    }
+    for (auto& e : ev)
+        if (!e) BP_CU(cudaEventCreate(&e));
+    BP_CU(cudaEventRecord(ev[0], s));
+
+    // ---- small per-program state and the pinned small area
+    constexpr int kTables = 20, kLists = 4;
+    small_progs_off = static_cast<size_t>(kTables) * (B + 1) * 4;
+    small_meta_off = small_progs_off + B * sizeof(Prog);
+    small_err_off = small_meta_off + B * 16;
+    small_list_off = small_err_off + B * sizeof(ErrorWord);
+    small_up_off = small_list_off + static_cast<size_t>(kLists) * (B + 1) * 4;  // 8-byte aligned
+    small_up_off = (small_up_off + 15) & ~size_t(15);
+    BP_CU(h_small.ensure(small_up_off + B * (8 + 8 + sizeof(SortSeg) + 8) + 64));
+    BP_CU(tabs.ensure(static_cast<size_t>(kTables) * (B + 1) * 4));
+    BP_CU(lists.ensure(static_cast<size_t>(kLists) * (B + 1) * 4));
+    BP_CU(progs.ensure(B * sizeof(Prog)));
+    BP_CU(errw.ensure(B * sizeof(ErrorWord)));
+    BP_CU(flags.ensure(B * 16));
+    BP_CU(meta.ensure(B * 16));
+    BP_CU(changed.ensure(16));
+    BP_CU(sort_err.ensure(sizeof(ErrorWord)));
+    BP_CU(cudaMemsetAsync(errw.p, 0, B * sizeof(ErrorWord), s));
+    BP_CU(cudaMemsetAsync(flags.p, 0, B * 16, s));
+    BP_CU(cudaMemsetAsync(meta.p, 0, B * 16, s));
+    BP_CU(cudaMemsetAsync(sort_err.p, 0, sizeof(ErrorWord), s));
+    if (!tab.p) {
+        BP_CU(tab.ensure(sizeof(CodeTables)));
+        BP_CU(cudaMemcpyAsync(tab.p, &tables(), sizeof(CodeTables), cudaMemcpyHostToDevice, s));
+        BP_CU(cudaStreamSynchronize(s));
+    }
+
+    // ---- inputs: gathered into pinned memory by host threads, one copy per field
+    {
+        std::vector<uint64_t> din(B);
+        uint64_t o = 0;
+        for (size_t p = 0; p < B; ++p) {
+            din[p] = o;
+            if (active[p]) o += n[p];
+        }
+        const uint64_t cap = std::max<uint64_t>(o, 1);
+        const size_t bytes = cap * (1 + 1 + 4 + 4 + 4 + 4);
+        BP_CU(h_in.ensure(bytes));
+        uint8_t* ht = h_in.at<uint8_t>();
+        uint8_t* hr = ht + cap;
+        int32_t* hpar = reinterpret_cast<int32_t*>(hr + cap);
+        int32_t* hdep = hpar + cap;
+        int32_t* hch = hdep + cap;
+        uint32_t* hdat = reinterpret_cast<uint32_t*>(hch + cap);
+        const int nt_ = std::max(1, std::min<int>(threads, static_cast<int>(B)));
+        std::vector<std::thread> pool;
+        for (int w = 0; w < nt_; ++w) {
+            pool.emplace_back([&, w] {
+                for (size_t p = static_cast<size_t>(w); p < B; p += static_cast<size_t>(nt_)) {
+                    if (!active[p]) continue;
+                    const ptl_ast_view& t = trees[p];
+                    const uint64_t d = din[p];
+                    std::memcpy(ht + d, t.type, n[p]);
+                    std::memcpy(hr + d, t.rtype, n[p]);
+                    std::memcpy(hpar + d, t.parent, 4 * n[p]);
+                    std::memcpy(hdep + d, t.depth, 4 * n[p]);
+                    std::memcpy(hch + d, t.child_idx, 4 * n[p]);
+                    std::memcpy(hdat + d, t.data, 4 * n[p]);
+                }
+            });
+        }
+        for (auto& t : pool) t.join();
+        BP_CU(in_type.ensure(cap));
+        BP_CU(in_rtype.ensure(cap));
+        BP_CU(in_parent.ensure(cap * 4));
+        BP_CU(in_depth.ensure(cap * 4));
+        BP_CU(in_child.ensure(cap * 4));
+        BP_CU(in_data.ensure(cap * 4));
+        BP_CU(cudaMemcpyAsync(in_type.p, ht, o, cudaMemcpyHostToDevice, s));
+        BP_CU(cudaMemcpyAsync(in_rtype.p, hr, o, cudaMemcpyHostToDevice, s));
+        BP_CU(cudaMemcpyAsync(in_parent.p, hpar, 4 * o, cudaMemcpyHostToDevice, s));
+        BP_CU(cudaMemcpyAsync(in_depth.p, hdep, 4 * o, cudaMemcpyHostToDevice, s));
+        BP_CU(cudaMemcpyAsync(in_child.p, hch, 4 * o, cudaMemcpyHostToDevice, s));
+        BP_CU(cudaMemcpyAsync(in_data.p, hdat, 4 * o, cudaMemcpyHostToDevice, s));
+        h2d += 18 * o;
+
+        // node, register and depth families
+        Layout Ln, Lr, Ls;
+        Ln.build(nb8, active);
+        Lr.build(n3, active);
+        Ls.build(md1, active);
+        BP_CU(family(Ln, {&nt, &rt, &nd1, &nd, &par, &ci, &dep, &sizes, &loc0, &loc, &pos, &decl}, 4));
+        BP_CU(family(Ln, {&fflag}, 1));
+        BP_CU(family(Lr, {&regs}, 4));
+        BP_CU(family(Ls, {&seen}, 4));
+        hp.assign(B, Prog{});
+        for (size_t p = 0; p < B; ++p) {
+            Prog& P = hp[p];
+            P.n = static_cast<uint32_t>(n[p]);
+            P.nb8 = static_cast<uint32_t>(nb8[p]);
+            P.max_depth = static_cast<uint32_t>(trees[p].max_depth);
+            P.in_type = in_type.at<uint8_t>(din[p]);
+            P.in_rtype = in_rtype.at<uint8_t>(din[p]);
+            P.in_parent = in_parent.at<int32_t>(din[p]);
+            P.in_depth = in_depth.at<int32_t>(din[p]);
+            P.in_child = in_child.at<int32_t>(din[p]);
+            P.in_data = in_data.at<uint32_t>(din[p]);
+            const uint64_t e = Ln.elem(p);
+            P.nt = nt.at<uint32_t>(e);
+            P.rt = rt.at<uint32_t>(e);
+            P.nd1 = nd1.at<uint32_t>(e);
+            P.nd = nd.at<uint32_t>(e);
+            P.par = par.at<int32_t>(e);
+            P.ci = ci.at<int32_t>(e);
+            P.dep = dep.at<int32_t>(e);
+            P.sizes = sizes.at<uint32_t>(e);
+            P.loc0 = loc0.at<uint32_t>(e);
+            P.loc = loc.at<uint32_t>(e);
+            P.pos = pos.at<uint32_t>(e);
+            P.decl = decl.at<uint32_t>(e);
+            P.fflag = fflag.at<uint8_t>(e);
+            P.regs = regs.at<uint32_t>(Lr.elem(p));
+            P.tab.t = tab.at<CodeTables>();
+            P.err = errw.at<ErrorWord>(p);
+            P.flags = flags.at<uint32_t>(4 * p);
+        }
+        upload_progs();
+
+        // ---- input checks
+        std::vector<uint64_t> soff(B);
+        for (size_t p = 0; p < B; ++p) soff[p] = Ls.elem(p);
+        BP_CU(seen_off.ensure(B * 8));
+        uint64_t* up_soff = reinterpret_cast<uint64_t*>(h_small.at<uint8_t>(small_up_off));
+        std::copy(soff.begin(), soff.end(), up_soff);
+        BP_CU(cudaMemcpyAsync(seen_off.p, up_soff, B * 8, cudaMemcpyHostToDevice, s));
+        const uint32_t t_n = tiles(0, n, batch_tile());
+        batch_stage(BatchStage::Validate, bl(0), t_n, nullptr, nullptr, nullptr);
+        batch_stage(BatchStage::DepthSeen, bl(0), t_n, nullptr, seen.at<uint32_t>(), seen_off.at<uint64_t>());
+        BP_CU(collect_errors());
+        {
+            std::vector<uint32_t> hs(Ls.total);
+            BP_CU(cudaMemcpyAsync(hs.data(), seen.p, Ls.total * 4, cudaMemcpyDeviceToHost, s));
+            BP_CU(cudaStreamSynchronize(s));
+            for (size_t p = 0; p < B; ++p) {
+                if (!active[p]) continue;
+                for (uint64_t d = 0; d < md1[p]; ++d) {
+                    if (!hs[soff[p] + d]) {  // depths 0..max_depth must all be populated
+                        active[p] = 0;
+                        status[p] = PTL_INVALID_AST;
+                        break;
+                    }
+                }
+            }
+        }
+
+        // ---- preprocess
+        const uint32_t t_nb8 = tiles(1, nb8, batch_tile());
+        batch_stage(BatchStage::Translate, bl(1), t_nb8, nullptr, nullptr, nullptr);
+        batch_stage(BatchStage::Preprocess, bl(1), t_nb8, nullptr, nullptr, nullptr);
+        BP_CU(cudaEventRecord(ev[1], s));
+
+        // ---- isn_cnt
+        const uint32_t st_nb8 = tiles(2, nb8, batch_scan_tile());
+        BP_CU(scan_status.ensure((static_cast<size_t>(st_nb8) + 8) * 8));
+        BP_CU(scan_counter.ensure(16));
+        ScanScratch sc{scan_status.at<unsigned long long>(), scan_counter.at<uint32_t>(), st_nb8 + 8};
+        batch_scan(BatchScan::Count, bl(2), st_nb8, sc, nullptr);
+        batch_stage(BatchStage::Fix, bl(1), t_nb8, nullptr, nullptr, nullptr);
+        batch_scan(BatchScan::Decl, bl(2), st_nb8, sc, meta.at<uint32_t>());
+        uint32_t* hm = read_meta();
+        BP_CU(collect_errors());
+        std::vector<uint64_t> F(B), fb8(B), fr(B);
+        for (size_t p = 0; p < B; ++p) {
+            if (!active[p]) continue;
+            F[p] = hm[4 * p];
+            if (F[p] == 0) {  // the reference takes the max of an empty range
+                active[p] = 0;
+                status[p] = PTL_UNSUPPORTED;
+                continue;
+            }
+            fb8[p] = r8(F[p]);
+            fr[p] = fb8[p] + 8;
+        }
+        Layout Lf;
+        Lf.build(fr, active);
+        BP_CU(family(Lf, {&fn_id, &fn_start, &fn_size, &fn_end, &fn_start0, &fn_size0}, 4));
+        BP_CU(family(Lf, {&lifetime}, 8));
+        for (size_t p = 0; p < B; ++p) {
+            Prog& P = hp[p];
+            P.F = static_cast<uint32_t>(F[p]);
+            P.fb8 = static_cast<uint32_t>(fb8[p]);
+            const uint64_t e = Lf.elem(p);
+            P.fn_id = fn_id.at<uint32_t>(e);
+            P.fn_start = fn_start.at<uint32_t>(e);
+            P.fn_size = fn_size.at<uint32_t>(e);
+            P.fn_end = fn_end.at<uint32_t>(e);
+            P.fn_start0 = fn_start0.at<uint32_t>(e);
+            P.fn_size0 = fn_size0.at<uint32_t>(e);
+            P.lifetime = lifetime.at<unsigned long long>(e);
+        }
+        upload_progs();
+        const uint32_t t_fb8 = tiles(3, fb8, batch_tile());
+        batch_stage(BatchStage::Functab, bl(3), t_fb8, meta.at<uint32_t>(), nullptr, nullptr);
+        hm = read_meta();
+        BP_CU(collect_errors());
+        std::vector<uint64_t> W(B), wb8(B), S(B), trig(B);
+        uint32_t min_lg = 31, max_lg = 1;
+        for (size_t p = 0; p < B; ++p) {
+            if (!active[p]) continue;
+            W[p] = hm[4 * p + 1];
+            S[p] = hm[4 * p + 2];
+            wb8[p] = r8(W[p]);
+            trig[p] = std::max<uint64_t>(S[p], 1) * 64;
+            if (W[p] == 0) {
+                active[p] = 0;
+                status[p] = PTL_UNSUPPORTED;
+            }
+        }
+        BP_CU(cudaEventRecord(ev[2], s));
+
+        // ---- isn_gen: depth order of every program in one introsort run, then the writes
+        Layout Lw;
+        Lw.build(wb8, active);
+        BP_CU(family(Lw, {&instr, &rd, &rs1, &rs2, &jt, &used_instrs, &symreg, &symswp, &stamp, &spill, &roffs}, 4));
+        BP_CU(family(Lw, {&owner}, 8));
+        BP_CU(family(Lw, {&used, &smark, &defpos}, 1));
+        for (size_t p = 0; p < B; ++p) {
+            Prog& P = hp[p];
+            P.W = static_cast<uint32_t>(W[p]);
+            P.wb8 = static_cast<uint32_t>(wb8[p]);
+            P.S = static_cast<uint32_t>(S[p]);
+            const uint64_t e = Lw.elem(p);
+            P.instr = instr.at<uint32_t>(e);
+            P.rd = rd.at<uint32_t>(e);
+            P.rs1 = rs1.at<uint32_t>(e);
+            P.rs2 = rs2.at<uint32_t>(e);
+            P.jt = jt.at<uint32_t>(e);
+            P.used_instrs = used_instrs.at<uint32_t>(e);
+            P.symreg = symreg.at<uint32_t>(e);
+            P.symswp = symswp.at<uint32_t>(e);
+            P.stamp = stamp.at<uint32_t>(e);
+            P.spill = spill.at<uint32_t>(e);
+            P.roffs = roffs.at<uint32_t>(e);
+            P.owner = owner.at<unsigned long long>(e);
+            P.used = used.at<uint8_t>(e);
+            P.smark = smark.at<uint8_t>(e);
+            P.defpos = defpos.at<uint8_t>(e);
+        }
+        upload_progs();
+        // sort scratch over all active programs' nodes
+        std::vector<uint64_t> aoff(B);
+        uint64_t at = 0, seg_cap = 16, tile_cap = 16, leaf_cap = 16;
+        std::vector<SortSeg> segs;
+        std::vector<uint32_t> leaves;
+        for (size_t p = 0; p < B; ++p) {
+            aoff[p] = at;
+            if (!active[p]) continue;
+            const uint64_t np = n[p];
+            seg_cap += np / 17 + 16;
+            tile_cap += np / 2048 + np / 17 + 16;
+            leaf_cap += np / 2 + 16;
+            if (np > 16) {
+                SortSeg g{};
+                g.first = static_cast<uint32_t>(at);
+                g.last = static_cast<uint32_t>(at + np);
+                g.dl = 2u * floor_log2(static_cast<uint32_t>(np));
+                segs.push_back(g);
+                const uint32_t lg = floor_log2(static_cast<uint32_t>(np));
+                min_lg = std::min(min_lg, lg);
+                max_lg = std::max(max_lg, lg);
+            } else if (np > 1) {
+                leaves.push_back(static_cast<uint32_t>(at));
+                leaves.push_back(static_cast<uint32_t>(at + np));
+            }
+            at += np;
+        }
+        if (at >= (1ull << 32)) return cuda_fail(cudaErrorInvalidValue, "batch larger than 2^32 nodes");
+        BP_CU(sa.ensure(std::max<uint64_t>(at, 1) * 8));
+        BP_CU(sapos.ensure(std::max<uint64_t>(at, 1) * 4));
+        BP_CU(sbpos.ensure(std::max<uint64_t>(at, 1) * 4));
+        BP_CU(seg0.ensure(seg_cap * sizeof(SortSeg)));
+        BP_CU(seg1.ensure(seg_cap * sizeof(SortSeg)));
+        BP_CU(tile_seg.ensure(tile_cap * 4));
+        BP_CU(tile_l.ensure(tile_cap * 4));
+        BP_CU(tile_r.ensure(tile_cap * 4));
+        BP_CU(leaf.ensure(2 * leaf_cap * 4));
+        BP_CU(heap.ensure(2 * leaf_cap * 4));
+        BP_CU(counters.ensure(64));
+        BP_CU(a_off.ensure(B * 8));
+        uint64_t* up_aoff = reinterpret_cast<uint64_t*>(h_small.at<uint8_t>(small_up_off + B * 8));
+        std::copy(aoff.begin(), aoff.end(), up_aoff);
+        BP_CU(cudaMemcpyAsync(a_off.p, up_aoff, B * 8, cudaMemcpyHostToDevice, s));
+        SortScratch ss{};
+        ss.a = sa.at<unsigned long long>();
+        ss.apos = sapos.at<uint32_t>();
+        ss.bpos = sbpos.at<uint32_t>();
+        ss.seg[0] = seg0.at<SortSeg>();
+        ss.seg[1] = seg1.at<SortSeg>();
+        ss.seg_cap = static_cast<uint32_t>(seg_cap);
+        ss.tile_seg = tile_seg.at<uint32_t>();
+        ss.tile_l = tile_l.at<uint32_t>();
+        ss.tile_r = tile_r.at<uint32_t>();
+        ss.tile_cap = static_cast<uint32_t>(tile_cap);
+        ss.leaf = leaf.at<uint32_t>();
+        ss.heap = heap.at<uint32_t>();
+        ss.leaf_cap = static_cast<uint32_t>(leaf_cap);
+        ss.counters = counters.at<uint32_t>();
+        const uint32_t t_n2 = tiles(4, n, batch_tile());
+        batch_sort_keys(bl(4), t_n2, sa.at<unsigned long long>(), a_off.at<uint64_t>(), false);
+        BP_CU(cudaMemsetAsync(counters.p, 0, 64, s));
+        SortSeg* up_segs = reinterpret_cast<SortSeg*>(h_small.at<uint8_t>(small_up_off + 2 * B * 8));
+        uint32_t* up_leaves = reinterpret_cast<uint32_t*>(h_small.at<uint8_t>(small_up_off + 2 * B * 8 + B * sizeof(SortSeg)));
+        uint32_t* up_nl = up_leaves + 2 * B;
+        if (!segs.empty()) {
+            std::copy(segs.begin(), segs.end(), up_segs);
+            BP_CU(cudaMemcpyAsync(seg0.p, up_segs, segs.size() * sizeof(SortSeg), cudaMemcpyHostToDevice, s));
+        }
+        if (!leaves.empty()) {
+            std::copy(leaves.begin(), leaves.end(), up_leaves);
+            *up_nl = static_cast<uint32_t>(leaves.size() / 2);
+            BP_CU(cudaMemcpyAsync(leaf.p, up_leaves, leaves.size() * 4, cudaMemcpyHostToDevice, s));
+            BP_CU(cudaMemcpyAsync(counters.at<uint32_t>(2), up_nl, 4, cudaMemcpyHostToDevice, s));
+        }
+        uint32_t rounds = 0;
+        BP_CU(run_sort_rounds(ss, static_cast<uint32_t>(segs.size()), min_lg > 4 ? min_lg - 4 : 1, 2 * max_lg + 4,
+                              sort_err.at<ErrorWord>(), s, &rounds));
+        batch_sort_keys(bl(4), t_n2, sa.at<unsigned long long>(), a_off.at<uint64_t>(), true);
+        batch_stage(BatchStage::Gen, bl(4), t_n2, nullptr, nullptr, nullptr);
+        {
+            ErrorWord se{};
+            BP_CU(cudaMemcpyAsync(&se, sort_err.p, sizeof(se), cudaMemcpyDeviceToHost, s));
+            BP_CU(collect_errors());
+            if (se.code != ST_OK) return cuda_fail(cudaErrorLaunchFailure, "depth order");
+        }
+        BP_CU(cudaEventRecord(ev[3], s));
+
+        // ---- optimize
+        const uint32_t t_wb8 = tiles(5, wb8, batch_tile());
+        batch_stage(BatchStage::OptMark, bl(5), t_wb8, nullptr, nullptr, nullptr);
+        uint32_t* hflag = reinterpret_cast<uint32_t*>(h_small.at<uint8_t>(small_meta_off));  // B*16 >= 4
+        for (uint32_t sweeps = 0;;) {
+            BP_CU(cudaMemsetAsync(changed.p, 0, 4, s));
+            for (int k = 0; k < 4; ++k) batch_sweep(bl(5), t_wb8, changed.at<uint32_t>());
+            sweeps += 4;
+            BP_CU(cudaMemcpyAsync(hflag, changed.p, 4, cudaMemcpyDeviceToHost, s));
+            BP_CU(cudaStreamSynchronize(s));
+            if (!*hflag) break;
+            if (sweeps > 64u + 4u * static_cast<uint32_t>(*std::max_element(W.begin(), W.end()))) break;
+        }
+        batch_stage(BatchStage::OptFinal, bl(5), t_wb8, nullptr, nullptr, nullptr);
+        BP_CU(collect_errors());
+        BP_CU(cudaEventRecord(ev[4], s));
+
+        // ---- regalloc
+        const uint32_t t_f = tiles(6, F, batch_tile());
+        batch_stage(BatchStage::InitLifetime, bl(6), t_f, nullptr, nullptr, nullptr);
+        Layout Lt;
+        Lt.build(trig, active);
+        BP_CU(trig_min.ensure(Lt.total * 4));
+        BP_CU(trig_max.ensure(Lt.total * 4));
+        BP_CU(cudaMemsetAsync(trig_min.p, 0xFF, Lt.total * 4, s));
+        BP_CU(cudaMemsetAsync(trig_max.p, 0, Lt.total * 4, s));
+        for (size_t p = 0; p < B; ++p) {
+            hp[p].trig_min = trig_min.at<uint32_t>(Lt.elem(p));
+            hp[p].trig_max = trig_max.at<uint32_t>(Lt.elem(p));
+        }
+        upload_progs();
+        const uint32_t t_w = tiles(7, W, batch_tile());
+        batch_stage(BatchStage::Cross, bl(7), t_w, nullptr, nullptr, nullptr);
+        uint32_t* hfl = reinterpret_cast<uint32_t*>(h_small.at<uint8_t>(small_meta_off));
+        BP_CU(cudaMemcpyAsync(hfl, flags.p, B * 16, cudaMemcpyDeviceToHost, s));
+        BP_CU(collect_errors());
+        std::vector<uint32_t> lane0_list, serial_list, active_list;
+        std::vector<uint8_t> lane0(B, 0);
+        std::vector<uint64_t> nfree(B, 0);
+        uint32_t max_g0 = 1;
+        for (size_t p = 0; p < B; ++p) {
+            if (!active[p]) continue;
+            active_list.push_back(static_cast<uint32_t>(p));
+            const uint64_t g0 = (F[p] + 7) / 8;
+            if (hfl[4 * p + 1] || g0 > 8192) {  // functions share symbols: the serial order
+                serial_list.push_back(static_cast<uint32_t>(p));
+                continue;
+            }
+            if (hfl[4 * p + 2]) hp[p].defpos = nullptr;  // a register with two definitions: hash row 0
+            lane0[p] = 1;
+            lane0_list.push_back(static_cast<uint32_t>(p));
+            nfree[p] = F[p] - g0;
+            max_g0 = std::max<uint32_t>(max_g0, static_cast<uint32_t>(g0));
+        }
+        upload_progs();
+        const uint32_t t_free = tiles(8, nfree, batch_free_tile(), &lane0);
+        batch_free_functions(bl(8), t_free);
+        const uint32_t* d_lane0 = upload_list(0, lane0_list);
+        BP_CU(batch_lane0(progs.at<Prog>(), d_lane0, static_cast<uint32_t>(lane0_list.size()), max_g0, s));
+        const uint32_t* d_serial = upload_list(1, serial_list);
+        batch_serial(progs.at<Prog>(), d_serial, static_cast<uint32_t>(serial_list.size()), s);
+        const uint32_t t_w_sp = tiles(13, W, batch_tile());
+        batch_stage(BatchStage::Spill, bl(13), t_w_sp, nullptr, nullptr, nullptr);
+        const uint32_t st_wb8 = tiles(9, wb8, batch_scan_tile());
+        BP_CU(scan_status.ensure((static_cast<size_t>(st_wb8) + 8) * 8));
+        sc = ScanScratch{scan_status.at<unsigned long long>(), scan_counter.at<uint32_t>(), st_wb8 + 8};
+        batch_scan(BatchScan::RaCount, bl(9), st_wb8, sc, nullptr);
+        const uint32_t* d_active = upload_list(2, active_list);
+        batch_sizes(false, progs.at<Prog>(), d_active, static_cast<uint32_t>(active_list.size()), meta.at<uint32_t>(), s);
+        hm = read_meta();
+        BP_CU(collect_errors());
+        std::vector<uint64_t> W2(B), w2b8(B), w2r(B);
+        for (size_t p = 0; p < B; ++p) {
+            if (!active[p]) continue;
+            W2[p] = hm[4 * p];
+            w2b8[p] = r8(W2[p]);
+            w2r[p] = w2b8[p] + 16;
+        }
+        Layout L2;
+        L2.build(w2r, active);
+        BP_CU(family(L2, {&ni, &nrd, &nr1, &nr2, &njt, &fsz, &joffs}, 4));
+        for (size_t p = 0; p < B; ++p) {
+            Prog& P = hp[p];
+            P.W2 = static_cast<uint32_t>(W2[p]);
+            P.w2b8 = static_cast<uint32_t>(w2b8[p]);
+            const uint64_t e = L2.elem(p);
+            P.ni = ni.at<uint32_t>(e);
+            P.nrd = nrd.at<uint32_t>(e);
+            P.nr1 = nr1.at<uint32_t>(e);
+            P.nr2 = nr2.at<uint32_t>(e);
+            P.njt = njt.at<uint32_t>(e);
+            P.fsz = fsz.at<uint32_t>(e);
+            P.joffs = joffs.at<uint32_t>(e);
+        }
+        upload_progs();
+        const uint32_t t_wb8_sc = tiles(14, wb8, batch_tile());
+        batch_stage(BatchStage::Scatter, bl(14), t_wb8_sc, nullptr, nullptr, nullptr);
+        const uint32_t t_f2 = tiles(10, F, batch_tile());
+        batch_stage(BatchStage::RaFunctab, bl(10), t_f2, nullptr, nullptr, nullptr);
+        BP_CU(cudaEventRecord(ev[5], s));
+
+        // ---- fix_jumps (+ postprocess)
+        const uint32_t st_w2 = tiles(11, w2b8, batch_scan_tile());
+        BP_CU(scan_status.ensure((static_cast<size_t>(st_w2) + 8) * 8));
+        sc = ScanScratch{scan_status.at<unsigned long long>(), scan_counter.at<uint32_t>(), st_w2 + 8};
+        batch_scan(BatchScan::FjSize, bl(11), st_w2, sc, nullptr);
+        std::vector<uint32_t> active_now;  // programs still running after regalloc
+        for (size_t p = 0; p < B; ++p)
+            if (active[p]) active_now.push_back(static_cast<uint32_t>(p));
+        const uint32_t* d_active2 = upload_list(3, active_now);
+        batch_sizes(true, progs.at<Prog>(), d_active2, static_cast<uint32_t>(active_now.size()), meta.at<uint32_t>(), s);
+        hm = read_meta();
+        BP_CU(collect_errors());
+        std::vector<uint64_t> W3(B), w3r(B);
+        for (size_t p = 0; p < B; ++p) {
+            if (!active[p]) continue;
+            W3[p] = hm[4 * p + 1];
+            w3r[p] = r8(W3[p]) + 8;
+        }
+        Layout Lo;
+        Lo.build(w3r, active);
+        BP_CU(family(Lo, {&out}, 4));
+        for (size_t p = 0; p < B; ++p) {
+            hp[p].W3 = static_cast<uint32_t>(W3[p]);
+            hp[p].out = out.at<uint32_t>(Lo.elem(p));
+        }
+        upload_progs();
+        const uint32_t t_w2 = tiles(12, W2, batch_tile());
+        batch_stage(BatchStage::FjEmit, bl(12), t_w2, nullptr, nullptr, nullptr);
+        const uint32_t t_f3 = tiles(15, F, batch_tile());
+        batch_stage(BatchStage::FjFunctab, bl(15), t_f3, nullptr, nullptr, nullptr);
+        BP_CU(cudaEventRecord(ev[6], s));
+        BP_CU(cudaEventRecord(ev[7], s));
+
+        // ---- results: the output words and function tables of every program, one copy each
+        BP_CU(h_out.ensure(Lo.total * 4));
+        BP_CU(h_fn.ensure(Lf.total * 4 * 4));
+        BP_CU(cudaMemcpyAsync(h_out.p, out.p, Lo.total * 4, cudaMemcpyDeviceToHost, s));
+        uint32_t* hf = h_fn.at<uint32_t>();
+        BP_CU(cudaMemcpyAsync(hf, fn_start.p, Lf.total * 4, cudaMemcpyDeviceToHost, s));
+        BP_CU(cudaMemcpyAsync(hf + Lf.total, fn_end.p, Lf.total * 4, cudaMemcpyDeviceToHost, s));
+        BP_CU(cudaMemcpyAsync(hf + 2 * Lf.total, fn_size.p, Lf.total * 4, cudaMemcpyDeviceToHost, s));
+        BP_CU(cudaMemcpyAsync(hf + 3 * Lf.total, fn_id.p, Lf.total * 4, cudaMemcpyDeviceToHost, s));
+        d2h += Lo.total * 4 + 4 * Lf.total * 4;
+        BP_CU(collect_errors());
+        for (size_t p = 0; p < B; ++p) {
+            BatchResult& r = res[p];
+            r.status = status[p];
+            if (!active[p]) continue;
+            r.words = h_out.at<uint32_t>(Lo.elem(p));
+            r.count = W3[p];
+            const uint64_t e = Lf.elem(p);
+            r.starts = hf + e;
+            r.ends = hf + Lf.total + e;
+            r.sizes = hf + 2 * Lf.total + e;
+            r.ids = hf + 3 * Lf.total + e;
+            r.functions = F[p];
+        }
+        float ms = 0;
+        for (int k = 0; k < 6; ++k) {
+            if (cudaEventElapsedTime(&ms, ev[k], ev[k + 1]) == cudaSuccess) ns[k] = static_cast<uint64_t>(ms * 1e6);
+        }
+        ns[6] = 0;  // postprocess is fused into fix_jumps
+    }
+    return PTL_OK;
+}
+
+}  // namespace
+
+BatchPipeline* BatchPipeline::create(int device, int host_threads, ptl_status* st) {
+    Pipeline* p = new (std::nothrow) Pipeline;
+    if (!p) {
+        if (st) *st = PTL_OOM;
+        return nullptr;
+    }
+    p->device = device;
+    p->threads = std::max(1, host_threads);
+    if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&p->s, cudaStreamNonBlocking) != cudaSuccess) {
+        delete p;
+        if (st) *st = PTL_CUDA_ERROR;
+        return nullptr;
+    }
+    if (st) *st = PTL_OK;
+    return p;
+}
+
+}  // namespace ptl

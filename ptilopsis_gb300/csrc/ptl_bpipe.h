@@ -1,0 +1,39 @@
+// Batched pipeline: many programs through the seven stages with one launch per stage
+// step (ptl_bpipe.cu).  Host-only interface (no CUDA types), used by ptl_batch.cpp.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <vector>
+
+#include "../../include/ptl_codegen.h"
+
+namespace ptl {
+
+// One program's output: pointers into the pipeline's host buffers, valid until its next
+// compile.
+struct BatchResult {
+    ptl_status status = PTL_OK;
+    const uint32_t* words = nullptr;
+    size_t count = 0;
+    const uint32_t *starts = nullptr, *ends = nullptr, *sizes = nullptr, *ids = nullptr;
+    size_t functions = 0;
+};
+
+class BatchPipeline {
+public:
+    // Device and pinned host memory are kept between calls and grow to the largest batch.
+    static BatchPipeline* create(int device, int host_threads, ptl_status* st);
+    virtual ~BatchPipeline() = default;
+    // Compiles count host trees; out[k] receives program k's output or its status.
+    // Returns PTL_OK unless the batch as a whole failed (CUDA error, out of memory).
+    virtual ptl_status compile(const ptl_ast_view* trees, size_t count, std::vector<BatchResult>& out) = 0;
+    // Device time of the last compile per stage (the reference's seven CSV columns), ns.
+    virtual void stage_ns(uint64_t ns[7]) const = 0;
+    // Host-to-device and device-to-host bytes of the last compile.
+    virtual void copied_bytes(uint64_t* h2d, uint64_t* d2h) const = 0;
+    // Detail of the last failure.
+    virtual const char* last_error() const = 0;
+};
+
+}  // namespace ptl

@@ -89,10 +89,12 @@ __global__ void k_init_lifetime(unsigned long long* lt, uint32_t F) {
         lt[k] = 0x1Full;
 }
 
-__global__ void k_depth_seen(const int32_t* depth, uint32_t n, uint32_t* seen) {
+__global__ void k_depth_seen(const int32_t* depth, uint32_t n, uint32_t max_depth, uint32_t* seen) {
     for (uint64_t k = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x; k < n;
-         k += static_cast<uint64_t>(gridDim.x) * blockDim.x)
-        seen[depth[k]] = 1;
+         k += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+        const int32_t d = depth[k];
+        if (d >= 0 && static_cast<uint32_t>(d) <= max_depth) seen[d] = 1;  // others fail validation
+    }
 }
 
 }  // namespace ptl
@@ -337,7 +339,7 @@ ptl_status run_pipeline(ptl_generator* g, bool profile, bool to_host, bool row0_
     k_validate<<<std::min<size_t>((n + 255) / 256, 152 * 16), 256, 0, s>>>(
         P.in_type, P.in_rtype, P.in_parent, P.in_depth, P.in_child, P.n, P.max_depth, P.err);
     note_launch();
-    k_depth_seen<<<std::min<size_t>((n + 255) / 256, 152 * 16), 256, 0, s>>>(P.in_depth, P.n,
+    k_depth_seen<<<std::min<size_t>((n + 255) / 256, 152 * 16), 256, 0, s>>>(P.in_depth, P.n, P.max_depth,
                                                                              g->depth_seen.at<uint32_t>());
     if (ptl_status st = check_error_word(g); st != PTL_OK) return st;
     {
@@ -395,7 +397,7 @@ ptl_status run_pipeline(ptl_generator* g, bool profile, bool to_host, bool row0_
     PTL_CU(g->sort_tile_r.ensure(tile_cap, 4));
     PTL_CU(g->sort_leaf.ensure(2 * leaf_cap, 4));
     PTL_CU(g->sort_heap.ensure(2 * leaf_cap, 4));
-    PTL_CU(g->sort_counters.ensure(4, 4));
+    PTL_CU(g->sort_counters.ensure(8, 4));
     SortScratch ss{};
     ss.a = g->sort_a.at<unsigned long long>();
     ss.apos = g->sort_apos.at<uint32_t>();

@@ -200,7 +200,27 @@ __global__ void k_sort_init(Prog P, SortScratch ss) {
     PTL_FOR(i, P.n) ss.a[i] = (static_cast<unsigned long long>(u32(P.dep[i])) << 32) | i;
 }
 
-__global__ void k_sort_tiles(SortScratch ss, const SortSeg* cur, SortSeg* curw, uint32_t nseg) {
+// The round kernels read this round's segment and tile counts on the device, so that
+// rounds run back to back without the host.  A capacity overflow (impossible by the
+// bounds the host sizes with, but checked) raises counters[5] and idles later kernels.
+__device__ __forceinline__ bool sort_overflow(const SortScratch& ss) {
+    return *reinterpret_cast<const volatile uint32_t*>(&ss.counters[5]) != 0;
+}
+__device__ __forceinline__ uint32_t sort_nseg(const SortScratch& ss) { return min(ss.counters[4], ss.seg_cap); }
+__device__ __forceinline__ uint32_t sort_ntiles(const SortScratch& ss) { return min(ss.counters[0], ss.tile_cap); }
+
+// Round start: the segments emitted by the previous round become this round's.
+__global__ void k_sort_round(SortScratch ss) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        ss.counters[4] = ss.counters[1];
+        ss.counters[1] = 0;
+        ss.counters[0] = 0;
+    }
+}
+
+__global__ void k_sort_tiles(SortScratch ss, const SortSeg* cur, SortSeg* curw) {
+    if (sort_overflow(ss)) return;
+    const uint32_t nseg = sort_nseg(ss);
     PTL_FOR(s, nseg) {
         SortSeg g = cur[s];
         median_to_first(ss.a, g.first, g.last);
@@ -209,11 +229,13 @@ __global__ void k_sort_tiles(SortScratch ss, const SortSeg* cur, SortSeg* curw, 
         g.tcount = (m1 + kSortTile - 1) / kSortTile;
         g.tbase = atomicAdd(&ss.counters[0], g.tcount);
         curw[s] = g;
-        if (g.tbase + g.tcount > ss.tile_cap) continue;  // the host sees the count and stops
+        if (g.tbase + g.tcount > ss.tile_cap) {
+            ss.counters[5] = 1;
+            continue;
+        }
         for (uint32_t k = 0; k < g.tcount; ++k) ss.tile_seg[g.tbase + k] = s;
     }
 }
-
 __device__ __forceinline__ uint32_t block_reduce_add(uint32_t v, uint32_t* sm) {
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
 #pragma unroll
@@ -232,37 +254,93 @@ constexpr uint32_t kSortItems = kSortTile / kThreads;  // 8 per thread
 
 __global__ void __launch_bounds__(kThreads) k_sort_count(SortScratch ss, const SortSeg* cur) {
     __shared__ uint32_t sm[kThreads / 32];
-    const uint32_t t = blockIdx.x;
-    const SortSeg g = cur[ss.tile_seg[t]];
-    const uint32_t lo = g.first + 1 + (t - g.tbase) * kSortTile;
-    const uint32_t hi = min(g.last, lo + kSortTile);
-    uint32_t cl = 0, cr = 0;
-    for (uint32_t p = lo + threadIdx.x; p < hi; p += kThreads) {
-        const int32_t k = skey(ss.a[p]);
-        cl += is_lstop(k, g.pivot);
-        cr += is_rstop(k, g.pivot);
-    }
-    const uint32_t tl = block_reduce_add(cl, sm);
-    const uint32_t tr = block_reduce_add(cr, sm);
-    if (threadIdx.x == 0) {
-        ss.tile_l[t] = tl;
-        ss.tile_r[t] = tr;
+    if (sort_overflow(ss)) return;
+    const uint32_t ntiles = sort_ntiles(ss);
+    for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const SortSeg g = cur[ss.tile_seg[t]];
+        const uint32_t lo = g.first + 1 + (t - g.tbase) * kSortTile;
+        const uint32_t hi = min(g.last, lo + kSortTile);
+        uint32_t cl = 0, cr = 0;
+        for (uint32_t p = lo + threadIdx.x; p < hi; p += kThreads) {
+            const int32_t k = skey(ss.a[p]);
+            cl += is_lstop(k, g.pivot);
+            cr += is_rstop(k, g.pivot);
+        }
+        const uint32_t tl = block_reduce_add(cl, sm);
+        const uint32_t tr = block_reduce_add(cr, sm);
+        if (threadIdx.x == 0) {
+            ss.tile_l[t] = tl;
+            ss.tile_r[t] = tr;
+        }
+        __syncthreads();
     }
 }
 
-// Exclusive offsets of the tile counts of each segment (one CTA per segment).
 __global__ void __launch_bounds__(kThreads) k_sort_segscan(SortScratch ss, SortSeg* cur) {
     __shared__ uint32_t sl[kThreads], sr[kThreads];
     __shared__ uint32_t carry_l, carry_r;
-    SortSeg& g = cur[blockIdx.x];
-    if (threadIdx.x == 0) { carry_l = 0; carry_r = 0; }
-    __syncthreads();
-    for (uint32_t c = 0; c < g.tcount; c += kThreads) {
-        const uint32_t k = c + threadIdx.x;
-        const uint32_t vl = k < g.tcount ? ss.tile_l[g.tbase + k] : 0u;
-        const uint32_t vr = k < g.tcount ? ss.tile_r[g.tbase + k] : 0u;
-        sl[threadIdx.x] = vl;
-        sr[threadIdx.x] = vr;
+    if (sort_overflow(ss)) return;
+    const uint32_t nseg = sort_nseg(ss);
+    for (uint32_t si = blockIdx.x; si < nseg; si += gridDim.x) {
+        SortSeg& g = cur[si];
+        if (threadIdx.x == 0) { carry_l = 0; carry_r = 0; }
+        __syncthreads();
+        for (uint32_t c = 0; c < g.tcount; c += kThreads) {
+            const uint32_t k = c + threadIdx.x;
+            const uint32_t vl = k < g.tcount ? ss.tile_l[g.tbase + k] : 0u;
+            const uint32_t vr = k < g.tcount ? ss.tile_r[g.tbase + k] : 0u;
+            sl[threadIdx.x] = vl;
+            sr[threadIdx.x] = vr;
+            __syncthreads();
+            for (uint32_t d = 1; d < kThreads; d <<= 1) {
+                const uint32_t al = threadIdx.x >= d ? sl[threadIdx.x - d] : 0u;
+                const uint32_t ar = threadIdx.x >= d ? sr[threadIdx.x - d] : 0u;
+                __syncthreads();
+                sl[threadIdx.x] += al;
+                sr[threadIdx.x] += ar;
+                __syncthreads();
+            }
+            if (k < g.tcount) {
+                ss.tile_l[g.tbase + k] = carry_l + sl[threadIdx.x] - vl;
+                ss.tile_r[g.tbase + k] = carry_r + sr[threadIdx.x] - vr;
+            }
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                carry_l += sl[kThreads - 1];
+                carry_r += sr[kThreads - 1];
+            }
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) {
+            g.nL = carry_l;
+            g.nR = carry_r;
+        }
+        __syncthreads();
+    }
+}
+
+// Stop positions by rank: A[rank] for L-stops, B[rank from the right] for R-stops.
+__global__ void __launch_bounds__(kThreads) k_sort_pos(SortScratch ss, const SortSeg* cur) {
+    __shared__ uint32_t sl[kThreads], sr[kThreads];
+    if (sort_overflow(ss)) return;
+    const uint32_t ntiles = sort_ntiles(ss);
+    for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const SortSeg g = cur[ss.tile_seg[t]];
+        const uint32_t lo = g.first + 1 + (t - g.tbase) * kSortTile;
+        const uint32_t hi = min(g.last, lo + kSortTile);
+        const uint32_t p0 = lo + threadIdx.x * kSortItems;
+        uint32_t fl = 0, fr = 0, cl = 0, cr = 0;
+#pragma unroll
+        for (uint32_t k = 0; k < kSortItems; ++k) {
+            const uint32_t p = p0 + k;
+            if (p < hi) {
+                const int32_t key = skey(ss.a[p]);
+                if (is_lstop(key, g.pivot)) { fl |= 1u << k; ++cl; }
+                if (is_rstop(key, g.pivot)) { fr |= 1u << k; ++cr; }
+            }
+        }
+        sl[threadIdx.x] = cl;
+        sr[threadIdx.x] = cr;
         __syncthreads();
         for (uint32_t d = 1; d < kThreads; d <<= 1) {
             const uint32_t al = threadIdx.x >= d ? sl[threadIdx.x - d] : 0u;
@@ -272,59 +350,15 @@ __global__ void __launch_bounds__(kThreads) k_sort_segscan(SortScratch ss, SortS
             sr[threadIdx.x] += ar;
             __syncthreads();
         }
-        if (k < g.tcount) {
-            ss.tile_l[g.tbase + k] = carry_l + sl[threadIdx.x] - vl;
-            ss.tile_r[g.tbase + k] = carry_r + sr[threadIdx.x] - vr;
-        }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            carry_l += sl[kThreads - 1];
-            carry_r += sr[kThreads - 1];
-        }
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) {
-        g.nL = carry_l;
-        g.nR = carry_r;
-    }
-}
-
-// Stop positions by rank: A[rank] for L-stops, B[rank from the right] for R-stops.
-__global__ void __launch_bounds__(kThreads) k_sort_pos(SortScratch ss, const SortSeg* cur) {
-    __shared__ uint32_t sl[kThreads], sr[kThreads];
-    const uint32_t t = blockIdx.x;
-    const SortSeg g = cur[ss.tile_seg[t]];
-    const uint32_t lo = g.first + 1 + (t - g.tbase) * kSortTile;
-    const uint32_t hi = min(g.last, lo + kSortTile);
-    const uint32_t p0 = lo + threadIdx.x * kSortItems;
-    uint32_t fl = 0, fr = 0, cl = 0, cr = 0;
+        uint32_t rl = ss.tile_l[t] + sl[threadIdx.x] - cl;
+        uint32_t rr = ss.tile_r[t] + sr[threadIdx.x] - cr;
 #pragma unroll
-    for (uint32_t k = 0; k < kSortItems; ++k) {
-        const uint32_t p = p0 + k;
-        if (p < hi) {
-            const int32_t key = skey(ss.a[p]);
-            if (is_lstop(key, g.pivot)) { fl |= 1u << k; ++cl; }
-            if (is_rstop(key, g.pivot)) { fr |= 1u << k; ++cr; }
+        for (uint32_t k = 0; k < kSortItems; ++k) {
+            const uint32_t p = p0 + k;
+            if ((fl >> k) & 1u) ss.apos[g.first + rl++] = p;
+            if ((fr >> k) & 1u) ss.bpos[g.first + (g.nR - 1u - rr++)] = p;
         }
-    }
-    sl[threadIdx.x] = cl;
-    sr[threadIdx.x] = cr;
-    __syncthreads();
-    for (uint32_t d = 1; d < kThreads; d <<= 1) {
-        const uint32_t al = threadIdx.x >= d ? sl[threadIdx.x - d] : 0u;
-        const uint32_t ar = threadIdx.x >= d ? sr[threadIdx.x - d] : 0u;
         __syncthreads();
-        sl[threadIdx.x] += al;
-        sr[threadIdx.x] += ar;
-        __syncthreads();
-    }
-    uint32_t rl = ss.tile_l[t] + sl[threadIdx.x] - cl;
-    uint32_t rr = ss.tile_r[t] + sr[threadIdx.x] - cr;
-#pragma unroll
-    for (uint32_t k = 0; k < kSortItems; ++k) {
-        const uint32_t p = p0 + k;
-        if ((fl >> k) & 1u) ss.apos[g.first + rl++] = p;
-        if ((fr >> k) & 1u) ss.bpos[g.first + (g.nR - 1u - rr++)] = p;
     }
 }
 
@@ -333,12 +367,14 @@ __device__ void sort_emit(SortScratch ss, SortSeg* next, uint32_t first, uint32_
         if (last - first > 1) {
             const uint32_t k = atomicAdd(&ss.counters[2], 1u);
             if (k < ss.leaf_cap) { ss.leaf[2 * k] = first; ss.leaf[2 * k + 1] = last; }
+            else ss.counters[5] = 1;
         }
         return;
     }
     if (dl == 0) {
         const uint32_t k = atomicAdd(&ss.counters[3], 1u);
         if (k < ss.leaf_cap) { ss.heap[2 * k] = first; ss.heap[2 * k + 1] = last; }
+        else ss.counters[5] = 1;
         return;
     }
     const uint32_t k = atomicAdd(&ss.counters[1], 1u);
@@ -348,10 +384,14 @@ __device__ void sort_emit(SortScratch ss, SortSeg* next, uint32_t first, uint32_
         c.last = last;
         c.dl = dl;
         next[k] = c;
+    } else {
+        ss.counters[5] = 1;
     }
 }
 
-__global__ void k_sort_cut(SortScratch ss, SortSeg* cur, uint32_t nseg, SortSeg* next, ErrorWord* err) {
+__global__ void k_sort_cut(SortScratch ss, SortSeg* cur, SortSeg* next, ErrorWord* err) {
+    if (sort_overflow(ss)) return;
+    const uint32_t nseg = sort_nseg(ss);
     PTL_FOR(s, nseg) {
         SortSeg& g = cur[s];
         if (g.nL == 0 || g.nR == 0) {  // the median move guarantees both kinds of stop
@@ -372,12 +412,15 @@ __global__ void k_sort_cut(SortScratch ss, SortSeg* cur, uint32_t nseg, SortSeg*
 }
 
 __global__ void __launch_bounds__(kThreads) k_sort_swap(SortScratch ss, const SortSeg* cur) {
-    const uint32_t t = blockIdx.x;
-    const SortSeg g = cur[ss.tile_seg[t]];
-    const uint32_t k0 = (t - g.tbase) * kSortTile;
-    const uint32_t k1 = min(g.K, k0 + kSortTile);
-    for (uint32_t k = k0 + threadIdx.x; k < k1; k += kThreads) {
-        sswap(ss.a, ss.apos[g.first + k], ss.bpos[g.first + k]);
+    if (sort_overflow(ss)) return;
+    const uint32_t ntiles = sort_ntiles(ss);
+    for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const SortSeg g = cur[ss.tile_seg[t]];
+        const uint32_t k0 = (t - g.tbase) * kSortTile;
+        const uint32_t k1 = min(g.K, k0 + kSortTile);
+        for (uint32_t k = k0 + threadIdx.x; k < k1; k += kThreads) {
+            sswap(ss.a, ss.apos[g.first + k], ss.bpos[g.first + k]);
+        }
     }
 }
 
@@ -464,20 +507,11 @@ __device__ bool ra_wait_chunk(const uint32_t* done, uint32_t c, uint32_t need, E
 //   2. symbol updates: a symbol updated by its owner ends swapped only if a later group
 //      also triggered it; other triggered symbols end swapped;
 //   3. row 0 takes, per physical register, the write of the highest group.
+// The lane-0 block: P's lane-0 functions in lock-step over S steps, K cache entries per
+// function in smem.  With chunks > 0 it waits on the independent functions' progress.
 template <int Q>
-__global__ void __launch_bounds__(1024) k_ra_steps(Prog P, uint32_t S, uint32_t K, uint32_t Kf, uint32_t chunks) {
-    extern __shared__ __align__(16) unsigned char smem[];
+__device__ void ra_lane0_block(const Prog& P, uint32_t S, uint32_t K, uint32_t chunks, unsigned char* smem) {
     const uint32_t tid = threadIdx.x, T = blockDim.x;
-    if (blockIdx.x > 0) {
-        uint32_t* tag = reinterpret_cast<uint32_t*>(smem);
-        const SymCache cf{tag, tag + T * Kf, Kf};
-        // the independent functions never need definition positions
-        Prog Pf = P;
-        Pf.defpos = nullptr;
-        const uint32_t f = free_function_of((blockIdx.x - 1u) * T + tid);
-        if (f < P.F) ra_free_function_cached(Pf, cf, tid, f, P.ra_chunks + chunks);
-        return;
-    }
     __shared__ uint32_t s_abort;
     const uint32_t* hist = P.ra_chunks;
     const uint32_t* done = P.ra_chunks + chunks;
@@ -596,6 +630,24 @@ __global__ void __launch_bounds__(1024) k_ra_steps(Prog P, uint32_t S, uint32_t 
     }
 }
 
+
+template <int Q>
+__global__ void __launch_bounds__(1024) k_ra_steps(Prog P, uint32_t S, uint32_t K, uint32_t Kf, uint32_t chunks) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const uint32_t tid = threadIdx.x, T = blockDim.x;
+    if (blockIdx.x > 0) {
+        uint32_t* tag = reinterpret_cast<uint32_t*>(smem);
+        const SymCache cf{tag, tag + T * Kf, Kf};
+        // the independent functions never need definition positions
+        Prog Pf = P;
+        Pf.defpos = nullptr;
+        const uint32_t f = free_function_of((blockIdx.x - 1u) * T + tid);
+        if (f < P.F) ra_free_function_cached(Pf, cf, tid, f, P.ra_chunks + chunks);
+        return;
+    }
+    ra_lane0_block<Q>(P, S, K, chunks, smem);
+}
+
 // flags[1]: functions share symbols; flags[2]: a lane-0 virtual register has two
 // definitions.  stamp counts the definitions (zeroed before).
 __global__ void k_ra_cross(Prog P) {
@@ -660,11 +712,67 @@ void launch_functab(const Prog& P, uint32_t* meta, cudaStream_t s) {
     k_functab_end<<<grid_for(bound), kThreads, 0, s>>>(P, meta);
 }
 
+// Introsort rounds over the nseg0 segments in ss.seg[0] (leaves and heaps already
+// recorded in the counters), then the heap and leaf passes.  The rounds run back to back on
+// the device; the host checks for the end (no segments left) after a first batch of
+// first_batch rounds and then every few rounds.  Rounds after the end find no segments and
+// return at once.
+cudaError_t run_sort_rounds(const SortScratch& ss, uint32_t nseg0, uint32_t first_batch, uint32_t max_rounds,
+                            ErrorWord* err, cudaStream_t s, uint32_t* rounds_out) {
+    cudaMemcpyAsync(ss.counters + 1, &nseg0, sizeof(uint32_t), cudaMemcpyHostToDevice, s);
+    const unsigned seg_grid = static_cast<unsigned>(std::min<uint64_t>(ss.seg_cap, 152ull * 8));
+    const unsigned tile_grid = static_cast<unsigned>(std::min<uint64_t>(ss.tile_cap, 152ull * 8));
+    uint32_t rounds = 0, nseg = nseg0;
+    int cur = 0;
+    uint32_t batch = std::max<uint32_t>(first_batch, 1u);
+    while (nseg > 0) {
+        for (uint32_t r = 0; r < batch; ++r) {
+            SortSeg* segs = ss.seg[cur];
+            SortSeg* next = ss.seg[cur ^ 1];
+            g_launches++;
+            k_sort_round<<<1, 32, 0, s>>>(ss);
+            g_launches++;
+            k_sort_tiles<<<grid_for(ss.seg_cap), kThreads, 0, s>>>(ss, segs, segs);
+            g_launches++;
+            k_sort_count<<<tile_grid, kThreads, 0, s>>>(ss, segs);
+            g_launches++;
+            k_sort_segscan<<<seg_grid, kThreads, 0, s>>>(ss, segs);
+            g_launches++;
+            k_sort_pos<<<tile_grid, kThreads, 0, s>>>(ss, segs);
+            g_launches++;
+            k_sort_cut<<<grid_for(ss.seg_cap), kThreads, 0, s>>>(ss, segs, next, err);
+            g_launches++;
+            k_sort_swap<<<tile_grid, kThreads, 0, s>>>(ss, segs);
+            cur ^= 1;
+            ++rounds;
+        }
+        uint32_t c[6] = {0, 0, 0, 0, 0, 0};
+        cudaMemcpyAsync(c, ss.counters, sizeof(c), cudaMemcpyDeviceToHost, s);
+        const cudaError_t e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) return e;
+        if (c[5]) return cudaErrorMemoryAllocation;
+        nseg = c[1];
+        // every round shortens each segment and the depth budget ends partitioning
+        // after 2*floor(log2 n) levels
+        if (nseg > 0 && rounds > max_rounds) return cudaErrorLaunchFailure;
+        batch = 4;
+    }
+    uint32_t lh[2] = {0, 0};
+    cudaMemcpyAsync(lh, ss.counters + 2, sizeof(lh), cudaMemcpyDeviceToHost, s);
+    cudaError_t e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return e;
+    if (lh[0] > ss.leaf_cap || lh[1] > ss.leaf_cap) return cudaErrorMemoryAllocation;
+    if (lh[1]) { g_launches++; k_sort_heaps<<<grid_for(lh[1]), kThreads, 0, s>>>(ss, lh[1]); }
+    if (lh[0]) { g_launches++; k_sort_leaves<<<grid_for(lh[0]), kThreads, 0, s>>>(ss, lh[0]); }
+    if (rounds_out) *rounds_out = rounds;
+    return cudaGetLastError();
+}
+
 cudaError_t run_depth_sort(const Prog& P, const SortScratch& ss, cudaStream_t s, uint32_t* rounds_out) {
     const uint32_t n = P.n;
     g_launches++;
     k_sort_init<<<grid_for(n), kThreads, 0, s>>>(P, ss);
-    cudaMemsetAsync(ss.counters, 0, sizeof(uint32_t) * 4, s);
+    cudaMemsetAsync(ss.counters, 0, sizeof(uint32_t) * 6, s);
     uint32_t nseg = 0;
     if (n > kSortThreshold) {
         SortSeg g{};
@@ -679,52 +787,13 @@ cudaError_t run_depth_sort(const Prog& P, const SortScratch& ss, cudaStream_t s,
         const uint32_t one = 1;
         cudaMemcpyAsync(ss.counters + 2, &one, sizeof(one), cudaMemcpyHostToDevice, s);
     }
-    uint32_t rounds = 0;
-    int cur = 0;
-    while (nseg > 0) {
-        SortSeg* segs = ss.seg[cur];
-        SortSeg* next = ss.seg[cur ^ 1];
-        cudaMemsetAsync(ss.counters, 0, sizeof(uint32_t) * 2, s);
-        g_launches++;
-        k_sort_tiles<<<grid_for(nseg), kThreads, 0, s>>>(ss, segs, segs, nseg);
-        uint32_t ntiles = 0;
-        cudaMemcpyAsync(&ntiles, ss.counters, sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
-        cudaError_t e = cudaStreamSynchronize(s);
-        if (e != cudaSuccess) return e;
-        if (ntiles > ss.tile_cap) return cudaErrorMemoryAllocation;
-        g_launches++;
-        k_sort_count<<<ntiles, kThreads, 0, s>>>(ss, segs);
-        g_launches++;
-        k_sort_segscan<<<nseg, kThreads, 0, s>>>(ss, segs);
-        g_launches++;
-        k_sort_pos<<<ntiles, kThreads, 0, s>>>(ss, segs);
-        g_launches++;
-        k_sort_cut<<<grid_for(nseg), kThreads, 0, s>>>(ss, segs, nseg, next, P.err);
-        g_launches++;
-        k_sort_swap<<<ntiles, kThreads, 0, s>>>(ss, segs);
-        cudaMemcpyAsync(&nseg, ss.counters + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
-        e = cudaStreamSynchronize(s);
-        if (e != cudaSuccess) return e;
-        if (nseg > ss.seg_cap) return cudaErrorMemoryAllocation;
-        cur ^= 1;
-        ++rounds;
-        // every round shortens each segment and the depth budget ends partitioning
-        // after 2*floor(log2 n) levels
-        if (rounds > 2u * floor_log2(n) + 4u) return cudaErrorLaunchFailure;
-    }
-    uint32_t lh[2] = {0, 0};
-    cudaMemcpyAsync(lh, ss.counters + 2, sizeof(lh), cudaMemcpyDeviceToHost, s);
-    cudaError_t e = cudaStreamSynchronize(s);
+    const uint32_t lg = floor_log2(std::max<uint32_t>(n, 2u));
+    const cudaError_t e = run_sort_rounds(ss, nseg, lg > 4u ? lg - 4u : 1u, 2u * lg + 4u, P.err, s, rounds_out);
     if (e != cudaSuccess) return e;
-    if (lh[0] > ss.leaf_cap || lh[1] > ss.leaf_cap) return cudaErrorMemoryAllocation;
-    if (lh[1]) { g_launches++; k_sort_heaps<<<grid_for(lh[1]), kThreads, 0, s>>>(ss, lh[1]); }
-    if (lh[0]) { g_launches++; k_sort_leaves<<<grid_for(lh[0]), kThreads, 0, s>>>(ss, lh[0]); }
     g_launches++;
     k_sort_out<<<grid_for(n), kThreads, 0, s>>>(P, ss);
-    if (rounds_out) *rounds_out = rounds;
     return cudaGetLastError();
 }
-
 void launch_gen(const Prog& P, cudaStream_t s) {
     g_launches++;
     k_gen_prop<<<grid_for(P.n), kThreads, 0, s>>>(P);
@@ -873,6 +942,413 @@ void launch_fixjumps_emit(const Prog& P, cudaStream_t s) {
     k_fj_emit<<<grid_for(P.W2), kThreads, 0, s>>>(P);
     g_launches++;
     k_fj_functab<<<grid_for(P.F), kThreads, 0, s>>>(P);
+}
+
+
+// ====================================================================== batched programs
+// Many programs per launch.  Each program keeps its own Prog view (device memory, one
+// per program) into arenas laid out per program with the generator's zero pads, so the
+// per-element stage functions run unchanged.  Work is cut into tiles that never straddle
+// programs: off[p] is the first tile of program p (exclusive prefix over the programs;
+// programs left out of a stage have no tiles).
+namespace {
+
+constexpr uint32_t kBTile = 1024;
+
+__device__ __forceinline__ uint32_t batch_program(const uint32_t* off, uint32_t B, uint32_t t) {
+    uint32_t lo = 0, hi = B;  // off[lo] <= t < off[hi]
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (off[mid] <= t) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+template <class Op>
+__global__ void __launch_bounds__(kThreads) k_batch(const Prog* progs, const uint32_t* off, uint32_t B, uint32_t total,
+                                                    Op op) {
+    for (uint32_t t = blockIdx.x; t < total; t += gridDim.x) {
+        const uint32_t p = batch_program(off, B, t);
+        const Prog& P = progs[p];
+        const uint32_t cnt = Op::count(P);
+        const uint32_t base = (t - off[p]) * kBTile;
+        for (uint32_t k = threadIdx.x; k < kBTile; k += kThreads) {
+            const uint32_t i = base + k;
+            if (i < cnt) op(P, i, p);
+        }
+    }
+}
+
+#define PTL_BATCH_OP(NAME, COUNT, BODY)                                                         \
+    struct NAME {                                                                              \
+        __device__ static uint32_t count(const Prog& P) { return COUNT; }                      \
+        __device__ void operator()(const Prog& P, uint32_t i, uint32_t p) const { BODY; }      \
+    };
+
+PTL_BATCH_OP(BValidate, P.n, if (st_input_bad(P, i)) record_error(P.err, ST_INVALID_AST, 0, i))
+PTL_BATCH_OP(BTranslate, P.nb8, st_translate(P, i))
+PTL_BATCH_OP(BPreArgs, P.nb8, st_pre_args(P, i))
+PTL_BATCH_OP(BPreLists, P.nb8, st_pre_lists(P, i))
+PTL_BATCH_OP(BPreFloat, P.nb8, st_pre_float(P, i))
+PTL_BATCH_OP(BPreFloatApply, P.nb8, st_pre_float_apply(P, i))
+PTL_BATCH_OP(BFixOwn, P.nb8, st_fix_own(P, i))
+PTL_BATCH_OP(BFixCond, P.nb8, st_fix_cond(P, i))
+PTL_BATCH_OP(BFunctab, P.fb8, st_functab(P, i))
+PTL_BATCH_OP(BGenProp, P.n, st_gen_prop(P, i))
+PTL_BATCH_OP(BGenClaim, P.n, st_gen_claim(P, i))
+PTL_BATCH_OP(BGenWrite, P.n, st_gen_write(P, i))
+PTL_BATCH_OP(BOptMark, P.wb8, st_opt_mark(P, i))
+PTL_BATCH_OP(BOptFinal, P.wb8, st_opt_final(P, i))
+PTL_BATCH_OP(BInitLifetime, P.F, P.lifetime[i] = 0x1Full)
+PTL_BATCH_OP(BSpill, P.W, st_ra_spill(P, i))
+PTL_BATCH_OP(BScatter, P.wb8, st_ra_scatter(P, i))
+PTL_BATCH_OP(BRaFunctab, P.F, st_fix_functab(P, i, P.roffs, P.W))
+PTL_BATCH_OP(BRaFrame, P.F, st_ra_frame(P, i))
+PTL_BATCH_OP(BFjEmit, P.W2, st_fj_emit(P, i))
+PTL_BATCH_OP(BFjFunctab, P.F, st_fix_functab(P, i, P.joffs, P.W2))
+PTL_BATCH_OP(BCross, P.W,
+             const uint32_t r = st_ra_cross(P, i, P.stamp);
+             if (r & 1u) atomicOr(&P.flags[1], 1u);
+             if (r & 2u) atomicOr(&P.flags[2], 1u))
+
+// per program: depths seen (seen + soff[p], max_depth + 1 entries)
+struct BDepthSeen {
+    uint32_t* seen;
+    const uint64_t* soff;
+    __device__ static uint32_t count(const Prog& P) { return P.n; }
+    __device__ void operator()(const Prog& P, uint32_t i, uint32_t p) const {
+        const int32_t d = P.in_depth[i];
+        if (d >= 0 && static_cast<uint32_t>(d) <= P.max_depth) seen[soff[p] + static_cast<uint32_t>(d)] = 1u;
+    }
+};
+// per program: word count and longest function (meta[4p + 1], meta[4p + 2])
+struct BFunctabEnd {
+    uint32_t* meta;
+    __device__ static uint32_t count(const Prog& P) { return P.fb8; }
+    __device__ void operator()(const Prog& P, uint32_t f, uint32_t p) const {
+        st_functab_end(P, f);
+        if (f < P.F) atomicMax(&meta[4u * p + 2u], P.fn_size[f]);
+        if (f == 0) meta[4u * p + 1u] = P.loc[P.n - 1];
+    }
+};
+// depth-order keys of all programs in one array, program p from aoff[p]
+struct BSortInit {
+    unsigned long long* a;
+    const uint64_t* aoff;
+    __device__ static uint32_t count(const Prog& P) { return P.n; }
+    __device__ void operator()(const Prog& P, uint32_t i, uint32_t p) const {
+        a[aoff[p] + i] = (static_cast<unsigned long long>(u32(P.dep[i])) << 32) | i;
+    }
+};
+struct BSortOut {
+    const unsigned long long* a;
+    const uint64_t* aoff;
+    __device__ static uint32_t count(const Prog& P) { return P.n; }
+    __device__ void operator()(const Prog& P, uint32_t i, uint32_t p) const { P.pos[sidx(a[aoff[p] + i])] = i; }
+};
+
+__global__ void __launch_bounds__(kThreads) k_batch_sweep(const Prog* progs, const uint32_t* off, uint32_t B,
+                                                          uint32_t total, uint32_t* changed) {
+    for (uint32_t t = blockIdx.x; t < total; t += gridDim.x) {
+        const uint32_t p = batch_program(off, B, t);
+        const Prog& P = progs[p];
+        const uint32_t base = (t - off[p]) * kBTile;
+        bool any = false;
+        for (uint32_t k = threadIdx.x; k < kBTile; k += kThreads) {
+            const uint32_t i = base + k;
+            if (i < P.wb8) any |= st_opt_sweep(P, i);
+        }
+        if (__syncthreads_or(any) && threadIdx.x == 0) *changed = 1u;
+    }
+}
+
+// per-program sizes after the regalloc and fix_jumps scans
+__global__ void k_batch_w2(const Prog* progs, const uint32_t* list, uint32_t count, uint32_t* meta) {
+    PTL_FOR(k, count) {
+        const Prog& P = progs[list[k]];
+        meta[4u * list[k]] = P.roffs[P.W - 1u] + 1u;
+    }
+}
+__global__ void k_batch_w3(const Prog* progs, const uint32_t* list, uint32_t count, uint32_t* meta) {
+    PTL_FOR(k, count) {
+        const Prog& P = progs[list[k]];
+        meta[4u * list[k] + 1u] = P.fsz[P.W2 - 1u] + P.joffs[P.W2 - 1u];
+    }
+}
+
+// ---- batched scan: the decoupled look-back scan with tiles per program; a tile looks
+// back only as far as its program's first tile.
+struct BScanCount {
+    __device__ static uint32_t count(const Prog& P) { return P.nb8; }
+    __device__ uint32_t load(const Prog& P, uint32_t i) const {
+        const uint32_t v = st_count(P, i);
+        P.sizes[i] = v;
+        return v;
+    }
+    __device__ void store(const Prog& P, uint32_t i, uint32_t v, uint32_t) const { P.loc0[i] = v; }
+};
+struct BScanDecl {
+    uint32_t* meta;
+    __device__ static uint32_t count(const Prog& P) { return P.nb8; }
+    __device__ uint32_t load(const Prog& P, uint32_t i) const { return P.nt[i] == RV_FUNC_DECL ? 1u : 0u; }
+    __device__ void store(const Prog& P, uint32_t i, uint32_t v, uint32_t p) const {
+        const bool is_decl = P.nt[i] == RV_FUNC_DECL;
+        if (is_decl) P.decl[v] = i;
+        if (i == P.nb8 - 1u) meta[4u * p] = v + (is_decl ? 1u : 0u);
+    }
+};
+struct BScanRaCount {
+    __device__ static uint32_t count(const Prog& P) { return P.wb8; }
+    __device__ uint32_t load(const Prog& P, uint32_t i) const { return st_ra_count(P, i); }
+    __device__ void store(const Prog& P, uint32_t i, uint32_t v, uint32_t) const { P.roffs[i] = v; }
+};
+struct BScanFjSize {
+    __device__ static uint32_t count(const Prog& P) { return P.w2b8; }
+    __device__ uint32_t load(const Prog& P, uint32_t i) const {
+        const uint32_t v = i < P.W2 ? st_fj_size(P, i) : 0u;
+        P.fsz[i] = v;
+        return v;
+    }
+    __device__ void store(const Prog& P, uint32_t i, uint32_t v, uint32_t) const { P.joffs[i] = v; }
+};
+
+template <class Op>
+__global__ void __launch_bounds__(kScanThreads) k_bscan(const Prog* progs, const uint32_t* off, uint32_t B, Op op,
+                                                        ScanScratch sc) {
+    constexpr int kWarps = kScanThreads / 32;
+    __shared__ uint32_t s_tile, s_prefix;
+    __shared__ uint32_t s_warp[kWarps];
+    if (threadIdx.x == 0) s_tile = atomicAdd(sc.counter, 1u);
+    __syncthreads();
+    const uint32_t tile = s_tile;
+    const uint32_t p = batch_program(off, B, tile);
+    const Prog& P = progs[p];
+    const uint32_t first = off[p];  // the program's first tile
+    const uint32_t count = Op::count(P);
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    const uint64_t wbase = static_cast<uint64_t>(tile - first) * kScanTile + static_cast<uint64_t>(warp) * 32u * kScanItems;
+    uint32_t v[kScanItems];
+    uint32_t carry = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        const uint64_t idx = wbase + static_cast<uint64_t>(k) * 32u + lane;
+        const uint32_t x = idx < count ? op.load(P, static_cast<uint32_t>(idx)) : 0u;
+        const uint32_t incl = warp_incl_scan(x);
+        v[k] = carry + incl - x;
+        carry += __shfl_sync(0xFFFFFFFFu, incl, 31);
+    }
+    if (lane == 0) s_warp[warp] = carry;
+    __syncthreads();
+    if (warp == 0) {
+        const uint32_t t = lane < kWarps ? s_warp[lane] : 0u;
+        const uint32_t incl = warp_incl_scan(t);
+        if (lane < kWarps) s_warp[lane] = incl - t;
+        const uint32_t aggregate = __shfl_sync(0xFFFFFFFFu, incl, kWarps - 1);
+        if (lane == 0) {
+            uint32_t prefix = 0;
+            if (tile == first) {
+                atomicExch(&sc.status[tile], (2ull << 32) | aggregate);
+            } else {
+                atomicExch(&sc.status[tile], (1ull << 32) | aggregate);
+                int64_t j = static_cast<int64_t>(tile) - 1;
+                uint32_t spins = 0;
+                while (j >= static_cast<int64_t>(first)) {
+                    const unsigned long long st = *reinterpret_cast<volatile unsigned long long*>(&sc.status[j]);
+                    const uint32_t flag = static_cast<uint32_t>(st >> 32);
+                    if (flag == 0) {
+                        if (++spins > kSpinLimit) {
+                            record_error(P.err, ST_DEVICE_TIMEOUT, W_SCAN, tile);
+                            break;
+                        }
+                        continue;
+                    }
+                    prefix += static_cast<uint32_t>(st);
+                    if (flag == 2) break;
+                    --j;
+                }
+                atomicExch(&sc.status[tile], (2ull << 32) | (prefix + aggregate));
+            }
+            s_prefix = prefix;
+        }
+    }
+    __syncthreads();
+    const uint32_t base = s_prefix + s_warp[warp];
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        const uint64_t idx = wbase + static_cast<uint64_t>(k) * 32u + lane;
+        if (idx < count) op.store(P, static_cast<uint32_t>(idx), base + v[k], p);
+    }
+}
+
+// ---- batched register allocation
+// Independent functions of all listed programs: one thread each (64 per block).
+__global__ void __launch_bounds__(kRaFreeThreads) k_batch_free(const Prog* progs, const uint32_t* off, uint32_t B,
+                                                               uint32_t total) {
+    __shared__ uint32_t tag[kRaFreeThreads * kRaFreeK];
+    __shared__ uint32_t val[kRaFreeThreads * kRaFreeK];
+    const SymCache c{tag, val, kRaFreeK};
+    for (uint32_t t = blockIdx.x; t < total; t += gridDim.x) {
+        const uint32_t p = batch_program(off, B, t);
+        Prog Pf = progs[p];
+        Pf.defpos = nullptr;  // the independent functions never need definition positions
+        const uint32_t f = free_function_of((t - off[p]) * kRaFreeThreads + threadIdx.x);
+        if (f < Pf.F) ra_free_function_cached(Pf, c, threadIdx.x, f);
+    }
+}
+
+// Lane-0 functions: one block per listed program (the program's view in shared memory).
+template <int Q>
+__global__ void __launch_bounds__(1024) k_batch_lane0(const Prog* progs, const uint32_t* list, uint32_t K) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ Prog sP;
+    const uint32_t p = list[blockIdx.x];
+    {
+        const uint64_t* src = reinterpret_cast<const uint64_t*>(&progs[p]);
+        uint64_t* dst = reinterpret_cast<uint64_t*>(&sP);
+        for (uint32_t k = threadIdx.x; k < sizeof(Prog) / 8; k += blockDim.x) dst[k] = src[k];
+    }
+    __syncthreads();
+    ra_lane0_block<Q>(sP, sP.S, K, 0u, smem);
+}
+
+__global__ void k_batch_serial(const Prog* progs, const uint32_t* list, uint32_t count) {
+    PTL_FOR(k, count) {
+        const Prog& P = progs[list[k]];
+        st_ra_serial(P, P.stamp);
+    }
+}
+
+template <class Op>
+void batch_launch(const BatchLaunch& bl, uint32_t total, const Op& op) {
+    if (total == 0) return;
+    g_launches++;
+    k_batch<Op><<<std::min<uint32_t>(total, 152u * 16u), kThreads, 0, bl.s>>>(bl.progs, bl.off, bl.B, total, op);
+}
+
+}  // namespace
+
+static_assert(sizeof(Prog) % 8 == 0, "Prog copies in 8-byte words");
+
+uint32_t batch_tile() { return kBTile; }
+uint32_t batch_scan_tile() { return kScanTile; }
+
+void batch_stage(BatchStage st, const BatchLaunch& bl, uint32_t total, uint32_t* meta, uint32_t* seen,
+                 const uint64_t* off64) {
+    switch (st) {
+        case BatchStage::Validate: batch_launch(bl, total, BValidate{}); break;
+        case BatchStage::DepthSeen: batch_launch(bl, total, BDepthSeen{seen, off64}); break;
+        case BatchStage::Translate: batch_launch(bl, total, BTranslate{}); break;
+        case BatchStage::Preprocess:
+            batch_launch(bl, total, BPreArgs{});
+            batch_launch(bl, total, BPreLists{});
+            batch_launch(bl, total, BPreFloat{});
+            batch_launch(bl, total, BPreFloatApply{});
+            break;
+        case BatchStage::Fix:
+            batch_launch(bl, total, BFixOwn{});
+            batch_launch(bl, total, BFixCond{});
+            break;
+        case BatchStage::Functab:
+            batch_launch(bl, total, BFunctab{});
+            batch_launch(bl, total, BFunctabEnd{meta});
+            break;
+        case BatchStage::Gen:
+            batch_launch(bl, total, BGenProp{});
+            batch_launch(bl, total, BGenClaim{});
+            batch_launch(bl, total, BGenWrite{});
+            break;
+        case BatchStage::OptMark: batch_launch(bl, total, BOptMark{}); break;
+        case BatchStage::OptFinal: batch_launch(bl, total, BOptFinal{}); break;
+        case BatchStage::InitLifetime: batch_launch(bl, total, BInitLifetime{}); break;
+        case BatchStage::Cross: batch_launch(bl, total, BCross{}); break;
+        case BatchStage::Spill: batch_launch(bl, total, BSpill{}); break;
+        case BatchStage::Scatter: batch_launch(bl, total, BScatter{}); break;
+        case BatchStage::RaFunctab:
+            batch_launch(bl, total, BRaFunctab{});
+            batch_launch(bl, total, BRaFrame{});
+            break;
+        case BatchStage::FjEmit: batch_launch(bl, total, BFjEmit{}); break;
+        case BatchStage::FjFunctab: batch_launch(bl, total, BFjFunctab{}); break;
+    }
+}
+
+void batch_sort_keys(const BatchLaunch& bl, uint32_t total, unsigned long long* a, const uint64_t* aoff, bool out) {
+    if (out) batch_launch(bl, total, BSortOut{a, aoff});
+    else batch_launch(bl, total, BSortInit{a, aoff});
+}
+
+void batch_sweep(const BatchLaunch& bl, uint32_t total, uint32_t* changed) {
+    if (total == 0) return;
+    g_launches++;
+    k_batch_sweep<<<std::min<uint32_t>(total, 152u * 16u), kThreads, 0, bl.s>>>(bl.progs, bl.off, bl.B, total, changed);
+}
+
+void batch_scan(BatchScan which, const BatchLaunch& bl, uint32_t tiles, const ScanScratch& sc, uint32_t* meta) {
+    if (tiles == 0) return;
+    cudaMemsetAsync(sc.status, 0, sizeof(unsigned long long) * tiles, bl.s);
+    cudaMemsetAsync(sc.counter, 0, sizeof(uint32_t), bl.s);
+    g_launches++;
+    switch (which) {
+        case BatchScan::Count: k_bscan<<<tiles, kScanThreads, 0, bl.s>>>(bl.progs, bl.off, bl.B, BScanCount{}, sc); break;
+        case BatchScan::Decl: k_bscan<<<tiles, kScanThreads, 0, bl.s>>>(bl.progs, bl.off, bl.B, BScanDecl{meta}, sc); break;
+        case BatchScan::RaCount: k_bscan<<<tiles, kScanThreads, 0, bl.s>>>(bl.progs, bl.off, bl.B, BScanRaCount{}, sc); break;
+        case BatchScan::FjSize: k_bscan<<<tiles, kScanThreads, 0, bl.s>>>(bl.progs, bl.off, bl.B, BScanFjSize{}, sc); break;
+    }
+}
+
+void batch_sizes(bool w3, const Prog* progs, const uint32_t* list, uint32_t count, uint32_t* meta, cudaStream_t s) {
+    if (count == 0) return;
+    g_launches++;
+    if (w3) k_batch_w3<<<grid_for(count), kThreads, 0, s>>>(progs, list, count, meta);
+    else k_batch_w2<<<grid_for(count), kThreads, 0, s>>>(progs, list, count, meta);
+}
+
+void batch_free_functions(const BatchLaunch& bl, uint32_t total) {
+    if (total == 0) return;
+    g_launches++;
+    k_batch_free<<<std::min<uint32_t>(total, 152u * 64u), kRaFreeThreads, 0, bl.s>>>(bl.progs, bl.off, bl.B, total);
+}
+
+uint32_t batch_free_tile() { return kRaFreeThreads; }
+
+cudaError_t batch_lane0(const Prog* progs, const uint32_t* list, uint32_t count, uint32_t max_g0, cudaStream_t s) {
+    if (count == 0) return cudaSuccess;
+    const uint32_t T = max_g0 <= 1024u ? std::max(64u, (max_g0 + 31u) & ~31u) : 1024u;
+    const uint32_t Q = (max_g0 + T - 1u) / T;
+    constexpr size_t kBudget = 160u * 1024u;
+    uint32_t K = 64;
+    const size_t fixed = sizeof(Ra2Shared) + 16ull * max_g0;
+    while (K > 1 && fixed + static_cast<size_t>(max_g0) * K * 8u > kBudget) K >>= 1;
+    const size_t smem = fixed + static_cast<size_t>(max_g0) * K * 8u + 16;
+    cudaError_t ce = cudaSuccess;
+    g_launches++;
+    switch (Q) {
+        case 1:
+            ce = cudaFuncSetAttribute(k_batch_lane0<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+            if (ce == cudaSuccess) k_batch_lane0<1><<<count, T, smem, s>>>(progs, list, K);
+            break;
+        case 2:
+            ce = cudaFuncSetAttribute(k_batch_lane0<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+            if (ce == cudaSuccess) k_batch_lane0<2><<<count, T, smem, s>>>(progs, list, K);
+            break;
+        case 3:
+        case 4:
+            ce = cudaFuncSetAttribute(k_batch_lane0<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+            if (ce == cudaSuccess) k_batch_lane0<4><<<count, T, smem, s>>>(progs, list, K);
+            break;
+        default:
+            ce = cudaFuncSetAttribute(k_batch_lane0<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+            if (ce == cudaSuccess) k_batch_lane0<8><<<count, T, smem, s>>>(progs, list, K);
+            break;
+    }
+    if (ce != cudaSuccess) return ce;
+    return cudaGetLastError();
+}
+
+void batch_serial(const Prog* progs, const uint32_t* list, uint32_t count, cudaStream_t s) {
+    if (count == 0) return;
+    g_launches++;
+    k_batch_serial<<<grid_for(count), kThreads, 0, s>>>(progs, list, count);
 }
 
 }  // namespace ptl

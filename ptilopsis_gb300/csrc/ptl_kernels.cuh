@@ -22,7 +22,8 @@ struct SortScratch {
     uint32_t* leaf;            // leaf ranges (first, last)
     uint32_t* heap;            // heap-sorted ranges
     uint32_t leaf_cap;
-    uint32_t* counters;        // [0] tiles [1] next segments [2] leaves [3] heaps
+    uint32_t* counters;        // [0] tiles [1] next segments [2] leaves [3] heaps [4] segments of
+                               // this round [5] capacity overflow
 };
 
 constexpr size_t kScanTileElems = 4096;  // elements per scan tile (ptl_kernels.cu)
@@ -55,5 +56,35 @@ void launch_regalloc_count_scan(const Prog& P, const ScanScratch& sc, cudaStream
 void launch_regalloc_emit(const Prog& P, cudaStream_t s);
 void launch_fixjumps_scan(const Prog& P, const ScanScratch& sc, cudaStream_t s);
 void launch_fixjumps_emit(const Prog& P, cudaStream_t s);
+
+// Introsort rounds over prepared segments (ss.seg[0], counters), then heaps and leaves.
+cudaError_t run_sort_rounds(const SortScratch& ss, uint32_t nseg0, uint32_t first_batch, uint32_t max_rounds,
+                            ErrorWord* err, cudaStream_t s, uint32_t* rounds_out);
+
+// ---- batched programs: per-program Prog views in device memory (progs[B]); off[B+1]
+// holds each program's first tile for the stage's element count.
+struct BatchLaunch {
+    const Prog* progs;
+    const uint32_t* off;
+    uint32_t B;
+    cudaStream_t s;
+};
+enum class BatchStage {
+    Validate, DepthSeen, Translate, Preprocess, Fix, Functab, Gen, OptMark, OptFinal, InitLifetime, Cross, Spill,
+    Scatter, RaFunctab, FjEmit, FjFunctab
+};
+enum class BatchScan { Count, Decl, RaCount, FjSize };
+uint32_t batch_tile();       // elements per tile of the element-wise stages
+uint32_t batch_scan_tile();  // elements per scan tile
+uint32_t batch_free_tile();  // independent functions per tile
+void batch_stage(BatchStage st, const BatchLaunch& bl, uint32_t total, uint32_t* meta, uint32_t* seen,
+                 const uint64_t* off64);
+void batch_sort_keys(const BatchLaunch& bl, uint32_t total, unsigned long long* a, const uint64_t* aoff, bool out);
+void batch_sweep(const BatchLaunch& bl, uint32_t total, uint32_t* changed);
+void batch_scan(BatchScan which, const BatchLaunch& bl, uint32_t tiles, const ScanScratch& sc, uint32_t* meta);
+void batch_sizes(bool w3, const Prog* progs, const uint32_t* list, uint32_t count, uint32_t* meta, cudaStream_t s);
+void batch_free_functions(const BatchLaunch& bl, uint32_t total);
+cudaError_t batch_lane0(const Prog* progs, const uint32_t* list, uint32_t count, uint32_t max_g0, cudaStream_t s);
+void batch_serial(const Prog* progs, const uint32_t* list, uint32_t count, cudaStream_t s);
 
 }  // namespace ptl

@@ -150,6 +150,22 @@ struct Prog {
     uint32_t* flags;      // [0] optimize changed
 };
 
+// ================================================================== input checks
+// The DepthTree contract (post-order, one root last, consistent depths, in-range types).
+PTL_HD bool st_input_bad(const Prog& P, uint32_t i) {
+    const uint32_t n = P.n;
+    bool bad = P.in_type[i] >= kNumPareasTypes || P.in_rtype[i] > 5;
+    const int32_t p = P.in_parent[i];
+    if (i == n - 1) {
+        bad |= p != -1 || P.in_depth[i] != 0;
+    } else {
+        bad |= p <= static_cast<int32_t>(i) || p >= static_cast<int32_t>(n) || P.in_child[i] < 0;
+        if (!bad) bad |= P.in_depth[i] != P.in_depth[p] + 1;
+    }
+    bad |= P.in_depth[i] < 0 || static_cast<uint32_t>(P.in_depth[i]) > P.max_depth;
+    return bad;
+}
+
 // ================================================================== preprocess
 // Constructor copy and Pareas -> rv type map: src/codegen/rv_generator.cpp:41-67.
 PTL_HD void st_translate(const Prog& P, uint32_t i) {

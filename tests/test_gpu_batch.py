@@ -99,3 +99,43 @@ def test_server_budget_admission(built_cuda):
         with pytest.raises(PtlError) as e:
             srv.submit(big)
         assert e.value.status == 4  # PTL_ADMISSION_DENIED
+
+
+def test_batch_program_failure_is_isolated(built_cuda):
+    """A malformed tree fails alone (INVALID_AST); the other programs of the batch are
+    still exact."""
+    from conftest import ast_to_tree
+    from ptilopsis_gb300.batch import BatchCompiler
+    trees = _programs(9, seed0=0x50544CE0)
+    bad = ast_to_tree(tree_to_ast(trees[4]))
+    bad.parent = bad.parent.copy()
+    bad.parent[3] = 1  # a parent before its child breaks post-order
+    trees[4] = bad
+    with BatchCompiler(workers=4) as b:
+        b.compile(trees, check=False)
+        assert b.status(4) == 1
+        for k, t in enumerate(trees):
+            if k == 4:
+                continue
+            assert b.status(k) == 0
+            w, tab = _alone(t)
+            _assert_same(b.result(k), w, tab, f"program {k}")
+
+
+def test_batch_fixtures_and_serial_path(built_cuda):
+    """The reference's fixtures in one batch, including the program whose functions share
+    symbols (serial register allocation), against the golden words."""
+    from conftest import ast_to_tree, load_fixture, manifest
+    from ptilopsis_gb300.batch import BatchCompiler
+    names = [f["name"] for f in manifest()["fixtures"]]
+    trees, golds = [], []
+    for nm in names:
+        ast, gold = load_fixture(nm)
+        trees.append(ast_to_tree(ast))
+        golds.append(gold)
+    with BatchCompiler(workers=4) as b:
+        b.compile(trees)
+        for k, nm in enumerate(names):
+            res = b.result(k)
+            np.testing.assert_array_equal(res.words, golds[k]["words"], err_msg=nm)
+            np.testing.assert_array_equal(res.table["starts"], golds[k]["fn_start"], err_msg=nm)
