@@ -1,25 +1,30 @@
-"""Benchmark: AST nodes/s of the GB300 code generator.
+"""Benchmark: AST nodes/s of the GB300 code generator, batched vs plain, bit-exact.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--config c1] [--impl gb300|reference]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--mode batched|single]
+                    [--programs P] [--config c1] [--impl gb300|reference]
 
-A step is one full compile (all seven stages) of one synthetic program.  The default
-workload is the large single program (config c1: ~4M nodes, 2,048 functions); the
-other configurations are parity-test cases.  Prints one JSON line (rank 0).
+Default (--mode batched): the batched workload, 4,096 seeded synthetic programs of
+1k..500k nodes (lognormal, ~285M nodes, 4..512 functions each).  A step compiles all of
+them through the batched pipeline (ptl_batch_compile: one launch per stage step for the
+whole batch).  Prints one JSON line (rank 0):
 
-  value       nodes/s with the tree already resident in HBM; device time of the
-              pipeline from CUDA events the library records on its own stream
-  e2e         the same through the public API with host buffers: host->device copy
-              of the six arrays, the compile, device->host copy of the words and the
-              function table, per step
-  roofline    the dominant kernel: algorithmic bytes per launch / its event-timed
-              duration, against the measured HBM copy bandwidth
-  cpu_baseline  the oracle's CPU restatement of the reference on the same program,
-              one thread, one compile
+  value       nodes/s with the trees resident in HBM: device time of the pipeline from the
+              CUDA events the library records on its stream (after the input copy, before
+              the output copy)
+  e2e         the same call timed on the host: gathering the host trees into pinned
+              memory, host->device, the pipeline, device->host of every program's words and
+              function table
+  plain       the plain pipeline (one program at a time, ptl_generator_*) on a sample of
+              the same programs; batched_over_plain = value / plain value
+  roofline    the dominant stage: algorithmic bytes / its event-timed duration, against
+              the measured HBM copy bandwidth
+  cpu_baseline  the oracle's CPU restatement on a bounded sample, on all host cores
 
---impl reference times the oracle restatement on the host cores, on the same workload
-(the reference itself is AVX2-only and cannot run on the aarch64 GPU hosts).
-Multi-GPU: every rank compiles its own replica (programs do not shard below the
-program level); value aggregates nodes over ranks, timed to the slowest rank.
+--mode single times one large program (config c1, ~4M nodes) per step instead.
+--impl reference times the oracle restatement on the host cores on a sample of the same
+workload (the reference itself is AVX2-only and cannot run on the aarch64 GPU hosts).
+Multi-GPU: every rank compiles its own batch (programs are independent, no collective on
+the data path); value aggregates nodes over ranks, timed to the slowest rank.
 """
 from __future__ import annotations
 
@@ -134,32 +139,196 @@ def cpu_baseline(tree, sample: str):
             "seconds": round(dt, 3), "words": int(len(res.words))}, res
 
 
+def to_ast(tree):
+    from oracle.refbind import Ast
+    return Ast(tree.type, tree.rtype, tree.parent, tree.depth, tree.child_idx, tree.data, tree.max_depth)
+
+
+def port_parallel(trees, threads):
+    """Oracle restatement over trees on `threads` host threads (the library call releases
+    the GIL); returns (nodes/s, seconds, outputs)."""
+    from concurrent.futures import ThreadPoolExecutor
+    from oracle import portbind
+    asts = [to_ast(t) for t in trees]
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(threads) as ex:
+        outs = list(ex.map(portbind.compile_ast, asts))
+    dt = time.perf_counter() - t0
+    return sum(t.n for t in trees) / dt, dt, outs
+
+
+def cpu_sample(trees, target_nodes):
+    """A bounded sample of the workload: indices of every k-th program until target_nodes."""
+    step = max(1, len(trees) // 256)
+    out, tot = [], 0
+    for k in range(0, len(trees), step):
+        out.append(k)
+        tot += trees[k].n
+        if tot >= target_nodes:
+            break
+    return out
+
+
+def make_workload(args, rank):
+    from concurrent.futures import ThreadPoolExecutor
+    from ptilopsis_gb300.synth import config_params, generate
+    base = rank * args.programs  # each rank its own programs
+    with ThreadPoolExecutor(min(32, os.cpu_count() or 8)) as ex:
+        return list(ex.map(lambda k: generate(config_params("c3", program=base + k)), range(args.programs)))
+
+
 def run_reference(args):
     rank, world, _ = env_rank()
     if rank != 0:
         return
     from ptilopsis_gb300 import build as b
-    from ptilopsis_gb300.synth import config_tree
     from oracle import portbind
     b.build_synth()
     portbind.build()
-    tree = config_tree(args.config, args.scale)
-    sample = f"one full compile of config {args.config} ({tree.n} nodes) per step, one thread"
+    threads = os.cpu_count() or 1
+    if args.mode == "single":
+        from ptilopsis_gb300.synth import config_tree
+        tree = config_tree(args.config, args.scale)
+        trees = [tree]
+        sample = f"one full compile of config {args.config} ({tree.n} nodes) per step, one thread"
+        threads = 1
+        workload = f"{args.config}: one synthetic program, {tree.n} nodes"
+    else:
+        all_trees = make_workload(args, 0)
+        trees = [all_trees[k] for k in cpu_sample(all_trees, 20_000_000)]
+        sample = (f"{len(trees)} of the {args.programs} batched-workload programs ({sum(t.n for t in trees)} nodes) "
+                  f"per step, {threads} threads")
+        workload = f"c3: {args.programs} synthetic programs, {sum(t.n for t in all_trees)} nodes (sampled)"
     for _ in range(args.warmup):
-        cpu_baseline(tree, sample)
+        port_parallel(trees, threads)
     times = []
     for _ in range(args.steps):
-        base, _ = cpu_baseline(tree, sample)
-        times.append(base["seconds"])
+        _, dt, _ = port_parallel(trees, threads)
+        times.append(dt)
     ms = 1000.0 * sum(times) / len(times)
-    value = tree.n / (ms / 1000.0)
+    value = sum(t.n for t in trees) / (ms / 1000.0)
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "u32", "data": "synthetic (seeded grammar)", "impl": "reference",
-            "config": {"workload": f"{args.config}: one synthetic program, {tree.n} nodes", "nodes": tree.n},
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "port", "sample": sample},
+            "config": {"workload": workload, "nodes_per_step": sum(t.n for t in trees)},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def run_batched(args):
+    import torch
+    rank, world, local = env_rank()
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    from ptilopsis_gb300 import RvGenerator, STAGES
+    from ptilopsis_gb300 import build as b
+    from ptilopsis_gb300.batch import BatchCompiler
+    from ptilopsis_gb300.codegen import kernel_launches
+    b.build_all()
+    trees = make_workload(args, rank)
+    nodes = sum(t.n for t in trees)
+    dev = torch.device("cuda", local)
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def max_over_ranks(x):
+        if dist is None:
+            return x
+        t = torch.tensor([x], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    bc = BatchCompiler(device=local, workers=min(32, os.cpu_count() or 8))
+    for _ in range(args.warmup):
+        bc.compile(trees)
+    barrier()
+    dev_ms, wall_ms, stage_sum = [], [], np.zeros(7)
+    launches0 = kernel_launches()
+    with ClockSampler(local) as clocks:
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            bc.compile(trees)
+            wall_ms.append(1000.0 * (time.perf_counter() - t0))
+            ns = np.array(bc.stage_ns(), dtype=np.float64)
+            stage_sum += ns
+            dev_ms.append(ns.sum() / 1e6)
+        barrier()
+    launches = (kernel_launches() - launches0) // args.steps
+    ms = max_over_ranks(float(np.mean(dev_ms)))
+    e2e_ms = max_over_ranks(float(np.mean(wall_ms)))
+    h2d, d2h = bc.copied_bytes()
+    value = world * nodes / (ms / 1000.0)
+    e2e = {"value": world * nodes / (e2e_ms / 1000.0), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+           "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_ms}
+
+    # per-program sizes for the algorithmic bytes
+    tot = {"n": 0, "W": 0, "W2": 0, "W3": 0}
+    for k in range(len(trees)):
+        for key, v in bc.sizes(k).items():
+            tot[key] += v
+    stage_ms = stage_sum / 1e6 / args.steps
+    dom = int(np.argmax(stage_ms[:6]))
+    name = STAGES[dom]
+    alg = STAGE_BYTES[name](tot["n"], tot["W"], tot["W2"], tot["W3"])
+    achieved = alg / (stage_ms[dom] / 1000.0) / 1e9
+    peak, peak_kind = peaks()
+    roofline = {"bound": "hbm", "kernel": f"{name} stage (all programs)", "achieved": achieved, "peak": peak,
+                "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind, "traffic": None,
+                "algorithmic_bytes_per_launch": int(alg),
+                "stage_ms": {s: round(float(v), 3) for s, v in zip(STAGES, stage_ms)}}
+
+    # the plain pipeline on a sample of the same programs, one at a time
+    sample = trees[:args.plain_sample]
+    sn = sum(t.n for t in sample)
+    gen = RvGenerator(sample[0], device=local)
+    gen.process()
+    plain_dev, plain_words = 0.0, []
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for t in sample:
+        gen.upload(t)
+        gen.process(profile=True)
+        plain_words.append(gen.get_instructions())
+        plain_dev += sum(gen.stage_ns()) / 1e9
+    plain_wall = time.perf_counter() - t0
+    gen.close()
+    plain = {"value": sn / plain_dev, "e2e_value": sn / plain_wall, "unit": UNIT, "programs": len(sample),
+             "nodes": sn, "sample": f"first {len(sample)} programs of the workload, one generator, one at a time"}
+    same_as_plain = all(np.array_equal(bc.words(k), plain_words[k]) for k in range(len(sample)))
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u32", "data": "synthetic (seeded grammar, no datasets)",
+            "config": {"workload": f"c3: {len(trees)} synthetic programs per GPU (1k..500k nodes, lognormal), "
+                                   f"{nodes} nodes, {tot['W3']} output words",
+                       "programs": len(trees), "nodes": nodes, "words": tot["W3"],
+                       "l2": "working set (~60 GB) > L2; no flush needed",
+                       "parallelism": f"replicas x{world} (each GPU its own batch)"},
+            "e2e": e2e, "plain": plain, "batched_over_plain": value / plain["value"],
+            "roofline": roofline, "gpu_launches": int(launches)}
+    if rank == 0:
+        line["clocks"] = clocks.summary()
+        line["bit_exact_vs_plain"] = bool(same_as_plain)
+        if not args.no_cpu_baseline:
+            threads = os.cpu_count() or 1
+            idx = cpu_sample(trees, args.cpu_nodes)
+            cs = [trees[k] for k in idx]
+            rate, dt, outs = port_parallel(cs, threads)
+            line["bit_exact_vs_oracle"] = bool(all(np.array_equal(bc.words(k), o.words) for k, o in zip(idx, outs)))
+            line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+                                    "sample": f"{len(cs)} programs ({sum(t.n for t in cs)} nodes) of the workload, "
+                                              f"{threads} threads", "seconds": round(dt, 3)}
+        print(json.dumps(line), flush=True)
+    bc.close()
+    if dist is not None:
+        dist.destroy_process_group()
 
 
 def run_gb300(args):
@@ -296,10 +465,16 @@ def main():
     ap.add_argument("--config", default="c1")
     ap.add_argument("--scale", type=float, default=1.0)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--mode", default="batched", choices=["batched", "single"])
+    ap.add_argument("--programs", type=int, default=4096)
+    ap.add_argument("--plain-sample", type=int, default=64)
+    ap.add_argument("--cpu-nodes", type=int, default=30_000_000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.mode == "batched":
+        run_batched(args)
     else:
         run_gb300(args)
 

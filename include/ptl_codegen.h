@@ -157,6 +157,8 @@ ptl_status ptl_batch_words(const ptl_batch* batch, size_t k, const uint32_t** wo
 ptl_status ptl_batch_function_table(const ptl_batch* batch, size_t k, const uint32_t** starts,
                                     const uint32_t** ends, const uint32_t** sizes, const uint32_t** ids,
                                     size_t* count);
+/* Program k's node count and its word counts after isn_gen, regalloc and fix_jumps. */
+ptl_status ptl_batch_sizes(const ptl_batch* batch, size_t k, uint64_t sizes[4]);
 /* Wall time of the last ptl_batch_compile, in ns. */
 uint64_t ptl_batch_elapsed_ns(const ptl_batch* batch);
 /* Device time per stage of the last compile (ptl_generator_stage_ns's seven columns). */

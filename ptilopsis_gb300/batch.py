@@ -32,6 +32,7 @@ def _bind(L):
     L.ptl_batch_elapsed_ns.argtypes = [vp]
     L.ptl_batch_elapsed_ns.restype = u64
     L.ptl_batch_stage_ns.argtypes = [vp, ctypes.POINTER(u64)]
+    L.ptl_batch_sizes.argtypes = [vp, sz, ctypes.POINTER(u64)]
     L.ptl_batch_copied_bytes.argtypes = [vp, ctypes.POINTER(u64), ctypes.POINTER(u64)]
     L.ptl_batch_last_error.argtypes = [vp]
     L.ptl_batch_last_error.restype = ctypes.c_char_p
@@ -50,7 +51,7 @@ def _bind(L):
     L.ptl_clock_ns.argtypes = []
     L.ptl_clock_ns.restype = u64
     for fn in ("ptl_batch_create", "ptl_batch_compile", "ptl_batch_status", "ptl_batch_words", "ptl_batch_stage_ns",
-               "ptl_batch_copied_bytes",
+               "ptl_batch_copied_bytes", "ptl_batch_sizes",
                "ptl_batch_function_table", "ptl_server_create", "ptl_server_submit", "ptl_server_poll",
                "ptl_server_result", "ptl_server_times", "ptl_server_release", "ptl_server_stats"):
         getattr(L, fn).restype = ctypes.c_int
@@ -106,6 +107,14 @@ class BatchCompiler:
         ns = (ctypes.c_uint64 * 7)()
         self._lib.ptl_batch_stage_ns(self._h, ns)
         return list(ns)
+
+    def sizes(self, k: int) -> dict:
+        """Program k's nodes and word counts after isn_gen, regalloc and fix_jumps."""
+        v = (ctypes.c_uint64 * 4)()
+        st = self._lib.ptl_batch_sizes(self._h, k, v)
+        if st != 0:
+            raise PtlError(st, f"ptl_batch_sizes({k})")
+        return {"n": int(v[0]), "W": int(v[1]), "W2": int(v[2]), "W3": int(v[3])}
 
     def copied_bytes(self) -> tuple:
         a, b = ctypes.c_uint64(), ctypes.c_uint64()

@@ -131,6 +131,17 @@ extern "C" ptl_status ptl_batch_function_table(const ptl_batch* b, size_t k, con
     return PTL_OK;
 }
 
+extern "C" ptl_status ptl_batch_sizes(const ptl_batch* b, size_t k, uint64_t sizes[4]) {
+    if (!b || !sizes || k >= b->results.size()) return PTL_BAD_ARGUMENT;
+    const ptl::BatchResult& r = b->results[k];
+    if (r.status != PTL_OK) return r.status;
+    sizes[0] = r.nodes;
+    sizes[1] = r.words_gen;
+    sizes[2] = r.words_ra;
+    sizes[3] = r.count;
+    return PTL_OK;
+}
+
 extern "C" uint64_t ptl_batch_elapsed_ns(const ptl_batch* b) { return b ? b->last_ns : 0; }
 
 extern "C" ptl_status ptl_batch_stage_ns(const ptl_batch* b, uint64_t ns[7]) {

@@ -270,7 +270,6 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
     }
     for (auto& e : ev)
         if (!e) BP_CU(cudaEventCreate(&e));
-    BP_CU(cudaEventRecord(ev[0], s));
 
     // ---- small per-program state and the pinned small area
     constexpr int kTables = 20, kLists = 4;
@@ -347,6 +346,7 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
         BP_CU(cudaMemcpyAsync(in_child.p, hch, 4 * o, cudaMemcpyHostToDevice, s));
         BP_CU(cudaMemcpyAsync(in_data.p, hdat, 4 * o, cudaMemcpyHostToDevice, s));
         h2d += 18 * o;
+        BP_CU(cudaEventRecord(ev[0], s));  // stage times start with the inputs on the device
 
         // node, register and depth families
         Layout Ln, Lr, Ls;
@@ -755,6 +755,9 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
             r.sizes = hf + 2 * Lf.total + e;
             r.ids = hf + 3 * Lf.total + e;
             r.functions = F[p];
+            r.nodes = n[p];
+            r.words_gen = W[p];
+            r.words_ra = W2[p];
         }
         float ms = 0;
         for (int k = 0; k < 6; ++k) {

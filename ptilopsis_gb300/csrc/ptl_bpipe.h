@@ -18,6 +18,7 @@ struct BatchResult {
     size_t count = 0;
     const uint32_t *starts = nullptr, *ends = nullptr, *sizes = nullptr, *ids = nullptr;
     size_t functions = 0;
+    uint64_t nodes = 0, words_gen = 0, words_ra = 0;  // n, words after isn_gen and regalloc
 };
 
 class BatchPipeline {
