@@ -129,7 +129,8 @@ public:
     DBuf trig_min, trig_max;
     DBuf ni, nrd, nr1, nr2, njt, fsz, joffs, out;
     DBuf errw, flags, meta, progs, tabs, lists, changed, sort_err, seen_off, a_off;
-    DBuf sa, sapos, sbpos, seg0, seg1, tile_seg, tile_l, tile_r, leaf, heap, counters, scan_status, scan_counter;
+    DBuf sa, sapos, sbpos, seg0, seg1, tile_seg, tile_l, tile_r, leaf, heap, counters, scan_status, scan_counter,
+        sort_local;
     PBuf h_in, h_out, h_fn, h_small;
 
     std::vector<uint8_t> active;
@@ -152,7 +153,7 @@ public:
                 &symswp, &stamp, &spill, &roffs, &owner, &used, &smark, &defpos, &trig_min, &trig_max, &ni, &nrd,
                 &nr1, &nr2, &njt, &fsz, &joffs, &out, &errw, &flags, &meta, &progs, &tabs, &lists, &changed,
                 &sort_err, &seen_off, &a_off, &sa, &sapos, &sbpos, &seg0, &seg1, &tile_seg, &tile_l, &tile_r,
-                &leaf, &heap, &counters, &scan_status, &scan_counter};
+                &leaf, &heap, &counters, &scan_status, &scan_counter, &sort_local};
     }
 
     ptl_status cuda_fail(cudaError_t e, const char* what) {
@@ -550,6 +551,7 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
         BP_CU(leaf.ensure(2 * leaf_cap * 4));
         BP_CU(heap.ensure(2 * leaf_cap * 4));
         BP_CU(counters.ensure(64));
+        BP_CU(sort_local.ensure(3 * seg_cap * 4));
         BP_CU(a_off.ensure(B * 8));
         uint64_t* up_aoff = reinterpret_cast<uint64_t*>(h_small.at<uint8_t>(small_up_off + B * 8));
         std::copy(aoff.begin(), aoff.end(), up_aoff);
@@ -569,6 +571,7 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
         ss.heap = heap.at<uint32_t>();
         ss.leaf_cap = static_cast<uint32_t>(leaf_cap);
         ss.counters = counters.at<uint32_t>();
+        ss.local = sort_local.at<uint32_t>();
         const uint32_t t_n2 = tiles(4, n, batch_tile());
         batch_sort_keys(bl(4), t_n2, sa.at<unsigned long long>(), a_off.at<uint64_t>(), false);
         BP_CU(cudaMemsetAsync(counters.p, 0, 64, s));
@@ -586,7 +589,7 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
             BP_CU(cudaMemcpyAsync(counters.at<uint32_t>(2), up_nl, 4, cudaMemcpyHostToDevice, s));
         }
         uint32_t rounds = 0;
-        BP_CU(run_sort_rounds(ss, static_cast<uint32_t>(segs.size()), min_lg > 4 ? min_lg - 4 : 1, 2 * max_lg + 4,
+        BP_CU(run_sort_rounds(ss, static_cast<uint32_t>(segs.size()), min_lg > 9 ? min_lg - 9 : 1, 2 * max_lg + 4,
                               sort_err.at<ErrorWord>(), s, &rounds));
         batch_sort_keys(bl(4), t_n2, sa.at<unsigned long long>(), a_off.at<uint64_t>(), true);
         batch_stage(BatchStage::Gen, bl(4), t_n2, nullptr, nullptr, nullptr);

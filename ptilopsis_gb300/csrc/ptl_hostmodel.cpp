@@ -6,6 +6,7 @@
 // oracle so the GPU algorithm is checked before it runs on a GPU.  The library API
 // never calls it: without the CUDA library the package refuses to compile anything.
 #include <algorithm>
+#include <array>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -96,8 +97,10 @@ struct Model {
         } else if (n > 1) {
             leaves.push_back({0, n});
         }
+        std::vector<std::array<uint32_t, 3>> locals;
         auto emit = [&](uint32_t first, uint32_t last, uint32_t dl) {
             if (last - first <= kSortThreshold) { if (last - first > 1) leaves.push_back({first, last}); return; }
+            if (dl > 0 && last - first <= kSortLocal) { locals.push_back({first, last, dl}); return; }
             if (dl == 0) { heaps.push_back({first, last}); return; }
             SortSeg c{}; c.first = first; c.last = last; c.dl = dl;
             next.push_back(c);
@@ -127,6 +130,13 @@ struct Model {
         }
         for (auto& h : heaps) heap_sort_range(a.data() + h.first, h.second - h.first);
         for (auto& l : leaves) leaf_sort(a.data(), l.first, l.second);
+        for (auto& r : locals) {  // one thread per range on the device, in a strided buffer
+            std::vector<unsigned long long> buf(static_cast<size_t>(r[1] - r[0]) * 3);
+            const Strided sb{buf.data() + 1, 3};
+            for (uint32_t i = 0; i < r[1] - r[0]; ++i) sb[i] = a[r[0] + i];
+            local_introsort(sb, 0u, r[1] - r[0], r[2]);
+            for (uint32_t i = 0; i < r[1] - r[0]; ++i) a[r[0] + i] = sb[i];
+        }
         for (uint32_t p = 0; p < n; ++p) pos.p[sidx(a[p])] = p;
     }
 

@@ -371,6 +371,12 @@ __device__ void sort_emit(SortScratch ss, SortSeg* next, uint32_t first, uint32_
         }
         return;
     }
+    if (dl > 0 && last - first <= kSortLocal) {  // finishes in one thread after the rounds
+        const uint32_t k = atomicAdd(&ss.counters[6], 1u);
+        if (k < ss.seg_cap) { ss.local[3 * k] = first; ss.local[3 * k + 1] = last; ss.local[3 * k + 2] = dl; }
+        else ss.counters[5] = 1;
+        return;
+    }
     if (dl == 0) {
         const uint32_t k = atomicAdd(&ss.counters[3], 1u);
         if (k < ss.leaf_cap) { ss.heap[2 * k] = first; ss.heap[2 * k + 1] = last; }
@@ -426,6 +432,21 @@ __global__ void __launch_bounds__(kThreads) k_sort_swap(SortScratch ss, const So
 
 __global__ void k_sort_leaves(SortScratch ss, uint32_t count) {
     PTL_FOR(k, count) leaf_sort(ss.a, ss.leaf[2 * k], ss.leaf[2 * k + 1]);
+}
+// One small range per thread, staged in shared memory (element k of thread t at
+// k * blockDim + t, so that the threads of a warp use different banks).
+constexpr int kSortLocalThreads = 64;
+__global__ void __launch_bounds__(kSortLocalThreads) k_sort_local(SortScratch ss, uint32_t count) {
+    extern __shared__ unsigned long long sbuf[];
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= count) return;
+    const uint32_t first = ss.local[3 * k], last = ss.local[3 * k + 1], dl = ss.local[3 * k + 2];
+    const uint32_t len = last - first;
+    if (len > kSortLocal) return;  // emitted only up to kSortLocal
+    const Strided buf{sbuf + threadIdx.x, blockDim.x};
+    for (uint32_t i = 0; i < len; ++i) buf[i] = ss.a[first + i];
+    local_introsort(buf, 0u, len, dl);
+    for (uint32_t i = 0; i < len; ++i) ss.a[first + i] = buf[i];
 }
 __global__ void k_sort_heaps(SortScratch ss, uint32_t count) {
     PTL_FOR(k, count) heap_sort_range(ss.a + ss.heap[2 * k], ss.heap[2 * k + 1] - ss.heap[2 * k]);
@@ -757,13 +778,20 @@ cudaError_t run_sort_rounds(const SortScratch& ss, uint32_t nseg0, uint32_t firs
         if (nseg > 0 && rounds > max_rounds) return cudaErrorLaunchFailure;
         batch = 4;
     }
-    uint32_t lh[2] = {0, 0};
+    uint32_t lh[5] = {0, 0, 0, 0, 0};  // leaves, heaps, -, -, small ranges
     cudaMemcpyAsync(lh, ss.counters + 2, sizeof(lh), cudaMemcpyDeviceToHost, s);
     cudaError_t e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return e;
-    if (lh[0] > ss.leaf_cap || lh[1] > ss.leaf_cap) return cudaErrorMemoryAllocation;
+    if (lh[0] > ss.leaf_cap || lh[1] > ss.leaf_cap || lh[4] > ss.seg_cap) return cudaErrorMemoryAllocation;
     if (lh[1]) { g_launches++; k_sort_heaps<<<grid_for(lh[1]), kThreads, 0, s>>>(ss, lh[1]); }
     if (lh[0]) { g_launches++; k_sort_leaves<<<grid_for(lh[0]), kThreads, 0, s>>>(ss, lh[0]); }
+    if (lh[4]) {
+        const size_t smem = static_cast<size_t>(kSortLocalThreads) * kSortLocal * sizeof(unsigned long long);
+        e = cudaFuncSetAttribute(k_sort_local, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+        if (e != cudaSuccess) return e;
+        g_launches++;
+        k_sort_local<<<(lh[4] + kSortLocalThreads - 1) / kSortLocalThreads, kSortLocalThreads, smem, s>>>(ss, lh[4]);
+    }
     if (rounds_out) *rounds_out = rounds;
     return cudaGetLastError();
 }
@@ -772,7 +800,7 @@ cudaError_t run_depth_sort(const Prog& P, const SortScratch& ss, cudaStream_t s,
     const uint32_t n = P.n;
     g_launches++;
     k_sort_init<<<grid_for(n), kThreads, 0, s>>>(P, ss);
-    cudaMemsetAsync(ss.counters, 0, sizeof(uint32_t) * 6, s);
+    cudaMemsetAsync(ss.counters, 0, sizeof(uint32_t) * 8, s);
     uint32_t nseg = 0;
     if (n > kSortThreshold) {
         SortSeg g{};
@@ -788,7 +816,7 @@ cudaError_t run_depth_sort(const Prog& P, const SortScratch& ss, cudaStream_t s,
         cudaMemcpyAsync(ss.counters + 2, &one, sizeof(one), cudaMemcpyHostToDevice, s);
     }
     const uint32_t lg = floor_log2(std::max<uint32_t>(n, 2u));
-    const cudaError_t e = run_sort_rounds(ss, nseg, lg > 4u ? lg - 4u : 1u, 2u * lg + 4u, P.err, s, rounds_out);
+    const cudaError_t e = run_sort_rounds(ss, nseg, lg > 9u ? lg - 9u : 1u, 2u * lg + 4u, P.err, s, rounds_out);
     if (e != cudaSuccess) return e;
     g_launches++;
     k_sort_out<<<grid_for(n), kThreads, 0, s>>>(P, ss);

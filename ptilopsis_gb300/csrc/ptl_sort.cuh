@@ -44,14 +44,16 @@ PTL_HD uint32_t floor_log2(uint32_t n) {
     return r;
 }
 
-PTL_HD void sswap(unsigned long long* a, uint32_t i, uint32_t j) {
+template <class Arr>
+PTL_HD void sswap(Arr a, uint32_t i, uint32_t j) {
     const unsigned long long t = a[i];
     a[i] = a[j];
     a[j] = t;
 }
 
 // std::__move_median_to_first(result = first, a = first+1, b = mid, c = last-1)
-PTL_HD void median_to_first(unsigned long long* a, uint32_t first, uint32_t last) {
+template <class Arr>
+PTL_HD void median_to_first(Arr a, uint32_t first, uint32_t last) {
     const uint32_t ia = first + 1, ib = first + (last - first) / 2, ic = last - 1;
     const int32_t ka = skey(a[ia]), kb = skey(a[ib]), kc = skey(a[ic]);
     uint32_t pick;
@@ -90,7 +92,8 @@ PTL_HD uint32_t partition_cut(const uint32_t* apos, const uint32_t* bpos, uint32
 }
 
 // libstdc++ __adjust_heap / __push_heap / make_heap / sort_heap on a[first, first+len).
-PTL_HD void heap_push(unsigned long long* a, int64_t hole, int64_t top, unsigned long long v) {
+template <class Arr>
+PTL_HD void heap_push(Arr a, int64_t hole, int64_t top, unsigned long long v) {
     int64_t parent = (hole - 1) / 2;
     while (hole > top && skey(a[parent]) < skey(v)) {
         a[hole] = a[parent];
@@ -100,7 +103,8 @@ PTL_HD void heap_push(unsigned long long* a, int64_t hole, int64_t top, unsigned
     a[hole] = v;
 }
 
-PTL_HD void heap_adjust(unsigned long long* a, int64_t hole, int64_t len, unsigned long long v) {
+template <class Arr>
+PTL_HD void heap_adjust(Arr a, int64_t hole, int64_t len, unsigned long long v) {
     const int64_t top = hole;
     int64_t second = hole;
     while (second < (len - 1) / 2) {
@@ -117,7 +121,8 @@ PTL_HD void heap_adjust(unsigned long long* a, int64_t hole, int64_t len, unsign
     heap_push(a, hole, top, v);
 }
 
-PTL_HD void heap_sort_range(unsigned long long* base, uint32_t len) {
+template <class Arr>
+PTL_HD void heap_sort_range(Arr base, uint32_t len) {
     if (len < 2) return;
     const int64_t n = len;
     for (int64_t parent = (n - 2) / 2;; --parent) {
@@ -133,7 +138,8 @@ PTL_HD void heap_sort_range(unsigned long long* base, uint32_t len) {
 }
 
 // Stable insertion sort by key (what the final insertion sort does to one small range).
-PTL_HD void leaf_sort(unsigned long long* a, uint32_t first, uint32_t last) {
+template <class Arr>
+PTL_HD void leaf_sort(Arr a, uint32_t first, uint32_t last) {
     for (uint32_t i = first + 1; i < last; ++i) {
         const unsigned long long v = a[i];
         uint32_t j = i;
@@ -142,6 +148,73 @@ PTL_HD void leaf_sort(unsigned long long* a, uint32_t first, uint32_t last) {
             --j;
         }
         a[j] = v;
+    }
+}
+
+// ---- small ranges in one thread
+// Ranges of at most kSortLocal elements with depth budget left finish in one thread: the
+// same steps as the rounds above, taken sequentially (they touch only their own range).
+constexpr uint32_t kSortLocal = 256;
+
+// An array view with a stride (element i at base[i * stride]).
+struct Strided {
+    unsigned long long* base;
+    uint32_t stride;
+    PTL_HD unsigned long long& operator[](int64_t i) const { return base[static_cast<uint64_t>(i) * stride]; }
+    PTL_HD Strided operator+(uint32_t k) const { return Strided{base + static_cast<uint64_t>(k) * stride, stride}; }
+};
+
+// libstdc++ __unguarded_partition of [first+1, last) around the key at first; returns
+// the cut.  The median move leaves an L-stop and an R-stop in range, so the scans stop
+// inside it; the bounds only keep a broken invariant in range.
+template <class Arr>
+PTL_HD uint32_t seq_partition(Arr a, uint32_t first, uint32_t last) {
+    const int32_t pivot = skey(a[first]);
+    uint32_t lo = first + 1, hi = last;
+    for (;;) {
+        while (lo < last && skey(a[lo]) < pivot) ++lo;
+        --hi;
+        while (hi > first && pivot < skey(a[hi])) --hi;
+        if (!(lo < hi)) return lo;
+        sswap(a, lo, hi);
+        ++lo;
+    }
+}
+
+// The introsort loop on [first, last) with depth budget dl, leaves and heap-sorted
+// ranges included (one thread).
+template <class Arr>
+PTL_HD void local_introsort(Arr a, uint32_t first, uint32_t last, uint32_t dl) {
+    uint32_t st_f[64], st_l[64], st_d[64];  // at most one pending range per depth level
+    int sp = 0;
+    st_f[0] = first;
+    st_l[0] = last;
+    st_d[0] = dl;
+    sp = 1;
+    while (sp > 0) {
+        --sp;
+        uint32_t f = st_f[sp], l = st_l[sp], d = st_d[sp];
+        for (;;) {
+            const uint32_t len = l - f;
+            if (len <= kSortThreshold) {
+                if (len > 1) leaf_sort(a, f, l);
+                break;
+            }
+            if (d == 0) {
+                heap_sort_range(a + f, len);
+                break;
+            }
+            median_to_first(a, f, l);
+            const uint32_t cut = seq_partition(a, f, l);
+            --d;
+            if (sp < 64) {
+                st_f[sp] = cut;
+                st_l[sp] = l;
+                st_d[sp] = d;
+                ++sp;
+            }
+            l = cut;
+        }
     }
 }
 
