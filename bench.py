@@ -216,6 +216,63 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def run_serving(device, args):
+    """Open-loop Poisson arrivals of compile requests (80% 1k..10k nodes, 20% lognormal in
+    100k..2M) at each rate; latency = completion - scheduled arrival, on the server's
+    clock.  The submitter is one Python thread: a rate it cannot keep up with shows as a
+    lower achieved rate (and as latency, since arrivals are scheduled)."""
+    from concurrent.futures import ThreadPoolExecutor
+    from ptilopsis_gb300 import RvGenerator
+    from ptilopsis_gb300.batch import CompileServer, clock_ns
+    from ptilopsis_gb300.synth import config_params, generate
+    n_req = args.serve_requests
+    with ThreadPoolExecutor(min(32, os.cpu_count() or 8)) as ex:
+        reqs = list(ex.map(lambda k: generate(config_params("c4", program=k)), range(n_req)))
+    rng = np.random.default_rng(0x50544C04)
+    out = {"slots": args.serve_slots, "memory_budget_gb": 120, "requests": n_req,
+           "request_nodes_mean": float(np.mean([t.n for t in reqs])), "rates": []}
+    with CompileServer(device=device, slots=args.serve_slots, memory_budget=120 << 30) as srv:
+        for t in [srv.submit(r) for r in reqs[:8]]:  # warm-up: arenas and code paths
+            srv.result(t)
+            srv.release(t)
+        for rate in args.serve_rates:
+            gaps = rng.exponential(1.0 / rate, n_req)
+            sched = np.cumsum(gaps)
+            t0 = clock_ns() + 2_000_000
+            tickets = []
+            for k, tr in enumerate(reqs):
+                due = t0 + int(sched[k] * 1e9)
+                while clock_ns() < due:
+                    pass
+                tickets.append(srv.submit(tr))
+            submit_end = clock_ns()
+            lat, last = [], 0
+            for k, tk in enumerate(tickets):
+                srv.poll(tk, wait=True)
+                _, _, done = srv.times(tk)
+                lat.append((done - (t0 + int(sched[k] * 1e9))) / 1e6)
+                last = max(last, done)
+                srv.release(tk)
+            lat = np.array(lat)
+            span = (last - t0) / 1e9
+            out["rates"].append({"rate_per_s": rate, "achieved_rate_per_s": n_req / ((submit_end - t0) / 1e9),
+                                 "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                                 "max_ms": float(lat.max()),
+                                 "nodes_per_s": float(sum(t.n for t in reqs) / span)})
+        out["batches"] = srv.stats()["batches"]
+        # results in the mix equal compiling alone (a sample)
+        tickets = [srv.submit(r) for r in reqs[:16]]
+        mixed = [srv.result(t).words for t in tickets]
+    with RvGenerator(reqs[0], device=device) as g:
+        same = True
+        for k in range(16):
+            g.upload(reqs[k])
+            g.process()
+            same &= bool(np.array_equal(g.get_instructions(), mixed[k]))
+    out["bit_exact_vs_plain"] = same
+    return out
+
+
 def run_batched(args):
     import torch
     rank, world, local = env_rank()
@@ -302,6 +359,7 @@ def run_batched(args):
     plain = {"value": sn / plain_dev, "e2e_value": sn / plain_wall, "unit": UNIT, "programs": len(sample),
              "nodes": sn, "sample": f"first {len(sample)} programs of the workload, one generator, one at a time"}
     same_as_plain = all(np.array_equal(bc.words(k), plain_words[k]) for k in range(len(sample)))
+    oracle_words = {k: bc.words(k) for k in cpu_sample(trees, args.cpu_nodes)} if rank == 0 else {}
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -313,20 +371,22 @@ def run_batched(args):
                        "parallelism": f"replicas x{world} (each GPU its own batch)"},
             "e2e": e2e, "plain": plain, "batched_over_plain": value / plain["value"],
             "roofline": roofline, "gpu_launches": int(launches)}
+    bc.close()
     if rank == 0:
         line["clocks"] = clocks.summary()
         line["bit_exact_vs_plain"] = bool(same_as_plain)
+        if not args.no_serving:
+            line["serving"] = run_serving(local, args)
         if not args.no_cpu_baseline:
             threads = os.cpu_count() or 1
             idx = cpu_sample(trees, args.cpu_nodes)
             cs = [trees[k] for k in idx]
             rate, dt, outs = port_parallel(cs, threads)
-            line["bit_exact_vs_oracle"] = bool(all(np.array_equal(bc.words(k), o.words) for k, o in zip(idx, outs)))
+            line["bit_exact_vs_oracle"] = bool(all(np.array_equal(oracle_words[k], o.words) for k, o in zip(idx, outs)))
             line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
                                     "sample": f"{len(cs)} programs ({sum(t.n for t in cs)} nodes) of the workload, "
                                               f"{threads} threads", "seconds": round(dt, 3)}
         print(json.dumps(line), flush=True)
-    bc.close()
     if dist is not None:
         dist.destroy_process_group()
 
@@ -470,6 +530,10 @@ def main():
     ap.add_argument("--plain-sample", type=int, default=64)
     ap.add_argument("--cpu-nodes", type=int, default=30_000_000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--serve-requests", type=int, default=1000)
+    ap.add_argument("--serve-slots", type=int, default=2)
+    ap.add_argument("--serve-rates", type=float, nargs="+", default=[1000.0, 10000.0, 50000.0])
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

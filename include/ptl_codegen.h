@@ -169,11 +169,13 @@ ptl_status ptl_batch_copied_bytes(const ptl_batch* batch, uint64_t* h2d, uint64_
 const char* ptl_batch_last_error(const ptl_batch* batch);
 void ptl_batch_destroy(ptl_batch* batch);
 
-/* ---- Compile server.  No counterpart in the reference.  `slots` worker threads, each
- * with a resident generator, take queued requests in arrival order as soon as a slot is
- * free and the request's device-memory estimate fits in what is left of memory_budget
- * (a later request that fits may pass one that does not); compiles of different slots
- * overlap on the GPU.  Results are identical to compiling each tree alone. */
+/* ---- Compile server.  No counterpart in the reference.  Continuous batching over
+ * `slots` lanes (1..16), each a batched pipeline with its own stream and resident arenas:
+ * a free lane takes every queued request, in arrival order, whose device-memory estimate
+ * fits in what is left of memory_budget (a later request that fits may pass one that
+ * does not; at most 64M nodes per batch) and compiles them together, while requests that
+ * arrive meanwhile go to the next free lane, so their work overlaps on the GPU.  Results
+ * are identical to compiling each tree alone. */
 typedef struct ptl_server ptl_server;
 ptl_status ptl_server_create(int device, int slots, uint64_t memory_budget, ptl_server** out);
 /* Copies a host tree into a request and queues it; PTL_ADMISSION_DENIED when the request
@@ -188,8 +190,9 @@ ptl_status ptl_server_result(ptl_server* server, uint64_t ticket, const uint32_t
 /* Submit, start and completion times of a finished request (ptl_clock_ns clock). */
 ptl_status ptl_server_times(ptl_server* server, uint64_t ticket, uint64_t times[3]);
 ptl_status ptl_server_release(ptl_server* server, uint64_t ticket);
-/* stats[0..3]: requests completed, nodes compiled, requests queued, admitted bytes in flight. */
-ptl_status ptl_server_stats(ptl_server* server, uint64_t stats[4]);
+/* stats[0..4]: requests completed, nodes compiled, requests queued, admitted bytes in
+ * flight, batches compiled. */
+ptl_status ptl_server_stats(ptl_server* server, uint64_t stats[5]);
 /* Destroys the server after the compiles in flight; queued requests are dropped. */
 void ptl_server_destroy(ptl_server* server);
 /* The monotonic clock of the server's times, in ns. */

@@ -161,10 +161,10 @@ class BatchCompiler:
 
 
 class CompileServer:
-    """Continuous-batching compile server: `slots` concurrent compiles, admission against a
-    device-memory budget (bytes)."""
+    """Continuous-batching compile server: `slots` batched-pipeline lanes, admission against
+    a device-memory budget (bytes)."""
 
-    def __init__(self, device: int = 0, slots: int = 8, memory_budget: int = 120 << 30):
+    def __init__(self, device: int = 0, slots: int = 2, memory_budget: int = 120 << 30):
         self._lib = _bind(lib())
         self._h = ctypes.c_void_p()
         st = self._lib.ptl_server_create(device, slots, memory_budget, ctypes.byref(self._h))
@@ -211,9 +211,10 @@ class CompileServer:
         self._lib.ptl_server_release(self._h, ticket)
 
     def stats(self) -> dict:
-        s = (ctypes.c_uint64 * 4)()
+        s = (ctypes.c_uint64 * 5)()
         self._lib.ptl_server_stats(self._h, s)
-        return {"completed": int(s[0]), "nodes": int(s[1]), "queued": int(s[2]), "bytes_in_flight": int(s[3])}
+        return {"completed": int(s[0]), "nodes": int(s[1]), "queued": int(s[2]), "bytes_in_flight": int(s[3]),
+                "batches": int(s[4])}
 
     def close(self) -> None:
         if self._h:

@@ -6,7 +6,7 @@
 // (one launch per stage step for the whole batch).  The server keeps a pool of worker
 // threads, each owning one generator: its device arena stays resident and grows to the
 // largest program it has compiled, and its stream lets the compiles of different workers
-// overlap on the GPU.
+// overlap on the GPU.  The server batches queued requests through batched pipelines.
 #include <algorithm>
 #include <atomic>
 #include <chrono>
@@ -33,35 +33,11 @@ uint64_t now_ns() {
             .count());
 }
 
-// One compiled program, copied out of the generator that made it.
+// One compiled program, copied out of the pipeline that made it.
 struct Result {
     ptl_status status = PTL_OK;
     std::vector<uint32_t> words, starts, ends, sizes, ids;
 };
-
-// Compiles tree on gen (created on first use) and copies the output into r.
-void compile_into(ptl_generator*& gen, int device, const ptl_ast_view& tree, Result& r) {
-    ptl_status st = gen ? ptl_generator_upload(gen, &tree) : ptl_generator_create(&tree, device, &gen);
-    if (st == PTL_OK) st = ptl_generator_process(gen, 0);
-    if (st == PTL_OK) {
-        const uint32_t* w = nullptr;
-        size_t n = 0;
-        st = ptl_generator_instructions(gen, &w, &n);
-        if (st == PTL_OK) r.words.assign(w, w + n);
-    }
-    if (st == PTL_OK) {
-        const uint32_t *s = nullptr, *e = nullptr, *z = nullptr, *id = nullptr;
-        size_t f = 0;
-        st = ptl_generator_function_table(gen, &s, &e, &z, &id, &f);
-        if (st == PTL_OK) {
-            r.starts.assign(s, s + f);
-            r.ends.assign(e, e + f);
-            r.sizes.assign(z, z + f);
-            r.ids.assign(id, id + f);
-        }
-    }
-    r.status = st;
-}
 
 // Device footprint of a compile, for admission: the generator's arrays for n nodes (about
 // 190 bytes per node with the word arrays at ~1.3 words per node and the scratch, plus
@@ -187,47 +163,80 @@ struct ptl_server {
     int device = 0;
     uint64_t budget = 0;
     uint64_t in_use = 0;       // admission estimates of the compiles in flight
+    uint64_t max_batch_nodes = 64ull << 20;
     std::mutex mu;
     std::condition_variable cv_work, cv_done;
     std::deque<std::shared_ptr<Request>> queue;
     std::unordered_map<uint64_t, std::shared_ptr<Request>> all;
-    std::vector<std::thread> workers;
-    std::vector<ptl_generator*> gens;
+    std::vector<std::thread> lanes;
+    std::vector<std::unique_ptr<ptl::BatchPipeline>> pipes;
     uint64_t next_ticket = 1;
     bool stopping = false;
-    uint64_t completed = 0, nodes_done = 0, busy_ns = 0;
+    uint64_t completed = 0, nodes_done = 0, batches = 0;
 
+    // Continuous batching: a free lane takes every queued request, in arrival order, that
+    // fits the memory left in the budget and the batch cap (a later request that fits may
+    // pass one that does not), and compiles them through its batched pipeline while the
+    // other lanes keep taking the requests that arrive meanwhile.
     void run(size_t w) {
+        std::vector<std::shared_ptr<Request>> batch;
+        std::vector<ptl_ast_view> views;
+        std::vector<ptl::BatchResult> res;
         for (;;) {
-            std::shared_ptr<Request> req;
+            batch.clear();
             {
                 std::unique_lock<std::mutex> lk(mu);
                 for (;;) {
                     if (stopping) return;
-                    // first queued request that fits the free budget: requests that
-                    // arrive while others compile are admitted as memory frees up
-                    auto it = std::find_if(queue.begin(), queue.end(),
-                                           [&](const std::shared_ptr<Request>& r) { return in_use + r->bytes <= budget; });
-                    if (it != queue.end()) {
-                        req = *it;
-                        queue.erase(it);
-                        in_use += req->bytes;
-                        break;
+                    uint64_t nodes = 0;
+                    for (auto it = queue.begin(); it != queue.end();) {
+                        const std::shared_ptr<Request>& r = *it;
+                        if (in_use + r->bytes <= budget && (batch.empty() || nodes + r->n <= max_batch_nodes)) {
+                            in_use += r->bytes;
+                            nodes += r->n;
+                            batch.push_back(r);
+                            it = queue.erase(it);
+                        } else {
+                            ++it;
+                        }
                     }
+                    if (!batch.empty()) break;
                     cv_work.wait(lk);
                 }
             }
-            req->t_start = now_ns();
-            const ptl_ast_view v = req->view();
-            compile_into(gens[w], device, v, req->result);
+            const uint64_t t0 = now_ns();
+            views.clear();
+            for (auto& r : batch) {
+                r->t_start = t0;
+                views.push_back(r->view());
+            }
+            const ptl_status st = pipes[w]->compile(views.data(), views.size(), res);
+            for (size_t k = 0; k < batch.size(); ++k) {
+                Result& out = batch[k]->result;
+                if (st != PTL_OK) {
+                    out.status = st;
+                    continue;
+                }
+                const ptl::BatchResult& r = res[k];
+                out.status = r.status;
+                if (r.status != PTL_OK) continue;
+                out.words.assign(r.words, r.words + r.count);
+                out.starts.assign(r.starts, r.starts + r.functions);
+                out.ends.assign(r.ends, r.ends + r.functions);
+                out.sizes.assign(r.sizes, r.sizes + r.functions);
+                out.ids.assign(r.ids, r.ids + r.functions);
+            }
             {
                 std::lock_guard<std::mutex> lk(mu);
-                req->t_done = now_ns();
-                req->done = true;
-                in_use -= req->bytes;
-                ++completed;
-                nodes_done += req->n;
-                busy_ns += req->t_done - req->t_start;
+                const uint64_t t1 = now_ns();
+                for (auto& r : batch) {
+                    r->t_done = t1;
+                    r->done = true;
+                    in_use -= r->bytes;
+                    ++completed;
+                    nodes_done += r->n;
+                }
+                ++batches;
             }
             cv_done.notify_all();
             cv_work.notify_all();
@@ -236,13 +245,21 @@ struct ptl_server {
 };
 
 extern "C" ptl_status ptl_server_create(int device, int slots, uint64_t memory_budget, ptl_server** out) {
-    if (!out || slots < 1 || slots > 256 || memory_budget == 0) return PTL_BAD_ARGUMENT;
+    if (!out || slots < 1 || slots > 16 || memory_budget == 0) return PTL_BAD_ARGUMENT;
     ptl_server* s = new (std::nothrow) ptl_server;
     if (!s) return PTL_OOM;
     s->device = device;
     s->budget = memory_budget;
-    s->gens.assign(static_cast<size_t>(slots), nullptr);
-    for (int w = 0; w < slots; ++w) s->workers.emplace_back([s, w] { s->run(static_cast<size_t>(w)); });
+    for (int w = 0; w < slots; ++w) {
+        ptl_status st = PTL_OK;
+        s->pipes.emplace_back(ptl::BatchPipeline::create(device, 8, &st));
+        if (!s->pipes.back()) {
+            s->pipes.clear();
+            delete s;
+            return st;
+        }
+    }
+    for (int w = 0; w < slots; ++w) s->lanes.emplace_back([s, w] { s->run(static_cast<size_t>(w)); });
     *out = s;
     return PTL_OK;
 }
@@ -329,14 +346,15 @@ extern "C" ptl_status ptl_server_release(ptl_server* s, uint64_t ticket) {
     return PTL_OK;
 }
 
-// stats: completed, nodes compiled, queued, in flight (admission bytes)
-extern "C" ptl_status ptl_server_stats(ptl_server* s, uint64_t stats[4]) {
+// stats: completed, nodes compiled, queued, in flight (admission bytes), batches run
+extern "C" ptl_status ptl_server_stats(ptl_server* s, uint64_t stats[5]) {
     if (!s || !stats) return PTL_BAD_ARGUMENT;
     std::lock_guard<std::mutex> lk(s->mu);
     stats[0] = s->completed;
     stats[1] = s->nodes_done;
     stats[2] = s->queue.size();
     stats[3] = s->in_use;
+    stats[4] = s->batches;
     return PTL_OK;
 }
 
@@ -349,7 +367,6 @@ extern "C" void ptl_server_destroy(ptl_server* s) {
         s->stopping = true;
     }
     s->cv_work.notify_all();
-    for (auto& t : s->workers) t.join();
-    for (ptl_generator* g : s->gens) ptl_generator_destroy(g);
+    for (auto& t : s->lanes) t.join();
     delete s;
 }

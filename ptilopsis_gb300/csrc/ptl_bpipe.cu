@@ -128,7 +128,7 @@ public:
     DBuf instr, rd, rs1, rs2, jt, used_instrs, symreg, symswp, stamp, spill, roffs, owner, used, smark, defpos;
     DBuf trig_min, trig_max;
     DBuf ni, nrd, nr1, nr2, njt, fsz, joffs, out;
-    DBuf errw, flags, meta, progs, tabs, lists, changed, sort_err, seen_off, a_off;
+    DBuf errw, flags, meta, progs, tabs, lists, changed, sort_err, seen_off, a_off, dirty, ra_sync;
     DBuf sa, sapos, sbpos, seg0, seg1, tile_seg, tile_l, tile_r, leaf, heap, counters, scan_status, scan_counter,
         sort_local;
     PBuf h_in, h_out, h_fn, h_small;
@@ -152,7 +152,7 @@ public:
                 &fn_end, &fn_start0, &fn_size0, &lifetime, &instr, &rd, &rs1, &rs2, &jt, &used_instrs, &symreg,
                 &symswp, &stamp, &spill, &roffs, &owner, &used, &smark, &defpos, &trig_min, &trig_max, &ni, &nrd,
                 &nr1, &nr2, &njt, &fsz, &joffs, &out, &errw, &flags, &meta, &progs, &tabs, &lists, &changed,
-                &sort_err, &seen_off, &a_off, &sa, &sapos, &sbpos, &seg0, &seg1, &tile_seg, &tile_l, &tile_r,
+                &sort_err, &seen_off, &a_off, &dirty, &ra_sync, &sa, &sapos, &sbpos, &seg0, &seg1, &tile_seg, &tile_l, &tile_r,
                 &leaf, &heap, &counters, &scan_status, &scan_counter, &sort_local};
     }
 
@@ -280,7 +280,7 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
     small_list_off = small_err_off + B * sizeof(ErrorWord);
     small_up_off = small_list_off + static_cast<size_t>(kLists) * (B + 1) * 4;  // 8-byte aligned
     small_up_off = (small_up_off + 15) & ~size_t(15);
-    BP_CU(h_small.ensure(small_up_off + B * (8 + 8 + sizeof(SortSeg) + 8) + 64));
+    BP_CU(h_small.ensure(small_up_off + B * (8 + 8 + sizeof(SortSeg) + 8 + 4) + 64));
     BP_CU(tabs.ensure(static_cast<size_t>(kTables) * (B + 1) * 4));
     BP_CU(lists.ensure(static_cast<size_t>(kLists) * (B + 1) * 4));
     BP_CU(progs.ensure(B * sizeof(Prog)));
@@ -604,10 +604,26 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
         // ---- optimize
         const uint32_t t_wb8 = tiles(5, wb8, batch_tile());
         batch_stage(BatchStage::OptMark, bl(5), t_wb8, nullptr, nullptr, nullptr);
-        uint32_t* hflag = reinterpret_cast<uint32_t*>(h_small.at<uint8_t>(small_meta_off));  // B*16 >= 4
+        uint32_t* hflag = reinterpret_cast<uint32_t*>(h_small.at<uint8_t>(small_meta_off));  // B*16 >= 8
+        // sweeps after the first revisit only the tiles whose marks changed (when every
+        // virtual result is its instruction's own word; else every tile, every sweep)
+        BP_CU(dirty.ensure(2ull * t_wb8 + 64));
+        BP_CU(cudaMemsetAsync(changed.p, 0, 8, s));
+        batch_selfdef(bl(5), t_wb8, changed.at<uint32_t>(1));
+        BP_CU(cudaMemcpyAsync(hflag + 1, changed.at<uint32_t>(1), 4, cudaMemcpyDeviceToHost, s));
+        BP_CU(cudaStreamSynchronize(s));
+        const bool worklist = hflag[1] == 0;
+        uint8_t* dbuf[2] = {dirty.at<uint8_t>(), dirty.at<uint8_t>(t_wb8 + 32)};
+        BP_CU(cudaMemsetAsync(dbuf[0], 1, t_wb8, s));
+        BP_CU(cudaMemsetAsync(dbuf[1], 0, t_wb8, s));
+        int cur = 0;
         for (uint32_t sweeps = 0;;) {
             BP_CU(cudaMemsetAsync(changed.p, 0, 4, s));
-            for (int k = 0; k < 4; ++k) batch_sweep(bl(5), t_wb8, changed.at<uint32_t>());
+            for (int k = 0; k < 4; ++k) {
+                batch_sweep(bl(5), t_wb8, changed.at<uint32_t>(), worklist ? dbuf[cur] : nullptr, dbuf[cur ^ 1]);
+                BP_CU(cudaMemsetAsync(dbuf[cur], 0, t_wb8, s));
+                cur ^= 1;
+            }
             sweeps += 4;
             BP_CU(cudaMemcpyAsync(hflag, changed.p, 4, cudaMemcpyDeviceToHost, s));
             BP_CU(cudaStreamSynchronize(s));
@@ -656,10 +672,31 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
             max_g0 = std::max<uint32_t>(max_g0, static_cast<uint32_t>(g0));
         }
         upload_progs();
-        const uint32_t t_free = tiles(8, nfree, batch_free_tile(), &lane0);
-        batch_free_functions(bl(8), t_free);
+        // independent functions and lane-0 passes of all programs in one persistent launch,
+        // longest programs (most steps) first
+        std::stable_sort(lane0_list.begin(), lane0_list.end(), [&](uint32_t x, uint32_t y) { return S[x] > S[y]; });
+        const uint32_t ra_T = batch_ra_threads(max_g0);
+        uint32_t ra_items = 0;  // per program: its independent-function tiles, then its lane-0 pass
+        {
+            uint32_t* h = table_slot(8);
+            for (size_t k = 0; k < lane0_list.size(); ++k) {
+                h[k] = ra_items;
+                ra_items += static_cast<uint32_t>((nfree[lane0_list[k]] + ra_T - 1) / ra_T) + 1u;
+            }
+            for (size_t k = lane0_list.size(); k <= B; ++k) h[k] = ra_items;
+            BP_CU(cudaMemcpyAsync(dtable_slot(8), h, (B + 1) * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
+        }
         const uint32_t* d_lane0 = upload_list(0, lane0_list);
-        BP_CU(batch_lane0(progs.at<Prog>(), d_lane0, static_cast<uint32_t>(lane0_list.size()), max_g0, s));
+        BP_CU(ra_sync.ensure(B * 8 + 64));
+        uint32_t* up_need = reinterpret_cast<uint32_t*>(h_small.at<uint8_t>(small_up_off + 3 * B * 8 + B * sizeof(SortSeg) + 16));
+        for (size_t p = 0; p < B; ++p) up_need[p] = static_cast<uint32_t>(nfree[p]);
+        uint32_t* d_need = ra_sync.at<uint32_t>();
+        uint32_t* d_done = ra_sync.at<uint32_t>(B);
+        uint32_t* d_queue = ra_sync.at<uint32_t>(2 * B);
+        BP_CU(cudaMemcpyAsync(d_need, up_need, B * 4, cudaMemcpyHostToDevice, s));
+        BP_CU(cudaMemsetAsync(d_done, 0, B * 4, s));
+        BP_CU(batch_regalloc(progs.at<Prog>(), dtable_slot(8), d_lane0, static_cast<uint32_t>(lane0_list.size()),
+                             ra_items, max_g0, d_need, d_done, d_queue, s));
         const uint32_t* d_serial = upload_list(1, serial_list);
         batch_serial(progs.at<Prog>(), d_serial, static_cast<uint32_t>(serial_list.size()), s);
         const uint32_t t_w_sp = tiles(13, W, batch_tile());

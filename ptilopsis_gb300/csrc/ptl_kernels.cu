@@ -1075,18 +1075,46 @@ struct BSortOut {
     __device__ void operator()(const Prog& P, uint32_t i, uint32_t p) const { P.pos[sidx(a[aoff[p] + i])] = i; }
 };
 
+// Optimize sweeps over the tiles marked in cur (all tiles when cur is null).  A sweep can
+// newly act on instruction i only after the used mark of its result (word rd_i - 64)
+// was cleared; when every virtual result is the instruction's own word, that word sits
+// in i's tile, so clearing a mark queues its tile in next for the following sweep.
 __global__ void __launch_bounds__(kThreads) k_batch_sweep(const Prog* progs, const uint32_t* off, uint32_t B,
-                                                          uint32_t total, uint32_t* changed) {
+                                                          uint32_t total, uint32_t* changed, const uint8_t* cur,
+                                                          uint8_t* next) {
     for (uint32_t t = blockIdx.x; t < total; t += gridDim.x) {
+        if (cur && !cur[t]) continue;
         const uint32_t p = batch_program(off, B, t);
         const Prog& P = progs[p];
         const uint32_t base = (t - off[p]) * kBTile;
         bool any = false;
         for (uint32_t k = threadIdx.x; k < kBTile; k += kThreads) {
             const uint32_t i = base + k;
-            if (i < P.wb8) any |= st_opt_sweep(P, i);
+            if (i >= P.wb8) break;
+            uint32_t cl[2];
+            const uint32_t nc = st_opt_sweep_cleared(P, i, cl);
+            for (uint32_t c = 0; c < nc; ++c) next[off[p] + cl[c] / kBTile] = 1;
+            any |= nc != 0;
         }
         if (__syncthreads_or(any) && threadIdx.x == 0) *changed = 1u;
+    }
+}
+
+// flag = 1 when some instruction's virtual result is not its own word.
+__global__ void __launch_bounds__(kThreads) k_batch_selfdef(const Prog* progs, const uint32_t* off, uint32_t B,
+                                                            uint32_t total, uint32_t* flag) {
+    for (uint32_t t = blockIdx.x; t < total; t += gridDim.x) {
+        const uint32_t p = batch_program(off, B, t);
+        const Prog& P = progs[p];
+        const uint32_t base = (t - off[p]) * kBTile;
+        bool odd = false;
+        for (uint32_t k = threadIdx.x; k < kBTile; k += kThreads) {
+            const uint32_t i = base + k;
+            if (i >= P.wb8) break;
+            const uint32_t r = P.rd[i];
+            odd |= s32(r) > 63 && r - 64u != i;
+        }
+        if (__syncthreads_or(odd) && threadIdx.x == 0) *flag = 1u;
     }
 }
 
@@ -1246,6 +1274,75 @@ __global__ void k_batch_serial(const Prog* progs, const uint32_t* list, uint32_t
     }
 }
 
+// Register allocation of every listed program in one persistent launch.  Blocks take
+// work items in order from a queue; program order[k] owns items item_off[k] ..
+// item_off[k+1]: first the tiles of its independent functions (T per tile), then its
+// lane-0 pass.  A block holding a lane-0 item waits until that program's independent
+// functions have all finished (their trigger records are complete); they were all handed
+// out before, to blocks that are running and never wait, so the wait ends.  It is bounded
+// all the same: after about a second the program records DEVICE_TIMEOUT and is skipped.
+struct BatchRa {
+    const Prog* progs;
+    const uint32_t* item_off;   // [n+1]
+    const uint32_t* order;      // [n] programs, longest first
+    uint32_t n, items;
+    const uint32_t* need;       // [B] independent functions per program
+    uint32_t* done;             // [B] finished independent functions
+    uint32_t* queue;
+    uint32_t K, Kf;
+};
+
+template <int Q, int MAXT>
+__global__ void __launch_bounds__(MAXT) k_batch_ra(BatchRa ra) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ uint32_t s_item, s_ok;
+    __shared__ Prog sP;
+    const uint32_t tid = threadIdx.x, T = blockDim.x;
+    for (;;) {
+        if (tid == 0) s_item = atomicAdd(ra.queue, 1u);
+        __syncthreads();
+        const uint32_t item = s_item;
+        if (item >= ra.items) break;
+        const uint32_t pos = batch_program(ra.item_off, ra.n, item);
+        const uint32_t p = ra.order[pos];
+        const uint32_t local = item - ra.item_off[pos];
+        const uint32_t free_tiles = ra.item_off[pos + 1] - ra.item_off[pos] - 1u;
+        if (local < free_tiles) {
+            Prog Pf = ra.progs[p];
+            Pf.defpos = nullptr;  // the independent functions never need definition positions
+            uint32_t* tag = reinterpret_cast<uint32_t*>(smem);
+            const SymCache cf{tag, tag + T * ra.Kf, ra.Kf};
+            const uint32_t f = free_function_of(local * T + tid);
+            if (f < Pf.F) {
+                ra_free_function_cached(Pf, cf, tid, f);
+                __threadfence();
+                atomicAdd(&ra.done[p], 1u);
+            }
+        } else {
+            if (tid == 0) {
+                s_ok = 1;
+                const uint32_t need = ra.need[p];
+                for (uint32_t polls = 0;; ++polls) {
+                    if (*reinterpret_cast<const volatile uint32_t*>(&ra.done[p]) >= need) break;
+                    if (polls > kRaWaitLimit) {
+                        record_error(ra.progs[p].err, ST_DEVICE_TIMEOUT, W_RA2, p);
+                        s_ok = 0;
+                        break;
+                    }
+                    __nanosleep(128);
+                }
+                __threadfence();
+            }
+            const uint64_t* src = reinterpret_cast<const uint64_t*>(&ra.progs[p]);
+            uint64_t* dst = reinterpret_cast<uint64_t*>(&sP);
+            for (uint32_t k = tid; k < sizeof(Prog) / 8; k += T) dst[k] = src[k];
+            __syncthreads();
+            if (s_ok) ra_lane0_block<Q>(sP, sP.S, ra.K, 0u, smem);
+        }
+        __syncthreads();  // before the next item reuses shared memory and s_item
+    }
+}
+
 template <class Op>
 void batch_launch(const BatchLaunch& bl, uint32_t total, const Op& op) {
     if (total == 0) return;
@@ -1305,10 +1402,17 @@ void batch_sort_keys(const BatchLaunch& bl, uint32_t total, unsigned long long* 
     else batch_launch(bl, total, BSortInit{a, aoff});
 }
 
-void batch_sweep(const BatchLaunch& bl, uint32_t total, uint32_t* changed) {
+void batch_sweep(const BatchLaunch& bl, uint32_t total, uint32_t* changed, const uint8_t* cur, uint8_t* next) {
     if (total == 0) return;
     g_launches++;
-    k_batch_sweep<<<std::min<uint32_t>(total, 152u * 16u), kThreads, 0, bl.s>>>(bl.progs, bl.off, bl.B, total, changed);
+    k_batch_sweep<<<std::min<uint32_t>(total, 152u * 16u), kThreads, 0, bl.s>>>(bl.progs, bl.off, bl.B, total, changed,
+                                                                                  cur, next);
+}
+
+void batch_selfdef(const BatchLaunch& bl, uint32_t total, uint32_t* flag) {
+    if (total == 0) return;
+    g_launches++;
+    k_batch_selfdef<<<std::min<uint32_t>(total, 152u * 16u), kThreads, 0, bl.s>>>(bl.progs, bl.off, bl.B, total, flag);
 }
 
 void batch_scan(BatchScan which, const BatchLaunch& bl, uint32_t tiles, const ScanScratch& sc, uint32_t* meta) {
@@ -1371,6 +1475,47 @@ cudaError_t batch_lane0(const Prog* progs, const uint32_t* list, uint32_t count,
     }
     if (ce != cudaSuccess) return ce;
     return cudaGetLastError();
+}
+
+cudaError_t batch_regalloc(const Prog* progs, const uint32_t* item_off, const uint32_t* order, uint32_t n,
+                           uint32_t items, uint32_t max_g0, const uint32_t* need, uint32_t* done, uint32_t* queue,
+                           cudaStream_t s) {
+    if (items == 0) return cudaSuccess;
+    const uint32_t T = batch_ra_threads(max_g0);
+    const uint32_t Q = (max_g0 + T - 1u) / T;
+    constexpr size_t kBudget = 160u * 1024u;
+    uint32_t K = 64;
+    const size_t fixed = sizeof(Ra2Shared) + 16ull * max_g0;
+    while (K > 1 && fixed + static_cast<size_t>(max_g0) * K * 8u > kBudget) K >>= 1;
+    uint32_t Kf = 64;
+    while (Kf > 1 && static_cast<size_t>(T) * Kf * 8u > kBudget) Kf >>= 1;
+    const size_t smem = std::max(fixed + static_cast<size_t>(max_g0) * K * 8u, static_cast<size_t>(T) * Kf * 8u) + 16;
+    BatchRa ra{progs, item_off, order, n, items, need, done, queue, K, Kf};
+    auto go = [&](auto kernel) -> cudaError_t {
+        cudaError_t ce = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+        if (ce != cudaSuccess) return ce;
+        int dev = 0, sms = 0, per_sm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, static_cast<int>(T), smem);
+        const unsigned grid = static_cast<unsigned>(std::max<uint64_t>(1, std::min<uint64_t>(items, static_cast<uint64_t>(std::max(per_sm, 1)) * sms)));
+        cudaMemsetAsync(queue, 0, sizeof(uint32_t), s);
+        g_launches++;
+        kernel<<<grid, T, smem, s>>>(ra);
+        return cudaGetLastError();
+    };
+    if (T <= 256u) return go(k_batch_ra<1, 256>);  // one slot per thread, registers to spare
+    switch (Q) {
+        case 1: return go(k_batch_ra<1, 1024>);
+        case 2: return go(k_batch_ra<2, 1024>);
+        case 3:
+        case 4: return go(k_batch_ra<4, 1024>);
+        default: return go(k_batch_ra<8, 1024>);
+    }
+}
+
+uint32_t batch_ra_threads(uint32_t max_g0) {
+    return max_g0 <= 1024u ? std::max(64u, (max_g0 + 31u) & ~31u) : 1024u;
 }
 
 void batch_serial(const Prog* progs, const uint32_t* list, uint32_t count, cudaStream_t s) {

@@ -81,11 +81,23 @@ uint32_t batch_free_tile();  // independent functions per tile
 void batch_stage(BatchStage st, const BatchLaunch& bl, uint32_t total, uint32_t* meta, uint32_t* seen,
                  const uint64_t* off64);
 void batch_sort_keys(const BatchLaunch& bl, uint32_t total, unsigned long long* a, const uint64_t* aoff, bool out);
-void batch_sweep(const BatchLaunch& bl, uint32_t total, uint32_t* changed);
+// One optimize sweep over the tiles marked in cur (all when cur is null); marks in next
+// the tiles a cleared mark makes live again.  Valid only when batch_selfdef found every
+// virtual result to be its instruction's own word (flag 0); otherwise pass cur = null.
+void batch_sweep(const BatchLaunch& bl, uint32_t total, uint32_t* changed, const uint8_t* cur, uint8_t* next);
+void batch_selfdef(const BatchLaunch& bl, uint32_t total, uint32_t* flag);
 void batch_scan(BatchScan which, const BatchLaunch& bl, uint32_t tiles, const ScanScratch& sc, uint32_t* meta);
 void batch_sizes(bool w3, const Prog* progs, const uint32_t* list, uint32_t count, uint32_t* meta, cudaStream_t s);
 void batch_free_functions(const BatchLaunch& bl, uint32_t total);
 cudaError_t batch_lane0(const Prog* progs, const uint32_t* list, uint32_t count, uint32_t max_g0, cudaStream_t s);
 void batch_serial(const Prog* progs, const uint32_t* list, uint32_t count, cudaStream_t s);
+// Register allocation steps of n programs in one persistent launch: program order[k]
+// owns work items item_off[k] .. item_off[k+1] (its independent functions in tiles of
+// batch_ra_threads(max_g0), then its lane-0 pass, which starts once its need[p]
+// independent functions, counted in done[p] (zeroed), have finished).
+uint32_t batch_ra_threads(uint32_t max_g0);
+cudaError_t batch_regalloc(const Prog* progs, const uint32_t* item_off, const uint32_t* order, uint32_t n,
+                           uint32_t items, uint32_t max_g0, const uint32_t* need, uint32_t* done, uint32_t* queue,
+                           cudaStream_t s);
 
 }  // namespace ptl

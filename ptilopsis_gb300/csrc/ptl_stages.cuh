@@ -546,18 +546,25 @@ PTL_HD void st_opt_mark(const Prog& P, uint32_t i) {
     }
 }
 
-// Returns true when it cleared a mark.
-PTL_HD bool st_opt_sweep(const Prog& P, uint32_t i) {
+// Clears the used marks of the operands of instruction i when its result is unused;
+// returns how many it cleared, their word indices in cleared[0..].
+PTL_HD uint32_t st_opt_sweep_cleared(const Prog& P, uint32_t i, uint32_t cleared[2]) {
     const uint32_t r = P.rd[i];
-    if (!(s32(r) > 63)) return false;
-    if (r - 64u >= P.W) { record_error(P.err, ST_UNSUPPORTED, W_OPT, i); return false; }
-    if (P.used[r - 64u]) return false;
-    bool changed = false;
+    if (!(s32(r) > 63)) return 0;
+    if (r - 64u >= P.W) { record_error(P.err, ST_UNSUPPORTED, W_OPT, i); return 0; }
+    if (P.used[r - 64u]) return 0;
+    uint32_t nc = 0;
     const int32_t a = s32(P.rs1[i] - 64u);
     const int32_t b = s32(P.rs2[i] - 64u);
-    if (a >= 0 && u32(a) < P.W && !P.smark[a] && P.used[a]) { P.used[a] = 0; changed = true; }
-    if (b >= 0 && u32(b) < P.W && !P.smark[b] && P.used[b]) { P.used[b] = 0; changed = true; }
-    return changed;
+    if (a >= 0 && u32(a) < P.W && !P.smark[a] && P.used[a]) { P.used[a] = 0; cleared[nc++] = u32(a); }
+    if (b >= 0 && u32(b) < P.W && !P.smark[b] && P.used[b]) { P.used[b] = 0; cleared[nc++] = u32(b); }
+    return nc;
+}
+
+// Returns true when it cleared a mark.
+PTL_HD bool st_opt_sweep(const Prog& P, uint32_t i) {
+    uint32_t cleared[2];
+    return st_opt_sweep_cleared(P, i, cleared) != 0;
 }
 
 PTL_HD void st_opt_final(const Prog& P, uint32_t i) {
