@@ -126,7 +126,7 @@ public:
     DBuf nt, rt, nd1, nd, par, ci, dep, sizes, loc0, loc, pos, decl, fflag, regs, seen;
     DBuf fn_id, fn_start, fn_size, fn_end, fn_start0, fn_size0, lifetime;
     DBuf instr, rd, rs1, rs2, jt, used_instrs, symreg, symswp, stamp, spill, roffs, owner, used, smark, defpos;
-    DBuf trig_min, trig_max;
+    DBuf trig_min, trig_max, ra_chunks;
     DBuf ni, nrd, nr1, nr2, njt, fsz, joffs, out;
     DBuf errw, flags, meta, progs, tabs, lists, changed, sort_err, seen_off, a_off, dirty, ra_sync;
     DBuf sa, sapos, sbpos, seg0, seg1, tile_seg, tile_l, tile_r, leaf, heap, counters, scan_status, scan_counter,
@@ -150,7 +150,7 @@ public:
         return {&tab, &in_type, &in_rtype, &in_parent, &in_depth, &in_child, &in_data, &nt, &rt, &nd1, &nd, &par,
                 &ci, &dep, &sizes, &loc0, &loc, &pos, &decl, &fflag, &regs, &seen, &fn_id, &fn_start, &fn_size,
                 &fn_end, &fn_start0, &fn_size0, &lifetime, &instr, &rd, &rs1, &rs2, &jt, &used_instrs, &symreg,
-                &symswp, &stamp, &spill, &roffs, &owner, &used, &smark, &defpos, &trig_min, &trig_max, &ni, &nrd,
+                &symswp, &stamp, &spill, &roffs, &owner, &used, &smark, &defpos, &trig_min, &trig_max, &ra_chunks, &ni, &nrd,
                 &nr1, &nr2, &njt, &fsz, &joffs, &out, &errw, &flags, &meta, &progs, &tabs, &lists, &changed,
                 &sort_err, &seen_off, &a_off, &dirty, &ra_sync, &sa, &sapos, &sbpos, &seg0, &seg1, &tile_seg, &tile_l, &tile_r,
                 &leaf, &heap, &counters, &scan_status, &scan_counter, &sort_local};
@@ -273,7 +273,7 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
         if (!e) BP_CU(cudaEventCreate(&e));
 
     // ---- small per-program state and the pinned small area
-    constexpr int kTables = 20, kLists = 4;
+    constexpr int kTables = 20, kLists = 4;  // table slots 0..16 are used
     small_progs_off = static_cast<size_t>(kTables) * (B + 1) * 4;
     small_meta_off = small_progs_off + B * sizeof(Prog);
     small_err_off = small_meta_off + B * 16;
@@ -637,15 +637,20 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
         // ---- regalloc
         const uint32_t t_f = tiles(6, F, batch_tile());
         batch_stage(BatchStage::InitLifetime, bl(6), t_f, nullptr, nullptr, nullptr);
-        Layout Lt;
+        Layout Lt, Lc;
         Lt.build(trig, active);
+        std::vector<uint64_t> chunk_words(B);
+        for (size_t p = 0; p < B; ++p) chunk_words[p] = 2 * (S[p] / 32 + 2);
+        Lc.build(chunk_words, active);
         BP_CU(trig_min.ensure(Lt.total * 4));
         BP_CU(trig_max.ensure(Lt.total * 4));
         BP_CU(cudaMemsetAsync(trig_min.p, 0xFF, Lt.total * 4, s));
         BP_CU(cudaMemsetAsync(trig_max.p, 0, Lt.total * 4, s));
+        BP_CU(family(Lc, {&ra_chunks}, 4));
         for (size_t p = 0; p < B; ++p) {
             hp[p].trig_min = trig_min.at<uint32_t>(Lt.elem(p));
             hp[p].trig_max = trig_max.at<uint32_t>(Lt.elem(p));
+            hp[p].ra_chunks = ra_chunks.at<uint32_t>(Lc.elem(p));
         }
         upload_progs();
         const uint32_t t_w = tiles(7, W, batch_tile());
@@ -687,16 +692,12 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
             BP_CU(cudaMemcpyAsync(dtable_slot(8), h, (B + 1) * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
         }
         const uint32_t* d_lane0 = upload_list(0, lane0_list);
-        BP_CU(ra_sync.ensure(B * 8 + 64));
-        uint32_t* up_need = reinterpret_cast<uint32_t*>(h_small.at<uint8_t>(small_up_off + 3 * B * 8 + B * sizeof(SortSeg) + 16));
-        for (size_t p = 0; p < B; ++p) up_need[p] = static_cast<uint32_t>(nfree[p]);
-        uint32_t* d_need = ra_sync.at<uint32_t>();
-        uint32_t* d_done = ra_sync.at<uint32_t>(B);
-        uint32_t* d_queue = ra_sync.at<uint32_t>(2 * B);
-        BP_CU(cudaMemcpyAsync(d_need, up_need, B * 4, cudaMemcpyHostToDevice, s));
-        BP_CU(cudaMemsetAsync(d_done, 0, B * 4, s));
+        BP_CU(ra_sync.ensure(64));
+        // per program: histogram of the independent functions' last chunks, then counts
+        const uint32_t t_hist = tiles(16, nfree, batch_tile(), &lane0);
+        batch_stage(BatchStage::RaHist, bl(16), t_hist, nullptr, nullptr, nullptr);
         BP_CU(batch_regalloc(progs.at<Prog>(), dtable_slot(8), d_lane0, static_cast<uint32_t>(lane0_list.size()),
-                             ra_items, max_g0, d_need, d_done, d_queue, s));
+                             ra_items, max_g0, ra_sync.at<uint32_t>(), s));
         const uint32_t* d_serial = upload_list(1, serial_list);
         batch_serial(progs.at<Prog>(), d_serial, static_cast<uint32_t>(serial_list.size()), s);
         const uint32_t t_w_sp = tiles(13, W, batch_tile());

@@ -1034,6 +1034,11 @@ PTL_BATCH_OP(BRaFunctab, P.F, st_fix_functab(P, i, P.roffs, P.W))
 PTL_BATCH_OP(BRaFrame, P.F, st_ra_frame(P, i))
 PTL_BATCH_OP(BFjEmit, P.W2, st_fj_emit(P, i))
 PTL_BATCH_OP(BFjFunctab, P.F, st_fix_functab(P, i, P.joffs, P.W2))
+// chunk histogram of a program's independent functions (see k_ra_chunk_hist)
+PTL_BATCH_OP(BRaHist, P.F - (P.F + 7u) / 8u,
+             const uint32_t f = free_function_of(i);
+             const uint32_t size = P.fn_size0[f];
+             if (s32(size) > 0) atomicAdd(&P.ra_chunks[(size - 1u) / kRaChunk], 1u))
 PTL_BATCH_OP(BCross, P.W,
              const uint32_t r = st_ra_cross(P, i, P.stamp);
              if (r & 1u) atomicOr(&P.flags[1], 1u);
@@ -1277,17 +1282,16 @@ __global__ void k_batch_serial(const Prog* progs, const uint32_t* list, uint32_t
 // Register allocation of every listed program in one persistent launch.  Blocks take
 // work items in order from a queue; program order[k] owns items item_off[k] ..
 // item_off[k+1]: first the tiles of its independent functions (T per tile), then its
-// lane-0 pass.  A block holding a lane-0 item waits until that program's independent
-// functions have all finished (their trigger records are complete); they were all handed
-// out before, to blocks that are running and never wait, so the wait ends.  It is bounded
-// all the same: after about a second the program records DEVICE_TIMEOUT and is skipped.
+// lane-0 pass.  The independent functions count the finished 32-step chunks of trigger
+// records in the program's ra_chunks record, and the lane-0 pass waits for each chunk
+// before it reads it, as the fused single-program launch does.  Every tile of a program
+// is handed out before its lane-0 item, to blocks that are running and never wait, so
+// the waits end; they are bounded all the same (DEVICE_TIMEOUT after about a second).
 struct BatchRa {
     const Prog* progs;
     const uint32_t* item_off;   // [n+1]
     const uint32_t* order;      // [n] programs, longest first
     uint32_t n, items;
-    const uint32_t* need;       // [B] independent functions per program
-    uint32_t* done;             // [B] finished independent functions
     uint32_t* queue;
     uint32_t K, Kf;
 };
@@ -1295,7 +1299,7 @@ struct BatchRa {
 template <int Q, int MAXT>
 __global__ void __launch_bounds__(MAXT) k_batch_ra(BatchRa ra) {
     extern __shared__ __align__(16) unsigned char smem[];
-    __shared__ uint32_t s_item, s_ok;
+    __shared__ uint32_t s_item;
     __shared__ Prog sP;
     const uint32_t tid = threadIdx.x, T = blockDim.x;
     for (;;) {
@@ -1313,31 +1317,14 @@ __global__ void __launch_bounds__(MAXT) k_batch_ra(BatchRa ra) {
             uint32_t* tag = reinterpret_cast<uint32_t*>(smem);
             const SymCache cf{tag, tag + T * ra.Kf, ra.Kf};
             const uint32_t f = free_function_of(local * T + tid);
-            if (f < Pf.F) {
-                ra_free_function_cached(Pf, cf, tid, f);
-                __threadfence();
-                atomicAdd(&ra.done[p], 1u);
-            }
+            const uint32_t chunks = (Pf.S + kRaChunk - 1u) / kRaChunk;
+            if (f < Pf.F) ra_free_function_cached(Pf, cf, tid, f, Pf.ra_chunks + chunks);
         } else {
-            if (tid == 0) {
-                s_ok = 1;
-                const uint32_t need = ra.need[p];
-                for (uint32_t polls = 0;; ++polls) {
-                    if (*reinterpret_cast<const volatile uint32_t*>(&ra.done[p]) >= need) break;
-                    if (polls > kRaWaitLimit) {
-                        record_error(ra.progs[p].err, ST_DEVICE_TIMEOUT, W_RA2, p);
-                        s_ok = 0;
-                        break;
-                    }
-                    __nanosleep(128);
-                }
-                __threadfence();
-            }
             const uint64_t* src = reinterpret_cast<const uint64_t*>(&ra.progs[p]);
             uint64_t* dst = reinterpret_cast<uint64_t*>(&sP);
             for (uint32_t k = tid; k < sizeof(Prog) / 8; k += T) dst[k] = src[k];
             __syncthreads();
-            if (s_ok) ra_lane0_block<Q>(sP, sP.S, ra.K, 0u, smem);
+            ra_lane0_block<Q>(sP, sP.S, ra.K, (sP.S + kRaChunk - 1u) / kRaChunk, smem);
         }
         __syncthreads();  // before the next item reuses shared memory and s_item
     }
@@ -1386,6 +1373,7 @@ void batch_stage(BatchStage st, const BatchLaunch& bl, uint32_t total, uint32_t*
         case BatchStage::OptFinal: batch_launch(bl, total, BOptFinal{}); break;
         case BatchStage::InitLifetime: batch_launch(bl, total, BInitLifetime{}); break;
         case BatchStage::Cross: batch_launch(bl, total, BCross{}); break;
+        case BatchStage::RaHist: batch_launch(bl, total, BRaHist{}); break;
         case BatchStage::Spill: batch_launch(bl, total, BSpill{}); break;
         case BatchStage::Scatter: batch_launch(bl, total, BScatter{}); break;
         case BatchStage::RaFunctab:
@@ -1478,8 +1466,7 @@ cudaError_t batch_lane0(const Prog* progs, const uint32_t* list, uint32_t count,
 }
 
 cudaError_t batch_regalloc(const Prog* progs, const uint32_t* item_off, const uint32_t* order, uint32_t n,
-                           uint32_t items, uint32_t max_g0, const uint32_t* need, uint32_t* done, uint32_t* queue,
-                           cudaStream_t s) {
+                           uint32_t items, uint32_t max_g0, uint32_t* queue, cudaStream_t s) {
     if (items == 0) return cudaSuccess;
     const uint32_t T = batch_ra_threads(max_g0);
     const uint32_t Q = (max_g0 + T - 1u) / T;
@@ -1490,7 +1477,7 @@ cudaError_t batch_regalloc(const Prog* progs, const uint32_t* item_off, const ui
     uint32_t Kf = 64;
     while (Kf > 1 && static_cast<size_t>(T) * Kf * 8u > kBudget) Kf >>= 1;
     const size_t smem = std::max(fixed + static_cast<size_t>(max_g0) * K * 8u, static_cast<size_t>(T) * Kf * 8u) + 16;
-    BatchRa ra{progs, item_off, order, n, items, need, done, queue, K, Kf};
+    BatchRa ra{progs, item_off, order, n, items, queue, K, Kf};
     auto go = [&](auto kernel) -> cudaError_t {
         cudaError_t ce = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
         if (ce != cudaSuccess) return ce;

@@ -71,7 +71,7 @@ struct BatchLaunch {
     cudaStream_t s;
 };
 enum class BatchStage {
-    Validate, DepthSeen, Translate, Preprocess, Fix, Functab, Gen, OptMark, OptFinal, InitLifetime, Cross, Spill,
+    Validate, DepthSeen, Translate, Preprocess, Fix, Functab, Gen, OptMark, OptFinal, InitLifetime, Cross, RaHist, Spill,
     Scatter, RaFunctab, FjEmit, FjFunctab
 };
 enum class BatchScan { Count, Decl, RaCount, FjSize };
@@ -93,11 +93,10 @@ cudaError_t batch_lane0(const Prog* progs, const uint32_t* list, uint32_t count,
 void batch_serial(const Prog* progs, const uint32_t* list, uint32_t count, cudaStream_t s);
 // Register allocation steps of n programs in one persistent launch: program order[k]
 // owns work items item_off[k] .. item_off[k+1] (its independent functions in tiles of
-// batch_ra_threads(max_g0), then its lane-0 pass, which starts once its need[p]
-// independent functions, counted in done[p] (zeroed), have finished).
+// batch_ra_threads(max_g0), then its lane-0 pass, which follows their progress through
+// the program's ra_chunks record: histogram (BatchStage::RaHist) then zeroed counts).
 uint32_t batch_ra_threads(uint32_t max_g0);
 cudaError_t batch_regalloc(const Prog* progs, const uint32_t* item_off, const uint32_t* order, uint32_t n,
-                           uint32_t items, uint32_t max_g0, const uint32_t* need, uint32_t* done, uint32_t* queue,
-                           cudaStream_t s);
+                           uint32_t items, uint32_t max_g0, uint32_t* queue, cudaStream_t s);
 
 }  // namespace ptl
