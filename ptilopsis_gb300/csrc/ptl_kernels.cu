@@ -543,10 +543,9 @@ __device__ void ra_lane0_block(const Prog& P, uint32_t S, uint32_t K, uint32_t c
     uint32_t* cval = ctag + G0 * K;
     const SymCache c{ctag, cval, K};
     const bool hashed = P.defpos == nullptr;
-    if (T < 64u) {  // the row-0 phases need a thread per physical register
-        if (tid == 0) record_error(P.err, ST_UNSUPPORTED, W_RA2, T);
-        return;
-    }
+    // Row-0 phases: thread tid handles physical registers tid, tid + T, ... (two each in a
+    // one-warp block, which small programs get: its barriers cost next to nothing).
+    constexpr uint32_t kRow = 64;
     // thread 0: independent functions still running in chunk wc (need)
     uint32_t need = 0, wc = 0;
     auto wait_for = [&](uint32_t chunk) {
@@ -566,21 +565,26 @@ __device__ void ra_lane0_block(const Prog& P, uint32_t S, uint32_t K, uint32_t c
         L[q].have_next = false;
         if (j < G0) ra2_slot_init(P, c, L[q], j, j);
     }
-    uint32_t tmin = 0xFFFFFFFFu, tmax = 0;  // trigger records, one step ahead
-    if (tid < 64) {
-        sh.R0[tid] = 0xFFFFFFFFu;
-        sh.R0own[tid] = 0xFFFFFFFFu;
-        for (uint32_t k = tid; k < kSnapHash; k += 64) {
-            sh.hkey[0][k] = sh.hkey[1][k] = 0;
-            sh.hmask[0][k] = sh.hmask[1][k] = 0;
-        }
+    uint32_t tmin[2] = {0xFFFFFFFFu, 0xFFFFFFFFu}, tmax[2] = {0, 0};  // trigger records, one step ahead
+    for (uint32_t p = tid; p < kRow; p += T) {
+        sh.R0[p] = 0xFFFFFFFFu;
+        sh.R0own[p] = 0xFFFFFFFFu;
+    }
+    for (uint32_t k = tid; k < kSnapHash; k += T) {
+        sh.hkey[0][k] = sh.hkey[1][k] = 0;
+        sh.hmask[0][k] = sh.hmask[1][k] = 0;
     }
     __syncthreads();
     if (s_abort) return;
     // trigger records are read from L2: lines of a chunk may sit in L1 from the chunk before
-    if (tid < 64 && S > 0) {
-        ra2_begin_p(sh, 0, tid, __ldcg(&P.trig_min[tid]), __ldcg(&P.trig_max[tid]), hashed);
-        if (S > 1) { tmin = __ldcg(&P.trig_min[64u + tid]); tmax = __ldcg(&P.trig_max[64u + tid]); }
+    if (S > 0) {
+#pragma unroll
+        for (uint32_t r = 0; r < 2; ++r) {  // T >= 32: at most two positions per thread
+            const uint32_t p = tid + r * T;
+            if (p >= kRow) continue;
+            ra2_begin_p(sh, 0, p, __ldcg(&P.trig_min[p]), __ldcg(&P.trig_max[p]), hashed);
+            if (S > 1) { tmin[r] = __ldcg(&P.trig_min[kRow + p]); tmax[r] = __ldcg(&P.trig_max[kRow + p]); }
+        }
     }
     __syncthreads();
     // Per step, three barriers: (load+compute) | (check + speculative apply + clear next
@@ -613,9 +617,10 @@ __device__ void ra_lane0_block(const Prog& P, uint32_t S, uint32_t K, uint32_t c
             const uint32_t j = tid + static_cast<uint32_t>(q) * T;
             if (j < G0) ra2_apply(P, c, sh, L[q], j, i, cur + 4u * j);
         }
-        if (hashed && tid < 64) snap_clear_next(sh, i, tid);
+        if (hashed)
+            for (uint32_t p = tid; p < kRow; p += T) snap_clear_next(sh, i, p);
         if (__syncthreads_or(flag)) {
-            if (tid < 64) sh.r0grp[tid] = 0;
+            for (uint32_t p = tid; p < kRow; p += T) sh.r0grp[p] = 0;
             for (uint32_t round = 0;; ++round) {
 #pragma unroll
                 for (int q = 0; q < Q; ++q) {
@@ -623,7 +628,8 @@ __device__ void ra_lane0_block(const Prog& P, uint32_t S, uint32_t K, uint32_t c
                     if (j < G0) ra2_round(sh, L[q]);
                 }
                 __syncthreads();
-                const bool changed = tid < 64 ? ra2_round_p(sh, tid) : false;
+                bool changed = false;
+                for (uint32_t p = tid; p < kRow; p += T) changed |= ra2_round_p(sh, p);
                 if (!__syncthreads_or(changed)) break;
                 if (round > G0 + 2u) {
                     if (tid == 0) record_error(P.err, ST_DEVICE_TIMEOUT, W_RA2, i);
@@ -637,13 +643,17 @@ __device__ void ra_lane0_block(const Prog& P, uint32_t S, uint32_t K, uint32_t c
             }
             __syncthreads();
         }
-        if (tid < 64) {
-            ra2_end_p(P, c, sh, tid, cur);
-            if (i + 1 < S) {
-                ra2_begin_p(sh, i + 1, tid, tmin, tmax, hashed);
-                if (i + 2 < S) {
-                    tmin = __ldcg(&P.trig_min[static_cast<size_t>(i + 2) * 64u + tid]);
-                    tmax = __ldcg(&P.trig_max[static_cast<size_t>(i + 2) * 64u + tid]);
+#pragma unroll
+        for (uint32_t r = 0; r < 2; ++r) {
+            const uint32_t p = tid + r * T;
+            if (p < kRow) {
+                ra2_end_p(P, c, sh, p, cur);
+                if (i + 1 < S) {
+                    ra2_begin_p(sh, i + 1, p, tmin[r], tmax[r], hashed);
+                    if (i + 2 < S) {
+                        tmin[r] = __ldcg(&P.trig_min[static_cast<size_t>(i + 2) * kRow + p]);
+                        tmax[r] = __ldcg(&P.trig_max[static_cast<size_t>(i + 2) * kRow + p]);
+                    }
                 }
             }
         }
@@ -905,7 +915,7 @@ cudaError_t launch_ra_steps_q(const Prog& P0, const Prog& Pfree, uint32_t G0, ui
 }
 
 cudaError_t launch_ra_steps(const Prog& P0, const Prog& Pfree, uint32_t G0, cudaStream_t s) {
-    const uint32_t T = G0 <= 1024u ? std::max(64u, (G0 + 31u) & ~31u) : 1024u;
+    const uint32_t T = G0 <= 1024u ? std::max(32u, (G0 + 31u) & ~31u) : 1024u;
     const uint32_t Q = (G0 + T - 1u) / T;
     switch (Q) {
         case 1: return launch_ra_steps_q<1>(P0, Pfree, G0, T, s);
@@ -1242,36 +1252,6 @@ __global__ void __launch_bounds__(kScanThreads) k_bscan(const Prog* progs, const
 }
 
 // ---- batched register allocation
-// Independent functions of all listed programs: one thread each (64 per block).
-__global__ void __launch_bounds__(kRaFreeThreads) k_batch_free(const Prog* progs, const uint32_t* off, uint32_t B,
-                                                               uint32_t total) {
-    __shared__ uint32_t tag[kRaFreeThreads * kRaFreeK];
-    __shared__ uint32_t val[kRaFreeThreads * kRaFreeK];
-    const SymCache c{tag, val, kRaFreeK};
-    for (uint32_t t = blockIdx.x; t < total; t += gridDim.x) {
-        const uint32_t p = batch_program(off, B, t);
-        Prog Pf = progs[p];
-        Pf.defpos = nullptr;  // the independent functions never need definition positions
-        const uint32_t f = free_function_of((t - off[p]) * kRaFreeThreads + threadIdx.x);
-        if (f < Pf.F) ra_free_function_cached(Pf, c, threadIdx.x, f);
-    }
-}
-
-// Lane-0 functions: one block per listed program (the program's view in shared memory).
-template <int Q>
-__global__ void __launch_bounds__(1024) k_batch_lane0(const Prog* progs, const uint32_t* list, uint32_t K) {
-    extern __shared__ __align__(16) unsigned char smem[];
-    __shared__ Prog sP;
-    const uint32_t p = list[blockIdx.x];
-    {
-        const uint64_t* src = reinterpret_cast<const uint64_t*>(&progs[p]);
-        uint64_t* dst = reinterpret_cast<uint64_t*>(&sP);
-        for (uint32_t k = threadIdx.x; k < sizeof(Prog) / 8; k += blockDim.x) dst[k] = src[k];
-    }
-    __syncthreads();
-    ra_lane0_block<Q>(sP, sP.S, K, 0u, smem);
-}
-
 __global__ void k_batch_serial(const Prog* progs, const uint32_t* list, uint32_t count) {
     PTL_FOR(k, count) {
         const Prog& P = progs[list[k]];
@@ -1423,58 +1403,18 @@ void batch_sizes(bool w3, const Prog* progs, const uint32_t* list, uint32_t coun
     else k_batch_w2<<<grid_for(count), kThreads, 0, s>>>(progs, list, count, meta);
 }
 
-void batch_free_functions(const BatchLaunch& bl, uint32_t total) {
-    if (total == 0) return;
-    g_launches++;
-    k_batch_free<<<std::min<uint32_t>(total, 152u * 64u), kRaFreeThreads, 0, bl.s>>>(bl.progs, bl.off, bl.B, total);
-}
-
-uint32_t batch_free_tile() { return kRaFreeThreads; }
-
-cudaError_t batch_lane0(const Prog* progs, const uint32_t* list, uint32_t count, uint32_t max_g0, cudaStream_t s) {
-    if (count == 0) return cudaSuccess;
-    const uint32_t T = max_g0 <= 1024u ? std::max(64u, (max_g0 + 31u) & ~31u) : 1024u;
-    const uint32_t Q = (max_g0 + T - 1u) / T;
-    constexpr size_t kBudget = 160u * 1024u;
-    uint32_t K = 64;
-    const size_t fixed = sizeof(Ra2Shared) + 16ull * max_g0;
-    while (K > 1 && fixed + static_cast<size_t>(max_g0) * K * 8u > kBudget) K >>= 1;
-    const size_t smem = fixed + static_cast<size_t>(max_g0) * K * 8u + 16;
-    cudaError_t ce = cudaSuccess;
-    g_launches++;
-    switch (Q) {
-        case 1:
-            ce = cudaFuncSetAttribute(k_batch_lane0<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-            if (ce == cudaSuccess) k_batch_lane0<1><<<count, T, smem, s>>>(progs, list, K);
-            break;
-        case 2:
-            ce = cudaFuncSetAttribute(k_batch_lane0<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-            if (ce == cudaSuccess) k_batch_lane0<2><<<count, T, smem, s>>>(progs, list, K);
-            break;
-        case 3:
-        case 4:
-            ce = cudaFuncSetAttribute(k_batch_lane0<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-            if (ce == cudaSuccess) k_batch_lane0<4><<<count, T, smem, s>>>(progs, list, K);
-            break;
-        default:
-            ce = cudaFuncSetAttribute(k_batch_lane0<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-            if (ce == cudaSuccess) k_batch_lane0<8><<<count, T, smem, s>>>(progs, list, K);
-            break;
-    }
-    if (ce != cudaSuccess) return ce;
-    return cudaGetLastError();
-}
-
 cudaError_t batch_regalloc(const Prog* progs, const uint32_t* item_off, const uint32_t* order, uint32_t n,
                            uint32_t items, uint32_t max_g0, uint32_t* queue, cudaStream_t s) {
     if (items == 0) return cudaSuccess;
     const uint32_t T = batch_ra_threads(max_g0);
     const uint32_t Q = (max_g0 + T - 1u) / T;
     constexpr size_t kBudget = 160u * 1024u;
-    uint32_t K = 64;
+    // Many programs share each SM here, so the symbol caches are kept small (16 entries)
+    // for occupancy; the single-program launch gives one program all it can use.
+    uint32_t K = 16;
     const size_t fixed = sizeof(Ra2Shared) + 16ull * max_g0;
     while (K > 1 && fixed + static_cast<size_t>(max_g0) * K * 8u > kBudget) K >>= 1;
-    uint32_t Kf = 64;
+    uint32_t Kf = 16;
     while (Kf > 1 && static_cast<size_t>(T) * Kf * 8u > kBudget) Kf >>= 1;
     const size_t smem = std::max(fixed + static_cast<size_t>(max_g0) * K * 8u, static_cast<size_t>(T) * Kf * 8u) + 16;
     BatchRa ra{progs, item_off, order, n, items, queue, K, Kf};
@@ -1502,7 +1442,7 @@ cudaError_t batch_regalloc(const Prog* progs, const uint32_t* item_off, const ui
 }
 
 uint32_t batch_ra_threads(uint32_t max_g0) {
-    return max_g0 <= 1024u ? std::max(64u, (max_g0 + 31u) & ~31u) : 1024u;
+    return max_g0 <= 1024u ? std::max(32u, (max_g0 + 31u) & ~31u) : 1024u;
 }
 
 void batch_serial(const Prog* progs, const uint32_t* list, uint32_t count, cudaStream_t s) {

@@ -77,7 +77,6 @@ enum class BatchStage {
 enum class BatchScan { Count, Decl, RaCount, FjSize };
 uint32_t batch_tile();       // elements per tile of the element-wise stages
 uint32_t batch_scan_tile();  // elements per scan tile
-uint32_t batch_free_tile();  // independent functions per tile
 void batch_stage(BatchStage st, const BatchLaunch& bl, uint32_t total, uint32_t* meta, uint32_t* seen,
                  const uint64_t* off64);
 void batch_sort_keys(const BatchLaunch& bl, uint32_t total, unsigned long long* a, const uint64_t* aoff, bool out);
@@ -88,8 +87,6 @@ void batch_sweep(const BatchLaunch& bl, uint32_t total, uint32_t* changed, const
 void batch_selfdef(const BatchLaunch& bl, uint32_t total, uint32_t* flag);
 void batch_scan(BatchScan which, const BatchLaunch& bl, uint32_t tiles, const ScanScratch& sc, uint32_t* meta);
 void batch_sizes(bool w3, const Prog* progs, const uint32_t* list, uint32_t count, uint32_t* meta, cudaStream_t s);
-void batch_free_functions(const BatchLaunch& bl, uint32_t total);
-cudaError_t batch_lane0(const Prog* progs, const uint32_t* list, uint32_t count, uint32_t max_g0, cudaStream_t s);
 void batch_serial(const Prog* progs, const uint32_t* list, uint32_t count, cudaStream_t s);
 // Register allocation steps of n programs in one persistent launch: program order[k]
 // owns work items item_off[k] .. item_off[k+1] (its independent functions in tiles of
