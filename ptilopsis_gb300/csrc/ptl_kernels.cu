@@ -433,20 +433,103 @@ __global__ void __launch_bounds__(kThreads) k_sort_swap(SortScratch ss, const So
 __global__ void k_sort_leaves(SortScratch ss, uint32_t count) {
     PTL_FOR(k, count) leaf_sort(ss.a, ss.leaf[2 * k], ss.leaf[2 * k + 1]);
 }
-// One small range per thread, staged in shared memory (element k of thread t at
-// k * blockDim + t, so that the threads of a warp use different banks).
-constexpr int kSortLocalThreads = 64;
-__global__ void __launch_bounds__(kSortLocalThreads) k_sort_local(SortScratch ss, uint32_t count) {
-    extern __shared__ unsigned long long sbuf[];
-    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= count) return;
-    const uint32_t first = ss.local[3 * k], last = ss.local[3 * k + 1], dl = ss.local[3 * k + 2];
+// One small range per warp, staged in shared memory.  Each partition step is the
+// closed form of the rounds above, computed by the warp: L-stop and R-stop positions by
+// ballot and prefix count, K by ballot (A[k] < B[k] holds on a prefix of k), the cut,
+// then the K swaps, whose pairs are disjoint, in parallel.  Pending ranges live on a
+// per-warp stack; ranges of at most 16 keys are collected and insertion-sorted one per
+// lane at the end, and a range whose depth budget is spent is heap-sorted by one lane.
+constexpr int kSortLocalWarps = 8;
+struct LocalWarpSmem {
+    unsigned long long buf[kSortLocal];
+    uint32_t A[kSortLocal], R[kSortLocal];
+    uint32_t st_f[64], st_l[64], st_d[64];
+    uint16_t leaf_f[kSortLocal / 2], leaf_l[kSortLocal / 2];
+};
+
+__global__ void __launch_bounds__(kSortLocalWarps * 32) k_sort_local(SortScratch ss, uint32_t count) {
+    extern __shared__ __align__(16) unsigned char lsm[];
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    LocalWarpSmem& w = reinterpret_cast<LocalWarpSmem*>(lsm)[warp];
+    const uint32_t r = blockIdx.x * kSortLocalWarps + warp;
+    if (r >= count) return;  // warp-uniform; the kernel has no block barrier
+    const uint32_t first = ss.local[3 * r], last = ss.local[3 * r + 1], dl = ss.local[3 * r + 2];
     const uint32_t len = last - first;
     if (len > kSortLocal) return;  // emitted only up to kSortLocal
-    const Strided buf{sbuf + threadIdx.x, blockDim.x};
-    for (uint32_t i = 0; i < len; ++i) buf[i] = ss.a[first + i];
-    local_introsort(buf, 0u, len, dl);
-    for (uint32_t i = 0; i < len; ++i) ss.a[first + i] = buf[i];
+    for (uint32_t i = lane; i < len; i += 32) w.buf[i] = ss.a[first + i];
+    const unsigned full = 0xFFFFFFFFu;
+    const unsigned lt = (1u << lane) - 1u;
+    uint32_t sp = 0, nleaf = 0;
+    if (lane == 0) { w.st_f[0] = 0; w.st_l[0] = len; w.st_d[0] = dl; }
+    sp = 1;
+    __syncwarp();
+    while (sp > 0) {
+        --sp;
+        const uint32_t f = w.st_f[sp], l = w.st_l[sp], d = w.st_d[sp];
+        __syncwarp();
+        const uint32_t m = l - f;
+        if (m <= kSortThreshold) {
+            if (m > 1) {
+                if (lane == 0) { w.leaf_f[nleaf] = static_cast<uint16_t>(f); w.leaf_l[nleaf] = static_cast<uint16_t>(l); }
+                ++nleaf;
+            }
+            continue;
+        }
+        if (d == 0) {
+            if (lane == 0) heap_sort_range(w.buf + f, m);
+            __syncwarp();
+            continue;
+        }
+        if (lane == 0) median_to_first(w.buf, f, l);
+        __syncwarp();
+        const int32_t pivot = skey(w.buf[f]);
+        uint32_t nL = 0, nR = 0;
+        for (uint32_t base = f + 1; base < l; base += 32) {
+            const uint32_t p = base + lane;
+            const bool in = p < l;
+            const int32_t k = in ? skey(w.buf[p]) : 0;
+            const bool isL = in && is_lstop(k, pivot), isR = in && is_rstop(k, pivot);
+            const unsigned bL = __ballot_sync(full, isL), bR = __ballot_sync(full, isR);
+            if (isL) w.A[nL + __popc(bL & lt)] = p;
+            if (isR) w.R[nR + __popc(bR & lt)] = p;  // left to right; B[k] = R[nR - 1 - k]
+            nL += __popc(bL);
+            nR += __popc(bR);
+        }
+        __syncwarp();
+        if (nL == 0 || nR == 0) {  // the median move guarantees both kinds of stop
+            if (lane == 0) ss.counters[5] = 1;  // the host reports the sort as failed
+            continue;
+        }
+        const uint32_t mn = nL < nR ? nL : nR;
+        uint32_t K = mn;  // the first k with !(A[k] < B[k]), else min(nL, nR)
+        for (uint32_t c = 0; c < mn; c += 32) {
+            const uint32_t k = c + lane;
+            const unsigned b = __ballot_sync(full, k < mn && !(w.A[k] < w.R[nR - 1u - k]));
+            if (b) {
+                K = c + static_cast<uint32_t>(__ffs(b) - 1);
+                break;
+            }
+        }
+        uint32_t cut;
+        if (K == 0) {
+            cut = w.A[0];
+        } else {
+            const uint32_t bk = w.R[nR - K];  // B[K-1]
+            cut = (K < nL && w.A[K] < bk) ? w.A[K] : bk;
+        }
+        for (uint32_t k = lane; k < K; k += 32) sswap(w.buf, w.A[k], w.R[nR - 1u - k]);
+        __syncwarp();
+        if (lane == 0 && sp + 2 <= 64) {
+            w.st_f[sp] = cut; w.st_l[sp] = l; w.st_d[sp] = d - 1;
+            w.st_f[sp + 1] = f; w.st_l[sp + 1] = cut; w.st_d[sp + 1] = d - 1;
+        }
+        sp = sp + 2 <= 64 ? sp + 2 : sp;
+        __syncwarp();
+    }
+    __syncwarp();
+    for (uint32_t i = lane; i < nleaf; i += 32) leaf_sort(w.buf, w.leaf_f[i], w.leaf_l[i]);
+    __syncwarp();
+    for (uint32_t i = lane; i < len; i += 32) ss.a[first + i] = w.buf[i];
 }
 __global__ void k_sort_heaps(SortScratch ss, uint32_t count) {
     PTL_FOR(k, count) heap_sort_range(ss.a + ss.heap[2 * k], ss.heap[2 * k + 1] - ss.heap[2 * k]);
@@ -796,11 +879,11 @@ cudaError_t run_sort_rounds(const SortScratch& ss, uint32_t nseg0, uint32_t firs
     if (lh[1]) { g_launches++; k_sort_heaps<<<grid_for(lh[1]), kThreads, 0, s>>>(ss, lh[1]); }
     if (lh[0]) { g_launches++; k_sort_leaves<<<grid_for(lh[0]), kThreads, 0, s>>>(ss, lh[0]); }
     if (lh[4]) {
-        const size_t smem = static_cast<size_t>(kSortLocalThreads) * kSortLocal * sizeof(unsigned long long);
+        const size_t smem = static_cast<size_t>(kSortLocalWarps) * sizeof(LocalWarpSmem);
         e = cudaFuncSetAttribute(k_sort_local, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
         if (e != cudaSuccess) return e;
         g_launches++;
-        k_sort_local<<<(lh[4] + kSortLocalThreads - 1) / kSortLocalThreads, kSortLocalThreads, smem, s>>>(ss, lh[4]);
+        k_sort_local<<<(lh[4] + kSortLocalWarps - 1) / kSortLocalWarps, kSortLocalWarps * 32, smem, s>>>(ss, lh[4]);
     }
     if (rounds_out) *rounds_out = rounds;
     return cudaGetLastError();
