@@ -371,7 +371,7 @@ __device__ void sort_emit(SortScratch ss, SortSeg* next, uint32_t first, uint32_
         }
         return;
     }
-    if (dl > 0 && last - first <= kSortLocal) {  // finishes in one thread after the rounds
+    if (dl > 0 && last - first <= kSortLocal) {  // finishes in one warp after the rounds
         const uint32_t k = atomicAdd(&ss.counters[6], 1u);
         if (k < ss.seg_cap) { ss.local[3 * k] = first; ss.local[3 * k + 1] = last; ss.local[3 * k + 2] = dl; }
         else ss.counters[5] = 1;
@@ -445,6 +445,7 @@ struct LocalWarpSmem {
     uint32_t A[kSortLocal], R[kSortLocal];
     uint32_t st_f[64], st_l[64], st_d[64];
     uint16_t leaf_f[kSortLocal / 2], leaf_l[kSortLocal / 2];
+    static_assert(kSortLocal <= 65535, "leaf bounds are 16-bit");
 };
 
 __global__ void __launch_bounds__(kSortLocalWarps * 32) k_sort_local(SortScratch ss, uint32_t count) {

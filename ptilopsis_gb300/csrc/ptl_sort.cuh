@@ -151,10 +151,11 @@ PTL_HD void leaf_sort(Arr a, uint32_t first, uint32_t last) {
     }
 }
 
-// ---- small ranges in one thread
-// Ranges of at most kSortLocal elements with depth budget left finish in one thread: the
-// same steps as the rounds above, taken sequentially (they touch only their own range).
-constexpr uint32_t kSortLocal = 256;
+// ---- small ranges
+// Ranges of at most kSortLocal elements with depth budget left finish without further
+// rounds (they touch only their own range): one warp each on the device (k_sort_local),
+// and local_introsort below, the same steps taken sequentially, in the host model.
+constexpr uint32_t kSortLocal = 512;
 
 // An array view with a stride (element i at base[i * stride]).
 struct Strided {
