@@ -306,7 +306,7 @@ def run_batched(args):
     for _ in range(args.warmup):
         bc.compile(trees)
     barrier()
-    dev_ms, wall_ms, stage_sum = [], [], np.zeros(7)
+    dev_ms, wall_ms, stage_sum, host_parts = [], [], np.zeros(7), np.zeros(3)
     launches0 = kernel_launches()
     with ClockSampler(local) as clocks:
         for _ in range(args.steps):
@@ -315,6 +315,8 @@ def run_batched(args):
             wall_ms.append(1000.0 * (time.perf_counter() - t0))
             ns = np.array(bc.stage_ns(), dtype=np.float64)
             stage_sum += ns
+            hp = bc.host_ns()
+            host_parts += np.array([hp["gather_ns"], hp["h2d_ns"], hp["d2h_ns"]], dtype=np.float64)
             dev_ms.append(ns.sum() / 1e6)
         barrier()
     launches = (kernel_launches() - launches0) // args.steps
@@ -322,8 +324,11 @@ def run_batched(args):
     e2e_ms = max_over_ranks(float(np.mean(wall_ms)))
     h2d, d2h = bc.copied_bytes()
     value = world * nodes / (ms / 1000.0)
+    hp_ms = host_parts / 1e6 / args.steps
     e2e = {"value": world * nodes / (e2e_ms / 1000.0), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
-           "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_ms}
+           "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_ms,
+           "parts_ms": {"gather_inputs": round(float(hp_ms[0]), 2), "h2d": round(float(hp_ms[1]), 2),
+                        "pipeline": round(float(np.mean(dev_ms)), 2), "d2h": round(float(hp_ms[2]), 2)}}
 
     # per-program sizes for the algorithmic bytes
     tot = {"n": 0, "W": 0, "W2": 0, "W3": 0}

@@ -167,6 +167,9 @@ ptl_status ptl_batch_stage_ns(const ptl_batch* batch, uint64_t ns[7]);
 ptl_status ptl_batch_copied_bytes(const ptl_batch* batch, uint64_t* h2d, uint64_t* d2h);
 /* Detail of the last batch-wide failure. */
 const char* ptl_batch_last_error(const ptl_batch* batch);
+/* Host-side parts of the last compile, ns: gathering the inputs into pinned memory, the
+ * input copy and the output copy (both device-timed). */
+ptl_status ptl_batch_host_ns(const ptl_batch* batch, uint64_t ns[3]);
 void ptl_batch_destroy(ptl_batch* batch);
 
 /* ---- Compile server.  No counterpart in the reference.  Continuous batching over

@@ -33,6 +33,7 @@ def _bind(L):
     L.ptl_batch_elapsed_ns.restype = u64
     L.ptl_batch_stage_ns.argtypes = [vp, ctypes.POINTER(u64)]
     L.ptl_batch_sizes.argtypes = [vp, sz, ctypes.POINTER(u64)]
+    L.ptl_batch_host_ns.argtypes = [vp, ctypes.POINTER(u64)]
     L.ptl_batch_copied_bytes.argtypes = [vp, ctypes.POINTER(u64), ctypes.POINTER(u64)]
     L.ptl_batch_last_error.argtypes = [vp]
     L.ptl_batch_last_error.restype = ctypes.c_char_p
@@ -51,7 +52,7 @@ def _bind(L):
     L.ptl_clock_ns.argtypes = []
     L.ptl_clock_ns.restype = u64
     for fn in ("ptl_batch_create", "ptl_batch_compile", "ptl_batch_status", "ptl_batch_words", "ptl_batch_stage_ns",
-               "ptl_batch_copied_bytes", "ptl_batch_sizes",
+               "ptl_batch_copied_bytes", "ptl_batch_sizes", "ptl_batch_host_ns",
                "ptl_batch_function_table", "ptl_server_create", "ptl_server_submit", "ptl_server_poll",
                "ptl_server_result", "ptl_server_times", "ptl_server_release", "ptl_server_stats"):
         getattr(L, fn).restype = ctypes.c_int
@@ -115,6 +116,12 @@ class BatchCompiler:
         if st != 0:
             raise PtlError(st, f"ptl_batch_sizes({k})")
         return {"n": int(v[0]), "W": int(v[1]), "W2": int(v[2]), "W3": int(v[3])}
+
+    def host_ns(self) -> dict:
+        """Host-side parts of the last compile: input gather, input copy, output copy."""
+        v = (ctypes.c_uint64 * 3)()
+        self._lib.ptl_batch_host_ns(self._h, v)
+        return {"gather_ns": int(v[0]), "h2d_ns": int(v[1]), "d2h_ns": int(v[2])}
 
     def copied_bytes(self) -> tuple:
         a, b = ctypes.c_uint64(), ctypes.c_uint64()

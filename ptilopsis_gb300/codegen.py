@@ -160,21 +160,32 @@ def _ptr(a) -> int:
     return a.data_ptr()
 
 
+_FIELDS = (("type", np.dtype(np.uint8)), ("rtype", np.dtype(np.uint8)), ("parent", np.dtype(np.int32)),
+           ("depth", np.dtype(np.int32)), ("child_idx", np.dtype(np.int32)), ("data", np.dtype(np.uint32)))
+
+
 def _view(tree: DepthTree, keep: list) -> _AstView:
-    v = _AstView()
-    v.n = tree.n
-    v.max_depth = int(tree.max_depth)
+    """The C view of a tree.  It is kept on the tree and reused while the tree holds the
+    same six array objects and max_depth (a view holds pointers, not contents)."""
+    arrs = (tree.type, tree.rtype, tree.parent, tree.depth, tree.child_idx, tree.data)
+    cached = tree.__dict__.get("_ptl_view")
+    if cached is not None and cached[2] == tree.max_depth and all(x is y for x, y in zip(cached[0], arrs)):
+        keep.append(cached)
+        return cached[1]
     on_dev = tree.on_device
-    arrays = []
-    for name, dt in (("type", np.uint8), ("rtype", np.uint8), ("parent", np.int32), ("depth", np.int32),
-                     ("child_idx", np.int32), ("data", np.uint32)):
-        a = getattr(tree, name)
-        if not on_dev:
-            a = np.ascontiguousarray(a, dt)
-        keep.append(a)
-        arrays.append(_ptr(a))
-    v.type, v.rtype, v.parent, v.depth, v.child_idx, v.data = arrays
-    v.on_device = 1 if on_dev else 0
+    held, ptrs = [], []
+    for a, (_, dt) in zip(arrs, _FIELDS):
+        if on_dev:
+            ptrs.append(a.data_ptr())
+        else:
+            if not (type(a) is np.ndarray and a.dtype == dt and a.flags.c_contiguous):
+                a = np.ascontiguousarray(a, dt)
+            ptrs.append(a.__array_interface__["data"][0])
+        held.append(a)
+    v = _AstView(int(arrs[0].shape[0]), int(tree.max_depth), *ptrs, 1 if on_dev else 0)
+    entry = (arrs, v, tree.max_depth, held)
+    tree.__dict__["_ptl_view"] = entry
+    keep.append(entry)
     return v
 
 

@@ -134,6 +134,12 @@ extern "C" ptl_status ptl_batch_copied_bytes(const ptl_batch* b, uint64_t* h2d, 
 
 extern "C" const char* ptl_batch_last_error(const ptl_batch* b) { return b ? b->pipe->last_error() : ""; }
 
+extern "C" ptl_status ptl_batch_host_ns(const ptl_batch* b, uint64_t ns[3]) {
+    if (!b || !ns) return PTL_BAD_ARGUMENT;
+    b->pipe->host_ns(ns);
+    return PTL_OK;
+}
+
 extern "C" void ptl_batch_destroy(ptl_batch* b) { delete b; }
 
 // ===================================================================== server

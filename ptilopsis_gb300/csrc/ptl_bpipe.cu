@@ -13,11 +13,14 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
+#include <chrono>
 #include <cstring>
 #include <mutex>
 #include <new>
 #include <string>
 #include <thread>
+#include <tuple>
 #include <vector>
 
 #include "ptl_bpipe.h"
@@ -117,6 +120,8 @@ public:
     int threads = 8;
     cudaStream_t s = nullptr;
     cudaEvent_t ev[8] = {};
+    cudaEvent_t ev_in = nullptr, ev_out0 = nullptr, ev_out1 = nullptr;  // input copy start, output copy
+    uint64_t hns[3] = {0, 0, 0};
     uint64_t ns[7] = {0, 0, 0, 0, 0, 0, 0};
     uint64_t h2d = 0, d2h = 0;
     std::string err_text;
@@ -144,6 +149,8 @@ public:
         h_small.release();
         for (auto& e : ev)
             if (e) cudaEventDestroy(e);
+        for (cudaEvent_t e : {ev_in, ev_out0, ev_out1})
+            if (e) cudaEventDestroy(e);
         if (s) cudaStreamDestroy(s);
     }
     std::vector<DBuf*> all() {
@@ -169,6 +176,9 @@ public:
         if (b) *b = d2h;
     }
     const char* last_error() const override { return err_text.c_str(); }
+    void host_ns(uint64_t out_ns[3]) const override {
+        for (int k = 0; k < 3; ++k) out_ns[k] = hns[k];
+    }
 
     // Zeroed family of per-program arrays.
     cudaError_t family(const Layout& L, std::initializer_list<DBuf*> bufs, size_t es) {
@@ -271,6 +281,9 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
     }
     for (auto& e : ev)
         if (!e) BP_CU(cudaEventCreate(&e));
+    for (cudaEvent_t* e : {&ev_in, &ev_out0, &ev_out1})
+        if (!*e) BP_CU(cudaEventCreate(e));
+    for (auto& x : hns) x = 0;
 
     // ---- small per-program state and the pinned small area
     constexpr int kTables = 20, kLists = 4;  // table slots 0..16 are used
@@ -299,28 +312,58 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
         BP_CU(cudaStreamSynchronize(s));
     }
 
-    // ---- inputs: gathered into pinned memory by host threads, one copy per field
+    // ---- inputs: gathered into pinned memory by host threads, one copy per field and
+    // chunk; a chunk's copies start as soon as its programs are gathered, so the copy
+    // engine runs under the gather of the next chunks
     {
-        std::vector<uint64_t> din(B);
+        std::vector<uint64_t> din(B + 1);
         uint64_t o = 0;
         for (size_t p = 0; p < B; ++p) {
             din[p] = o;
             if (active[p]) o += n[p];
         }
+        din[B] = o;
         const uint64_t cap = std::max<uint64_t>(o, 1);
         const size_t bytes = cap * (1 + 1 + 4 + 4 + 4 + 4);
         BP_CU(h_in.ensure(bytes));
+        BP_CU(in_type.ensure(cap));
+        BP_CU(in_rtype.ensure(cap));
+        BP_CU(in_parent.ensure(cap * 4));
+        BP_CU(in_depth.ensure(cap * 4));
+        BP_CU(in_child.ensure(cap * 4));
+        BP_CU(in_data.ensure(cap * 4));
         uint8_t* ht = h_in.at<uint8_t>();
         uint8_t* hr = ht + cap;
         int32_t* hpar = reinterpret_cast<int32_t*>(hr + cap);
         int32_t* hdep = hpar + cap;
         int32_t* hch = hdep + cap;
         uint32_t* hdat = reinterpret_cast<uint32_t*>(hch + cap);
+        // chunks of about o / kInChunks nodes, cut at program boundaries
+        constexpr size_t kInChunks = 8;
+        std::vector<size_t> cfirst{0};
+        std::vector<uint32_t> chunk_of(B);
+        for (size_t p = 0; p < B; ++p) {
+            const size_t c = cfirst.size() - 1;
+            chunk_of[p] = static_cast<uint32_t>(c);
+            if (p + 1 < B && cfirst.size() < kInChunks && din[p + 1] * kInChunks >= o * cfirst.size())
+                cfirst.push_back(p + 1);
+        }
+        const size_t C = cfirst.size();
+        cfirst.push_back(B);
+        std::vector<std::atomic<uint32_t>> left(C);
+        for (size_t c = 0; c < C; ++c) {
+            uint32_t k = 0;
+            for (size_t p = cfirst[c]; p < cfirst[c + 1]; ++p) k += active[p] ? 1u : 0u;
+            left[c].store(k, std::memory_order_relaxed);
+        }
+        std::atomic<size_t> next{0};
+        const auto g0 = std::chrono::steady_clock::now();
         const int nt_ = std::max(1, std::min<int>(threads, static_cast<int>(B)));
         std::vector<std::thread> pool;
         for (int w = 0; w < nt_; ++w) {
-            pool.emplace_back([&, w] {
-                for (size_t p = static_cast<size_t>(w); p < B; p += static_cast<size_t>(nt_)) {
+            pool.emplace_back([&] {
+                for (size_t p = next.fetch_add(1, std::memory_order_relaxed); p < B;
+                     p = next.fetch_add(1, std::memory_order_relaxed)) {
                     if (!active[p]) continue;
                     const ptl_ast_view& t = trees[p];
                     const uint64_t d = din[p];
@@ -330,22 +373,31 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
                     std::memcpy(hdep + d, t.depth, 4 * n[p]);
                     std::memcpy(hch + d, t.child_idx, 4 * n[p]);
                     std::memcpy(hdat + d, t.data, 4 * n[p]);
+                    left[chunk_of[p]].fetch_sub(1, std::memory_order_release);
                 }
             });
         }
+        // every program is gathered by some worker, so each chunk's count reaches zero
+        cudaError_t ce = cudaEventRecord(ev_in, s);
+        for (size_t c = 0; c < C && ce == cudaSuccess; ++c) {
+            while (left[c].load(std::memory_order_acquire) != 0) std::this_thread::yield();
+            const uint64_t a = din[cfirst[c]], m = din[cfirst[c + 1]] - a;
+            if (m == 0) continue;
+            for (auto [dst, src, w] : {std::tuple<void*, const void*, uint64_t>{in_type.p, ht, 1},
+                                       {in_rtype.p, hr, 1},
+                                       {in_parent.p, hpar, 4},
+                                       {in_depth.p, hdep, 4},
+                                       {in_child.p, hch, 4},
+                                       {in_data.p, hdat, 4}}) {
+                ce = cudaMemcpyAsync(static_cast<uint8_t*>(dst) + w * a, static_cast<const uint8_t*>(src) + w * a,
+                                     w * m, cudaMemcpyHostToDevice, s);
+                if (ce != cudaSuccess) break;
+            }
+        }
         for (auto& t : pool) t.join();
-        BP_CU(in_type.ensure(cap));
-        BP_CU(in_rtype.ensure(cap));
-        BP_CU(in_parent.ensure(cap * 4));
-        BP_CU(in_depth.ensure(cap * 4));
-        BP_CU(in_child.ensure(cap * 4));
-        BP_CU(in_data.ensure(cap * 4));
-        BP_CU(cudaMemcpyAsync(in_type.p, ht, o, cudaMemcpyHostToDevice, s));
-        BP_CU(cudaMemcpyAsync(in_rtype.p, hr, o, cudaMemcpyHostToDevice, s));
-        BP_CU(cudaMemcpyAsync(in_parent.p, hpar, 4 * o, cudaMemcpyHostToDevice, s));
-        BP_CU(cudaMemcpyAsync(in_depth.p, hdep, 4 * o, cudaMemcpyHostToDevice, s));
-        BP_CU(cudaMemcpyAsync(in_child.p, hch, 4 * o, cudaMemcpyHostToDevice, s));
-        BP_CU(cudaMemcpyAsync(in_data.p, hdat, 4 * o, cudaMemcpyHostToDevice, s));
+        hns[0] = static_cast<uint64_t>(std::chrono::duration_cast<std::chrono::nanoseconds>(
+                                           std::chrono::steady_clock::now() - g0).count());
+        BP_CU(ce);
         h2d += 18 * o;
         BP_CU(cudaEventRecord(ev[0], s));  // stage times start with the inputs on the device
 
@@ -776,6 +828,7 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
         // ---- results: the output words and function tables of every program, one copy each
         BP_CU(h_out.ensure(Lo.total * 4));
         BP_CU(h_fn.ensure(Lf.total * 4 * 4));
+        BP_CU(cudaEventRecord(ev_out0, s));
         BP_CU(cudaMemcpyAsync(h_out.p, out.p, Lo.total * 4, cudaMemcpyDeviceToHost, s));
         uint32_t* hf = h_fn.at<uint32_t>();
         BP_CU(cudaMemcpyAsync(hf, fn_start.p, Lf.total * 4, cudaMemcpyDeviceToHost, s));
@@ -783,6 +836,7 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
         BP_CU(cudaMemcpyAsync(hf + 2 * Lf.total, fn_size.p, Lf.total * 4, cudaMemcpyDeviceToHost, s));
         BP_CU(cudaMemcpyAsync(hf + 3 * Lf.total, fn_id.p, Lf.total * 4, cudaMemcpyDeviceToHost, s));
         d2h += Lo.total * 4 + 4 * Lf.total * 4;
+        BP_CU(cudaEventRecord(ev_out1, s));
         BP_CU(collect_errors());
         for (size_t p = 0; p < B; ++p) {
             BatchResult& r = res[p];
@@ -805,6 +859,8 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
             if (cudaEventElapsedTime(&ms, ev[k], ev[k + 1]) == cudaSuccess) ns[k] = static_cast<uint64_t>(ms * 1e6);
         }
         ns[6] = 0;  // postprocess is fused into fix_jumps
+        if (cudaEventElapsedTime(&ms, ev_in, ev[0]) == cudaSuccess) hns[1] = static_cast<uint64_t>(ms * 1e6);
+        if (cudaEventElapsedTime(&ms, ev_out0, ev_out1) == cudaSuccess) hns[2] = static_cast<uint64_t>(ms * 1e6);
     }
     return PTL_OK;
 }

@@ -33,6 +33,9 @@ public:
     virtual void stage_ns(uint64_t ns[7]) const = 0;
     // Host-to-device and device-to-host bytes of the last compile.
     virtual void copied_bytes(uint64_t* h2d, uint64_t* d2h) const = 0;
+    // Host-side parts of the last compile, ns: gathering the inputs into pinned memory,
+    // the input copy, the output copy (device-timed).
+    virtual void host_ns(uint64_t ns[3]) const = 0;
     // Detail of the last failure.
     virtual const char* last_error() const = 0;
 };
