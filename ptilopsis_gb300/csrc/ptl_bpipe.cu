@@ -135,7 +135,7 @@ public:
     DBuf ni, nrd, nr1, nr2, njt, fsz, joffs, out;
     DBuf errw, flags, meta, progs, tabs, lists, changed, sort_err, seen_off, a_off, dirty, ra_sync;
     DBuf sa, sapos, sbpos, seg0, seg1, tile_seg, tile_l, tile_r, leaf, heap, counters, scan_status, scan_counter,
-        sort_local;
+        sort_local, sort_equal;
     PBuf h_in, h_out, h_fn, h_small;
 
     std::vector<uint8_t> active;
@@ -160,7 +160,7 @@ public:
                 &symswp, &stamp, &spill, &roffs, &owner, &used, &smark, &defpos, &trig_min, &trig_max, &ra_chunks, &ni, &nrd,
                 &nr1, &nr2, &njt, &fsz, &joffs, &out, &errw, &flags, &meta, &progs, &tabs, &lists, &changed,
                 &sort_err, &seen_off, &a_off, &dirty, &ra_sync, &sa, &sapos, &sbpos, &seg0, &seg1, &tile_seg, &tile_l, &tile_r,
-                &leaf, &heap, &counters, &scan_status, &scan_counter, &sort_local};
+                &leaf, &heap, &counters, &scan_status, &scan_counter, &sort_local, &sort_equal};
     }
 
     ptl_status cuda_fail(cudaError_t e, const char* what) {
@@ -293,7 +293,7 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
     small_list_off = small_err_off + B * sizeof(ErrorWord);
     small_up_off = small_list_off + static_cast<size_t>(kLists) * (B + 1) * 4;  // 8-byte aligned
     small_up_off = (small_up_off + 15) & ~size_t(15);
-    BP_CU(h_small.ensure(small_up_off + B * (8 + 8 + sizeof(SortSeg) + 8 + 4) + 64));
+    BP_CU(h_small.ensure(small_up_off + B * (8 + 8 + sizeof(SortSeg) + 8 + 12) + 64));
     BP_CU(tabs.ensure(static_cast<size_t>(kTables) * (B + 1) * 4));
     BP_CU(lists.ensure(static_cast<size_t>(kLists) * (B + 1) * 4));
     BP_CU(progs.ensure(B * sizeof(Prog)));
@@ -568,7 +568,7 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
         std::vector<uint64_t> aoff(B);
         uint64_t at = 0, seg_cap = 16, tile_cap = 16, leaf_cap = 16;
         std::vector<SortSeg> segs;
-        std::vector<uint32_t> leaves;
+        std::vector<uint32_t> leaves, blocks;
         for (size_t p = 0; p < B; ++p) {
             aoff[p] = at;
             if (!active[p]) continue;
@@ -576,7 +576,7 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
             seg_cap += np / 17 + 16;
             tile_cap += np / 2048 + np / 17 + 16;
             leaf_cap += np / 2 + 16;
-            if (np > 16) {
+            if (np > kSortBlock) {
                 SortSeg g{};
                 g.first = static_cast<uint32_t>(at);
                 g.last = static_cast<uint32_t>(at + np);
@@ -585,6 +585,10 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
                 const uint32_t lg = floor_log2(static_cast<uint32_t>(np));
                 min_lg = std::min(min_lg, lg);
                 max_lg = std::max(max_lg, lg);
+            } else if (np > kSortThreshold) {  // one block sorts the whole program
+                blocks.push_back(static_cast<uint32_t>(at));
+                blocks.push_back(static_cast<uint32_t>(at + np));
+                blocks.push_back(2u * floor_log2(static_cast<uint32_t>(np)));
             } else if (np > 1) {
                 leaves.push_back(static_cast<uint32_t>(at));
                 leaves.push_back(static_cast<uint32_t>(at + np));
@@ -604,6 +608,7 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
         BP_CU(heap.ensure(2 * leaf_cap * 4));
         BP_CU(counters.ensure(64));
         BP_CU(sort_local.ensure(3 * seg_cap * 4));
+        BP_CU(sort_equal.ensure(2 * seg_cap * 4));
         BP_CU(a_off.ensure(B * 8));
         uint64_t* up_aoff = reinterpret_cast<uint64_t*>(h_small.at<uint8_t>(small_up_off + B * 8));
         std::copy(aoff.begin(), aoff.end(), up_aoff);
@@ -624,12 +629,21 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
         ss.leaf_cap = static_cast<uint32_t>(leaf_cap);
         ss.counters = counters.at<uint32_t>();
         ss.local = sort_local.at<uint32_t>();
+        ss.equal = sort_equal.at<uint32_t>();
         const uint32_t t_n2 = tiles(4, n, batch_tile());
         batch_sort_keys(bl(4), t_n2, sa.at<unsigned long long>(), a_off.at<uint64_t>(), false);
         BP_CU(cudaMemsetAsync(counters.p, 0, 64, s));
         SortSeg* up_segs = reinterpret_cast<SortSeg*>(h_small.at<uint8_t>(small_up_off + 2 * B * 8));
         uint32_t* up_leaves = reinterpret_cast<uint32_t*>(h_small.at<uint8_t>(small_up_off + 2 * B * 8 + B * sizeof(SortSeg)));
         uint32_t* up_nl = up_leaves + 2 * B;
+        uint32_t* up_blocks = up_nl + 4;
+        uint32_t* up_nb = up_blocks + 3 * B;
+        if (!blocks.empty()) {
+            std::copy(blocks.begin(), blocks.end(), up_blocks);
+            *up_nb = static_cast<uint32_t>(blocks.size() / 3);
+            BP_CU(cudaMemcpyAsync(sort_local.p, up_blocks, blocks.size() * 4, cudaMemcpyHostToDevice, s));
+            BP_CU(cudaMemcpyAsync(counters.at<uint32_t>(6), up_nb, 4, cudaMemcpyHostToDevice, s));
+        }
         if (!segs.empty()) {
             std::copy(segs.begin(), segs.end(), up_segs);
             BP_CU(cudaMemcpyAsync(seg0.p, up_segs, segs.size() * sizeof(SortSeg), cudaMemcpyHostToDevice, s));
@@ -641,7 +655,8 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
             BP_CU(cudaMemcpyAsync(counters.at<uint32_t>(2), up_nl, 4, cudaMemcpyHostToDevice, s));
         }
         uint32_t rounds = 0;
-        BP_CU(run_sort_rounds(ss, static_cast<uint32_t>(segs.size()), min_lg > 9 ? min_lg - 9 : 1, 2 * max_lg + 4,
+        const uint32_t lb = floor_log2(kSortBlock);
+        BP_CU(run_sort_rounds(ss, static_cast<uint32_t>(segs.size()), min_lg > lb ? min_lg - lb : 1, 2 * max_lg + 4,
                               sort_err.at<ErrorWord>(), s, &rounds));
         batch_sort_keys(bl(4), t_n2, sa.at<unsigned long long>(), a_off.at<uint64_t>(), true);
         batch_stage(BatchStage::Gen, bl(4), t_n2, nullptr, nullptr, nullptr);

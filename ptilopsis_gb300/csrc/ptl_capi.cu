@@ -117,7 +117,7 @@ struct ptl_generator {
     DevBuf symreg, symswp, stamp, defpos, lifetime, trig_min, trig_max, ra_chunks, spill, roffs;
     DevBuf ni, nrd, nr1, nr2, njt, fsz, joffs, out;
     DevBuf sort_a, sort_apos, sort_bpos, sort_seg0, sort_seg1, sort_tile_seg, sort_tile_l, sort_tile_r,
-        sort_leaf, sort_heap, sort_counters, sort_local;
+        sort_leaf, sort_heap, sort_counters, sort_local, sort_equal;
     DevBuf scan_status, scan_counter, meta, flags, errw, tables, depth_seen;
 
     // results
@@ -139,7 +139,7 @@ struct ptl_generator {
                 &instr, &rd, &rs1, &rs2, &jt, &owner, &used, &smark, &used_instrs, &symreg, &symswp,
                 &stamp, &defpos, &lifetime, &trig_min, &trig_max, &ra_chunks, &spill, &roffs, &ni, &nrd, &nr1, &nr2, &njt,
                 &fsz, &joffs, &out, &sort_a, &sort_apos, &sort_bpos, &sort_seg0, &sort_seg1,
-                &sort_tile_seg, &sort_tile_l, &sort_tile_r, &sort_leaf, &sort_heap, &sort_counters, &sort_local,
+                &sort_tile_seg, &sort_tile_l, &sort_tile_r, &sort_leaf, &sort_heap, &sort_counters, &sort_local, &sort_equal,
                 &scan_status, &scan_counter, &meta, &flags, &errw, &tables, &depth_seen};
     }
 };
@@ -399,6 +399,7 @@ ptl_status run_pipeline(ptl_generator* g, bool profile, bool to_host, bool row0_
     PTL_CU(g->sort_heap.ensure(2 * leaf_cap, 4));
     PTL_CU(g->sort_counters.ensure(8, 4));
     PTL_CU(g->sort_local.ensure(3 * seg_cap, 4));
+    PTL_CU(g->sort_equal.ensure(2 * seg_cap, 4));
     SortScratch ss{};
     ss.a = g->sort_a.at<unsigned long long>();
     ss.apos = g->sort_apos.at<uint32_t>();
@@ -415,6 +416,7 @@ ptl_status run_pipeline(ptl_generator* g, bool profile, bool to_host, bool row0_
     ss.leaf_cap = static_cast<uint32_t>(leaf_cap);
     ss.counters = g->sort_counters.at<uint32_t>();
     ss.local = g->sort_local.at<uint32_t>();
+    ss.equal = g->sort_equal.at<uint32_t>();
 
     const size_t wb8 = r8(g->W);
     for (DevBuf* b : {&g->instr, &g->rd, &g->rs1, &g->rs2, &g->jt, &g->used_instrs, &g->symreg, &g->symswp,

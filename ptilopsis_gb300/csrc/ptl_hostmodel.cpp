@@ -90,26 +90,29 @@ struct Model {
         std::vector<uint32_t> apos(n), bpos(n);
         std::vector<SortSeg> cur, next;
         std::vector<std::pair<uint32_t, uint32_t>> leaves, heaps;
-        if (n > kSortThreshold) {
-            SortSeg g{};
-            g.first = 0; g.last = n; g.dl = 2u * floor_log2(n);
-            cur.push_back(g);
-        } else if (n > 1) {
-            leaves.push_back({0, n});
-        }
         std::vector<std::array<uint32_t, 3>> locals;
-        auto emit = [&](uint32_t first, uint32_t last, uint32_t dl) {
+        std::vector<std::pair<uint32_t, uint32_t>> equal;
+        auto emit = [&](uint32_t first, uint32_t last, uint32_t dl, bool eq) {
+            if (eq && last - first <= kSortThreshold) return;  // a stable sort of equal keys
+            if (eq && dl >= equal_levels(last - first)) { equal.push_back({first, last}); return; }
             if (last - first <= kSortThreshold) { if (last - first > 1) leaves.push_back({first, last}); return; }
-            if (dl > 0 && last - first <= kSortLocal) { locals.push_back({first, last, dl}); return; }
+            if (dl > 0 && last - first <= kSortBlock) { locals.push_back({first, last, dl}); return; }
             if (dl == 0) { heaps.push_back({first, last}); return; }
             SortSeg c{}; c.first = first; c.last = last; c.dl = dl;
             next.push_back(c);
         };
+        if (n > 1) emit(0, n, 2u * floor_log2(n), false);  // the whole array: rounds, or one block
+        cur.swap(next);
         while (!cur.empty()) {
             next.clear();
             for (SortSeg& g : cur) {
                 median_to_first(a.data(), g.first, g.last);
                 g.pivot = skey(a[g.first]);
+                g.kmin = g.kmax = g.pivot;
+                for (uint32_t p = g.first + 1; p < g.last; ++p) {
+                    g.kmin = std::min(g.kmin, skey(a[p]));
+                    g.kmax = std::max(g.kmax, skey(a[p]));
+                }
                 uint32_t nl = 0, nr_total = 0;
                 for (uint32_t p = g.first + 1; p < g.last; ++p) nr_total += is_rstop(skey(a[p]), g.pivot);
                 uint32_t rl = 0;
@@ -123,8 +126,8 @@ struct Model {
                 g.K = partition_k(apos.data() + g.first, bpos.data() + g.first, g.nL, g.nR);
                 g.cut = partition_cut(apos.data() + g.first, bpos.data() + g.first, g.nL, g.K);
                 for (uint32_t k = 0; k < g.K; ++k) sswap(a.data(), apos[g.first + k], bpos[g.first + k]);
-                emit(g.first, g.cut, g.dl - 1);
-                emit(g.cut, g.last, g.dl - 1);
+                emit(g.first, g.cut, g.dl - 1, g.kmin == g.pivot);
+                emit(g.cut, g.last, g.dl - 1, g.kmax == g.pivot);
             }
             cur.swap(next);
         }
@@ -136,6 +139,12 @@ struct Model {
             for (uint32_t i = 0; i < r[1] - r[0]; ++i) sb[i] = a[r[0] + i];
             local_introsort(sb, 0u, r[1] - r[0], r[2]);
             for (uint32_t i = 0; i < r[1] - r[0]; ++i) a[r[0] + i] = sb[i];
+        }
+        for (auto& r : equal) {  // one block per range on the device, through apos
+            const uint32_t m = r.second - r.first;
+            for (uint32_t i = 0; i < m; ++i) apos[r.first + equal_final_index(i, m)] = sidx(a[r.first + i]);
+            const unsigned long long key = a[r.first] & 0xFFFFFFFF00000000ull;
+            for (uint32_t i = 0; i < m; ++i) a[r.first + i] = key | apos[r.first + i];
         }
         for (uint32_t p = 0; p < n; ++p) pos.p[sidx(a[p])] = p;
     }

@@ -225,6 +225,7 @@ __global__ void k_sort_tiles(SortScratch ss, const SortSeg* cur, SortSeg* curw) 
         SortSeg g = cur[s];
         median_to_first(ss.a, g.first, g.last);
         g.pivot = skey(ss.a[g.first]);
+        g.kmin = g.kmax = g.pivot;  // k_sort_count folds in the other keys
         const uint32_t m1 = g.last - g.first - 1;
         g.tcount = (m1 + kSortTile - 1) / kSortTile;
         g.tbase = atomicAdd(&ss.counters[0], g.tcount);
@@ -252,25 +253,43 @@ __device__ __forceinline__ uint32_t block_reduce_add(uint32_t v, uint32_t* sm) {
 
 constexpr uint32_t kSortItems = kSortTile / kThreads;  // 8 per thread
 
-__global__ void __launch_bounds__(kThreads) k_sort_count(SortScratch ss, const SortSeg* cur) {
+// Stop counts per tile, and the least and greatest key of each segment (atomics on the
+// segment record; a part of the next split is known to hold one key when its bound on
+// the pivot's side meets the pivot).
+__global__ void __launch_bounds__(kThreads) k_sort_count(SortScratch ss, SortSeg* cur) {
     __shared__ uint32_t sm[kThreads / 32];
+    __shared__ int32_t smn[kThreads / 32], smx[kThreads / 32];
     if (sort_overflow(ss)) return;
     const uint32_t ntiles = sort_ntiles(ss);
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
-        const SortSeg g = cur[ss.tile_seg[t]];
+        const uint32_t si = ss.tile_seg[t];
+        const SortSeg g = cur[si];
         const uint32_t lo = g.first + 1 + (t - g.tbase) * kSortTile;
         const uint32_t hi = min(g.last, lo + kSortTile);
         uint32_t cl = 0, cr = 0;
+        int32_t mn = g.pivot, mx = g.pivot;
         for (uint32_t p = lo + threadIdx.x; p < hi; p += kThreads) {
             const int32_t k = skey(ss.a[p]);
             cl += is_lstop(k, g.pivot);
             cr += is_rstop(k, g.pivot);
+            mn = min(mn, k);
+            mx = max(mx, k);
         }
-        const uint32_t tl = block_reduce_add(cl, sm);
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1) {
+            mn = min(mn, __shfl_down_sync(0xFFFFFFFFu, mn, d));
+            mx = max(mx, __shfl_down_sync(0xFFFFFFFFu, mx, d));
+        }
+        if (lane == 0) { smn[warp] = mn; smx[warp] = mx; }
+        const uint32_t tl = block_reduce_add(cl, sm);  // its barriers publish smn / smx
         const uint32_t tr = block_reduce_add(cr, sm);
         if (threadIdx.x == 0) {
             ss.tile_l[t] = tl;
             ss.tile_r[t] = tr;
+            for (uint32_t w = 1; w < kThreads / 32; ++w) { mn = min(mn, smn[w]); mx = max(mx, smx[w]); }
+            if (mn < g.pivot) atomicMin(&cur[si].kmin, mn);
+            if (mx > g.pivot) atomicMax(&cur[si].kmax, mx);
         }
         __syncthreads();
     }
@@ -362,7 +381,15 @@ __global__ void __launch_bounds__(kThreads) k_sort_pos(SortScratch ss, const Sor
     }
 }
 
-__device__ void sort_emit(SortScratch ss, SortSeg* next, uint32_t first, uint32_t last, uint32_t dl) {
+// Routes a part of a split: eq says its keys are all equal.
+__device__ void sort_emit(SortScratch ss, SortSeg* next, uint32_t first, uint32_t last, uint32_t dl, bool eq) {
+    if (eq && last - first <= kSortThreshold) return;  // a stable sort of equal keys moves nothing
+    if (eq && dl >= equal_levels(last - first)) {      // final order in closed form (k_sort_equal)
+        const uint32_t k = atomicAdd(&ss.counters[7], 1u);
+        if (k < ss.seg_cap) { ss.equal[2 * k] = first; ss.equal[2 * k + 1] = last; }
+        else ss.counters[5] = 1;
+        return;
+    }
     if (last - first <= kSortThreshold) {
         if (last - first > 1) {
             const uint32_t k = atomicAdd(&ss.counters[2], 1u);
@@ -371,7 +398,7 @@ __device__ void sort_emit(SortScratch ss, SortSeg* next, uint32_t first, uint32_
         }
         return;
     }
-    if (dl > 0 && last - first <= kSortLocal) {  // finishes in one warp after the rounds
+    if (dl > 0 && last - first <= kSortBlock) {  // finishes in one block after the rounds
         const uint32_t k = atomicAdd(&ss.counters[6], 1u);
         if (k < ss.seg_cap) { ss.local[3 * k] = first; ss.local[3 * k + 1] = last; ss.local[3 * k + 2] = dl; }
         else ss.counters[5] = 1;
@@ -412,8 +439,8 @@ __global__ void k_sort_cut(SortScratch ss, SortSeg* cur, SortSeg* next, ErrorWor
             g.K = 0;
             continue;
         }
-        sort_emit(ss, next, g.first, g.cut, g.dl - 1);
-        sort_emit(ss, next, g.cut, g.last, g.dl - 1);
+        sort_emit(ss, next, g.first, g.cut, g.dl - 1, g.kmin == g.pivot);
+        sort_emit(ss, next, g.cut, g.last, g.dl - 1, g.kmax == g.pivot);
     }
 }
 
@@ -433,79 +460,220 @@ __global__ void __launch_bounds__(kThreads) k_sort_swap(SortScratch ss, const So
 __global__ void k_sort_leaves(SortScratch ss, uint32_t count) {
     PTL_FOR(k, count) leaf_sort(ss.a, ss.leaf[2 * k], ss.leaf[2 * k + 1]);
 }
-// One small range per warp, staged in shared memory.  Each partition step is the
-// closed form of the rounds above, computed by the warp: L-stop and R-stop positions by
-// ballot and prefix count, K by ballot (A[k] < B[k] holds on a prefix of k), the cut,
-// then the K swaps, whose pairs are disjoint, in parallel.  Pending ranges live on a
-// per-warp stack; ranges of at most 16 keys are collected and insertion-sorted one per
-// lane at the end, and a range whose depth budget is spent is heap-sorted by one lane.
-constexpr int kSortLocalWarps = 8;
-struct LocalWarpSmem {
-    unsigned long long buf[kSortLocal];
-    uint32_t A[kSortLocal], R[kSortLocal];
-    uint32_t st_f[64], st_l[64], st_d[64];
-    uint16_t leaf_f[kSortLocal / 2], leaf_l[kSortLocal / 2];
-    static_assert(kSortLocal <= 65535, "leaf bounds are 16-bit");
+// ---- ranges of at most kSortBlock keys: one block each, in shared memory
+// The partition steps are the closed form of the rounds above.  Parts longer than
+// kSortLocal are split by the whole block (stop positions by ballot and a scan over
+// (sweep, warp) counts, K by binary search, the K disjoint swaps in parallel); shorter
+// parts are finished by one warp each.  Every part's start is marked in a bitmask, so
+// the final ranges tile the buffer: a range of at most 16 keys (a leaf) is written back
+// by stable rank, a range of equal keys in closed form, a heap-sorted range as it is.
+// The smaller part of a split is taken first, so the pending stacks stay within
+// log2(kSortBlock) entries.
+constexpr int kSortBlockThreads = 512;
+constexpr int kSortBlockWarps = kSortBlockThreads / 32;
+constexpr uint32_t kSortBlockSweeps = (kSortBlock + kSortBlockThreads - 1) / kSortBlockThreads;
+constexpr uint32_t kSortBlockLists = kSortBlock / (kSortThreshold + 1) + 2;
+constexpr uint32_t kSortStack = 16;
+static_assert(kSortBlock <= 65535 && kSortBlockSweeps <= 32, "16-bit positions, 32-bit sweep masks");
+
+struct BlockSortSmem {
+    unsigned long long buf[kSortBlock];
+    uint16_t A[kSortBlock], R[kSortBlock];  // stop positions of the part being split (at its offset)
+    uint32_t starts[kSortBlock / 32 + 1];   // bit j: a part starts at j (bit m: the end)
+    uint16_t sm_f[kSortBlockLists], sm_l[kSortBlockLists], sm_d[kSortBlockLists];     // warp parts
+    uint16_t fin_f[kSortBlockLists], fin_l[kSortBlockLists], fin_h[kSortBlockLists];  // equal (0) / heap (1)
+    uint16_t st_f[kSortBlockWarps][kSortStack], st_l[kSortBlockWarps][kSortStack], st_d[kSortBlockWarps][kSortStack];
+    uint32_t bst_f[kSortStack], bst_l[kSortStack], bst_d[kSortStack];
+    uint32_t cntL[kSortBlockSweeps * kSortBlockWarps], cntR[kSortBlockSweeps * kSortBlockWarps];
+    int32_t wmin[kSortBlockWarps], wmax[kSortBlockWarps];
+    int32_t kmin, kmax;
+    uint32_t nL, nR, K, cut;
+    uint32_t n_sm, n_fin, next_sm, n_bst, bad;
+    uint32_t cur_f, cur_l, cur_d, have;
 };
 
-__global__ void __launch_bounds__(kSortLocalWarps * 32) k_sort_local(SortScratch ss, uint32_t count) {
-    extern __shared__ __align__(16) unsigned char lsm[];
-    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
-    LocalWarpSmem& w = reinterpret_cast<LocalWarpSmem*>(lsm)[warp];
-    const uint32_t r = blockIdx.x * kSortLocalWarps + warp;
-    if (r >= count) return;  // warp-uniform; the kernel has no block barrier
-    const uint32_t first = ss.local[3 * r], last = ss.local[3 * r + 1], dl = ss.local[3 * r + 2];
-    const uint32_t len = last - first;
-    if (len > kSortLocal) return;  // emitted only up to kSortLocal
-    for (uint32_t i = lane; i < len; i += 32) w.buf[i] = ss.a[first + i];
-    const unsigned full = 0xFFFFFFFFu;
-    const unsigned lt = (1u << lane) - 1u;
-    uint32_t sp = 0, nleaf = 0;
-    if (lane == 0) { w.st_f[0] = 0; w.st_l[0] = len; w.st_d[0] = dl; }
-    sp = 1;
-    __syncwarp();
-    while (sp > 0) {
-        --sp;
-        const uint32_t f = w.st_f[sp], l = w.st_l[sp], d = w.st_d[sp];
-        __syncwarp();
-        const uint32_t m = l - f;
-        if (m <= kSortThreshold) {
-            if (m > 1) {
-                if (lane == 0) { w.leaf_f[nleaf] = static_cast<uint16_t>(f); w.leaf_l[nleaf] = static_cast<uint16_t>(l); }
-                ++nleaf;
+// Marks the start of part [f, l) (depth budget d, eq: its keys are all equal) and lists
+// it if it is final; returns whether it must be split further.
+__device__ bool bsort_route(BlockSortSmem& w, uint32_t f, uint32_t l, uint32_t d, bool eq) {
+    atomicOr(&w.starts[f >> 5], 1u << (f & 31u));
+    const uint32_t m = l - f;
+    if (m <= kSortThreshold) return false;  // a leaf
+    const bool closed = eq && d >= equal_levels(m);
+    if (closed || d == 0) {
+        const uint32_t k = atomicAdd(&w.n_fin, 1u);
+        if (k < kSortBlockLists) {
+            w.fin_f[k] = static_cast<uint16_t>(f);
+            w.fin_l[k] = static_cast<uint16_t>(l);
+            w.fin_h[k] = closed ? 0 : 1;
+        } else {
+            w.bad = 1;
+        }
+        return false;
+    }
+    return true;
+}
+
+__device__ void bsort_push_small(BlockSortSmem& w, uint32_t f, uint32_t l, uint32_t d) {
+    const uint32_t k = atomicAdd(&w.n_sm, 1u);
+    if (k < kSortBlockLists) {
+        w.sm_f[k] = static_cast<uint16_t>(f);
+        w.sm_l[k] = static_cast<uint16_t>(l);
+        w.sm_d[k] = static_cast<uint16_t>(d);
+    } else {
+        w.bad = 1;
+    }
+}
+
+__device__ __forceinline__ int32_t warp_min_i32(int32_t v) {
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) v = min(v, __shfl_xor_sync(0xFFFFFFFFu, v, d));
+    return v;
+}
+__device__ __forceinline__ int32_t warp_max_i32(int32_t v) {
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) v = max(v, __shfl_xor_sync(0xFFFFFFFFu, v, d));
+    return v;
+}
+
+// One block-wide split of [f, l); sets w.K / w.cut / w.kmin / w.kmax (w.bad on a broken
+// invariant).  Every thread calls it; it ends with a barrier.
+__device__ void bsort_split_block(BlockSortSmem& w, uint32_t f, uint32_t l) {
+    const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+    const unsigned full = 0xFFFFFFFFu, lt = (1u << lane) - 1u;
+    constexpr uint32_t T = kSortBlockThreads;
+    if (tid == 0) median_to_first(w.buf, f, l);
+    __syncthreads();
+    const int32_t pivot = skey(w.buf[f]);
+    const uint32_t sweeps = (l - f - 1u + T - 1u) / T;
+    uint32_t fl = 0, fr = 0;
+    int32_t mn = pivot, mx = pivot;
+    for (uint32_t k = 0; k < sweeps; ++k) {
+        const uint32_t p = f + 1u + k * T + tid;
+        const bool in = p < l;
+        const int32_t key = in ? skey(w.buf[p]) : pivot;
+        const bool isL = in && is_lstop(key, pivot), isR = in && is_rstop(key, pivot);
+        mn = min(mn, key);
+        mx = max(mx, key);
+        fl |= static_cast<uint32_t>(isL) << k;
+        fr |= static_cast<uint32_t>(isR) << k;
+        const unsigned bL = __ballot_sync(full, isL), bR = __ballot_sync(full, isR);
+        if (lane == 0) {
+            w.cntL[k * kSortBlockWarps + warp] = __popc(bL);
+            w.cntR[k * kSortBlockWarps + warp] = __popc(bR);
+        }
+    }
+    mn = warp_min_i32(mn);
+    mx = warp_max_i32(mx);
+    if (lane == 0) { w.wmin[warp] = mn; w.wmax[warp] = mx; }
+    __syncthreads();
+    if (warp == 0) {
+        // exclusive scan of the (sweep, warp) counts in that order, 8 entries per lane
+        constexpr uint32_t E = kSortBlockSweeps * kSortBlockWarps, per = E / 32;
+        const uint32_t used = sweeps * kSortBlockWarps;
+        uint32_t vl[per], vr[per], sl = 0, sr = 0;
+#pragma unroll
+        for (uint32_t q = 0; q < per; ++q) {
+            const uint32_t e = lane * per + q;
+            vl[q] = e < used ? w.cntL[e] : 0u;
+            vr[q] = e < used ? w.cntR[e] : 0u;
+            sl += vl[q];
+            sr += vr[q];
+        }
+        uint32_t il = sl, ir = sr;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t al = __shfl_up_sync(full, il, d), ar = __shfl_up_sync(full, ir, d);
+            if (lane >= static_cast<uint32_t>(d)) { il += al; ir += ar; }
+        }
+        uint32_t ol = il - sl, orr = ir - sr;
+#pragma unroll
+        for (uint32_t q = 0; q < per; ++q) {
+            const uint32_t e = lane * per + q;
+            if (e < used) { w.cntL[e] = ol; w.cntR[e] = orr; }
+            ol += vl[q];
+            orr += vr[q];
+        }
+        int32_t a = lane < kSortBlockWarps ? w.wmin[lane] : pivot, b = lane < kSortBlockWarps ? w.wmax[lane] : pivot;
+        a = warp_min_i32(a);
+        b = warp_max_i32(b);
+        if (lane == 31) { w.nL = il; w.nR = ir; }
+        if (lane == 0) { w.kmin = a; w.kmax = b; }
+    }
+    __syncthreads();
+    for (uint32_t k = 0; k < sweeps; ++k) {
+        const bool isL = (fl >> k) & 1u, isR = (fr >> k) & 1u;
+        const unsigned bL = __ballot_sync(full, isL), bR = __ballot_sync(full, isR);
+        const uint32_t p = f + 1u + k * T + tid;
+        if (isL) w.A[f + w.cntL[k * kSortBlockWarps + warp] + __popc(bL & lt)] = static_cast<uint16_t>(p);
+        if (isR) w.R[f + w.cntR[k * kSortBlockWarps + warp] + __popc(bR & lt)] = static_cast<uint16_t>(p);
+    }
+    __syncthreads();
+    if (tid == 0) {
+        const uint32_t nL = w.nL, nR = w.nR;
+        uint32_t K = 0, cut = 0;
+        if (nL == 0 || nR == 0) {  // the median move guarantees both kinds of stop
+            w.bad = 1;
+        } else {
+            uint32_t lo = 0, hi = nL < nR ? nL : nR;  // K: A[k] < B[k] holds on a prefix of k
+            while (lo < hi) {
+                const uint32_t mid = (lo + hi) / 2;
+                if (w.A[f + mid] < w.R[f + nR - 1u - mid]) lo = mid + 1; else hi = mid;
             }
-            continue;
+            K = lo;
+            if (K == 0) {
+                cut = w.A[f];
+            } else {
+                const uint32_t bk = w.R[f + nR - K];  // B[K-1]
+                cut = (K < nL && w.A[f + K] < bk) ? w.A[f + K] : bk;
+            }
+            if (cut <= f || cut >= l) { w.bad = 1; K = 0; }
         }
-        if (d == 0) {
-            if (lane == 0) heap_sort_range(w.buf + f, m);
-            __syncwarp();
-            continue;
-        }
+        w.K = K;
+        w.cut = cut;
+    }
+    __syncthreads();
+    const uint32_t K = w.K, nR = w.nR;
+    for (uint32_t k = tid; k < K; k += T) sswap(w.buf, w.A[f + k], w.R[f + nR - 1u - k]);
+    __syncthreads();
+}
+
+// One warp finishes part [f, l) (more than 16 keys, depth budget d > 0) and every part
+// of it that must be split further.
+__device__ void bsort_warp(BlockSortSmem& w, uint32_t f, uint32_t l, uint32_t d) {
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    const unsigned full = 0xFFFFFFFFu, lt = (1u << lane) - 1u;
+    uint32_t sp = 0;
+    for (;;) {
         if (lane == 0) median_to_first(w.buf, f, l);
         __syncwarp();
         const int32_t pivot = skey(w.buf[f]);
         uint32_t nL = 0, nR = 0;
+        int32_t mn = pivot, mx = pivot;
         for (uint32_t base = f + 1; base < l; base += 32) {
             const uint32_t p = base + lane;
             const bool in = p < l;
-            const int32_t k = in ? skey(w.buf[p]) : 0;
+            const int32_t k = in ? skey(w.buf[p]) : pivot;
             const bool isL = in && is_lstop(k, pivot), isR = in && is_rstop(k, pivot);
+            mn = min(mn, k);
+            mx = max(mx, k);
             const unsigned bL = __ballot_sync(full, isL), bR = __ballot_sync(full, isR);
-            if (isL) w.A[nL + __popc(bL & lt)] = p;
-            if (isR) w.R[nR + __popc(bR & lt)] = p;  // left to right; B[k] = R[nR - 1 - k]
+            if (isL) w.A[f + nL + __popc(bL & lt)] = static_cast<uint16_t>(p);
+            if (isR) w.R[f + nR + __popc(bR & lt)] = static_cast<uint16_t>(p);  // B[k] = R[nR - 1 - k]
             nL += __popc(bL);
             nR += __popc(bR);
         }
+        mn = warp_min_i32(mn);
+        mx = warp_max_i32(mx);
         __syncwarp();
         if (nL == 0 || nR == 0) {  // the median move guarantees both kinds of stop
-            if (lane == 0) ss.counters[5] = 1;  // the host reports the sort as failed
-            continue;
+            if (lane == 0) w.bad = 1;
+            return;
         }
-        const uint32_t mn = nL < nR ? nL : nR;
-        uint32_t K = mn;  // the first k with !(A[k] < B[k]), else min(nL, nR)
-        for (uint32_t c = 0; c < mn; c += 32) {
+        const uint32_t mnc = nL < nR ? nL : nR;
+        uint32_t K = mnc;
+        for (uint32_t c = 0; c < mnc; c += 32) {
             const uint32_t k = c + lane;
-            const unsigned b = __ballot_sync(full, k < mn && !(w.A[k] < w.R[nR - 1u - k]));
+            const unsigned b = __ballot_sync(full, k < mnc && !(w.A[f + k] < w.R[f + nR - 1u - k]));
             if (b) {
                 K = c + static_cast<uint32_t>(__ffs(b) - 1);
                 break;
@@ -513,24 +681,182 @@ __global__ void __launch_bounds__(kSortLocalWarps * 32) k_sort_local(SortScratch
         }
         uint32_t cut;
         if (K == 0) {
-            cut = w.A[0];
+            cut = w.A[f];
         } else {
-            const uint32_t bk = w.R[nR - K];  // B[K-1]
-            cut = (K < nL && w.A[K] < bk) ? w.A[K] : bk;
+            const uint32_t bk = w.R[f + nR - K];
+            cut = (K < nL && w.A[f + K] < bk) ? w.A[f + K] : bk;
         }
-        for (uint32_t k = lane; k < K; k += 32) sswap(w.buf, w.A[k], w.R[nR - 1u - k]);
+        if (cut <= f || cut >= l) {
+            if (lane == 0) w.bad = 1;
+            return;
+        }
+        for (uint32_t k = lane; k < K; k += 32) sswap(w.buf, w.A[f + k], w.R[f + nR - 1u - k]);
         __syncwarp();
-        if (lane == 0 && sp + 2 <= 64) {
-            w.st_f[sp] = cut; w.st_l[sp] = l; w.st_d[sp] = d - 1;
-            w.st_f[sp + 1] = f; w.st_l[sp + 1] = cut; w.st_d[sp + 1] = d - 1;
+        uint32_t go = 0;
+        if (lane == 0) {
+            go = (bsort_route(w, f, cut, d - 1, mn == pivot) ? 1u : 0u) |
+                 (bsort_route(w, cut, l, d - 1, mx == pivot) ? 2u : 0u);
         }
-        sp = sp + 2 <= 64 ? sp + 2 : sp;
+        go = __shfl_sync(full, go, 0);
+        --d;
+        if (go == 3u) {  // take the smaller part, keep the larger
+            const bool left_small = cut - f <= l - cut;
+            if (lane == 0) {
+                if (sp < kSortStack) {
+                    w.st_f[warp][sp] = static_cast<uint16_t>(left_small ? cut : f);
+                    w.st_l[warp][sp] = static_cast<uint16_t>(left_small ? l : cut);
+                    w.st_d[warp][sp] = static_cast<uint16_t>(d);
+                } else {
+                    w.bad = 1;
+                }
+            }
+            ++sp;
+            if (sp > kSortStack) return;
+            if (left_small) l = cut; else f = cut;
+        } else if (go == 1u) {
+            l = cut;
+        } else if (go == 2u) {
+            f = cut;
+        } else {
+            if (sp == 0) return;
+            --sp;
+            __syncwarp();
+            f = w.st_f[warp][sp];
+            l = w.st_l[warp][sp];
+            d = w.st_d[warp][sp];
+        }
         __syncwarp();
     }
-    __syncwarp();
-    for (uint32_t i = lane; i < nleaf; i += 32) leaf_sort(w.buf, w.leaf_f[i], w.leaf_l[i]);
-    __syncwarp();
-    for (uint32_t i = lane; i < len; i += 32) ss.a[first + i] = w.buf[i];
+}
+
+__global__ void __launch_bounds__(kSortBlockThreads) k_sort_block(SortScratch ss, uint32_t count, ErrorWord* err) {
+    extern __shared__ __align__(16) unsigned char bsm[];
+    BlockSortSmem& w = *reinterpret_cast<BlockSortSmem*>(bsm);
+    const uint32_t tid = threadIdx.x, lane = tid & 31u;
+    constexpr uint32_t T = kSortBlockThreads;
+    for (uint32_t r = blockIdx.x; r < count; r += gridDim.x) {
+        const uint32_t first = ss.local[3 * r], last = ss.local[3 * r + 1], dl = ss.local[3 * r + 2];
+        const uint32_t m = last - first;
+        if (m > kSortBlock || m < 2) {  // emitted only up to kSortBlock (block-uniform)
+            if (tid == 0) record_error(err, ST_UNSUPPORTED, W_SORT, first);
+            continue;
+        }
+        for (uint32_t j = tid; j < m; j += T) w.buf[j] = ss.a[first + j];
+        for (uint32_t j = tid; j < kSortBlock / 32 + 1; j += T) w.starts[j] = 0;
+        if (tid == 0) {
+            w.n_sm = w.n_fin = w.next_sm = w.n_bst = w.bad = 0;
+            w.have = 0;
+        }
+        __syncthreads();
+        if (tid == 0) {
+            w.starts[m >> 5] |= 1u << (m & 31u);
+            if (bsort_route(w, 0, m, dl, false)) {
+                if (m <= kSortLocal) {
+                    bsort_push_small(w, 0, m, dl);
+                } else {
+                    w.cur_f = 0; w.cur_l = m; w.cur_d = dl; w.have = 1;
+                }
+            }
+        }
+        __syncthreads();
+        // parts longer than kSortLocal: the whole block
+        while (w.have) {
+            const uint32_t f = w.cur_f, l = w.cur_l, d = w.cur_d;
+            bsort_split_block(w, f, l);
+            if (tid == 0) {
+                w.have = 0;
+                if (!w.bad) {
+                    const uint32_t cut = w.cut;
+                    const int32_t pivot = skey(w.buf[f]);
+                    const bool gl = bsort_route(w, f, cut, d - 1, w.kmin == pivot);
+                    const bool gr = bsort_route(w, cut, l, d - 1, w.kmax == pivot);
+                    // warp-sized parts are listed; of two block-sized parts the larger waits
+                    const bool bl = gl && cut - f > kSortLocal, br = gr && l - cut > kSortLocal;
+                    if (gl && !bl) bsort_push_small(w, f, cut, d - 1);
+                    if (gr && !br) bsort_push_small(w, cut, l, d - 1);
+                    if (bl && br) {
+                        const bool left_small = cut - f <= l - cut;
+                        if (w.n_bst < kSortStack) {
+                            w.bst_f[w.n_bst] = left_small ? cut : f;
+                            w.bst_l[w.n_bst] = left_small ? l : cut;
+                            w.bst_d[w.n_bst] = d - 1;
+                            ++w.n_bst;
+                        } else {
+                            w.bad = 1;
+                        }
+                        w.cur_f = left_small ? f : cut; w.cur_l = left_small ? cut : l; w.cur_d = d - 1; w.have = 1;
+                    } else if (bl || br) {
+                        w.cur_f = bl ? f : cut; w.cur_l = bl ? cut : l; w.cur_d = d - 1; w.have = 1;
+                    }
+                    if (!w.have && w.n_bst > 0 && !w.bad) {
+                        --w.n_bst;
+                        w.cur_f = w.bst_f[w.n_bst]; w.cur_l = w.bst_l[w.n_bst]; w.cur_d = w.bst_d[w.n_bst];
+                        w.have = 1;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+        // parts of at most kSortLocal keys: a warp each
+        const uint32_t n_sm = min(w.n_sm, kSortBlockLists);
+        for (;;) {
+            uint32_t idx = 0;
+            if (lane == 0) idx = atomicAdd(&w.next_sm, 1u);
+            idx = __shfl_sync(0xFFFFFFFFu, idx, 0);
+            if (idx >= n_sm) break;
+            bsort_warp(w, w.sm_f[idx], w.sm_l[idx], w.sm_d[idx]);
+        }
+        __syncthreads();
+        const uint32_t n_fin = min(w.n_fin, kSortBlockLists);
+        for (uint32_t k = tid; k < n_fin; k += T)
+            if (w.fin_h[k]) heap_sort_range(w.buf + w.fin_f[k], static_cast<uint32_t>(w.fin_l[k] - w.fin_f[k]));
+        __syncthreads();
+        // write-back: leaves by stable rank
+        for (uint32_t j = tid; j < m; j += T) {
+            const uint32_t wi = j >> 5, b = j & 31u;
+            uint32_t x = w.starts[wi] & (0xFFFFFFFFu >> (31u - b));
+            int32_t s0 = -1;
+            if (x) s0 = static_cast<int32_t>(wi * 32u + 31u - __clz(x));
+            else if (wi > 0 && (x = w.starts[wi - 1]) != 0) s0 = static_cast<int32_t>((wi - 1u) * 32u + 31u - __clz(x));
+            if (s0 < 0 || j - static_cast<uint32_t>(s0) >= kSortThreshold) continue;
+            x = b == 31u ? 0u : (w.starts[wi] & (0xFFFFFFFFu << (b + 1u)));
+            uint32_t e0;
+            if (x) e0 = wi * 32u + __ffs(x) - 1u;
+            else if ((x = w.starts[wi + 1]) != 0) e0 = (wi + 1u) * 32u + __ffs(x) - 1u;
+            else continue;
+            const uint32_t s = static_cast<uint32_t>(s0);
+            if (e0 - s > kSortThreshold) continue;
+            const int32_t kj = skey(w.buf[j]);
+            uint32_t rank = 0;
+            for (uint32_t q = s; q < e0; ++q) {
+                const int32_t kq = skey(w.buf[q]);
+                rank += (kq < kj || (kq == kj && q < j)) ? 1u : 0u;
+            }
+            ss.a[first + s + rank] = w.buf[j];
+        }
+        // equal-key ranges in closed form, heap-sorted ranges as they are
+        for (uint32_t k = 0; k < n_fin; ++k) {
+            const uint32_t f = w.fin_f[k], len = w.fin_l[k] - w.fin_f[k];
+            const bool heap = w.fin_h[k] != 0;
+            for (uint32_t i = tid; i < len; i += T)
+                ss.a[first + f + (heap ? i : equal_final_index(i, len))] = w.buf[f + i];
+        }
+        if (tid == 0 && w.bad) record_error(err, ST_UNSUPPORTED, W_SORT, first);
+        __syncthreads();
+    }
+}
+
+// Equal-key ranges found by the rounds: one block per range places each (key, index)
+// pair at its closed-form position, through apos (free after the rounds).
+__global__ void __launch_bounds__(kThreads) k_sort_equal(SortScratch ss, uint32_t count) {
+    for (uint32_t r = blockIdx.x; r < count; r += gridDim.x) {
+        const uint32_t first = ss.equal[2 * r], m = ss.equal[2 * r + 1] - first;
+        for (uint32_t i = threadIdx.x; i < m; i += kThreads) ss.apos[first + equal_final_index(i, m)] = sidx(ss.a[first + i]);
+        __syncthreads();
+        const unsigned long long key = ss.a[first] & 0xFFFFFFFF00000000ull;
+        for (uint32_t i = threadIdx.x; i < m; i += kThreads) ss.a[first + i] = key | ss.apos[first + i];
+        __syncthreads();
+    }
 }
 __global__ void k_sort_heaps(SortScratch ss, uint32_t count) {
     PTL_FOR(k, count) heap_sort_range(ss.a + ss.heap[2 * k], ss.heap[2 * k + 1] - ss.heap[2 * k]);
@@ -872,19 +1198,24 @@ cudaError_t run_sort_rounds(const SortScratch& ss, uint32_t nseg0, uint32_t firs
         if (nseg > 0 && rounds > max_rounds) return cudaErrorLaunchFailure;
         batch = 4;
     }
-    uint32_t lh[5] = {0, 0, 0, 0, 0};  // leaves, heaps, -, -, small ranges
+    uint32_t lh[6] = {0, 0, 0, 0, 0, 0};  // leaves, heaps, -, overflow, block ranges, equal ranges
     cudaMemcpyAsync(lh, ss.counters + 2, sizeof(lh), cudaMemcpyDeviceToHost, s);
     cudaError_t e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return e;
-    if (lh[0] > ss.leaf_cap || lh[1] > ss.leaf_cap || lh[4] > ss.seg_cap) return cudaErrorMemoryAllocation;
+    if (lh[3] || lh[0] > ss.leaf_cap || lh[1] > ss.leaf_cap || lh[4] > ss.seg_cap || lh[5] > ss.seg_cap)
+        return cudaErrorMemoryAllocation;
     if (lh[1]) { g_launches++; k_sort_heaps<<<grid_for(lh[1]), kThreads, 0, s>>>(ss, lh[1]); }
     if (lh[0]) { g_launches++; k_sort_leaves<<<grid_for(lh[0]), kThreads, 0, s>>>(ss, lh[0]); }
+    if (lh[5]) {
+        g_launches++;
+        k_sort_equal<<<static_cast<unsigned>(std::min<uint32_t>(lh[5], 152u * 8u)), kThreads, 0, s>>>(ss, lh[5]);
+    }
     if (lh[4]) {
-        const size_t smem = static_cast<size_t>(kSortLocalWarps) * sizeof(LocalWarpSmem);
-        e = cudaFuncSetAttribute(k_sort_local, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+        const size_t smem = sizeof(BlockSortSmem);
+        e = cudaFuncSetAttribute(k_sort_block, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
         if (e != cudaSuccess) return e;
         g_launches++;
-        k_sort_local<<<(lh[4] + kSortLocalWarps - 1) / kSortLocalWarps, kSortLocalWarps * 32, smem, s>>>(ss, lh[4]);
+        k_sort_block<<<lh[4], kSortBlockThreads, smem, s>>>(ss, lh[4], err);
     }
     if (rounds_out) *rounds_out = rounds;
     return cudaGetLastError();
@@ -896,13 +1227,18 @@ cudaError_t run_depth_sort(const Prog& P, const SortScratch& ss, cudaStream_t s,
     k_sort_init<<<grid_for(n), kThreads, 0, s>>>(P, ss);
     cudaMemsetAsync(ss.counters, 0, sizeof(uint32_t) * 8, s);
     uint32_t nseg = 0;
-    if (n > kSortThreshold) {
+    if (n > kSortBlock) {
         SortSeg g{};
         g.first = 0;
         g.last = n;
         g.dl = 2u * floor_log2(n);
         cudaMemcpyAsync(ss.seg[0], &g, sizeof(g), cudaMemcpyHostToDevice, s);
         nseg = 1;
+    } else if (n > kSortThreshold) {  // one block sorts it all
+        static const uint32_t one = 1;
+        const uint32_t range[3] = {0, n, 2u * floor_log2(n)};
+        cudaMemcpyAsync(ss.local, range, sizeof(range), cudaMemcpyHostToDevice, s);
+        cudaMemcpyAsync(ss.counters + 6, &one, sizeof(one), cudaMemcpyHostToDevice, s);
     } else if (n > 1) {
         const uint32_t leaf[2] = {0, n};
         cudaMemcpyAsync(ss.leaf, leaf, sizeof(leaf), cudaMemcpyHostToDevice, s);
@@ -910,7 +1246,8 @@ cudaError_t run_depth_sort(const Prog& P, const SortScratch& ss, cudaStream_t s,
         cudaMemcpyAsync(ss.counters + 2, &one, sizeof(one), cudaMemcpyHostToDevice, s);
     }
     const uint32_t lg = floor_log2(std::max<uint32_t>(n, 2u));
-    const cudaError_t e = run_sort_rounds(ss, nseg, lg > 9u ? lg - 9u : 1u, 2u * lg + 4u, P.err, s, rounds_out);
+    const uint32_t lb = floor_log2(kSortBlock);
+    const cudaError_t e = run_sort_rounds(ss, nseg, lg > lb ? lg - lb : 1u, 2u * lg + 4u, P.err, s, rounds_out);
     if (e != cudaSuccess) return e;
     g_launches++;
     k_sort_out<<<grid_for(n), kThreads, 0, s>>>(P, ss);

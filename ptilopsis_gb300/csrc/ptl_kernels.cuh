@@ -22,9 +22,11 @@ struct SortScratch {
     uint32_t* leaf;            // leaf ranges (first, last)
     uint32_t* heap;            // heap-sorted ranges
     uint32_t leaf_cap;
-    uint32_t* local;           // small ranges (first, last, depth budget) finished in one thread
+    uint32_t* local;           // ranges of at most kSortBlock keys (first, last, depth budget),
+                               // finished one block each (k_sort_block)
+    uint32_t* equal;           // equal-key ranges (first, last) found by the rounds
     uint32_t* counters;        // [0] tiles [1] next segments [2] leaves [3] heaps [4] segments of
-                               // this round [5] capacity overflow [6] small ranges
+                               // this round [5] capacity overflow [6] block ranges [7] equal ranges
 };
 
 constexpr size_t kScanTileElems = 4096;  // elements per scan tile (ptl_kernels.cu)

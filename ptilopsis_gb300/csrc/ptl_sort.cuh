@@ -30,6 +30,7 @@ struct SortSeg {
     uint32_t tbase, tcount;  // tiles of [first+1, last)
     uint32_t nL, nR;       // stop counts
     uint32_t K, cut;
+    int32_t kmin, kmax;    // least and greatest key in [first, last)
 };
 
 constexpr uint32_t kSortThreshold = 16;   // libstdc++ _S_threshold
@@ -137,6 +138,44 @@ PTL_HD void heap_sort_range(Arr base, uint32_t len) {
     }
 }
 
+// ---- ranges of equal keys
+// On a range whose keys are all equal every comparison is false, so introsort's steps
+// depend on the range's length m alone: the median move swaps first with mid = m/2, the
+// Hoare scan stops at every element and swaps positions 1+k and m-1-k for k < s =
+// (m-1)/2, and the range splits at s+1; the final insertion sort moves nothing.  An
+// element's final index follows by descending these splits, which replaces every round
+// below such a range.
+
+// Levels the descent takes: the larger part of a split holds ceil(m/2) keys.
+PTL_HD uint32_t equal_levels(uint32_t m) {
+    uint32_t l = 0;
+    while (m > kSortThreshold) {
+        m -= m / 2;
+        ++l;
+    }
+    return l;
+}
+
+// Final index of the element at index i of an equal-key range of m elements, given a
+// depth budget of at least equal_levels(m) (no heap sort on the way).
+PTL_HD uint32_t equal_final_index(uint32_t i, uint32_t m) {
+    uint32_t off = 0;
+    while (m > kSortThreshold) {
+        const uint32_t mid = m / 2, s = (m - 1u) / 2u;
+        if (i == 0) i = mid;
+        else if (i == mid) i = 0;
+        if ((i >= 1u && i <= s) || i >= m - s) i = m - i;
+        if (i <= s) {
+            m = s + 1u;
+        } else {
+            i -= s + 1u;
+            off += s + 1u;
+            m -= s + 1u;
+        }
+    }
+    return off + i;
+}
+
 // Stable insertion sort by key (what the final insertion sort does to one small range).
 template <class Arr>
 PTL_HD void leaf_sort(Arr a, uint32_t first, uint32_t last) {
@@ -151,10 +190,12 @@ PTL_HD void leaf_sort(Arr a, uint32_t first, uint32_t last) {
     }
 }
 
-// ---- small ranges
-// Ranges of at most kSortLocal elements with depth budget left finish without further
-// rounds (they touch only their own range): one warp each on the device (k_sort_local),
-// and local_introsort below, the same steps taken sequentially, in the host model.
+// ---- ranges that fit on chip
+// Ranges of at most kSortBlock elements with depth budget left finish without further
+// rounds (they touch only their own range): one block each on the device (k_sort_block,
+// whose warps take the parts of at most kSortLocal elements), and local_introsort
+// below, the same steps taken sequentially, in the host model.
+constexpr uint32_t kSortBlock = 8192;
 constexpr uint32_t kSortLocal = 512;
 
 // An array view with a stride (element i at base[i * stride]).

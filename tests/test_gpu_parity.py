@@ -144,3 +144,36 @@ def test_gpu_large_program_against_oracle(built_cuda):
     words, table, _ = gpu_compile(tree)
     np.testing.assert_array_equal(words, ref.words)
     np.testing.assert_array_equal(table["starts"], ref.bufs["fn_start"])
+
+
+def _program_by_size(lo, hi):
+    from ptilopsis_gb300.synth import config_params, generate
+    for k in range(64):
+        t = generate(config_params("c3", program=k))
+        if lo <= t.n <= hi:
+            return t
+    raise AssertionError(f"no program of {lo}..{hi} nodes")
+
+
+@pytest.mark.parametrize("case", ["one_block", "rounds_then_blocks", "equal_key_ranges"])
+def test_gpu_depth_order_equals_std_sort(built_cuda, case):
+    """isn_gen's depth order (libstdc++ std::sort of node ids by depth) against the
+    oracle's std::sort: a program of at most 8,192 nodes (one block sorts it), one above
+    that (partition rounds, then blocks), and a 1M-node program whose depth levels hold
+    tens of thousands of nodes each (ranges of equal keys finished in closed form)."""
+    from oracle import portbind
+    from ptilopsis_gb300 import RvGenerator
+    from ptilopsis_gb300.synth import config_params, generate
+    if case == "one_block":
+        tree = _program_by_size(1000, 8192)
+    elif case == "rounds_then_blocks":
+        tree = _program_by_size(8193, 200_000)
+    else:
+        tree = generate(config_params("c1", scale=0.25))
+    perm = portbind.depth_sort(np.ascontiguousarray(tree.depth, np.int32))
+    want = np.empty(tree.n, np.uint32)
+    want[perm] = np.arange(tree.n, dtype=np.uint32)
+    with RvGenerator(tree) as gen:
+        gen.process()
+        got = gen.snapshot("depth_order_pos")
+    np.testing.assert_array_equal(got[:tree.n], want)

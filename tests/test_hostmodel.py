@@ -101,8 +101,9 @@ def test_depth_order_emulation_equals_std_sort(built, mode):
     from oracle import portbind
     L = hostmodel()
     rng = np.random.default_rng(hash(mode) & 0xFFFF)
-    for _ in range(40):
-        n = int(rng.integers(1, 6000))
+    for case in range(48):
+        # up to 8,192 keys one block sorts the array; above, partition rounds come first
+        n = int(rng.integers(1, 6000)) if case < 40 else int(rng.integers(8193, 60000))
         kmax = int(rng.integers(1, 80))
         if mode == "random":
             keys = rng.integers(0, kmax, n)
