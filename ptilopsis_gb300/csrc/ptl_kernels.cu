@@ -1511,28 +1511,78 @@ struct BSortOut {
     __device__ void operator()(const Prog& P, uint32_t i, uint32_t p) const { P.pos[sidx(a[aoff[p] + i])] = i; }
 };
 
-// Optimize sweeps over the tiles marked in cur (all tiles when cur is null).  A sweep can
-// newly act on instruction i only after the used mark of its result (word rd_i - 64)
-// was cleared; when every virtual result is the instruction's own word, that word sits
-// in i's tile, so clearing a mark queues its tile in next for the following sweep.
+// Optimize sweeps over the tiles marked in cur (all tiles when cur is null).  A block
+// takes a tile's used marks into shared memory and sweeps the tile to its own fixed
+// point (clearing only ever removes marks, so any fair order of the updates reaches the
+// same fixed point); marks it clears in other tiles are cleared in global memory and
+// queue those tiles in next.  When every virtual result is the instruction's own word
+// (cur given), an instruction acts only on a mark of its own tile, so only such cross-tile
+// clears make another sweep necessary; otherwise every tile is swept until a sweep
+// changes nothing.  The block writes back zeros only, so clears by other blocks are
+// never undone.
+constexpr uint32_t kSweepItems = kBTile / kThreads;
 __global__ void __launch_bounds__(kThreads) k_batch_sweep(const Prog* progs, const uint32_t* off, uint32_t B,
                                                           uint32_t total, uint32_t* changed, const uint8_t* cur,
                                                           uint8_t* next) {
+    __shared__ uint8_t s_used[kBTile];
     for (uint32_t t = blockIdx.x; t < total; t += gridDim.x) {
-        if (cur && !cur[t]) continue;
+        if (cur && !cur[t]) continue;  // block-uniform
         const uint32_t p = batch_program(off, B, t);
         const Prog& P = progs[p];
         const uint32_t base = (t - off[p]) * kBTile;
-        bool any = false;
-        for (uint32_t k = threadIdx.x; k < kBTile; k += kThreads) {
-            const uint32_t i = base + k;
-            if (i >= P.wb8) break;
-            uint32_t cl[2];
-            const uint32_t nc = st_opt_sweep_cleared(P, i, cl);
-            for (uint32_t c = 0; c < nc; ++c) next[off[p] + cl[c] / kBTile] = 1;
-            any |= nc != 0;
+        const uint32_t W = P.W, lim = min(kBTile, P.wb8 - base);
+        uint32_t rd[kSweepItems], r1[kSweepItems], r2[kSweepItems];
+        uint32_t pending = 0;  // bit e: instruction e of this thread may still act
+#pragma unroll
+        for (uint32_t e = 0; e < kSweepItems; ++e) {
+            const uint32_t k = threadIdx.x + e * kThreads;
+            if (k < lim) {
+                s_used[k] = P.used[base + k];
+                rd[e] = P.rd[base + k];
+                r1[e] = P.rs1[base + k];
+                r2[e] = P.rs2[base + k];
+                if (s32(rd[e]) > 63) pending |= 1u << e;
+            }
         }
-        if (__syncthreads_or(any) && threadIdx.x == 0) *changed = 1u;
+        __syncthreads();
+        bool cross = false, local = false;
+        for (;;) {
+            bool ch = false;
+#pragma unroll
+            for (uint32_t e = 0; e < kSweepItems; ++e) {
+                if (!((pending >> e) & 1u)) continue;
+                const uint32_t r = rd[e] - 64u;
+                if (r >= W) {
+                    record_error(P.err, ST_UNSUPPORTED, W_OPT, base + threadIdx.x + e * kThreads);
+                    pending &= ~(1u << e);
+                    continue;
+                }
+                const bool live = r - base < lim ? s_used[r - base] != 0
+                                                 : *reinterpret_cast<const volatile uint8_t*>(&P.used[r]) != 0;
+                if (live) continue;
+                pending &= ~(1u << e);  // dead: its operands lose their marks, once
+#pragma unroll
+                for (uint32_t o = 0; o < 2; ++o) {
+                    const int32_t a = s32((o == 0 ? r1[e] : r2[e]) - 64u);
+                    if (a < 0 || u32(a) >= W || P.smark[a]) continue;
+                    if (u32(a) - base < lim) {
+                        if (s_used[u32(a) - base]) { s_used[u32(a) - base] = 0; ch = true; }
+                    } else if (*reinterpret_cast<volatile uint8_t*>(&P.used[a])) {
+                        P.used[a] = 0;
+                        next[off[p] + u32(a) / kBTile] = 1;
+                        cross = true;
+                    }
+                }
+            }
+            local |= ch;
+            if (!__syncthreads_or(ch)) break;
+        }
+#pragma unroll
+        for (uint32_t e = 0; e < kSweepItems; ++e) {
+            const uint32_t k = threadIdx.x + e * kThreads;
+            if (k < lim && s_used[k] == 0) P.used[base + k] = 0;
+        }
+        if (__syncthreads_or(cross || (cur == nullptr && local)) && threadIdx.x == 0) *changed = 1u;
     }
 }
 

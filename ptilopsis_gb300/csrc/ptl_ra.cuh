@@ -365,9 +365,12 @@ PTL_HD void ra2_apply(const Prog& P, const SymCache& c, Ra2Shared& sh, Ra2Slot& 
     if (s32(S.ord) > 63) sym_write(P, c, slot, S.ord, S.rdr, false, (S.rdr & 63u) + 1u);
     if (s32(S.r1) > 63) sym_write(P, c, slot, S.r1, S.r1r, false);
     if (s32(S.r2) > 63) sym_write(P, c, slot, S.r2, S.r2r, false);
-    if (l_ord) sym_write(P, c, slot, S.ord, P.symreg[S.ord - 64u], true);
-    if (l_r1) sym_write(P, c, slot, S.r1, P.symreg[S.r1 - 64u], true);
-    if (l_r2) sym_write(P, c, slot, S.r2, P.symreg[S.r2 - 64u], true);
+    // a swapped symbol keeps the register just written for it (the last of the three
+    // writes above that names it): the values are known here, no global read needed
+    const bool r2v = s32(S.r2) > 63, r1v = s32(S.r1) > 63;
+    if (l_ord) sym_write(P, c, slot, S.ord, (r2v && S.r2 == S.ord) ? S.r2r : ((r1v && S.r1 == S.ord) ? S.r1r : S.rdr), true);
+    if (l_r1) sym_write(P, c, slot, S.r1, (r2v && S.r2 == S.r1) ? S.r2r : S.r1r, true);
+    if (l_r2) sym_write(P, c, slot, S.r2, S.r2r, true);
     // rdr < 64 always, and a clear never lands on the rd position, so each group writes
     // one value per position
     cur[3] = S.rdr & 63u;

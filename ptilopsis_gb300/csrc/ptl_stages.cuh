@@ -58,20 +58,37 @@ PTL_HD uint32_t ctz64(uint64_t t) {
 }
 
 // ------------------------------------------------------------------ table access
+// Table reads: the tables never change while a kernel runs, so the device reads them
+// through the read-only path, which also lets the compiler reuse a read across stores.
+template <class T>
+PTL_HD T tab_ld(const T* p) {
+#if defined(__CUDA_ARCH__)
+    return __ldg(p);
+#else
+    return *p;
+#endif
+}
+
 struct Tab {
     const CodeTables* t;
-    PTL_HD uint32_t row(uint32_t type) const { return t->row_of[type & 0xFFu]; }
+    PTL_HD uint32_t row(uint32_t type) const { return tab_ld(&t->row_of[type & 0xFFu]); }
     // The reference indexes its tables with type*24 + slot*6 + rtype; types are < 256 and
     // validated data types are <= 5, so the dense row lookup is exact.
-    PTL_HD uint32_t size(uint32_t type, uint32_t rt) const { return t->size[row(type)][rt]; }
-    PTL_HD bool has_instr(uint32_t type, uint32_t s, uint32_t rt) const { return (t->has_instr[row(type)][s] >> rt) & 1u; }
-    PTL_HD bool has_output(uint32_t type, uint32_t s, uint32_t rt) const { return (t->has_output[row(type)][s] >> rt) & 1u; }
-    PTL_HD uint32_t pai(uint32_t type, uint32_t s, uint32_t rt) const { return t->pai[row(type)][s][rt]; }
-    PTL_HD uint32_t out(uint32_t type, uint32_t s, uint32_t rt) const { return t->out[row(type)][s][rt]; }
-    PTL_HD uint32_t cnst(uint32_t type, uint32_t s) const { return t->cnst[row(type)][s]; }
-    PTL_HD uint32_t jt(uint32_t type, uint32_t s) const { return t->jt[row(type)][s]; }
-    PTL_HD uint32_t opd(uint32_t type, uint32_t s, uint32_t rt, uint32_t k) const { return t->opd[row(type)][s][rt][k]; }
-    PTL_HD uint32_t word(uint32_t type, uint32_t s, uint32_t rt) const { return t->instr[row(type)][s][rt]; }
+    PTL_HD uint32_t size(uint32_t type, uint32_t rt) const { return tab_ld(&t->size[row(type)][rt]); }
+    PTL_HD bool has_instr(uint32_t type, uint32_t s, uint32_t rt) const {
+        return (tab_ld(&t->has_instr[row(type)][s]) >> rt) & 1u;
+    }
+    PTL_HD bool has_output(uint32_t type, uint32_t s, uint32_t rt) const {
+        return (tab_ld(&t->has_output[row(type)][s]) >> rt) & 1u;
+    }
+    PTL_HD uint32_t pai(uint32_t type, uint32_t s, uint32_t rt) const { return tab_ld(&t->pai[row(type)][s][rt]); }
+    PTL_HD uint32_t out(uint32_t type, uint32_t s, uint32_t rt) const { return tab_ld(&t->out[row(type)][s][rt]); }
+    PTL_HD uint32_t cnst(uint32_t type, uint32_t s) const { return tab_ld(&t->cnst[row(type)][s]); }
+    PTL_HD uint32_t jt(uint32_t type, uint32_t s) const { return tab_ld(&t->jt[row(type)][s]); }
+    PTL_HD uint32_t opd(uint32_t type, uint32_t s, uint32_t rt, uint32_t k) const {
+        return tab_ld(&t->opd[row(type)][s][rt][k]);
+    }
+    PTL_HD uint32_t word(uint32_t type, uint32_t s, uint32_t rt) const { return tab_ld(&t->instr[row(type)][s][rt]); }
 };
 
 // ------------------------------------------------------------------ program view
@@ -366,17 +383,36 @@ struct GenLane {
     int32_t pai;
 };
 
-PTL_HD GenLane gen_lane(const Prog& P, uint32_t x, uint32_t s) {
+// What the four lanes of node x read from the node arrays, read once per node (the
+// stages store between lanes, so per-lane reads would be repeated after each store).
+struct GenNode {
+    uint32_t x, t, rt, par, ntp, ci, loc, nd;
+};
+
+PTL_HD GenNode gen_node(const Prog& P, uint32_t x) {
+    GenNode N;
+    N.x = x;
+    N.t = P.nt[x];
+    N.rt = P.rt[x];
+    N.par = u32(P.par[x]);
+    N.ntp = s32(N.par) == -1 ? 0u : P.nt[s32(N.par)];  // the parent's type
+    N.ci = u32(P.ci[x]);
+    N.loc = P.loc[x];
+    N.nd = P.nd[x];
+    return N;
+}
+
+PTL_HD GenLane gen_lane(const Prog& P, const GenNode& N, uint32_t s) {
     GenLane L;
-    const uint32_t t = P.nt[x];
-    const uint32_t rt = P.rt[x];
+    const uint32_t t = N.t;
+    const uint32_t rt = N.rt;
     L.has = P.tab.has_instr(t, s, rt);
     L.prop = L.has || s == 0;
-    L.par = L.prop ? u32(P.par[x]) : 0u;
+    L.par = L.prop ? N.par : 0u;
     L.nopar = s32(L.par) == -1;
     L.lfp = !L.nopar && L.prop;
-    L.pt = L.lfp ? P.nt[s32(L.par)] : 0u;
-    L.ci = L.lfp ? u32(P.ci[x]) : 0u;
+    L.pt = L.lfp ? N.ntp : 0u;
+    L.ci = L.lfp ? N.ci : 0u;
     L.nonc = ((L.pt & RV_IF) == RV_IF) && !(L.ci == (L.pt & 1u));
     L.call = L.nonc;
     if ((L.nopar || !L.nonc) && L.prop) {
@@ -385,14 +421,14 @@ PTL_HD GenLane gen_lane(const Prog& P, uint32_t x, uint32_t s) {
         if (calc == 2 && s32(rt) > 1) L.call = true;
     }
     L.pai = L.call ? s32(L.par * 3u + L.ci) : -1;
-    L.iib = s + (L.prop ? P.loc[x] : 0u);
+    L.iib = s + (L.prop ? N.loc : 0u);
     uint32_t r = 0;
     if (L.has) {
         const uint32_t calc = P.tab.out(t, s, rt);
         if (calc == 3) r |= 32u;
         if (calc == 4) r |= 10u;
-        if (calc == 1) r |= P.nd[x] + 10u;
-        if (calc == 2) r |= P.nd[x] + 42u;
+        if (calc == 1) r |= N.nd + 10u;
+        if (calc == 2) r |= N.nd + 42u;
         bool hov = L.call;
         if (calc == 0 && P.tab.has_output(t, s, rt)) hov = true;
         if (hov) r |= L.iib + 64u;
@@ -409,10 +445,11 @@ PTL_HD GenLane gen_lane(const Prog& P, uint32_t x, uint32_t s) {
 // writer (child indices 0..2), so all nodes write at once; the node's last writing lane
 // wins, as in the reference.
 PTL_HD void st_gen_prop(const Prog& P, uint32_t x) {
+    const GenNode N = gen_node(P, x);
     int32_t target = -1;
     uint32_t value = 0;
     for (uint32_t s = 0; s < 4; ++s) {
-        const GenLane L = gen_lane(P, x, s);
+        const GenLane L = gen_lane(P, N, s);
         if (L.pai >= 0) {
             target = L.pai;
             value = L.dpv;
@@ -421,25 +458,27 @@ PTL_HD void st_gen_prop(const Prog& P, uint32_t x) {
     if (target < 0) return;
     // A child index above 2 would write into another node's registers; the reference's
     // result then depends on its visiting order.  Programs from the front end never do.
-    if (u32(P.ci[x]) > 2u || u32(target) >= 3u * P.n) {
+    if (N.ci > 2u || u32(target) >= 3u * P.n) {
         record_error(P.err, ST_UNSUPPORTED, W_GEN, x);
         return;
     }
     P.regs[target] = value;
 }
 
-// Where the lane's instruction goes, rv_generator_avx.cpp:713-750.
-PTL_HD uint32_t gen_loc(const Prog& P, uint32_t x, uint32_t s, const GenLane& L) {
-    const uint32_t t = P.nt[x];
+// Where the lane's instruction goes, rv_generator_avx.cpp:713-750.  r1 / r2: the node's
+// registers 1 and 2 (read only by if-else and while nodes).
+PTL_HD uint32_t gen_loc(const Prog& P, const GenNode& N, uint32_t s, const GenLane& L, uint32_t r1, uint32_t r2) {
+    const uint32_t t = N.t;
     uint32_t loc = L.has ? L.iib : 0u;
     const bool ie = s == 1 && t == RV_IF_ELSE;
     const bool wh = s == 1 && t == RV_WHILE;
-    if (ie || wh) loc = P.regs[x * 3u + (ie ? 1u : 0u) + (wh ? 2u : 0u)];
+    if (ie) loc = r1;
+    if (wh) loc = r2;
     const bool add2 = t == RV_FUNC_DECL || (s > 1 && t == RV_FUNC_DECL_DUMMY);
     const bool fcal = s == 1 && t == RV_FUNC_CALL_ARG_LIST;
     if (add2 || fcal) loc += 2u;
     if (fcal) {
-        const int64_t prev = static_cast<int64_t>(x) - 1;
+        const int64_t prev = static_cast<int64_t>(N.x) - 1;
         if ((P.nt[prev] & RV_FUNC_CALL_ARG) == RV_FUNC_CALL_ARG) loc += u32(P.ci[prev]);
     }
     return loc;
@@ -447,36 +486,44 @@ PTL_HD uint32_t gen_loc(const Prog& P, uint32_t x, uint32_t s, const GenLane& L)
 
 // Levels run deepest first; within a level the reference visits nodes in its sorted
 // order, two nodes per body and slots in order.  A later visit overwrites an earlier
-// one at the same word, so the write with the largest key wins.
-PTL_HD unsigned long long gen_key(const Prog& P, uint32_t x, uint32_t s) {
+// one at the same word, so the write with the largest key wins.  The slot is the key's
+// low two bits.
+PTL_HD unsigned long long gen_key(const Prog& P, uint32_t x) {
     const unsigned long long lvl = static_cast<unsigned long long>(P.max_depth - u32(P.dep[x]));
-    return (lvl << 40) | (static_cast<unsigned long long>(P.pos[x]) << 2) | s;
+    return (lvl << 40) | (static_cast<unsigned long long>(P.pos[x]) << 2);
 }
 
 PTL_HD void st_gen_claim(const Prog& P, uint32_t x) {
+    const GenNode N = gen_node(P, x);
+    const unsigned long long key = gen_key(P, x);
+    const bool loop2 = N.t == RV_IF_ELSE || N.t == RV_WHILE;  // slot 1 goes where a register says
+    const uint32_t r1 = loop2 ? P.regs[x * 3u + 1u] : 0u, r2 = loop2 ? P.regs[x * 3u + 2u] : 0u;
     for (uint32_t s = 0; s < 4; ++s) {
-        const GenLane L = gen_lane(P, x, s);
+        const GenLane L = gen_lane(P, N, s);
         if (!L.has) continue;
-        const uint32_t loc = gen_loc(P, x, s, L);
+        const uint32_t loc = gen_loc(P, N, s, L, r1, r2);
         if (loc >= P.W) {
             record_error(P.err, ST_UNSUPPORTED, W_GEN, x);
             continue;
         }
-        at_max_u64(&P.owner[loc], gen_key(P, x, s));
+        at_max_u64(&P.owner[loc], key | s);
     }
 }
 
 PTL_HD void st_gen_write(const Prog& P, uint32_t x) {
-    const uint32_t t = P.nt[x];
-    const uint32_t rt = P.rt[x];
+    const GenNode N = gen_node(P, x);
+    const uint32_t t = N.t;
+    const uint32_t rt = N.rt;
+    const unsigned long long key = gen_key(P, x);
+    const uint32_t reg[3] = {P.regs[x * 3u], P.regs[x * 3u + 1u], P.regs[x * 3u + 2u]};
+    const uint32_t nd = N.nd;
     for (uint32_t s = 0; s < 4; ++s) {
-        const GenLane L = gen_lane(P, x, s);
+        const GenLane L = gen_lane(P, N, s);
         if (!L.has) continue;
-        const uint32_t loc = gen_loc(P, x, s, L);
-        if (loc >= P.W || P.owner[loc] != gen_key(P, x, s)) continue;
+        const uint32_t loc = gen_loc(P, N, s, L, reg[1], reg[2]);
+        if (loc >= P.W || P.owner[loc] != (key | s)) continue;
         // instruction word and constants, :752-779
         uint32_t w = P.tab.word(t, s, rt);
-        const uint32_t nd = P.nd[x];
         const uint32_t cc = P.tab.cnst(t, s);
         if (cc == 1) w |= nd & 0xFFFFF000u;
         if (cc == 2) w |= (nd & 0xFFFu) << 20;
@@ -488,7 +535,7 @@ PTL_HD void st_gen_write(const Prog& P, uint32_t x) {
         const uint32_t jc = P.tab.jt(t, s);
         uint32_t jv = 0;
         if (s32(jc) > 0 && !(s32(jc) > 5)) {
-            uint32_t v = P.regs[x * 3u + 1u + (s32(jc) > 2 ? 1u : 0u)];
+            uint32_t v = s32(jc) > 2 ? reg[2] : reg[1];
             if ((jc & 1u) == 0) v += 1u;
             jv = v;
         }
@@ -504,11 +551,11 @@ PTL_HD void st_gen_write(const Prog& P, uint32_t x) {
             const uint32_t c = P.tab.opd(t, s, rt, k);
             uint32_t a = 0;
             if (c == 1 || c == 4 || c == 5 || c == 6) {
-                uint32_t ri = x * 3u;
+                uint32_t ri = 0;
                 if (c == 1) ri += k;
                 if (c == 4 || c == 5) ri += 1u;
                 if (c == 5) ri -= k;
-                a = P.regs[ri];
+                a = ri == 0 ? reg[0] : (ri == 1 ? reg[1] : reg[2]);
             }
             if (c == 2) a |= nd + 10u;
             if (c == 3) a |= nd + 42u;
