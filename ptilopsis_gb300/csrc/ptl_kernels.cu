@@ -253,6 +253,29 @@ __device__ __forceinline__ uint32_t block_reduce_add(uint32_t v, uint32_t* sm) {
 
 constexpr uint32_t kSortItems = kSortTile / kThreads;  // 8 per thread
 
+// Exclusive prefix sums of a and b over the block's threads (kThreads), by warp shuffles
+// and one pass over the warp totals; *tot receives the two block totals.  sm holds
+// 2 * kThreads / 32 + 2 words; the caller synchronises before reusing it.
+__device__ __forceinline__ void block_excl_scan2(uint32_t a, uint32_t b, uint32_t* sm, uint32_t* ea, uint32_t* eb,
+                                                 uint32_t* tot) {
+    constexpr uint32_t W = kThreads / 32;
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    const uint32_t ia = warp_incl_scan(a), ib = warp_incl_scan(b);
+    if (lane == 31) { sm[warp] = ia; sm[W + warp] = ib; }
+    __syncthreads();
+    if (warp == 0) {
+        const uint32_t va = lane < W ? sm[lane] : 0u, vb = lane < W ? sm[W + lane] : 0u;
+        const uint32_t sa = warp_incl_scan(va), sb = warp_incl_scan(vb);
+        if (lane < W) { sm[lane] = sa - va; sm[W + lane] = sb - vb; }
+        if (lane == W - 1) { sm[2 * W] = sa; sm[2 * W + 1] = sb; }
+    }
+    __syncthreads();
+    *ea = sm[warp] + ia - a;
+    *eb = sm[W + warp] + ib - b;
+    tot[0] = sm[2 * W];
+    tot[1] = sm[2 * W + 1];
+}
+
 // Stop counts per tile, and the least and greatest key of each segment (atomics on the
 // segment record; a part of the next split is known to hold one key when its bound on
 // the pivot's side meets the pivot).
@@ -296,51 +319,36 @@ __global__ void __launch_bounds__(kThreads) k_sort_count(SortScratch ss, SortSeg
 }
 
 __global__ void __launch_bounds__(kThreads) k_sort_segscan(SortScratch ss, SortSeg* cur) {
-    __shared__ uint32_t sl[kThreads], sr[kThreads];
-    __shared__ uint32_t carry_l, carry_r;
+    __shared__ uint32_t sm[2 * kThreads / 32 + 2];
     if (sort_overflow(ss)) return;
     const uint32_t nseg = sort_nseg(ss);
     for (uint32_t si = blockIdx.x; si < nseg; si += gridDim.x) {
         SortSeg& g = cur[si];
-        if (threadIdx.x == 0) { carry_l = 0; carry_r = 0; }
-        __syncthreads();
+        uint32_t carry_l = 0, carry_r = 0;
         for (uint32_t c = 0; c < g.tcount; c += kThreads) {
             const uint32_t k = c + threadIdx.x;
             const uint32_t vl = k < g.tcount ? ss.tile_l[g.tbase + k] : 0u;
             const uint32_t vr = k < g.tcount ? ss.tile_r[g.tbase + k] : 0u;
-            sl[threadIdx.x] = vl;
-            sr[threadIdx.x] = vr;
-            __syncthreads();
-            for (uint32_t d = 1; d < kThreads; d <<= 1) {
-                const uint32_t al = threadIdx.x >= d ? sl[threadIdx.x - d] : 0u;
-                const uint32_t ar = threadIdx.x >= d ? sr[threadIdx.x - d] : 0u;
-                __syncthreads();
-                sl[threadIdx.x] += al;
-                sr[threadIdx.x] += ar;
-                __syncthreads();
-            }
+            uint32_t el, er, tot[2];
+            block_excl_scan2(vl, vr, sm, &el, &er, tot);
             if (k < g.tcount) {
-                ss.tile_l[g.tbase + k] = carry_l + sl[threadIdx.x] - vl;
-                ss.tile_r[g.tbase + k] = carry_r + sr[threadIdx.x] - vr;
+                ss.tile_l[g.tbase + k] = carry_l + el;
+                ss.tile_r[g.tbase + k] = carry_r + er;
             }
-            __syncthreads();
-            if (threadIdx.x == 0) {
-                carry_l += sl[kThreads - 1];
-                carry_r += sr[kThreads - 1];
-            }
+            carry_l += tot[0];
+            carry_r += tot[1];
             __syncthreads();
         }
         if (threadIdx.x == 0) {
             g.nL = carry_l;
             g.nR = carry_r;
         }
-        __syncthreads();
     }
 }
 
 // Stop positions by rank: A[rank] for L-stops, B[rank from the right] for R-stops.
 __global__ void __launch_bounds__(kThreads) k_sort_pos(SortScratch ss, const SortSeg* cur) {
-    __shared__ uint32_t sl[kThreads], sr[kThreads];
+    __shared__ uint32_t sm[2 * kThreads / 32 + 2];
     if (sort_overflow(ss)) return;
     const uint32_t ntiles = sort_ntiles(ss);
     for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
@@ -358,19 +366,10 @@ __global__ void __launch_bounds__(kThreads) k_sort_pos(SortScratch ss, const Sor
                 if (is_rstop(key, g.pivot)) { fr |= 1u << k; ++cr; }
             }
         }
-        sl[threadIdx.x] = cl;
-        sr[threadIdx.x] = cr;
-        __syncthreads();
-        for (uint32_t d = 1; d < kThreads; d <<= 1) {
-            const uint32_t al = threadIdx.x >= d ? sl[threadIdx.x - d] : 0u;
-            const uint32_t ar = threadIdx.x >= d ? sr[threadIdx.x - d] : 0u;
-            __syncthreads();
-            sl[threadIdx.x] += al;
-            sr[threadIdx.x] += ar;
-            __syncthreads();
-        }
-        uint32_t rl = ss.tile_l[t] + sl[threadIdx.x] - cl;
-        uint32_t rr = ss.tile_r[t] + sr[threadIdx.x] - cr;
+        uint32_t el, er, tot[2];
+        block_excl_scan2(cl, cr, sm, &el, &er, tot);
+        uint32_t rl = ss.tile_l[t] + el;
+        uint32_t rr = ss.tile_r[t] + er;
 #pragma unroll
         for (uint32_t k = 0; k < kSortItems; ++k) {
             const uint32_t p = p0 + k;

@@ -103,7 +103,7 @@ def test_depth_order_emulation_equals_std_sort(built, mode):
     rng = np.random.default_rng(hash(mode) & 0xFFFF)
     for case in range(48):
         # up to 8,192 keys one block sorts the array; above, partition rounds come first
-        n = int(rng.integers(1, 6000)) if case < 40 else int(rng.integers(8193, 60000))
+        n = int(rng.integers(1, 6000)) if case < 40 else int(rng.integers(8193, 80000))
         kmax = int(rng.integers(1, 80))
         if mode == "random":
             keys = rng.integers(0, kmax, n)
