@@ -168,7 +168,10 @@ struct Model {
         }
         for (int p = 0; p < 64; ++p) { sh.R0[p] = 0xFFFFFFFFu; sh.R0own[p] = 0xFFFFFFFFu; }
         if (S > 0) for (uint32_t p = 0; p < 64; ++p) ra2_begin_p(sh, 0, p, P.trig_min[p], P.trig_max[p], hashed);
-        for (uint32_t i = 0; i < S; ++i) {
+        uint32_t s0 = 0;  // steps with a lane-0 function still running
+        for (uint32_t j = 0; j < G0; ++j) s0 = std::max(s0, ra2_lane0_size(L[j]));
+        s0 = std::min(s0, S);
+        for (uint32_t i = 0; i < s0; ++i) {
             bool in_row0 = false;
             for (uint32_t j = 0; j < G0; ++j) {
                 ra2_load(P, L[j], i, cur.data() + 4 * j);
@@ -198,6 +201,9 @@ struct Model {
                                 P.trig_max[static_cast<size_t>(i + 1) * 64 + p], hashed);
                 }
             }
+        }
+        {  // the steps after the last lane-0 function only mark row 0's symbols
+            for (uint32_t p = 0; p < 64; ++p) ra2_tail_p(P, c, sh, p, s0, S);
         }
         P = Psave;
     }

@@ -942,7 +942,7 @@ __device__ bool ra_wait_chunk(const uint32_t* done, uint32_t c, uint32_t need, E
 template <int Q>
 __device__ void ra_lane0_block(const Prog& P, uint32_t S, uint32_t K, uint32_t chunks, unsigned char* smem) {
     const uint32_t tid = threadIdx.x, T = blockDim.x;
-    __shared__ uint32_t s_abort;
+    __shared__ uint32_t s_abort, s_s0;
     const uint32_t* hist = P.ra_chunks;
     const uint32_t* done = P.ra_chunks + chunks;
     Ra2Shared& sh = *reinterpret_cast<Ra2Shared*>(smem);
@@ -955,24 +955,31 @@ __device__ void ra_lane0_block(const Prog& P, uint32_t S, uint32_t K, uint32_t c
     // Row-0 phases: thread tid handles physical registers tid, tid + T, ... (two each in a
     // one-warp block, which small programs get: its barriers cost next to nothing).
     constexpr uint32_t kRow = 64;
-    // thread 0: independent functions still running in chunk wc (need)
-    uint32_t need = 0, wc = 0;
+    // thread 0: independent functions still running in chunk wc (need); chunks below
+    // `waited` are complete
+    uint32_t need = 0, wc = 0, waited = 0;
     auto wait_for = [&](uint32_t chunk) {
         while (wc < chunk) need -= hist[wc++];
         if (!ra_wait_chunk(done, chunk, need, P.err)) s_abort = 1;
+        waited = chunk + 1;
     };
     if (tid == 0) {
         s_abort = 0;
+        s_s0 = 0;
         for (uint32_t x = 0; x < chunks; ++x) need += hist[x];
         if (chunks > 0 && S > 0) wait_for(0);
     }
+    __syncthreads();
     Ra2Slot L[Q];
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
         const uint32_t j = tid + static_cast<uint32_t>(q) * T;
         L[q].act = false;
         L[q].have_next = false;
-        if (j < G0) ra2_slot_init(P, c, L[q], j, j);
+        if (j < G0) {
+            ra2_slot_init(P, c, L[q], j, j);
+            atomicMax(&s_s0, ra2_lane0_size(L[q]));
+        }
     }
     uint32_t tmin[2] = {0xFFFFFFFFu, 0xFFFFFFFFu}, tmax[2] = {0, 0};  // trigger records, one step ahead
     for (uint32_t p = tid; p < kRow; p += T) {
@@ -997,8 +1004,10 @@ __device__ void ra_lane0_block(const Prog& P, uint32_t S, uint32_t K, uint32_t c
     }
     __syncthreads();
     // Per step, three barriers: (load+compute) | (check + speculative apply + clear next
-    // hash) | (marks, row 0, next step's snapshot).
-    for (uint32_t i = 0; i < S; ++i) {
+    // hash) | (marks, row 0, next step's snapshot).  Steps run while a lane-0 function is
+    // still running (s0); the rest come down to ra2_tail_p.
+    const uint32_t s0 = min(s_s0, S);
+    for (uint32_t i = 0; i < s0; ++i) {
         if (tid == 0 && chunks > 0 && i + 2 < S && (i + 2) % kRaChunk == 0) wait_for((i + 2) / kRaChunk);
         bool in_row0 = false;
 #pragma unroll
@@ -1068,6 +1077,13 @@ __device__ void ra_lane0_block(const Prog& P, uint32_t S, uint32_t K, uint32_t c
         }
         __syncthreads();
     }
+    if (s0 >= S || s_abort) return;
+    // the remaining steps' trigger records, then one check per row-0 position
+    if (tid == 0)
+        for (uint32_t x = waited; x < chunks && !s_abort; ++x) wait_for(x);
+    __syncthreads();
+    if (s_abort) return;
+    for (uint32_t p = tid; p < kRow; p += T) ra2_tail_p(P, c, sh, p, s0, S);
 }
 
 

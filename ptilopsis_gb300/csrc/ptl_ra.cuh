@@ -402,4 +402,34 @@ PTL_HD void ra2_end_p(const Prog& P, const SymCache& c, Ra2Shared& sh, uint32_t 
     }
 }
 
+// ---------------------------------------------------------------- the tail of the pass
+// Steps that change row 0: every lane-0 function has run its last step by s0 (the
+// longest lane-0 function).  From s0 on no slot is active, so no slot writes row 0 or
+// updates a symbol, and a step only marks the symbol row 0 holds at each position that
+// another function triggers.  Row 0 no longer changes and a mark only sets a flag, so the
+// steps s0..S-1 come down to one check per position (ra2_tail_p).
+PTL_HD uint32_t ra2_lane0_size(const Ra2Slot& L) { return s32(L.size) > 0 ? L.size : 0u; }
+
+PTL_HD uint32_t ld_records(const uint32_t* p) {
+#if defined(__CUDA_ARCH__)
+    return __ldcg(p);  // written by other blocks
+#else
+    return *p;
+#endif
+}
+
+// Position p after step s0-1: its symbol is marked when any step in [s0, S) has another
+// function's trigger record there.
+PTL_HD void ra2_tail_p(const Prog& P, const SymCache& c, const Ra2Shared& sh, uint32_t p, uint32_t s0, uint32_t S) {
+    const uint32_t v = sh.R0[p];
+    if (s32(v - 64u) < 0) return;
+    bool hit = false;
+    for (uint32_t i = s0; i < S && !hit; i += 8) {
+#pragma unroll
+        for (uint32_t k = 0; k < 8; ++k)
+            if (i + k < S) hit |= ld_records(&P.trig_min[static_cast<size_t>(i + k) * 64u + p]) != 0xFFFFFFFFu;
+    }
+    if (hit) sym_mark(P, c, sh.R0own[p], v);
+}
+
 }  // namespace ptl
