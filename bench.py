@@ -57,6 +57,30 @@ STAGE_BYTES = {
 }
 
 
+def stage_rooflines(stage_ms, tot, peak):
+    """Per stage: algorithmic bytes over its event-timed time, as a fraction of the HBM
+    peak; the scan, generation and compaction stages (isn_cnt, isn_gen, optimize) as a
+    group; regalloc also as instruction steps per second (its step loop is a dependent
+    chain per function, not a bandwidth-bound pass)."""
+    from ptilopsis_gb300 import STAGES
+    out, grp_b, grp_ms = {}, 0.0, 0.0
+    for s, ms in zip(STAGES, stage_ms):
+        if s not in STAGE_BYTES or ms <= 0:
+            continue
+        b = STAGE_BYTES[s](tot["n"], tot["W"], tot["W2"], tot["W3"])
+        gbs = b / (ms / 1000.0) / 1e9
+        out[s] = {"ms": round(float(ms), 3), "algorithmic_bytes": int(b), "achieved_gbs": round(gbs, 1),
+                  "frac": round(gbs / peak, 4)}
+        if s in ("isn_cnt", "isn_gen", "optimize"):
+            grp_b += b
+            grp_ms += ms
+    group = {"stages": ["isn_cnt", "isn_gen", "optimize"], "algorithmic_bytes": int(grp_b),
+             "ms": round(grp_ms, 3), "frac": round(grp_b / (grp_ms / 1000.0) / 1e9 / peak, 4) if grp_ms else None}
+    ra_ms = float(stage_ms[STAGES.index("regalloc")])
+    ra = {"instruction_steps": int(tot["W"]), "steps_per_s": tot["W"] / (ra_ms / 1000.0) if ra_ms else None}
+    return {"stages": out, "scan_gen_compaction": group, "regalloc_steps": ra}
+
+
 def env_rank():
     return (int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)),
             int(os.environ.get("LOCAL_RANK", 0)))
@@ -344,7 +368,8 @@ def run_batched(args):
     roofline = {"bound": "hbm", "kernel": f"{name} stage (all programs)", "achieved": achieved, "peak": peak,
                 "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind, "traffic": None,
                 "algorithmic_bytes_per_launch": int(alg),
-                "stage_ms": {s: round(float(v), 3) for s, v in zip(STAGES, stage_ms)}}
+                "stage_ms": {s: round(float(v), 3) for s, v in zip(STAGES, stage_ms)},
+                **stage_rooflines(stage_ms, tot, peak)}
 
     # the plain pipeline on a sample of the same programs, one at a time
     sample = trees[:args.plain_sample]
@@ -486,7 +511,8 @@ def run_gb300(args):
     roofline = {"bound": "hbm", "kernel": f"{name} stage", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "peak_source": peak_kind, "traffic": None,
                 "algorithmic_bytes_per_launch": int(alg),
-                "stage_ms": {s: round(float(v), 4) for s, v in zip(STAGES, stage_ms)}}
+                "stage_ms": {s: round(float(v), 4) for s, v in zip(STAGES, stage_ms)},
+                **stage_rooflines(stage_ms, {"n": n, "W": sizes["W"], "W2": sizes["W2"], "W3": W3}, peak)}
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_all, "higher_is_better": True, "scaling": "weak",
