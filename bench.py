@@ -243,8 +243,9 @@ def run_reference(args):
 def run_serving(device, args):
     """Open-loop Poisson arrivals of compile requests (80% 1k..10k nodes, 20% lognormal in
     100k..2M) at each rate; latency = completion - scheduled arrival, on the server's
-    clock.  The submitter is one Python thread: a rate it cannot keep up with shows as a
-    lower achieved rate (and as latency, since arrivals are scheduled)."""
+    clock.  The submitter is one Python thread lending each request's arrays to the server
+    (no copy at submit); a rate it cannot keep up with shows as a lower achieved rate (and
+    as latency, since arrivals are scheduled)."""
     from concurrent.futures import ThreadPoolExecutor
     from ptilopsis_gb300 import RvGenerator
     from ptilopsis_gb300.batch import CompileServer, clock_ns
@@ -256,7 +257,7 @@ def run_serving(device, args):
     out = {"slots": args.serve_slots, "memory_budget_gb": 120, "requests": n_req,
            "request_nodes_mean": float(np.mean([t.n for t in reqs])), "rates": []}
     with CompileServer(device=device, slots=args.serve_slots, memory_budget=120 << 30) as srv:
-        for t in [srv.submit(r) for r in reqs[:8]]:  # warm-up: arenas and code paths
+        for t in [srv.submit(r, copy=False) for r in reqs[:8]]:  # warm-up: arenas and code paths
             srv.result(t)
             srv.release(t)
         for rate in args.serve_rates:
@@ -268,7 +269,7 @@ def run_serving(device, args):
                 due = t0 + int(sched[k] * 1e9)
                 while clock_ns() < due:
                     pass
-                tickets.append(srv.submit(tr))
+                tickets.append(srv.submit(tr, copy=False))  # the requests outlive their tickets
             submit_end = clock_ns()
             lat, last = [], 0
             for k, tk in enumerate(tickets):

@@ -184,6 +184,11 @@ ptl_status ptl_server_create(int device, int slots, uint64_t memory_budget, ptl_
 /* Copies a host tree into a request and queues it; PTL_ADMISSION_DENIED when the request
  * alone exceeds the budget. */
 ptl_status ptl_server_submit(ptl_server* server, const ptl_ast_view* tree, uint64_t* ticket);
+/* As ptl_server_submit; with PTL_SUBMIT_BORROW the request refers to the caller's arrays
+ * instead of copying them (submit costs O(1)), and the caller keeps them alive and
+ * unchanged until ptl_server_release of the ticket. */
+#define PTL_SUBMIT_BORROW 1u
+ptl_status ptl_server_submit_flags(ptl_server* server, const ptl_ast_view* tree, uint32_t flags, uint64_t* ticket);
 /* *done = 1 once the request finished (wait != 0 blocks until then); returns its status. */
 ptl_status ptl_server_poll(ptl_server* server, uint64_t ticket, int wait, int* done);
 /* Output of a finished request (the table pointers may be NULL); valid until release. */

@@ -41,6 +41,7 @@ def _bind(L):
     L.ptl_batch_destroy.restype = None
     L.ptl_server_create.argtypes = [ctypes.c_int, ctypes.c_int, u64, ctypes.POINTER(vp)]
     L.ptl_server_submit.argtypes = [vp, ctypes.POINTER(_AstView), ctypes.POINTER(u64)]
+    L.ptl_server_submit_flags.argtypes = [vp, ctypes.POINTER(_AstView), ctypes.c_uint32, ctypes.POINTER(u64)]
     L.ptl_server_poll.argtypes = [vp, u64, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
     L.ptl_server_result.argtypes = [vp, u64, ctypes.POINTER(_u32p), ctypes.POINTER(sz)] + \
         [ctypes.POINTER(_u32p)] * 4 + [ctypes.POINTER(sz)]
@@ -53,7 +54,7 @@ def _bind(L):
     L.ptl_clock_ns.restype = u64
     for fn in ("ptl_batch_create", "ptl_batch_compile", "ptl_batch_status", "ptl_batch_words", "ptl_batch_stage_ns",
                "ptl_batch_copied_bytes", "ptl_batch_sizes", "ptl_batch_host_ns",
-               "ptl_batch_function_table", "ptl_server_create", "ptl_server_submit", "ptl_server_poll",
+               "ptl_batch_function_table", "ptl_server_create", "ptl_server_submit", "ptl_server_submit_flags", "ptl_server_poll",
                "ptl_server_result", "ptl_server_times", "ptl_server_release", "ptl_server_stats"):
         getattr(L, fn).restype = ctypes.c_int
     L._ptl_batch_bound = True
@@ -174,17 +175,22 @@ class CompileServer:
     def __init__(self, device: int = 0, slots: int = 2, memory_budget: int = 120 << 30):
         self._lib = _bind(lib())
         self._h = ctypes.c_void_p()
+        self._held = {}  # ticket -> the arrays a borrowed request refers to
         st = self._lib.ptl_server_create(device, slots, memory_budget, ctypes.byref(self._h))
         if st != 0:
             raise PtlError(st, "ptl_server_create")
 
-    def submit(self, tree: DepthTree) -> int:
+    def submit(self, tree: DepthTree, copy: bool = True) -> int:
+        """Queues a host tree.  copy=False lends the tree's arrays to the server instead of
+        copying them (the server keeps a reference until release(ticket))."""
         keep: list = []
         view = _view(tree, keep)
         t = ctypes.c_uint64()
-        st = self._lib.ptl_server_submit(self._h, ctypes.byref(view), ctypes.byref(t))
+        st = self._lib.ptl_server_submit_flags(self._h, ctypes.byref(view), 0 if copy else 1, ctypes.byref(t))
         if st != 0:
             raise PtlError(st, "ptl_server_submit")
+        if not copy:
+            self._held[int(t.value)] = keep
         return int(t.value)
 
     def poll(self, ticket: int, wait: bool = False) -> bool:
@@ -215,7 +221,8 @@ class CompileServer:
         return int(t[0]), int(t[1]), int(t[2])
 
     def release(self, ticket: int) -> None:
-        self._lib.ptl_server_release(self._h, ticket)
+        if self._lib.ptl_server_release(self._h, ticket) == 0:
+            self._held.pop(ticket, None)
 
     def stats(self) -> dict:
         s = (ctypes.c_uint64 * 5)()
@@ -227,6 +234,7 @@ class CompileServer:
         if self._h:
             self._lib.ptl_server_destroy(self._h)
             self._h = ctypes.c_void_p()
+        self._held.clear()
 
     def __enter__(self):
         return self

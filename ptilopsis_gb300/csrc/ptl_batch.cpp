@@ -145,19 +145,23 @@ extern "C" void ptl_batch_destroy(ptl_batch* b) { delete b; }
 // ===================================================================== server
 namespace {
 
-// A request owns a copy of its tree (the caller's arrays may go away after submit).
+// A request owns a copy of its tree (the caller's arrays may go away after submit), or,
+// submitted with PTL_SUBMIT_BORROW, refers to the caller's arrays until it is released.
 struct Request {
     uint64_t ticket = 0;
     size_t n = 0, max_depth = 0;
     std::vector<uint8_t> type, rtype;
     std::vector<int32_t> parent, depth, child;
     std::vector<uint32_t> data;
+    bool borrowed = false;
+    ptl_ast_view borrowed_view{};
     uint64_t bytes = 0;        // admission estimate
     uint64_t t_submit = 0, t_start = 0, t_done = 0;
     bool done = false;
     Result result;
 
     ptl_ast_view view() const {
+        if (borrowed) return borrowed_view;
         return ptl_ast_view{n,           max_depth,    type.data(),  rtype.data(), parent.data(),
                             depth.data(), child.data(), data.data(), 0};
     }
@@ -271,7 +275,12 @@ extern "C" ptl_status ptl_server_create(int device, int slots, uint64_t memory_b
 }
 
 extern "C" ptl_status ptl_server_submit(ptl_server* s, const ptl_ast_view* tree, uint64_t* ticket) {
-    if (!s || !tree || !ticket || tree->on_device) return PTL_BAD_ARGUMENT;
+    return ptl_server_submit_flags(s, tree, 0, ticket);
+}
+
+extern "C" ptl_status ptl_server_submit_flags(ptl_server* s, const ptl_ast_view* tree, uint32_t flags,
+                                              uint64_t* ticket) {
+    if (!s || !tree || !ticket || tree->on_device || (flags & ~PTL_SUBMIT_BORROW)) return PTL_BAD_ARGUMENT;
     auto req = std::make_shared<Request>();
     const size_t n = tree->n;
     req->n = n;
@@ -280,12 +289,17 @@ extern "C" ptl_status ptl_server_submit(ptl_server* s, const ptl_ast_view* tree,
     if (req->bytes > s->budget) return PTL_ADMISSION_DENIED;  // could never be admitted
     if (n && (!tree->type || !tree->rtype || !tree->parent || !tree->depth || !tree->child_idx || !tree->data))
         return PTL_BAD_ARGUMENT;
-    req->type.assign(tree->type, tree->type + n);
-    req->rtype.assign(tree->rtype, tree->rtype + n);
-    req->parent.assign(tree->parent, tree->parent + n);
-    req->depth.assign(tree->depth, tree->depth + n);
-    req->child.assign(tree->child_idx, tree->child_idx + n);
-    req->data.assign(tree->data, tree->data + n);
+    if (flags & PTL_SUBMIT_BORROW) {
+        req->borrowed = true;
+        req->borrowed_view = *tree;
+    } else {
+        req->type.assign(tree->type, tree->type + n);
+        req->rtype.assign(tree->rtype, tree->rtype + n);
+        req->parent.assign(tree->parent, tree->parent + n);
+        req->depth.assign(tree->depth, tree->depth + n);
+        req->child.assign(tree->child_idx, tree->child_idx + n);
+        req->data.assign(tree->data, tree->data + n);
+    }
     {
         std::lock_guard<std::mutex> lk(s->mu);
         req->ticket = s->next_ticket++;

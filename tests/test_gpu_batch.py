@@ -67,12 +67,15 @@ def test_batch_uneven_sizes(built_cuda):
             _assert_same(b.result(k), w, tab, f"program {k} ({t.n} nodes)")
 
 
-def test_server_results_same_alone_and_in_the_mix(built_cuda):
+@pytest.mark.parametrize("copy", [True, False])
+def test_server_results_same_alone_and_in_the_mix(built_cuda, copy):
+    """Requests compiled in the server's batches equal each tree compiled alone, whether
+    the server copies a request's arrays or borrows them (PTL_SUBMIT_BORROW)."""
     from ptilopsis_gb300.batch import CompileServer
     trees = _programs(40, seed0=0x50544CB0)
     alone = [_alone(t) for t in trees]
     with CompileServer(slots=6, memory_budget=8 << 30) as srv:
-        tickets = [srv.submit(t) for t in trees]
+        tickets = [srv.submit(t, copy=copy) for t in trees]
         for k, tk in enumerate(tickets):
             _assert_same(srv.result(tk), *alone[k], f"request {k}")
             s, st, d = srv.times(tk)
