@@ -327,7 +327,19 @@ def run_batched(args):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         return float(t.item())
 
-    bc = BatchCompiler(device=local, workers=min(32, os.cpu_count() or 8))
+    # tile sizes by measurement, on other programs of the same distribution (untimed)
+    tiles = None
+    if not args.no_autotune:
+        from concurrent.futures import ThreadPoolExecutor
+        from ptilopsis_gb300.batch import autotune
+        from ptilopsis_gb300.synth import config_params, generate
+        with ThreadPoolExecutor(min(32, os.cpu_count() or 8)) as ex:
+            tune = list(ex.map(lambda k: generate(config_params("c3", program=1_000_000 + 512 * rank + k)),
+                               range(min(512, args.programs))))
+        tuned = autotune(tune, device=local, workers=min(32, os.cpu_count() or 8), save=False)
+        tiles = (tuned["elem_tile"], tuned["sweep_tile"])
+        del tune
+    bc = BatchCompiler(device=local, workers=min(32, os.cpu_count() or 8), tiles=tiles)
     for _ in range(args.warmup):
         bc.compile(trees)
     barrier()
@@ -399,7 +411,10 @@ def run_batched(args):
                                    f"{nodes} nodes, {tot['W3']} output words",
                        "programs": len(trees), "nodes": nodes, "words": tot["W3"],
                        "l2": "working set (~60 GB) > L2; no flush needed",
-                       "parallelism": f"replicas x{world} (each GPU its own batch)"},
+                       "parallelism": f"replicas x{world} (each GPU its own batch)",
+                       "tiles": {"elem": bc.tiles()[0], "sweep": bc.tiles()[1],
+                                 "chosen_by": "defaults" if tiles is None else
+                                 "autotune on 512 other programs of the same distribution"}},
             "e2e": e2e, "plain": plain, "batched_over_plain": value / plain["value"],
             "roofline": roofline, "gpu_launches": int(launches)}
     bc.close()
@@ -563,6 +578,7 @@ def main():
     ap.add_argument("--cpu-nodes", type=int, default=30_000_000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--serve-requests", type=int, default=1000)
     ap.add_argument("--serve-slots", type=int, default=2)
     ap.add_argument("--serve-rates", type=float, nargs="+", default=[1000.0, 10000.0, 50000.0])

@@ -170,6 +170,12 @@ const char* ptl_batch_last_error(const ptl_batch* batch);
 /* Host-side parts of the last compile, ns: gathering the inputs into pinned memory, the
  * input copy and the output copy (both device-timed). */
 ptl_status ptl_batch_host_ns(const ptl_batch* batch, uint64_t ns[3]);
+/* Elements per tile of the batched element-wise stages (a power of two, 256..65536) and of
+ * the optimize sweeps (512, 1024 or 2048); defaults 1024 and 1024.  No reference
+ * counterpart: the reference's -i flag (minimum work per thread) is its nearest knob.
+ * ptilopsis_gb300.batch.autotune measures the candidates and caches the choice. */
+ptl_status ptl_batch_set_tiles(ptl_batch* batch, uint32_t elem_tile, uint32_t sweep_tile);
+ptl_status ptl_batch_tiles(const ptl_batch* batch, uint32_t tiles[2]);
 void ptl_batch_destroy(ptl_batch* batch);
 
 /* ---- Compile server.  No counterpart in the reference.  Continuous batching over

@@ -10,12 +10,14 @@ identical to compiling it alone.
 from __future__ import annotations
 
 import ctypes
+import json
+import os
 from dataclasses import dataclass
 from typing import List, Optional, Sequence
 
 import numpy as np
 
-from .codegen import DepthTree, PtlError, _AstView, _view, lib
+from .codegen import DepthTree, PtlError, _AstView, _view, device_info, lib
 
 _u32p = ctypes.POINTER(ctypes.c_uint32)
 
@@ -37,6 +39,8 @@ def _bind(L):
     L.ptl_batch_copied_bytes.argtypes = [vp, ctypes.POINTER(u64), ctypes.POINTER(u64)]
     L.ptl_batch_last_error.argtypes = [vp]
     L.ptl_batch_last_error.restype = ctypes.c_char_p
+    L.ptl_batch_set_tiles.argtypes = [vp, ctypes.c_uint32, ctypes.c_uint32]
+    L.ptl_batch_tiles.argtypes = [vp, ctypes.POINTER(ctypes.c_uint32)]
     L.ptl_batch_destroy.argtypes = [vp]
     L.ptl_batch_destroy.restype = None
     L.ptl_server_create.argtypes = [ctypes.c_int, ctypes.c_int, u64, ctypes.POINTER(vp)]
@@ -53,7 +57,7 @@ def _bind(L):
     L.ptl_clock_ns.argtypes = []
     L.ptl_clock_ns.restype = u64
     for fn in ("ptl_batch_create", "ptl_batch_compile", "ptl_batch_status", "ptl_batch_words", "ptl_batch_stage_ns",
-               "ptl_batch_copied_bytes", "ptl_batch_sizes", "ptl_batch_host_ns",
+               "ptl_batch_copied_bytes", "ptl_batch_sizes", "ptl_batch_host_ns", "ptl_batch_set_tiles", "ptl_batch_tiles",
                "ptl_batch_function_table", "ptl_server_create", "ptl_server_submit", "ptl_server_submit_flags", "ptl_server_poll",
                "ptl_server_result", "ptl_server_times", "ptl_server_release", "ptl_server_stats"):
         getattr(L, fn).restype = ctypes.c_int
@@ -78,16 +82,93 @@ def clock_ns() -> int:
     return int(_bind(lib()).ptl_clock_ns())
 
 
+# ---- tile-size autotuning
+ELEM_TILES = (1024, 2048, 4096, 8192)   # candidates for the element-wise stages
+SWEEP_TILES = (512, 1024, 2048)         # candidates for the optimize sweeps
+
+
+def autotune_cache_path() -> str:
+    """Where tuned tile sizes are kept (PTL_AUTOTUNE_CACHE overrides)."""
+    return os.environ.get("PTL_AUTOTUNE_CACHE",
+                          os.path.join(os.path.expanduser("~"), ".cache", "ptilopsis_gb300", "autotune.json"))
+
+
+def _device_key(device: int) -> str:
+    d = device_info(device) or {"name": "unknown", "sm_count": 0, "cc": (0, 0)}
+    return f"{d['name']}|sm_{d['cc'][0]}{d['cc'][1]}|{d['sm_count']}SM"
+
+
+def cached_tiles(device: int = 0) -> Optional[tuple]:
+    """(element tile, sweep tile) tuned earlier for this device, or None."""
+    try:
+        with open(autotune_cache_path()) as f:
+            e = json.load(f).get(_device_key(device))
+        return (int(e["elem_tile"]), int(e["sweep_tile"])) if e else None
+    except (OSError, ValueError, KeyError, TypeError):
+        return None
+
+
+def autotune(trees: Sequence[DepthTree], device: int = 0, workers: int = 8, reps: int = 2, save: bool = True) -> dict:
+    """Chooses the tile sizes of the batched pipeline by measurement: the element-wise
+    tile first (sweep tile at its default), then the sweep tile with that choice; each
+    candidate is timed as the best of `reps` compiles of `trees` (device time of all
+    stages, CUDA events).  With save, the choice is cached for this device."""
+    def timed(b, e, w):
+        b.set_tiles(e, w)
+        best = None
+        for _ in range(reps):
+            b.compile(trees)
+            t = sum(b.stage_ns()) / 1e6
+            best = t if best is None else min(best, t)
+        return best
+
+    with BatchCompiler(device, workers, tiles=None) as b:
+        b.compile(trees)  # arenas and code paths
+        elem = {e: timed(b, e, 1024) for e in ELEM_TILES}
+        e_best = min(elem, key=elem.get)
+        sweep = {w: (elem[e_best] if w == 1024 else timed(b, e_best, w)) for w in SWEEP_TILES}
+        w_best = min(sweep, key=sweep.get)
+    out = {"elem_tile": e_best, "sweep_tile": w_best, "ms_by_elem_tile": elem, "ms_by_sweep_tile": sweep,
+           "programs": len(trees), "nodes": int(sum(t.n for t in trees)), "device": _device_key(device)}
+    if save:
+        path = autotune_cache_path()
+        try:
+            with open(path) as f:
+                table = json.load(f)
+        except (OSError, ValueError):
+            table = {}
+        table[out["device"]] = {k: out[k] for k in ("elem_tile", "sweep_tile", "programs", "nodes")}
+        os.makedirs(os.path.dirname(path), exist_ok=True)
+        with open(path, "w") as f:
+            json.dump(table, f, indent=1)
+    return out
+
+
 class BatchCompiler:
     """Compiles many programs per call through the batched pipeline (one launch per stage
-    step for the whole batch); `workers` host threads gather the inputs."""
+    step for the whole batch); `workers` host threads gather the inputs.  tiles: "cached"
+    applies this device's autotuned tile sizes when there are some, None keeps the
+    defaults, a pair (element tile, sweep tile) sets them."""
 
-    def __init__(self, device: int = 0, workers: int = 8):
+    def __init__(self, device: int = 0, workers: int = 8, tiles="cached"):
         self._lib = _bind(lib())
         self._h = ctypes.c_void_p()
         st = self._lib.ptl_batch_create(device, workers, ctypes.byref(self._h))
         if st != 0:
             raise PtlError(st, "ptl_batch_create")
+        choice = cached_tiles(device) if isinstance(tiles, str) and tiles == "cached" else tiles
+        if choice:
+            self.set_tiles(*choice)
+
+    def set_tiles(self, elem_tile: int, sweep_tile: int) -> None:
+        st = self._lib.ptl_batch_set_tiles(self._h, elem_tile, sweep_tile)
+        if st != 0:
+            raise PtlError(st, f"ptl_batch_set_tiles({elem_tile}, {sweep_tile})")
+
+    def tiles(self) -> tuple:
+        v = (ctypes.c_uint32 * 2)()
+        self._lib.ptl_batch_tiles(self._h, v)
+        return int(v[0]), int(v[1])
 
     def compile(self, trees: Sequence[DepthTree], check: bool = True) -> None:
         """Compiles the trees (host arrays); results via result(k).  With check=False a

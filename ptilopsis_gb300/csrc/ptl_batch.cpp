@@ -140,6 +140,17 @@ extern "C" ptl_status ptl_batch_host_ns(const ptl_batch* b, uint64_t ns[3]) {
     return PTL_OK;
 }
 
+extern "C" ptl_status ptl_batch_set_tiles(ptl_batch* b, uint32_t elem_tile, uint32_t sweep_tile) {
+    if (!b) return PTL_BAD_ARGUMENT;
+    return b->pipe->set_tiles(elem_tile, sweep_tile) ? PTL_OK : PTL_BAD_ARGUMENT;
+}
+
+extern "C" ptl_status ptl_batch_tiles(const ptl_batch* b, uint32_t tiles[2]) {
+    if (!b || !tiles) return PTL_BAD_ARGUMENT;
+    b->pipe->tiles(tiles);
+    return PTL_OK;
+}
+
 extern "C" void ptl_batch_destroy(ptl_batch* b) { delete b; }
 
 // ===================================================================== server

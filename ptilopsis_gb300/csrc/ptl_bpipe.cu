@@ -176,6 +176,16 @@ public:
         if (b) *b = d2h;
     }
     const char* last_error() const override { return err_text.c_str(); }
+    bool set_tiles(uint32_t e, uint32_t w) override {
+        if (!batch_tile_ok(e) || !batch_sweep_tile_ok(w)) return false;
+        elem_tile = e;
+        sweep_tile = w;
+        return true;
+    }
+    void tiles(uint32_t out[2]) const override {
+        out[0] = elem_tile;
+        out[1] = sweep_tile;
+    }
     void host_ns(uint64_t out_ns[3]) const override {
         for (int k = 0; k < 3; ++k) out_ns[k] = hns[k];
     }
@@ -198,6 +208,7 @@ public:
     // Tile table for per-program counts (inactive programs get none); uploads to slot k
     // and returns the total tile count.
     uint32_t tiles(int k, const std::vector<uint64_t>& counts, uint64_t tile, const std::vector<uint8_t>* only = nullptr) {
+        slot_tile[k] = static_cast<uint32_t>(tile);
         uint32_t* h = table_slot(k);
         uint64_t t = 0;
         for (size_t p = 0; p < B; ++p) {
@@ -209,7 +220,12 @@ public:
         cudaMemcpyAsync(dtable_slot(k), h, (B + 1) * sizeof(uint32_t), cudaMemcpyHostToDevice, s);
         return static_cast<uint32_t>(t);
     }
-    BatchLaunch bl(int k) { return BatchLaunch{progs.at<Prog>(), dtable_slot(k), static_cast<uint32_t>(B), s}; }
+    BatchLaunch bl(int k) {
+        return BatchLaunch{progs.at<Prog>(), dtable_slot(k), static_cast<uint32_t>(B), s, slot_tile[k]};
+    }
+    // tile sizes: element-wise stages, optimize sweeps (chosen by the autotuner or the defaults)
+    uint32_t elem_tile = batch_tile(), sweep_tile = 1024;
+    uint32_t slot_tile[32] = {};
 
     std::vector<Prog> hp;  // host copies of the views
     Prog* h_progs() { return reinterpret_cast<Prog*>(h_small.at<uint8_t>(small_progs_off)); }
@@ -286,7 +302,7 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
     for (auto& x : hns) x = 0;
 
     // ---- small per-program state and the pinned small area
-    constexpr int kTables = 20, kLists = 4;  // table slots 0..16 are used
+    constexpr int kTables = 20, kLists = 4;  // table slots 0..17 are used
     small_progs_off = static_cast<size_t>(kTables) * (B + 1) * 4;
     small_meta_off = small_progs_off + B * sizeof(Prog);
     small_err_off = small_meta_off + B * 16;
@@ -450,7 +466,7 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
         uint64_t* up_soff = reinterpret_cast<uint64_t*>(h_small.at<uint8_t>(small_up_off));
         std::copy(soff.begin(), soff.end(), up_soff);
         BP_CU(cudaMemcpyAsync(seen_off.p, up_soff, B * 8, cudaMemcpyHostToDevice, s));
-        const uint32_t t_n = tiles(0, n, batch_tile());
+        const uint32_t t_n = tiles(0, n, elem_tile);
         batch_stage(BatchStage::Validate, bl(0), t_n, nullptr, nullptr, nullptr);
         batch_stage(BatchStage::DepthSeen, bl(0), t_n, nullptr, seen.at<uint32_t>(), seen_off.at<uint64_t>());
         BP_CU(collect_errors());
@@ -471,7 +487,7 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
         }
 
         // ---- preprocess
-        const uint32_t t_nb8 = tiles(1, nb8, batch_tile());
+        const uint32_t t_nb8 = tiles(1, nb8, elem_tile);
         batch_stage(BatchStage::Translate, bl(1), t_nb8, nullptr, nullptr, nullptr);
         batch_stage(BatchStage::Preprocess, bl(1), t_nb8, nullptr, nullptr, nullptr);
         BP_CU(cudaEventRecord(ev[1], s));
@@ -516,7 +532,7 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
             P.lifetime = lifetime.at<unsigned long long>(e);
         }
         upload_progs();
-        const uint32_t t_fb8 = tiles(3, fb8, batch_tile());
+        const uint32_t t_fb8 = tiles(3, fb8, elem_tile);
         batch_stage(BatchStage::Functab, bl(3), t_fb8, meta.at<uint32_t>(), nullptr, nullptr);
         hm = read_meta();
         BP_CU(collect_errors());
@@ -630,7 +646,7 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
         ss.counters = counters.at<uint32_t>();
         ss.local = sort_local.at<uint32_t>();
         ss.equal = sort_equal.at<uint32_t>();
-        const uint32_t t_n2 = tiles(4, n, batch_tile());
+        const uint32_t t_n2 = tiles(4, n, elem_tile);
         batch_sort_keys(bl(4), t_n2, sa.at<unsigned long long>(), a_off.at<uint64_t>(), false);
         BP_CU(cudaMemsetAsync(counters.p, 0, 64, s));
         SortSeg* up_segs = reinterpret_cast<SortSeg*>(h_small.at<uint8_t>(small_up_off + 2 * B * 8));
@@ -669,26 +685,28 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
         BP_CU(cudaEventRecord(ev[3], s));
 
         // ---- optimize
-        const uint32_t t_wb8 = tiles(5, wb8, batch_tile());
+        const uint32_t t_wb8 = tiles(5, wb8, elem_tile);
         batch_stage(BatchStage::OptMark, bl(5), t_wb8, nullptr, nullptr, nullptr);
         uint32_t* hflag = reinterpret_cast<uint32_t*>(h_small.at<uint8_t>(small_meta_off));  // B*16 >= 8
         // sweeps after the first revisit only the tiles whose marks changed (when every
-        // virtual result is its instruction's own word; else every tile, every sweep)
-        BP_CU(dirty.ensure(2ull * t_wb8 + 64));
+        // virtual result is its instruction's own word; else every tile, every sweep);
+        // they have their own tile size
+        const uint32_t t_sw = tiles(17, wb8, sweep_tile);
+        BP_CU(dirty.ensure(2ull * t_sw + 64));
         BP_CU(cudaMemsetAsync(changed.p, 0, 8, s));
-        batch_selfdef(bl(5), t_wb8, changed.at<uint32_t>(1));
+        batch_selfdef(bl(17), t_sw, changed.at<uint32_t>(1));
         BP_CU(cudaMemcpyAsync(hflag + 1, changed.at<uint32_t>(1), 4, cudaMemcpyDeviceToHost, s));
         BP_CU(cudaStreamSynchronize(s));
         const bool worklist = hflag[1] == 0;
-        uint8_t* dbuf[2] = {dirty.at<uint8_t>(), dirty.at<uint8_t>(t_wb8 + 32)};
-        BP_CU(cudaMemsetAsync(dbuf[0], 1, t_wb8, s));
-        BP_CU(cudaMemsetAsync(dbuf[1], 0, t_wb8, s));
+        uint8_t* dbuf[2] = {dirty.at<uint8_t>(), dirty.at<uint8_t>(t_sw + 32)};
+        BP_CU(cudaMemsetAsync(dbuf[0], 1, t_sw, s));
+        BP_CU(cudaMemsetAsync(dbuf[1], 0, t_sw, s));
         int cur = 0;
         for (uint32_t sweeps = 0;;) {
             BP_CU(cudaMemsetAsync(changed.p, 0, 4, s));
             for (int k = 0; k < 4; ++k) {
-                batch_sweep(bl(5), t_wb8, changed.at<uint32_t>(), worklist ? dbuf[cur] : nullptr, dbuf[cur ^ 1]);
-                BP_CU(cudaMemsetAsync(dbuf[cur], 0, t_wb8, s));
+                batch_sweep(bl(17), t_sw, changed.at<uint32_t>(), worklist ? dbuf[cur] : nullptr, dbuf[cur ^ 1]);
+                BP_CU(cudaMemsetAsync(dbuf[cur], 0, t_sw, s));
                 cur ^= 1;
             }
             sweeps += 4;
@@ -702,7 +720,7 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
         BP_CU(cudaEventRecord(ev[4], s));
 
         // ---- regalloc
-        const uint32_t t_f = tiles(6, F, batch_tile());
+        const uint32_t t_f = tiles(6, F, elem_tile);
         batch_stage(BatchStage::InitLifetime, bl(6), t_f, nullptr, nullptr, nullptr);
         Layout Lt, Lc;
         Lt.build(trig, active);
@@ -720,7 +738,7 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
             hp[p].ra_chunks = ra_chunks.at<uint32_t>(Lc.elem(p));
         }
         upload_progs();
-        const uint32_t t_w = tiles(7, W, batch_tile());
+        const uint32_t t_w = tiles(7, W, elem_tile);
         batch_stage(BatchStage::Cross, bl(7), t_w, nullptr, nullptr, nullptr);
         uint32_t* hfl = reinterpret_cast<uint32_t*>(h_small.at<uint8_t>(small_meta_off));
         BP_CU(cudaMemcpyAsync(hfl, flags.p, B * 16, cudaMemcpyDeviceToHost, s));
@@ -761,13 +779,13 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
         const uint32_t* d_lane0 = upload_list(0, lane0_list);
         BP_CU(ra_sync.ensure(64));
         // per program: histogram of the independent functions' last chunks, then counts
-        const uint32_t t_hist = tiles(16, nfree, batch_tile(), &lane0);
+        const uint32_t t_hist = tiles(16, nfree, elem_tile, &lane0);
         batch_stage(BatchStage::RaHist, bl(16), t_hist, nullptr, nullptr, nullptr);
         BP_CU(batch_regalloc(progs.at<Prog>(), dtable_slot(8), d_lane0, static_cast<uint32_t>(lane0_list.size()),
                              ra_items, max_g0, ra_sync.at<uint32_t>(), s));
         const uint32_t* d_serial = upload_list(1, serial_list);
         batch_serial(progs.at<Prog>(), d_serial, static_cast<uint32_t>(serial_list.size()), s);
-        const uint32_t t_w_sp = tiles(13, W, batch_tile());
+        const uint32_t t_w_sp = tiles(13, W, elem_tile);
         batch_stage(BatchStage::Spill, bl(13), t_w_sp, nullptr, nullptr, nullptr);
         const uint32_t st_wb8 = tiles(9, wb8, batch_scan_tile());
         BP_CU(scan_status.ensure((static_cast<size_t>(st_wb8) + 8) * 8));
@@ -801,9 +819,9 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
             P.joffs = joffs.at<uint32_t>(e);
         }
         upload_progs();
-        const uint32_t t_wb8_sc = tiles(14, wb8, batch_tile());
+        const uint32_t t_wb8_sc = tiles(14, wb8, elem_tile);
         batch_stage(BatchStage::Scatter, bl(14), t_wb8_sc, nullptr, nullptr, nullptr);
-        const uint32_t t_f2 = tiles(10, F, batch_tile());
+        const uint32_t t_f2 = tiles(10, F, elem_tile);
         batch_stage(BatchStage::RaFunctab, bl(10), t_f2, nullptr, nullptr, nullptr);
         BP_CU(cudaEventRecord(ev[5], s));
 
@@ -833,9 +851,9 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
             hp[p].out = out.at<uint32_t>(Lo.elem(p));
         }
         upload_progs();
-        const uint32_t t_w2 = tiles(12, W2, batch_tile());
+        const uint32_t t_w2 = tiles(12, W2, elem_tile);
         batch_stage(BatchStage::FjEmit, bl(12), t_w2, nullptr, nullptr, nullptr);
-        const uint32_t t_f3 = tiles(15, F, batch_tile());
+        const uint32_t t_f3 = tiles(15, F, elem_tile);
         batch_stage(BatchStage::FjFunctab, bl(15), t_f3, nullptr, nullptr, nullptr);
         BP_CU(cudaEventRecord(ev[6], s));
         BP_CU(cudaEventRecord(ev[7], s));

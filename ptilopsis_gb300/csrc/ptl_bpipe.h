@@ -36,6 +36,10 @@ public:
     // Host-side parts of the last compile, ns: gathering the inputs into pinned memory,
     // the input copy, the output copy (device-timed).
     virtual void host_ns(uint64_t ns[3]) const = 0;
+    // Elements per tile of the element-wise stages and of the optimize sweeps; returns
+    // false (and changes nothing) for sizes the kernels do not take.
+    virtual bool set_tiles(uint32_t elem_tile, uint32_t sweep_tile) = 0;
+    virtual void tiles(uint32_t out[2]) const = 0;
     // Detail of the last failure.
     virtual const char* last_error() const = 0;
 };

@@ -1427,7 +1427,7 @@ void launch_fixjumps_emit(const Prog& P, cudaStream_t s) {
 // programs left out of a stage have no tiles).
 namespace {
 
-constexpr uint32_t kBTile = 1024;
+constexpr uint32_t kBTile = 1024;  // default; the tile is a launch parameter (BatchLaunch::tile)
 
 __device__ __forceinline__ uint32_t batch_program(const uint32_t* off, uint32_t B, uint32_t t) {
     uint32_t lo = 0, hi = B;  // off[lo] <= t < off[hi]
@@ -1440,13 +1440,13 @@ __device__ __forceinline__ uint32_t batch_program(const uint32_t* off, uint32_t 
 
 template <class Op>
 __global__ void __launch_bounds__(kThreads) k_batch(const Prog* progs, const uint32_t* off, uint32_t B, uint32_t total,
-                                                    Op op) {
+                                                    uint32_t tile, Op op) {
     for (uint32_t t = blockIdx.x; t < total; t += gridDim.x) {
         const uint32_t p = batch_program(off, B, t);
         const Prog& P = progs[p];
         const uint32_t cnt = Op::count(P);
-        const uint32_t base = (t - off[p]) * kBTile;
-        for (uint32_t k = threadIdx.x; k < kBTile; k += kThreads) {
+        const uint32_t base = (t - off[p]) * tile;
+        for (uint32_t k = threadIdx.x; k < tile; k += kThreads) {
             const uint32_t i = base + k;
             if (i < cnt) op(P, i, p);
         }
@@ -1535,17 +1535,19 @@ struct BSortOut {
 // clears make another sweep necessary; otherwise every tile is swept until a sweep
 // changes nothing.  The block writes back zeros only, so clears by other blocks are
 // never undone.
-constexpr uint32_t kSweepItems = kBTile / kThreads;
+template <uint32_t TILE>
 __global__ void __launch_bounds__(kThreads) k_batch_sweep(const Prog* progs, const uint32_t* off, uint32_t B,
                                                           uint32_t total, uint32_t* changed, const uint8_t* cur,
                                                           uint8_t* next) {
-    __shared__ uint8_t s_used[kBTile];
+    constexpr uint32_t kSweepItems = TILE / kThreads;
+    static_assert(kSweepItems >= 1 && kSweepItems <= 32, "pending bits");
+    __shared__ uint8_t s_used[TILE];
     for (uint32_t t = blockIdx.x; t < total; t += gridDim.x) {
         if (cur && !cur[t]) continue;  // block-uniform
         const uint32_t p = batch_program(off, B, t);
         const Prog& P = progs[p];
-        const uint32_t base = (t - off[p]) * kBTile;
-        const uint32_t W = P.W, lim = min(kBTile, P.wb8 - base);
+        const uint32_t base = (t - off[p]) * TILE;
+        const uint32_t W = P.W, lim = min(TILE, P.wb8 - base);
         uint32_t rd[kSweepItems], r1[kSweepItems], r2[kSweepItems];
         uint32_t pending = 0;  // bit e: instruction e of this thread may still act
 #pragma unroll
@@ -1584,7 +1586,7 @@ __global__ void __launch_bounds__(kThreads) k_batch_sweep(const Prog* progs, con
                         if (s_used[u32(a) - base]) { s_used[u32(a) - base] = 0; ch = true; }
                     } else if (*reinterpret_cast<volatile uint8_t*>(&P.used[a])) {
                         P.used[a] = 0;
-                        next[off[p] + u32(a) / kBTile] = 1;
+                        next[off[p] + u32(a) / TILE] = 1;
                         cross = true;
                     }
                 }
@@ -1603,13 +1605,13 @@ __global__ void __launch_bounds__(kThreads) k_batch_sweep(const Prog* progs, con
 
 // flag = 1 when some instruction's virtual result is not its own word.
 __global__ void __launch_bounds__(kThreads) k_batch_selfdef(const Prog* progs, const uint32_t* off, uint32_t B,
-                                                            uint32_t total, uint32_t* flag) {
+                                                            uint32_t total, uint32_t tile, uint32_t* flag) {
     for (uint32_t t = blockIdx.x; t < total; t += gridDim.x) {
         const uint32_t p = batch_program(off, B, t);
         const Prog& P = progs[p];
-        const uint32_t base = (t - off[p]) * kBTile;
+        const uint32_t base = (t - off[p]) * tile;
         bool odd = false;
-        for (uint32_t k = threadIdx.x; k < kBTile; k += kThreads) {
+        for (uint32_t k = threadIdx.x; k < tile; k += kThreads) {
             const uint32_t i = base + k;
             if (i >= P.wb8) break;
             const uint32_t r = P.rd[i];
@@ -1800,7 +1802,8 @@ template <class Op>
 void batch_launch(const BatchLaunch& bl, uint32_t total, const Op& op) {
     if (total == 0) return;
     g_launches++;
-    k_batch<Op><<<std::min<uint32_t>(total, 152u * 16u), kThreads, 0, bl.s>>>(bl.progs, bl.off, bl.B, total, op);
+    k_batch<Op><<<std::min<uint32_t>(total, 152u * 16u), kThreads, 0, bl.s>>>(bl.progs, bl.off, bl.B, total, bl.tile,
+                                                                               op);
 }
 
 }  // namespace
@@ -1856,17 +1859,25 @@ void batch_sort_keys(const BatchLaunch& bl, uint32_t total, unsigned long long* 
     else batch_launch(bl, total, BSortInit{a, aoff});
 }
 
+bool batch_tile_ok(uint32_t tile) { return tile >= kThreads && tile <= 65536u && (tile & (tile - 1)) == 0; }
+bool batch_sweep_tile_ok(uint32_t tile) { return tile == 512u || tile == 1024u || tile == 2048u; }
+
 void batch_sweep(const BatchLaunch& bl, uint32_t total, uint32_t* changed, const uint8_t* cur, uint8_t* next) {
     if (total == 0) return;
     g_launches++;
-    k_batch_sweep<<<std::min<uint32_t>(total, 152u * 16u), kThreads, 0, bl.s>>>(bl.progs, bl.off, bl.B, total, changed,
-                                                                                  cur, next);
+    const unsigned grid = std::min<uint32_t>(total, 152u * 16u);
+    switch (bl.tile) {
+        case 512u: k_batch_sweep<512u><<<grid, kThreads, 0, bl.s>>>(bl.progs, bl.off, bl.B, total, changed, cur, next); break;
+        case 2048u: k_batch_sweep<2048u><<<grid, kThreads, 0, bl.s>>>(bl.progs, bl.off, bl.B, total, changed, cur, next); break;
+        default: k_batch_sweep<1024u><<<grid, kThreads, 0, bl.s>>>(bl.progs, bl.off, bl.B, total, changed, cur, next); break;
+    }
 }
 
 void batch_selfdef(const BatchLaunch& bl, uint32_t total, uint32_t* flag) {
     if (total == 0) return;
     g_launches++;
-    k_batch_selfdef<<<std::min<uint32_t>(total, 152u * 16u), kThreads, 0, bl.s>>>(bl.progs, bl.off, bl.B, total, flag);
+    k_batch_selfdef<<<std::min<uint32_t>(total, 152u * 16u), kThreads, 0, bl.s>>>(bl.progs, bl.off, bl.B, total,
+                                                                                    bl.tile, flag);
 }
 
 void batch_scan(BatchScan which, const BatchLaunch& bl, uint32_t tiles, const ScanScratch& sc, uint32_t* meta) {

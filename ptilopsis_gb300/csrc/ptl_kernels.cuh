@@ -68,16 +68,20 @@ cudaError_t run_sort_rounds(const SortScratch& ss, uint32_t nseg0, uint32_t firs
 // holds each program's first tile for the stage's element count.
 struct BatchLaunch {
     const Prog* progs;
-    const uint32_t* off;
+    const uint32_t* off;   // tile table built with `tile` elements per tile
     uint32_t B;
     cudaStream_t s;
+    uint32_t tile;
 };
 enum class BatchStage {
     Validate, DepthSeen, Translate, Preprocess, Fix, Functab, Gen, OptMark, OptFinal, InitLifetime, Cross, RaHist, Spill,
     Scatter, RaFunctab, FjEmit, FjFunctab
 };
 enum class BatchScan { Count, Decl, RaCount, FjSize };
-uint32_t batch_tile();       // elements per tile of the element-wise stages
+uint32_t batch_tile();       // default elements per tile of the element-wise stages
+// Tile sizes the element-wise kernels and the optimize sweeps accept (powers of two).
+bool batch_tile_ok(uint32_t tile);
+bool batch_sweep_tile_ok(uint32_t tile);
 uint32_t batch_scan_tile();  // elements per scan tile
 void batch_stage(BatchStage st, const BatchLaunch& bl, uint32_t total, uint32_t* meta, uint32_t* seen,
                  const uint64_t* off64);

@@ -142,3 +142,29 @@ def test_batch_fixtures_and_serial_path(built_cuda):
             res = b.result(k)
             np.testing.assert_array_equal(res.words, golds[k]["words"], err_msg=nm)
             np.testing.assert_array_equal(res.table["starts"], golds[k]["fn_start"], err_msg=nm)
+
+
+def test_batch_tile_sizes_leave_results_unchanged(built_cuda, tmp_path, monkeypatch):
+    """Every tile size the autotuner may pick gives the same words as the defaults; sizes
+    the kernels do not take are refused; a tuned choice is cached per device and applied
+    by the next compiler."""
+    from ptilopsis_gb300 import PtlError
+    from ptilopsis_gb300.batch import BatchCompiler, autotune, cached_tiles
+    trees = _programs(12, seed0=0x50544CF0)
+    with BatchCompiler(workers=4, tiles=None) as b:
+        b.compile(trees)
+        want = [b.words(k) for k in range(len(trees))]
+        for elem, sweep in ((256, 512), (2048, 2048), (8192, 1024), (65536, 512)):
+            b.set_tiles(elem, sweep)
+            assert b.tiles() == (elem, sweep)
+            b.compile(trees)
+            for k in range(len(trees)):
+                np.testing.assert_array_equal(b.words(k), want[k], err_msg=f"tiles {elem}/{sweep}, program {k}")
+        for bad in ((1000, 1024), (128, 1024), (1024, 4096)):
+            with pytest.raises(PtlError):
+                b.set_tiles(*bad)
+    monkeypatch.setenv("PTL_AUTOTUNE_CACHE", str(tmp_path / "autotune.json"))
+    got = autotune(trees[:4], reps=1)
+    assert cached_tiles() == (got["elem_tile"], got["sweep_tile"])
+    with BatchCompiler(workers=2) as b:
+        assert b.tiles() == (got["elem_tile"], got["sweep_tile"])
