@@ -328,8 +328,8 @@ def run_batched(args):
         return float(t.item())
 
     # tile sizes by measurement, on other programs of the same distribution (untimed)
-    tiles = None
-    if not args.no_autotune:
+    tiles = tuple(args.tiles) if args.tiles else None
+    if tiles is None and not args.no_autotune:
         from concurrent.futures import ThreadPoolExecutor
         from ptilopsis_gb300.batch import autotune
         from ptilopsis_gb300.synth import config_params, generate
@@ -413,7 +413,7 @@ def run_batched(args):
                        "l2": "working set (~60 GB) > L2; no flush needed",
                        "parallelism": f"replicas x{world} (each GPU its own batch)",
                        "tiles": {"elem": bc.tiles()[0], "sweep": bc.tiles()[1],
-                                 "chosen_by": "defaults" if tiles is None else
+                                 "chosen_by": "defaults" if tiles is None else "--tiles" if args.tiles else
                                  "autotune on 512 other programs of the same distribution"}},
             "e2e": e2e, "plain": plain, "batched_over_plain": value / plain["value"],
             "roofline": roofline, "gpu_launches": int(launches)}
@@ -579,6 +579,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--tiles", type=int, nargs=2, metavar=("ELEM", "SWEEP"),
+                    help="tile sizes of the batched pipeline instead of autotuning them")
     ap.add_argument("--serve-requests", type=int, default=1000)
     ap.add_argument("--serve-slots", type=int, default=2)
     ap.add_argument("--serve-rates", type=float, nargs="+", default=[1000.0, 10000.0, 50000.0])
