@@ -15,6 +15,7 @@
 #include <algorithm>
 #include <atomic>
 #include <chrono>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <new>
@@ -136,7 +137,9 @@ public:
     DBuf errw, flags, meta, progs, tabs, lists, changed, sort_err, seen_off, a_off, dirty, ra_sync;
     DBuf sa, sapos, sbpos, seg0, seg1, tile_seg, tile_l, tile_r, leaf, heap, counters, scan_status, scan_counter,
         sort_local, sort_equal;
-    PBuf h_in, h_out, h_fn, h_small;
+    PBuf h_in, h_out, h_fn, h_small, h_gp;
+    DBuf d_gp;                 // host-gather parameters (source pointers, offsets, counts)
+    bool direct_host = false;  // the device reads pageable host memory coherently
 
     std::vector<uint8_t> active;
     std::vector<ptl_status> status;
@@ -147,6 +150,8 @@ public:
         h_out.release();
         h_fn.release();
         h_small.release();
+        h_gp.release();
+        d_gp.release();
         for (auto& e : ev)
             if (e) cudaEventDestroy(e);
         for (cudaEvent_t e : {ev_in, ev_out0, ev_out1})
@@ -328,93 +333,125 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
         BP_CU(cudaStreamSynchronize(s));
     }
 
-    // ---- inputs: gathered into pinned memory by host threads, one copy per field and
-    // chunk; a chunk's copies start as soon as its programs are gathered, so the copy
-    // engine runs under the gather of the next chunks
+    // ---- inputs.  A program's input region starts at a multiple of 16 elements.  On a
+    // device with coherent access to pageable host memory a kernel reads the caller's
+    // arrays directly; otherwise host threads gather them into pinned memory, one copy per
+    // field and chunk, and a chunk's copies start as soon as its programs are gathered, so
+    // the copy engine runs under the gather of the next chunks
     {
         std::vector<uint64_t> din(B + 1);
-        uint64_t o = 0;
+        uint64_t o = 0, nodes_in = 0;
         for (size_t p = 0; p < B; ++p) {
             din[p] = o;
-            if (active[p]) o += n[p];
+            if (active[p]) {
+                o += (n[p] + 15) & ~uint64_t(15);
+                nodes_in += n[p];
+            }
         }
         din[B] = o;
-        const uint64_t cap = std::max<uint64_t>(o, 1);
-        const size_t bytes = cap * (1 + 1 + 4 + 4 + 4 + 4);
-        BP_CU(h_in.ensure(bytes));
+        const uint64_t cap = std::max<uint64_t>(o, 16);
         BP_CU(in_type.ensure(cap));
         BP_CU(in_rtype.ensure(cap));
         BP_CU(in_parent.ensure(cap * 4));
         BP_CU(in_depth.ensure(cap * 4));
         BP_CU(in_child.ensure(cap * 4));
         BP_CU(in_data.ensure(cap * 4));
-        uint8_t* ht = h_in.at<uint8_t>();
-        uint8_t* hr = ht + cap;
-        int32_t* hpar = reinterpret_cast<int32_t*>(hr + cap);
-        int32_t* hdep = hpar + cap;
-        int32_t* hch = hdep + cap;
-        uint32_t* hdat = reinterpret_cast<uint32_t*>(hch + cap);
-        // chunks of about o / kInChunks nodes, cut at program boundaries
-        constexpr size_t kInChunks = 8;
-        std::vector<size_t> cfirst{0};
-        std::vector<uint32_t> chunk_of(B);
-        for (size_t p = 0; p < B; ++p) {
-            const size_t c = cfirst.size() - 1;
-            chunk_of[p] = static_cast<uint32_t>(c);
-            if (p + 1 < B && cfirst.size() < kInChunks && din[p + 1] * kInChunks >= o * cfirst.size())
-                cfirst.push_back(p + 1);
-        }
-        const size_t C = cfirst.size();
-        cfirst.push_back(B);
-        std::vector<std::atomic<uint32_t>> left(C);
-        for (size_t c = 0; c < C; ++c) {
-            uint32_t k = 0;
-            for (size_t p = cfirst[c]; p < cfirst[c + 1]; ++p) k += active[p] ? 1u : 0u;
-            left[c].store(k, std::memory_order_relaxed);
-        }
-        std::atomic<size_t> next{0};
-        const auto g0 = std::chrono::steady_clock::now();
-        const int nt_ = std::max(1, std::min<int>(threads, static_cast<int>(B)));
-        std::vector<std::thread> pool;
-        for (int w = 0; w < nt_; ++w) {
-            pool.emplace_back([&] {
-                for (size_t p = next.fetch_add(1, std::memory_order_relaxed); p < B;
-                     p = next.fetch_add(1, std::memory_order_relaxed)) {
-                    if (!active[p]) continue;
-                    const ptl_ast_view& t = trees[p];
-                    const uint64_t d = din[p];
-                    std::memcpy(ht + d, t.type, n[p]);
-                    std::memcpy(hr + d, t.rtype, n[p]);
-                    std::memcpy(hpar + d, t.parent, 4 * n[p]);
-                    std::memcpy(hdep + d, t.depth, 4 * n[p]);
-                    std::memcpy(hch + d, t.child_idx, 4 * n[p]);
-                    std::memcpy(hdat + d, t.data, 4 * n[p]);
-                    left[chunk_of[p]].fetch_sub(1, std::memory_order_release);
-                }
-            });
-        }
-        // every program is gathered by some worker, so each chunk's count reaches zero
-        cudaError_t ce = cudaEventRecord(ev_in, s);
-        for (size_t c = 0; c < C && ce == cudaSuccess; ++c) {
-            while (left[c].load(std::memory_order_acquire) != 0) std::this_thread::yield();
-            const uint64_t a = din[cfirst[c]], m = din[cfirst[c + 1]] - a;
-            if (m == 0) continue;
-            for (auto [dst, src, w] : {std::tuple<void*, const void*, uint64_t>{in_type.p, ht, 1},
-                                       {in_rtype.p, hr, 1},
-                                       {in_parent.p, hpar, 4},
-                                       {in_depth.p, hdep, 4},
-                                       {in_child.p, hch, 4},
-                                       {in_data.p, hdat, 4}}) {
-                ce = cudaMemcpyAsync(static_cast<uint8_t*>(dst) + w * a, static_cast<const uint8_t*>(src) + w * a,
-                                     w * m, cudaMemcpyHostToDevice, s);
-                if (ce != cudaSuccess) break;
+        if (direct_host) {
+            const auto g0 = std::chrono::steady_clock::now();
+            BP_CU(h_gp.ensure(B * 8 * 8));
+            BP_CU(d_gp.ensure(B * 8 * 8));
+            const void** hsrc = reinterpret_cast<const void**>(h_gp.p);  // [6][B]
+            uint64_t* hdin = reinterpret_cast<uint64_t*>(hsrc + 6 * B);
+            uint64_t* hn = hdin + B;
+            for (size_t p = 0; p < B; ++p) {
+                const ptl_ast_view& t = trees[p];
+                const void* f[6] = {t.type, t.rtype, t.parent, t.depth, t.child_idx, t.data};
+                for (int k = 0; k < 6; ++k) hsrc[k * B + p] = f[k];
+                hdin[p] = din[p];
+                hn[p] = active[p] ? n[p] : 0;
             }
+            BP_CU(cudaMemcpyAsync(d_gp.p, h_gp.p, B * 8 * 8, cudaMemcpyHostToDevice, s));
+            const uint32_t t_g = tiles(18, n, kGatherTile);
+            hns[0] = static_cast<uint64_t>(std::chrono::duration_cast<std::chrono::nanoseconds>(
+                                               std::chrono::steady_clock::now() - g0).count());
+            BP_CU(cudaEventRecord(ev_in, s));
+            const void* const* dsrc = static_cast<const void* const*>(d_gp.p);
+            const uint64_t* ddin = reinterpret_cast<const uint64_t*>(dsrc + 6 * B);
+            uint8_t* dsts[6] = {in_type.at<uint8_t>(), in_rtype.at<uint8_t>(), in_parent.at<uint8_t>(),
+                                in_depth.at<uint8_t>(), in_child.at<uint8_t>(), in_data.at<uint8_t>()};
+            for (int k = 0; k < 6; ++k)
+                batch_gather_host(bl(18), t_g, HostGather{dsrc + k * B, ddin, ddin + B, dsts[k], k < 2 ? 1u : 4u});
+        } else {
+            const size_t bytes = cap * (1 + 1 + 4 + 4 + 4 + 4);
+            BP_CU(h_in.ensure(bytes));
+            uint8_t* ht = h_in.at<uint8_t>();
+            uint8_t* hr = ht + cap;
+            int32_t* hpar = reinterpret_cast<int32_t*>(hr + cap);
+            int32_t* hdep = hpar + cap;
+            int32_t* hch = hdep + cap;
+            uint32_t* hdat = reinterpret_cast<uint32_t*>(hch + cap);
+            // chunks of about o / kInChunks nodes, cut at program boundaries
+            constexpr size_t kInChunks = 8;
+            std::vector<size_t> cfirst{0};
+            std::vector<uint32_t> chunk_of(B);
+            for (size_t p = 0; p < B; ++p) {
+                const size_t c = cfirst.size() - 1;
+                chunk_of[p] = static_cast<uint32_t>(c);
+                if (p + 1 < B && cfirst.size() < kInChunks && din[p + 1] * kInChunks >= o * cfirst.size())
+                    cfirst.push_back(p + 1);
+            }
+            const size_t C = cfirst.size();
+            cfirst.push_back(B);
+            std::vector<std::atomic<uint32_t>> left(C);
+            for (size_t c = 0; c < C; ++c) {
+                uint32_t k = 0;
+                for (size_t p = cfirst[c]; p < cfirst[c + 1]; ++p) k += active[p] ? 1u : 0u;
+                left[c].store(k, std::memory_order_relaxed);
+            }
+            std::atomic<size_t> next{0};
+            const auto g0 = std::chrono::steady_clock::now();
+            const int nt_ = std::max(1, std::min<int>(threads, static_cast<int>(B)));
+            std::vector<std::thread> pool;
+            for (int w = 0; w < nt_; ++w) {
+                pool.emplace_back([&] {
+                    for (size_t p = next.fetch_add(1, std::memory_order_relaxed); p < B;
+                         p = next.fetch_add(1, std::memory_order_relaxed)) {
+                        if (!active[p]) continue;
+                        const ptl_ast_view& t = trees[p];
+                        const uint64_t d = din[p];
+                        std::memcpy(ht + d, t.type, n[p]);
+                        std::memcpy(hr + d, t.rtype, n[p]);
+                        std::memcpy(hpar + d, t.parent, 4 * n[p]);
+                        std::memcpy(hdep + d, t.depth, 4 * n[p]);
+                        std::memcpy(hch + d, t.child_idx, 4 * n[p]);
+                        std::memcpy(hdat + d, t.data, 4 * n[p]);
+                        left[chunk_of[p]].fetch_sub(1, std::memory_order_release);
+                    }
+                });
+            }
+            // every program is gathered by some worker, so each chunk's count reaches zero
+            cudaError_t ce = cudaEventRecord(ev_in, s);
+            for (size_t c = 0; c < C && ce == cudaSuccess; ++c) {
+                while (left[c].load(std::memory_order_acquire) != 0) std::this_thread::yield();
+                const uint64_t a = din[cfirst[c]], m = din[cfirst[c + 1]] - a;
+                if (m == 0) continue;
+                for (auto [dst, src, w] : {std::tuple<void*, const void*, uint64_t>{in_type.p, ht, 1},
+                                           {in_rtype.p, hr, 1},
+                                           {in_parent.p, hpar, 4},
+                                           {in_depth.p, hdep, 4},
+                                           {in_child.p, hch, 4},
+                                           {in_data.p, hdat, 4}}) {
+                    ce = cudaMemcpyAsync(static_cast<uint8_t*>(dst) + w * a, static_cast<const uint8_t*>(src) + w * a,
+                                         w * m, cudaMemcpyHostToDevice, s);
+                    if (ce != cudaSuccess) break;
+                }
+            }
+            for (auto& t : pool) t.join();
+            hns[0] = static_cast<uint64_t>(std::chrono::duration_cast<std::chrono::nanoseconds>(
+                                               std::chrono::steady_clock::now() - g0).count());
+            BP_CU(ce);
         }
-        for (auto& t : pool) t.join();
-        hns[0] = static_cast<uint64_t>(std::chrono::duration_cast<std::chrono::nanoseconds>(
-                                           std::chrono::steady_clock::now() - g0).count());
-        BP_CU(ce);
-        h2d += 18 * o;
+        h2d += 18 * nodes_in;
         BP_CU(cudaEventRecord(ev[0], s));  // stage times start with the inputs on the device
 
         // node, register and depth families
@@ -913,6 +950,10 @@ BatchPipeline* BatchPipeline::create(int device, int host_threads, ptl_status* s
         if (st) *st = PTL_CUDA_ERROR;
         return nullptr;
     }
+    int pageable = 0;
+    if (cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, device) != cudaSuccess) pageable = 0;
+    const char* env = std::getenv("PTL_HOST_GATHER");  // "1": gather through pinned memory regardless
+    p->direct_host = pageable == 1 && !(env && env[0] == '1');
     if (st) *st = PTL_OK;
     return p;
 }

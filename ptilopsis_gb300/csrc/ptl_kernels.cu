@@ -1603,6 +1603,29 @@ __global__ void __launch_bounds__(kThreads) k_batch_sweep(const Prog* progs, con
     }
 }
 
+// Input gather from host memory: a tile is kGatherTile elements of one program; 16-byte
+// moves when the host array is 16-byte aligned (the device side always is), bytes
+// otherwise.
+__global__ void __launch_bounds__(kThreads) k_gather_host(HostGather g, const uint32_t* off, uint32_t B,
+                                                          uint32_t total) {
+    for (uint32_t t = blockIdx.x; t < total; t += gridDim.x) {
+        const uint32_t p = batch_program(off, B, t);
+        const uint64_t e0 = static_cast<uint64_t>(t - off[p]) * kGatherTile;
+        if (e0 >= g.n[p]) continue;
+        const uint64_t nb = min(static_cast<uint64_t>(kGatherTile), g.n[p] - e0) * g.esize;
+        const uint8_t* s = static_cast<const uint8_t*>(g.src[p]) + e0 * g.esize;
+        uint8_t* d = g.dst + (g.din[p] + e0) * g.esize;
+        uint64_t done = 0;
+        if ((reinterpret_cast<uintptr_t>(s) & 15u) == 0) {
+            const uint64_t n16 = nb / 16;
+            for (uint64_t k = threadIdx.x; k < n16; k += kThreads)
+                reinterpret_cast<uint4*>(d)[k] = reinterpret_cast<const uint4*>(s)[k];
+            done = n16 * 16;
+        }
+        for (uint64_t k = done + threadIdx.x; k < nb; k += kThreads) d[k] = s[k];
+    }
+}
+
 // flag = 1 when some instruction's virtual result is not its own word.
 __global__ void __launch_bounds__(kThreads) k_batch_selfdef(const Prog* progs, const uint32_t* off, uint32_t B,
                                                             uint32_t total, uint32_t tile, uint32_t* flag) {
@@ -1857,6 +1880,12 @@ void batch_stage(BatchStage st, const BatchLaunch& bl, uint32_t total, uint32_t*
 void batch_sort_keys(const BatchLaunch& bl, uint32_t total, unsigned long long* a, const uint64_t* aoff, bool out) {
     if (out) batch_launch(bl, total, BSortOut{a, aoff});
     else batch_launch(bl, total, BSortInit{a, aoff});
+}
+
+void batch_gather_host(const BatchLaunch& bl, uint32_t total, const HostGather& g) {
+    if (total == 0) return;
+    g_launches++;
+    k_gather_host<<<std::min<uint32_t>(total, 152u * 16u), kThreads, 0, bl.s>>>(g, bl.off, bl.B, total);
 }
 
 bool batch_tile_ok(uint32_t tile) { return tile >= kThreads && tile <= 65536u && (tile & (tile - 1)) == 0; }

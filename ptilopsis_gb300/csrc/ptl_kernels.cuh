@@ -90,6 +90,20 @@ void batch_sort_keys(const BatchLaunch& bl, uint32_t total, unsigned long long* 
 // the tiles a cleared mark makes live again.  Valid only when batch_selfdef found every
 // virtual result to be its instruction's own word (flag 0); otherwise pass cur = null.
 void batch_sweep(const BatchLaunch& bl, uint32_t total, uint32_t* changed, const uint8_t* cur, uint8_t* next);
+
+// One input field of every program copied from the caller's host arrays into the device
+// input arena by a kernel that reads host memory directly (devices with coherent access
+// to pageable memory).  Program p's elements go to dst + din[p] * esize, din[p] a multiple
+// of 16; the table bl.off counts tiles of kGatherTile elements per program.
+struct HostGather {
+    const void* const* src;  // [B] host arrays of this field
+    const uint64_t* din;     // [B] first element in dst
+    const uint64_t* n;       // [B] elements
+    uint8_t* dst;
+    uint32_t esize;          // 1 or 4
+};
+constexpr uint32_t kGatherTile = 4096;
+void batch_gather_host(const BatchLaunch& bl, uint32_t total, const HostGather& g);
 void batch_selfdef(const BatchLaunch& bl, uint32_t total, uint32_t* flag);
 void batch_scan(BatchScan which, const BatchLaunch& bl, uint32_t tiles, const ScanScratch& sc, uint32_t* meta);
 void batch_sizes(bool w3, const Prog* progs, const uint32_t* list, uint32_t count, uint32_t* meta, cudaStream_t s);

@@ -168,3 +168,39 @@ def test_batch_tile_sizes_leave_results_unchanged(built_cuda, tmp_path, monkeypa
     assert cached_tiles() == (got["elem_tile"], got["sweep_tile"])
     with BatchCompiler(workers=2) as b:
         assert b.tiles() == (got["elem_tile"], got["sweep_tile"])
+
+
+def _misaligned(tree):
+    """The same tree with every array starting one element past a 16-byte boundary."""
+    import dataclasses
+    out = {}
+    for f in ("type", "rtype", "parent", "depth", "child_idx", "data"):
+        a = np.ascontiguousarray(getattr(tree, f))
+        buf = np.empty(a.shape[0] + 16, a.dtype)
+        off = 1
+        while (buf[off:].ctypes.data % 16) == 0:
+            off += 1
+        buf[off:off + a.shape[0]] = a
+        out[f] = buf[off:off + a.shape[0]]
+        assert out[f].ctypes.data % 16 != 0
+    return dataclasses.replace(tree, **out)
+
+
+def test_batch_input_paths_agree(built_cuda, monkeypatch):
+    """The inputs reach the device either by a kernel reading the caller's arrays (where
+    the device reads pageable host memory; arrays off a 16-byte boundary take the byte
+    path) or through pinned memory (PTL_HOST_GATHER=1); both give the same words."""
+    from ptilopsis_gb300.batch import BatchCompiler
+    trees = _programs(10, seed0=0x50544D00)
+    odd = [_misaligned(t) if k % 2 else t for k, t in enumerate(trees)]
+    with BatchCompiler(workers=4) as b:
+        b.compile(trees)
+        want = [b.words(k) for k in range(len(trees))]
+        b.compile(odd)
+        for k in range(len(trees)):
+            np.testing.assert_array_equal(b.words(k), want[k], err_msg=f"program {k}, misaligned inputs")
+    monkeypatch.setenv("PTL_HOST_GATHER", "1")
+    with BatchCompiler(workers=4) as b:
+        b.compile(odd)
+        for k in range(len(trees)):
+            np.testing.assert_array_equal(b.words(k), want[k], err_msg=f"program {k}, pinned gather")
