@@ -180,11 +180,13 @@ void ptl_batch_destroy(ptl_batch* batch);
 
 /* ---- Compile server.  No counterpart in the reference.  Continuous batching over
  * `slots` lanes (1..16), each a batched pipeline with its own stream and resident arenas:
- * a free lane takes every queued request, in arrival order, whose device-memory estimate
- * fits in what is left of memory_budget (a later request that fits may pass one that
- * does not; at most 64M nodes per batch) and compiles them together, while requests that
- * arrive meanwhile go to the next free lane, so their work overlaps on the GPU.  Results
- * are identical to compiling each tree alone. */
+ * a free lane takes every queued request of its size class (below or above 64k nodes;
+ * the first half of the lanes prefers small requests, the others large ones, and a lane
+ * takes the other class when its own has nothing queued), in arrival order, whose
+ * device-memory estimate fits in what is left of memory_budget (a later request that fits
+ * may pass one that does not; at most 64M nodes per batch) and compiles them together,
+ * while requests that arrive meanwhile go to the next free lane, so their work overlaps on
+ * the GPU.  Results are identical to compiling each tree alone. */
 typedef struct ptl_server ptl_server;
 ptl_status ptl_server_create(int device, int slots, uint64_t memory_budget, ptl_server** out);
 /* Copies a host tree into a request and queues it; PTL_ADMISSION_DENIED when the request

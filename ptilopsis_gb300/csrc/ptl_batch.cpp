@@ -185,6 +185,12 @@ struct ptl_server {
     uint64_t budget = 0;
     uint64_t in_use = 0;       // admission estimates of the compiles in flight
     uint64_t max_batch_nodes = 64ull << 20;
+    // Requests below small_nodes are "small"; lanes w < small_lanes prefer them and the
+    // others prefer large requests, so a small request is not batched behind a large one
+    // whose register allocation chain sets the batch's duration.  A lane whose class has
+    // nothing queued takes the other class.
+    uint64_t small_nodes = 64ull << 10;
+    size_t small_lanes = 1;
     std::mutex mu;
     std::condition_variable cv_work, cv_done;
     std::deque<std::shared_ptr<Request>> queue;
@@ -195,30 +201,36 @@ struct ptl_server {
     bool stopping = false;
     uint64_t completed = 0, nodes_done = 0, batches = 0;
 
-    // Continuous batching: a free lane takes every queued request, in arrival order, that
-    // fits the memory left in the budget and the batch cap (a later request that fits may
-    // pass one that does not), and compiles them through its batched pipeline while the
-    // other lanes keep taking the requests that arrive meanwhile.
+    // Continuous batching: a free lane takes every queued request of its size class, in
+    // arrival order, that fits the memory left in the budget and the batch cap (a later
+    // request that fits may pass one that does not) -- or of the other class when its own
+    // has none -- and compiles them through its batched pipeline while the other lanes
+    // keep taking the requests that arrive meanwhile.
     void run(size_t w) {
         std::vector<std::shared_ptr<Request>> batch;
         std::vector<ptl_ast_view> views;
         std::vector<ptl::BatchResult> res;
+        const bool prefer_small = w < small_lanes;
         for (;;) {
             batch.clear();
             {
                 std::unique_lock<std::mutex> lk(mu);
                 for (;;) {
                     if (stopping) return;
-                    uint64_t nodes = 0;
-                    for (auto it = queue.begin(); it != queue.end();) {
-                        const std::shared_ptr<Request>& r = *it;
-                        if (in_use + r->bytes <= budget && (batch.empty() || nodes + r->n <= max_batch_nodes)) {
-                            in_use += r->bytes;
-                            nodes += r->n;
-                            batch.push_back(r);
-                            it = queue.erase(it);
-                        } else {
-                            ++it;
+                    for (int pass = 0; pass < 2 && batch.empty(); ++pass) {
+                        const bool want_small = (pass == 0) == prefer_small;
+                        uint64_t nodes = 0;
+                        for (auto it = queue.begin(); it != queue.end();) {
+                            const std::shared_ptr<Request>& r = *it;
+                            const bool fits = in_use + r->bytes <= budget && (batch.empty() || nodes + r->n <= max_batch_nodes);
+                            if ((r->n < small_nodes) == want_small && fits) {
+                                in_use += r->bytes;
+                                nodes += r->n;
+                                batch.push_back(r);
+                                it = queue.erase(it);
+                            } else {
+                                ++it;
+                            }
                         }
                     }
                     if (!batch.empty()) break;
@@ -271,6 +283,7 @@ extern "C" ptl_status ptl_server_create(int device, int slots, uint64_t memory_b
     if (!s) return PTL_OOM;
     s->device = device;
     s->budget = memory_budget;
+    s->small_lanes = slots > 1 ? static_cast<size_t>(slots) / 2 : 1;
     for (int w = 0; w < slots; ++w) {
         ptl_status st = PTL_OK;
         s->pipes.emplace_back(ptl::BatchPipeline::create(device, 8, &st));
