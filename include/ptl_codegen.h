@@ -181,8 +181,8 @@ void ptl_batch_destroy(ptl_batch* batch);
 /* ---- Compile server.  No counterpart in the reference.  Continuous batching over
  * `slots` lanes (1..16), each a batched pipeline with its own stream and resident arenas:
  * a free lane takes every queued request of its size class (below or above 64k nodes;
- * the first half of the lanes prefers small requests, the others large ones, and a lane
- * takes the other class when its own has nothing queued), in arrival order, whose
+ * with two or more lanes the first half takes only small requests, the others large ones
+ * and small ones when no large one is queued), in arrival order, whose
  * device-memory estimate fits in what is left of memory_budget (a later request that fits
  * may pass one that does not; at most 64M nodes per batch) and compiles them together,
  * while requests that arrive meanwhile go to the next free lane, so their work overlaps on
@@ -206,6 +206,9 @@ ptl_status ptl_server_result(ptl_server* server, uint64_t ticket, const uint32_t
 /* Submit, start and completion times of a finished request (ptl_clock_ns clock). */
 ptl_status ptl_server_times(ptl_server* server, uint64_t ticket, uint64_t times[3]);
 ptl_status ptl_server_release(ptl_server* server, uint64_t ticket);
+/* Detail of a finished ticket's batch-wide failure (CUDA_ERROR, OOM); "" otherwise.
+ * Valid until the ticket is released. */
+const char* ptl_server_error(ptl_server* server, uint64_t ticket);
 /* stats[0..4]: requests completed, nodes compiled, requests queued, admitted bytes in
  * flight, batches compiled. */
 ptl_status ptl_server_stats(ptl_server* server, uint64_t stats[5]);

@@ -51,6 +51,8 @@ def _bind(L):
         [ctypes.POINTER(_u32p)] * 4 + [ctypes.POINTER(sz)]
     L.ptl_server_times.argtypes = [vp, u64, ctypes.POINTER(u64)]
     L.ptl_server_release.argtypes = [vp, u64]
+    L.ptl_server_error.argtypes = [vp, u64]
+    L.ptl_server_error.restype = ctypes.c_char_p
     L.ptl_server_stats.argtypes = [vp, ctypes.POINTER(u64)]
     L.ptl_server_destroy.argtypes = [vp]
     L.ptl_server_destroy.restype = None
@@ -278,7 +280,8 @@ class CompileServer:
         done = ctypes.c_int()
         st = self._lib.ptl_server_poll(self._h, ticket, 1 if wait else 0, ctypes.byref(done))
         if st != 0:
-            raise PtlError(st, f"request {ticket}")
+            why = (self._lib.ptl_server_error(self._h, ticket) or b"").decode()
+            raise PtlError(st, f"request {ticket}" + (f": {why}" if why else ""))
         return bool(done.value)
 
     def result(self, ticket: int) -> Compiled:

@@ -36,6 +36,7 @@ uint64_t now_ns() {
 // One compiled program, copied out of the pipeline that made it.
 struct Result {
     ptl_status status = PTL_OK;
+    std::string error;  // detail of a batch-wide failure
     std::vector<uint32_t> words, starts, ends, sizes, ids;
 };
 
@@ -185,10 +186,10 @@ struct ptl_server {
     uint64_t budget = 0;
     uint64_t in_use = 0;       // admission estimates of the compiles in flight
     uint64_t max_batch_nodes = 64ull << 20;
-    // Requests below small_nodes are "small"; lanes w < small_lanes prefer them and the
-    // others prefer large requests, so a small request is not batched behind a large one
-    // whose register allocation chain sets the batch's duration.  A lane whose class has
-    // nothing queued takes the other class.
+    // Requests below small_nodes are "small"; lanes w < small_lanes take only those, so a
+    // small request never waits behind a large one whose register allocation chain sets a
+    // batch's duration.  The other lanes prefer large requests and take small ones when no
+    // large request is queued.
     uint64_t small_nodes = 64ull << 10;
     size_t small_lanes = 1;
     std::mutex mu;
@@ -203,9 +204,9 @@ struct ptl_server {
 
     // Continuous batching: a free lane takes every queued request of its size class, in
     // arrival order, that fits the memory left in the budget and the batch cap (a later
-    // request that fits may pass one that does not) -- or of the other class when its own
-    // has none -- and compiles them through its batched pipeline while the other lanes
-    // keep taking the requests that arrive meanwhile.
+    // request that fits may pass one that does not) -- a large-request lane takes small
+    // requests when it has no large one -- and compiles them through its batched pipeline
+    // while the other lanes keep taking the requests that arrive meanwhile.
     void run(size_t w) {
         std::vector<std::shared_ptr<Request>> batch;
         std::vector<ptl_ast_view> views;
@@ -217,7 +218,7 @@ struct ptl_server {
                 std::unique_lock<std::mutex> lk(mu);
                 for (;;) {
                     if (stopping) return;
-                    for (int pass = 0; pass < 2 && batch.empty(); ++pass) {
+                    for (int pass = 0; pass < (prefer_small ? 1 : 2) && batch.empty(); ++pass) {
                         const bool want_small = (pass == 0) == prefer_small;
                         uint64_t nodes = 0;
                         for (auto it = queue.begin(); it != queue.end();) {
@@ -248,6 +249,8 @@ struct ptl_server {
                 Result& out = batch[k]->result;
                 if (st != PTL_OK) {
                     out.status = st;
+                    const char* why = pipes[w]->last_error();
+                    out.error = why ? why : "";
                     continue;
                 }
                 const ptl::BatchResult& r = res[k];
@@ -283,10 +286,16 @@ extern "C" ptl_status ptl_server_create(int device, int slots, uint64_t memory_b
     if (!s) return PTL_OOM;
     s->device = device;
     s->budget = memory_budget;
-    s->small_lanes = slots > 1 ? static_cast<size_t>(slots) / 2 : 1;
+    s->small_lanes = slots > 1 ? static_cast<size_t>(slots) / 2 : 0;  // one lane takes everything
     for (int w = 0; w < slots; ++w) {
         ptl_status st = PTL_OK;
-        s->pipes.emplace_back(ptl::BatchPipeline::create(device, 8, &st));
+        // small-request lanes run at the highest stream priority: their short, latency-bound
+        // batches get SMs ahead of the large batches' blocks
+        s->pipes.emplace_back(ptl::BatchPipeline::create(device, 8, &st, static_cast<size_t>(w) < s->small_lanes));
+        // a large-request lane's persistent regalloc launch leaves half the SMs' block slots
+        // to the small-request lanes
+        if (s->pipes.back() && s->small_lanes > 0 && static_cast<size_t>(w) >= s->small_lanes)
+            s->pipes.back()->set_regalloc_share(0.5);
         if (!s->pipes.back()) {
             s->pipes.clear();
             delete s;
@@ -367,6 +376,15 @@ extern "C" ptl_status ptl_server_result(ptl_server* s, uint64_t ticket, const ui
         *functions = r.starts.size();
     }
     return PTL_OK;
+}
+
+// Detail of a finished ticket's batch-wide failure ("" when there was none).
+extern "C" const char* ptl_server_error(ptl_server* s, uint64_t ticket) {
+    if (!s) return "";
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->all.find(ticket);
+    if (it == s->all.end() || !it->second->done) return "";
+    return it->second->result.error.c_str();
 }
 
 // Submit, start and completion times (steady clock, ns) of a finished ticket.

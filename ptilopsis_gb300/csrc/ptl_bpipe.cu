@@ -181,6 +181,7 @@ public:
         if (b) *b = d2h;
     }
     const char* last_error() const override { return err_text.c_str(); }
+    void set_regalloc_share(double share) override { ra_share = std::min(1.0, std::max(0.05, share)); }
     bool set_tiles(uint32_t e, uint32_t w) override {
         if (!batch_tile_ok(e) || !batch_sweep_tile_ok(w)) return false;
         elem_tile = e;
@@ -230,6 +231,7 @@ public:
     }
     // tile sizes: element-wise stages, optimize sweeps (chosen by the autotuner or the defaults)
     uint32_t elem_tile = batch_tile(), sweep_tile = 1024;
+    double ra_share = 1.0;  // part of the resident blocks the persistent regalloc launch takes
     uint32_t slot_tile[32] = {};
 
     std::vector<Prog> hp;  // host copies of the views
@@ -819,7 +821,7 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
         const uint32_t t_hist = tiles(16, nfree, elem_tile, &lane0);
         batch_stage(BatchStage::RaHist, bl(16), t_hist, nullptr, nullptr, nullptr);
         BP_CU(batch_regalloc(progs.at<Prog>(), dtable_slot(8), d_lane0, static_cast<uint32_t>(lane0_list.size()),
-                             ra_items, max_g0, ra_sync.at<uint32_t>(), s));
+                             ra_items, max_g0, ra_sync.at<uint32_t>(), s, ra_share));
         const uint32_t* d_serial = upload_list(1, serial_list);
         batch_serial(progs.at<Prog>(), d_serial, static_cast<uint32_t>(serial_list.size()), s);
         const uint32_t t_w_sp = tiles(13, W, elem_tile);
@@ -937,7 +939,7 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
 
 }  // namespace
 
-BatchPipeline* BatchPipeline::create(int device, int host_threads, ptl_status* st) {
+BatchPipeline* BatchPipeline::create(int device, int host_threads, ptl_status* st, bool urgent) {
     Pipeline* p = new (std::nothrow) Pipeline;
     if (!p) {
         if (st) *st = PTL_OOM;
@@ -945,7 +947,9 @@ BatchPipeline* BatchPipeline::create(int device, int host_threads, ptl_status* s
     }
     p->device = device;
     p->threads = std::max(1, host_threads);
-    if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&p->s, cudaStreamNonBlocking) != cudaSuccess) {
+    int lo = 0, hi = 0;  // stream priorities: numerically lower is more urgent
+    if (cudaSetDevice(device) != cudaSuccess || cudaDeviceGetStreamPriorityRange(&lo, &hi) != cudaSuccess ||
+        cudaStreamCreateWithPriority(&p->s, cudaStreamNonBlocking, urgent ? hi : lo) != cudaSuccess) {
         delete p;
         if (st) *st = PTL_CUDA_ERROR;
         return nullptr;

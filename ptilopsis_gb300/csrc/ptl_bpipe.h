@@ -24,7 +24,8 @@ struct BatchResult {
 class BatchPipeline {
 public:
     // Device and pinned host memory are kept between calls and grow to the largest batch.
-    static BatchPipeline* create(int device, int host_threads, ptl_status* st);
+    // urgent: the pipeline's stream gets the device's highest stream priority.
+    static BatchPipeline* create(int device, int host_threads, ptl_status* st, bool urgent = false);
     virtual ~BatchPipeline() = default;
     // Compiles count host trees; out[k] receives program k's output or its status.
     // Returns PTL_OK unless the batch as a whole failed (CUDA error, out of memory).
@@ -39,6 +40,9 @@ public:
     // Elements per tile of the element-wise stages and of the optimize sweeps; returns
     // false (and changes nothing) for sizes the kernels do not take.
     virtual bool set_tiles(uint32_t elem_tile, uint32_t sweep_tile) = 0;
+    // The part of the device's resident blocks the persistent regalloc launch may take
+    // (default 1); less leaves SMs to pipelines on other streams.
+    virtual void set_regalloc_share(double share) = 0;
     virtual void tiles(uint32_t out[2]) const = 0;
     // Detail of the last failure.
     virtual const char* last_error() const = 0;

@@ -6,9 +6,35 @@
 
 #include <algorithm>
 #include <atomic>
+#include <map>
+#include <mutex>
+#include <utility>
 
 #include "ptl_kernels.cuh"
 #include "ptl_ra.cuh"
+
+namespace ptl {
+
+// A kernel's largest dynamic shared memory is one attribute per function and device,
+// shared by every host thread: batched pipelines on several threads (the compile server's
+// lanes) launch the same kernels with different sizes.  So the attribute is only ever
+// raised, under a lock, to the largest size requested so far; a launch that set it never
+// finds it lowered by another thread before it runs.
+cudaError_t allow_dynamic_smem(const void* kernel, size_t bytes) {
+    static std::mutex mu;
+    static std::map<std::pair<int, const void*>, size_t> granted;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lk(mu);
+    size_t& g = granted[{dev, kernel}];
+    if (bytes <= g) return cudaSuccess;
+    e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(bytes));
+    if (e == cudaSuccess) g = bytes;
+    return e;
+}
+
+}  // namespace ptl
 
 namespace ptl {
 
@@ -922,6 +948,117 @@ __device__ bool ra_wait_chunk(const uint32_t* done, uint32_t c, uint32_t need, E
     }
 }
 
+// The lane-0 pass of a program with one lane-0 function (at most 8 functions) whose
+// registers are each defined once.  Every other function is in group 0, so no mark of an
+// earlier group exists (the check and the Jacobi rounds never act), no later group
+// triggers a position the slot reads (no swapped rewrites), and the slot wins every row-0
+// position it writes.  Lane 0 of warp 0 runs the slot; the warp turns each step's trigger
+// records into a 64-bit mask by ballot.  Row 0 stays in shared memory beside a mask of
+// the positions that hold virtual registers.  No block barrier: the other warps return.
+__device__ void ra_lane0_single(const Prog& P, uint32_t S, uint32_t K, uint32_t chunks, unsigned char* smem) {
+    constexpr uint32_t kNone = 0xFFFFFFFFu;
+    constexpr unsigned full = 0xFFFFFFFFu;
+    const uint32_t lane = threadIdx.x;  // warp 0 only
+    const uint32_t* hist = P.ra_chunks;
+    const uint32_t* done = P.ra_chunks + chunks;
+    Ra2Shared& sh = *reinterpret_cast<Ra2Shared*>(smem);
+    uint32_t* cur = reinterpret_cast<uint32_t*>(smem + sizeof(Ra2Shared));
+    uint32_t* ctag = cur + 4u;
+    uint32_t* cval = ctag + K;
+    const SymCache c{ctag, cval, K};
+    uint32_t need = 0, wc = 0, waited = 0;  // lane 0: progress of the other functions
+    auto wait_for = [&](uint32_t chunk) -> int {
+        while (wc < chunk) need -= hist[wc++];
+        waited = chunk + 1;
+        return ra_wait_chunk(done, chunk, need, P.err) ? 0 : 1;
+    };
+    int abort = 0;
+    Ra2Slot L;
+    L.act = false;
+    L.have_next = false;
+    uint32_t s0 = 0;
+    if (lane == 0) {
+        for (uint32_t x = 0; x < chunks; ++x) need += hist[x];
+        if (chunks > 0 && S > 0) abort = wait_for(0);
+        ra2_slot_init(P, c, L, 0, 0);
+        s0 = min(ra2_lane0_size(L), S);
+    }
+    sh.R0[lane] = sh.R0[lane + 32] = kNone;
+    sh.R0own[lane] = sh.R0own[lane + 32] = kNone;
+    s0 = __shfl_sync(full, s0, 0);
+    if (__shfl_sync(full, abort, 0)) return;
+    unsigned long long occ = 0;  // lane 0: positions whose row-0 entry is a virtual register
+    uint32_t t0 = 0, t1 = 0;     // this step's records at positions lane and lane + 32
+    if (s0 > 0) {
+        t0 = __ldcg(&P.trig_max[lane]);
+        t1 = __ldcg(&P.trig_max[32u + lane]);
+    }
+    __syncwarp();
+    for (uint32_t i = 0; i < s0; ++i) {
+        if (chunks > 0 && i + 2 < S && (i + 2) % kRaChunk == 0) {
+            int ab = 0;
+            if (lane == 0) ab = wait_for((i + 2) / kRaChunk);
+            if (__shfl_sync(full, ab, 0)) return;
+        }
+        const unsigned long long others = static_cast<unsigned long long>(__ballot_sync(full, t0 != 0)) |
+                                          (static_cast<unsigned long long>(__ballot_sync(full, t1 != 0)) << 32);
+        if (i + 1 < S) {  // records of the next step (its chunk is complete: waited above)
+            t0 = __ldcg(&P.trig_max[static_cast<size_t>(i + 1) * 64u + lane]);
+            t1 = __ldcg(&P.trig_max[static_cast<size_t>(i + 1) * 64u + 32u + lane]);
+        }
+        if (lane == 0) {
+            ra2_load(P, L, i, cur);
+            RaStep& St = L.S;
+            unsigned long long marks = others & occ;
+            if (L.act) {
+                uint32_t r1reg = 0, r2reg = 0;
+                bool r1s = false, r2s = false;
+                if (s32(St.r1) > 63) sym_read(P, c, 0, St.r1, &r1reg, &r1s);
+                if (s32(St.r2) > 63) sym_read(P, c, 0, St.r2, &r2reg, &r2s);
+                ra_compute(St, L.lifetime, r1reg, r1s, r2reg, r2s);
+                L.lt_new = St.cleared | St.rdm;
+                if (s32(St.ord) > 63) sym_write(P, c, 0, St.ord, St.rdr, false, (St.rdr & 63u) + 1u);
+                if (s32(St.r1) > 63) sym_write(P, c, 0, St.r1, St.r1r, false);
+                if (s32(St.r2) > 63) sym_write(P, c, 0, St.r2, St.r2r, false);
+                marks = (others | St.trig) & occ;
+            }
+            // marks on the symbols row 0 held at the step's start, unless the slot updated them
+            for (unsigned long long m = marks; m; m &= m - 1) {
+                const uint32_t v = sh.R0[ctz64(m)];
+                const bool updated = L.act && ((s32(St.ord) > 63 && St.ord == v) || (s32(St.r1) > 63 && St.r1 == v) ||
+                                               (s32(St.r2) > 63 && St.r2 == v));
+                if (!updated) sym_mark(P, c, 0, v);
+            }
+            // row 0: the defined register at its position, cleared entries at rs1 / rs2
+            if (L.act) {
+                if (St.ord != 0) {
+                    const uint32_t q = St.rdr & 63u;
+                    sh.R0[q] = St.ord;
+                    sh.R0own[q] = 0;
+                    occ = s32(St.ord - 64u) >= 0 ? (occ | (1ull << q)) : (occ & ~(1ull << q));
+                }
+                for (const uint32_t r : {St.r1r, St.r2r}) {
+                    if (r != St.rdr && s32(r) >= 0 && r < 64u) {
+                        sh.R0[r] = kNone;
+                        sh.R0own[r] = 0;
+                        occ &= ~(1ull << r);
+                    }
+                }
+            }
+        }
+        __syncwarp();
+    }
+    if (s0 >= S) return;
+    // the steps after the slot's last one only mark row 0's symbols
+    int ab = 0;
+    if (lane == 0)
+        for (uint32_t x = waited; x < chunks && !ab; ++x) ab = wait_for(x);
+    if (__shfl_sync(full, ab, 0)) return;
+    __syncwarp();
+    ra2_tail_p(P, c, sh, lane, s0, S);
+    ra2_tail_p(P, c, sh, lane + 32u, s0, S);
+}
+
 // Register allocation steps in one launch.  Block 0 runs the lane-0 functions (f % 8 ==
 // 0) in lock-step; thread t runs slots t, t+T, ... (Q per thread), slot = group index.
 // Blocks 1.. run the independent functions, one per thread, and count finished chunks
@@ -941,6 +1078,10 @@ __device__ bool ra_wait_chunk(const uint32_t* done, uint32_t c, uint32_t need, E
 // function in smem.  With chunks > 0 it waits on the independent functions' progress.
 template <int Q>
 __device__ void ra_lane0_block(const Prog& P, uint32_t S, uint32_t K, uint32_t chunks, unsigned char* smem) {
+    if (P.F <= 8u && P.defpos) {  // one lane-0 function: warp 0 alone, no block barriers
+        if (threadIdx.x < 32) ra_lane0_single(P, S, K, chunks, smem);
+        return;
+    }
     const uint32_t tid = threadIdx.x, T = blockDim.x;
     __shared__ uint32_t s_abort, s_s0;
     const uint32_t* hist = P.ra_chunks;
@@ -1227,7 +1368,7 @@ cudaError_t run_sort_rounds(const SortScratch& ss, uint32_t nseg0, uint32_t firs
     }
     if (lh[4]) {
         const size_t smem = sizeof(BlockSortSmem);
-        e = cudaFuncSetAttribute(k_sort_block, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+        e = allow_dynamic_smem(reinterpret_cast<const void*>(k_sort_block), smem);
         if (e != cudaSuccess) return e;
         g_launches++;
         k_sort_block<<<lh[4], kSortBlockThreads, smem, s>>>(ss, lh[4], err);
@@ -1314,7 +1455,7 @@ cudaError_t launch_ra_steps_q(const Prog& P0, const Prog& Pfree, uint32_t G0, ui
     uint32_t Kf = 64;
     while (Kf > 1 && static_cast<size_t>(T) * Kf * 8u > kBudget) Kf >>= 1;
     const size_t smem = std::max(fixed + static_cast<size_t>(G0) * K * 8u, static_cast<size_t>(T) * Kf * 8u) + 16;
-    cudaError_t ce = cudaFuncSetAttribute(k_ra_steps<Q>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+    cudaError_t ce = allow_dynamic_smem(reinterpret_cast<const void*>(k_ra_steps<Q>), smem);
     if (ce != cudaSuccess) return ce;
     uint32_t S = P0.S;
     // One launch when its blocks can all be resident: the independent functions run
@@ -1930,7 +2071,7 @@ void batch_sizes(bool w3, const Prog* progs, const uint32_t* list, uint32_t coun
 }
 
 cudaError_t batch_regalloc(const Prog* progs, const uint32_t* item_off, const uint32_t* order, uint32_t n,
-                           uint32_t items, uint32_t max_g0, uint32_t* queue, cudaStream_t s) {
+                           uint32_t items, uint32_t max_g0, uint32_t* queue, cudaStream_t s, double share) {
     if (items == 0) return cudaSuccess;
     const uint32_t T = batch_ra_threads(max_g0);
     const uint32_t Q = (max_g0 + T - 1u) / T;
@@ -1945,13 +2086,15 @@ cudaError_t batch_regalloc(const Prog* progs, const uint32_t* item_off, const ui
     const size_t smem = std::max(fixed + static_cast<size_t>(max_g0) * K * 8u, static_cast<size_t>(T) * Kf * 8u) + 16;
     BatchRa ra{progs, item_off, order, n, items, queue, K, Kf};
     auto go = [&](auto kernel) -> cudaError_t {
-        cudaError_t ce = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+        cudaError_t ce = allow_dynamic_smem(reinterpret_cast<const void*>(kernel), smem);
         if (ce != cudaSuccess) return ce;
         int dev = 0, sms = 0, per_sm = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, static_cast<int>(T), smem);
-        const unsigned grid = static_cast<unsigned>(std::max<uint64_t>(1, std::min<uint64_t>(items, static_cast<uint64_t>(std::max(per_sm, 1)) * sms)));
+        const uint64_t resident = static_cast<uint64_t>(std::max(per_sm, 1)) * sms;
+        const uint64_t allowed = std::max<uint64_t>(1, static_cast<uint64_t>(static_cast<double>(resident) * share));
+        const unsigned grid = static_cast<unsigned>(std::max<uint64_t>(1, std::min<uint64_t>(items, allowed)));
         cudaMemsetAsync(queue, 0, sizeof(uint32_t), s);
         g_launches++;
         kernel<<<grid, T, smem, s>>>(ra);

@@ -113,7 +113,9 @@ void batch_serial(const Prog* progs, const uint32_t* list, uint32_t count, cudaS
 // batch_ra_threads(max_g0), then its lane-0 pass, which follows their progress through
 // the program's ra_chunks record: histogram (BatchStage::RaHist) then zeroed counts).
 uint32_t batch_ra_threads(uint32_t max_g0);
+// share: the part of the device's resident blocks the persistent launch may take (1 =
+// all; less leaves room for other streams' kernels, e.g. a compile server's other lanes).
 cudaError_t batch_regalloc(const Prog* progs, const uint32_t* item_off, const uint32_t* order, uint32_t n,
-                           uint32_t items, uint32_t max_g0, uint32_t* queue, cudaStream_t s);
+                           uint32_t items, uint32_t max_g0, uint32_t* queue, cudaStream_t s, double share = 1.0);
 
 }  // namespace ptl
