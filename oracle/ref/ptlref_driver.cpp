@@ -39,6 +39,7 @@
 #include <string>
 #include <string_view>
 #include <thread>
+#include <mutex>
 #include <tuple>
 #include <type_traits>
 #include <unordered_map>
@@ -136,6 +137,18 @@ extern "C" void ptlref_free_tree(ptlref_tree* t) {
     std::memset(t, 0, sizeof(*t));
 }
 
+// The reference's destructor (src/codegen/rv_generator_avx.cpp:70-80) releases its
+// worker threads and detaches them; they then read the destroyed generator's fields as
+// they wake, a use after free that crashed the calling process at random.  The harness
+// never destroys a generator: each is kept in a list that is never freed (not even at
+// exit), and its workers stay parked on its barrier.
+static void keep_alive(std::unique_ptr<rv_generator_avx> gen) {
+    static std::mutex mu;
+    static auto* kept = new std::vector<std::unique_ptr<rv_generator_avx>>();
+    std::lock_guard<std::mutex> lk(mu);
+    kept->push_back(std::move(gen));
+}
+
 extern "C" int ptlref_compile(const ptlref_tree* in, int threads, int sync, int altblock,
                               uint32_t mininstr, int snapshots, ptlref_result* out,
                               char* err, size_t errlen) {
@@ -157,7 +170,9 @@ extern "C" int ptlref_compile(const ptlref_tree* in, int threads, int sync, int 
         std::streambuf* saved = std::cerr.rdbuf(nullptr);
         auto gen = std::make_unique<rv_generator_avx>(*tree, threads, sync, altblock != 0, mininstr);
         std::cerr.rdbuf(saved);
-        out->threads_used = static_cast<int>(gen->threads);
+        rv_generator_avx* g = gen.get();
+        keep_alive(std::move(gen));  // before any stage can throw
+        out->threads_used = static_cast<int>(g->threads);
 
         using clock = std::chrono::steady_clock;
         auto timed = [&](int idx, auto fn) {
@@ -168,66 +183,63 @@ extern "C" int ptlref_compile(const ptlref_tree* in, int threads, int sync, int 
                 std::chrono::duration_cast<std::chrono::nanoseconds>(t1 - t0).count());
         };
 
-        timed(0, [&] { gen->preprocess(); });
+        timed(0, [&] { g->preprocess(); });
         if (snapshots) {
-            out->bufs[PTLREF_PRE_TYPE] = copy_buf(gen->node_types);
-            out->bufs[PTLREF_PRE_RTYPE] = copy_buf(gen->result_types);
-            out->bufs[PTLREF_PRE_DATA] = copy_buf(gen->node_data);
+            out->bufs[PTLREF_PRE_TYPE] = copy_buf(g->node_types);
+            out->bufs[PTLREF_PRE_RTYPE] = copy_buf(g->result_types);
+            out->bufs[PTLREF_PRE_DATA] = copy_buf(g->node_data);
         }
-        timed(1, [&] { gen->isn_cnt(); });
+        timed(1, [&] { g->isn_cnt(); });
         if (snapshots) {
-            out->bufs[PTLREF_CNT_SIZE] = copy_buf(gen->node_sizes);
-            out->bufs[PTLREF_CNT_LOC] = copy_buf(gen->node_locations);
-            out->bufs[PTLREF_CNT_FN_ID] = copy_buf(gen->function_ids);
-            out->bufs[PTLREF_CNT_FN_START] = copy_buf(gen->func_starts);
-            out->bufs[PTLREF_CNT_FN_END] = copy_buf(gen->func_ends);
-            out->bufs[PTLREF_CNT_FN_SIZE] = copy_buf(gen->function_sizes);
+            out->bufs[PTLREF_CNT_SIZE] = copy_buf(g->node_sizes);
+            out->bufs[PTLREF_CNT_LOC] = copy_buf(g->node_locations);
+            out->bufs[PTLREF_CNT_FN_ID] = copy_buf(g->function_ids);
+            out->bufs[PTLREF_CNT_FN_START] = copy_buf(g->func_starts);
+            out->bufs[PTLREF_CNT_FN_END] = copy_buf(g->func_ends);
+            out->bufs[PTLREF_CNT_FN_SIZE] = copy_buf(g->function_sizes);
         }
-        timed(2, [&] { gen->isn_gen(); });
+        timed(2, [&] { g->isn_gen(); });
         if (snapshots) {
-            out->bufs[PTLREF_GEN_INSTR] = copy_buf(gen->instr);
-            out->bufs[PTLREF_GEN_RD] = copy_buf(gen->rd_avx);
-            out->bufs[PTLREF_GEN_RS1] = copy_buf(gen->rs1_avx);
-            out->bufs[PTLREF_GEN_RS2] = copy_buf(gen->rs2_avx);
-            out->bufs[PTLREF_GEN_JT] = copy_buf(gen->jt_avx);
+            out->bufs[PTLREF_GEN_INSTR] = copy_buf(g->instr);
+            out->bufs[PTLREF_GEN_RD] = copy_buf(g->rd_avx);
+            out->bufs[PTLREF_GEN_RS1] = copy_buf(g->rs1_avx);
+            out->bufs[PTLREF_GEN_RS2] = copy_buf(g->rs2_avx);
+            out->bufs[PTLREF_GEN_JT] = copy_buf(g->jt_avx);
         }
-        timed(3, [&] { gen->optimize(); });
+        timed(3, [&] { g->optimize(); });
         if (snapshots) {
-            out->bufs[PTLREF_OPT_USED] = copy_buf(gen->used_instrs_avx);
+            out->bufs[PTLREF_OPT_USED] = copy_buf(g->used_instrs_avx);
         }
-        timed(4, [&] { gen->regalloc(); });
+        timed(4, [&] { g->regalloc(); });
         if (snapshots) {
-            out->bufs[PTLREF_RA_INSTR] = copy_buf(gen->instr);
-            out->bufs[PTLREF_RA_RD] = copy_buf(gen->rd_avx);
-            out->bufs[PTLREF_RA_RS1] = copy_buf(gen->rs1_avx);
-            out->bufs[PTLREF_RA_RS2] = copy_buf(gen->rs2_avx);
-            out->bufs[PTLREF_RA_JT] = copy_buf(gen->jt_avx);
-            out->bufs[PTLREF_RA_FN_START] = copy_buf(gen->func_starts);
-            out->bufs[PTLREF_RA_FN_END] = copy_buf(gen->func_ends);
-            out->bufs[PTLREF_RA_FN_SIZE] = copy_buf(gen->function_sizes);
+            out->bufs[PTLREF_RA_INSTR] = copy_buf(g->instr);
+            out->bufs[PTLREF_RA_RD] = copy_buf(g->rd_avx);
+            out->bufs[PTLREF_RA_RS1] = copy_buf(g->rs1_avx);
+            out->bufs[PTLREF_RA_RS2] = copy_buf(g->rs2_avx);
+            out->bufs[PTLREF_RA_JT] = copy_buf(g->jt_avx);
+            out->bufs[PTLREF_RA_FN_START] = copy_buf(g->func_starts);
+            out->bufs[PTLREF_RA_FN_END] = copy_buf(g->func_ends);
+            out->bufs[PTLREF_RA_FN_SIZE] = copy_buf(g->function_sizes);
         }
-        timed(5, [&] { gen->fix_jumps(); });
+        timed(5, [&] { g->fix_jumps(); });
         if (snapshots) {
-            out->bufs[PTLREF_FJ_INSTR] = copy_buf(gen->instr);
-            out->bufs[PTLREF_FJ_RD] = copy_buf(gen->rd_avx);
-            out->bufs[PTLREF_FJ_RS1] = copy_buf(gen->rs1_avx);
-            out->bufs[PTLREF_FJ_RS2] = copy_buf(gen->rs2_avx);
-            out->bufs[PTLREF_FJ_JT] = copy_buf(gen->jt_avx);
-            out->bufs[PTLREF_FJ_FN_START] = copy_buf(gen->func_starts);
-            out->bufs[PTLREF_FJ_FN_END] = copy_buf(gen->func_ends);
-            out->bufs[PTLREF_FJ_FN_SIZE] = copy_buf(gen->function_sizes);
+            out->bufs[PTLREF_FJ_INSTR] = copy_buf(g->instr);
+            out->bufs[PTLREF_FJ_RD] = copy_buf(g->rd_avx);
+            out->bufs[PTLREF_FJ_RS1] = copy_buf(g->rs1_avx);
+            out->bufs[PTLREF_FJ_RS2] = copy_buf(g->rs2_avx);
+            out->bufs[PTLREF_FJ_JT] = copy_buf(g->jt_avx);
+            out->bufs[PTLREF_FJ_FN_START] = copy_buf(g->func_starts);
+            out->bufs[PTLREF_FJ_FN_END] = copy_buf(g->func_ends);
+            out->bufs[PTLREF_FJ_FN_SIZE] = copy_buf(g->function_sizes);
         }
-        timed(6, [&] { gen->postprocess(); });
+        timed(6, [&] { g->postprocess(); });
 
-        out->bufs[PTLREF_OUT_WORDS] = copy_buf(gen->instr);
-        out->bufs[PTLREF_FN_START] = copy_buf(gen->func_starts);
-        out->bufs[PTLREF_FN_END] = copy_buf(gen->func_ends);
-        out->bufs[PTLREF_FN_SIZE] = copy_buf(gen->function_sizes);
-        out->bufs[PTLREF_FN_ID] = copy_buf(gen->function_ids);
+        out->bufs[PTLREF_OUT_WORDS] = copy_buf(g->instr);
+        out->bufs[PTLREF_FN_START] = copy_buf(g->func_starts);
+        out->bufs[PTLREF_FN_END] = copy_buf(g->func_ends);
+        out->bufs[PTLREF_FN_SIZE] = copy_buf(g->function_sizes);
+        out->bufs[PTLREF_FN_ID] = copy_buf(g->function_ids);
 
-        saved = std::cerr.rdbuf(nullptr);
-        gen.reset();
-        std::cerr.rdbuf(saved);
         return 0;
     } catch (const std::exception& e) {
         set_err(err, errlen, e.what());

@@ -79,13 +79,12 @@ _lib = None
 
 
 def build(ref_root: str = REF_ROOT_DEFAULT, quiet: bool = True) -> bool:
-    """Compile the reference into oracle/_ref (no-op when it is already built).
+    """Compile the reference into oracle/_ref (make rebuilds only what changed; where the
+    reference tree is absent an existing build is used as it is).
 
-    Returns False where the reference tree is absent or the host is not x86-64."""
-    if os.path.exists(LIB_PATH):
-        return True
+    Returns False where there is neither a build nor a reference tree on an x86-64 host."""
     if not os.path.isdir(ref_root) or os.uname().machine not in ("x86_64", "AMD64"):
-        return False
+        return os.path.exists(LIB_PATH)
     cmd = ["make", "-C", os.path.join(HERE, "ref"), f"REF={ref_root}", f"-j{os.cpu_count() or 4}"]
     res = subprocess.run(cmd, capture_output=quiet)
     return res.returncode == 0 and os.path.exists(LIB_PATH)
