@@ -499,8 +499,8 @@ PTL_HD void st_gen_claim(const Prog& P, uint32_t x) {
     const bool loop2 = N.t == RV_IF_ELSE || N.t == RV_WHILE;  // slot 1 goes where a register says
     const uint32_t r1 = loop2 ? P.regs[x * 3u + 1u] : 0u, r2 = loop2 ? P.regs[x * 3u + 2u] : 0u;
     for (uint32_t s = 0; s < 4; ++s) {
+        if (!P.tab.has_instr(N.t, s, N.rt)) continue;  // most slots: no instruction
         const GenLane L = gen_lane(P, N, s);
-        if (!L.has) continue;
         const uint32_t loc = gen_loc(P, N, s, L, r1, r2);
         if (loc >= P.W) {
             record_error(P.err, ST_UNSUPPORTED, W_GEN, x);
@@ -518,8 +518,8 @@ PTL_HD void st_gen_write(const Prog& P, uint32_t x) {
     const uint32_t reg[3] = {P.regs[x * 3u], P.regs[x * 3u + 1u], P.regs[x * 3u + 2u]};
     const uint32_t nd = N.nd;
     for (uint32_t s = 0; s < 4; ++s) {
+        if (!P.tab.has_instr(t, s, rt)) continue;  // most slots: no instruction
         const GenLane L = gen_lane(P, N, s);
-        if (!L.has) continue;
         const uint32_t loc = gen_loc(P, N, s, L, reg[1], reg[2]);
         if (loc >= P.W || P.owner[loc] != (key | s)) continue;
         // instruction word and constants, :752-779
