@@ -232,6 +232,7 @@ public:
     // tile sizes: element-wise stages, optimize sweeps (chosen by the autotuner or the defaults)
     uint32_t elem_tile = batch_tile(), sweep_tile = 1024;
     double ra_share = 1.0;  // part of the resident blocks the persistent regalloc launch takes
+    SortRoundGraph sort_graph;  // a pair of depth-sort rounds, replayed
     uint32_t slot_tile[32] = {};
 
     std::vector<Prog> hp;  // host copies of the views
@@ -712,7 +713,7 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
         uint32_t rounds = 0;
         const uint32_t lb = floor_log2(kSortBlock);
         BP_CU(run_sort_rounds(ss, static_cast<uint32_t>(segs.size()), min_lg > lb ? min_lg - lb : 1, 2 * max_lg + 4,
-                              sort_err.at<ErrorWord>(), s, &rounds));
+                              sort_err.at<ErrorWord>(), s, &rounds, &sort_graph));
         batch_sort_keys(bl(4), t_n2, sa.at<unsigned long long>(), a_off.at<uint64_t>(), true);
         batch_stage(BatchStage::Gen, bl(4), t_n2, nullptr, nullptr, nullptr);
         {

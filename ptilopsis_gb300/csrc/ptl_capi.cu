@@ -126,6 +126,7 @@ struct ptl_generator {
     bool host_valid = false;
     uint64_t stage_ns[7] = {0, 0, 0, 0, 0, 0, 0};
     uint32_t sort_rounds = 0, opt_sweeps = 0;
+    SortRoundGraph sort_graph;  // a pair of depth-sort rounds, replayed
     bool ra_serial = false;
 
     ~ptl_generator() {
@@ -435,7 +436,7 @@ ptl_status run_pipeline(ptl_generator* g, bool profile, bool to_host, bool row0_
     if (!prog_ready(P, {P.instr, P.rd, P.rs1, P.rs2, P.jt, P.used_instrs, P.symreg, P.symswp, P.stamp, P.spill,
                         P.defpos, P.roffs, P.owner, P.used, P.smark, P.pos, P.regs}))
         return fail(g, PTL_CUDA_ERROR, "internal: unallocated word arrays");
-    PTL_CU(run_depth_sort(P, ss, s, &g->sort_rounds));
+    PTL_CU(run_depth_sort(P, ss, s, &g->sort_rounds, &g->sort_graph));
     launch_gen(P, s);
     if (ptl_status st = check_error_word(g); st != PTL_OK) return st;
     timer.mark();

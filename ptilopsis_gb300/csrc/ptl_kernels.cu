@@ -1314,34 +1314,80 @@ void launch_functab(const Prog& P, uint32_t* meta, cudaStream_t s) {
 // the device; the host checks for the end (no segments left) after a first batch of
 // first_batch rounds and then every few rounds.  Rounds after the end find no segments and
 // return at once.
-cudaError_t run_sort_rounds(const SortScratch& ss, uint32_t nseg0, uint32_t first_batch, uint32_t max_rounds,
-                            ErrorWord* err, cudaStream_t s, uint32_t* rounds_out) {
-    cudaMemcpyAsync(ss.counters + 1, &nseg0, sizeof(uint32_t), cudaMemcpyHostToDevice, s);
+namespace {
+constexpr uint32_t kRoundLaunches = 7;  // kernels per partition round
+
+void launch_sort_round(const SortScratch& ss, SortSeg* segs, SortSeg* next, ErrorWord* err, cudaStream_t s) {
     const unsigned seg_grid = static_cast<unsigned>(std::min<uint64_t>(ss.seg_cap, 152ull * 8));
     const unsigned tile_grid = static_cast<unsigned>(std::min<uint64_t>(ss.tile_cap, 152ull * 8));
+    k_sort_round<<<1, 32, 0, s>>>(ss);
+    k_sort_tiles<<<grid_for(ss.seg_cap), kThreads, 0, s>>>(ss, segs, segs);
+    k_sort_count<<<tile_grid, kThreads, 0, s>>>(ss, segs);
+    k_sort_segscan<<<seg_grid, kThreads, 0, s>>>(ss, segs);
+    k_sort_pos<<<tile_grid, kThreads, 0, s>>>(ss, segs);
+    k_sort_cut<<<grid_for(ss.seg_cap), kThreads, 0, s>>>(ss, segs, next, err);
+    k_sort_swap<<<tile_grid, kThreads, 0, s>>>(ss, segs);
+}
+
+bool same_layout(const SortScratch& a, const SortScratch& b) {
+    return a.a == b.a && a.apos == b.apos && a.bpos == b.bpos && a.seg[0] == b.seg[0] && a.seg[1] == b.seg[1] &&
+           a.seg_cap == b.seg_cap && a.tile_seg == b.tile_seg && a.tile_l == b.tile_l && a.tile_r == b.tile_r &&
+           a.tile_cap == b.tile_cap && a.leaf == b.leaf && a.heap == b.heap && a.leaf_cap == b.leaf_cap &&
+           a.local == b.local && a.equal == b.equal && a.counters == b.counters;
+}
+
+// The graph of two rounds for this layout (captured when it has none or another).
+cudaError_t round_pair_graph(SortRoundGraph& g, const SortScratch& ss, ErrorWord* err, cudaStream_t s) {
+    if (g.exec && g.err == err && same_layout(g.ss, ss)) return cudaSuccess;
+    if (g.exec) {
+        cudaGraphExecDestroy(g.exec);
+        g.exec = nullptr;
+    }
+    cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return e;
+    launch_sort_round(ss, ss.seg[0], ss.seg[1], err, s);
+    launch_sort_round(ss, ss.seg[1], ss.seg[0], err, s);
+    cudaGraph_t graph = nullptr;
+    e = cudaStreamEndCapture(s, &graph);
+    if (e != cudaSuccess) return e;
+    e = cudaGraphInstantiate(&g.exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+        g.exec = nullptr;
+        return e;
+    }
+    g.ss = ss;
+    g.err = err;
+    return cudaSuccess;
+}
+}  // namespace
+
+cudaError_t run_sort_rounds(const SortScratch& ss, uint32_t nseg0, uint32_t first_batch, uint32_t max_rounds,
+                            ErrorWord* err, cudaStream_t s, uint32_t* rounds_out, SortRoundGraph* graph) {
+    cudaMemcpyAsync(ss.counters + 1, &nseg0, sizeof(uint32_t), cudaMemcpyHostToDevice, s);
     uint32_t rounds = 0, nseg = nseg0;
     int cur = 0;
     uint32_t batch = std::max<uint32_t>(first_batch, 1u);
+    if (graph && nseg > 0) {
+        const cudaError_t e = round_pair_graph(*graph, ss, err, s);
+        if (e != cudaSuccess) return e;
+        batch += batch & 1u;  // whole pairs; a round after the end finds no segments
+    }
     while (nseg > 0) {
-        for (uint32_t r = 0; r < batch; ++r) {
-            SortSeg* segs = ss.seg[cur];
-            SortSeg* next = ss.seg[cur ^ 1];
-            g_launches++;
-            k_sort_round<<<1, 32, 0, s>>>(ss);
-            g_launches++;
-            k_sort_tiles<<<grid_for(ss.seg_cap), kThreads, 0, s>>>(ss, segs, segs);
-            g_launches++;
-            k_sort_count<<<tile_grid, kThreads, 0, s>>>(ss, segs);
-            g_launches++;
-            k_sort_segscan<<<seg_grid, kThreads, 0, s>>>(ss, segs);
-            g_launches++;
-            k_sort_pos<<<tile_grid, kThreads, 0, s>>>(ss, segs);
-            g_launches++;
-            k_sort_cut<<<grid_for(ss.seg_cap), kThreads, 0, s>>>(ss, segs, next, err);
-            g_launches++;
-            k_sort_swap<<<tile_grid, kThreads, 0, s>>>(ss, segs);
-            cur ^= 1;
-            ++rounds;
+        if (graph) {
+            for (uint32_t r = 0; r < batch; r += 2) {
+                const cudaError_t e = cudaGraphLaunch(graph->exec, s);
+                if (e != cudaSuccess) return e;
+                g_launches += 2 * kRoundLaunches;
+                rounds += 2;
+            }
+        } else {
+            for (uint32_t r = 0; r < batch; ++r) {
+                launch_sort_round(ss, ss.seg[cur], ss.seg[cur ^ 1], err, s);
+                g_launches += kRoundLaunches;
+                cur ^= 1;
+                ++rounds;
+            }
         }
         uint32_t c[6] = {0, 0, 0, 0, 0, 0};
         cudaMemcpyAsync(c, ss.counters, sizeof(c), cudaMemcpyDeviceToHost, s);
@@ -1377,7 +1423,8 @@ cudaError_t run_sort_rounds(const SortScratch& ss, uint32_t nseg0, uint32_t firs
     return cudaGetLastError();
 }
 
-cudaError_t run_depth_sort(const Prog& P, const SortScratch& ss, cudaStream_t s, uint32_t* rounds_out) {
+cudaError_t run_depth_sort(const Prog& P, const SortScratch& ss, cudaStream_t s, uint32_t* rounds_out,
+                           SortRoundGraph* graph) {
     const uint32_t n = P.n;
     g_launches++;
     k_sort_init<<<grid_for(n), kThreads, 0, s>>>(P, ss);
@@ -1403,7 +1450,7 @@ cudaError_t run_depth_sort(const Prog& P, const SortScratch& ss, cudaStream_t s,
     }
     const uint32_t lg = floor_log2(std::max<uint32_t>(n, 2u));
     const uint32_t lb = floor_log2(kSortBlock);
-    const cudaError_t e = run_sort_rounds(ss, nseg, lg > lb ? lg - lb : 1u, 2u * lg + 4u, P.err, s, rounds_out);
+    const cudaError_t e = run_sort_rounds(ss, nseg, lg > lb ? lg - lb : 1u, 2u * lg + 4u, P.err, s, rounds_out, graph);
     if (e != cudaSuccess) return e;
     g_launches++;
     k_sort_out<<<grid_for(n), kThreads, 0, s>>>(P, ss);

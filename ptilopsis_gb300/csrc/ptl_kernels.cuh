@@ -49,9 +49,6 @@ void launch_fix(const Prog& P, cudaStream_t s);
 void launch_decl_scan(const Prog& P, uint32_t* flags_tmp, const ScanScratch& sc, cudaStream_t s);
 void launch_functab(const Prog& P, uint32_t* meta, cudaStream_t s);
 
-// Depth-order emulation; returns a CUDA error and needs the host for its round loop.
-cudaError_t run_depth_sort(const Prog& P, const SortScratch& ss, cudaStream_t s, uint32_t* rounds_out);
-
 void launch_gen(const Prog& P, cudaStream_t s);
 cudaError_t run_optimize(const Prog& P, cudaStream_t s, uint32_t* sweeps_out);
 cudaError_t run_regalloc_steps(const Prog& P, cudaStream_t s, bool* serial_out, bool row0_hash);
@@ -60,9 +57,30 @@ void launch_regalloc_emit(const Prog& P, cudaStream_t s);
 void launch_fixjumps_scan(const Prog& P, const ScanScratch& sc, cudaStream_t s);
 void launch_fixjumps_emit(const Prog& P, cudaStream_t s);
 
+// Two partition rounds as one CUDA graph.  Every launch of a round takes its arguments
+// from the scratch layout (pointers, capacities) and reads its counts on the device, and
+// the segment lists alternate, so a pair of rounds ends where it began and replays as one
+// graph launch.  Captured on first use and again when the layout changes.
+struct SortRoundGraph {
+    cudaGraphExec_t exec = nullptr;
+    SortScratch ss{};
+    ErrorWord* err = nullptr;
+    SortRoundGraph() = default;
+    SortRoundGraph(const SortRoundGraph&) = delete;
+    SortRoundGraph& operator=(const SortRoundGraph&) = delete;
+    ~SortRoundGraph() {
+        if (exec) cudaGraphExecDestroy(exec);
+    }
+};
+
+// Depth-order emulation; returns a CUDA error and needs the host for its round loop.
+cudaError_t run_depth_sort(const Prog& P, const SortScratch& ss, cudaStream_t s, uint32_t* rounds_out,
+                           SortRoundGraph* graph = nullptr);
+
 // Introsort rounds over prepared segments (ss.seg[0], counters), then heaps and leaves.
+// With graph, rounds run as replays of a captured pair.
 cudaError_t run_sort_rounds(const SortScratch& ss, uint32_t nseg0, uint32_t first_batch, uint32_t max_rounds,
-                            ErrorWord* err, cudaStream_t s, uint32_t* rounds_out);
+                            ErrorWord* err, cudaStream_t s, uint32_t* rounds_out, SortRoundGraph* graph = nullptr);
 
 // ---- batched programs: per-program Prog views in device memory (progs[B]); off[B+1]
 // holds each program's first tile for the stage's element count.
