@@ -178,6 +178,16 @@ ptl_status ptl_batch_set_tiles(ptl_batch* batch, uint32_t elem_tile, uint32_t sw
 ptl_status ptl_batch_tiles(const ptl_batch* batch, uint32_t tiles[2]);
 void ptl_batch_destroy(ptl_batch* batch);
 
+/* ---- Text output.  ptl_to_asm replaces rv_generator::to_asm
+ * (src/codegen/rv_generator.cpp:121-127): one line per word, "name operands\n", as
+ * rvdisasm::instruction prints it.  ptl_disassemble replaces rvdisasm::disassemble
+ * (src/disassembler.cpp:411-451): the coloured listing with indices, addresses, bytes and
+ * "funcN:" labels at the word indices in func_starts (n > 0).  Both write at most cap
+ * bytes to out and set *len to the text's full length; out = NULL only measures. */
+ptl_status ptl_to_asm(const uint32_t* words, size_t n, char* out, size_t cap, size_t* len);
+ptl_status ptl_disassemble(const uint32_t* words, size_t n, uint64_t start_addr, const uint64_t* func_starts,
+                           size_t nfunc, char* out, size_t cap, size_t* len);
+
 /* ---- Compile server.  No counterpart in the reference.  Continuous batching over
  * `slots` lanes (1..16), each a batched pipeline with its own stream and resident arenas:
  * a free lane takes every queued request of its size class (below or above 64k nodes;

@@ -72,6 +72,12 @@ void ptlref_free_result(ptlref_result* r);
 /* Flat dumps of the reference tables; see ptlport_table in oracle/port/ptl_port.h. */
 size_t ptlref_table(int which, uint32_t* out);
 
+/* The reference's text output of words (rv_generator::to_asm, rvdisasm::disassemble)
+ * into out (at most cap bytes); returns the text's full length. */
+size_t ptlref_to_asm(const uint32_t* words, size_t n, char* out, size_t cap);
+size_t ptlref_disassemble(const uint32_t* words, size_t n, uint64_t start_addr, const uint64_t* func_starts,
+                          size_t nfunc, char* out, size_t cap);
+
 #ifdef __cplusplus
 }
 #endif

@@ -59,6 +59,7 @@
 #define protected public
 #include "codegen/depthtree.hpp"
 #include "codegen/rv_generator_avx.hpp"
+#include "disassembler.hpp"
 #undef private
 #undef protected
 
@@ -281,4 +282,26 @@ extern "C" size_t ptlref_table(int which, uint32_t* out) {
     }
     if (out) std::memcpy(out, src, count * 4);
     return count;
+}
+
+namespace {
+size_t put_text(const std::string& t, char* out, size_t cap) {
+    if (out) std::memcpy(out, t.data(), std::min(cap, t.size()));
+    return t.size();
+}
+}  // namespace
+
+extern "C" size_t ptlref_to_asm(const uint32_t* words, size_t n, char* out, size_t cap) {
+    std::ostringstream os;
+    for (size_t k = 0; k < n; ++k) os << rvdisasm::instruction(words[k]) << '\n';  // rv_generator::to_asm
+    return put_text(os.str(), out, cap);
+}
+
+extern "C" size_t ptlref_disassemble(const uint32_t* words, size_t n, uint64_t start_addr, const uint64_t* func_starts,
+                                     size_t nfunc, char* out, size_t cap) {
+    std::vector<uint32_t> w(words, words + n);
+    std::vector<uint64_t> f(func_starts, func_starts + nfunc);
+    std::ostringstream os;
+    rvdisasm::disassemble(os, w, start_addr, f);
+    return put_text(os.str(), out, cap);
 }

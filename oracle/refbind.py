@@ -164,3 +164,32 @@ def compile_ast(ast: Ast, threads: int = 1, sync: int = 0, altblock: int = 0,
         return out
     finally:
         L.ptlref_free_result(ctypes.byref(r))
+
+
+def to_asm(words) -> str:
+    """The reference's rv_generator::to_asm text of the words."""
+    L = lib()
+    w = np.ascontiguousarray(words, np.uint32)
+    fn = L.ptlref_to_asm
+    fn.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_char_p, ctypes.c_size_t]
+    fn.restype = ctypes.c_size_t
+    n = fn(w.ctypes.data, w.shape[0], None, 0)
+    buf = ctypes.create_string_buffer(n + 1)
+    fn(w.ctypes.data, w.shape[0], buf, n)
+    return buf.raw[:n].decode()
+
+
+def disassemble(words, start_addr: int = 0, func_starts=()) -> str:
+    """The reference's rvdisasm::disassemble listing of the words."""
+    L = lib()
+    w = np.ascontiguousarray(words, np.uint32)
+    f = np.ascontiguousarray(func_starts, np.uint64)
+    fn = L.ptlref_disassemble
+    fn.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_size_t,
+                   ctypes.c_char_p, ctypes.c_size_t]
+    fn.restype = ctypes.c_size_t
+    n = fn(w.ctypes.data, w.shape[0], start_addr, f.ctypes.data, f.shape[0], None, 0)
+    buf = ctypes.create_string_buffer(n + 1)
+    fn(w.ctypes.data, w.shape[0], start_addr, f.ctypes.data, f.shape[0], buf, n)
+    return buf.raw[:n].decode()
+

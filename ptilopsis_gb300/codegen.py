@@ -273,6 +273,10 @@ class RvGenerator:
         little-endian 32-bit words."""
         stream.write(self.get_instructions().astype("<u4").tobytes())
 
+    def to_asm(self) -> str:
+        """rv_generator::to_asm (src/codegen/rv_generator.cpp:121-127): one line per word."""
+        return to_asm(self.get_instructions())
+
     def close(self) -> None:
         if self._h:
             self._lib.ptl_generator_destroy(self._h)
@@ -309,3 +313,38 @@ def device_info(device: int = 0) -> Optional[dict]:
     if L.ptl_device_info(device, name, 256, ctypes.byref(sm), ctypes.byref(ma), ctypes.byref(mi)) != 0:
         return None
     return {"name": name.value.decode(), "sm_count": sm.value, "cc": (ma.value, mi.value)}
+
+
+def _text(fn, *args) -> str:
+    n = ctypes.c_size_t()
+    st = fn(*args, None, 0, ctypes.byref(n))
+    if st != 0:
+        raise PtlError(st, fn.__name__)
+    buf = ctypes.create_string_buffer(n.value + 1)
+    st = fn(*args, buf, n.value, ctypes.byref(n))
+    if st != 0:
+        raise PtlError(st, fn.__name__)
+    return buf.raw[:n.value].decode()
+
+
+def to_asm(words) -> str:
+    """The words as RISC-V assembly, one instruction per line (ptl_to_asm)."""
+    L = lib()
+    w = np.ascontiguousarray(words, np.uint32)
+    L.ptl_to_asm.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_char_p, ctypes.c_size_t,
+                             ctypes.POINTER(ctypes.c_size_t)]
+    L.ptl_to_asm.restype = ctypes.c_int
+    return _text(L.ptl_to_asm, w.ctypes.data, w.shape[0])
+
+
+def disassemble(words, start_addr: int = 0, func_starts=()) -> str:
+    """The coloured listing of the words with indices, addresses, bytes and function
+    labels at the word indices in func_starts (ptl_disassemble)."""
+    L = lib()
+    w = np.ascontiguousarray(words, np.uint32)
+    f = np.ascontiguousarray(func_starts, np.uint64)
+    L.ptl_disassemble.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_uint64, ctypes.c_void_p,
+                                  ctypes.c_size_t, ctypes.c_char_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]
+    L.ptl_disassemble.restype = ctypes.c_int
+    return _text(L.ptl_disassemble, w.ctypes.data, w.shape[0], start_addr, f.ctypes.data, f.shape[0])
+
