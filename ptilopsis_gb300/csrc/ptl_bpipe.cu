@@ -726,15 +726,15 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
 
         // ---- optimize
         const uint32_t t_wb8 = tiles(5, wb8, elem_tile);
-        batch_stage(BatchStage::OptMark, bl(5), t_wb8, nullptr, nullptr, nullptr);
+        BP_CU(cudaMemsetAsync(changed.p, 0, 8, s));
+        // the marks, and whether some virtual result is not its instruction's own word
+        batch_stage(BatchStage::OptMark, bl(5), t_wb8, changed.at<uint32_t>(1), nullptr, nullptr);
         uint32_t* hflag = reinterpret_cast<uint32_t*>(h_small.at<uint8_t>(small_meta_off));  // B*16 >= 8
         // sweeps after the first revisit only the tiles whose marks changed (when every
         // virtual result is its instruction's own word; else every tile, every sweep);
         // they have their own tile size
         const uint32_t t_sw = tiles(17, wb8, sweep_tile);
         BP_CU(dirty.ensure(2ull * t_sw + 64));
-        BP_CU(cudaMemsetAsync(changed.p, 0, 8, s));
-        batch_selfdef(bl(17), t_sw, changed.at<uint32_t>(1));
         BP_CU(cudaMemcpyAsync(hflag + 1, changed.at<uint32_t>(1), 4, cudaMemcpyDeviceToHost, s));
         BP_CU(cudaStreamSynchronize(s));
         const bool worklist = hflag[1] == 0;

@@ -1629,6 +1629,7 @@ __device__ __forceinline__ uint32_t batch_program(const uint32_t* off, uint32_t 
 template <class Op>
 __global__ void __launch_bounds__(kThreads) k_batch(const Prog* progs, const uint32_t* off, uint32_t B, uint32_t total,
                                                     uint32_t tile, Op op) {
+    Op o = op;  // per-thread copy: an op may carry state from element to element
     for (uint32_t t = blockIdx.x; t < total; t += gridDim.x) {
         const uint32_t p = batch_program(off, B, t);
         const Prog& P = progs[p];
@@ -1636,7 +1637,7 @@ __global__ void __launch_bounds__(kThreads) k_batch(const Prog* progs, const uin
         const uint32_t base = (t - off[p]) * tile;
         for (uint32_t k = threadIdx.x; k < tile; k += kThreads) {
             const uint32_t i = base + k;
-            if (i < cnt) op(P, i, p);
+            if (i < cnt) o(P, i, p);
         }
     }
 }
@@ -1659,10 +1660,29 @@ PTL_BATCH_OP(BFunctab, P.fb8, st_functab(P, i))
 PTL_BATCH_OP(BGenProp, P.n, st_gen_prop(P, i))
 PTL_BATCH_OP(BGenClaim, P.n, st_gen_claim(P, i))
 PTL_BATCH_OP(BGenWrite, P.n, st_gen_write(P, i))
-PTL_BATCH_OP(BOptMark, P.wb8, st_opt_mark(P, i))
+// marks, and odd = 1 when some virtual result is not its instruction's own word (what
+// the optimize sweeps' worklist needs to know)
+struct BOptMark {
+    uint32_t* odd;
+    __device__ static uint32_t count(const Prog& P) { return P.wb8; }
+    __device__ void operator()(const Prog& P, uint32_t i, uint32_t) const {
+        st_opt_mark(P, i);
+        const uint32_t r = P.rd[i];
+        if (s32(r) > 63 && r - 64u != i) atomicOr(odd, 1u);
+    }
+};
 PTL_BATCH_OP(BOptFinal, P.wb8, st_opt_final(P, i))
 PTL_BATCH_OP(BInitLifetime, P.F, P.lifetime[i] = 0x1Full)
-PTL_BATCH_OP(BSpill, P.W, st_ra_spill(P, i))
+// spill flags and cross checks find each word's function from the thread's previous
+// word (the same program, 256 words earlier within a tile)
+struct BSpill {
+    uint32_t hint = 0xFFFFFFFFu, hp = 0xFFFFFFFFu;
+    __device__ static uint32_t count(const Prog& P) { return P.W; }
+    __device__ void operator()(const Prog& P, uint32_t i, uint32_t p) {
+        if (p != hp) { hp = p; hint = 0xFFFFFFFFu; }
+        st_ra_spill(P, i, &hint);
+    }
+};
 PTL_BATCH_OP(BScatter, P.wb8, st_ra_scatter(P, i))
 PTL_BATCH_OP(BRaFunctab, P.F, st_fix_functab(P, i, P.roffs, P.W))
 PTL_BATCH_OP(BRaFrame, P.F, st_ra_frame(P, i))
@@ -1673,10 +1693,16 @@ PTL_BATCH_OP(BRaHist, P.F - (P.F + 7u) / 8u,
              const uint32_t f = free_function_of(i);
              const uint32_t size = P.fn_size0[f];
              if (s32(size) > 0) atomicAdd(&P.ra_chunks[(size - 1u) / kRaChunk], 1u))
-PTL_BATCH_OP(BCross, P.W,
-             const uint32_t r = st_ra_cross(P, i, P.stamp);
-             if (r & 1u) atomicOr(&P.flags[1], 1u);
-             if (r & 2u) atomicOr(&P.flags[2], 1u))
+struct BCross {
+    uint32_t hint = 0xFFFFFFFFu, hp = 0xFFFFFFFFu;
+    __device__ static uint32_t count(const Prog& P) { return P.W; }
+    __device__ void operator()(const Prog& P, uint32_t i, uint32_t p) {
+        if (p != hp) { hp = p; hint = 0xFFFFFFFFu; }
+        const uint32_t r = st_ra_cross(P, i, P.stamp, &hint);
+        if (r & 1u) atomicOr(&P.flags[1], 1u);
+        if (r & 2u) atomicOr(&P.flags[2], 1u);
+    }
+};
 
 // per program: depths seen (seen + soff[p], max_depth + 1 entries)
 struct BDepthSeen {
@@ -1811,24 +1837,6 @@ __global__ void __launch_bounds__(kThreads) k_gather_host(HostGather g, const ui
             done = n16 * 16;
         }
         for (uint64_t k = done + threadIdx.x; k < nb; k += kThreads) d[k] = s[k];
-    }
-}
-
-// flag = 1 when some instruction's virtual result is not its own word.
-__global__ void __launch_bounds__(kThreads) k_batch_selfdef(const Prog* progs, const uint32_t* off, uint32_t B,
-                                                            uint32_t total, uint32_t tile, uint32_t* flag) {
-    for (uint32_t t = blockIdx.x; t < total; t += gridDim.x) {
-        const uint32_t p = batch_program(off, B, t);
-        const Prog& P = progs[p];
-        const uint32_t base = (t - off[p]) * tile;
-        bool odd = false;
-        for (uint32_t k = threadIdx.x; k < tile; k += kThreads) {
-            const uint32_t i = base + k;
-            if (i >= P.wb8) break;
-            const uint32_t r = P.rd[i];
-            odd |= s32(r) > 63 && r - 64u != i;
-        }
-        if (__syncthreads_or(odd) && threadIdx.x == 0) *flag = 1u;
     }
 }
 
@@ -2049,7 +2057,7 @@ void batch_stage(BatchStage st, const BatchLaunch& bl, uint32_t total, uint32_t*
             batch_launch(bl, total, BGenClaim{});
             batch_launch(bl, total, BGenWrite{});
             break;
-        case BatchStage::OptMark: batch_launch(bl, total, BOptMark{}); break;
+        case BatchStage::OptMark: batch_launch(bl, total, BOptMark{meta}); break;  // meta: the odd flag
         case BatchStage::OptFinal: batch_launch(bl, total, BOptFinal{}); break;
         case BatchStage::InitLifetime: batch_launch(bl, total, BInitLifetime{}); break;
         case BatchStage::Cross: batch_launch(bl, total, BCross{}); break;
@@ -2088,13 +2096,6 @@ void batch_sweep(const BatchLaunch& bl, uint32_t total, uint32_t* changed, const
         case 2048u: k_batch_sweep<2048u><<<grid, kThreads, 0, bl.s>>>(bl.progs, bl.off, bl.B, total, changed, cur, next); break;
         default: k_batch_sweep<1024u><<<grid, kThreads, 0, bl.s>>>(bl.progs, bl.off, bl.B, total, changed, cur, next); break;
     }
-}
-
-void batch_selfdef(const BatchLaunch& bl, uint32_t total, uint32_t* flag) {
-    if (total == 0) return;
-    g_launches++;
-    k_batch_selfdef<<<std::min<uint32_t>(total, 152u * 16u), kThreads, 0, bl.s>>>(bl.progs, bl.off, bl.B, total,
-                                                                                    bl.tile, flag);
 }
 
 void batch_scan(BatchScan which, const BatchLaunch& bl, uint32_t tiles, const ScanScratch& sc, uint32_t* meta) {

@@ -105,8 +105,9 @@ void batch_stage(BatchStage st, const BatchLaunch& bl, uint32_t total, uint32_t*
                  const uint64_t* off64);
 void batch_sort_keys(const BatchLaunch& bl, uint32_t total, unsigned long long* a, const uint64_t* aoff, bool out);
 // One optimize sweep over the tiles marked in cur (all when cur is null); marks in next
-// the tiles a cleared mark makes live again.  Valid only when batch_selfdef found every
-// virtual result to be its instruction's own word (flag 0); otherwise pass cur = null.
+// the tiles a cleared mark makes live again.  Valid only when the OptMark stage found
+// every virtual result to be its instruction's own word (its flag 0); otherwise pass
+// cur = null.
 void batch_sweep(const BatchLaunch& bl, uint32_t total, uint32_t* changed, const uint8_t* cur, uint8_t* next);
 
 // One input field of every program copied from the caller's host arrays into the device
@@ -122,7 +123,6 @@ struct HostGather {
 };
 constexpr uint32_t kGatherTile = 4096;
 void batch_gather_host(const BatchLaunch& bl, uint32_t total, const HostGather& g);
-void batch_selfdef(const BatchLaunch& bl, uint32_t total, uint32_t* flag);
 void batch_scan(BatchScan which, const BatchLaunch& bl, uint32_t tiles, const ScanScratch& sc, uint32_t* meta);
 void batch_sizes(bool w3, const Prog* progs, const uint32_t* list, uint32_t count, uint32_t* meta, cudaStream_t s);
 void batch_serial(const Prog* progs, const uint32_t* list, uint32_t count, cudaStream_t s);

@@ -716,12 +716,30 @@ PTL_HD bool ra_in_range(const Prog& P, uint32_t r) { return !(s32(r) > 63) || r 
 // symbol table and take the serial path below.  Bit 1: a lane-0 instruction defines a
 // virtual register that an earlier-counted instruction also defines (defcnt counts the
 // definitions, zeroed beforehand); the lane-0 pass then finds row-0 values by hashing.
-PTL_HD uint32_t st_ra_cross(const Prog& P, uint32_t i, uint32_t* defcnt) {
+// The function holding word i: the last function start <= i (0 when the first start is
+// past i).  The starts never decrease (6 + loc of the declarations, which no fix-up rule
+// moves, over an exclusive scan of sizes), so "start <= i" holds on a prefix and both the
+// bisection and a walk find its end.  hint: the answer for an earlier word of the same
+// program; from it a short walk forward replaces the bisection.
+PTL_HD uint32_t function_of(const Prog& P, uint32_t i, uint32_t hint = 0xFFFFFFFFu) {
+    if (hint < P.F && P.fn_start0[hint] <= i) {
+        uint32_t f = hint;
+        for (int k = 0; k < 4; ++k) {
+            if (f + 1u >= P.F || P.fn_start0[f + 1u] > i) return f;
+            ++f;
+        }
+    }
     uint32_t lo = 0, hi = P.F;
     while (hi - lo > 1) {
         const uint32_t mid = (lo + hi) / 2;
         if (P.fn_start0[mid] <= i) lo = mid; else hi = mid;
     }
+    return lo;
+}
+
+PTL_HD uint32_t st_ra_cross(const Prog& P, uint32_t i, uint32_t* defcnt, uint32_t* hint = nullptr) {
+    const uint32_t lo = function_of(P, i, hint ? *hint : 0xFFFFFFFFu);
+    if (hint) *hint = lo;
     const uint32_t rd = P.rd[i];
     if (!ra_own(P, lo, P.rs1[i]) || !ra_own(P, lo, P.rs2[i]) || !ra_own(P, lo, rd)) return 1u;
     if ((lo & 7u) != 0 || !(s32(rd) > 63)) return 0u;
@@ -801,14 +819,11 @@ PTL_HD void st_ra_serial(const Prog& P, uint32_t* active) {
 
 // Spill flag per virtual register: the reference copies swapped-ness of the symbol at
 // each function start down to the function's other registers (:1464-1469).
-PTL_HD void st_ra_spill(const Prog& P, uint32_t v) {
+PTL_HD void st_ra_spill(const Prog& P, uint32_t v, uint32_t* hint = nullptr) {
     // last function start <= v (starts are ascending in valid programs; the reference's
-    // fill follows index order, which is what the binary search reproduces)
-    uint32_t lo = 0, hi = P.F;
-    while (hi - lo > 1) {
-        const uint32_t mid = (lo + hi) / 2;
-        if (P.fn_start0[mid] <= v) lo = mid; else hi = mid;
-    }
+    // fill follows index order, which is what function_of's bisection reproduces)
+    const uint32_t lo = function_of(P, v, hint ? *hint : 0xFFFFFFFFu);
+    if (hint) *hint = lo;
     const uint32_t s = P.fn_start0[lo];
     P.spill[v] = s <= v ? (P.symswp[s] & 1u) : 0u;
 }
