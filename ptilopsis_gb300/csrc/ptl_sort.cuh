@@ -196,7 +196,7 @@ PTL_HD void leaf_sort(Arr a, uint32_t first, uint32_t last) {
 // whose warps take the parts of at most kSortLocal elements), and local_introsort
 // below, the same steps taken sequentially, in the host model.
 constexpr uint32_t kSortBlock = 8192;
-constexpr uint32_t kSortLocal = 512;
+constexpr uint32_t kSortLocal = 256;
 
 // An array view with a stride (element i at base[i * stride]).
 struct Strided {
