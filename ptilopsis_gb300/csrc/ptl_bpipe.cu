@@ -30,9 +30,9 @@
 namespace ptl {
 namespace {
 
-constexpr uint64_t kFront = 16, kBack = 80;
+constexpr uint64_t kFront = kArenaFront, kBack = kArenaBack;
 inline uint64_t r8(uint64_t n) { return (n + 7) & ~uint64_t(7); }
-inline uint64_t region(uint64_t count) { return (count + kFront + kBack + 31) & ~uint64_t(31); }
+inline uint64_t region(uint64_t count) { return arena_region(count); }
 
 struct DBuf {
     void* p = nullptr;
@@ -129,12 +129,12 @@ public:
 
     DBuf tab;  // CodeTables
     DBuf in_type, in_rtype, in_parent, in_depth, in_child, in_data;
-    DBuf nt, rt, nd1, nd, par, ci, dep, sizes, loc0, loc, pos, decl, fflag, regs, seen;
+    DBuf nt, rt, nd1, nd, par, ci, dep, loc0, loc, pos, decl, fflag, regs;
     DBuf fn_id, fn_start, fn_size, fn_end, fn_start0, fn_size0, lifetime;
     DBuf instr, rd, rs1, rs2, jt, used_instrs, symreg, symswp, stamp, spill, roffs, owner, used, smark, defpos;
     DBuf trig_min, trig_max, ra_chunks;
-    DBuf ni, nrd, nr1, nr2, njt, fsz, joffs, out;
-    DBuf errw, flags, meta, progs, tabs, lists, changed, sort_err, seen_off, a_off, dirty, ra_sync;
+    DBuf ni, nrd, nr1, nr2, njt, joffs, out;
+    DBuf errw, flags, meta, progs, tabs, lists, changed, sort_err, a_off, dirty, ra_sync;
     DBuf sa, sapos, sbpos, seg0, seg1, tile_seg, tile_l, tile_r, leaf, heap, counters, scan_status, scan_counter,
         sort_local, sort_equal;
     PBuf h_in, h_out, h_fn, h_small, h_gp;
@@ -160,11 +160,11 @@ public:
     }
     std::vector<DBuf*> all() {
         return {&tab, &in_type, &in_rtype, &in_parent, &in_depth, &in_child, &in_data, &nt, &rt, &nd1, &nd, &par,
-                &ci, &dep, &sizes, &loc0, &loc, &pos, &decl, &fflag, &regs, &seen, &fn_id, &fn_start, &fn_size,
+                &ci, &dep, &loc0, &loc, &pos, &decl, &fflag, &regs, &fn_id, &fn_start, &fn_size,
                 &fn_end, &fn_start0, &fn_size0, &lifetime, &instr, &rd, &rs1, &rs2, &jt, &used_instrs, &symreg,
                 &symswp, &stamp, &spill, &roffs, &owner, &used, &smark, &defpos, &trig_min, &trig_max, &ra_chunks, &ni, &nrd,
-                &nr1, &nr2, &njt, &fsz, &joffs, &out, &errw, &flags, &meta, &progs, &tabs, &lists, &changed,
-                &sort_err, &seen_off, &a_off, &dirty, &ra_sync, &sa, &sapos, &sbpos, &seg0, &seg1, &tile_seg, &tile_l, &tile_r,
+                &nr1, &nr2, &njt, &joffs, &out, &errw, &flags, &meta, &progs, &tabs, &lists, &changed,
+                &sort_err, &a_off, &dirty, &ra_sync, &sa, &sapos, &sbpos, &seg0, &seg1, &tile_seg, &tile_l, &tile_r,
                 &leaf, &heap, &counters, &scan_status, &scan_counter, &sort_local, &sort_equal};
     }
 
@@ -201,6 +201,18 @@ public:
         for (DBuf* b : bufs) {
             cudaError_t e = b->ensure(L.total * es);
             if (e == cudaSuccess) e = cudaMemsetAsync(b->p, 0, L.total * es, s);
+            if (e != cudaSuccess) return e;
+        }
+        return cudaSuccess;
+    }
+    // A family the stages write in full (ArenaGuard): no zeroing, batch_guards clears the
+    // pads.  With poison set (PTL_POISON_ARENAS=1 in the environment) its bytes are filled
+    // with 0xA5 first, so a stage that read an element before writing it would show.
+    bool poison = false;
+    cudaError_t family_written(const Layout& L, std::initializer_list<DBuf*> bufs, size_t es) {
+        for (DBuf* b : bufs) {
+            cudaError_t e = b->ensure(L.total * es);
+            if (e == cudaSuccess && poison) e = cudaMemsetAsync(b->p, 0xA5, L.total * es, s);
             if (e != cudaSuccess) return e;
         }
         return cudaSuccess;
@@ -283,10 +295,14 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
     if (!trees) return PTL_BAD_ARGUMENT;
     if (count > (1u << 24)) return PTL_BAD_ARGUMENT;
     BP_CU(cudaSetDevice(device));
+    {
+        const char* pz = std::getenv("PTL_POISON_ARENAS");
+        poison = pz && pz[0] == '1';
+    }
     B = count;
     active.assign(B, 1);
     status.assign(B, PTL_OK);
-    std::vector<uint64_t> n(B), nb8(B), n3(B), md1(B);
+    std::vector<uint64_t> n(B), nb8(B), n3(B);
     uint64_t ntot = 0;
     for (size_t p = 0; p < B; ++p) {
         const ptl_ast_view& t = trees[p];
@@ -300,7 +316,6 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
         n[p] = t.n;
         nb8[p] = r8(t.n);
         n3[p] = 3 * t.n;
-        md1[p] = t.max_depth + 1;
         ntot += t.n;
     }
     for (auto& e : ev)
@@ -310,7 +325,7 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
     for (auto& x : hns) x = 0;
 
     // ---- small per-program state and the pinned small area
-    constexpr int kTables = 20, kLists = 4;  // table slots 0..17 are used
+    constexpr int kTables = 22, kLists = 4;  // table slots 0..21 are used
     small_progs_off = static_cast<size_t>(kTables) * (B + 1) * 4;
     small_meta_off = small_progs_off + B * sizeof(Prog);
     small_err_off = small_meta_off + B * 16;
@@ -458,14 +473,13 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
         BP_CU(cudaEventRecord(ev[0], s));  // stage times start with the inputs on the device
 
         // node, register and depth families
-        Layout Ln, Lr, Ls;
+        Layout Ln, Lr;
         Ln.build(nb8, active);
         Lr.build(n3, active);
-        Ls.build(md1, active);
-        BP_CU(family(Ln, {&nt, &rt, &nd1, &nd, &par, &ci, &dep, &sizes, &loc0, &loc, &pos, &decl}, 4));
-        BP_CU(family(Ln, {&fflag}, 1));
+        BP_CU(family_written(Ln, {&nt, &rt, &nd1, &nd, &par, &ci, &dep, &loc0, &loc}, 4));
+        BP_CU(family_written(Ln, {&fflag}, 1));
+        BP_CU(family(Ln, {&pos, &decl}, 4));
         BP_CU(family(Lr, {&regs}, 4));
-        BP_CU(family(Ls, {&seen}, 4));
         hp.assign(B, Prog{});
         for (size_t p = 0; p < B; ++p) {
             Prog& P = hp[p];
@@ -486,7 +500,6 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
             P.par = par.at<int32_t>(e);
             P.ci = ci.at<int32_t>(e);
             P.dep = dep.at<int32_t>(e);
-            P.sizes = sizes.at<uint32_t>(e);
             P.loc0 = loc0.at<uint32_t>(e);
             P.loc = loc.at<uint32_t>(e);
             P.pos = pos.at<uint32_t>(e);
@@ -499,37 +512,28 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
         }
         upload_progs();
 
-        // ---- input checks
-        std::vector<uint64_t> soff(B);
-        for (size_t p = 0; p < B; ++p) soff[p] = Ls.elem(p);
-        BP_CU(seen_off.ensure(B * 8));
-        uint64_t* up_soff = reinterpret_cast<uint64_t*>(h_small.at<uint8_t>(small_up_off));
-        std::copy(soff.begin(), soff.end(), up_soff);
-        BP_CU(cudaMemcpyAsync(seen_off.p, up_soff, B * 8, cudaMemcpyHostToDevice, s));
-        const uint32_t t_n = tiles(0, n, elem_tile);
-        batch_stage(BatchStage::Validate, bl(0), t_n, nullptr, nullptr, nullptr);
-        batch_stage(BatchStage::DepthSeen, bl(0), t_n, nullptr, seen.at<uint32_t>(), seen_off.at<uint64_t>());
-        BP_CU(collect_errors());
+        // ---- input checks and copy, one pass; then preprocess on the valid programs
         {
-            std::vector<uint32_t> hs(Ls.total);
-            BP_CU(cudaMemcpyAsync(hs.data(), seen.p, Ls.total * 4, cudaMemcpyDeviceToHost, s));
-            BP_CU(cudaStreamSynchronize(s));
+            std::vector<uint64_t> gc(B);
+            for (size_t p = 0; p < B; ++p) gc[p] = region(nb8[p]) - nb8[p];
+            const uint32_t t_g = tiles(0, gc, elem_tile);
+            batch_guards(ArenaGuard::Nodes, bl(0), t_g);
+        }
+        const uint32_t t_in = tiles(8, nb8, elem_tile);
+        batch_stage(BatchStage::Ingest, bl(8), t_in, nullptr);
+        {
+            uint32_t* hfl = reinterpret_cast<uint32_t*>(h_small.at<uint8_t>(small_meta_off));
+            BP_CU(cudaMemcpyAsync(hfl, flags.p, B * 16, cudaMemcpyDeviceToHost, s));
+            BP_CU(collect_errors());
             for (size_t p = 0; p < B; ++p) {
-                if (!active[p]) continue;
-                for (uint64_t d = 0; d < md1[p]; ++d) {
-                    if (!hs[soff[p] + d]) {  // depths 0..max_depth must all be populated
-                        active[p] = 0;
-                        status[p] = PTL_INVALID_AST;
-                        break;
-                    }
+                if (active[p] && !hfl[4 * p + 3]) {  // depths 0..max_depth must all be populated
+                    active[p] = 0;
+                    status[p] = PTL_INVALID_AST;
                 }
             }
         }
-
-        // ---- preprocess
         const uint32_t t_nb8 = tiles(1, nb8, elem_tile);
-        batch_stage(BatchStage::Translate, bl(1), t_nb8, nullptr, nullptr, nullptr);
-        batch_stage(BatchStage::Preprocess, bl(1), t_nb8, nullptr, nullptr, nullptr);
+        batch_stage(BatchStage::Preprocess, bl(1), t_nb8, nullptr);
         BP_CU(cudaEventRecord(ev[1], s));
 
         // ---- isn_cnt
@@ -538,7 +542,7 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
         BP_CU(scan_counter.ensure(16));
         ScanScratch sc{scan_status.at<unsigned long long>(), scan_counter.at<uint32_t>(), st_nb8 + 8};
         batch_scan(BatchScan::Count, bl(2), st_nb8, sc, nullptr);
-        batch_stage(BatchStage::Fix, bl(1), t_nb8, nullptr, nullptr, nullptr);
+        batch_stage(BatchStage::Fix, bl(1), t_nb8, nullptr);
         batch_scan(BatchScan::Decl, bl(2), st_nb8, sc, meta.at<uint32_t>());
         uint32_t* hm = read_meta();
         BP_CU(collect_errors());
@@ -573,7 +577,7 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
         }
         upload_progs();
         const uint32_t t_fb8 = tiles(3, fb8, elem_tile);
-        batch_stage(BatchStage::Functab, bl(3), t_fb8, meta.at<uint32_t>(), nullptr, nullptr);
+        batch_stage(BatchStage::Functab, bl(3), t_fb8, meta.at<uint32_t>());
         hm = read_meta();
         BP_CU(collect_errors());
         std::vector<uint64_t> W(B), wb8(B), S(B), trig(B);
@@ -594,7 +598,8 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
         // ---- isn_gen: depth order of every program in one introsort run, then the writes
         Layout Lw;
         Lw.build(wb8, active);
-        BP_CU(family(Lw, {&instr, &rd, &rs1, &rs2, &jt, &used_instrs, &symreg, &symswp, &stamp, &spill, &roffs}, 4));
+        BP_CU(family(Lw, {&instr, &rd, &rs1, &rs2, &jt, &symreg, &symswp, &stamp}, 4));
+        BP_CU(family_written(Lw, {&used_instrs, &spill, &roffs}, 4));
         BP_CU(family(Lw, {&owner}, 8));
         BP_CU(family(Lw, {&used, &smark, &defpos}, 1));
         for (size_t p = 0; p < B; ++p) {
@@ -620,6 +625,12 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
             P.defpos = defpos.at<uint8_t>(e);
         }
         upload_progs();
+        {
+            std::vector<uint64_t> gc(B);
+            for (size_t p = 0; p < B; ++p) gc[p] = region(wb8[p]) - W[p];
+            const uint32_t t_g = tiles(20, gc, elem_tile);
+            batch_guards(ArenaGuard::Words, bl(20), t_g);
+        }
         // sort scratch over all active programs' nodes
         std::vector<uint64_t> aoff(B);
         uint64_t at = 0, seg_cap = 16, tile_cap = 16, leaf_cap = 16;
@@ -715,7 +726,7 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
         BP_CU(run_sort_rounds(ss, static_cast<uint32_t>(segs.size()), min_lg > lb ? min_lg - lb : 1, 2 * max_lg + 4,
                               sort_err.at<ErrorWord>(), s, &rounds, &sort_graph));
         batch_sort_keys(bl(4), t_n2, sa.at<unsigned long long>(), a_off.at<uint64_t>(), true);
-        batch_stage(BatchStage::Gen, bl(4), t_n2, nullptr, nullptr, nullptr);
+        batch_stage(BatchStage::Gen, bl(4), t_n2, nullptr);
         {
             ErrorWord se{};
             BP_CU(cudaMemcpyAsync(&se, sort_err.p, sizeof(se), cudaMemcpyDeviceToHost, s));
@@ -728,7 +739,7 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
         const uint32_t t_wb8 = tiles(5, wb8, elem_tile);
         BP_CU(cudaMemsetAsync(changed.p, 0, 8, s));
         // the marks, and whether some virtual result is not its instruction's own word
-        batch_stage(BatchStage::OptMark, bl(5), t_wb8, changed.at<uint32_t>(1), nullptr, nullptr);
+        batch_stage(BatchStage::OptMark, bl(5), t_wb8, changed.at<uint32_t>(1));
         uint32_t* hflag = reinterpret_cast<uint32_t*>(h_small.at<uint8_t>(small_meta_off));  // B*16 >= 8
         // sweeps after the first revisit only the tiles whose marks changed (when every
         // virtual result is its instruction's own word; else every tile, every sweep);
@@ -755,13 +766,13 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
             if (!*hflag) break;
             if (sweeps > 64u + 4u * static_cast<uint32_t>(*std::max_element(W.begin(), W.end()))) break;
         }
-        batch_stage(BatchStage::OptFinal, bl(5), t_wb8, nullptr, nullptr, nullptr);
+        batch_stage(BatchStage::OptFinal, bl(5), t_wb8, nullptr);
         BP_CU(collect_errors());
         BP_CU(cudaEventRecord(ev[4], s));
 
         // ---- regalloc
         const uint32_t t_f = tiles(6, F, elem_tile);
-        batch_stage(BatchStage::InitLifetime, bl(6), t_f, nullptr, nullptr, nullptr);
+        batch_stage(BatchStage::InitLifetime, bl(6), t_f, nullptr);
         Layout Lt, Lc;
         Lt.build(trig, active);
         std::vector<uint64_t> chunk_words(B);
@@ -779,7 +790,7 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
         }
         upload_progs();
         const uint32_t t_w = tiles(7, W, elem_tile);
-        batch_stage(BatchStage::Cross, bl(7), t_w, nullptr, nullptr, nullptr);
+        batch_stage(BatchStage::Cross, bl(7), t_w, nullptr);
         uint32_t* hfl = reinterpret_cast<uint32_t*>(h_small.at<uint8_t>(small_meta_off));
         BP_CU(cudaMemcpyAsync(hfl, flags.p, B * 16, cudaMemcpyDeviceToHost, s));
         BP_CU(collect_errors());
@@ -820,13 +831,13 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
         BP_CU(ra_sync.ensure(64));
         // per program: histogram of the independent functions' last chunks, then counts
         const uint32_t t_hist = tiles(16, nfree, elem_tile, &lane0);
-        batch_stage(BatchStage::RaHist, bl(16), t_hist, nullptr, nullptr, nullptr);
+        batch_stage(BatchStage::RaHist, bl(16), t_hist, nullptr);
         BP_CU(batch_regalloc(progs.at<Prog>(), dtable_slot(8), d_lane0, static_cast<uint32_t>(lane0_list.size()),
                              ra_items, max_g0, ra_sync.at<uint32_t>(), s, ra_share));
         const uint32_t* d_serial = upload_list(1, serial_list);
         batch_serial(progs.at<Prog>(), d_serial, static_cast<uint32_t>(serial_list.size()), s);
         const uint32_t t_w_sp = tiles(13, W, elem_tile);
-        batch_stage(BatchStage::Spill, bl(13), t_w_sp, nullptr, nullptr, nullptr);
+        batch_stage(BatchStage::Spill, bl(13), t_w_sp, nullptr);
         const uint32_t st_wb8 = tiles(9, wb8, batch_scan_tile());
         BP_CU(scan_status.ensure((static_cast<size_t>(st_wb8) + 8) * 8));
         sc = ScanScratch{scan_status.at<unsigned long long>(), scan_counter.at<uint32_t>(), st_wb8 + 8};
@@ -844,7 +855,8 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
         }
         Layout L2;
         L2.build(w2r, active);
-        BP_CU(family(L2, {&ni, &nrd, &nr1, &nr2, &njt, &fsz, &joffs}, 4));
+        BP_CU(family(L2, {&ni, &nrd, &nr1, &nr2, &njt}, 4));
+        BP_CU(family_written(L2, {&joffs}, 4));
         for (size_t p = 0; p < B; ++p) {
             Prog& P = hp[p];
             P.W2 = static_cast<uint32_t>(W2[p]);
@@ -855,14 +867,19 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
             P.nr1 = nr1.at<uint32_t>(e);
             P.nr2 = nr2.at<uint32_t>(e);
             P.njt = njt.at<uint32_t>(e);
-            P.fsz = fsz.at<uint32_t>(e);
             P.joffs = joffs.at<uint32_t>(e);
         }
         upload_progs();
+        {
+            std::vector<uint64_t> gc(B);
+            for (size_t p = 0; p < B; ++p) gc[p] = region(w2r[p]) - w2b8[p];
+            const uint32_t t_g = tiles(21, gc, elem_tile);
+            batch_guards(ArenaGuard::Words2, bl(21), t_g);
+        }
         const uint32_t t_wb8_sc = tiles(14, wb8, elem_tile);
-        batch_stage(BatchStage::Scatter, bl(14), t_wb8_sc, nullptr, nullptr, nullptr);
+        batch_stage(BatchStage::Scatter, bl(14), t_wb8_sc, nullptr);
         const uint32_t t_f2 = tiles(10, F, elem_tile);
-        batch_stage(BatchStage::RaFunctab, bl(10), t_f2, nullptr, nullptr, nullptr);
+        batch_stage(BatchStage::RaFunctab, bl(10), t_f2, nullptr);
         BP_CU(cudaEventRecord(ev[5], s));
 
         // ---- fix_jumps (+ postprocess)
@@ -885,16 +902,16 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
         }
         Layout Lo;
         Lo.build(w3r, active);
-        BP_CU(family(Lo, {&out}, 4));
+        BP_CU(family_written(Lo, {&out}, 4));  // fix_jumps writes words [0, W3); only those are read
         for (size_t p = 0; p < B; ++p) {
             hp[p].W3 = static_cast<uint32_t>(W3[p]);
             hp[p].out = out.at<uint32_t>(Lo.elem(p));
         }
         upload_progs();
         const uint32_t t_w2 = tiles(12, W2, elem_tile);
-        batch_stage(BatchStage::FjEmit, bl(12), t_w2, nullptr, nullptr, nullptr);
+        batch_stage(BatchStage::FjEmit, bl(12), t_w2, nullptr);
         const uint32_t t_f3 = tiles(15, F, elem_tile);
-        batch_stage(BatchStage::FjFunctab, bl(15), t_f3, nullptr, nullptr, nullptr);
+        batch_stage(BatchStage::FjFunctab, bl(15), t_f3, nullptr);
         BP_CU(cudaEventRecord(ev[6], s));
         BP_CU(cudaEventRecord(ev[7], s));
 

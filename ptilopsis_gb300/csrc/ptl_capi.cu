@@ -63,38 +63,10 @@ inline size_t r8(size_t n) { return (n + 7) & ~size_t(7); }
 
 }  // namespace
 
-// Input checks: the DepthTree contract (post-order, one root, consistent depths).
-__global__ void k_validate(const uint8_t* type, const uint8_t* rtype, const int32_t* parent,
-                           const int32_t* depth, const int32_t* child, uint32_t n, uint32_t max_depth,
-                           ErrorWord* err) {
-    for (uint64_t k = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x; k < n;
-         k += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
-        const uint32_t i = static_cast<uint32_t>(k);
-        bool bad = type[i] >= kNumPareasTypes || rtype[i] > 5;
-        const int32_t p = parent[i];
-        if (i == n - 1) {
-            bad |= p != -1 || depth[i] != 0;
-        } else {
-            bad |= p <= static_cast<int32_t>(i) || p >= static_cast<int32_t>(n) || child[i] < 0;
-            if (!bad) bad |= depth[i] != depth[p] + 1;
-        }
-        bad |= depth[i] < 0 || static_cast<uint32_t>(depth[i]) > max_depth;
-        if (bad) record_error(err, ST_INVALID_AST, 0, i);
-    }
-}
-
 __global__ void k_init_lifetime(unsigned long long* lt, uint32_t F) {
     for (uint64_t k = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x; k < F;
          k += static_cast<uint64_t>(gridDim.x) * blockDim.x)
         lt[k] = 0x1Full;
-}
-
-__global__ void k_depth_seen(const int32_t* depth, uint32_t n, uint32_t max_depth, uint32_t* seen) {
-    for (uint64_t k = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x; k < n;
-         k += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
-        const int32_t d = depth[k];
-        if (d >= 0 && static_cast<uint32_t>(d) <= max_depth) seen[d] = 1;  // others fail validation
-    }
 }
 
 }  // namespace ptl
@@ -118,7 +90,7 @@ struct ptl_generator {
     DevBuf ni, nrd, nr1, nr2, njt, fsz, joffs, out;
     DevBuf sort_a, sort_apos, sort_bpos, sort_seg0, sort_seg1, sort_tile_seg, sort_tile_l, sort_tile_r,
         sort_leaf, sort_heap, sort_counters, sort_local, sort_equal;
-    DevBuf scan_status, scan_counter, meta, flags, errw, tables, depth_seen;
+    DevBuf scan_status, scan_counter, meta, flags, errw, tables;
 
     // results
     uint32_t F = 0, W = 0, W2 = 0, W3 = 0, S = 0;
@@ -141,7 +113,7 @@ struct ptl_generator {
                 &stamp, &defpos, &lifetime, &trig_min, &trig_max, &ra_chunks, &spill, &roffs, &ni, &nrd, &nr1, &nr2, &njt,
                 &fsz, &joffs, &out, &sort_a, &sort_apos, &sort_bpos, &sort_seg0, &sort_seg1,
                 &sort_tile_seg, &sort_tile_l, &sort_tile_r, &sort_leaf, &sort_heap, &sort_counters, &sort_local, &sort_equal,
-                &scan_status, &scan_counter, &meta, &flags, &errw, &tables, &depth_seen};
+                &scan_status, &scan_counter, &meta, &flags, &errw, &tables};
     }
 };
 
@@ -317,8 +289,6 @@ ptl_status run_pipeline(ptl_generator* g, bool profile, bool to_host, bool row0_
     PTL_CU(g->decl.zero(s));
     PTL_CU(g->regs.ensure(3 * n, 4));
     PTL_CU(g->regs.zero(s));
-    PTL_CU(g->depth_seen.ensure(g->max_depth + 1, 4));
-    PTL_CU(g->depth_seen.zero(s));
     PTL_CU(g->scan_counter.ensure(1, 4));
     // Tile-status scratch for a scan over `count` elements (grows with the word counts).
     auto scan_for = [&](size_t count, ScanScratch* sc) -> cudaError_t {
@@ -335,27 +305,16 @@ ptl_status run_pipeline(ptl_generator* g, bool profile, bool to_host, bool row0_
     g->F = g->W = g->W2 = g->W3 = g->S = 0;
     Prog P = make_prog(g);
 
-    // ---- input checks
-    note_launch();
-    k_validate<<<std::min<size_t>((n + 255) / 256, 152 * 16), 256, 0, s>>>(
-        P.in_type, P.in_rtype, P.in_parent, P.in_depth, P.in_child, P.n, P.max_depth, P.err);
-    note_launch();
-    k_depth_seen<<<std::min<size_t>((n + 255) / 256, 152 * 16), 256, 0, s>>>(P.in_depth, P.n, P.max_depth,
-                                                                             g->depth_seen.at<uint32_t>());
-    if (ptl_status st = check_error_word(g); st != PTL_OK) return st;
-    {
-        std::vector<uint32_t> seen(g->max_depth + 1);
-        PTL_CU(cudaMemcpyAsync(seen.data(), g->depth_seen.at<uint32_t>(), seen.size() * 4, cudaMemcpyDeviceToHost, s));
-        PTL_CU(cudaStreamSynchronize(s));
-        for (uint32_t v : seen) {
-            if (!v) return fail(g, PTL_INVALID_AST, "input: depths 0..max_depth are not all populated");
-        }
-    }
-
-    // ---- preprocess
+    // ---- input checks and copy, one pass; then preprocess
     if (!prog_ready(P, {P.nt, P.rt, P.nd1, P.nd, P.par, P.ci, P.dep, P.fflag, P.sizes, P.loc0, P.loc, P.decl}))
         return fail(g, PTL_CUDA_ERROR, "internal: unallocated node arrays");
-    launch_translate(P, s);
+    launch_ingest(P, s);
+    {
+        uint32_t reach = 0;  // some node sits at max_depth (read with the error word's sync)
+        PTL_CU(cudaMemcpyAsync(&reach, P.flags + 3, sizeof(reach), cudaMemcpyDeviceToHost, s));
+        if (ptl_status st = check_error_word(g); st != PTL_OK) return st;
+        if (!reach) return fail(g, PTL_INVALID_AST, "input: depths 0..max_depth are not all populated");
+    }
     launch_preprocess(P, s);
     timer.mark();
 

@@ -224,7 +224,10 @@ struct Model {
         P = Prog{};
         P.n = n; P.nb8 = nb8; P.max_depth = static_cast<uint32_t>(max_depth);
         bind();
-        for (uint32_t i = 0; i < nb8; ++i) st_translate(P, i);
+        bool reach = false;
+        for (uint32_t i = 0; i < nb8; ++i) reach |= st_ingest(P, i);
+        if (!check()) return err.code;
+        if (!reach) return ST_INVALID_AST;
         for (uint32_t i = 0; i < nb8; ++i) st_pre_args(P, i);
         for (uint32_t i = 0; i < nb8; ++i) st_pre_lists(P, i);
         for (uint32_t i = 0; i < nb8; ++i) st_pre_float(P, i);

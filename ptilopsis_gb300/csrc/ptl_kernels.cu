@@ -57,7 +57,9 @@ inline unsigned grid_for(uint64_t n, int threads = kThreads) {
         if (const uint32_t i = static_cast<uint32_t>(i##_); true)
 
 // ------------------------------------------------------------------ element-wise stages
-__global__ void k_translate(Prog P) { PTL_FOR(i, P.nb8) st_translate(P, i); }
+__global__ void k_ingest(Prog P) {
+    PTL_FOR(i, P.nb8) if (st_ingest(P, i)) P.flags[3] = 1u;
+}
 __global__ void k_pre_args(Prog P) { PTL_FOR(i, P.nb8) st_pre_args(P, i); }
 __global__ void k_pre_lists(Prog P) { PTL_FOR(i, P.nb8) st_pre_lists(P, i); }
 __global__ void k_pre_float(Prog P) { PTL_FOR(i, P.nb8) st_pre_float(P, i); }
@@ -1269,9 +1271,9 @@ uint64_t launch_count() { return g_launches.load(); }
 void note_launch() { g_launches++; }
 
 // ====================================================================== launchers
-void launch_translate(const Prog& P, cudaStream_t s) {
+void launch_ingest(const Prog& P, cudaStream_t s) {
     g_launches++;
-    k_translate<<<grid_for(P.nb8), kThreads, 0, s>>>(P);
+    k_ingest<<<grid_for(P.nb8), kThreads, 0, s>>>(P);
 }
 
 void launch_preprocess(const Prog& P, cudaStream_t s) {
@@ -1648,8 +1650,7 @@ __global__ void __launch_bounds__(kThreads) k_batch(const Prog* progs, const uin
         __device__ void operator()(const Prog& P, uint32_t i, uint32_t p) const { BODY; }      \
     };
 
-PTL_BATCH_OP(BValidate, P.n, if (st_input_bad(P, i)) record_error(P.err, ST_INVALID_AST, 0, i))
-PTL_BATCH_OP(BTranslate, P.nb8, st_translate(P, i))
+PTL_BATCH_OP(BIngest, P.nb8, if (st_ingest(P, i)) P.flags[3] = 1u)
 PTL_BATCH_OP(BPreArgs, P.nb8, st_pre_args(P, i))
 PTL_BATCH_OP(BPreLists, P.nb8, st_pre_lists(P, i))
 PTL_BATCH_OP(BPreFloat, P.nb8, st_pre_float(P, i))
@@ -1660,6 +1661,33 @@ PTL_BATCH_OP(BFunctab, P.fb8, st_functab(P, i))
 PTL_BATCH_OP(BGenProp, P.n, st_gen_prop(P, i))
 PTL_BATCH_OP(BGenClaim, P.n, st_gen_claim(P, i))
 PTL_BATCH_OP(BGenWrite, P.n, st_gen_write(P, i))
+// Pads of the families the stages write in full (ArenaGuard): guard element j of a
+// program is j - kArenaFront before its first element, then written + (j - kArenaFront).
+__device__ __forceinline__ int64_t guard_index(uint32_t j, uint32_t written) {
+    return j < kArenaFront ? static_cast<int64_t>(j) - static_cast<int64_t>(kArenaFront)
+                           : static_cast<int64_t>(written) + static_cast<int64_t>(j - kArenaFront);
+}
+struct BGuardNodes {
+    __device__ static uint32_t count(const Prog& P) { return static_cast<uint32_t>(arena_region(P.nb8) - P.nb8); }
+    __device__ void operator()(const Prog& P, uint32_t j, uint32_t) const {
+        const int64_t x = guard_index(j, P.nb8);
+        P.nt[x] = 0; P.rt[x] = 0; P.nd1[x] = 0; P.nd[x] = 0; P.par[x] = 0; P.ci[x] = 0; P.dep[x] = 0;
+        P.loc0[x] = 0; P.loc[x] = 0; P.fflag[x] = 0;
+    }
+};
+struct BGuardWords {
+    __device__ static uint32_t count(const Prog& P) { return static_cast<uint32_t>(arena_region(P.wb8) - P.W); }
+    __device__ void operator()(const Prog& P, uint32_t j, uint32_t) const {
+        const int64_t x = guard_index(j, P.W);
+        P.used_instrs[x] = 0; P.spill[x] = 0; P.roffs[x] = 0;
+    }
+};
+struct BGuardWords2 {
+    __device__ static uint32_t count(const Prog& P) {
+        return static_cast<uint32_t>(arena_region(P.w2b8 + 16u) - P.w2b8);
+    }
+    __device__ void operator()(const Prog& P, uint32_t j, uint32_t) const { P.joffs[guard_index(j, P.w2b8)] = 0; }
+};
 // marks, and odd = 1 when some virtual result is not its instruction's own word (what
 // the optimize sweeps' worklist needs to know)
 struct BOptMark {
@@ -1704,16 +1732,6 @@ struct BCross {
     }
 };
 
-// per program: depths seen (seen + soff[p], max_depth + 1 entries)
-struct BDepthSeen {
-    uint32_t* seen;
-    const uint64_t* soff;
-    __device__ static uint32_t count(const Prog& P) { return P.n; }
-    __device__ void operator()(const Prog& P, uint32_t i, uint32_t p) const {
-        const int32_t d = P.in_depth[i];
-        if (d >= 0 && static_cast<uint32_t>(d) <= P.max_depth) seen[soff[p] + static_cast<uint32_t>(d)] = 1u;
-    }
-};
 // per program: word count and longest function (meta[4p + 1], meta[4p + 2])
 struct BFunctabEnd {
     uint32_t* meta;
@@ -1850,7 +1868,7 @@ __global__ void k_batch_w2(const Prog* progs, const uint32_t* list, uint32_t cou
 __global__ void k_batch_w3(const Prog* progs, const uint32_t* list, uint32_t count, uint32_t* meta) {
     PTL_FOR(k, count) {
         const Prog& P = progs[list[k]];
-        meta[4u * list[k] + 1u] = P.fsz[P.W2 - 1u] + P.joffs[P.W2 - 1u];
+        meta[4u * list[k] + 1u] = st_fj_size(P, P.W2 - 1u) + P.joffs[P.W2 - 1u];
     }
 }
 
@@ -1858,11 +1876,7 @@ __global__ void k_batch_w3(const Prog* progs, const uint32_t* list, uint32_t cou
 // back only as far as its program's first tile.
 struct BScanCount {
     __device__ static uint32_t count(const Prog& P) { return P.nb8; }
-    __device__ uint32_t load(const Prog& P, uint32_t i) const {
-        const uint32_t v = st_count(P, i);
-        P.sizes[i] = v;
-        return v;
-    }
+    __device__ uint32_t load(const Prog& P, uint32_t i) const { return st_count(P, i); }
     __device__ void store(const Prog& P, uint32_t i, uint32_t v, uint32_t) const { P.loc0[i] = v; }
 };
 struct BScanDecl {
@@ -1882,11 +1896,7 @@ struct BScanRaCount {
 };
 struct BScanFjSize {
     __device__ static uint32_t count(const Prog& P) { return P.w2b8; }
-    __device__ uint32_t load(const Prog& P, uint32_t i) const {
-        const uint32_t v = i < P.W2 ? st_fj_size(P, i) : 0u;
-        P.fsz[i] = v;
-        return v;
-    }
+    __device__ uint32_t load(const Prog& P, uint32_t i) const { return i < P.W2 ? st_fj_size(P, i) : 0u; }
     __device__ void store(const Prog& P, uint32_t i, uint32_t v, uint32_t) const { P.joffs[i] = v; }
 };
 
@@ -2032,12 +2042,17 @@ static_assert(sizeof(Prog) % 8 == 0, "Prog copies in 8-byte words");
 uint32_t batch_tile() { return kBTile; }
 uint32_t batch_scan_tile() { return kScanTile; }
 
-void batch_stage(BatchStage st, const BatchLaunch& bl, uint32_t total, uint32_t* meta, uint32_t* seen,
-                 const uint64_t* off64) {
+void batch_guards(ArenaGuard g, const BatchLaunch& bl, uint32_t total) {
+    switch (g) {
+        case ArenaGuard::Nodes: batch_launch(bl, total, BGuardNodes{}); break;
+        case ArenaGuard::Words: batch_launch(bl, total, BGuardWords{}); break;
+        case ArenaGuard::Words2: batch_launch(bl, total, BGuardWords2{}); break;
+    }
+}
+
+void batch_stage(BatchStage st, const BatchLaunch& bl, uint32_t total, uint32_t* meta) {
     switch (st) {
-        case BatchStage::Validate: batch_launch(bl, total, BValidate{}); break;
-        case BatchStage::DepthSeen: batch_launch(bl, total, BDepthSeen{seen, off64}); break;
-        case BatchStage::Translate: batch_launch(bl, total, BTranslate{}); break;
+        case BatchStage::Ingest: batch_launch(bl, total, BIngest{}); break;
         case BatchStage::Preprocess:
             batch_launch(bl, total, BPreArgs{});
             batch_launch(bl, total, BPreLists{});

@@ -42,7 +42,7 @@ uint64_t launch_count();
 void note_launch();
 
 // Element-wise stages (grid-stride launches of the per-thread functions).
-void launch_translate(const Prog& P, cudaStream_t s);
+void launch_ingest(const Prog& P, cudaStream_t s);  // input checks + copy; flags[3]: max_depth reached
 void launch_preprocess(const Prog& P, cudaStream_t s);
 void launch_count_scan(const Prog& P, const ScanScratch& sc, cudaStream_t s);
 void launch_fix(const Prog& P, cudaStream_t s);
@@ -92,7 +92,7 @@ struct BatchLaunch {
     uint32_t tile;
 };
 enum class BatchStage {
-    Validate, DepthSeen, Translate, Preprocess, Fix, Functab, Gen, OptMark, OptFinal, InitLifetime, Cross, RaHist, Spill,
+    Ingest, Preprocess, Fix, Functab, Gen, OptMark, OptFinal, InitLifetime, Cross, RaHist, Spill,
     Scatter, RaFunctab, FjEmit, FjFunctab
 };
 enum class BatchScan { Count, Decl, RaCount, FjSize };
@@ -101,8 +101,20 @@ uint32_t batch_tile();       // default elements per tile of the element-wise st
 bool batch_tile_ok(uint32_t tile);
 bool batch_sweep_tile_ok(uint32_t tile);
 uint32_t batch_scan_tile();  // elements per scan tile
-void batch_stage(BatchStage st, const BatchLaunch& bl, uint32_t total, uint32_t* meta, uint32_t* seen,
-                 const uint64_t* off64);
+void batch_stage(BatchStage st, const BatchLaunch& bl, uint32_t total, uint32_t* meta);
+
+// Batched arenas: a program's region in an array family holds kArenaFront zero elements,
+// its elements, then zeros up to the next multiple of 32 that is at least kArenaBack past
+// them (stages read a little before and past a program's elements).
+constexpr uint64_t kArenaFront = 16, kArenaBack = 80;
+PTL_HD uint64_t arena_region(uint64_t count) { return (count + kArenaFront + kArenaBack + 31) & ~uint64_t(31); }
+// Families whose elements the stages write in full before reading them; only the pads
+// need zeroing, which batch_guards does (per program, region(count) - written elements):
+//   Nodes: nt rt nd1 nd par ci dep loc0 loc fflag, written [0, nb8), count nb8;
+//   Words: used_instrs spill roffs, written from [0, W), count wb8;
+//   Words2: joffs, written [0, w2b8), count w2b8 + 16.
+enum class ArenaGuard { Nodes, Words, Words2 };
+void batch_guards(ArenaGuard g, const BatchLaunch& bl, uint32_t total);
 void batch_sort_keys(const BatchLaunch& bl, uint32_t total, unsigned long long* a, const uint64_t* aoff, bool out);
 // One optimize sweep over the tiles marked in cur (all when cur is null); marks in next
 // the tiles a cleared mark makes live again.  Valid only when the OptMark stage found

@@ -115,7 +115,7 @@ struct Prog {
     int32_t* ci;
     int32_t* dep;
     uint8_t* fflag;   // pass 3: becomes FLOAT
-    uint32_t* sizes;
+    uint32_t* sizes;  // node code sizes, kept for stage snapshots (null in a batch)
     uint32_t* loc0;   // scan result
     uint32_t* loc;    // after fix
     uint32_t* regs;   // isn_gen registers, 3 per node
@@ -142,7 +142,7 @@ struct Prog {
     // regalloc
     uint32_t* symreg;
     uint32_t* symswp;
-    uint32_t* stamp;
+    uint32_t* stamp;      // definitions per virtual register (regalloc cross check)
     uint8_t* defpos;      // row-0 position + 1 of each lane-0 definition; null: use the row-0 hash
     unsigned long long* lifetime;
     uint32_t* trig_min;   // [S][64] min group+1 of non-lane-0 triggers, 0xFFFFFFFF = none
@@ -150,7 +150,6 @@ struct Prog {
     uint32_t* ra_chunks;  // [2][S/32 + 2]: per progress chunk, independent functions ending there; chunks done
     uint32_t S;           // longest function (steps)
     uint32_t* spill;
-    uint32_t* rcount;
     uint32_t* roffs;
     uint32_t* ni;
     uint32_t* nrd;
@@ -158,46 +157,50 @@ struct Prog {
     uint32_t* nr2;
     uint32_t* njt;
     // fix_jumps
-    uint32_t* fsz;
+    uint32_t* fsz;    // word sizes, kept for the size read-back (null in a batch)
     uint32_t* joffs;
     uint32_t* out;
     // tables, errors, scratch flags
     Tab tab;
     ErrorWord* err;
-    uint32_t* flags;      // [0] optimize changed
+    uint32_t* flags;      // [0] optimize changed, [1] [2] regalloc checks, [3] a node at max_depth
 };
 
-// ================================================================== input checks
-// The DepthTree contract (post-order, one root last, consistent depths, in-range types).
-PTL_HD bool st_input_bad(const Prog& P, uint32_t i) {
-    const uint32_t n = P.n;
-    bool bad = P.in_type[i] >= kNumPareasTypes || P.in_rtype[i] > 5;
-    const int32_t p = P.in_parent[i];
-    if (i == n - 1) {
-        bad |= p != -1 || P.in_depth[i] != 0;
-    } else {
-        bad |= p <= static_cast<int32_t>(i) || p >= static_cast<int32_t>(n) || P.in_child[i] < 0;
-        if (!bad) bad |= P.in_depth[i] != P.in_depth[p] + 1;
-    }
-    bad |= P.in_depth[i] < 0 || static_cast<uint32_t>(P.in_depth[i]) > P.max_depth;
-    return bad;
-}
-
-// ================================================================== preprocess
-// Constructor copy and Pareas -> rv type map: src/codegen/rv_generator.cpp:41-67.
-PTL_HD void st_translate(const Prog& P, uint32_t i) {
-    if (i < P.n) {
-        const uint32_t ty = P.in_type[i];
-        P.nt[i] = ty < kNumPareasTypes ? P.tab.t->pareas_to_rv[ty] : 0u;
-        P.rt[i] = P.in_rtype[i];
-        P.par[i] = P.in_parent[i];
-        P.ci[i] = P.in_child[i];
-        P.nd1[i] = P.in_data[i];
-        P.dep[i] = P.in_depth[i];
-    } else {
-        P.nt[i] = 0; P.rt[i] = 0; P.par[i] = 0; P.ci[i] = 0; P.nd1[i] = 0; P.dep[i] = 0;
-    }
+// ================================================================== input checks and copy
+// One pass over the six input arrays: the DepthTree contract (post-order, one root last,
+// consistent depths, in-range types; a bad node records INVALID_AST with its index), then
+// the constructor copy and the Pareas -> rv type map (src/codegen/rv_generator.cpp:41-67);
+// lanes past n become zero.  Returns whether node i is valid and sits at max_depth: with
+// every node one level below its parent, depths 0..max_depth are all populated exactly
+// when some node reaches max_depth.
+PTL_HD bool st_ingest(const Prog& P, uint32_t i) {
     P.fflag[i] = 0;
+    if (i >= P.n) {
+        P.nt[i] = 0; P.rt[i] = 0; P.par[i] = 0; P.ci[i] = 0; P.nd1[i] = 0; P.dep[i] = 0;
+        return false;
+    }
+    const uint32_t n = P.n;
+    const uint32_t ty = P.in_type[i];
+    const uint32_t rty = P.in_rtype[i];
+    const int32_t p = P.in_parent[i];
+    const int32_t c = P.in_child[i];
+    const int32_t d = P.in_depth[i];
+    const uint32_t data = P.in_data[i];
+    bool bad = ty >= kNumPareasTypes || rty > 5 || d < 0 || static_cast<uint32_t>(d) > P.max_depth;
+    if (i == n - 1) {
+        bad |= p != -1 || d != 0;
+    } else {
+        bad |= p <= static_cast<int32_t>(i) || p >= static_cast<int32_t>(n) || c < 0;
+        if (!bad) bad |= d - 1 != P.in_depth[p];  // d >= 0 here
+    }
+    if (bad) record_error(P.err, ST_INVALID_AST, 0, i);
+    P.nt[i] = ty < kNumPareasTypes ? P.tab.t->pareas_to_rv[ty] : 0u;
+    P.rt[i] = rty;
+    P.par[i] = p;
+    P.ci[i] = c;
+    P.nd1[i] = data;
+    P.dep[i] = d;
+    return !bad && static_cast<uint32_t>(d) == P.max_depth;
 }
 
 // Function-argument registers and stack slots, rv_generator_avx.cpp:126-213.

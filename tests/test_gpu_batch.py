@@ -204,3 +204,29 @@ def test_batch_input_paths_agree(built_cuda, monkeypatch):
         b.compile(odd)
         for k in range(len(trees)):
             np.testing.assert_array_equal(b.words(k), want[k], err_msg=f"program {k}, pinned gather")
+
+
+def test_batch_poisoned_arenas(built_cuda, monkeypatch):
+    """Arrays the stages write in full are not zeroed between compiles.  With
+    PTL_POISON_ARENAS=1 their bytes are filled with 0xA5 before every compile (only the
+    pads are cleared), so a stage that read one of them before writing it would change
+    the words: every program still equals its plain compile, over two calls of different
+    sizes and an invalid program."""
+    from conftest import ast_to_tree
+    from ptilopsis_gb300.batch import BatchCompiler
+    monkeypatch.setenv("PTL_POISON_ARENAS", "1")
+    first = _programs(12, seed0=0x50544D40)
+    second = _programs(7, seed0=0x50544D60, max_fns=40)
+    bad = ast_to_tree(tree_to_ast(second[2]))
+    bad.max_depth = bad.max_depth + 1  # a depth with no node
+    second[2] = bad
+    with BatchCompiler(workers=4) as b:
+        for trees in (first, second):
+            b.compile(trees, check=False)
+            for k, t in enumerate(trees):
+                if t is bad:
+                    assert b.status(k) == 1  # INVALID_AST
+                    continue
+                assert b.status(k) == 0
+                w, tab = _alone(t)
+                _assert_same(b.result(k), w, tab, f"program {k} ({t.n} nodes)")

@@ -133,6 +133,13 @@ def test_gpu_rejects_malformed_tree(built_cuda):
         with pytest.raises(PtlError) as e:
             gen.process()
     assert e.value.status == 1
+    # a declared max_depth that no node reaches leaves a depth level empty
+    empty = ast_to_tree(tree_to_ast(tree))
+    empty.max_depth = empty.max_depth + 1
+    with RvGenerator(empty) as gen:
+        with pytest.raises(PtlError) as e:
+            gen.process()
+    assert e.value.status == 1 and "not all populated" in str(e.value)
 
 
 def test_gpu_large_program_against_oracle(built_cuda):
