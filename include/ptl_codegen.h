@@ -176,6 +176,10 @@ ptl_status ptl_batch_host_ns(const ptl_batch* batch, uint64_t ns[3]);
  * ptilopsis_gb300.batch.autotune measures the candidates and caches the choice. */
 ptl_status ptl_batch_set_tiles(ptl_batch* batch, uint32_t elem_tile, uint32_t sweep_tile);
 ptl_status ptl_batch_tiles(const ptl_batch* batch, uint32_t tiles[2]);
+/* The part (0, 1] of the device's resident blocks the persistent register-allocation
+ * launch may take (default 1).  Batches compiled at the same time on other handles of the
+ * same device run beside it when it takes less. */
+ptl_status ptl_batch_set_regalloc_share(ptl_batch* batch, double share);
 void ptl_batch_destroy(ptl_batch* batch);
 
 /* ---- Text output.  ptl_to_asm replaces rv_generator::to_asm

@@ -41,6 +41,7 @@ def _bind(L):
     L.ptl_batch_last_error.restype = ctypes.c_char_p
     L.ptl_batch_set_tiles.argtypes = [vp, ctypes.c_uint32, ctypes.c_uint32]
     L.ptl_batch_tiles.argtypes = [vp, ctypes.POINTER(ctypes.c_uint32)]
+    L.ptl_batch_set_regalloc_share.argtypes = [vp, ctypes.c_double]
     L.ptl_batch_destroy.argtypes = [vp]
     L.ptl_batch_destroy.restype = None
     L.ptl_server_create.argtypes = [ctypes.c_int, ctypes.c_int, u64, ctypes.POINTER(vp)]
@@ -60,6 +61,7 @@ def _bind(L):
     L.ptl_clock_ns.restype = u64
     for fn in ("ptl_batch_create", "ptl_batch_compile", "ptl_batch_status", "ptl_batch_words", "ptl_batch_stage_ns",
                "ptl_batch_copied_bytes", "ptl_batch_sizes", "ptl_batch_host_ns", "ptl_batch_set_tiles", "ptl_batch_tiles",
+               "ptl_batch_set_regalloc_share",
                "ptl_batch_function_table", "ptl_server_create", "ptl_server_submit", "ptl_server_submit_flags", "ptl_server_poll",
                "ptl_server_result", "ptl_server_times", "ptl_server_release", "ptl_server_stats"):
         getattr(L, fn).restype = ctypes.c_int
@@ -166,6 +168,13 @@ class BatchCompiler:
         st = self._lib.ptl_batch_set_tiles(self._h, elem_tile, sweep_tile)
         if st != 0:
             raise PtlError(st, f"ptl_batch_set_tiles({elem_tile}, {sweep_tile})")
+
+    def set_regalloc_share(self, share: float) -> None:
+        """Part of the device's resident blocks the persistent register-allocation launch
+        may take (default 1); less leaves room for batches compiled beside this one."""
+        st = self._lib.ptl_batch_set_regalloc_share(self._h, float(share))
+        if st != 0:
+            raise PtlError(st, f"ptl_batch_set_regalloc_share({share})")
 
     def tiles(self) -> tuple:
         v = (ctypes.c_uint32 * 2)()

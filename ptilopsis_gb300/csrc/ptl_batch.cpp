@@ -146,6 +146,12 @@ extern "C" ptl_status ptl_batch_set_tiles(ptl_batch* b, uint32_t elem_tile, uint
     return b->pipe->set_tiles(elem_tile, sweep_tile) ? PTL_OK : PTL_BAD_ARGUMENT;
 }
 
+extern "C" ptl_status ptl_batch_set_regalloc_share(ptl_batch* b, double share) {
+    if (!b || !(share > 0.0 && share <= 1.0)) return PTL_BAD_ARGUMENT;
+    b->pipe->set_regalloc_share(share);
+    return PTL_OK;
+}
+
 extern "C" ptl_status ptl_batch_tiles(const ptl_batch* b, uint32_t tiles[2]) {
     if (!b || !tiles) return PTL_BAD_ARGUMENT;
     b->pipe->tiles(tiles);

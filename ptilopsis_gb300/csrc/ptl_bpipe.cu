@@ -130,7 +130,7 @@ public:
     DBuf tab;  // CodeTables
     DBuf in_type, in_rtype, in_parent, in_depth, in_child, in_data;
     DBuf nt, rt, nd1, nd, par, ci, dep, loc0, loc, pos, decl, fflag, regs;
-    DBuf fn_id, fn_start, fn_size, fn_end, fn_start0, fn_size0, lifetime;
+    DBuf fn_id, fn_start, fn_size, fn_end, fn_start0, fn_size0, ra_order, lifetime;
     DBuf instr, rd, rs1, rs2, jt, used_instrs, symreg, symswp, stamp, spill, roffs, owner, used, smark, defpos;
     DBuf trig_min, trig_max, ra_chunks;
     DBuf ni, nrd, nr1, nr2, njt, joffs, out;
@@ -161,7 +161,7 @@ public:
     std::vector<DBuf*> all() {
         return {&tab, &in_type, &in_rtype, &in_parent, &in_depth, &in_child, &in_data, &nt, &rt, &nd1, &nd, &par,
                 &ci, &dep, &loc0, &loc, &pos, &decl, &fflag, &regs, &fn_id, &fn_start, &fn_size,
-                &fn_end, &fn_start0, &fn_size0, &lifetime, &instr, &rd, &rs1, &rs2, &jt, &used_instrs, &symreg,
+                &fn_end, &fn_start0, &fn_size0, &ra_order, &lifetime, &instr, &rd, &rs1, &rs2, &jt, &used_instrs, &symreg,
                 &symswp, &stamp, &spill, &roffs, &owner, &used, &smark, &defpos, &trig_min, &trig_max, &ra_chunks, &ni, &nrd,
                 &nr1, &nr2, &njt, &joffs, &out, &errw, &flags, &meta, &progs, &tabs, &lists, &changed,
                 &sort_err, &a_off, &dirty, &ra_sync, &sa, &sapos, &sbpos, &seg0, &seg1, &tile_seg, &tile_l, &tile_r,
@@ -519,8 +519,8 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
             const uint32_t t_g = tiles(0, gc, elem_tile);
             batch_guards(ArenaGuard::Nodes, bl(0), t_g);
         }
-        const uint32_t t_in = tiles(8, nb8, elem_tile);
-        batch_stage(BatchStage::Ingest, bl(8), t_in, nullptr);
+        const uint32_t t_in = tiles(19, nb8, elem_tile);
+        batch_stage(BatchStage::Ingest, bl(19), t_in, nullptr);
         {
             uint32_t* hfl = reinterpret_cast<uint32_t*>(h_small.at<uint8_t>(small_meta_off));
             BP_CU(cudaMemcpyAsync(hfl, flags.p, B * 16, cudaMemcpyDeviceToHost, s));
@@ -560,7 +560,7 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
         }
         Layout Lf;
         Lf.build(fr, active);
-        BP_CU(family(Lf, {&fn_id, &fn_start, &fn_size, &fn_end, &fn_start0, &fn_size0}, 4));
+        BP_CU(family(Lf, {&fn_id, &fn_start, &fn_size, &fn_end, &fn_start0, &fn_size0, &ra_order}, 4));
         BP_CU(family(Lf, {&lifetime}, 8));
         for (size_t p = 0; p < B; ++p) {
             Prog& P = hp[p];
@@ -573,6 +573,7 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
             P.fn_end = fn_end.at<uint32_t>(e);
             P.fn_start0 = fn_start0.at<uint32_t>(e);
             P.fn_size0 = fn_size0.at<uint32_t>(e);
+            P.ra_order = ra_order.at<uint32_t>(e);
             P.lifetime = lifetime.at<unsigned long long>(e);
         }
         upload_progs();
@@ -828,6 +829,7 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
             BP_CU(cudaMemcpyAsync(dtable_slot(8), h, (B + 1) * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
         }
         const uint32_t* d_lane0 = upload_list(0, lane0_list);
+        batch_free_order(progs.at<Prog>(), d_lane0, static_cast<uint32_t>(lane0_list.size()), s);
         BP_CU(ra_sync.ensure(64));
         // per program: histogram of the independent functions' last chunks, then counts
         const uint32_t t_hist = tiles(16, nfree, elem_tile, &lane0);

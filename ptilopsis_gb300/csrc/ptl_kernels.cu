@@ -921,6 +921,57 @@ __global__ void __launch_bounds__(kRaFreeThreads) k_ra_free_cached(Prog P) {
     if (f < P.F) ra_free_function_cached(P, c, threadIdx.x, f);
 }
 
+// The independent functions of each listed program, longest first, into ra_order: a
+// warp's lanes step together until its longest function ends, so functions of similar
+// length side by side waste few lane-steps (the functions are independent, so any order
+// gives the same result).  One block per program: a bitonic sort of (size, index) in
+// shared memory; programs with more than kOrderMax independent functions keep the
+// function order.
+constexpr uint32_t kOrderMax = 4096;
+constexpr uint32_t kOrderThreads = 256;
+__global__ void __launch_bounds__(kOrderThreads) k_free_order(const Prog* progs, const uint32_t* list,
+                                                               uint32_t count) {
+    __shared__ unsigned long long key[kOrderMax];
+    const uint32_t tid = threadIdx.x;
+    for (uint32_t k = blockIdx.x; k < count; k += gridDim.x) {
+        const Prog& P = progs[list[k]];
+        const uint32_t nfree = P.F - (P.F + 7u) / 8u;
+        if (nfree > kOrderMax) {
+            for (uint32_t x = tid; x < nfree; x += kOrderThreads) P.ra_order[x] = free_function_of(x);
+            continue;
+        }
+        uint32_t m = 1;
+        while (m < nfree) m <<= 1;
+        for (uint32_t x = tid; x < m; x += kOrderThreads) {
+            unsigned long long v = ~0ull;
+            if (x < nfree) {
+                const uint32_t size = P.fn_size0[free_function_of(x)];
+                v = (static_cast<unsigned long long>(~(s32(size) > 0 ? size : 0u)) << 32) | x;
+            }
+            key[x] = v;
+        }
+        __syncthreads();
+        for (uint32_t len = 2; len <= m; len <<= 1) {
+            for (uint32_t stride = len >> 1; stride > 0; stride >>= 1) {
+                for (uint32_t x = tid; x < m; x += kOrderThreads) {
+                    const uint32_t y = x ^ stride;
+                    if (y > x) {
+                        const unsigned long long a = key[x], b = key[y];
+                        if ((a > b) == ((x & len) == 0)) {
+                            key[x] = b;
+                            key[y] = a;
+                        }
+                    }
+                }
+                __syncthreads();
+            }
+        }
+        for (uint32_t x = tid; x < nfree; x += kOrderThreads)
+            P.ra_order[x] = free_function_of(static_cast<uint32_t>(key[x]));
+        __syncthreads();  // before the next program refills key
+    }
+}
+
 // Progress chunks: hist[x] = independent functions whose last step falls in chunk x.
 __global__ void k_ra_chunk_hist(Prog P, uint32_t nfree) {
     PTL_FOR(k, nfree) {
@@ -2013,7 +2064,9 @@ __global__ void __launch_bounds__(MAXT) k_batch_ra(BatchRa ra) {
             Pf.defpos = nullptr;  // the independent functions never need definition positions
             uint32_t* tag = reinterpret_cast<uint32_t*>(smem);
             const SymCache cf{tag, tag + T * ra.Kf, ra.Kf};
-            const uint32_t f = free_function_of(local * T + tid);
+            const uint32_t x = local * T + tid;
+            const uint32_t nfree = Pf.F - (Pf.F + 7u) / 8u;
+            const uint32_t f = x < nfree ? (Pf.ra_order ? Pf.ra_order[x] : free_function_of(x)) : Pf.F;
             const uint32_t chunks = (Pf.S + kRaChunk - 1u) / kRaChunk;
             if (f < Pf.F) ra_free_function_cached(Pf, cf, tid, f, Pf.ra_chunks + chunks);
         } else {
@@ -2124,6 +2177,12 @@ void batch_scan(BatchScan which, const BatchLaunch& bl, uint32_t tiles, const Sc
         case BatchScan::RaCount: k_bscan<<<tiles, kScanThreads, 0, bl.s>>>(bl.progs, bl.off, bl.B, BScanRaCount{}, sc); break;
         case BatchScan::FjSize: k_bscan<<<tiles, kScanThreads, 0, bl.s>>>(bl.progs, bl.off, bl.B, BScanFjSize{}, sc); break;
     }
+}
+
+void batch_free_order(const Prog* progs, const uint32_t* list, uint32_t count, cudaStream_t s) {
+    if (count == 0) return;
+    g_launches++;
+    k_free_order<<<std::min<uint32_t>(count, 152u * 8u), kOrderThreads, 0, s>>>(progs, list, count);
 }
 
 void batch_sizes(bool w3, const Prog* progs, const uint32_t* list, uint32_t count, uint32_t* meta, cudaStream_t s) {

@@ -137,6 +137,8 @@ constexpr uint32_t kGatherTile = 4096;
 void batch_gather_host(const BatchLaunch& bl, uint32_t total, const HostGather& g);
 void batch_scan(BatchScan which, const BatchLaunch& bl, uint32_t tiles, const ScanScratch& sc, uint32_t* meta);
 void batch_sizes(bool w3, const Prog* progs, const uint32_t* list, uint32_t count, uint32_t* meta, cudaStream_t s);
+// ra_order of each listed program: its independent functions, longest first.
+void batch_free_order(const Prog* progs, const uint32_t* list, uint32_t count, cudaStream_t s);
 void batch_serial(const Prog* progs, const uint32_t* list, uint32_t count, cudaStream_t s);
 // Register allocation steps of n programs in one persistent launch: program order[k]
 // owns work items item_off[k] .. item_off[k+1] (its independent functions in tiles of

@@ -148,6 +148,7 @@ struct Prog {
     uint32_t* trig_min;   // [S][64] min group+1 of non-lane-0 triggers, 0xFFFFFFFF = none
     uint32_t* trig_max;   // [S][64] max group+1, 0 = none
     uint32_t* ra_chunks;  // [2][S/32 + 2]: per progress chunk, independent functions ending there; chunks done
+    uint32_t* ra_order;   // independent functions, longest first (null: function order)
     uint32_t S;           // longest function (steps)
     uint32_t* spill;
     uint32_t* roffs;
