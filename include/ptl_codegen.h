@@ -163,6 +163,9 @@ ptl_status ptl_batch_sizes(const ptl_batch* batch, size_t k, uint64_t sizes[4]);
 uint64_t ptl_batch_elapsed_ns(const ptl_batch* batch);
 /* Device time per stage of the last compile (ptl_generator_stage_ns's seven columns). */
 ptl_status ptl_batch_stage_ns(const ptl_batch* batch, uint64_t ns[7]);
+/* Device time of the last compile from its inputs on the device to its outputs complete
+ * (before the output copy), in ns. */
+uint64_t ptl_batch_device_ns(const ptl_batch* batch);
 /* Bytes copied host-to-device and device-to-host by the last compile. */
 ptl_status ptl_batch_copied_bytes(const ptl_batch* batch, uint64_t* h2d, uint64_t* d2h);
 /* Detail of the last batch-wide failure. */

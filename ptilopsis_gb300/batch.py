@@ -42,6 +42,8 @@ def _bind(L):
     L.ptl_batch_set_tiles.argtypes = [vp, ctypes.c_uint32, ctypes.c_uint32]
     L.ptl_batch_tiles.argtypes = [vp, ctypes.POINTER(ctypes.c_uint32)]
     L.ptl_batch_set_regalloc_share.argtypes = [vp, ctypes.c_double]
+    L.ptl_batch_device_ns.argtypes = [vp]
+    L.ptl_batch_device_ns.restype = u64
     L.ptl_batch_destroy.argtypes = [vp]
     L.ptl_batch_destroy.restype = None
     L.ptl_server_create.argtypes = [ctypes.c_int, ctypes.c_int, u64, ctypes.POINTER(vp)]
@@ -201,6 +203,11 @@ class BatchCompiler:
         ns = (ctypes.c_uint64 * 7)()
         self._lib.ptl_batch_stage_ns(self._h, ns)
         return list(ns)
+
+    def device_ns(self) -> int:
+        """Device time of the last compile from its inputs on the device to its outputs
+        complete (before the output copy)."""
+        return int(self._lib.ptl_batch_device_ns(self._h))
 
     def sizes(self, k: int) -> dict:
         """Program k's nodes and word counts after isn_gen, regalloc and fix_jumps."""

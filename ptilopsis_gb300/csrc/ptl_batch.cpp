@@ -127,6 +127,8 @@ extern "C" ptl_status ptl_batch_stage_ns(const ptl_batch* b, uint64_t ns[7]) {
     return PTL_OK;
 }
 
+extern "C" uint64_t ptl_batch_device_ns(const ptl_batch* b) { return b ? b->pipe->device_ns() : 0; }
+
 extern "C" ptl_status ptl_batch_copied_bytes(const ptl_batch* b, uint64_t* h2d, uint64_t* d2h) {
     if (!b) return PTL_BAD_ARGUMENT;
     b->pipe->copied_bytes(h2d, d2h);

@@ -284,6 +284,10 @@ public:
     }
 
     ptl_status compile(const ptl_ast_view* trees, size_t count, std::vector<BatchResult>& res) override;
+    uint64_t device_ns() const override {
+        float ms = 0;
+        return cudaEventElapsedTime(&ms, ev[0], ev[7]) == cudaSuccess ? static_cast<uint64_t>(ms * 1e6) : 0;
+    }
 };
 
 ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vector<BatchResult>& res) {

@@ -32,6 +32,9 @@ public:
     virtual ptl_status compile(const ptl_ast_view* trees, size_t count, std::vector<BatchResult>& out) = 0;
     // Device time of the last compile per stage (the reference's seven CSV columns), ns.
     virtual void stage_ns(uint64_t ns[7]) const = 0;
+    // Device time of the last compile from its inputs on the device to its outputs
+    // complete (before the output copy), ns.
+    virtual uint64_t device_ns() const = 0;
     // Host-to-device and device-to-host bytes of the last compile.
     virtual void copied_bytes(uint64_t* h2d, uint64_t* d2h) const = 0;
     // Host-side parts of the last compile, ns: gathering the inputs into pinned memory,

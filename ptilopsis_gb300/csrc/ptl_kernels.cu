@@ -1888,7 +1888,10 @@ __global__ void __launch_bounds__(kThreads) k_batch_sweep(const Prog* progs, con
 
 // Input gather from host memory: a tile is kGatherTile elements of one program; 16-byte
 // moves when the host array is 16-byte aligned (the device side always is), bytes
-// otherwise.
+// otherwise.  Each thread has kGatherDepth reads in flight, so a grid of two blocks per
+// SM covers the host link's latency and leaves the SMs to kernels of another stream (a
+// batch's second half copies its inputs under the first half's stages).
+constexpr int kGatherDepth = 8;
 __global__ void __launch_bounds__(kThreads) k_gather_host(HostGather g, const uint32_t* off, uint32_t B,
                                                           uint32_t total) {
     for (uint32_t t = blockIdx.x; t < total; t += gridDim.x) {
@@ -1901,8 +1904,21 @@ __global__ void __launch_bounds__(kThreads) k_gather_host(HostGather g, const ui
         uint64_t done = 0;
         if ((reinterpret_cast<uintptr_t>(s) & 15u) == 0) {
             const uint64_t n16 = nb / 16;
-            for (uint64_t k = threadIdx.x; k < n16; k += kThreads)
-                reinterpret_cast<uint4*>(d)[k] = reinterpret_cast<const uint4*>(s)[k];
+            const uint4* s16 = reinterpret_cast<const uint4*>(s);
+            uint4* d16 = reinterpret_cast<uint4*>(d);
+            for (uint64_t base = threadIdx.x; base < n16; base += static_cast<uint64_t>(kThreads) * kGatherDepth) {
+                uint4 v[kGatherDepth];
+#pragma unroll
+                for (int u = 0; u < kGatherDepth; ++u) {
+                    const uint64_t k = base + static_cast<uint64_t>(u) * kThreads;
+                    if (k < n16) v[u] = s16[k];
+                }
+#pragma unroll
+                for (int u = 0; u < kGatherDepth; ++u) {
+                    const uint64_t k = base + static_cast<uint64_t>(u) * kThreads;
+                    if (k < n16) d16[k] = v[u];
+                }
+            }
             done = n16 * 16;
         }
         for (uint64_t k = done + threadIdx.x; k < nb; k += kThreads) d[k] = s[k];
@@ -2149,7 +2165,7 @@ void batch_sort_keys(const BatchLaunch& bl, uint32_t total, unsigned long long* 
 void batch_gather_host(const BatchLaunch& bl, uint32_t total, const HostGather& g) {
     if (total == 0) return;
     g_launches++;
-    k_gather_host<<<std::min<uint32_t>(total, 152u * 16u), kThreads, 0, bl.s>>>(g, bl.off, bl.B, total);
+    k_gather_host<<<std::min<uint32_t>(total, 152u * 2u), kThreads, 0, bl.s>>>(g, bl.off, bl.B, total);
 }
 
 bool batch_tile_ok(uint32_t tile) { return tile >= kThreads && tile <= 65536u && (tile & (tile - 1)) == 0; }

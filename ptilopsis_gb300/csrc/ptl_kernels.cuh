@@ -133,7 +133,7 @@ struct HostGather {
     uint8_t* dst;
     uint32_t esize;          // 1 or 4
 };
-constexpr uint32_t kGatherTile = 4096;
+constexpr uint32_t kGatherTile = 32768;
 void batch_gather_host(const BatchLaunch& bl, uint32_t total, const HostGather& g);
 void batch_scan(BatchScan which, const BatchLaunch& bl, uint32_t tiles, const ScanScratch& sc, uint32_t* meta);
 void batch_sizes(bool w3, const Prog* progs, const uint32_t* list, uint32_t count, uint32_t* meta, cudaStream_t s);
