@@ -185,6 +185,43 @@ ptl_status ptl_batch_tiles(const ptl_batch* batch, uint32_t tiles[2]);
 ptl_status ptl_batch_set_regalloc_share(ptl_batch* batch, double share);
 void ptl_batch_destroy(ptl_batch* batch);
 
+/* ---- AST flattening.  ptl_flatten replaces DepthTree::DepthTree(ASTNode*)
+ * (pareas-ast/src/codegen/depthtree.cpp:11-100, the pointer-tree walk at :52-100) on the
+ * GPU.  The reference walks the parser's pointer tree; a pointer tree does not cross to a
+ * device, so the input is that tree as arrays in any node order: node v's parent is
+ * parent[v] (-1 for the one root) and its place among its parent's children is
+ * child_idx[v] (0 .. children-1).  The output is the DepthTree the reference builds: the
+ * nodes in post-order (children in child_idx order before their parent), depth from the
+ * root, parents as post-order indices, the root's child index -1 (the reference's
+ * SIZE_MAX), and max_depth; order[v] (optional) receives v's post-order index.  Arrays
+ * that are not one tree with child indices 0 .. k-1 (two roots or none, a parent out of
+ * range, a child index out of range or taken twice, nodes the root does not reach) give
+ * PTL_INVALID_AST.  Inputs and outputs are host arrays unless on_device; n < 2^31. */
+typedef struct {
+    size_t n;
+    const uint8_t* type;
+    const uint8_t* rtype;
+    const int32_t* parent;
+    const int32_t* child_idx;
+    const uint32_t* data;
+    int on_device;
+} ptl_tree_view;
+
+typedef struct {
+    uint8_t* type;
+    uint8_t* rtype;
+    int32_t* parent;
+    int32_t* depth;
+    int32_t* child_idx;
+    uint32_t* data;
+    int32_t* order;    /* may be null */
+    size_t max_depth;  /* written */
+    int on_device;
+} ptl_depth_tree_out;
+
+/* stream: a cudaStream_t (null: the default stream).  Blocks until the result is ready. */
+ptl_status ptl_flatten(const ptl_tree_view* in, ptl_depth_tree_out* out, int device, void* stream);
+
 /* ---- Text output.  ptl_to_asm replaces rv_generator::to_asm
  * (src/codegen/rv_generator.cpp:121-127): one line per word, "name operands\n", as
  * rvdisasm::instruction prints it.  ptl_disassemble replaces rvdisasm::disassemble

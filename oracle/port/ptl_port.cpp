@@ -998,3 +998,74 @@ extern "C" size_t ptlport_table(int which, uint32_t* out) {
     if (out) std::memcpy(out, src, count * 4);
     return count;
 }
+
+// ---------------------------------------------------------------- AST flattening
+// DepthTree::construct (pareas-ast/src/codegen/depthtree.cpp:52-100): a depth-first walk
+// from the root that pushes a node's children last-to-first and emits a node once all
+// its children are emitted, so children come in order before their parent (post-order);
+// depth is the walk depth, the root's child index is SIZE_MAX (-1 as int32), parents are
+// rewritten to emitted indices.  Here the children come from child_idx instead of an
+// ASTNode's child vector.
+extern "C" int ptlport_flatten(size_t n, const uint8_t* type, const uint8_t* rtype, const int32_t* parent,
+                               const int32_t* child_idx, const uint32_t* data, uint8_t* o_type, uint8_t* o_rtype,
+                               int32_t* o_parent, int32_t* o_depth, int32_t* o_child, uint32_t* o_data,
+                               int32_t* order, size_t* max_depth) {
+    if (n == 0 || n >= (1ull << 31)) return PTLPORT_EINVAL;
+    std::vector<uint32_t> deg(n, 0), off(n + 1, 0);
+    int64_t root = -1;
+    for (size_t v = 0; v < n; ++v) {
+        const int32_t p = parent[v];
+        if (p == -1) {
+            if (root >= 0) return PTLPORT_EINVAL;  // two roots
+            root = static_cast<int64_t>(v);
+        } else if (p < 0 || static_cast<size_t>(p) >= n || child_idx[v] < 0) {
+            return PTLPORT_EINVAL;
+        } else {
+            ++deg[static_cast<size_t>(p)];
+        }
+    }
+    if (root < 0) return PTLPORT_EINVAL;
+    for (size_t v = 0; v < n; ++v) off[v + 1] = off[v] + deg[v];
+    std::vector<int64_t> kids(n, -1);
+    for (size_t v = 0; v < n; ++v) {
+        const int32_t p = parent[v];
+        if (p == -1) continue;
+        const uint32_t c = static_cast<uint32_t>(child_idx[v]);
+        if (c >= deg[static_cast<size_t>(p)]) return PTLPORT_EINVAL;
+        int64_t& slot = kids[off[static_cast<size_t>(p)] + c];
+        if (slot >= 0) return PTLPORT_EINVAL;  // two children with one index
+        slot = static_cast<int64_t>(v);
+    }
+    struct Frame { size_t v, depth, next; };
+    std::vector<Frame> stack;
+    stack.push_back({static_cast<size_t>(root), 0, 0});
+    std::vector<int32_t> post(n, -1);
+    size_t emitted = 0, md = 0;
+    while (!stack.empty()) {
+        Frame& f = stack.back();
+        if (f.next < deg[f.v]) {
+            const size_t c = static_cast<size_t>(kids[off[f.v] + f.next++]);
+            const size_t d = f.depth + 1;
+            stack.push_back({c, d, 0});
+            continue;
+        }
+        const size_t v = f.v, d = f.depth;
+        stack.pop_back();
+        post[v] = static_cast<int32_t>(emitted);
+        o_type[emitted] = type[v];
+        o_rtype[emitted] = rtype[v];
+        o_depth[emitted] = static_cast<int32_t>(d);
+        o_child[emitted] = static_cast<int64_t>(v) == root ? -1 : child_idx[v];
+        o_data[emitted] = data[v];
+        if (d > md) md = d;
+        ++emitted;
+    }
+    if (emitted != n) return PTLPORT_EINVAL;  // nodes the root does not reach
+    for (size_t v = 0; v < n; ++v) {
+        const int32_t p = parent[v];
+        o_parent[post[v]] = p == -1 ? -1 : post[static_cast<size_t>(p)];
+        if (order) order[v] = post[v];
+    }
+    *max_depth = md;
+    return PTLPORT_OK;
+}

@@ -72,6 +72,18 @@ void ptlport_depth_sort(const int32_t* keys, size_t n, uint32_t* perm);
  * Returns the element count (out may be NULL to query it). */
 size_t ptlport_table(int which, uint32_t* out);
 
+/* DepthTree::DepthTree(ASTNode*) (pareas-ast/src/codegen/depthtree.cpp:11-100) over a
+ * parent-pointer tree in any node order: node v's parent is parent[v] (-1 for the one
+ * root) and its place among its parent's children is child_idx[v].  Writes the DepthTree
+ * arrays in post-order (children in child_idx order before their parent), depth from the
+ * root, parents as post-order indices, the root's child_idx -1, order[v] = v's post-order
+ * index and *max_depth.  Returns PTLPORT_EINVAL when the arrays are not one tree with
+ * child indices 0..k-1 at every node. */
+int ptlport_flatten(size_t n, const uint8_t* type, const uint8_t* rtype, const int32_t* parent,
+                    const int32_t* child_idx, const uint32_t* data, uint8_t* o_type, uint8_t* o_rtype,
+                    int32_t* o_parent, int32_t* o_depth, int32_t* o_child, uint32_t* o_data, int32_t* order,
+                    size_t* max_depth);
+
 #ifdef __cplusplus
 }
 #endif

@@ -64,6 +64,9 @@ def lib():
         L.ptlport_depth_sort.argtypes = [i32p, ctypes.c_size_t, u32p]
         L.ptlport_table.argtypes = [ctypes.c_int, u32p]
         L.ptlport_table.restype = ctypes.c_size_t
+        L.ptlport_flatten.argtypes = [ctypes.c_size_t, u8p, u8p, i32p, i32p, u32p, u8p, u8p, i32p, i32p, i32p, u32p,
+                                      i32p, ctypes.POINTER(ctypes.c_size_t)]
+        L.ptlport_flatten.restype = ctypes.c_int
         _lib = L
     return _lib
 
@@ -91,6 +94,30 @@ def compile_ast(ast: Ast, snapshots: bool = False) -> RefResult:
         return out
     finally:
         L.ptlport_free_result(ctypes.byref(r))
+
+
+def flatten(type_, rtype, parent, child_idx, data):
+    """DepthTree construction (pareas-ast/src/codegen/depthtree.cpp:11-100) from a
+    parent-pointer tree in any node order: returns (Ast in post-order, order) with
+    order[v] = v's post-order index; raises PortError for arrays that are not one tree."""
+    L = lib()
+    a = [np.ascontiguousarray(type_, np.uint8), np.ascontiguousarray(rtype, np.uint8),
+         np.ascontiguousarray(parent, np.int32), np.ascontiguousarray(child_idx, np.int32),
+         np.ascontiguousarray(data, np.uint32)]
+    n = a[0].shape[0]
+    o = [np.empty(n, np.uint8), np.empty(n, np.uint8), np.empty(n, np.int32), np.empty(n, np.int32),
+         np.empty(n, np.int32), np.empty(n, np.uint32)]
+    order = np.empty(n, np.int32)
+    md = ctypes.c_size_t(0)
+    p = lambda x, t: x.ctypes.data_as(ctypes.POINTER(t))
+    u8, i32, u32 = ctypes.c_uint8, ctypes.c_int32, ctypes.c_uint32
+    rc = L.ptlport_flatten(n, p(a[0], u8), p(a[1], u8), p(a[2], i32), p(a[3], i32), p(a[4], u32),
+                           p(o[0], u8), p(o[1], u8), p(o[2], i32), p(o[3], i32), p(o[4], i32), p(o[5], u32),
+                           p(order, i32), ctypes.byref(md))
+    if rc != 0:
+        raise PortError(rc, "oracle flatten: the arrays are not one tree")
+    return Ast(type=o[0], rtype=o[1], parent=o[2], depth=o[3], child_idx=o[4], data=o[5],
+               max_depth=int(md.value)), order
 
 
 def depth_sort(keys: np.ndarray) -> np.ndarray:

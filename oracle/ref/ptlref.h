@@ -56,6 +56,13 @@ typedef struct {
     int threads_used;
 } ptlref_result;
 
+/* Build the reference's pointer tree (ASTNode, children in child_idx order) from a
+ * parent-pointer tree in any node order (parent[v] = -1 for the root) and flatten it with
+ * the reference's DepthTree constructor (pareas-ast/src/codegen/depthtree.cpp:11-100).
+ * The input must be one tree; returns 0 on success (free with ptlref_free_tree). */
+int ptlref_flatten(size_t n, const uint8_t* type, const uint8_t* rtype, const int32_t* parent,
+                   const int32_t* child_idx, const uint32_t* data, ptlref_tree* out);
+
 /* Parse a Pareas source file with the reference front end (pareas-ast) and flatten it
  * into a DepthTree.  Returns 0 on success; on failure writes a message into err. */
 int ptlref_parse_file(const char* path, ptlref_tree* out, char* err, size_t errlen);

@@ -90,7 +90,59 @@ struct borrowed_tree {
     DepthTree* get() { return reinterpret_cast<DepthTree*>(storage); }
 };
 
+void copy_tree(const DepthTree& tree, ptlref_tree* out) {
+    size_t n = tree.filledNodes();
+    out->n = n;
+    out->max_depth = tree.maxDepth();
+    out->type = static_cast<uint8_t*>(std::malloc(std::max<size_t>(1, n)));
+    out->rtype = static_cast<uint8_t*>(std::malloc(std::max<size_t>(1, n)));
+    out->parent = static_cast<int32_t*>(std::malloc(std::max<size_t>(1, n) * 4));
+    out->depth = static_cast<int32_t*>(std::malloc(std::max<size_t>(1, n) * 4));
+    out->child_idx = static_cast<int32_t*>(std::malloc(std::max<size_t>(1, n) * 4));
+    out->data = static_cast<uint32_t*>(std::malloc(std::max<size_t>(1, n) * 4));
+    std::memcpy(out->type, tree.getNodeTypes().data(), n);
+    std::memcpy(out->rtype, tree.getResultingTypes().data(), n);
+    std::memcpy(out->parent, tree.getParents().data(), n * 4);
+    std::memcpy(out->depth, tree.getDepth().data(), n * 4);
+    std::memcpy(out->child_idx, tree.getChildren().data(), n * 4);
+    std::memcpy(out->data, tree.getNodeData().data(), n * 4);
+}
+
 }  // namespace
+
+extern "C" int ptlref_flatten(size_t n, const uint8_t* type, const uint8_t* rtype, const int32_t* parent,
+                              const int32_t* child_idx, const uint32_t* data, ptlref_tree* out) {
+    // The pointer tree the reference flattens: one ASTNode per node, children in
+    // child_idx order, built leaves first (an ASTNode takes its children when made).
+    if (n == 0) return 1;
+    std::vector<std::vector<size_t>> kids(n);
+    size_t root = n;
+    for (size_t v = 0; v < n; ++v) {
+        if (parent[v] == -1) root = v;
+        else kids[static_cast<size_t>(parent[v])].push_back(v);
+    }
+    if (root == n) return 1;
+    for (auto& k : kids)
+        std::sort(k.begin(), k.end(), [&](size_t a, size_t b) { return child_idx[a] < child_idx[b]; });
+    std::vector<ASTNode*> made(n, nullptr);
+    std::vector<std::pair<size_t, size_t>> stack{{root, 0}};
+    while (!stack.empty()) {
+        auto& [v, next] = stack.back();
+        if (next < kids[v].size()) {
+            const size_t c = kids[v][next++];
+            stack.push_back({c, 0});
+            continue;
+        }
+        std::vector<ASTNode*> ch;
+        for (size_t c : kids[v]) ch.push_back(made[c]);
+        made[v] = new ASTNode(static_cast<NodeType>(type[v]), static_cast<DataType>(rtype[v]), data[v], ch);
+        stack.pop_back();
+    }
+    std::unique_ptr<ASTNode> node(made[root]);
+    DepthTree tree(node.get());
+    copy_tree(tree, out);
+    return 0;
+}
 
 extern "C" int ptlref_parse_file(const char* path, ptlref_tree* out, char* err, size_t errlen) {
     try {
@@ -105,22 +157,7 @@ extern "C" int ptlref_parse_file(const char* path, ptlref_tree* out, char* err, 
         std::unique_ptr<ASTNode> node(parser.parse());
         node->resolveType();
         DepthTree tree(node.get());
-
-        size_t n = tree.filledNodes();
-        out->n = n;
-        out->max_depth = tree.maxDepth();
-        out->type = static_cast<uint8_t*>(std::malloc(std::max<size_t>(1, n)));
-        out->rtype = static_cast<uint8_t*>(std::malloc(std::max<size_t>(1, n)));
-        out->parent = static_cast<int32_t*>(std::malloc(std::max<size_t>(1, n) * 4));
-        out->depth = static_cast<int32_t*>(std::malloc(std::max<size_t>(1, n) * 4));
-        out->child_idx = static_cast<int32_t*>(std::malloc(std::max<size_t>(1, n) * 4));
-        out->data = static_cast<uint32_t*>(std::malloc(std::max<size_t>(1, n) * 4));
-        std::memcpy(out->type, tree.getNodeTypes().data(), n);
-        std::memcpy(out->rtype, tree.getResultingTypes().data(), n);
-        std::memcpy(out->parent, tree.getParents().data(), n * 4);
-        std::memcpy(out->depth, tree.getDepth().data(), n * 4);
-        std::memcpy(out->child_idx, tree.getChildren().data(), n * 4);
-        std::memcpy(out->data, tree.getNodeData().data(), n * 4);
+        copy_tree(tree, out);
         return 0;
     } catch (const std::exception& e) {
         set_err(err, errlen, e.what());

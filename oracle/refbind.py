@@ -108,6 +108,10 @@ def lib():
                                      ctypes.c_char_p, ctypes.c_size_t]
         L.ptlref_compile.restype = ctypes.c_int
         L.ptlref_free_result.argtypes = [ctypes.POINTER(_Result)]
+        u8p, i32p, u32p = (ctypes.POINTER(ctypes.c_uint8), ctypes.POINTER(ctypes.c_int32),
+                           ctypes.POINTER(ctypes.c_uint32))
+        L.ptlref_flatten.argtypes = [ctypes.c_size_t, u8p, u8p, i32p, i32p, u32p, ctypes.POINTER(_Tree)]
+        L.ptlref_flatten.restype = ctypes.c_int
         _lib = L
     return _lib
 
@@ -125,6 +129,28 @@ def parse_file(path: str) -> Ast:
     rc = L.ptlref_parse_file(path.encode(), ctypes.byref(t), err, 1024)
     if rc != 0:
         raise RuntimeError(f"reference front end failed on {path}: {err.value.decode()}")
+    try:
+        return Ast(type=_np(t.type, t.n, np.uint8), rtype=_np(t.rtype, t.n, np.uint8),
+                   parent=_np(t.parent, t.n, np.int32), depth=_np(t.depth, t.n, np.int32),
+                   child_idx=_np(t.child_idx, t.n, np.int32), data=_np(t.data, t.n, np.uint32),
+                   max_depth=int(t.max_depth))
+    finally:
+        L.ptlref_free_tree(ctypes.byref(t))
+
+
+def flatten(type_, rtype, parent, child_idx, data) -> Ast:
+    """The reference's DepthTree constructor on the pointer tree (ASTNode) that a
+    parent-pointer tree in any node order describes (one tree required)."""
+    L = lib()
+    a = [np.ascontiguousarray(type_, np.uint8), np.ascontiguousarray(rtype, np.uint8),
+         np.ascontiguousarray(parent, np.int32), np.ascontiguousarray(child_idx, np.int32),
+         np.ascontiguousarray(data, np.uint32)]
+    p = lambda x, t: x.ctypes.data_as(ctypes.POINTER(t))
+    t = _Tree()
+    rc = L.ptlref_flatten(a[0].shape[0], p(a[0], ctypes.c_uint8), p(a[1], ctypes.c_uint8), p(a[2], ctypes.c_int32),
+                          p(a[3], ctypes.c_int32), p(a[4], ctypes.c_uint32), ctypes.byref(t))
+    if rc != 0:
+        raise RuntimeError("reference flatten failed")
     try:
         return Ast(type=_np(t.type, t.n, np.uint8), rtype=_np(t.rtype, t.n, np.uint8),
                    parent=_np(t.parent, t.n, np.int32), depth=_np(t.depth, t.n, np.int32),

@@ -348,3 +348,42 @@ def disassemble(words, start_addr: int = 0, func_starts=()) -> str:
     L.ptl_disassemble.restype = ctypes.c_int
     return _text(L.ptl_disassemble, w.ctypes.data, w.shape[0], start_addr, f.ctypes.data, f.shape[0])
 
+
+
+class _TreeView(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_size_t), ("type", ctypes.c_void_p), ("rtype", ctypes.c_void_p),
+                ("parent", ctypes.c_void_p), ("child_idx", ctypes.c_void_p), ("data", ctypes.c_void_p),
+                ("on_device", ctypes.c_int)]
+
+
+class _TreeOut(ctypes.Structure):
+    _fields_ = [("type", ctypes.c_void_p), ("rtype", ctypes.c_void_p), ("parent", ctypes.c_void_p),
+                ("depth", ctypes.c_void_p), ("child_idx", ctypes.c_void_p), ("data", ctypes.c_void_p),
+                ("order", ctypes.c_void_p), ("max_depth", ctypes.c_size_t), ("on_device", ctypes.c_int)]
+
+
+def flatten(type_, rtype, parent, child_idx, data, device: int = 0):
+    """The DepthTree of a parent-pointer tree given in any node order (ptl_flatten on the
+    GPU; the reference builds it from its pointer tree, pareas-ast/src/codegen/
+    depthtree.cpp:11-100).  parent[v] is -1 for the root; child_idx[v] is v's place among
+    its parent's children.  Returns (DepthTree in post-order, order) with order[v] = v's
+    post-order index; raises PtlError (INVALID_AST) for arrays that are not one tree."""
+    L = lib()
+    L.ptl_flatten.argtypes = [ctypes.POINTER(_TreeView), ctypes.POINTER(_TreeOut), ctypes.c_int, ctypes.c_void_p]
+    L.ptl_flatten.restype = ctypes.c_int
+    a = [np.ascontiguousarray(type_, np.uint8), np.ascontiguousarray(rtype, np.uint8),
+         np.ascontiguousarray(parent, np.int32), np.ascontiguousarray(child_idx, np.int32),
+         np.ascontiguousarray(data, np.uint32)]
+    n = a[0].shape[0]
+    if any(x.shape[0] != n for x in a):
+        raise ValueError("the five arrays must have one length")
+    o = [np.empty(n, np.uint8), np.empty(n, np.uint8), np.empty(n, np.int32), np.empty(n, np.int32),
+         np.empty(n, np.int32), np.empty(n, np.uint32), np.empty(n, np.int32)]
+    v = _TreeView(n, *(x.ctypes.data for x in a), 0)
+    r = _TreeOut(*(x.ctypes.data for x in o), 0, 0)
+    st = L.ptl_flatten(ctypes.byref(v), ctypes.byref(r), device, None)
+    if st != 0:
+        raise PtlError(st, "ptl_flatten: the arrays are not one tree" if st == 1 else "ptl_flatten")
+    tree = DepthTree(type=o[0], rtype=o[1], parent=o[2], depth=o[3], child_idx=o[4], data=o[5],
+                     max_depth=int(r.max_depth))
+    return tree, o[6]
