@@ -19,6 +19,8 @@ whole batch).  Prints one JSON line (rank 0):
   roofline    the dominant stage: algorithmic bytes / its event-timed duration, against
               the measured HBM copy bandwidth
   cpu_baseline  the oracle's CPU restatement on a bounded sample, on all host cores
+  flatten     AST flattening (ptl_flatten) on 16 programs given in random node order,
+              host arrays in and out, against the oracle's restatement on one core
 
 --mode single times one large program (config c1, ~4M nodes) per step instead.
 --impl reference times the oracle restatement on the host cores on a sample of the same
@@ -298,6 +300,49 @@ def run_serving(device, args):
     return out
 
 
+def run_flatten(trees, device, reps=3):
+    """AST flattening (ptl_flatten, the GPU's DepthTree construction) on the 16 largest of
+    the first 256 programs, each given in a seeded random node order, through the public
+    call with host arrays in and out; checked against the original post-order trees, and
+    the oracle's single-thread restatement timed on the same inputs."""
+    from oracle import portbind
+    from ptilopsis_gb300 import flatten
+    pick = sorted(trees[:256], key=lambda t: -t.n)[:16]
+    cases = []
+    for k, t in enumerate(pick):
+        rng = np.random.default_rng(0x50544F00 + k)
+        perm = rng.permutation(t.n)
+        par = np.where(t.parent >= 0, perm[np.maximum(t.parent, 0)], -1).astype(np.int32)
+        arrs = []
+        for x in (t.type, t.rtype, par, t.child_idx, t.data):
+            y = np.empty_like(x)
+            y[perm] = x
+            arrs.append(y)
+        cases.append(arrs)
+    nodes = sum(t.n for t in pick)
+    for arrs in cases[:2]:
+        flatten(*arrs, device=device)  # warm-up
+    best, exact = None, True
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        outs = [flatten(*arrs, device=device)[0] for arrs in cases]
+        dt = time.perf_counter() - t0
+        best = dt if best is None else min(best, dt)
+    for t, o in zip(pick, outs):
+        exact &= all(np.array_equal(getattr(o, f), getattr(t, f))
+                     for f in ("type", "rtype", "parent", "depth", "child_idx", "data")) and o.max_depth == t.max_depth
+    t0 = time.perf_counter()
+    for arrs in cases:
+        portbind.flatten(*arrs)
+    cpu = time.perf_counter() - t0
+    return {"value": nodes / best, "unit": UNIT, "nodes": nodes,
+            "sample": f"16 largest of the first 256 programs, nodes in seeded random order, host arrays in and out "
+                      f"(best of {reps})",
+            "bit_exact_vs_post_order": bool(exact),
+            "cpu_baseline": {"value": nodes / cpu, "unit": UNIT, "cores": 1, "kind": "port",
+                             "sample": "the same 16 inputs, the oracle's restatement of DepthTree::construct"}}
+
+
 def run_batched(args):
     import torch
     rank, world, local = env_rank()
@@ -423,6 +468,8 @@ def run_batched(args):
         line["bit_exact_vs_plain"] = bool(same_as_plain)
         if not args.no_serving:
             line["serving"] = run_serving(local, args)
+        if not args.no_flatten:
+            line["flatten"] = run_flatten(trees, local)
         if not args.no_cpu_baseline:
             threads = os.cpu_count() or 1
             idx = cpu_sample(trees, args.cpu_nodes)
@@ -578,6 +625,7 @@ def main():
     ap.add_argument("--cpu-nodes", type=int, default=30_000_000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--no-flatten", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--tiles", type=int, nargs=2, metavar=("ELEM", "SWEEP"),
                     help="tile sizes of the batched pipeline instead of autotuning them")
