@@ -367,10 +367,14 @@ def flatten(type_, rtype, parent, child_idx, data, device: int = 0):
     GPU; the reference builds it from its pointer tree, pareas-ast/src/codegen/
     depthtree.cpp:11-100).  parent[v] is -1 for the root; child_idx[v] is v's place among
     its parent's children.  Returns (DepthTree in post-order, order) with order[v] = v's
-    post-order index; raises PtlError (INVALID_AST) for arrays that are not one tree."""
+    post-order index; raises PtlError (INVALID_AST) for arrays that are not one tree.
+    With CUDA tensors in, the result stays on their device (a DepthTree of CUDA tensors
+    that RvGenerator compiles without a host round trip)."""
     L = lib()
     L.ptl_flatten.argtypes = [ctypes.POINTER(_TreeView), ctypes.POINTER(_TreeOut), ctypes.c_int, ctypes.c_void_p]
     L.ptl_flatten.restype = ctypes.c_int
+    if getattr(type_, "is_cuda", False):
+        return _flatten_device(L, type_, rtype, parent, child_idx, data)
     a = [np.ascontiguousarray(type_, np.uint8), np.ascontiguousarray(rtype, np.uint8),
          np.ascontiguousarray(parent, np.int32), np.ascontiguousarray(child_idx, np.int32),
          np.ascontiguousarray(data, np.uint32)]
@@ -382,6 +386,28 @@ def flatten(type_, rtype, parent, child_idx, data, device: int = 0):
     v = _TreeView(n, *(x.ctypes.data for x in a), 0)
     r = _TreeOut(*(x.ctypes.data for x in o), 0, 0)
     st = L.ptl_flatten(ctypes.byref(v), ctypes.byref(r), device, None)
+    if st != 0:
+        raise PtlError(st, "ptl_flatten: the arrays are not one tree" if st == 1 else "ptl_flatten")
+    tree = DepthTree(type=o[0], rtype=o[1], parent=o[2], depth=o[3], child_idx=o[4], data=o[5],
+                     max_depth=int(r.max_depth))
+    return tree, o[6]
+
+
+def _flatten_device(L, type_, rtype, parent, child_idx, data):
+    import torch
+    dev = type_.device
+    a = [type_.to(torch.uint8).contiguous(), rtype.to(dev, torch.uint8).contiguous(),
+         parent.to(dev, torch.int32).contiguous(), child_idx.to(dev, torch.int32).contiguous(),
+         (data.view(torch.int32) if data.dtype == torch.uint32 else data.to(dev, torch.int32)).contiguous()]
+    n = int(a[0].shape[0])
+    if any(int(x.shape[0]) != n for x in a):
+        raise ValueError("the five arrays must have one length")
+    dts = (torch.uint8, torch.uint8, torch.int32, torch.int32, torch.int32, torch.int32, torch.int32)
+    o = [torch.empty(n, dtype=dt, device=dev) for dt in dts]
+    v = _TreeView(n, *(x.data_ptr() for x in a), 1)
+    r = _TreeOut(*(x.data_ptr() for x in o), 0, 1)
+    stream = torch.cuda.current_stream(dev).cuda_stream
+    st = L.ptl_flatten(ctypes.byref(v), ctypes.byref(r), dev.index or 0, ctypes.c_void_p(stream))
     if st != 0:
         raise PtlError(st, "ptl_flatten: the arrays are not one tree" if st == 1 else "ptl_flatten")
     tree = DepthTree(type=o[0], rtype=o[1], parent=o[2], depth=o[3], child_idx=o[4], data=o[5],

@@ -130,3 +130,21 @@ def test_gpu_flatten_rejects_malformed(built_cuda):
         with pytest.raises(PtlError) as e:
             flatten(*arrs)
         assert e.value.status == 1, name
+
+
+@pytest.mark.gpu
+def test_gpu_flatten_on_device_then_compile(built_cuda):
+    """Device arrays in, a device DepthTree out, compiled from device memory: the words of
+    the original tree, with no host copy of the flattened arrays."""
+    import torch
+    from ptilopsis_gb300 import RvGenerator, compile_tree, flatten
+    t = synth_tree(0x50544E50, fns=30)
+    arrs, perm = shuffled(t, 4)
+    dev = [torch.from_numpy(x.view(np.int32) if x.dtype == np.uint32 else x).cuda() for x in arrs]
+    flat, order = flatten(*dev)
+    assert flat.on_device and int(flat.max_depth) == int(t.max_depth)
+    assert_tree(flat.numpy(), t, "device flatten")
+    np.testing.assert_array_equal(order.cpu().numpy()[perm], np.arange(t.n))
+    with RvGenerator(flat) as g:
+        g.process()
+        np.testing.assert_array_equal(g.get_instructions(), compile_tree(t))
