@@ -5,7 +5,10 @@
 The reference reads Pareas source and flattens it with its front end; the GPU generator's
 boundary is the flattened tree, so <infile> is a DepthTree saved as .npz (arrays type,
 rtype, parent, depth, child_idx, data and the scalar max_depth, as save_tree writes
-them), or - for the same bytes on stdin.  Output as the reference writes it: raw 32-bit
+them), or - for the same bytes on stdin.  A file without depth and max_depth holds the
+parser's tree in any node order (parent -1 for the root, child_idx the place among the
+parent's children; save_unordered writes it): it is flattened on the GPU first
+(ptl_flatten, the reference's DepthTree construction).  Output as the reference writes it: raw 32-bit
 words (to_binary) to ./c.out, or with -S assembly text (to_asm) to <infile stem>.s; -o -
 writes to stdout.  -p prints the reference's profiling CSV (stage names, then
 nanoseconds; src/codegen/rv_generator.cpp:150-162) with the GPU's per-stage device times.
@@ -31,11 +34,25 @@ def save_tree(tree, path_or_file) -> None:
              **{f: np.ascontiguousarray(getattr(tree, f)) for f in FIELDS})
 
 
-def load_tree(path_or_file):
+UNORDERED = ("type", "rtype", "parent", "child_idx", "data")
+
+
+def save_unordered(type_, rtype, parent, child_idx, data, path_or_file) -> None:
+    """Writes a parser's tree in any node order (no depth) as the .npz the command line
+    flattens before compiling."""
+    np.savez(path_or_file, type=np.ascontiguousarray(type_, np.uint8), rtype=np.ascontiguousarray(rtype, np.uint8),
+             parent=np.ascontiguousarray(parent, np.int32), child_idx=np.ascontiguousarray(child_idx, np.int32),
+             data=np.ascontiguousarray(data, np.uint32))
+
+
+def load_tree(path_or_file, device: int = 0):
     from .codegen import DepthTree
     z = np.load(path_or_file)
     dt = {"type": np.uint8, "rtype": np.uint8, "parent": np.int32, "depth": np.int32, "child_idx": np.int32,
           "data": np.uint32}
+    if "depth" not in z.files:
+        from .codegen import flatten
+        return flatten(*(np.ascontiguousarray(z[f], dt[f]) for f in UNORDERED), device=device)[0]
     return DepthTree(max_depth=int(z["max_depth"]), **{f: np.ascontiguousarray(z[f], dt[f]) for f in FIELDS})
 
 
@@ -74,7 +91,7 @@ def main(argv: Optional[List[str]] = None) -> int:
         return 1
     else:
         src = args.infile
-    tree = load_tree(src)
+    tree = load_tree(src, device=args.device)
     outfile = args.outfile
     if outfile is None:
         outfile = (os.path.splitext(os.path.basename(args.infile))[0] + ".s") if args.asm else "c.out"

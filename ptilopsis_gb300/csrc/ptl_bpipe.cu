@@ -754,15 +754,16 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
         BP_CU(cudaMemcpyAsync(hflag + 1, changed.at<uint32_t>(1), 4, cudaMemcpyDeviceToHost, s));
         BP_CU(cudaStreamSynchronize(s));
         const bool worklist = hflag[1] == 0;
+        // a worklist holds one byte per tile and, after them, whether any tile is marked
         uint8_t* dbuf[2] = {dirty.at<uint8_t>(), dirty.at<uint8_t>(t_sw + 32)};
-        BP_CU(cudaMemsetAsync(dbuf[0], 1, t_sw, s));
-        BP_CU(cudaMemsetAsync(dbuf[1], 0, t_sw, s));
+        BP_CU(cudaMemsetAsync(dbuf[0], 1, t_sw + 1, s));
+        BP_CU(cudaMemsetAsync(dbuf[1], 0, t_sw + 1, s));
         int cur = 0;
         for (uint32_t sweeps = 0;;) {
             BP_CU(cudaMemsetAsync(changed.p, 0, 4, s));
             for (int k = 0; k < 4; ++k) {
                 batch_sweep(bl(17), t_sw, changed.at<uint32_t>(), worklist ? dbuf[cur] : nullptr, dbuf[cur ^ 1]);
-                BP_CU(cudaMemsetAsync(dbuf[cur], 0, t_sw, s));
+                BP_CU(cudaMemsetAsync(dbuf[cur], 0, t_sw + 1, s));
                 cur ^= 1;
             }
             sweeps += 4;

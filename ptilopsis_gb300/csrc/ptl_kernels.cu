@@ -1825,6 +1825,7 @@ __global__ void __launch_bounds__(kThreads) k_batch_sweep(const Prog* progs, con
     constexpr uint32_t kSweepItems = TILE / kThreads;
     static_assert(kSweepItems >= 1 && kSweepItems <= 32, "pending bits");
     __shared__ uint8_t s_used[TILE];
+    if (cur && !cur[total]) return;  // no tile was marked: nothing to sweep
     for (uint32_t t = blockIdx.x; t < total; t += gridDim.x) {
         if (cur && !cur[t]) continue;  // block-uniform
         const uint32_t p = batch_program(off, B, t);
@@ -1870,6 +1871,7 @@ __global__ void __launch_bounds__(kThreads) k_batch_sweep(const Prog* progs, con
                     } else if (*reinterpret_cast<volatile uint8_t*>(&P.used[a])) {
                         P.used[a] = 0;
                         next[off[p] + u32(a) / TILE] = 1;
+                        next[total] = 1;  // some tile is marked
                         cross = true;
                     }
                 }
@@ -1889,8 +1891,8 @@ __global__ void __launch_bounds__(kThreads) k_batch_sweep(const Prog* progs, con
 // Input gather from host memory: a tile is kGatherTile elements of one program; 16-byte
 // moves when the host array is 16-byte aligned (the device side always is), bytes
 // otherwise.  Each thread has kGatherDepth reads in flight, so a grid of two blocks per
-// SM covers the host link's latency and leaves the SMs to kernels of another stream (a
-// batch's second half copies its inputs under the first half's stages).
+// SM covers the host link's latency and leaves the SMs to kernels of other streams (the
+// compile server's lanes).
 constexpr int kGatherDepth = 8;
 __global__ void __launch_bounds__(kThreads) k_gather_host(HostGather g, const uint32_t* off, uint32_t B,
                                                           uint32_t total) {

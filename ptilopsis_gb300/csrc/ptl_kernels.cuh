@@ -117,9 +117,10 @@ enum class ArenaGuard { Nodes, Words, Words2 };
 void batch_guards(ArenaGuard g, const BatchLaunch& bl, uint32_t total);
 void batch_sort_keys(const BatchLaunch& bl, uint32_t total, unsigned long long* a, const uint64_t* aoff, bool out);
 // One optimize sweep over the tiles marked in cur (all when cur is null); marks in next
-// the tiles a cleared mark makes live again.  Valid only when the OptMark stage found
-// every virtual result to be its instruction's own word (its flag 0); otherwise pass
-// cur = null.
+// the tiles a cleared mark makes live again.  Both hold total + 1 bytes: the last says
+// whether any tile is marked (a sweep with none returns at once).  Valid only when the
+// OptMark stage found every virtual result to be its instruction's own word (its flag
+// 0); otherwise pass cur = null.
 void batch_sweep(const BatchLaunch& bl, uint32_t total, uint32_t* changed, const uint8_t* cur, uint8_t* next);
 
 // One input field of every program copied from the caller's host arrays into the device

@@ -55,3 +55,17 @@ def test_cli_compiles_like_the_reference(built_cuda, tmp_path):
     assert (tmp_path / "prog.s").read_text() == to_asm(golden["words"])
     r = _run(["-", "-S", "-o", "-"], tmp_path, stdin=(tmp_path / "prog.npz").read_bytes())
     assert r.returncode == 0 and r.stdout.decode() == to_asm(golden["words"])
+    # the parser's tree in a shuffled node order, flattened on the GPU before the compile
+    from ptilopsis_gb300.cli import save_unordered
+    t = ast_to_tree(ast)
+    perm = np.random.default_rng(7).permutation(t.n)
+    par = np.where(t.parent >= 0, perm[np.maximum(t.parent, 0)], -1)
+    arrs = []
+    for x in (t.type, t.rtype, par, t.child_idx, t.data):
+        y = np.empty_like(x)
+        y[perm] = x
+        arrs.append(y)
+    save_unordered(*arrs, tmp_path / "unordered.npz")
+    r = _run(["unordered.npz", "-o", "u.out"], tmp_path)
+    assert r.returncode == 0, r.stderr
+    np.testing.assert_array_equal(np.fromfile(tmp_path / "u.out", "<u4"), golden["words"])
