@@ -230,3 +230,22 @@ def test_batch_poisoned_arenas(built_cuda, monkeypatch):
                 assert b.status(k) == 0
                 w, tab = _alone(t)
                 _assert_same(b.result(k), w, tab, f"program {k} ({t.n} nodes)")
+
+
+def test_batch_regalloc_share_and_device_window(built_cuda):
+    """A smaller share of resident blocks for the regalloc launch changes no word; the
+    device window of a compile is positive and within its wall time."""
+    from ptilopsis_gb300 import PtlError
+    from ptilopsis_gb300.batch import BatchCompiler
+    trees = _programs(10, seed0=0x50544DA0)
+    with BatchCompiler(workers=4) as b:
+        b.compile(trees)
+        want = [b.words(k).copy() for k in range(len(trees))]
+        for share in (0.5, 0.1):
+            b.set_regalloc_share(share)
+            b.compile(trees)
+            for k in range(len(trees)):
+                np.testing.assert_array_equal(b.words(k), want[k], err_msg=f"share {share} program {k}")
+            assert 0 < b.device_ns() <= b.elapsed_ns()
+        with pytest.raises(PtlError):
+            b.set_regalloc_share(0.0)
