@@ -186,8 +186,15 @@ class BatchCompiler:
     def compile(self, trees: Sequence[DepthTree], check: bool = True) -> None:
         """Compiles the trees (host arrays); results via result(k).  With check=False a
         program's own failure is left to status(k)."""
-        keep: list = []
-        views = (_AstView * len(trees))(*[_view(t, keep) for t in trees])
+        # the view array is kept while the same trees (with the same cached views) come back
+        cached = getattr(self, "_views", None)
+        if (cached is not None and len(cached[0]) == len(trees)
+                and all(t.__dict__.get("_ptl_view") is e for t, e in zip(trees, cached[0]))):
+            views = cached[1]
+        else:
+            keep: list = []
+            views = (_AstView * len(trees))(*[_view(t, keep) for t in trees])
+            self._views = (keep, views)
         self._n = len(trees)
         st = self._lib.ptl_batch_compile(self._h, views, len(trees))
         if st != 0 and (check or self._batch_failed()):

@@ -69,6 +69,11 @@ class DepthTree:
     data: object        # u32
     max_depth: int
 
+    def __setattr__(self, name, value):
+        # a replaced array or max_depth makes the cached C view (_view) stale
+        self.__dict__.pop("_ptl_view", None)
+        object.__setattr__(self, name, value)
+
     @property
     def n(self) -> int:
         return int(self.type.shape[0])
@@ -165,13 +170,13 @@ _FIELDS = (("type", np.dtype(np.uint8)), ("rtype", np.dtype(np.uint8)), ("parent
 
 
 def _view(tree: DepthTree, keep: list) -> _AstView:
-    """The C view of a tree.  It is kept on the tree and reused while the tree holds the
-    same six array objects and max_depth (a view holds pointers, not contents)."""
-    arrs = (tree.type, tree.rtype, tree.parent, tree.depth, tree.child_idx, tree.data)
+    """The C view of a tree.  It is kept on the tree until one of its fields is assigned
+    (DepthTree.__setattr__ drops it): a view holds pointers, not contents."""
     cached = tree.__dict__.get("_ptl_view")
-    if cached is not None and cached[2] == tree.max_depth and all(x is y for x, y in zip(cached[0], arrs)):
+    if cached is not None:
         keep.append(cached)
         return cached[1]
+    arrs = (tree.type, tree.rtype, tree.parent, tree.depth, tree.child_idx, tree.data)
     on_dev = tree.on_device
     held, ptrs = [], []
     for a, (_, dt) in zip(arrs, _FIELDS):
