@@ -367,20 +367,40 @@ __global__ void __launch_bounds__(kThreads) k_sort_segscan(SortScratch ss, SortS
             carry_r += tot[1];
             __syncthreads();
         }
+        // A bound on the pair count K: at any position x, K <= max(L-stops before x,
+        // R-stops from x on) -- were K larger, the K-th L-stop would sit at or after x and
+        // its pair, further right, would leave K R-stops from x on.  The minimum over the
+        // tile starts (and the end) keeps it in g.K until the cut; stops ranked past it
+        // are never swapped, so their positions need not be written.
+        uint32_t kb = carry_l;
+        for (uint32_t k = threadIdx.x; k < g.tcount; k += kThreads)
+            kb = min(kb, max(ss.tile_l[g.tbase + k], carry_r - ss.tile_r[g.tbase + k]));
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1) kb = min(kb, __shfl_down_sync(0xFFFFFFFFu, kb, d));
+        if ((threadIdx.x & 31u) == 0) sm[threadIdx.x >> 5] = kb;
+        __syncthreads();
         if (threadIdx.x == 0) {
+            for (uint32_t w = 1; w < kThreads / 32; ++w) kb = min(kb, sm[w]);
             g.nL = carry_l;
             g.nR = carry_r;
+            g.K = kb;
         }
+        __syncthreads();
     }
 }
 
-// Stop positions by rank: A[rank] for L-stops, B[rank from the right] for R-stops.
+// Stop positions by rank: A[rank] for L-stops, B[rank from the right] for R-stops, for
+// ranks up to the segment's bound on K (g.K, from k_sort_segscan) -- the cut reads
+// A[0..K] and B[0..K-1].  A tile with no stop in that range is not read.
 __global__ void __launch_bounds__(kThreads) k_sort_pos(SortScratch ss, const SortSeg* cur) {
     __shared__ uint32_t sm[2 * kThreads / 32 + 2];
     if (sort_overflow(ss)) return;
     const uint32_t ntiles = sort_ntiles(ss);
     for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const SortSeg g = cur[ss.tile_seg[t]];
+        const uint32_t kb1 = g.K + 1u;  // ranks below this are written
+        const uint32_t rnext = t + 1u < g.tbase + g.tcount ? ss.tile_r[t + 1u] : g.nR;
+        if (ss.tile_l[t] >= kb1 && g.nR - rnext >= kb1) continue;  // block-uniform
         const uint32_t lo = g.first + 1 + (t - g.tbase) * kSortTile;
         const uint32_t hi = min(g.last, lo + kSortTile);
         const uint32_t p0 = lo + threadIdx.x * kSortItems;
@@ -401,8 +421,14 @@ __global__ void __launch_bounds__(kThreads) k_sort_pos(SortScratch ss, const Sor
 #pragma unroll
         for (uint32_t k = 0; k < kSortItems; ++k) {
             const uint32_t p = p0 + k;
-            if ((fl >> k) & 1u) ss.apos[g.first + rl++] = p;
-            if ((fr >> k) & 1u) ss.bpos[g.first + (g.nR - 1u - rr++)] = p;
+            if ((fl >> k) & 1u) {
+                if (rl < kb1) ss.apos[g.first + rl] = p;
+                ++rl;
+            }
+            if ((fr >> k) & 1u) {
+                const uint32_t rk = g.nR - 1u - rr++;
+                if (rk < kb1) ss.bpos[g.first + rk] = p;
+            }
         }
         __syncthreads();
     }
@@ -459,7 +485,8 @@ __global__ void k_sort_cut(SortScratch ss, SortSeg* cur, SortSeg* next, ErrorWor
             g.K = 0;
             continue;
         }
-        g.K = partition_k(ss.apos + g.first, ss.bpos + g.first, g.nL, g.nR);
+        // positions are written for ranks up to the bound g.K only; K <= g.K
+        g.K = partition_k(ss.apos + g.first, ss.bpos + g.first, min(g.nL, g.K), g.nR);
         g.cut = partition_cut(ss.apos + g.first, ss.bpos + g.first, g.nL, g.K);
         if (g.cut <= g.first || g.cut >= g.last) {
             record_error(err, ST_UNSUPPORTED, W_SORT, g.first);
