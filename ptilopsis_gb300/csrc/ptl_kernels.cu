@@ -591,12 +591,12 @@ __device__ __forceinline__ int32_t warp_max_i32(int32_t v) {
 
 // One block-wide split of [f, l); sets w.K / w.cut / w.kmin / w.kmax (w.bad on a broken
 // invariant).  Every thread calls it; it ends with a barrier.
+// The caller has moved the median to f (thread 0, before the barrier that publishes the
+// part).
 __device__ void bsort_split_block(BlockSortSmem& w, uint32_t f, uint32_t l) {
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
     const unsigned full = 0xFFFFFFFFu, lt = (1u << lane) - 1u;
     constexpr uint32_t T = kSortBlockThreads;
-    if (tid == 0) median_to_first(w.buf, f, l);
-    __syncthreads();
     const int32_t pivot = skey(w.buf[f]);
     const uint32_t sweeps = (l - f - 1u + T - 1u) / T;
     uint32_t fl = 0, fr = 0;
@@ -662,28 +662,41 @@ __device__ void bsort_split_block(BlockSortSmem& w, uint32_t f, uint32_t l) {
         if (isR) w.R[f + w.cntR[k * kSortBlockWarps + warp] + __popc(bR & lt)] = static_cast<uint16_t>(p);
     }
     __syncthreads();
-    if (tid == 0) {
+    if (warp == 0) {
         const uint32_t nL = w.nL, nR = w.nR;
         uint32_t K = 0, cut = 0;
         if (nL == 0 || nR == 0) {  // the median move guarantees both kinds of stop
-            w.bad = 1;
+            if (lane == 0) w.bad = 1;
         } else {
-            uint32_t lo = 0, hi = nL < nR ? nL : nR;  // K: A[k] < B[k] holds on a prefix of k
-            while (lo < hi) {
-                const uint32_t mid = (lo + hi) / 2;
-                if (w.A[f + mid] < w.R[f + nR - 1u - mid]) lo = mid + 1; else hi = mid;
+            // K: A[k] < B[k] holds on a prefix of k, and K is in [lo, hi].  32 probes per
+            // round narrow the range to one of 33 slices; the last round tests each index.
+            uint32_t lo = 0, hi = nL < nR ? nL : nR;
+            while (hi - lo > 32u) {
+                const uint64_t span = hi - lo;
+                const uint32_t q = lo + static_cast<uint32_t>(span * (lane + 1u) / 33u);
+                const uint32_t c = __popc(__ballot_sync(full, w.A[f + q] < w.R[f + nR - 1u - q]));
+                const uint32_t nlo = c == 0 ? lo : lo + static_cast<uint32_t>(span * c / 33u) + 1u;
+                const uint32_t nhi = c == 32 ? hi : lo + static_cast<uint32_t>(span * (c + 1u) / 33u);
+                lo = nlo;
+                hi = nhi;
             }
-            K = lo;
+            const uint32_t q = lo + lane;
+            K = lo + __popc(__ballot_sync(full, q < hi && w.A[f + q] < w.R[f + nR - 1u - q]));
             if (K == 0) {
                 cut = w.A[f];
             } else {
                 const uint32_t bk = w.R[f + nR - K];  // B[K-1]
                 cut = (K < nL && w.A[f + K] < bk) ? w.A[f + K] : bk;
             }
-            if (cut <= f || cut >= l) { w.bad = 1; K = 0; }
+            if (cut <= f || cut >= l) {
+                if (lane == 0) w.bad = 1;
+                K = 0;
+            }
         }
-        w.K = K;
-        w.cut = cut;
+        if (lane == 0) {
+            w.K = K;
+            w.cut = cut;
+        }
     }
     __syncthreads();
     const uint32_t K = w.K, nR = w.nR;
@@ -809,6 +822,7 @@ __global__ void __launch_bounds__(kSortBlockThreads) k_sort_block(SortScratch ss
                     bsort_push_small(w, 0, m, dl);
                 } else {
                     w.cur_f = 0; w.cur_l = m; w.cur_d = dl; w.have = 1;
+                    median_to_first(w.buf, 0, m);
                 }
             }
         }
@@ -847,6 +861,7 @@ __global__ void __launch_bounds__(kSortBlockThreads) k_sort_block(SortScratch ss
                         w.cur_f = w.bst_f[w.n_bst]; w.cur_l = w.bst_l[w.n_bst]; w.cur_d = w.bst_d[w.n_bst];
                         w.have = 1;
                     }
+                    if (w.have) median_to_first(w.buf, w.cur_f, w.cur_l);  // the next split's pivot
                 }
             }
             __syncthreads();
