@@ -498,6 +498,9 @@ __global__ void k_sort_cut(SortScratch ss, SortSeg* cur, SortSeg* next, ErrorWor
     }
 }
 
+// The K swaps of a segment touch disjoint positions (every A[k] lies left of every B[k'],
+// k, k' < K), so a thread loads all of its tile's pairs and their keys before it stores
+// any: the loads of a tile are in flight together instead of one dependent pair at a time.
 __global__ void __launch_bounds__(kThreads) k_sort_swap(SortScratch ss, const SortSeg* cur) {
     if (sort_overflow(ss)) return;
     const uint32_t ntiles = sort_ntiles(ss);
@@ -505,8 +508,30 @@ __global__ void __launch_bounds__(kThreads) k_sort_swap(SortScratch ss, const So
         const SortSeg g = cur[ss.tile_seg[t]];
         const uint32_t k0 = (t - g.tbase) * kSortTile;
         const uint32_t k1 = min(g.K, k0 + kSortTile);
-        for (uint32_t k = k0 + threadIdx.x; k < k1; k += kThreads) {
-            sswap(ss.a, ss.apos[g.first + k], ss.bpos[g.first + k]);
+        if (k0 >= k1) continue;
+        uint32_t pa[kSortItems], pb[kSortItems];
+        unsigned long long va[kSortItems], vb[kSortItems];
+#pragma unroll
+        for (uint32_t u = 0; u < kSortItems; ++u) {
+            const uint32_t k = k0 + threadIdx.x + u * kThreads;
+            if (k < k1) {
+                pa[u] = ss.apos[g.first + k];
+                pb[u] = ss.bpos[g.first + k];
+            }
+        }
+#pragma unroll
+        for (uint32_t u = 0; u < kSortItems; ++u) {
+            if (k0 + threadIdx.x + u * kThreads < k1) {
+                va[u] = ss.a[pa[u]];
+                vb[u] = ss.a[pb[u]];
+            }
+        }
+#pragma unroll
+        for (uint32_t u = 0; u < kSortItems; ++u) {
+            if (k0 + threadIdx.x + u * kThreads < k1) {
+                ss.a[pa[u]] = vb[u];
+                ss.a[pb[u]] = va[u];
+            }
         }
     }
 }
