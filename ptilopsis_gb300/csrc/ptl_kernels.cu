@@ -320,12 +320,19 @@ __global__ void __launch_bounds__(kThreads) k_sort_count(SortScratch ss, SortSeg
         const uint32_t hi = min(g.last, lo + kSortTile);
         uint32_t cl = 0, cr = 0;
         int32_t mn = g.pivot, mx = g.pivot;
-        for (uint32_t p = lo + threadIdx.x; p < hi; p += kThreads) {
-            const int32_t k = skey(ss.a[p]);
-            cl += is_lstop(k, g.pivot);
-            cr += is_rstop(k, g.pivot);
-            mn = min(mn, k);
-            mx = max(mx, k);
+        int32_t key[kSortItems];  // the tile's keys of this thread, loaded together
+#pragma unroll
+        for (uint32_t u = 0; u < kSortItems; ++u) {
+            const uint32_t p = lo + threadIdx.x + u * kThreads;
+            key[u] = p < hi ? skey(ss.a[p]) : g.pivot;
+        }
+#pragma unroll
+        for (uint32_t u = 0; u < kSortItems; ++u) {
+            if (lo + threadIdx.x + u * kThreads >= hi) continue;
+            cl += is_lstop(key[u], g.pivot);
+            cr += is_rstop(key[u], g.pivot);
+            mn = min(mn, key[u]);
+            mx = max(mx, key[u]);
         }
 #pragma unroll
         for (int d = 16; d > 0; d >>= 1) {
