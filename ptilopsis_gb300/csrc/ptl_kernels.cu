@@ -1757,29 +1757,57 @@ template <class Op>
 __global__ void __launch_bounds__(kThreads) k_batch(const Prog* progs, const uint32_t* off, uint32_t B, uint32_t total,
                                                     uint32_t tile, Op op) {
     Op o = op;  // per-thread copy: an op may carry state from element to element
-    for (uint32_t t = blockIdx.x; t < total; t += gridDim.x) {
-        const uint32_t p = batch_program(off, B, t);
-        const Prog& P = progs[p];
-        const uint32_t cnt = Op::count(P);
-        const uint32_t base = (t - off[p]) * tile;
-        for (uint32_t k = threadIdx.x; k < tile; k += kThreads) {
-            const uint32_t i = base + k;
-            if (i < cnt) o(P, i, p);
+    if constexpr (Op::kViewInShared) {
+        // The tile's program view in shared memory: read from global memory, its
+        // pointers would be reloaded after every store an op makes (the compiler cannot
+        // rule out that the store hit the view).  Worth its copy and two barriers for the
+        // ops with many fields per element (regalloc, isn_gen).
+        __shared__ Prog sP;
+        uint32_t have = 0xFFFFFFFFu;
+        for (uint32_t t = blockIdx.x; t < total; t += gridDim.x) {
+            const uint32_t p = batch_program(off, B, t);
+            if (p != have) {  // block-uniform
+                __syncthreads();  // every thread is done with the previous view
+                const uint64_t* src = reinterpret_cast<const uint64_t*>(&progs[p]);
+                uint64_t* dst = reinterpret_cast<uint64_t*>(&sP);
+                for (uint32_t k = threadIdx.x; k < sizeof(Prog) / 8; k += kThreads) dst[k] = src[k];
+                __syncthreads();
+                have = p;
+            }
+            const uint32_t cnt = Op::count(sP);
+            const uint32_t base = (t - off[p]) * tile;
+            for (uint32_t k = threadIdx.x; k < tile; k += kThreads) {
+                const uint32_t i = base + k;
+                if (i < cnt) o(sP, i, p);
+            }
+        }
+    } else {
+        for (uint32_t t = blockIdx.x; t < total; t += gridDim.x) {
+            const uint32_t p = batch_program(off, B, t);
+            const Prog& P = progs[p];
+            const uint32_t cnt = Op::count(P);
+            const uint32_t base = (t - off[p]) * tile;
+            for (uint32_t k = threadIdx.x; k < tile; k += kThreads) {
+                const uint32_t i = base + k;
+                if (i < cnt) o(P, i, p);
+            }
         }
     }
 }
 
-#define PTL_BATCH_OP(NAME, COUNT, BODY)                                                         \
+#define PTL_BATCH_OP_V(NAME, SHARED, COUNT, BODY)                                               \
     struct NAME {                                                                              \
+        static constexpr bool kViewInShared = SHARED;                                          \
         __device__ static uint32_t count(const Prog& P) { return COUNT; }                      \
         __device__ void operator()(const Prog& P, uint32_t i, uint32_t p) const { BODY; }      \
     };
+#define PTL_BATCH_OP(NAME, COUNT, BODY) PTL_BATCH_OP_V(NAME, true, COUNT, BODY)
 
-PTL_BATCH_OP(BIngest, P.nb8, if (st_ingest(P, i)) P.flags[3] = 1u)
-PTL_BATCH_OP(BPreArgs, P.nb8, st_pre_args(P, i))
-PTL_BATCH_OP(BPreLists, P.nb8, st_pre_lists(P, i))
-PTL_BATCH_OP(BPreFloat, P.nb8, st_pre_float(P, i))
-PTL_BATCH_OP(BPreFloatApply, P.nb8, st_pre_float_apply(P, i))
+PTL_BATCH_OP_V(BIngest, false, P.nb8, if (st_ingest(P, i)) P.flags[3] = 1u)
+PTL_BATCH_OP_V(BPreArgs, false, P.nb8, st_pre_args(P, i))
+PTL_BATCH_OP_V(BPreLists, false, P.nb8, st_pre_lists(P, i))
+PTL_BATCH_OP_V(BPreFloat, false, P.nb8, st_pre_float(P, i))
+PTL_BATCH_OP_V(BPreFloatApply, false, P.nb8, st_pre_float_apply(P, i))
 PTL_BATCH_OP(BFixOwn, P.nb8, st_fix_own(P, i))
 PTL_BATCH_OP(BFixCond, P.nb8, st_fix_cond(P, i))
 PTL_BATCH_OP(BFunctab, P.fb8, st_functab(P, i))
@@ -1793,6 +1821,7 @@ __device__ __forceinline__ int64_t guard_index(uint32_t j, uint32_t written) {
                            : static_cast<int64_t>(written) + static_cast<int64_t>(j - kArenaFront);
 }
 struct BGuardNodes {
+    static constexpr bool kViewInShared = false;
     __device__ static uint32_t count(const Prog& P) { return static_cast<uint32_t>(arena_region(P.nb8) - P.nb8); }
     __device__ void operator()(const Prog& P, uint32_t j, uint32_t) const {
         const int64_t x = guard_index(j, P.nb8);
@@ -1801,6 +1830,7 @@ struct BGuardNodes {
     }
 };
 struct BGuardWords {
+    static constexpr bool kViewInShared = false;
     __device__ static uint32_t count(const Prog& P) { return static_cast<uint32_t>(arena_region(P.wb8) - P.W); }
     __device__ void operator()(const Prog& P, uint32_t j, uint32_t) const {
         const int64_t x = guard_index(j, P.W);
@@ -1808,6 +1838,7 @@ struct BGuardWords {
     }
 };
 struct BGuardWords2 {
+    static constexpr bool kViewInShared = false;
     __device__ static uint32_t count(const Prog& P) {
         return static_cast<uint32_t>(arena_region(P.w2b8 + 16u) - P.w2b8);
     }
@@ -1816,6 +1847,7 @@ struct BGuardWords2 {
 // marks, and odd = 1 when some virtual result is not its instruction's own word (what
 // the optimize sweeps' worklist needs to know)
 struct BOptMark {
+    static constexpr bool kViewInShared = true;
     uint32_t* odd;
     __device__ static uint32_t count(const Prog& P) { return P.wb8; }
     __device__ void operator()(const Prog& P, uint32_t i, uint32_t) const {
@@ -1829,6 +1861,7 @@ PTL_BATCH_OP(BInitLifetime, P.F, P.lifetime[i] = 0x1Full)
 // spill flags and cross checks find each word's function from the thread's previous
 // word (the same program, 256 words earlier within a tile)
 struct BSpill {
+    static constexpr bool kViewInShared = true;
     uint32_t hint = 0xFFFFFFFFu, hp = 0xFFFFFFFFu;
     __device__ static uint32_t count(const Prog& P) { return P.W; }
     __device__ void operator()(const Prog& P, uint32_t i, uint32_t p) {
@@ -1839,14 +1872,15 @@ struct BSpill {
 PTL_BATCH_OP(BScatter, P.wb8, st_ra_scatter(P, i))
 PTL_BATCH_OP(BRaFunctab, P.F, st_fix_functab(P, i, P.roffs, P.W))
 PTL_BATCH_OP(BRaFrame, P.F, st_ra_frame(P, i))
-PTL_BATCH_OP(BFjEmit, P.W2, st_fj_emit(P, i))
-PTL_BATCH_OP(BFjFunctab, P.F, st_fix_functab(P, i, P.joffs, P.W2))
+PTL_BATCH_OP_V(BFjEmit, false, P.W2, st_fj_emit(P, i))
+PTL_BATCH_OP_V(BFjFunctab, false, P.F, st_fix_functab(P, i, P.joffs, P.W2))
 // chunk histogram of a program's independent functions (see k_ra_chunk_hist)
 PTL_BATCH_OP(BRaHist, P.F - (P.F + 7u) / 8u,
              const uint32_t f = free_function_of(i);
              const uint32_t size = P.fn_size0[f];
              if (s32(size) > 0) atomicAdd(&P.ra_chunks[(size - 1u) / kRaChunk], 1u))
 struct BCross {
+    static constexpr bool kViewInShared = true;
     uint32_t hint = 0xFFFFFFFFu, hp = 0xFFFFFFFFu;
     __device__ static uint32_t count(const Prog& P) { return P.W; }
     __device__ void operator()(const Prog& P, uint32_t i, uint32_t p) {
@@ -1859,6 +1893,7 @@ struct BCross {
 
 // per program: word count and longest function (meta[4p + 1], meta[4p + 2])
 struct BFunctabEnd {
+    static constexpr bool kViewInShared = true;
     uint32_t* meta;
     __device__ static uint32_t count(const Prog& P) { return P.fb8; }
     __device__ void operator()(const Prog& P, uint32_t f, uint32_t p) const {
@@ -1869,6 +1904,7 @@ struct BFunctabEnd {
 };
 // depth-order keys of all programs in one array, program p from aoff[p]
 struct BSortInit {
+    static constexpr bool kViewInShared = true;
     unsigned long long* a;
     const uint64_t* aoff;
     __device__ static uint32_t count(const Prog& P) { return P.n; }
@@ -1877,6 +1913,7 @@ struct BSortInit {
     }
 };
 struct BSortOut {
+    static constexpr bool kViewInShared = true;
     const unsigned long long* a;
     const uint64_t* aoff;
     __device__ static uint32_t count(const Prog& P) { return P.n; }
