@@ -2090,11 +2090,18 @@ __global__ void __launch_bounds__(kScanThreads) k_bscan(const Prog* progs, const
     constexpr int kWarps = kScanThreads / 32;
     __shared__ uint32_t s_tile, s_prefix;
     __shared__ uint32_t s_warp[kWarps];
+    __shared__ Prog sP;  // the program view, out of reach of the ops' stores (as in k_batch)
     if (threadIdx.x == 0) s_tile = atomicAdd(sc.counter, 1u);
     __syncthreads();
     const uint32_t tile = s_tile;
     const uint32_t p = batch_program(off, B, tile);
-    const Prog& P = progs[p];
+    {
+        const uint64_t* src = reinterpret_cast<const uint64_t*>(&progs[p]);
+        uint64_t* dst = reinterpret_cast<uint64_t*>(&sP);
+        for (uint32_t k = threadIdx.x; k < sizeof(Prog) / 8; k += kScanThreads) dst[k] = src[k];
+    }
+    __syncthreads();
+    const Prog& P = sP;
     const uint32_t first = off[p];  // the program's first tile
     const uint32_t count = Op::count(P);
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
