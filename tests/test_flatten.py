@@ -77,6 +77,25 @@ def test_oracle_flatten_pinned_to_reference():
         assert_tree(portbind.flatten(*arrs)[0], refbind.flatten(*arrs), f"case {k}")
 
 
+def _fixture_cases():
+    """The reference front end's own DepthTrees (committed fixtures, built by the
+    reference's DepthTree constructor), each given in a seeded random node order."""
+    from conftest import ast_to_tree, load_fixture, manifest
+    out = []
+    for k, fx in enumerate(manifest()["fixtures"]):
+        ast, _ = load_fixture(fx["name"])
+        tree = ast_to_tree(ast)
+        out.append((fx["name"], tree, shuffled(tree, 0x50544E60 + k)[0]))
+    return out
+
+
+def test_oracle_flatten_pinned_to_reference_fixtures():
+    """Runs anywhere: the restatement rebuilds exactly the trees the reference built."""
+    from oracle import portbind
+    for name, tree, arrs in _fixture_cases():
+        assert_tree(portbind.flatten(*arrs)[0], tree, name)
+
+
 def test_oracle_flatten_rejects_malformed():
     from oracle import portbind
     base = list(star(5))
@@ -103,6 +122,13 @@ def test_gpu_flatten_equals_oracle(built_cuda):
         got, order = flatten(*arrs)
         assert_tree(got, want, f"case {k} ({arrs[0].shape[0]} nodes)")
         np.testing.assert_array_equal(order, want_order, err_msg=f"case {k} order")
+
+
+@pytest.mark.gpu
+def test_gpu_flatten_reference_fixtures(built_cuda):
+    from ptilopsis_gb300 import flatten
+    for name, tree, arrs in _fixture_cases():
+        assert_tree(flatten(*arrs)[0], tree, name)
 
 
 @pytest.mark.gpu
