@@ -183,24 +183,68 @@ def port_parallel(trees, threads):
     return sum(t.n for t in trees) / dt, dt, outs
 
 
-def cpu_sample(trees, target_nodes):
-    """A bounded sample of the workload: indices of every k-th program until target_nodes."""
-    step = max(1, len(trees) // 256)
-    out, tot = [], 0
-    for k in range(0, len(trees), step):
-        out.append(k)
-        tot += trees[k].n
-        if tot >= target_nodes:
-            break
-    return out
+def reduce_max(x: float, dist=None, device=None) -> float:
+    """The largest of the ranks' values (a step is as slow as its slowest rank); with no
+    process group, x itself.  device: where the reduction tensor lives (a CUDA device for
+    NCCL, None for gloo)."""
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
 
 
-def make_workload(args, rank):
+def planned_nodes(k: int) -> float:
+    """Program k's planned size (functions x mean function size), known before it is
+    generated."""
+    from ptilopsis_gb300.synth import config_params
+    p = config_params("c3", program=k)
+    return p.n_functions * p.median_fn_nodes * float(np.exp(p.sigma ** 2 / 2))
+
+
+def rank_programs(programs: int, rank: int, world: int) -> list:
+    """The program indices one rank compiles: the N x `programs` programs of the whole
+    job, split over the N ranks by planned size (shard_programs), so that every rank has
+    about `programs` programs and the same number of nodes (weak scaling: the work per
+    GPU is fixed as N grows; programs are independent, so no rank exchanges data)."""
+    from ptilopsis_gb300.batch import shard_programs
+    if world == 1:
+        return list(range(programs))
+    sizes = [planned_nodes(k) for k in range(programs * world)]
+    return shard_programs(sizes, world)[rank]
+
+
+def make_workload(args, rank, world=1):
     from concurrent.futures import ThreadPoolExecutor
     from ptilopsis_gb300.synth import config_params, generate
-    base = rank * args.programs  # each rank its own programs
+    idx = rank_programs(args.programs, rank, world)
     with ThreadPoolExecutor(min(32, os.cpu_count() or 8)) as ex:
-        return list(ex.map(lambda k: generate(config_params("c3", program=base + k)), range(args.programs)))
+        return list(ex.map(lambda k: generate(config_params("c3", program=k)), idx))
+
+
+def batched_config(trees, words):
+    """The workload description both arms print (the GPU arm's tiles and parallelism are
+    separate keys)."""
+    nodes = sum(t.n for t in trees)
+    return {"workload": f"c3: {len(trees)} synthetic programs per GPU (1k..500k nodes, lognormal), {nodes} nodes, "
+                        f"{words} output words",
+            "programs": len(trees), "nodes": nodes, "words": int(words)}
+
+
+def compare_all(trees, words_of, table_of, outs):
+    """Every program's words and function table against the oracle's outputs."""
+    equal, first_bad = 0, None
+    for k, o in enumerate(outs):
+        tab = table_of(k)
+        ok = np.array_equal(words_of(k), o.words) and all(
+            np.array_equal(tab[a], o.bufs[b]) for a, b in (("starts", "fn_start"), ("ends", "fn_end"),
+                                                            ("sizes", "fn_size"), ("ids", "fn_id")))
+        equal += ok
+        if not ok and first_bad is None:
+            first_bad = k
+    return {"programs": len(outs), "equal": int(equal), "first_mismatch": first_bad,
+            "compared": "words and function table of every program"}
 
 
 def run_reference(args):
@@ -219,24 +263,32 @@ def run_reference(args):
         sample = f"one full compile of config {args.config} ({tree.n} nodes) per step, one thread"
         threads = 1
         workload = f"{args.config}: one synthetic program, {tree.n} nodes"
+        config = {"workload": workload, "nodes_per_step": tree.n}
     else:
-        all_trees = make_workload(args, 0)
-        trees = [all_trees[k] for k in cpu_sample(all_trees, 20_000_000)]
-        sample = (f"{len(trees)} of the {args.programs} batched-workload programs ({sum(t.n for t in trees)} nodes) "
-                  f"per step, {threads} threads")
-        workload = f"c3: {args.programs} synthetic programs, {sum(t.n for t in all_trees)} nodes (sampled)"
-    for _ in range(args.warmup):
-        port_parallel(trees, threads)
+        trees = make_workload(args, 0)
+        sample = (f"all {len(trees)} programs of the batched workload ({sum(t.n for t in trees)} nodes) per step, "
+                  f"{threads} threads, one program per thread at a time")
+        config = None
+    words = 0
+    for k in range(args.warmup):
+        _, _, outs = port_parallel(trees, threads)
+        if k == 0:
+            words = sum(len(o.words) for o in outs)
+        del outs
     times = []
     for _ in range(args.steps):
-        _, dt, _ = port_parallel(trees, threads)
+        _, dt, outs = port_parallel(trees, threads)
         times.append(dt)
+        words = sum(len(o.words) for o in outs)
+        del outs
+    if config is None:
+        config = batched_config(trees, words)
     ms = 1000.0 * sum(times) / len(times)
     value = sum(t.n for t in trees) / (ms / 1000.0)
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "u32", "data": "synthetic (seeded grammar)", "impl": "reference",
-            "config": {"workload": workload, "nodes_per_step": sum(t.n for t in trees)},
+            "config": config,
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -287,16 +339,24 @@ def run_serving(device, args):
                                  "max_ms": float(lat.max()),
                                  "nodes_per_s": float(sum(t.n for t in reqs) / span)})
         out["batches"] = srv.stats()["batches"]
-        # results in the mix equal compiling alone (a sample)
-        tickets = [srv.submit(r) for r in reqs[:16]]
-        mixed = [srv.result(t).words for t in tickets]
+        # results in the mix equal compiling alone and the oracle: the first 64 requests
+        # submitted together, so that they are batched with one another
+        k_mix = min(64, n_req)
+        tickets = [srv.submit(r) for r in reqs[:k_mix]]
+        mixed = [srv.result(t) for t in tickets]
+        for t in tickets:
+            srv.release(t)
     with RvGenerator(reqs[0], device=device) as g:
         same = True
-        for k in range(16):
+        for k in range(k_mix):
             g.upload(reqs[k])
             g.process()
-            same &= bool(np.array_equal(g.get_instructions(), mixed[k]))
+            same &= bool(np.array_equal(g.get_instructions(), mixed[k].words))
     out["bit_exact_vs_plain"] = same
+    _, _, outs = port_parallel(reqs[:k_mix], os.cpu_count() or 1)
+    chk = compare_all(reqs[:k_mix], lambda k: mixed[k].words, lambda k: mixed[k].table, outs)
+    out["bit_exact_vs_oracle"] = chk["equal"] == chk["programs"]
+    out["oracle_check"] = chk
     return out
 
 
@@ -356,7 +416,7 @@ def run_batched(args):
     from ptilopsis_gb300.batch import BatchCompiler
     from ptilopsis_gb300.codegen import kernel_launches
     b.build_all()
-    trees = make_workload(args, rank)
+    trees = make_workload(args, rank, world)
     nodes = sum(t.n for t in trees)
     dev = torch.device("cuda", local)
 
@@ -366,11 +426,7 @@ def run_batched(args):
         torch.cuda.synchronize()
 
     def max_over_ranks(x):
-        if dist is None:
-            return x
-        t = torch.tensor([x], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+        return reduce_max(x, dist, dev)
 
     # tile sizes by measurement, on other programs of the same distribution (untimed)
     tiles = tuple(args.tiles) if args.tiles else None
@@ -447,19 +503,27 @@ def run_batched(args):
     plain = {"value": sn / plain_dev, "e2e_value": sn / plain_wall, "unit": UNIT, "programs": len(sample),
              "nodes": sn, "sample": f"first {len(sample)} programs of the workload, one generator, one at a time"}
     same_as_plain = all(np.array_equal(bc.words(k), plain_words[k]) for k in range(len(sample)))
-    oracle_words = {k: bc.words(k) for k in cpu_sample(trees, args.cpu_nodes)} if rank == 0 else {}
+    oracle_check, cpu_line = None, None
+    if rank == 0 and not args.no_cpu_baseline:
+        # the oracle on every program of the batch, on all host cores (outside the timed
+        # region); its time is the CPU baseline
+        threads = os.cpu_count() or 1
+        rate, dt, outs = port_parallel(trees, threads)
+        oracle_check = compare_all(trees, bc.words, bc.function_table, outs)
+        del outs
+        cpu_line = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+                    "sample": f"all {len(trees)} programs of the workload ({nodes} nodes), {threads} threads",
+                    "seconds": round(dt, 3)}
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "u32", "data": "synthetic (seeded grammar, no datasets)",
-            "config": {"workload": f"c3: {len(trees)} synthetic programs per GPU (1k..500k nodes, lognormal), "
-                                   f"{nodes} nodes, {tot['W3']} output words",
-                       "programs": len(trees), "nodes": nodes, "words": tot["W3"],
-                       "l2": "working set (~60 GB) > L2; no flush needed",
-                       "parallelism": f"replicas x{world} (each GPU its own batch)",
-                       "tiles": {"elem": bc.tiles()[0], "sweep": bc.tiles()[1],
-                                 "chosen_by": "defaults" if tiles is None else "--tiles" if args.tiles else
-                                 "autotune on 512 other programs of the same distribution"}},
+            "config": batched_config(trees, tot["W3"]),
+            "l2": "working set (~60 GB) > L2; no flush needed",
+            "parallelism": f"replicas x{world} (each GPU its own batch)",
+            "tiles": {"elem": bc.tiles()[0], "sweep": bc.tiles()[1],
+                      "chosen_by": "defaults" if tiles is None else "--tiles" if args.tiles else
+                      "autotune on 512 other programs of the same distribution"},
             "e2e": e2e, "plain": plain, "batched_over_plain": value / plain["value"],
             "roofline": roofline, "gpu_launches": int(launches)}
     bc.close()
@@ -470,15 +534,10 @@ def run_batched(args):
             line["serving"] = run_serving(local, args)
         if not args.no_flatten:
             line["flatten"] = run_flatten(trees, local)
-        if not args.no_cpu_baseline:
-            threads = os.cpu_count() or 1
-            idx = cpu_sample(trees, args.cpu_nodes)
-            cs = [trees[k] for k in idx]
-            rate, dt, outs = port_parallel(cs, threads)
-            line["bit_exact_vs_oracle"] = bool(all(np.array_equal(oracle_words[k], o.words) for k, o in zip(idx, outs)))
-            line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
-                                    "sample": f"{len(cs)} programs ({sum(t.n for t in cs)} nodes) of the workload, "
-                                              f"{threads} threads", "seconds": round(dt, 3)}
+        if oracle_check is not None:
+            line["bit_exact_vs_oracle"] = oracle_check["equal"] == oracle_check["programs"]
+            line["oracle_check"] = oracle_check
+            line["cpu_baseline"] = cpu_line
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
@@ -622,7 +681,6 @@ def main():
     ap.add_argument("--mode", default="batched", choices=["batched", "single"])
     ap.add_argument("--programs", type=int, default=4096)
     ap.add_argument("--plain-sample", type=int, default=64)
-    ap.add_argument("--cpu-nodes", type=int, default=30_000_000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--no-flatten", action="store_true")

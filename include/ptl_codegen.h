@@ -129,13 +129,16 @@ size_t ptl_code_table(int which, uint32_t* out);
  * registers (the arrays ptl_generator_snapshot returns for which = 14..17), device
  * pointers on the current device.  used_instrs receives count words: 0xFFFFFFFF for a
  * word that stays, 0 for one the pass removes (ptl_generator_snapshot's which = 19).
- * stream is a cudaStream_t (NULL = the legacy default stream); the call returns when
- * the result is written.  count > PTL_OPTIMIZE_NOALLOC_MAX_WORDS returns
- * PTL_BAD_ARGUMENT before touching anything, as do null or non-device pointers.
- * The first call on each device looks up the scratch array's address with that
- * device current (cudaGetSymbolAddress); make that first call before any stream
- * capture begins.  Calls on one device are serialised by a lock because they share
- * the scratch; device work that used the same scratch concurrently would race. */
+ * stream is a cudaStream_t (NULL = the legacy default stream); the call blocks the
+ * host until the result is written (it reads a changed flag back between sweeps), so a
+ * stream that is being captured gets PTL_BAD_ARGUMENT with nothing queued on it.
+ * count > PTL_OPTIMIZE_NOALLOC_MAX_WORDS returns PTL_BAD_ARGUMENT before touching
+ * anything, as do null or non-device pointers.  The first call on each device looks up
+ * the scratch array's address with that device current (cudaGetSymbolAddress); make
+ * that first call before any stream capture begins.  Calls on one device are
+ * serialised by a lock because they share the scratch, and every return, failures
+ * included, comes after the call's device work has finished; device work that used the
+ * same scratch concurrently would race. */
 #define PTL_OPTIMIZE_NOALLOC_MAX_WORDS (1u << 22)
 ptl_status ptl_optimize_noalloc(const uint32_t* instr, const uint32_t* rd, const uint32_t* rs1,
                                 const uint32_t* rs2, size_t count, uint32_t* used_instrs, void* stream);

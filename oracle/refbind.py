@@ -16,7 +16,18 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_ref", "libptlref.so")
-REF_ROOT_DEFAULT = "/root/reference"
+
+
+def ref_root() -> str:
+    """The reference source tree: $PTL_REFERENCE_ROOT, else the REF default of the build
+    recipe (oracle/ref/Makefile), which is where the reference is mounted for the build."""
+    env = os.environ.get("PTL_REFERENCE_ROOT")
+    if env:
+        return env
+    res = subprocess.run(["make", "-s", "--no-print-directory", "-C", os.path.join(HERE, "ref"), "print-ref"],
+                         capture_output=True, text=True)
+    return res.stdout.strip() if res.returncode == 0 else ""
+
 
 BUF_NAMES = [
     "out_words", "fn_start", "fn_end", "fn_size", "fn_id",
@@ -78,16 +89,27 @@ class RefResult:
 _lib = None
 
 
-def build(ref_root: str = REF_ROOT_DEFAULT, quiet: bool = True) -> bool:
+def build(ref_root: str | None = None, quiet: bool = True) -> bool:
     """Compile the reference into oracle/_ref (make rebuilds only what changed; where the
     reference tree is absent an existing build is used as it is).
 
     Returns False where there is neither a build nor a reference tree on an x86-64 host."""
-    if not os.path.isdir(ref_root) or os.uname().machine not in ("x86_64", "AMD64"):
+    ref_root = ref_root or ref_root_cached()
+    if not ref_root or not os.path.isdir(ref_root) or os.uname().machine not in ("x86_64", "AMD64"):
         return os.path.exists(LIB_PATH)
     cmd = ["make", "-C", os.path.join(HERE, "ref"), f"REF={ref_root}", f"-j{os.cpu_count() or 4}"]
     res = subprocess.run(cmd, capture_output=quiet)
     return res.returncode == 0 and os.path.exists(LIB_PATH)
+
+
+_root = None
+
+
+def ref_root_cached() -> str:
+    global _root
+    if _root is None:
+        _root = ref_root()
+    return _root
 
 
 def available() -> bool:

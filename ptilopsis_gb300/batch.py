@@ -356,6 +356,24 @@ class CompileServer:
             pass
 
 
+def shard_programs(sizes: Sequence[int], world: int) -> List[List[int]]:
+    """Splits a set of independent programs over `world` GPUs by size: longest first,
+    each to the GPU with the fewest nodes so far (ties to the lower rank).  Programs
+    share nothing, so the shards need no exchange; every GPU compiles its own list, in
+    the order given (ascending program index).  Deterministic, so every rank computes
+    the same split without communicating."""
+    if world < 1:
+        raise ValueError("world must be at least 1")
+    order = sorted(range(len(sizes)), key=lambda k: (-int(sizes[k]), k))
+    load = [0] * world
+    shards: List[List[int]] = [[] for _ in range(world)]
+    for k in order:
+        r = min(range(world), key=lambda i: (load[i], i))
+        shards[r].append(k)
+        load[r] += int(sizes[k])
+    return [sorted(x) for x in shards]
+
+
 def compile_many(trees: Sequence[DepthTree], device: int = 0, workers: int = 8) -> List[Compiled]:
     with BatchCompiler(device, workers) as b:
         b.compile(trees)

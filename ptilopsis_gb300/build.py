@@ -29,7 +29,7 @@ CUDA_LIB = os.path.join(LIBDIR, "libptl_gb300.so")
 SYNTH_LIB = os.path.join(LIBDIR, "libptlsynth.so")
 HOSTMODEL_LIB = os.path.join(LIBDIR, "libptl_hostmodel.so")
 
-HEADERS = ["ptl_common.cuh", "ptl_stages.cuh", "ptl_sort.cuh", "ptl_ra.cuh", "ptl_kernels.cuh", "ptl_bpipe.h"]
+HEADERS = ["ptl_device.h", "ptl_common.cuh", "ptl_stages.cuh", "ptl_sort.cuh", "ptl_ra.cuh", "ptl_kernels.cuh", "ptl_bpipe.h"]
 
 
 def _nvcc() -> str:

@@ -298,7 +298,8 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
     if (count == 0) return PTL_OK;
     if (!trees) return PTL_BAD_ARGUMENT;
     if (count > (1u << 24)) return PTL_BAD_ARGUMENT;
-    BP_CU(cudaSetDevice(device));
+    const DeviceScope on_device(device);
+    BP_CU(on_device.err);
     {
         const char* pz = std::getenv("PTL_POISON_ARENAS");
         poison = pz && pz[0] == '1';
@@ -973,7 +974,8 @@ BatchPipeline* BatchPipeline::create(int device, int host_threads, ptl_status* s
     p->device = device;
     p->threads = std::max(1, host_threads);
     int lo = 0, hi = 0;  // stream priorities: numerically lower is more urgent
-    if (cudaSetDevice(device) != cudaSuccess || cudaDeviceGetStreamPriorityRange(&lo, &hi) != cudaSuccess ||
+    const DeviceScope on_device(device);
+    if (!on_device.ok() || cudaDeviceGetStreamPriorityRange(&lo, &hi) != cudaSuccess ||
         cudaStreamCreateWithPriority(&p->s, cudaStreamNonBlocking, urgent ? hi : lo) != cudaSuccess) {
         delete p;
         if (st) *st = PTL_CUDA_ERROR;

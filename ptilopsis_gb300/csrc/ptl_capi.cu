@@ -511,7 +511,8 @@ bool view_ok(const ptl_ast_view* tree) {
 ptl_status ptl_generator_upload(ptl_generator* g, const ptl_ast_view* tree) {
     if (!g || !view_ok(tree)) return PTL_BAD_ARGUMENT;
     if (tree->max_depth == 0) return PTL_INVALID_AST;
-    if (cudaSetDevice(g->device) != cudaSuccess) return fail(g, PTL_CUDA_ERROR, "cudaSetDevice");
+    const DeviceScope on_device(g->device);
+    if (!on_device.ok()) return fail(g, PTL_CUDA_ERROR, "cudaSetDevice");
     const cudaError_t e = upload_inputs(g, tree);
     if (e != cudaSuccess) return cuda_fail(g, e, "upload");
     return PTL_OK;
@@ -529,7 +530,8 @@ ptl_status ptl_generator_create(const ptl_ast_view* tree, int device, ptl_genera
     g->device = device;
     g->n = tree->n;
     g->max_depth = tree->max_depth;
-    cudaError_t e = cudaSetDevice(device);
+    const DeviceScope on_device(device);
+    cudaError_t e = on_device.err;
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = upload_inputs(g, tree);
     if (e == cudaSuccess) e = g->tables.ensure(sizeof(CodeTables), 1);
@@ -548,7 +550,8 @@ ptl_status ptl_generator_create(const ptl_ast_view* tree, int device, ptl_genera
 
 ptl_status ptl_generator_process(ptl_generator* g, int profile) {
     if (!g) return PTL_BAD_ARGUMENT;
-    if (cudaSetDevice(g->device) != cudaSuccess) return fail(g, PTL_CUDA_ERROR, "cudaSetDevice");
+    const DeviceScope on_device(g->device);
+    if (!on_device.ok()) return fail(g, PTL_CUDA_ERROR, "cudaSetDevice");
     const ptl_status st = run_pipeline(g, (profile & 1) != 0, (profile & 2) == 0, (profile & 4) != 0);
     if (st == PTL_OK) g->last_error.clear();
     return st;

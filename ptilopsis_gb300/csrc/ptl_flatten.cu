@@ -26,6 +26,7 @@
 #include <cstdint>
 
 #include "../../include/ptl_codegen.h"
+#include "ptl_device.h"
 
 namespace {
 
@@ -244,7 +245,8 @@ extern "C" ptl_status ptl_flatten(const ptl_tree_view* in, ptl_depth_tree_out* o
         !out->parent || !out->depth || !out->child_idx || !out->data)
         return PTL_BAD_ARGUMENT;
     const uint32_t n = static_cast<uint32_t>(n64);
-    if (cudaSetDevice(device) != cudaSuccess) return PTL_CUDA_ERROR;
+    const ptl::DeviceScope on_device(device);
+    if (!on_device.ok()) return PTL_CUDA_ERROR;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
 
     // device copies of the inputs (or the caller's device arrays) and of the outputs

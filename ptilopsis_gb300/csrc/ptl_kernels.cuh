@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 
+#include "ptl_device.h"
 #include "ptl_stages.cuh"
 #include "ptl_sort.cuh"
 

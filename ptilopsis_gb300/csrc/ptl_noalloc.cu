@@ -73,8 +73,20 @@ bool is_device_pointer(const void* p, int device) {
     return (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) && a.device == device;
 }
 
+// Once work is queued on the caller's stream, every return waits for it: the lock that
+// serialises calls on this device is released on return, and the next call (perhaps on
+// another stream) reuses the scratch at once.
+struct DrainOnReturn {
+    cudaStream_t s;
+    ~DrainOnReturn() {
+        cudaStreamSynchronize(s);
+        cudaGetLastError();
+    }
+};
+
 ptl_status run(const uint32_t* instr, const uint32_t* rd, const uint32_t* rs1, const uint32_t* rs2,
                uint32_t count, uint32_t* used_instrs, cudaStream_t s, unsigned char* base) {
+    DrainOnReturn drain{s};
     Prog P{};
     P.W = count;
     P.wb8 = count;
@@ -141,6 +153,13 @@ extern "C" ptl_status ptl_optimize_noalloc(const uint32_t* instr, const uint32_t
                           static_cast<const void*>(used_instrs)}) {
         if (!is_device_pointer(p, dev)) return PTL_BAD_ARGUMENT;
     }
+    // the call waits for its result on the host, which a capturing stream cannot do
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(static_cast<cudaStream_t>(stream), &cap) != cudaSuccess) {
+        cudaGetLastError();
+        return PTL_BAD_ARGUMENT;
+    }
+    if (cap != cudaStreamCaptureStatusNone) return PTL_BAD_ARGUMENT;
     std::lock_guard<std::mutex> hold(d.lock);
     return run(instr, rd, rs1, rs2, static_cast<uint32_t>(count), used_instrs, static_cast<cudaStream_t>(stream),
                d.base);

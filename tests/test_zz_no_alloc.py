@@ -120,3 +120,30 @@ def test_no_alloc_optimize_rejects_oversize_and_bad_pointers(built_cuda):
     assert f(None, vp(small[1].data_ptr()), vp(small[2].data_ptr()), vp(small[3].data_ptr()), 8,
              vp(out.data_ptr()), s) == 7
     assert _run(f, small, 0, out) == 0
+
+
+def test_no_alloc_optimize_refuses_a_capturing_stream(built_cuda):
+    """The call waits on the host for its changed flag, which a stream being captured
+    into a graph cannot do: it must return PTL_BAD_ARGUMENT and queue nothing."""
+    import torch
+    f = _entry()
+    dev = torch.device("cuda", 0)
+    from ptilopsis_gb300.synth import SynthParams, generate
+    instr, rd, rs1, rs2, used = _generator_stream(generate(SynthParams(seed=0x50544C48, n_functions=8)))
+    arrs = [torch.from_numpy(a.astype(np.uint32).view(np.int32)).to(dev) for a in (instr, rd, rs1, rs2)]
+    out = torch.zeros(len(used), dtype=torch.int32, device=dev)
+    assert _run(f, arrs, len(used), out) == 0  # the device's set-up happens outside the capture
+    np.testing.assert_array_equal(out.cpu().numpy().view(np.uint32), used)
+    out.fill_(0x5A5A5A5A)
+    torch.cuda.synchronize()
+    side = torch.cuda.Stream(device=dev)
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph, stream=side, capture_error_mode="relaxed"):
+        rc = _run(f, arrs, len(used), out, stream=side)
+    assert rc == 7  # PTL_BAD_ARGUMENT
+    torch.cuda.synchronize()
+    assert bool((out == 0x5A5A5A5A).all())
+    # and the stream works normally once the capture is over
+    assert _run(f, arrs, len(used), out, stream=side) == 0
+    side.synchronize()
+    np.testing.assert_array_equal(out.cpu().numpy().view(np.uint32), used)
