@@ -69,3 +69,31 @@ def ast_to_tree(ast):
 def reference_available() -> bool:
     from oracle import refbind
     return refbind.build()
+
+
+def manifest_large() -> dict:
+    with open(os.path.join(GOLDEN, "manifest_large.json")) as f:
+        return json.load(f)
+
+
+_large_cache: dict = {}
+
+
+def load_large(name: str):
+    """(Ast, manifest entry) of one of the reference's larger Pareas inputs, decoded from
+    tests/golden/large and checked against the CRCs of the tree the reference front end
+    built (tests/golden/codec.py)."""
+    if name not in _large_cache:
+        if GOLDEN not in sys.path:
+            sys.path.insert(0, GOLDEN)
+        import codec
+        from oracle.refbind import Ast
+        entry = next(e for e in manifest_large()["fixtures"] if e["name"] == name)
+        with open(os.path.join(GOLDEN, "large", name + ".tree.xz"), "rb") as f:
+            arrs = codec.decode(f.read())
+        got = codec.tree_crcs(*arrs)
+        assert got == entry["tree_crcs"], f"{name}: decoded tree differs from the reference front end's"
+        ast = Ast(*arrs, max_depth=entry["max_depth"])
+        _large_cache.clear()  # one large tree at a time
+        _large_cache[name] = (ast, entry)
+    return _large_cache[name]

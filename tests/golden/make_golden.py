@@ -3,7 +3,8 @@
 Run in the x86-64 build container, where the reference tree is mounted and
 oracle/ref/Makefile has built it into oracle/_ref:
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py            # small fixtures, synthetic seeds, tables
+    python tests/golden/make_golden.py --large    # the reference's larger Pareas inputs
 
 For each fixture it stores the DepthTree the reference front end (pareas-ast) builds
 from one of the reference's own Pareas test inputs, and what the reference generator
@@ -27,7 +28,7 @@ sys.path.insert(0, ROOT)
 
 from oracle import refbind  # noqa: E402
 
-REF = refbind.REF_ROOT_DEFAULT
+REF = refbind.ref_root_cached()
 FIXTURES = [
     "testfiles/pareas/basic/1.in",
     "testfiles/pareas/basic/2.in",
@@ -58,6 +59,47 @@ def table_crcs() -> dict:
         L.ptlref_table(w, a.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)))
         out[str(w)] = [int(n), crc(a)]
     return out
+
+
+# The reference's larger Pareas inputs (testfiles/pareas; basic/6,7 and shape/1,2 are not
+# shipped).  Their trees are kept in the compact form of codec.py, their outputs as CRCs:
+# the reference takes minutes per shape/* input at one worker thread, the restatement and
+# the GPU a second, so the tests recompute the outputs and compare CRCs.
+LARGE = (["basic/4", "basic/5"] + [f"funclen/{i}" for i in range(1, 9)] + [f"shape/{i}" for i in range(3, 7)])
+
+
+def _large_one(rel: str) -> dict:
+    import time
+    sys.path.insert(0, HERE)
+    import codec
+    t0 = time.time()
+    ast = refbind.parse_file(os.path.join(REF, "testfiles/pareas", rel + ".in"))
+    res = refbind.compile_ast(ast, threads=1, snapshots=True)
+    name = "pareas_" + rel.replace("/", "_")
+    with open(os.path.join(HERE, "large", name + ".tree.xz"), "wb") as f:
+        f.write(codec.encode(ast.type, ast.rtype, ast.parent, ast.data))
+    return {"name": name, "source": f"testfiles/pareas/{rel}.in", "n": int(ast.n), "max_depth": int(ast.max_depth),
+            "tree_crcs": codec.tree_crcs(ast.type, ast.rtype, ast.parent, ast.depth, ast.child_idx, ast.data),
+            "words": int(len(res.words)), "n_funcs": int(len(res.bufs["fn_id"])),
+            "snapshots": {k: [int(len(v)), crc(v)] for k, v in res.bufs.items()},
+            "reference_s": round(time.time() - t0, 1)}
+
+
+def main_large() -> None:
+    import multiprocessing as mp
+    if not refbind.build(REF):
+        raise SystemExit("the reference could not be built here (needs the reference tree on x86-64)")
+    os.makedirs(os.path.join(HERE, "large"), exist_ok=True)
+    # longest first (shape/* run minutes in the reference's register allocation)
+    order = sorted(LARGE, key=lambda r: (not r.startswith("shape"), r))
+    with mp.get_context("spawn").Pool(max(1, min(len(order), (os.cpu_count() or 2) - 1))) as pool:
+        entries = {}
+        for e in pool.imap_unordered(_large_one, order):
+            entries[e["name"]] = e
+            print(f"{e['source']}: {e['n']} nodes -> {e['words']} words ({e['reference_s']} s)", flush=True)
+    out = {"fixtures": [entries["pareas_" + r.replace("/", "_")] for r in LARGE]}
+    with open(os.path.join(HERE, "manifest_large.json"), "w") as f:
+        json.dump(out, f, indent=1, sort_keys=True)
 
 
 def main() -> None:
@@ -98,4 +140,7 @@ def main() -> None:
 
 
 if __name__ == "__main__":
-    main()
+    if "--large" in sys.argv[1:]:
+        main_large()
+    else:
+        main()

@@ -68,7 +68,7 @@ def test_port_matches_reference_stage_by_stage(built, rel):
     if not reference_available():
         pytest.skip("reference not buildable on this host")
     from oracle import portbind, refbind
-    ast = refbind.parse_file(os.path.join(refbind.REF_ROOT_DEFAULT, "testfiles/pareas", rel))
+    ast = refbind.parse_file(os.path.join(refbind.ref_root_cached(), "testfiles/pareas", rel))
     ref = refbind.compile_ast(ast, snapshots=True)
     port = portbind.compile_ast(ast, snapshots=True)
     for name in STAGE_BUFS:
@@ -97,3 +97,17 @@ def test_depth_sort_is_libstdcxx_sort(built):
     perm = portbind.depth_sort(keys)
     assert np.all(np.diff(keys[perm]) >= 0)
     assert sorted(perm.tolist()) == list(range(len(keys)))
+
+
+@pytest.mark.parametrize("fx", [f["name"] for f in __import__("conftest").manifest_large()["fixtures"]])
+def test_port_matches_reference_on_large_inputs(built, fx):
+    """The reference's larger Pareas inputs (basic/4-5, funclen/1-8, shape/3-6; deep
+    shape/* trees exercise the lane-0 coupling of register allocation): every one of the
+    36 stage arrays of the restatement against the CRCs of the reference's own run."""
+    from conftest import load_large
+    from oracle import portbind
+    ast, entry = load_large(fx)
+    res = portbind.compile_ast(ast, snapshots=True)
+    assert len(res.words) == entry["words"]
+    for name, (length, c) in entry["snapshots"].items():
+        assert len(res.bufs[name]) == length and crc(res.bufs[name]) == c, name
