@@ -444,7 +444,7 @@ def run_batched(args):
     for _ in range(args.warmup):
         bc.compile(trees)
     barrier()
-    dev_ms, wall_ms, stage_sum, host_parts = [], [], np.zeros(7), np.zeros(3)
+    dev_ms, wall_ms, sort_ms, stage_sum, host_parts = [], [], [], np.zeros(7), np.zeros(3)
     launches0 = kernel_launches()
     with ClockSampler(local) as clocks:
         for _ in range(args.steps):
@@ -456,6 +456,7 @@ def run_batched(args):
             hp = bc.host_ns()
             host_parts += np.array([hp["gather_ns"], hp["h2d_ns"], hp["d2h_ns"]], dtype=np.float64)
             dev_ms.append(bc.device_ns() / 1e6)
+            sort_ms.append(bc.depth_sort_ns() / 1e6)
         barrier()
     launches = (kernel_launches() - launches0) // args.steps
     ms = max_over_ranks(float(np.mean(dev_ms)))
@@ -483,6 +484,7 @@ def run_batched(args):
                 "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind, "traffic": None,
                 "algorithmic_bytes_per_launch": int(alg),
                 "stage_ms": {s: round(float(v), 3) for s, v in zip(STAGES, stage_ms)},
+                "depth_sort_ms": round(float(np.mean(sort_ms)), 3),  # part of isn_gen
                 **stage_rooflines(stage_ms, tot, peak)}
 
     # the plain pipeline on a sample of the same programs, one at a time

@@ -169,6 +169,10 @@ ptl_status ptl_batch_stage_ns(const ptl_batch* batch, uint64_t ns[7]);
 /* Device time of the last compile from its inputs on the device to its outputs complete
  * (before the output copy), in ns. */
 uint64_t ptl_batch_device_ns(const ptl_batch* batch);
+/* Device time of the last compile's depth sort (isn_gen's ordering of nodes by depth,
+ * rv_generator_avx.cpp:526-566), in ns: the part of the isn_gen stage time that goes to
+ * the sort rather than to the instruction writes. */
+uint64_t ptl_batch_depth_sort_ns(const ptl_batch* batch);
 /* Bytes copied host-to-device and device-to-host by the last compile. */
 ptl_status ptl_batch_copied_bytes(const ptl_batch* batch, uint64_t* h2d, uint64_t* d2h);
 /* Detail of the last batch-wide failure. */
@@ -234,6 +238,19 @@ ptl_status ptl_flatten(const ptl_tree_view* in, ptl_depth_tree_out* out, int dev
 ptl_status ptl_to_asm(const uint32_t* words, size_t n, char* out, size_t cap, size_t* len);
 ptl_status ptl_disassemble(const uint32_t* words, size_t n, uint64_t start_addr, const uint64_t* func_starts,
                            size_t nfunc, char* out, size_t cap, size_t* len);
+
+/* ---- Object output.  No counterpart in the reference, which writes the raw words only
+ * (rv_generator::to_binary, src/codegen/rv_generator.cpp:116-119).  Wraps the words and
+ * the function table (ptl_generator_function_table's starts and ends, in words, in
+ * address order) into an ELF64 little-endian RISC-V relocatable object: .text holds the
+ * words, and each function is a global STT_FUNC symbol "funcN" (N = its position in the
+ * table, the labels of ptl_disassemble) with value start*4 and size (end-start)*4.  The
+ * generator's jumps are pc-relative within the program, so there are no relocations.
+ * Writes the object to out (capacity bytes) and its size to *size; out = NULL only
+ * measures.  PTL_BAD_ARGUMENT for a table that is not in address order or runs past the
+ * words, or a capacity below the size. */
+ptl_status ptl_write_elf(const uint32_t* words, size_t n_words, const uint32_t* func_starts,
+                         const uint32_t* func_ends, size_t n_funcs, uint8_t* out, size_t capacity, size_t* size);
 
 /* ---- Compile server.  No counterpart in the reference.  Continuous batching over
  * `slots` lanes (1..16), each a batched pipeline with its own stream and resident arenas:

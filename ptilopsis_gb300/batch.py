@@ -44,6 +44,8 @@ def _bind(L):
     L.ptl_batch_set_regalloc_share.argtypes = [vp, ctypes.c_double]
     L.ptl_batch_device_ns.argtypes = [vp]
     L.ptl_batch_device_ns.restype = u64
+    L.ptl_batch_depth_sort_ns.argtypes = [vp]
+    L.ptl_batch_depth_sort_ns.restype = u64
     L.ptl_batch_destroy.argtypes = [vp]
     L.ptl_batch_destroy.restype = None
     L.ptl_server_create.argtypes = [ctypes.c_int, ctypes.c_int, u64, ctypes.POINTER(vp)]
@@ -215,6 +217,10 @@ class BatchCompiler:
         """Device time of the last compile from its inputs on the device to its outputs
         complete (before the output copy)."""
         return int(self._lib.ptl_batch_device_ns(self._h))
+
+    def depth_sort_ns(self) -> int:
+        """Device time of the last compile's depth sort (part of the isn_gen stage)."""
+        return int(self._lib.ptl_batch_depth_sort_ns(self._h))
 
     def sizes(self, k: int) -> dict:
         """Program k's nodes and word counts after isn_gen, regalloc and fix_jumps."""

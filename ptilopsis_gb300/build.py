@@ -59,7 +59,7 @@ def _src(*names: str) -> list[str]:
 def build_cuda(force: bool = False) -> str:
     hdrs = _src(*HEADERS) + [os.path.join(ROOT, "include", "ptl_codegen.h")]
     units = [("ptl_kernels.cu", "nvcc"), ("ptl_capi.cu", "nvcc"), ("ptl_noalloc.cu", "nvcc"), ("ptl_bpipe.cu", "nvcc"),
-             ("ptl_flatten.cu", "nvcc"), ("ptl_tables.cpp", "cxx"), ("ptl_batch.cpp", "cxx"), ("ptl_disasm.cpp", "cxx")]
+             ("ptl_flatten.cu", "nvcc"), ("ptl_tables.cpp", "cxx"), ("ptl_batch.cpp", "cxx"), ("ptl_disasm.cpp", "cxx"), ("ptl_elf.cpp", "cxx")]
     all_src = _src(*(u for u, _ in units)) + hdrs
     if not force and _newer(CUDA_LIB, all_src):
         return CUDA_LIB

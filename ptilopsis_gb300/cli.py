@@ -12,8 +12,9 @@ parent's children; save_unordered writes it): it is flattened on the GPU first
 words (to_binary) to ./c.out, or with -S assembly text (to_asm) to <infile stem>.s; -o -
 writes to stdout.  -p prints the reference's profiling CSV (stage names, then
 nanoseconds; src/codegen/rv_generator.cpp:150-162) with the GPU's per-stage device times.
--t, -m, -b and -i set how the reference schedules its CPU threads; they are accepted and
-have no effect here.  -s (the scalar generator) is not part of this implementation.
+--elf <file> also writes the program as an ELF64 RISC-V relocatable object (an option the
+reference does not have; ptl_write_elf).  -t, -m, -b and -i set how the reference
+schedules its CPU threads; they are accepted and have no effect here.  -s (the scalar generator) is not part of this implementation.
 """
 from __future__ import annotations
 
@@ -71,6 +72,7 @@ def _parser() -> argparse.ArgumentParser:
     ap.add_argument("-i", "--mininstr", type=int, default=0, help="accepted for compatibility; no effect")
     ap.add_argument("-p", "--profile", action="store_true", help="profiling CSV to stdout")
     ap.add_argument("--device", type=int, default=0, help="CUDA device")
+    ap.add_argument("--elf", dest="elf", help="also write an ELF64 RISC-V relocatable object (one symbol per function)")
     return ap
 
 
@@ -105,6 +107,9 @@ def main(argv: Optional[List[str]] = None) -> int:
         if args.debug or args.tree:
             words = gen.get_instructions()
             print(f"Number of nodes: {tree.n}\nMax depth: {tree.max_depth}\nOutput words: {len(words)}")
+        if args.elf:
+            with open(args.elf, "wb") as f:
+                f.write(gen.to_elf())
         if outfile == "-":
             if args.asm:
                 sys.stdout.write(gen.to_asm())

@@ -282,6 +282,12 @@ class RvGenerator:
         """rv_generator::to_asm (src/codegen/rv_generator.cpp:121-127): one line per word."""
         return to_asm(self.get_instructions())
 
+    def to_elf(self) -> bytes:
+        """The words and function table as an ELF64 RISC-V relocatable object
+        (ptl_write_elf; the reference writes raw words only)."""
+        t = self.function_table()
+        return to_elf(self.get_instructions(), t["starts"], t["ends"])
+
     def close(self) -> None:
         if self._h:
             self._lib.ptl_generator_destroy(self._h)
@@ -353,6 +359,31 @@ def disassemble(words, start_addr: int = 0, func_starts=()) -> str:
     L.ptl_disassemble.restype = ctypes.c_int
     return _text(L.ptl_disassemble, w.ctypes.data, w.shape[0], start_addr, f.ctypes.data, f.shape[0])
 
+
+def to_elf(words, func_starts, func_ends) -> bytes:
+    """An ELF64 little-endian RISC-V relocatable object: .text holds the words, and
+    function k of the table (starts/ends in words, address order) is the global
+    function symbol "func<k>" (ptl_write_elf)."""
+    L = lib()
+    w = np.ascontiguousarray(words, np.uint32)
+    s = np.ascontiguousarray(func_starts, np.uint32)
+    e = np.ascontiguousarray(func_ends, np.uint32)
+    if s.shape != e.shape:
+        raise ValueError("func_starts and func_ends differ in length")
+    vp = ctypes.c_void_p
+    L.ptl_write_elf.argtypes = [vp, ctypes.c_size_t, vp, vp, ctypes.c_size_t, vp, ctypes.c_size_t,
+                                ctypes.POINTER(ctypes.c_size_t)]
+    L.ptl_write_elf.restype = ctypes.c_int
+    n = ctypes.c_size_t()
+    args = (w.ctypes.data, w.shape[0], s.ctypes.data, e.ctypes.data, s.shape[0])
+    st = L.ptl_write_elf(*args, None, 0, ctypes.byref(n))
+    if st != 0:
+        raise PtlError(st, "ptl_write_elf")
+    buf = (ctypes.c_uint8 * max(n.value, 1))()
+    st = L.ptl_write_elf(*args, ctypes.addressof(buf), n.value, ctypes.byref(n))
+    if st != 0:
+        raise PtlError(st, "ptl_write_elf")
+    return bytes(buf)[:n.value]
 
 
 class _TreeView(ctypes.Structure):

@@ -128,6 +128,7 @@ extern "C" ptl_status ptl_batch_stage_ns(const ptl_batch* b, uint64_t ns[7]) {
 }
 
 extern "C" uint64_t ptl_batch_device_ns(const ptl_batch* b) { return b ? b->pipe->device_ns() : 0; }
+extern "C" uint64_t ptl_batch_depth_sort_ns(const ptl_batch* b) { return b ? b->pipe->depth_sort_ns() : 0; }
 
 extern "C" ptl_status ptl_batch_copied_bytes(const ptl_batch* b, uint64_t* h2d, uint64_t* d2h) {
     if (!b) return PTL_BAD_ARGUMENT;

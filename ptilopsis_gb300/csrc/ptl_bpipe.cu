@@ -122,6 +122,7 @@ public:
     cudaStream_t s = nullptr;
     cudaEvent_t ev[8] = {};
     cudaEvent_t ev_in = nullptr, ev_out0 = nullptr, ev_out1 = nullptr;  // input copy start, output copy
+    cudaEvent_t ev_sort0 = nullptr, ev_sort1 = nullptr;  // the depth sort inside isn_gen
     uint64_t hns[3] = {0, 0, 0};
     uint64_t ns[7] = {0, 0, 0, 0, 0, 0, 0};
     uint64_t h2d = 0, d2h = 0;
@@ -154,7 +155,7 @@ public:
         d_gp.release();
         for (auto& e : ev)
             if (e) cudaEventDestroy(e);
-        for (cudaEvent_t e : {ev_in, ev_out0, ev_out1})
+        for (cudaEvent_t e : {ev_in, ev_out0, ev_out1, ev_sort0, ev_sort1})
             if (e) cudaEventDestroy(e);
         if (s) cudaStreamDestroy(s);
     }
@@ -284,6 +285,8 @@ public:
     }
 
     ptl_status compile(const ptl_ast_view* trees, size_t count, std::vector<BatchResult>& res) override;
+    uint64_t sort_ns = 0;  // device time of the last compile's depth sort
+    uint64_t depth_sort_ns() const override { return sort_ns; }
     uint64_t device_ns() const override {
         float ms = 0;
         return cudaEventElapsedTime(&ms, ev[0], ev[7]) == cudaSuccess ? static_cast<uint64_t>(ms * 1e6) : 0;
@@ -325,7 +328,7 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
     }
     for (auto& e : ev)
         if (!e) BP_CU(cudaEventCreate(&e));
-    for (cudaEvent_t* e : {&ev_in, &ev_out0, &ev_out1})
+    for (cudaEvent_t* e : {&ev_in, &ev_out0, &ev_out1, &ev_sort0, &ev_sort1})
         if (!*e) BP_CU(cudaEventCreate(e));
     for (auto& x : hns) x = 0;
 
@@ -704,6 +707,7 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
         ss.local = sort_local.at<uint32_t>();
         ss.equal = sort_equal.at<uint32_t>();
         const uint32_t t_n2 = tiles(4, n, elem_tile);
+        BP_CU(cudaEventRecord(ev_sort0, s));
         batch_sort_keys(bl(4), t_n2, sa.at<unsigned long long>(), a_off.at<uint64_t>(), false);
         BP_CU(cudaMemsetAsync(counters.p, 0, 64, s));
         SortSeg* up_segs = reinterpret_cast<SortSeg*>(h_small.at<uint8_t>(small_up_off + 2 * B * 8));
@@ -732,6 +736,7 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
         BP_CU(run_sort_rounds(ss, static_cast<uint32_t>(segs.size()), min_lg > lb ? min_lg - lb : 1, 2 * max_lg + 4,
                               sort_err.at<ErrorWord>(), s, &rounds, &sort_graph));
         batch_sort_keys(bl(4), t_n2, sa.at<unsigned long long>(), a_off.at<uint64_t>(), true);
+        BP_CU(cudaEventRecord(ev_sort1, s));
         batch_stage(BatchStage::Gen, bl(4), t_n2, nullptr);
         {
             ErrorWord se{};
@@ -958,6 +963,7 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
         }
         ns[6] = 0;  // postprocess is fused into fix_jumps
         if (cudaEventElapsedTime(&ms, ev_in, ev[0]) == cudaSuccess) hns[1] = static_cast<uint64_t>(ms * 1e6);
+        sort_ns = cudaEventElapsedTime(&ms, ev_sort0, ev_sort1) == cudaSuccess ? static_cast<uint64_t>(ms * 1e6) : 0;
         if (cudaEventElapsedTime(&ms, ev_out0, ev_out1) == cudaSuccess) hns[2] = static_cast<uint64_t>(ms * 1e6);
     }
     return PTL_OK;

@@ -35,6 +35,8 @@ public:
     // Device time of the last compile from its inputs on the device to its outputs
     // complete (before the output copy), ns.
     virtual uint64_t device_ns() const = 0;
+    // Device time of the last compile's depth sort (part of isn_gen), ns.
+    virtual uint64_t depth_sort_ns() const = 0;
     // Host-to-device and device-to-host bytes of the last compile.
     virtual void copied_bytes(uint64_t* h2d, uint64_t* d2h) const = 0;
     // Host-side parts of the last compile, ns: gathering the inputs into pinned memory,

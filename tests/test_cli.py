@@ -53,6 +53,10 @@ def test_cli_compiles_like_the_reference(built_cuda, tmp_path):
     r = _run(["prog.npz", "-S"], tmp_path)
     assert r.returncode == 0, r.stderr
     assert (tmp_path / "prog.s").read_text() == to_asm(golden["words"])
+    from ptilopsis_gb300 import to_elf
+    r = _run(["prog.npz", "--elf", "prog.o"], tmp_path)
+    assert r.returncode == 0, r.stderr
+    assert (tmp_path / "prog.o").read_bytes() == to_elf(golden["words"], golden["fn_start"], golden["fn_end"])
     r = _run(["-", "-S", "-o", "-"], tmp_path, stdin=(tmp_path / "prog.npz").read_bytes())
     assert r.returncode == 0 and r.stdout.decode() == to_asm(golden["words"])
     # the parser's tree in a shuffled node order, flattened on the GPU before the compile
