@@ -228,7 +228,6 @@ struct Model {
         for (uint32_t i = 0; i < nb8; ++i) reach |= st_ingest(P, i);
         if (!check()) return err.code;
         if (!reach) return ST_INVALID_AST;
-        for (uint32_t i = 0; i < nb8; ++i) st_pre_args(P, i);
         for (uint32_t i = 0; i < nb8; ++i) st_pre_lists(P, i);
         for (uint32_t i = 0; i < nb8; ++i) st_pre_float(P, i);
         for (uint32_t i = 0; i < nb8; ++i) st_pre_float_apply(P, i);

@@ -60,7 +60,6 @@ inline unsigned grid_for(uint64_t n, int threads = kThreads) {
 __global__ void k_ingest(Prog P) {
     PTL_FOR(i, P.nb8) if (st_ingest(P, i)) P.flags[3] = 1u;
 }
-__global__ void k_pre_args(Prog P) { PTL_FOR(i, P.nb8) st_pre_args(P, i); }
 __global__ void k_pre_lists(Prog P) { PTL_FOR(i, P.nb8) st_pre_lists(P, i); }
 __global__ void k_pre_float(Prog P) { PTL_FOR(i, P.nb8) st_pre_float(P, i); }
 __global__ void k_pre_float_apply(Prog P) { PTL_FOR(i, P.nb8) st_pre_float_apply(P, i); }
@@ -85,6 +84,46 @@ __device__ __forceinline__ uint32_t warp_incl_scan(uint32_t x) {
         if (lane >= static_cast<uint32_t>(d)) x += y;
     }
     return x;
+}
+
+// The look-back of a tile past its program's first tile, by one whole warp: lane k reads
+// the status of tile j-k, so each round trip to L2 examines 32 predecessors.  Partial
+// aggregates (flag 1) are summed up to the nearest tile that has published its inclusive
+// prefix (flag 2); a window with a tile that has published nothing yet (flag 0) in front
+// of that one is read again.  Every lane gets the exclusive prefix.  Bounded like every
+// device wait: after kSpinLimit re-reads it records ST_DEVICE_TIMEOUT and returns what it
+// has, so the tile still publishes and no successor waits forever.
+__device__ uint32_t warp_lookback(unsigned long long* status, uint32_t tile, uint32_t first, ErrorWord* err) {
+    constexpr unsigned full = 0xFFFFFFFFu;
+    const uint32_t lane = threadIdx.x & 31u;
+    uint32_t prefix = 0, spins = 0;
+    int64_t j = static_cast<int64_t>(tile) - 1;
+    for (;;) {
+        const int64_t idx = j - static_cast<int64_t>(lane);
+        // tiles before the first one never matter: the first tile publishes its inclusive
+        // prefix directly and is met before them
+        const unsigned long long st = idx >= static_cast<int64_t>(first)
+                                          ? *reinterpret_cast<volatile unsigned long long*>(&status[idx])
+                                          : (2ull << 32);
+        const uint32_t flag = static_cast<uint32_t>(st >> 32);
+        const unsigned incl = __ballot_sync(full, flag == 2u);
+        const unsigned none = __ballot_sync(full, flag == 0u);
+        const uint32_t k = incl ? static_cast<uint32_t>(__ffs(static_cast<int>(incl)) - 1) : 31u;
+        const unsigned upto = k == 31u ? full : ((1u << (k + 1u)) - 1u);
+        if (none & upto) {
+            if (++spins > kSpinLimit) {
+                if (lane == 0) record_error(err, ST_DEVICE_TIMEOUT, W_SCAN, tile);
+                return prefix;
+            }
+            continue;
+        }
+        uint32_t v = lane <= k ? static_cast<uint32_t>(st) : 0u;
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1) v += __shfl_xor_sync(full, v, d);
+        prefix += v;
+        if (incl) return prefix;
+        j -= 32;
+    }
 }
 
 template <class Load, class Store>
@@ -114,32 +153,15 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(Load load, Store store, u
         const uint32_t incl = warp_incl_scan(t);
         if (lane < kWarps) s_warp[lane] = incl - t;
         const uint32_t aggregate = __shfl_sync(0xFFFFFFFFu, incl, kWarps - 1);
-        if (lane == 0) {
-            uint32_t prefix = 0;
-            if (tile == 0) {
-                atomicExch(&sc.status[0], (2ull << 32) | aggregate);
-            } else {
-                atomicExch(&sc.status[tile], (1ull << 32) | aggregate);
-                int64_t j = static_cast<int64_t>(tile) - 1;
-                uint32_t spins = 0;
-                while (j >= 0) {
-                    const unsigned long long st = *reinterpret_cast<volatile unsigned long long*>(&sc.status[j]);
-                    const uint32_t flag = static_cast<uint32_t>(st >> 32);
-                    if (flag == 0) {
-                        if (++spins > kSpinLimit) {
-                            record_error(err, ST_DEVICE_TIMEOUT, W_SCAN, tile);
-                            break;
-                        }
-                        continue;
-                    }
-                    prefix += static_cast<uint32_t>(st);
-                    if (flag == 2) break;
-                    --j;
-                }
-                atomicExch(&sc.status[tile], (2ull << 32) | (prefix + aggregate));
-            }
-            s_prefix = prefix;
+        uint32_t prefix = 0;
+        if (tile == 0) {
+            if (lane == 0) atomicExch(&sc.status[0], (2ull << 32) | aggregate);
+        } else {
+            if (lane == 0) atomicExch(&sc.status[tile], (1ull << 32) | aggregate);
+            prefix = warp_lookback(sc.status, tile, 0u, err);
+            if (lane == 0) atomicExch(&sc.status[tile], (2ull << 32) | (prefix + aggregate));
         }
+        if (lane == 0) s_prefix = prefix;
     }
     __syncthreads();
     const uint32_t base = s_prefix + s_warp[warp];
@@ -1403,8 +1425,6 @@ void launch_ingest(const Prog& P, cudaStream_t s) {
 
 void launch_preprocess(const Prog& P, cudaStream_t s) {
     g_launches++;
-    k_pre_args<<<grid_for(P.nb8), kThreads, 0, s>>>(P);
-    g_launches++;
     k_pre_lists<<<grid_for(P.nb8), kThreads, 0, s>>>(P);
     g_launches++;
     k_pre_float<<<grid_for(P.nb8), kThreads, 0, s>>>(P);
@@ -1804,7 +1824,6 @@ __global__ void __launch_bounds__(kThreads) k_batch(const Prog* progs, const uin
 #define PTL_BATCH_OP(NAME, COUNT, BODY) PTL_BATCH_OP_V(NAME, true, COUNT, BODY)
 
 PTL_BATCH_OP_V(BIngest, false, P.nb8, if (st_ingest(P, i)) P.flags[3] = 1u)
-PTL_BATCH_OP_V(BPreArgs, false, P.nb8, st_pre_args(P, i))
 PTL_BATCH_OP_V(BPreLists, false, P.nb8, st_pre_lists(P, i))
 PTL_BATCH_OP_V(BPreFloat, false, P.nb8, st_pre_float(P, i))
 PTL_BATCH_OP_V(BPreFloatApply, false, P.nb8, st_pre_float_apply(P, i))
@@ -2147,32 +2166,15 @@ __global__ void __launch_bounds__(kScanThreads) k_bscan(const Prog* progs, const
         const uint32_t incl = warp_incl_scan(t);
         if (lane < kWarps) s_warp[lane] = incl - t;
         const uint32_t aggregate = __shfl_sync(0xFFFFFFFFu, incl, kWarps - 1);
-        if (lane == 0) {
-            uint32_t prefix = 0;
-            if (tile == first) {
-                atomicExch(&sc.status[tile], (2ull << 32) | aggregate);
-            } else {
-                atomicExch(&sc.status[tile], (1ull << 32) | aggregate);
-                int64_t j = static_cast<int64_t>(tile) - 1;
-                uint32_t spins = 0;
-                while (j >= static_cast<int64_t>(first)) {
-                    const unsigned long long st = *reinterpret_cast<volatile unsigned long long*>(&sc.status[j]);
-                    const uint32_t flag = static_cast<uint32_t>(st >> 32);
-                    if (flag == 0) {
-                        if (++spins > kSpinLimit) {
-                            record_error(P.err, ST_DEVICE_TIMEOUT, W_SCAN, tile);
-                            break;
-                        }
-                        continue;
-                    }
-                    prefix += static_cast<uint32_t>(st);
-                    if (flag == 2) break;
-                    --j;
-                }
-                atomicExch(&sc.status[tile], (2ull << 32) | (prefix + aggregate));
-            }
-            s_prefix = prefix;
+        uint32_t prefix = 0;
+        if (tile == first) {
+            if (lane == 0) atomicExch(&sc.status[tile], (2ull << 32) | aggregate);
+        } else {
+            if (lane == 0) atomicExch(&sc.status[tile], (1ull << 32) | aggregate);
+            prefix = warp_lookback(sc.status, tile, first, P.err);
+            if (lane == 0) atomicExch(&sc.status[tile], (2ull << 32) | (prefix + aggregate));
         }
+        if (lane == 0) s_prefix = prefix;
     }
     __syncthreads();
     const uint32_t base = s_prefix + s_warp[warp];
@@ -2271,7 +2273,6 @@ void batch_stage(BatchStage st, const BatchLaunch& bl, uint32_t total, uint32_t*
     switch (st) {
         case BatchStage::Ingest: batch_launch(bl, total, BIngest{}); break;
         case BatchStage::Preprocess:
-            batch_launch(bl, total, BPreArgs{});
             batch_launch(bl, total, BPreLists{});
             batch_launch(bl, total, BPreFloat{});
             batch_launch(bl, total, BPreFloatApply{});

@@ -92,11 +92,17 @@ PTL_HD void ra_free_function_cached(const Prog& P, const SymCache& c, uint32_t s
     unsigned long long lifetime = 0x1Full;
     const uint32_t g1 = f / 8u + 1u;
     const uint32_t start = P.fn_start0[f], size = P.fn_size0[f];
-    RaStep next;
+    // Each thread walks its own function, so a warp's loads of one step touch 32 lines:
+    // the instruction of step i+2 is loaded during step i, two steps of work ahead of
+    // its use, which covers the latency of a read that misses the L1.
+    RaStep next, next2;
     bool have = ra_load_at(P, start, size, 0, next);
+    bool have2 = ra_load_at(P, start, size, 1, next2);
     for (uint32_t i = 0; have; ++i) {
         RaStep S = next;
-        have = ra_load_at(P, start, size, i + 1, next);  // issue the next step's loads early
+        next = next2;
+        have = have2;
+        have2 = ra_load_at(P, start, size, i + 2, next2);
         if (S.ins == 0x000000EFu || !ra_own_in(start, size, S.r1) || !ra_own_in(start, size, S.r2) ||
             !ra_own_in(start, size, S.ord)) {
             record_error(P.err, ST_UNSUPPORTED, W_RA1, start + i);

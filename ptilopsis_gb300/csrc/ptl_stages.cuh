@@ -167,11 +167,43 @@ struct Prog {
     uint32_t* flags;      // [0] optimize changed, [1] [2] regalloc checks, [3] a node at max_depth
 };
 
+// Function-argument registers and stack slots, rv_generator_avx.cpp:126-213, on one
+// node's type t, data type rt, data nd and child index ci.  The reference runs it over
+// 8-lane blocks, but every lane reads and writes only its own node (non-argument lanes
+// keep their values), so the input pass applies it as it writes each node.
+PTL_HD void pre_args(uint32_t& t, uint32_t rt, uint32_t& nd, uint32_t ci) {
+    if ((t & 0xF0u) != 0xF0u) return;
+    const bool is_float = rt == DT_FLOAT || rt == DT_FLOAT_REF;
+    const bool is_int = !is_float;
+    {
+        const uint32_t float_data = is_float ? nd : 0u;
+        const bool comp = s32(float_data) > 7;
+        uint32_t reg_offset = (ci - float_data) + float_data - 8u;
+        const bool on_stack = (s32(reg_offset) > 7) && comp;
+        const bool as_int = !on_stack && comp;
+        if (on_stack) t |= 0b10u;
+        if (as_int) t |= 0b01u;
+        if (on_stack) reg_offset -= 8u;
+        if (comp) nd = reg_offset;
+    }
+    {
+        const uint32_t int_data = is_int ? nd : 0u;
+        const uint32_t float_args = ci - int_data;
+        uint32_t reg_offset = int_data + (float_args - ((s32(float_args) > 7) ? 8u : 0u));
+        // The reference ANDs its comparison mask with the data value itself (:198).
+        const uint32_t on_stack = (s32(reg_offset) > 7 ? 0xFFFFFFFFu : 0u) & int_data;
+        t |= on_stack & 0b10u;
+        reg_offset -= 8u & on_stack;
+        if (is_int) nd = reg_offset;
+    }
+}
+
 // ================================================================== input checks and copy
 // One pass over the six input arrays: the DepthTree contract (post-order, one root last,
 // consistent depths, in-range types; a bad node records INVALID_AST with its index), then
-// the constructor copy and the Pareas -> rv type map (src/codegen/rv_generator.cpp:41-67);
-// lanes past n become zero.  Returns whether node i is valid and sits at max_depth: with
+// the constructor copy and the Pareas -> rv type map (src/codegen/rv_generator.cpp:41-67)
+// and preprocess's function-argument pass (pre_args); lanes past n become zero.  Returns
+// whether node i is valid and sits at max_depth: with
 // every node one level below its parent, depths 0..max_depth are all populated exactly
 // when some node reaches max_depth.
 PTL_HD bool st_ingest(const Prog& P, uint32_t i) {
@@ -195,48 +227,16 @@ PTL_HD bool st_ingest(const Prog& P, uint32_t i) {
         if (!bad) bad |= d - 1 != P.in_depth[p];  // d >= 0 here
     }
     if (bad) record_error(P.err, ST_INVALID_AST, 0, i);
-    P.nt[i] = ty < kNumPareasTypes ? P.tab.t->pareas_to_rv[ty] : 0u;
+    uint32_t t = ty < kNumPareasTypes ? P.tab.t->pareas_to_rv[ty] : 0u;
+    uint32_t nd = data;
+    pre_args(t, rty, nd, u32(c));  // preprocess's first pass, fused
+    P.nt[i] = t;
     P.rt[i] = rty;
     P.par[i] = p;
     P.ci[i] = c;
-    P.nd1[i] = data;
+    P.nd1[i] = nd;
     P.dep[i] = d;
     return !bad && static_cast<uint32_t>(d) == P.max_depth;
-}
-
-// Function-argument registers and stack slots, rv_generator_avx.cpp:126-213.
-// Per lane: non-argument lanes of a block keep their values.
-PTL_HD void st_pre_args(const Prog& P, uint32_t i) {
-    uint32_t t = P.nt[i];
-    if ((t & 0xF0u) != 0xF0u) return;
-    const uint32_t rt = P.rt[i];
-    const bool is_float = rt == DT_FLOAT || rt == DT_FLOAT_REF;
-    const bool is_int = !is_float;
-    uint32_t nd = P.nd1[i];
-    const uint32_t ci = u32(P.ci[i]);
-    {
-        const uint32_t float_data = is_float ? nd : 0u;
-        const bool comp = s32(float_data) > 7;
-        uint32_t reg_offset = (ci - float_data) + float_data - 8u;
-        const bool on_stack = (s32(reg_offset) > 7) && comp;
-        const bool as_int = !on_stack && comp;
-        if (on_stack) t |= 0b10u;
-        if (as_int) t |= 0b01u;
-        if (on_stack) reg_offset -= 8u;
-        if (comp) nd = reg_offset;
-    }
-    {
-        const uint32_t int_data = is_int ? nd : 0u;
-        const uint32_t float_args = ci - int_data;
-        uint32_t reg_offset = int_data + (float_args - ((s32(float_args) > 7) ? 8u : 0u));
-        // The reference ANDs its comparison mask with the data value itself (:198).
-        const uint32_t on_stack = (s32(reg_offset) > 7 ? 0xFFFFFFFFu : 0u) & int_data;
-        t |= on_stack & 0b10u;
-        reg_offset -= 8u & on_stack;
-        if (is_int) nd = reg_offset;
-    }
-    P.nt[i] = t;
-    P.nd1[i] = nd;
 }
 
 // Value the call-list pass stores into lane i (or the lane's own data):
