@@ -333,7 +333,7 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
     for (auto& x : hns) x = 0;
 
     // ---- small per-program state and the pinned small area
-    constexpr int kTables = 23, kLists = 4;  // table slots 0..22 are used
+    constexpr int kTables = 22, kLists = 4;  // table slots 0..21 are used
     small_progs_off = static_cast<size_t>(kTables) * (B + 1) * 4;
     small_meta_off = small_progs_off + B * sizeof(Prog);
     small_err_off = small_meta_off + B * 16;
@@ -825,25 +825,18 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
             max_g0 = std::max<uint32_t>(max_g0, static_cast<uint32_t>(g0));
         }
         upload_progs();
-        // the independent functions of all programs first (one launch), then the lane-0
-        // passes (one persistent launch, one item per program), longest programs (most
-        // steps) first in both
+        // independent functions and lane-0 passes of all programs in one persistent launch,
+        // longest programs (most steps) first
         std::stable_sort(lane0_list.begin(), lane0_list.end(), [&](uint32_t x, uint32_t y) { return S[x] > S[y]; });
-        const uint32_t free_T = batch_ra_free_tile();
-        uint32_t free_tiles = 0;
-        {
-            uint32_t* h = table_slot(22);
-            for (size_t k = 0; k < lane0_list.size(); ++k) {
-                h[k] = free_tiles;
-                free_tiles += static_cast<uint32_t>((nfree[lane0_list[k]] + free_T - 1) / free_T);
-            }
-            for (size_t k = lane0_list.size(); k <= B; ++k) h[k] = free_tiles;
-            BP_CU(cudaMemcpyAsync(dtable_slot(22), h, (B + 1) * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
-        }
-        const uint32_t ra_items = static_cast<uint32_t>(lane0_list.size());  // one lane-0 item per program
+        const uint32_t ra_T = batch_ra_threads(max_g0);
+        uint32_t ra_items = 0;  // per program: its independent-function tiles, then its lane-0 pass
         {
             uint32_t* h = table_slot(8);
-            for (size_t k = 0; k <= B; ++k) h[k] = static_cast<uint32_t>(std::min<size_t>(k, lane0_list.size()));
+            for (size_t k = 0; k < lane0_list.size(); ++k) {
+                h[k] = ra_items;
+                ra_items += static_cast<uint32_t>((nfree[lane0_list[k]] + ra_T - 1) / ra_T) + 1u;
+            }
+            for (size_t k = lane0_list.size(); k <= B; ++k) h[k] = ra_items;
             BP_CU(cudaMemcpyAsync(dtable_slot(8), h, (B + 1) * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
         }
         const uint32_t* d_lane0 = upload_list(0, lane0_list);
@@ -852,8 +845,6 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
         // per program: histogram of the independent functions' last chunks, then counts
         const uint32_t t_hist = tiles(16, nfree, elem_tile, &lane0);
         batch_stage(BatchStage::RaHist, bl(16), t_hist, nullptr);
-        BP_CU(batch_regalloc_free(progs.at<Prog>(), dtable_slot(22), d_lane0, static_cast<uint32_t>(lane0_list.size()),
-                                  free_tiles, ra_sync.at<uint32_t>(4), s, ra_share));
         BP_CU(batch_regalloc(progs.at<Prog>(), dtable_slot(8), d_lane0, static_cast<uint32_t>(lane0_list.size()),
                              ra_items, max_g0, ra_sync.at<uint32_t>(), s, ra_share));
         const uint32_t* d_serial = upload_list(1, serial_list);

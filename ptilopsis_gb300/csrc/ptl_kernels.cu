@@ -2210,56 +2210,6 @@ struct BatchRa {
     uint32_t K, Kf;
 };
 
-// The independent functions of a batch, before any lane-0 pass: one function per thread,
-// kRaBatchFreeThreads per tile, the tiles of the listed programs in list order (longest
-// step chains first), handed out by ticket.  Without the lane-0 code beside it the loop
-// needs few registers and a small symbol cache, so many warps per SM hide its memory
-// latency; the lane-0 passes that follow find every trigger record complete.
-constexpr uint32_t kRaBatchFreeThreads = 128;
-constexpr uint32_t kRaBatchFreeK = 16;
-struct BatchRaFree {
-    const Prog* progs;
-    const uint32_t* tile_off;  // [n+1] first tile of each listed program
-    const uint32_t* order;     // [n] programs, in list order
-    uint32_t n, tiles;
-    uint32_t* queue;
-};
-
-__global__ void __launch_bounds__(kRaBatchFreeThreads) k_batch_ra_free(BatchRaFree ra) {
-    __shared__ uint32_t tag[kRaBatchFreeThreads * kRaBatchFreeK];
-    __shared__ uint32_t val[kRaBatchFreeThreads * kRaBatchFreeK];
-    __shared__ uint32_t s_tile;
-    __shared__ Prog sP;  // the program view, out of reach of the loop's stores (as in k_batch)
-    const SymCache c{tag, val, kRaBatchFreeK};
-    const uint32_t tid = threadIdx.x;
-    uint32_t have = 0xFFFFFFFFu;
-    for (;;) {
-        if (tid == 0) s_tile = atomicAdd(ra.queue, 1u);
-        __syncthreads();
-        const uint32_t t = s_tile;
-        if (t >= ra.tiles) break;
-        const uint32_t pos = batch_program(ra.tile_off, ra.n, t);
-        const uint32_t p = ra.order[pos];
-        if (p != have) {  // block-uniform
-            const uint64_t* src = reinterpret_cast<const uint64_t*>(&ra.progs[p]);
-            uint64_t* dst = reinterpret_cast<uint64_t*>(&sP);
-            for (uint32_t k = tid; k < sizeof(Prog) / 8; k += kRaBatchFreeThreads) dst[k] = src[k];
-            __syncthreads();
-            if (tid == 0) sP.defpos = nullptr;  // independent functions never need definition positions
-            __syncthreads();
-            have = p;
-        }
-        const uint32_t x = (t - ra.tile_off[pos]) * kRaBatchFreeThreads + tid;
-        const uint32_t nfree = sP.F - (sP.F + 7u) / 8u;
-        if (x < nfree) {
-            const uint32_t f = sP.ra_order ? sP.ra_order[x] : free_function_of(x);
-            const uint32_t chunks = (sP.S + kRaChunk - 1u) / kRaChunk;
-            if (f < sP.F) ra_free_function_cached(sP, c, tid, f, sP.ra_chunks + chunks);
-        }
-        __syncthreads();  // before s_tile and the view are reused
-    }
-}
-
 template <int Q, int MAXT>
 __global__ void __launch_bounds__(MAXT) k_batch_ra(BatchRa ra) {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -2446,24 +2396,6 @@ cudaError_t batch_regalloc(const Prog* progs, const uint32_t* item_off, const ui
         default: return go(k_batch_ra<8, 1024>);
     }
 }
-
-cudaError_t batch_regalloc_free(const Prog* progs, const uint32_t* tile_off, const uint32_t* order, uint32_t n,
-                                uint32_t tiles, uint32_t* queue, cudaStream_t s, double share) {
-    if (tiles == 0) return cudaSuccess;
-    int dev = 0, sms = 0, per_sm = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_ra_free, static_cast<int>(kRaBatchFreeThreads), 0);
-    const uint64_t resident = static_cast<uint64_t>(std::max(per_sm, 1)) * sms;
-    const uint64_t allowed = std::max<uint64_t>(1, static_cast<uint64_t>(static_cast<double>(resident) * share));
-    const unsigned grid = static_cast<unsigned>(std::max<uint64_t>(1, std::min<uint64_t>(tiles, allowed)));
-    cudaMemsetAsync(queue, 0, sizeof(uint32_t), s);
-    g_launches++;
-    k_batch_ra_free<<<grid, kRaBatchFreeThreads, 0, s>>>(BatchRaFree{progs, tile_off, order, n, tiles, queue});
-    return cudaGetLastError();
-}
-
-uint32_t batch_ra_free_tile() { return kRaBatchFreeThreads; }
 
 uint32_t batch_ra_threads(uint32_t max_g0) {
     return max_g0 <= 1024u ? std::max(32u, (max_g0 + 31u) & ~31u) : 1024u;

@@ -147,13 +147,6 @@ void batch_serial(const Prog* progs, const uint32_t* list, uint32_t count, cudaS
 // batch_ra_threads(max_g0), then its lane-0 pass, which follows their progress through
 // the program's ra_chunks record: histogram (BatchStage::RaHist) then zeroed counts).
 uint32_t batch_ra_threads(uint32_t max_g0);
-// The independent functions of n programs first, on their own: program order[k] owns
-// tiles tile_off[k] .. tile_off[k+1] of batch_ra_free_tile() functions each.  Run before
-// batch_regalloc with one item per program (its lane-0 pass only), whose progress waits
-// then find every chunk complete.
-uint32_t batch_ra_free_tile();
-cudaError_t batch_regalloc_free(const Prog* progs, const uint32_t* tile_off, const uint32_t* order, uint32_t n,
-                                uint32_t tiles, uint32_t* queue, cudaStream_t s, double share = 1.0);
 // share: the part of the device's resident blocks the persistent launch may take (1 =
 // all; less leaves room for other streams' kernels, e.g. a compile server's other lanes).
 cudaError_t batch_regalloc(const Prog* progs, const uint32_t* item_off, const uint32_t* order, uint32_t n,
