@@ -295,66 +295,129 @@ def run_reference(args):
 
 
 def run_serving(device, args):
-    """Open-loop Poisson arrivals of compile requests (80% 1k..10k nodes, 20% lognormal in
-    100k..2M) at each rate; latency = completion - scheduled arrival, on the server's
-    clock.  The submitter is one Python thread lending each request's arrays to the server
-    (no copy at submit); a rate it cannot keep up with shows as a lower achieved rate (and
-    as latency, since arrivals are scheduled)."""
+    """Open-loop Poisson arrivals of compile requests at each rate for a fixed window of
+    arrivals (args.serve_seconds), drawn from a pool of distinct requests (80% 1k..10k
+    nodes, 20% lognormal in 100k..2M; request k is pool[k % pool size]), each lent to the
+    server (no copy at submit).  Latency = completion - scheduled arrival, on the server's
+    clock.  Per rate: the completion rate inside the window and over the whole run, the
+    queue depth sampled every 50 ms, and whether the offered load is above what the
+    server completes (then the queue grows for the whole window and the latencies grow
+    with it: they are reported, but they measure the window's length).  Requests still
+    queued args.serve_drain seconds after the window are left unserved and counted."""
+    import threading
     from concurrent.futures import ThreadPoolExecutor
     from ptilopsis_gb300 import RvGenerator
     from ptilopsis_gb300.batch import CompileServer, clock_ns
     from ptilopsis_gb300.synth import config_params, generate
-    n_req = args.serve_requests
+    n_pool = args.serve_requests
     with ThreadPoolExecutor(min(32, os.cpu_count() or 8)) as ex:
-        reqs = list(ex.map(lambda k: generate(config_params("c4", program=k)), range(n_req)))
+        pool = list(ex.map(lambda k: generate(config_params("c4", program=k)), range(n_pool)))
+    pool_nodes = np.array([t.n for t in pool], dtype=np.float64)
     rng = np.random.default_rng(0x50544C04)
-    out = {"slots": args.serve_slots, "memory_budget_gb": 120, "requests": n_req,
-           "request_nodes_mean": float(np.mean([t.n for t in reqs])), "rates": []}
-    with CompileServer(device=device, slots=args.serve_slots, memory_budget=120 << 30) as srv:
-        for t in [srv.submit(r, copy=False) for r in reqs[:8]]:  # warm-up: arenas and code paths
-            srv.result(t)
-            srv.release(t)
-        for rate in args.serve_rates:
-            gaps = rng.exponential(1.0 / rate, n_req)
-            sched = np.cumsum(gaps)
-            t0 = clock_ns() + 2_000_000
-            tickets = []
-            for k, tr in enumerate(reqs):
+    budget = 120 << 30
+    out = {"slots": args.serve_slots, "memory_budget_gb": 120, "distinct_requests": n_pool,
+           "request_nodes_mean": float(pool_nodes.mean()), "window_s": args.serve_seconds,
+           "drain_limit_s": args.serve_drain, "rates": []}
+    for rate in args.serve_rates:
+        with CompileServer(device=device, slots=args.serve_slots, memory_budget=budget) as srv:
+            for t in [srv.submit(r, copy=False) for r in pool[:8]]:  # warm-up: arenas and code paths
+                srv.result(t)
+                srv.release(t)
+            sched = np.cumsum(rng.exponential(1.0 / rate, int(rate * args.serve_seconds * 1.5) + 16))
+            sched = sched[sched < args.serve_seconds]
+            m = len(sched)
+            tickets = np.zeros(m, dtype=np.int64)
+            submitted = threading.Event()
+            n_sub = [0]
+            done_ns = np.zeros(m, dtype=np.int64)
+            depth = []
+            stop = threading.Event()
+
+            def sampler():
+                while not stop.is_set():
+                    st, mem = srv.stats(), srv.memory()
+                    depth.append((clock_ns(), st["queued"], st["bytes_in_flight"], mem["held"]))
+                    stop.wait(0.05)
+
+            def reaper():
+                k = 0
+                while k < m:
+                    if k >= n_sub[0]:
+                        if submitted.is_set() and k >= n_sub[0]:
+                            break
+                        time.sleep(0.0005)
+                        continue
+                    tk = int(tickets[k])
+                    if srv.poll(tk):
+                        done_ns[k] = srv.times(tk)[2]
+                        srv.release(tk)
+                        k += 1
+                    elif stop.is_set():
+                        break
+                    else:
+                        time.sleep(0.0002)
+
+            ts = threading.Thread(target=sampler, daemon=True)
+            tr = threading.Thread(target=reaper, daemon=True)
+            t0 = clock_ns() + 5_000_000
+            ts.start()
+            tr.start()
+            for k in range(m):
                 due = t0 + int(sched[k] * 1e9)
                 while clock_ns() < due:
                     pass
-                tickets.append(srv.submit(tr, copy=False))  # the requests outlive their tickets
+                tickets[k] = srv.submit(pool[k % n_pool], copy=False)  # the pool outlives the server
+                n_sub[0] = k + 1
             submit_end = clock_ns()
-            lat, last = [], 0
-            for k, tk in enumerate(tickets):
-                srv.poll(tk, wait=True)
-                _, _, done = srv.times(tk)
-                lat.append((done - (t0 + int(sched[k] * 1e9))) / 1e6)
-                last = max(last, done)
-                srv.release(tk)
-            lat = np.array(lat)
-            span = (last - t0) / 1e9
-            out["rates"].append({"rate_per_s": rate, "achieved_rate_per_s": n_req / ((submit_end - t0) / 1e9),
-                                 "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
-                                 "max_ms": float(lat.max()),
-                                 "nodes_per_s": float(sum(t.n for t in reqs) / span)})
-        out["batches"] = srv.stats()["batches"]
-        # results in the mix equal compiling alone and the oracle: the first 64 requests
-        # submitted together, so that they are batched with one another
-        k_mix = min(64, n_req)
-        tickets = [srv.submit(r) for r in reqs[:k_mix]]
+            submitted.set()
+            tr.join(timeout=args.serve_drain)
+            stop.set()
+            tr.join()
+            ts.join()
+            end_ns = clock_ns()
+        arrive = t0 + (sched * 1e9).astype(np.int64)
+        fin = done_ns > 0
+        lat = (done_ns[fin] - arrive[fin]) / 1e6
+        win_end = t0 + int(args.serve_seconds * 1e9)
+        in_win = fin & (done_ns <= win_end)
+        nodes_k = pool_nodes[np.arange(m) % n_pool]
+        offered = float(nodes_k.sum() / args.serve_seconds)
+        done_rate_win = float(nodes_k[in_win].sum() / args.serve_seconds)
+        q = np.array([d[1] for d in depth]) if depth else np.zeros(1)
+        out["rates"].append({
+            "rate_per_s": rate, "requests": int(m),
+            "achieved_submit_rate_per_s": m / ((submit_end - t0) / 1e9),
+            "completed_in_window": int(in_win.sum()), "completed": int(fin.sum()),
+            "unserved_at_drain_limit": int(m - fin.sum()),
+            "completion_rate_per_s": float(in_win.sum() / args.serve_seconds),
+            "offered_nodes_per_s": offered, "completed_nodes_per_s_in_window": done_rate_win,
+            "sustained_nodes_per_s": float(nodes_k[fin].sum() / max((end_ns - t0) / 1e9, 1e-9)),
+            "above_capacity": bool(done_rate_win < 0.95 * offered),
+            "p50_ms": float(np.percentile(lat, 50)) if len(lat) else None,
+            "p99_ms": float(np.percentile(lat, 99)) if len(lat) else None,
+            "max_ms": float(lat.max()) if len(lat) else None,
+            "queue_depth": {"max": int(q.max()), "at_window_end": int(q[min(len(q) - 1, int(args.serve_seconds / 0.05))]),
+                            "samples_every_ms": 50,
+                            "series": [int(x) for x in q[::max(1, len(q) // 40)]]},
+            "device_bytes_held_max": int(max((d[3] for d in depth), default=0)),
+            "memory_budget_bytes": budget})
+    # results in the mix equal compiling alone and the oracle: the first 64 requests
+    # submitted together, so that they are batched with one another
+    k_mix = min(64, n_pool)
+    with CompileServer(device=device, slots=args.serve_slots, memory_budget=budget) as srv:
+        tickets = [srv.submit(r) for r in pool[:k_mix]]
         mixed = [srv.result(t) for t in tickets]
         for t in tickets:
             srv.release(t)
-    with RvGenerator(reqs[0], device=device) as g:
+    with RvGenerator(pool[0], device=device) as g:
         same = True
         for k in range(k_mix):
-            g.upload(reqs[k])
+            g.upload(pool[k])
             g.process()
             same &= bool(np.array_equal(g.get_instructions(), mixed[k].words))
     out["bit_exact_vs_plain"] = same
-    _, _, outs = port_parallel(reqs[:k_mix], os.cpu_count() or 1)
-    chk = compare_all(reqs[:k_mix], lambda k: mixed[k].words, lambda k: mixed[k].table, outs)
+    _, _, outs = port_parallel(pool[:k_mix], os.cpu_count() or 1)
+    chk = compare_all(pool[:k_mix], lambda k: mixed[k].words, lambda k: mixed[k].table, outs)
     out["bit_exact_vs_oracle"] = chk["equal"] == chk["programs"]
     out["oracle_check"] = chk
     return out
@@ -689,7 +752,9 @@ def main():
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--tiles", type=int, nargs=2, metavar=("ELEM", "SWEEP"),
                     help="tile sizes of the batched pipeline instead of autotuning them")
-    ap.add_argument("--serve-requests", type=int, default=1000)
+    ap.add_argument("--serve-requests", type=int, default=1000, help="distinct serving requests (the pool)")
+    ap.add_argument("--serve-seconds", type=float, default=5.0, help="arrival window per rate")
+    ap.add_argument("--serve-drain", type=float, default=10.0, help="seconds after the window before the rest is dropped")
     ap.add_argument("--serve-slots", type=int, default=2)
     ap.add_argument("--serve-rates", type=float, nargs="+", default=[1000.0, 10000.0, 50000.0])
     args = ap.parse_args()

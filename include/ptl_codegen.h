@@ -286,6 +286,14 @@ const char* ptl_server_error(ptl_server* server, uint64_t ticket);
 /* stats[0..4]: requests completed, nodes compiled, requests queued, admitted bytes in
  * flight, batches compiled. */
 ptl_status ptl_server_stats(ptl_server* server, uint64_t stats[5]);
+/* Device memory of the server's lanes: mem[0] the bytes their arenas hold now, mem[1]
+ * what admission charges now (per lane the larger of its arenas and the estimate of the
+ * batch it is compiling), mem[2] the largest charge seen after a compile, mem[3] the
+ * budget.  A batch is admitted only when the charges fit in the budget: an idle lane
+ * frees its arenas when a queued request needs the memory, and a lane whose arenas
+ * outgrew its batch's estimate frees them after the compile, so mem[0] <= mem[3] between
+ * compiles. */
+ptl_status ptl_server_memory(ptl_server* server, uint64_t mem[4]);
 /* Destroys the server after the compiles in flight; queued requests are dropped. */
 void ptl_server_destroy(ptl_server* server);
 /* The monotonic clock of the server's times, in ns. */

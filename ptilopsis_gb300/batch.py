@@ -59,6 +59,7 @@ def _bind(L):
     L.ptl_server_error.argtypes = [vp, u64]
     L.ptl_server_error.restype = ctypes.c_char_p
     L.ptl_server_stats.argtypes = [vp, ctypes.POINTER(u64)]
+    L.ptl_server_memory.argtypes = [vp, ctypes.POINTER(u64)]
     L.ptl_server_destroy.argtypes = [vp]
     L.ptl_server_destroy.restype = None
     L.ptl_clock_ns.argtypes = []
@@ -67,7 +68,7 @@ def _bind(L):
                "ptl_batch_copied_bytes", "ptl_batch_sizes", "ptl_batch_host_ns", "ptl_batch_set_tiles", "ptl_batch_tiles",
                "ptl_batch_set_regalloc_share",
                "ptl_batch_function_table", "ptl_server_create", "ptl_server_submit", "ptl_server_submit_flags", "ptl_server_poll",
-               "ptl_server_result", "ptl_server_times", "ptl_server_release", "ptl_server_stats"):
+               "ptl_server_result", "ptl_server_times", "ptl_server_release", "ptl_server_stats", "ptl_server_memory"):
         getattr(L, fn).restype = ctypes.c_int
     L._ptl_batch_bound = True
     return L
@@ -342,6 +343,13 @@ class CompileServer:
         self._lib.ptl_server_stats(self._h, s)
         return {"completed": int(s[0]), "nodes": int(s[1]), "queued": int(s[2]), "bytes_in_flight": int(s[3]),
                 "batches": int(s[4])}
+
+    def memory(self) -> dict:
+        """Device memory of the lanes: held (bytes their arenas hold now), charged (what
+        admission counts now), peak_charged (largest charge after a compile), budget."""
+        m = (ctypes.c_uint64 * 4)()
+        self._lib.ptl_server_memory(self._h, m)
+        return {"held": int(m[0]), "charged": int(m[1]), "peak_charged": int(m[2]), "budget": int(m[3])}
 
     def close(self) -> None:
         if self._h:

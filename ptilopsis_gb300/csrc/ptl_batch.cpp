@@ -40,10 +40,12 @@ struct Result {
     std::vector<uint32_t> words, starts, ends, sizes, ids;
 };
 
-// Device footprint of a compile, for admission: the generator's arrays for n nodes (about
-// 190 bytes per node with the word arrays at ~1.3 words per node and the scratch, plus
-// the arena's growth margin) and fixed scratch.
-uint64_t footprint(size_t n) { return 64ull * 1024 * 1024 + 256ull * n; }
+// Device footprint of a batch of n nodes in all, for admission: the pipeline's arrays
+// (about 210 bytes per node with the word arrays at ~1.25 words per node and the sort and
+// regalloc scratch), the arenas' 25% growth margin, and fixed scratch.  A lane that
+// finds its arenas past the estimate after a compile frees them (see ptl_server::run),
+// so the budget holds between compiles whatever the estimate.
+uint64_t footprint(size_t n) { return 64ull * 1024 * 1024 + 288ull * n; }
 
 }  // namespace
 
@@ -194,6 +196,19 @@ struct ptl_server {
     int device = 0;
     uint64_t budget = 0;
     uint64_t in_use = 0;       // admission estimates of the compiles in flight
+    // Device memory per lane: what its arenas hold (resident, measured after each compile)
+    // and the estimate of the batch it is compiling (reserved, 0 when idle).  A lane is
+    // charged the larger of the two, and a batch is admitted only when every lane's charge
+    // fits in the budget; an idle lane whose resident arenas stand in the way of a queued
+    // request is asked to free them (trim).
+    std::vector<uint64_t> resident, reserved;
+    std::vector<uint8_t> trim;
+    uint64_t charged(size_t skip = SIZE_MAX) const {
+        uint64_t t = 0;
+        for (size_t w = 0; w < resident.size(); ++w)
+            if (w != skip) t += std::max(resident[w], reserved[w]);
+        return t;
+    }
     uint64_t max_batch_nodes = 64ull << 20;
     // Requests below small_nodes are "small"; lanes w < small_lanes take only those, so a
     // small request never waits behind a large one whose register allocation chain sets a
@@ -210,6 +225,7 @@ struct ptl_server {
     uint64_t next_ticket = 1;
     bool stopping = false;
     uint64_t completed = 0, nodes_done = 0, batches = 0;
+    uint64_t peak_resident = 0;  // largest total of the lanes' charges seen after a compile
 
     // Continuous batching: a free lane takes every queued request of its size class, in
     // arrival order, that fits the memory left in the budget and the batch cap (a later
@@ -227,23 +243,64 @@ struct ptl_server {
                 std::unique_lock<std::mutex> lk(mu);
                 for (;;) {
                     if (stopping) return;
+                    if (trim[w]) {  // another lane needs the memory this idle lane's arenas hold
+                        lk.unlock();  // cudaFree waits for the device: not under the lock
+                        pipes[w]->release_memory();
+                        lk.lock();
+                        resident[w] = 0;
+                        trim[w] = 0;
+                        cv_work.notify_all();
+                        continue;
+                    }
+                    const uint64_t others = charged(w);
+                    uint64_t need_min = UINT64_MAX;  // smallest estimate of a request that waits for memory
+                    uint64_t batch_bytes = 0;
                     for (int pass = 0; pass < (prefer_small ? 1 : 2) && batch.empty(); ++pass) {
                         const bool want_small = (pass == 0) == prefer_small;
                         uint64_t nodes = 0;
                         for (auto it = queue.begin(); it != queue.end();) {
                             const std::shared_ptr<Request>& r = *it;
-                            const bool fits = in_use + r->bytes <= budget && (batch.empty() || nodes + r->n <= max_batch_nodes);
-                            if ((r->n < small_nodes) == want_small && fits) {
-                                in_use += r->bytes;
+                            if ((r->n < small_nodes) != want_small) {
+                                ++it;
+                                continue;
+                            }
+                            const uint64_t need = footprint(nodes + r->n);
+                            const bool fits = others + std::max(resident[w], need) <= budget &&
+                                              (batch.empty() || nodes + r->n <= max_batch_nodes);
+                            if (fits) {
                                 nodes += r->n;
                                 batch.push_back(r);
                                 it = queue.erase(it);
                             } else {
+                                if (batch.empty()) need_min = std::min(need_min, need);
                                 ++it;
                             }
                         }
+                        batch_bytes = footprint(nodes);
                     }
-                    if (!batch.empty()) break;
+                    if (!batch.empty()) {
+                        reserved[w] = batch_bytes;
+                        for (auto& r : batch) in_use += r->bytes;
+                        break;
+                    }
+                    if (need_min != UINT64_MAX) {  // a request waits for memory
+                        if (resident[w] > 0 && others + need_min <= budget) {
+                            // this lane's own high-water arenas are what stands in the way
+                            lk.unlock();
+                            pipes[w]->release_memory();
+                            lk.lock();
+                            resident[w] = 0;
+                            continue;
+                        }
+                        bool asked = false;  // else the idle lanes' arenas
+                        for (size_t v = 0; v < pipes.size(); ++v) {
+                            if (v != w && reserved[v] == 0 && resident[v] > 0 && !trim[v]) {
+                                trim[v] = 1;
+                                asked = true;
+                            }
+                        }
+                        if (asked) cv_work.notify_all();
+                    }
                     cv_work.wait(lk);
                 }
             }
@@ -254,6 +311,7 @@ struct ptl_server {
                 views.push_back(r->view());
             }
             const ptl_status st = pipes[w]->compile(views.data(), views.size(), res);
+            uint64_t held = pipes[w]->device_bytes();
             for (size_t k = 0; k < batch.size(); ++k) {
                 Result& out = batch[k]->result;
                 if (st != PTL_OK) {
@@ -271,6 +329,7 @@ struct ptl_server {
                 out.sizes.assign(r.sizes, r.sizes + r.functions);
                 out.ids.assign(r.ids, r.ids + r.functions);
             }
+            bool give_back = false;
             {
                 std::lock_guard<std::mutex> lk(mu);
                 const uint64_t t1 = now_ns();
@@ -282,6 +341,16 @@ struct ptl_server {
                     nodes_done += r->n;
                 }
                 ++batches;
+                // the arenas stay charged until they are freed
+                resident[w] = held;
+                reserved[w] = 0;
+                peak_resident = std::max(peak_resident, charged());
+                give_back = charged() > budget;  // they outgrew the batch's estimate
+            }
+            if (give_back) {
+                pipes[w]->release_memory();
+                std::lock_guard<std::mutex> lk(mu);
+                resident[w] = 0;
             }
             cv_done.notify_all();
             cv_work.notify_all();
@@ -296,6 +365,9 @@ extern "C" ptl_status ptl_server_create(int device, int slots, uint64_t memory_b
     s->device = device;
     s->budget = memory_budget;
     s->small_lanes = slots > 1 ? static_cast<size_t>(slots) / 2 : 0;  // one lane takes everything
+    s->resident.assign(static_cast<size_t>(slots), 0);
+    s->reserved.assign(static_cast<size_t>(slots), 0);
+    s->trim.assign(static_cast<size_t>(slots), 0);
     for (int w = 0; w < slots; ++w) {
         ptl_status st = PTL_OK;
         // small-request lanes run at the highest stream priority: their short, latency-bound
@@ -426,6 +498,18 @@ extern "C" ptl_status ptl_server_stats(ptl_server* s, uint64_t stats[5]) {
     stats[2] = s->queue.size();
     stats[3] = s->in_use;
     stats[4] = s->batches;
+    return PTL_OK;
+}
+
+extern "C" ptl_status ptl_server_memory(ptl_server* s, uint64_t mem[4]) {
+    if (!s || !mem) return PTL_BAD_ARGUMENT;
+    std::lock_guard<std::mutex> lk(s->mu);
+    uint64_t held = 0;
+    for (uint64_t r : s->resident) held += r;
+    mem[0] = held;
+    mem[1] = s->charged();
+    mem[2] = s->peak_resident;
+    mem[3] = s->budget;
     return PTL_OK;
 }
 

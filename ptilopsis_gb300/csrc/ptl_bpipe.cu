@@ -182,6 +182,16 @@ public:
         if (b) *b = d2h;
     }
     const char* last_error() const override { return err_text.c_str(); }
+    uint64_t device_bytes() const override {
+        uint64_t t = d_gp.bytes;
+        for (const DBuf* b : const_cast<Pipeline*>(this)->all()) t += b->bytes;
+        return t;
+    }
+    void release_memory() override {
+        const DeviceScope on_device(device);
+        for (DBuf* b : all()) b->release();
+        d_gp.release();
+    }
     void set_regalloc_share(double share) override { ra_share = std::min(1.0, std::max(0.05, share)); }
     bool set_tiles(uint32_t e, uint32_t w) override {
         if (!batch_tile_ok(e) || !batch_sweep_tile_ok(w)) return false;

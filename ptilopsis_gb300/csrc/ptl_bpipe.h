@@ -51,6 +51,10 @@ public:
     virtual void tiles(uint32_t out[2]) const = 0;
     // Detail of the last failure.
     virtual const char* last_error() const = 0;
+    // Device memory the pipeline's arenas hold now, bytes.
+    virtual uint64_t device_bytes() const = 0;
+    // Frees the arenas (between compiles only); the next compile allocates them again.
+    virtual void release_memory() = 0;
 };
 
 }  // namespace ptl

@@ -91,17 +91,56 @@ def test_server_budget_admission(built_cuda):
     from ptilopsis_gb300.batch import CompileServer
     trees = _programs(10, seed0=0x50544CC0)
     alone = [_alone(t) for t in trees]
-    budget = (64 << 20) + 256 * max(t.n for t in trees)  # one compile in flight at a time
+    budget = (64 << 20) + 288 * max(t.n for t in trees)  # one compile in flight at a time
     with CompileServer(slots=4, memory_budget=budget) as srv:
         tickets = [srv.submit(t) for t in trees]
         for k, tk in enumerate(tickets):
             _assert_same(srv.result(tk), *alone[k], f"request {k}")
         from ptilopsis_gb300.synth import SynthParams, generate
         big = generate(SynthParams(seed=0x50544CD0, n_functions=100, median_fn_nodes=900.0))
-        assert 256 * big.n + (64 << 20) > budget
+        assert 288 * big.n + (64 << 20) > budget
         with pytest.raises(PtlError) as e:
             srv.submit(big)
         assert e.value.status == 4  # PTL_ADMISSION_DENIED
+
+
+def test_server_device_memory_stays_within_budget(built_cuda):
+    """The lanes' resident arenas count against the budget: with a budget a few batches
+    wide, the device memory the server holds -- by its own account and by the device's
+    free memory, sampled every millisecond -- stays within it while a mix of small and
+    large requests (the serving size mix) runs on four lanes, and every result is exact."""
+    import threading
+    import time
+    import torch
+    from ptilopsis_gb300.batch import CompileServer
+    from ptilopsis_gb300.synth import config_params, generate
+    trees = [generate(config_params("c4", program=k)) for k in range(48)]
+    assert max(t.n for t in trees) > 100_000 and min(t.n for t in trees) < 10_000
+    budget = 2 << 30
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info(0)[0]
+    peak, held_max, stop = [0], [0], threading.Event()
+    with CompileServer(slots=4, memory_budget=budget) as srv:
+        def sampler():
+            while not stop.is_set():
+                peak[0] = max(peak[0], free0 - torch.cuda.mem_get_info(0)[0])
+                held_max[0] = max(held_max[0], srv.memory()["held"])
+                time.sleep(0.001)
+        th = threading.Thread(target=sampler, daemon=True)
+        th.start()
+        for rnd in range(2):  # two rounds: arenas kept from the first must be charged in the second
+            tickets = [srv.submit(t, copy=False) for t in trees]
+            outs = [srv.result(tk) for tk in tickets]
+            for tk in tickets:
+                srv.release(tk)
+        stop.set()
+        th.join()
+        mem = srv.memory()
+    assert mem["peak_charged"] <= budget and held_max[0] <= budget, (mem, held_max[0])
+    assert peak[0] <= budget + (128 << 20), f"device memory {peak[0] / 2**30:.2f} GiB over a {budget / 2**30} GiB budget"
+    for k in range(0, len(trees), 6):
+        w, tab = _alone(trees[k])
+        _assert_same(outs[k], w, tab, f"request {k}")
 
 
 def test_batch_program_failure_is_isolated(built_cuda):
