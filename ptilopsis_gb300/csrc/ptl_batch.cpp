@@ -210,6 +210,7 @@ struct ptl_server {
         return t;
     }
     uint64_t max_batch_nodes = 64ull << 20;
+    static constexpr size_t kLookAhead = 4096;  // queued requests examined per batch formed
     // Requests below small_nodes are "small"; lanes w < small_lanes take only those, so a
     // small request never waits behind a large one whose register allocation chain sets a
     // batch's duration.  The other lanes prefer large requests and take small ones when no
@@ -218,7 +219,10 @@ struct ptl_server {
     size_t small_lanes = 1;
     std::mutex mu;
     std::condition_variable cv_work, cv_done;
-    std::deque<std::shared_ptr<Request>> queue;
+    // queued requests by size class (0: small, 1: large), each in arrival order; a lane
+    // takes from the front, so a batch leaves its queue in O(1) per request however long
+    // the queue has grown
+    std::deque<std::shared_ptr<Request>> queue[2];
     std::unordered_map<uint64_t, std::shared_ptr<Request>> all;
     std::vector<std::thread> lanes;
     std::vector<std::unique_ptr<ptl::BatchPipeline>> pipes;
@@ -258,19 +262,20 @@ struct ptl_server {
                     for (int pass = 0; pass < (prefer_small ? 1 : 2) && batch.empty(); ++pass) {
                         const bool want_small = (pass == 0) == prefer_small;
                         uint64_t nodes = 0;
-                        for (auto it = queue.begin(); it != queue.end();) {
+                        std::deque<std::shared_ptr<Request>>& q = queue[want_small ? 0 : 1];
+                        // a request that does not fit may be passed by later ones that do, within a
+                        // bounded look-ahead (the lock is held while a batch is formed)
+                        size_t looked = 0;
+                        for (auto it = q.begin(); it != q.end() && nodes < max_batch_nodes && looked < kLookAhead;
+                             ++looked) {
                             const std::shared_ptr<Request>& r = *it;
-                            if ((r->n < small_nodes) != want_small) {
-                                ++it;
-                                continue;
-                            }
                             const uint64_t need = footprint(nodes + r->n);
                             const bool fits = others + std::max(resident[w], need) <= budget &&
                                               (batch.empty() || nodes + r->n <= max_batch_nodes);
                             if (fits) {
                                 nodes += r->n;
                                 batch.push_back(r);
-                                it = queue.erase(it);
+                                it = q.erase(it);  // at the front unless an earlier request waits
                             } else {
                                 if (batch.empty()) need_min = std::min(need_min, need);
                                 ++it;
@@ -419,7 +424,7 @@ extern "C" ptl_status ptl_server_submit_flags(ptl_server* s, const ptl_ast_view*
         req->ticket = s->next_ticket++;
         req->t_submit = now_ns();
         s->all[req->ticket] = req;
-        s->queue.push_back(req);
+        s->queue[n < s->small_nodes ? 0 : 1].push_back(req);
         *ticket = req->ticket;
     }
     s->cv_work.notify_one();
@@ -495,7 +500,7 @@ extern "C" ptl_status ptl_server_stats(ptl_server* s, uint64_t stats[5]) {
     std::lock_guard<std::mutex> lk(s->mu);
     stats[0] = s->completed;
     stats[1] = s->nodes_done;
-    stats[2] = s->queue.size();
+    stats[2] = s->queue[0].size() + s->queue[1].size();
     stats[3] = s->in_use;
     stats[4] = s->batches;
     return PTL_OK;
