@@ -256,11 +256,14 @@ ptl_status ptl_write_elf(const uint32_t* words, size_t n_words, const uint32_t* 
  * `slots` lanes (1..16), each a batched pipeline with its own stream and resident arenas:
  * a free lane takes every queued request of its size class (below or above 64k nodes;
  * with two or more lanes the first half takes only small requests, the others large ones
- * and small ones when no large one is queued), in arrival order, whose
+ * and small ones when no large one is queued), in arrival order, while the batch's
  * device-memory estimate fits in what is left of memory_budget (a later request that fits
  * may pass one that does not; at most 64M nodes per batch) and compiles them together,
  * while requests that arrive meanwhile go to the next free lane, so their work overlaps on
- * the GPU.  Results are identical to compiling each tree alone. */
+ * the GPU.  memory_budget bounds the device memory the lanes hold: each lane is charged
+ * the larger of its resident arenas and its batch's estimate, idle lanes free their
+ * arenas when a queued request needs the memory (ptl_server_memory).  Results are
+ * identical to compiling each tree alone. */
 typedef struct ptl_server ptl_server;
 ptl_status ptl_server_create(int device, int slots, uint64_t memory_budget, ptl_server** out);
 /* Copies a host tree into a request and queues it; PTL_ADMISSION_DENIED when the request
