@@ -59,6 +59,13 @@ STAGE_BYTES = {
 }
 
 
+# DRAM bytes the isn_gen stage's kernels (the depth sort and the instruction writes)
+# moved per node in one ncu capture of a batched compile of the workload's first 256
+# programs (profiles/isn_gen_traffic_256_programs.md); the batch's traffic is estimated as
+# this times its nodes.
+ISN_GEN_DRAM_BYTES_PER_NODE = 371.1
+
+
 def stage_rooflines(stage_ms, tot, peak):
     """Per stage: algorithmic bytes over its event-timed time, as a fraction of the HBM
     peak; the scan, generation and compaction stages (isn_cnt, isn_gen, optimize) as a
@@ -543,8 +550,12 @@ def run_batched(args):
     alg = STAGE_BYTES[name](tot["n"], tot["W"], tot["W2"], tot["W3"])
     achieved = alg / (stage_ms[dom] / 1000.0) / 1e9
     peak, peak_kind = peaks()
+    traffic = ISN_GEN_DRAM_BYTES_PER_NODE * tot["n"] if name == "isn_gen" else None
     roofline = {"bound": "hbm", "kernel": f"{name} stage (all programs)", "achieved": achieved, "peak": peak,
-                "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind, "traffic": None,
+                "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
+                "traffic_source": ("ncu dram__bytes_read.sum + dram__bytes_write.sum of the stage's kernels on the "
+                                   "first 256 programs, per node, times this batch's nodes") if traffic else None,
+                "traffic_over_algorithmic": round(traffic / alg, 2) if traffic else None,
                 "algorithmic_bytes_per_launch": int(alg),
                 "stage_ms": {s: round(float(v), 3) for s, v in zip(STAGES, stage_ms)},
                 "depth_sort_ms": round(float(np.mean(sort_ms)), 3),  # part of isn_gen
