@@ -64,6 +64,15 @@ ptl_status ptl_generator_create(const ptl_ast_view* tree, int device, ptl_genera
  * trees are copied on the generator's stream. */
 ptl_status ptl_generator_upload(ptl_generator* gen, const ptl_ast_view* tree);
 
+/* Replaces the scalar generator's constructor, rv_generator_st(const DepthTree&)
+ * (include/codegen/rv_generator.hpp:82-84; main.cpp:123-124 picks it for -s): the same
+ * generator object, whose process runs the single-threaded proof of concept's stages
+ * (src/codegen/rv_generator.cpp:129-1736) instead of rv_generator_avx's.  Its output
+ * differs from the AVX generator's (argument placement, float comparisons, isn_gen's
+ * parent slots and jump targets, per-function register state and preserved registers)
+ * and is bit-identical to rv_generator_st's.  Every other call below applies unchanged. */
+ptl_status ptl_generator_create_scalar(const ptl_ast_view* tree, int device, ptl_generator** out);
+
 /* Replaces rv_generator_avx::process(bool profile) (rv_generator_avx.cpp:104-120): runs
  * the seven stages.  Unlike the reference, which mutates its arrays and cannot be run
  * twice, process may be called again and recompiles from the copied tree.

@@ -74,6 +74,9 @@ void ptlref_free_tree(ptlref_tree* t);
 int ptlref_compile(const ptlref_tree* in, int threads, int sync, int altblock,
                    uint32_t mininstr, int snapshots, ptlref_result* out,
                    char* err, size_t errlen);
+/* Run the reference's scalar generator rv_generator_st (its -s flag), with the same
+ * snapshot slots. */
+int ptlref_compile_scalar(const ptlref_tree* in, int snapshots, ptlref_result* out, char* err, size_t errlen);
 void ptlref_free_result(ptlref_result* r);
 
 /* Flat dumps of the reference tables; see ptlport_table in oracle/port/ptl_port.h. */

@@ -285,6 +285,88 @@ extern "C" int ptlref_compile(const ptlref_tree* in, int threads, int sync, int 
     }
 }
 
+// The reference's scalar generator rv_generator_st (src/codegen/rv_generator.cpp:129-1736,
+// the -s flag of src/main.cpp), stage by stage with the same snapshot slots.  It owns no
+// threads, so it is destroyed normally.
+extern "C" int ptlref_compile_scalar(const ptlref_tree* in, int snapshots, ptlref_result* out, char* err,
+                                     size_t errlen) {
+    std::memset(out, 0, sizeof(*out));
+    borrowed_tree bt;
+    DepthTree* tree = bt.get();
+    tree->node_types = in->type;
+    tree->resulting_types = in->rtype;
+    tree->parents = in->parent;
+    tree->depth = in->depth;
+    tree->child_idx = in->child_idx;
+    tree->node_data = in->data;
+    tree->max_nodes = in->n;
+    tree->filled_nodes = in->n;
+    tree->max_depth = in->max_depth;
+    try {
+        rv_generator_st gen(*tree);
+        rv_generator_st* g = &gen;
+        out->threads_used = 1;
+        using clock = std::chrono::steady_clock;
+        auto timed = [&](int idx, auto fn) {
+            auto t0 = clock::now();
+            fn();
+            auto t1 = clock::now();
+            out->stage_ns[idx] = static_cast<uint64_t>(
+                std::chrono::duration_cast<std::chrono::nanoseconds>(t1 - t0).count());
+        };
+        auto words = [&](int i, int r, int a, int b, int j) {
+            out->bufs[i] = copy_buf(g->instructions);
+            out->bufs[r] = copy_buf(g->rd);
+            out->bufs[a] = copy_buf(g->rs1);
+            out->bufs[b] = copy_buf(g->rs2);
+            out->bufs[j] = copy_buf(g->jt);
+        };
+        timed(0, [&] { g->preprocess(); });
+        if (snapshots) {
+            out->bufs[PTLREF_PRE_TYPE] = copy_buf(g->node_types);
+            out->bufs[PTLREF_PRE_RTYPE] = copy_buf(g->result_types);
+            out->bufs[PTLREF_PRE_DATA] = copy_buf(g->node_data);
+        }
+        timed(1, [&] { g->isn_cnt(); });
+        if (snapshots) {
+            out->bufs[PTLREF_CNT_SIZE] = copy_buf(g->node_sizes);
+            out->bufs[PTLREF_CNT_LOC] = copy_buf(g->node_locations);
+            out->bufs[PTLREF_CNT_FN_ID] = copy_buf(g->function_ids);
+            out->bufs[PTLREF_CNT_FN_START] = copy_buf(g->func_starts);
+            out->bufs[PTLREF_CNT_FN_END] = copy_buf(g->func_ends);
+            out->bufs[PTLREF_CNT_FN_SIZE] = copy_buf(g->function_sizes);
+        }
+        timed(2, [&] { g->isn_gen(); });
+        if (snapshots) words(PTLREF_GEN_INSTR, PTLREF_GEN_RD, PTLREF_GEN_RS1, PTLREF_GEN_RS2, PTLREF_GEN_JT);
+        timed(3, [&] { g->optimize(); });
+        if (snapshots) out->bufs[PTLREF_OPT_USED] = copy_buf(g->used_instrs);
+        timed(4, [&] { g->regalloc(); });
+        if (snapshots) {
+            words(PTLREF_RA_INSTR, PTLREF_RA_RD, PTLREF_RA_RS1, PTLREF_RA_RS2, PTLREF_RA_JT);
+            out->bufs[PTLREF_RA_FN_START] = copy_buf(g->func_starts);
+            out->bufs[PTLREF_RA_FN_END] = copy_buf(g->func_ends);
+            out->bufs[PTLREF_RA_FN_SIZE] = copy_buf(g->function_sizes);
+        }
+        timed(5, [&] { g->fix_jumps(); });
+        if (snapshots) {
+            words(PTLREF_FJ_INSTR, PTLREF_FJ_RD, PTLREF_FJ_RS1, PTLREF_FJ_RS2, PTLREF_FJ_JT);
+            out->bufs[PTLREF_FJ_FN_START] = copy_buf(g->func_starts);
+            out->bufs[PTLREF_FJ_FN_END] = copy_buf(g->func_ends);
+            out->bufs[PTLREF_FJ_FN_SIZE] = copy_buf(g->function_sizes);
+        }
+        timed(6, [&] { g->postprocess(); });
+        out->bufs[PTLREF_OUT_WORDS] = copy_buf(g->instructions);
+        out->bufs[PTLREF_FN_START] = copy_buf(g->func_starts);
+        out->bufs[PTLREF_FN_END] = copy_buf(g->func_ends);
+        out->bufs[PTLREF_FN_SIZE] = copy_buf(g->function_sizes);
+        out->bufs[PTLREF_FN_ID] = copy_buf(g->function_ids);
+        return 0;
+    } catch (const std::exception& e) {
+        set_err(err, errlen, e.what());
+        return 2;
+    }
+}
+
 extern "C" void ptlref_free_result(ptlref_result* r) {
     for (auto& b : r->bufs) {
         std::free(b.p);

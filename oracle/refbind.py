@@ -130,6 +130,9 @@ def lib():
                                      ctypes.c_char_p, ctypes.c_size_t]
         L.ptlref_compile.restype = ctypes.c_int
         L.ptlref_free_result.argtypes = [ctypes.POINTER(_Result)]
+        L.ptlref_compile_scalar.argtypes = [ctypes.POINTER(_Tree), ctypes.c_int, ctypes.POINTER(_Result),
+                                            ctypes.c_char_p, ctypes.c_size_t]
+        L.ptlref_compile_scalar.restype = ctypes.c_int
         u8p, i32p, u32p = (ctypes.POINTER(ctypes.c_uint8), ctypes.POINTER(ctypes.c_int32),
                            ctypes.POINTER(ctypes.c_uint32))
         L.ptlref_flatten.argtypes = [ctypes.c_size_t, u8p, u8p, i32p, i32p, u32p, ctypes.POINTER(_Tree)]
@@ -205,6 +208,38 @@ def compile_ast(ast: Ast, threads: int = 1, sync: int = 0, altblock: int = 0,
         raise RuntimeError("reference generator failed: " + err.value.decode())
     try:
         out = RefResult(stage_ns=list(r.stage_ns), threads_used=r.threads_used)
+        for i, name in enumerate(BUF_NAMES):
+            b = r.bufs[i]
+            if b.p:
+                out.bufs[name] = _np(b.p, b.n, np.uint32)
+        return out
+    finally:
+        L.ptlref_free_result(ctypes.byref(r))
+
+
+def compile_ast_scalar(ast: Ast, snapshots: bool = False) -> RefResult:
+    """The reference's scalar generator (rv_generator_st, src/codegen/rv_generator.cpp:
+    129-1736; the -s flag) on the tree, with the same snapshot names as compile_ast."""
+    L = lib()
+    keep = [np.ascontiguousarray(ast.type, np.uint8), np.ascontiguousarray(ast.rtype, np.uint8),
+            np.ascontiguousarray(ast.parent, np.int32), np.ascontiguousarray(ast.depth, np.int32),
+            np.ascontiguousarray(ast.child_idx, np.int32), np.ascontiguousarray(ast.data, np.uint32)]
+    t = _Tree()
+    t.n = ast.n
+    t.max_depth = int(ast.max_depth)
+    t.type = keep[0].ctypes.data_as(ctypes.POINTER(ctypes.c_uint8))
+    t.rtype = keep[1].ctypes.data_as(ctypes.POINTER(ctypes.c_uint8))
+    t.parent = keep[2].ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+    t.depth = keep[3].ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+    t.child_idx = keep[4].ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+    t.data = keep[5].ctypes.data_as(ctypes.POINTER(ctypes.c_uint32))
+    r = _Result()
+    err = ctypes.create_string_buffer(1024)
+    rc = L.ptlref_compile_scalar(ctypes.byref(t), int(snapshots), ctypes.byref(r), err, 1024)
+    if rc != 0:
+        raise RuntimeError("reference scalar generator failed: " + err.value.decode())
+    try:
+        out = RefResult(stage_ns=list(r.stage_ns), threads_used=1)
         for i, name in enumerate(BUF_NAMES):
             b = r.bufs[i]
             if b.p:

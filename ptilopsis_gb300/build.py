@@ -29,7 +29,8 @@ CUDA_LIB = os.path.join(LIBDIR, "libptl_gb300.so")
 SYNTH_LIB = os.path.join(LIBDIR, "libptlsynth.so")
 HOSTMODEL_LIB = os.path.join(LIBDIR, "libptl_hostmodel.so")
 
-HEADERS = ["ptl_device.h", "ptl_common.cuh", "ptl_stages.cuh", "ptl_sort.cuh", "ptl_ra.cuh", "ptl_kernels.cuh", "ptl_bpipe.h"]
+HEADERS = ["ptl_device.h", "ptl_common.cuh", "ptl_stages.cuh", "ptl_sort.cuh", "ptl_ra.cuh", "ptl_scalar.cuh", "ptl_kernels.cuh",
+           "ptl_bpipe.h"]
 
 
 def _nvcc() -> str:
@@ -90,7 +91,8 @@ def build_synth(force: bool = False) -> str:
 
 
 def build_hostmodel(force: bool = False) -> str:
-    srcs = _src("ptl_hostmodel.cpp", "ptl_tables.cpp", "ptl_common.cuh", "ptl_stages.cuh", "ptl_sort.cuh", "ptl_ra.cuh")
+    srcs = _src("ptl_hostmodel.cpp", "ptl_tables.cpp", "ptl_common.cuh", "ptl_stages.cuh", "ptl_sort.cuh", "ptl_ra.cuh",
+                "ptl_scalar.cuh")
     if not force and _newer(HOSTMODEL_LIB, srcs):
         return HOSTMODEL_LIB
     os.makedirs(LIBDIR, exist_ok=True)

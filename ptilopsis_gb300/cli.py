@@ -14,7 +14,8 @@ writes to stdout.  -p prints the reference's profiling CSV (stage names, then
 nanoseconds; src/codegen/rv_generator.cpp:150-162) with the GPU's per-stage device times.
 --elf <file> also writes the program as an ELF64 RISC-V relocatable object (an option the
 reference does not have; ptl_write_elf).  -t, -m, -b and -i set how the reference
-schedules its CPU threads; they are accepted and have no effect here.  -s (the scalar generator) is not part of this implementation.
+schedules its CPU threads; they are accepted and have no effect here.  -s selects the
+scalar generator's semantics (rv_generator_st, main.cpp:123-124), also on the GPU.
 """
 from __future__ import annotations
 
@@ -64,7 +65,7 @@ def _parser() -> argparse.ArgumentParser:
     ap.add_argument("-S", dest="asm", action="store_true", help="output assembly instead of machine code")
     ap.add_argument("-o", dest="outfile", help="output filename (default: ./c.out, or <infile>.s with -S; - for stdout)")
     ap.add_argument("-d", "--debug", action="store_true", help="print tree and output sizes")
-    ap.add_argument("-s", "--simple", action="store_true", help="the scalar generator (not available)")
+    ap.add_argument("-s", "--simple", action="store_true", help="use the scalar generator's semantics")
     ap.add_argument("-f", "--tree", action="store_true", help="print tree info")
     ap.add_argument("-t", "--threads", type=int, default=-1, help="accepted for compatibility; no effect")
     ap.add_argument("-m", "--sync", type=int, default=0, help="accepted for compatibility; no effect")
@@ -83,9 +84,6 @@ def profile_csv(stage_names: List[str], stage_ns: List[int]) -> str:
 
 def main(argv: Optional[List[str]] = None) -> int:
     args = _parser().parse_args(argv)
-    if args.simple:
-        print("the scalar generator (-s) is not part of this implementation", file=sys.stderr)
-        return 1
     if args.infile == "-":
         src = io.BytesIO(sys.stdin.buffer.read())
     elif not os.path.exists(args.infile):
@@ -99,7 +97,7 @@ def main(argv: Optional[List[str]] = None) -> int:
         outfile = (os.path.splitext(os.path.basename(args.infile))[0] + ".s") if args.asm else "c.out"
 
     from .codegen import STAGES, RvGenerator
-    with RvGenerator(tree, device=args.device) as gen:
+    with RvGenerator(tree, device=args.device, scalar=args.simple) as gen:
         gen.process(profile=True)
         if args.profile:
             sys.stdout.write(profile_csv(STAGES, gen.stage_ns()))

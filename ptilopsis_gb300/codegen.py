@@ -132,6 +132,7 @@ def lib():
         L = ctypes.CDLL(LIB_PATH)
         vp, sz, u32p = ctypes.c_void_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_uint32)
         L.ptl_generator_create.argtypes = [ctypes.POINTER(_AstView), ctypes.c_int, ctypes.POINTER(vp)]
+        L.ptl_generator_create_scalar.argtypes = [ctypes.POINTER(_AstView), ctypes.c_int, ctypes.POINTER(vp)]
         L.ptl_generator_process.argtypes = [vp, ctypes.c_int]
         L.ptl_generator_upload.argtypes = [vp, ctypes.POINTER(_AstView)]
         L.ptl_kernel_launches.argtypes = []
@@ -151,7 +152,7 @@ def lib():
         L.ptl_code_table.restype = ctypes.c_size_t
         L.ptl_device_info.argtypes = [ctypes.c_int, ctypes.c_char_p, sz, ctypes.POINTER(ctypes.c_int),
                                       ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
-        for fn in ("ptl_generator_create", "ptl_generator_process", "ptl_generator_upload", "ptl_generator_instructions",
+        for fn in ("ptl_generator_create", "ptl_generator_create_scalar", "ptl_generator_process", "ptl_generator_upload", "ptl_generator_instructions",
                    "ptl_generator_device_instructions", "ptl_generator_function_table",
                    "ptl_generator_stage_ns", "ptl_generator_snapshot", "ptl_compile", "ptl_device_info"):
             getattr(L, fn).restype = ctypes.c_int
@@ -204,17 +205,21 @@ def code_table(which: int) -> np.ndarray:
 
 
 class RvGenerator:
-    """GPU counterpart of rv_generator_avx (include/codegen/rv_generator_avx.hpp:26-148)."""
+    """GPU counterpart of rv_generator_avx (include/codegen/rv_generator_avx.hpp:26-148);
+    with scalar=True, of the single-threaded rv_generator_st (include/codegen/
+    rv_generator.hpp:82-100, the -s flag of src/main.cpp), whose output differs."""
 
-    def __init__(self, tree: DepthTree, device: int = 0):
+    def __init__(self, tree: DepthTree, device: int = 0, scalar: bool = False):
         self._lib = lib()
         self._h = ctypes.c_void_p()
         keep: list = []
         view = _view(tree, keep)
-        st = self._lib.ptl_generator_create(ctypes.byref(view), device, ctypes.byref(self._h))
+        create = self._lib.ptl_generator_create_scalar if scalar else self._lib.ptl_generator_create
+        st = create(ctypes.byref(view), device, ctypes.byref(self._h))
         if st != 0:
-            raise PtlError(st, "ptl_generator_create")
+            raise PtlError(st, "ptl_generator_create_scalar" if scalar else "ptl_generator_create")
         self.n = tree.n
+        self.scalar = scalar
 
     def _check(self, st: int, what: str) -> None:
         if st != 0:
@@ -306,8 +311,8 @@ class RvGenerator:
         self.close()
 
 
-def compile_tree(tree: DepthTree, device: int = 0, profile: bool = False) -> np.ndarray:
-    with RvGenerator(tree, device) as gen:
+def compile_tree(tree: DepthTree, device: int = 0, profile: bool = False, scalar: bool = False) -> np.ndarray:
+    with RvGenerator(tree, device, scalar=scalar) as gen:
         gen.process(profile=profile)
         return gen.get_instructions()
 

@@ -91,6 +91,8 @@ struct ptl_generator {
     DevBuf sort_a, sort_apos, sort_bpos, sort_seg0, sort_seg1, sort_tile_seg, sort_tile_l, sort_tile_r,
         sort_leaf, sort_heap, sort_counters, sort_local, sort_equal;
     DevBuf scan_status, scan_counter, meta, flags, errw, tables;
+    DevBuf preserve, sregs, ssteps, sextra, sclaim;  // scalar register allocation
+    bool scalar = false;  // the scalar generator's semantics (rv_generator_st)
 
     // results
     uint32_t F = 0, W = 0, W2 = 0, W3 = 0, S = 0;
@@ -113,7 +115,8 @@ struct ptl_generator {
                 &stamp, &defpos, &lifetime, &trig_min, &trig_max, &ra_chunks, &spill, &roffs, &ni, &nrd, &nr1, &nr2, &njt,
                 &fsz, &joffs, &out, &sort_a, &sort_apos, &sort_bpos, &sort_seg0, &sort_seg1,
                 &sort_tile_seg, &sort_tile_l, &sort_tile_r, &sort_leaf, &sort_heap, &sort_counters, &sort_local, &sort_equal,
-                &scan_status, &scan_counter, &meta, &flags, &errw, &tables};
+                &scan_status, &scan_counter, &meta, &flags, &errw, &tables, &preserve, &sregs, &ssteps,
+                &sextra, &sclaim};
     }
 };
 
@@ -211,6 +214,7 @@ Prog make_prog(ptl_generator* g) {
     P.tab.t = g->tables.at<CodeTables>();
     P.err = g->errw.at<ErrorWord>();
     P.flags = g->flags.at<uint32_t>();
+    P.scalar = g->scalar ? 1u : 0u;
     return P;
 }
 
@@ -315,7 +319,8 @@ ptl_status run_pipeline(ptl_generator* g, bool profile, bool to_host, bool row0_
         if (ptl_status st = check_error_word(g); st != PTL_OK) return st;
         if (!reach) return fail(g, PTL_INVALID_AST, "input: depths 0..max_depth are not all populated");
     }
-    launch_preprocess(P, s);
+    if (g->scalar) launch_preprocess_scalar(P, s);
+    else launch_preprocess(P, s);
     timer.mark();
 
     // ---- isn_cnt: count + scan, fixes, function table
@@ -396,7 +401,8 @@ ptl_status run_pipeline(ptl_generator* g, bool profile, bool to_host, bool row0_
                         P.defpos, P.roffs, P.owner, P.used, P.smark, P.pos, P.regs}))
         return fail(g, PTL_CUDA_ERROR, "internal: unallocated word arrays");
     PTL_CU(run_depth_sort(P, ss, s, &g->sort_rounds, &g->sort_graph));
-    launch_gen(P, s);
+    if (g->scalar) launch_gen_scalar(P, s);
+    else launch_gen(P, s);
     if (ptl_status st = check_error_word(g); st != PTL_OK) return st;
     timer.mark();
 
@@ -408,20 +414,42 @@ ptl_status run_pipeline(ptl_generator* g, bool profile, bool to_host, bool row0_
     // ---- regalloc
     PTL_CU(g->lifetime.ensure(fb8, 8));
     PTL_CU(g->lifetime.zero(s));
-    note_launch();
-    k_init_lifetime<<<std::min<size_t>((g->F + 255) / 256, 1024), 256, 0, s>>>(g->lifetime.at<unsigned long long>(), g->F);
-    const size_t trig = static_cast<size_t>(std::max<uint32_t>(g->S, 1)) * 64;
-    PTL_CU(g->trig_min.ensure(trig, 4));
-    PTL_CU(g->trig_min.fill(s, 0xFF));
-    PTL_CU(g->trig_max.ensure(trig, 4));
-    PTL_CU(g->trig_max.zero(s));
-    PTL_CU(g->ra_chunks.ensure(2 * (static_cast<size_t>(g->S) / 32 + 2), 4));
-    P = make_prog(g);
-    if (!prog_ready(P, {P.lifetime, P.trig_min, P.trig_max, P.ra_chunks}))
-        return fail(g, PTL_CUDA_ERROR, "internal: unallocated regalloc state");
-    PTL_CU(run_regalloc_steps(P, s, &g->ra_serial, row0_hash));
-    PTL_CU(scan_for(wb8, &sc));
-    launch_regalloc_count_scan(P, sc, s);
+    if (g->scalar) {
+        PTL_CU(g->preserve.ensure(fb8, 8));
+        PTL_CU(g->preserve.zero(s));
+        PTL_CU(g->sextra.ensure(wb8, 4));
+        P = make_prog(g);
+        if (!prog_ready(P, {P.lifetime, g->preserve.at<void>(), g->sextra.at<void>()}))
+            return fail(g, PTL_CUDA_ERROR, "internal: unallocated regalloc state");
+        bool cross = false;
+        PTL_CU(scalar_regalloc_cross(P, s, &cross));
+        if (cross) {
+            PTL_CU(g->sregs.ensure(static_cast<size_t>(g->F) * 64, 4));
+            PTL_CU(g->ssteps.ensure(g->F, sizeof(SRaStep)));
+            launch_scalar_ra_serial(P, g->sregs.at<int32_t>(), g->ssteps.at<SRaStep>(),
+                                    g->preserve.at<unsigned long long>(), s);
+        } else {
+            launch_scalar_ra_free(P, g->preserve.at<unsigned long long>(), s);
+        }
+        g->ra_serial = cross;
+        PTL_CU(scan_for(wb8, &sc));
+        launch_scalar_ra_count_scan(P, g->preserve.at<unsigned long long>(), g->sextra.at<uint32_t>(), sc, s);
+    } else {
+        note_launch();
+        k_init_lifetime<<<std::min<size_t>((g->F + 255) / 256, 1024), 256, 0, s>>>(g->lifetime.at<unsigned long long>(), g->F);
+        const size_t trig = static_cast<size_t>(std::max<uint32_t>(g->S, 1)) * 64;
+        PTL_CU(g->trig_min.ensure(trig, 4));
+        PTL_CU(g->trig_min.fill(s, 0xFF));
+        PTL_CU(g->trig_max.ensure(trig, 4));
+        PTL_CU(g->trig_max.zero(s));
+        PTL_CU(g->ra_chunks.ensure(2 * (static_cast<size_t>(g->S) / 32 + 2), 4));
+        P = make_prog(g);
+        if (!prog_ready(P, {P.lifetime, P.trig_min, P.trig_max, P.ra_chunks}))
+            return fail(g, PTL_CUDA_ERROR, "internal: unallocated regalloc state");
+        PTL_CU(run_regalloc_steps(P, s, &g->ra_serial, row0_hash));
+        PTL_CU(scan_for(wb8, &sc));
+        launch_regalloc_count_scan(P, sc, s);
+    }
     uint32_t last_off = 0;
     PTL_CU(read1(g, P.roffs + (g->W - 1), &last_off));
     if (ptl_status st = check_error_word(g); st != PTL_OK) return st;
@@ -434,7 +462,12 @@ ptl_status run_pipeline(ptl_generator* g, bool profile, bool to_host, bool row0_
     P = make_prog(g);
     if (!prog_ready(P, {P.ni, P.nrd, P.nr1, P.nr2, P.njt, P.fsz, P.joffs}))
         return fail(g, PTL_CUDA_ERROR, "internal: unallocated regalloc output");
-    launch_regalloc_emit(P, s);
+    if (g->scalar) {
+        PTL_CU(g->sclaim.ensure(g->W2, 8));
+        launch_scalar_ra_emit(P, g->preserve.at<unsigned long long>(), g->sclaim.at<unsigned long long>(), s);
+    } else {
+        launch_regalloc_emit(P, s);
+    }
     for (int k = 0; k < 3; ++k) {
         DevBuf* src[3] = {&g->fn_start, &g->fn_end, &g->fn_size};
         DevBuf* dst[3] = {&g->fn_ra_start, &g->fn_ra_end, &g->fn_ra_size};
@@ -546,6 +579,12 @@ ptl_status ptl_generator_create(const ptl_ast_view* tree, int device, ptl_genera
     }
     *out = g;
     return PTL_OK;
+}
+
+ptl_status ptl_generator_create_scalar(const ptl_ast_view* tree, int device, ptl_generator** out) {
+    const ptl_status st = ptl_generator_create(tree, device, out);
+    if (st == PTL_OK) (*out)->scalar = true;
+    return st;
 }
 
 ptl_status ptl_generator_process(ptl_generator* g, int profile) {

@@ -17,6 +17,7 @@
 #include "ptl_sort.cuh"
 #include "ptl_stages.cuh"
 #include "ptl_ra.cuh"
+#include "ptl_scalar.cuh"
 
 using namespace ptl;
 
@@ -25,6 +26,8 @@ namespace {
 uint32_t g_cache_k = 4;  // entries per function of the lane-0 symbol cache
 bool g_force_hashed = false;  // lane-0 pass finds row-0 values by hashing even when definitions are unique
 bool g_last_hashed = false;   // the last compile had a lane-0 virtual register with two definitions
+bool g_last_cross = false;    // the last scalar compile took the serial register allocation
+bool g_force_serial = false;  // scalar register allocation in the reference's order for every program
 
 template <typename T>
 struct HBuf {
@@ -208,8 +211,42 @@ struct Model {
         P = Psave;
     }
 
+    // The scalar generator's register allocation (ptl_scalar.cuh), from the optimized words
+    // to the regalloc output (the spill offsets, the count scan, the scatter, the moved
+    // function table and the frame words).
+    void scalar_regalloc(uint32_t F, uint32_t W, uint32_t wb8) {
+        uint32_t cross = 0;
+        for (uint32_t i = 0; i < W; ++i) cross |= st_ra_cross(P, i, stamp.p) & 1u;
+        std::vector<unsigned long long> preserve(F, 0);
+        if (cross || g_force_serial) {
+            std::vector<int32_t> sregs(static_cast<size_t>(F) * 64);
+            std::vector<SRaStep> steps(F);
+            s_ra_serial(P, sregs.data(), steps.data(), preserve.data());
+        } else {
+            int32_t sregs[64];
+            for (uint32_t f = 0; f < F; ++f) s_ra_function(P, f, sregs, preserve.data());
+        }
+        g_last_cross = cross != 0;
+        if (!check()) return;
+        for (uint32_t v = 0; v < W; ++v) st_ra_spill(P, v);
+        std::vector<uint32_t> extra(wb8 + 16, 0);
+        for (uint32_t f = 0; f < F; ++f) st_s_preserve_counts(P, f, preserve.data(), extra.data());
+        if (!check()) return;
+        exclusive_scan(wb8, [&](uint32_t i) { return st_s_ra_count(P, i, extra.data()); }, roffs.p);
+        if (!check()) return;
+        const uint32_t W2 = roffs.p[W - 1] + 1;
+        const uint32_t w2b8 = static_cast<uint32_t>(r8(W2));
+        for (auto* b : {&ni, &nrd, &nr1, &nr2, &njt, &fsz, &joffs}) b->ensure(w2b8 + 16);
+        P.W2 = W2; P.w2b8 = w2b8;
+        bind();
+        for (uint32_t i = 0; i < wb8; ++i) st_s_ra_scatter(P, i);
+        for (uint32_t f = 0; f < F; ++f) st_fix_functab(P, f, P.roffs, W);
+        for (uint32_t pass = 0; pass < 3; ++pass)
+            for (uint32_t f = 0; f < F; ++f) st_s_frame(P, f, pass, preserve.data(), 0, nullptr);
+    }
+
     int run(const uint8_t* type, const uint8_t* rtype, const int32_t* parent, const int32_t* depth,
-            const int32_t* child, const uint32_t* data, size_t n_, size_t max_depth) {
+            const int32_t* child, const uint32_t* data, size_t n_, size_t max_depth, bool scalar) {
         build_code_tables(&tab);
         const uint32_t n = static_cast<uint32_t>(n_);
         const uint32_t nb8 = static_cast<uint32_t>(r8(n));
@@ -223,13 +260,19 @@ struct Model {
         regs.ensure(3ull * n);
         P = Prog{};
         P.n = n; P.nb8 = nb8; P.max_depth = static_cast<uint32_t>(max_depth);
+        P.scalar = scalar ? 1u : 0u;
         bind();
         bool reach = false;
         for (uint32_t i = 0; i < nb8; ++i) reach |= st_ingest(P, i);
         if (!check()) return err.code;
         if (!reach) return ST_INVALID_AST;
-        for (uint32_t i = 0; i < nb8; ++i) st_pre_lists(P, i);
-        for (uint32_t i = 0; i < nb8; ++i) st_pre_float(P, i);
+        if (scalar) {
+            for (uint32_t i = 0; i < nb8; ++i) st_s_pre_lists(P, i);
+            for (uint32_t i = 0; i < nb8; ++i) st_s_pre_float(P, i);
+        } else {
+            for (uint32_t i = 0; i < nb8; ++i) st_pre_lists(P, i);
+            for (uint32_t i = 0; i < nb8; ++i) st_pre_float(P, i);
+        }
         for (uint32_t i = 0; i < nb8; ++i) st_pre_float_apply(P, i);
         if (!check()) return err.code;
         exclusive_scan(nb8, [&](uint32_t i) { const uint32_t v = st_count(P, i); P.sizes[i] = v; return v; }, loc0.p);
@@ -259,9 +302,15 @@ struct Model {
         P.W = W; P.wb8 = wb8; P.S = S;
         bind();
         depth_sort(n);
-        for (uint32_t x = 0; x < n; ++x) st_gen_prop(P, x);
-        for (uint32_t x = 0; x < n; ++x) st_gen_claim(P, x);
-        for (uint32_t x = 0; x < n; ++x) st_gen_write(P, x);
+        if (scalar) {
+            for (uint32_t x = 0; x < n; ++x) st_s_gen_prop(P, x);
+            for (uint32_t x = 0; x < n; ++x) st_s_gen_claim(P, x);
+            for (uint32_t x = 0; x < n; ++x) st_s_gen_write(P, x);
+        } else {
+            for (uint32_t x = 0; x < n; ++x) st_gen_prop(P, x);
+            for (uint32_t x = 0; x < n; ++x) st_gen_claim(P, x);
+            for (uint32_t x = 0; x < n; ++x) st_gen_write(P, x);
+        }
         if (!check()) return err.code;
         for (uint32_t i = 0; i < wb8; ++i) st_opt_mark(P, i);
         for (;;) {
@@ -278,32 +327,38 @@ struct Model {
         bind();
         defpos.ensure(wb8);
         bind();
-        uint32_t flagbits = 0;
-        for (uint32_t i = 0; i < W; ++i) flagbits |= st_ra_cross(P, i, stamp.p);
-        const uint32_t G0 = (F + 7) / 8;
-        if ((flagbits & 1u) || G0 > 8192u) {
-            st_ra_serial(P, stamp.p);
+        if (scalar) {
+            scalar_regalloc(F, W, wb8);
+            if (!check()) return err.code;
         } else {
-            std::vector<uint32_t> tag(64), val(64);
-            const SymCache c1{tag.data(), val.data(), 64};
-            Prog Pfree = P;
-            Pfree.defpos = nullptr;
-            for (uint32_t f = 0; f < F; ++f) if (f & 7u) ra_free_function_cached(Pfree, c1, 0, f);
-            lane0_cached(S, hm_cache_k, (flagbits & 2u) != 0 || g_force_hashed);
-            g_last_hashed = (flagbits & 2u) != 0;
+            uint32_t flagbits = 0;
+            for (uint32_t i = 0; i < W; ++i) flagbits |= st_ra_cross(P, i, stamp.p);
+            const uint32_t G0 = (F + 7) / 8;
+            if ((flagbits & 1u) || G0 > 8192u) {
+                st_ra_serial(P, stamp.p);
+            } else {
+                std::vector<uint32_t> tag(64), val(64);
+                const SymCache c1{tag.data(), val.data(), 64};
+                Prog Pfree = P;
+                Pfree.defpos = nullptr;
+                for (uint32_t f = 0; f < F; ++f) if (f & 7u) ra_free_function_cached(Pfree, c1, 0, f);
+                lane0_cached(S, hm_cache_k, (flagbits & 2u) != 0 || g_force_hashed);
+                g_last_hashed = (flagbits & 2u) != 0;
+            }
+            for (uint32_t v = 0; v < W; ++v) st_ra_spill(P, v);
+            exclusive_scan(wb8, [&](uint32_t i) { return st_ra_count(P, i); }, roffs.p);
+            if (!check()) return err.code;
+            const uint32_t W2 = roffs.p[W - 1] + 1;
+            const uint32_t w2b8 = static_cast<uint32_t>(r8(W2));
+            for (auto* b : {&ni, &nrd, &nr1, &nr2, &njt, &fsz, &joffs}) b->ensure(w2b8 + 16);
+            P.W2 = W2; P.w2b8 = w2b8;
+            bind();
+            for (uint32_t i = 0; i < wb8; ++i) st_ra_scatter(P, i);
+            for (uint32_t f = 0; f < F; ++f) st_fix_functab(P, f, P.roffs, W);
+            for (uint32_t f = 0; f < F; ++f) st_ra_frame(P, f);
         }
-        for (uint32_t v = 0; v < W; ++v) st_ra_spill(P, v);
-        exclusive_scan(wb8, [&](uint32_t i) { return st_ra_count(P, i); }, roffs.p);
-        if (!check()) return err.code;
-        const uint32_t W2 = roffs.p[W - 1] + 1;
-        const uint32_t w2b8 = static_cast<uint32_t>(r8(W2));
-        for (auto* b : {&ni, &nrd, &nr1, &nr2, &njt, &fsz, &joffs}) b->ensure(w2b8 + 16);
-        P.W2 = W2; P.w2b8 = w2b8;
-        bind();
-        for (uint32_t i = 0; i < wb8; ++i) st_ra_scatter(P, i);
-        for (uint32_t f = 0; f < F; ++f) st_fix_functab(P, f, P.roffs, W);
-        for (uint32_t f = 0; f < F; ++f) st_ra_frame(P, f);
         for (uint32_t f = 0; f < F; ++f) { fn_ra_start.p[f] = fn_start.p[f]; fn_ra_end.p[f] = fn_end.p[f]; fn_ra_size.p[f] = fn_size.p[f]; }
+        const uint32_t W2 = P.W2, w2b8 = P.w2b8;
         exclusive_scan(w2b8, [&](uint32_t i) { const uint32_t v = i < W2 ? st_fj_size(P, i) : 0u; P.fsz[i] = v; return v; }, joffs.p);
         const uint32_t W3 = fsz.p[W2 - 1] + joffs.p[W2 - 1];
         out.ensure(r8(W3) + 8);
@@ -325,13 +380,14 @@ struct ptlhm_buf {
 };
 
 // Same slot numbers as ptl_generator_snapshot (include/ptl_codegen.h).
-int ptlhm_compile(const uint8_t* type, const uint8_t* rtype, const int32_t* parent, const int32_t* depth,
-                  const int32_t* child, const uint32_t* data, size_t n, size_t max_depth, ptlhm_buf* bufs,
-                  int nbufs, uint32_t* err_out) {
+// scalar: the scalar generator's semantics.
+int ptlhm_compile_mode(const uint8_t* type, const uint8_t* rtype, const int32_t* parent, const int32_t* depth,
+                       const int32_t* child, const uint32_t* data, size_t n, size_t max_depth, ptlhm_buf* bufs,
+                       int nbufs, uint32_t* err_out, int scalar) {
     Model* m = new Model();
     int rc = 0;
     try {
-        rc = m->run(type, rtype, parent, depth, child, data, n, max_depth);
+        rc = m->run(type, rtype, parent, depth, child, data, n, max_depth, scalar != 0);
     } catch (const std::exception&) {
         rc = ST_UNSUPPORTED;
     }
@@ -359,6 +415,15 @@ int ptlhm_compile(const uint8_t* type, const uint8_t* rtype, const int32_t* pare
     delete m;
     return rc;
 }
+
+int ptlhm_compile(const uint8_t* type, const uint8_t* rtype, const int32_t* parent, const int32_t* depth,
+                  const int32_t* child, const uint32_t* data, size_t n, size_t max_depth, ptlhm_buf* bufs,
+                  int nbufs, uint32_t* err_out) {
+    return ptlhm_compile_mode(type, rtype, parent, depth, child, data, n, max_depth, bufs, nbufs, err_out, 0);
+}
+
+int ptlhm_last_cross(void) { return g_last_cross ? 1 : 0; }
+void ptlhm_set_scalar_serial(int on) { g_force_serial = on != 0; }
 
 void ptlhm_set_cache_entries(uint32_t k) { g_cache_k = k; }
 void ptlhm_set_hashed(int on) { g_force_hashed = on != 0; }

@@ -1412,6 +1412,35 @@ __global__ void k_ra_frame(Prog P) { PTL_FOR(f, P.F) st_ra_frame(P, f); }
 __global__ void k_fj_emit(Prog P) { PTL_FOR(i, P.W2) st_fj_emit(P, i); }
 __global__ void k_fj_functab(Prog P) { PTL_FOR(f, P.F) st_fix_functab(P, f, P.joffs, P.W2); }
 
+// ------------------------------------------------------------------ scalar semantics
+// The stages where the scalar generator differs (ptl_scalar.cuh).
+__global__ void k_s_pre_lists(Prog P) { PTL_FOR(i, P.nb8) st_s_pre_lists(P, i); }
+__global__ void k_s_pre_float(Prog P) { PTL_FOR(i, P.nb8) st_s_pre_float(P, i); }
+__global__ void k_s_gen_prop(Prog P) { PTL_FOR(x, P.n) st_s_gen_prop(P, x); }
+__global__ void k_s_gen_claim(Prog P) { PTL_FOR(x, P.n) st_s_gen_claim(P, x); }
+__global__ void k_s_gen_write(Prog P) { PTL_FOR(x, P.n) st_s_gen_write(P, x); }
+// One thread per function, its 64-entry register state in local memory.
+constexpr int kScalarRaThreads = 128;
+__global__ void __launch_bounds__(kScalarRaThreads) k_s_ra_free(Prog P, unsigned long long* preserve) {
+    int32_t regs[64];
+    PTL_FOR(f, P.F) s_ra_function(P, f, regs, preserve);
+}
+__global__ void k_s_ra_serial(Prog P, int32_t* regs, SRaStep* steps, unsigned long long* preserve) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) s_ra_serial(P, regs, steps, preserve);
+}
+__global__ void k_s_preserve_counts(Prog P, const unsigned long long* preserve, uint32_t* extra) {
+    PTL_FOR(f, P.F) st_s_preserve_counts(P, f, preserve, extra);
+}
+__global__ void k_s_ra_scatter(Prog P) { PTL_FOR(i, P.wb8) st_s_ra_scatter(P, i); }
+__global__ void k_s_frame(Prog P, const unsigned long long* preserve, int mode, unsigned long long* claim) {
+    PTL_FOR(t, 3ull * P.F) st_s_frame(P, t % P.F, t / P.F, preserve, mode, claim);
+}
+struct SRaCountLoad {
+    Prog P;
+    const uint32_t* extra;
+    __device__ uint32_t operator()(uint32_t i) const { return st_s_ra_count(P, i, extra); }
+};
+
 }  // namespace
 
 uint64_t launch_count() { return g_launches.load(); }
@@ -1740,6 +1769,70 @@ void launch_regalloc_emit(const Prog& P, cudaStream_t s) {
     k_ra_functab<<<grid_for(P.F), kThreads, 0, s>>>(P);
     g_launches++;
     k_ra_frame<<<grid_for(P.F), kThreads, 0, s>>>(P);
+}
+
+void launch_preprocess_scalar(const Prog& P, cudaStream_t s) {
+    g_launches++;
+    k_s_pre_lists<<<grid_for(P.nb8), kThreads, 0, s>>>(P);
+    g_launches++;
+    k_s_pre_float<<<grid_for(P.nb8), kThreads, 0, s>>>(P);
+    g_launches++;
+    k_pre_float_apply<<<grid_for(P.nb8), kThreads, 0, s>>>(P);
+}
+
+void launch_gen_scalar(const Prog& P, cudaStream_t s) {
+    g_launches++;
+    k_s_gen_prop<<<grid_for(P.n), kThreads, 0, s>>>(P);
+    g_launches++;
+    k_s_gen_claim<<<grid_for(P.n), kThreads, 0, s>>>(P);
+    g_launches++;
+    k_s_gen_write<<<grid_for(P.n), kThreads, 0, s>>>(P);
+}
+
+cudaError_t scalar_regalloc_cross(const Prog& P, cudaStream_t s, bool* cross) {
+    cudaMemsetAsync(P.flags + 1, 0, 2 * sizeof(uint32_t), s);
+    cudaMemsetAsync(P.stamp, 0, sizeof(uint32_t) * P.W, s);
+    g_launches++;
+    k_ra_cross<<<grid_for(P.W), kThreads, 0, s>>>(P);
+    uint32_t fl = 0;
+    cudaMemcpyAsync(&fl, P.flags + 1, sizeof(fl), cudaMemcpyDeviceToHost, s);
+    const cudaError_t e = cudaStreamSynchronize(s);
+    *cross = fl != 0;
+    return e;
+}
+
+void launch_scalar_ra_free(const Prog& P, unsigned long long* preserve, cudaStream_t s) {
+    g_launches++;
+    k_s_ra_free<<<grid_for(P.F, kScalarRaThreads), kScalarRaThreads, 0, s>>>(P, preserve);
+}
+
+void launch_scalar_ra_serial(const Prog& P, int32_t* regs, SRaStep* steps, unsigned long long* preserve,
+                             cudaStream_t s) {
+    g_launches++;
+    k_s_ra_serial<<<1, 1, 0, s>>>(P, regs, steps, preserve);
+}
+
+void launch_scalar_ra_count_scan(const Prog& P, const unsigned long long* preserve, uint32_t* extra,
+                                 const ScanScratch& sc, cudaStream_t s) {
+    g_launches++;
+    k_ra_spill<<<grid_for(P.W), kThreads, 0, s>>>(P);
+    cudaMemsetAsync(extra, 0, sizeof(uint32_t) * P.wb8, s);
+    g_launches++;
+    k_s_preserve_counts<<<grid_for(P.F), kThreads, 0, s>>>(P, preserve, extra);
+    run_scan(SRaCountLoad{P, extra}, StoreTo{P.roffs}, P.wb8, sc, P.err, s);
+}
+
+void launch_scalar_ra_emit(const Prog& P, const unsigned long long* preserve, unsigned long long* claim,
+                           cudaStream_t s) {
+    g_launches++;
+    k_s_ra_scatter<<<grid_for(P.wb8), kThreads, 0, s>>>(P);
+    g_launches++;
+    k_ra_functab<<<grid_for(P.F), kThreads, 0, s>>>(P);
+    cudaMemsetAsync(claim, 0, sizeof(unsigned long long) * P.W2, s);
+    g_launches++;
+    k_s_frame<<<grid_for(3ull * P.F), kThreads, 0, s>>>(P, preserve, 1, claim);
+    g_launches++;
+    k_s_frame<<<grid_for(3ull * P.F), kThreads, 0, s>>>(P, preserve, 2, claim);
 }
 
 void launch_fixjumps_scan(const Prog& P, const ScanScratch& sc, cudaStream_t s) {

@@ -6,6 +6,7 @@
 #include "ptl_device.h"
 #include "ptl_stages.cuh"
 #include "ptl_sort.cuh"
+#include "ptl_scalar.cuh"
 
 namespace ptl {
 
@@ -57,6 +58,22 @@ void launch_regalloc_count_scan(const Prog& P, const ScanScratch& sc, cudaStream
 void launch_regalloc_emit(const Prog& P, cudaStream_t s);
 void launch_fixjumps_scan(const Prog& P, const ScanScratch& sc, cudaStream_t s);
 void launch_fixjumps_emit(const Prog& P, cudaStream_t s);
+
+// The scalar generator's stages where they differ (ptl_scalar.cuh).  Register
+// allocation: the cross check (functions naming each other's words take the serial
+// order), then one thread per function or the serial kernel (regs: F x 64, steps: F),
+// each leaving the preserve masks; the count scan with the preserve words (extra: wb8
+// counts); the scatter, the moved function table and the frame words (claim: W2 keys).
+void launch_preprocess_scalar(const Prog& P, cudaStream_t s);
+void launch_gen_scalar(const Prog& P, cudaStream_t s);
+cudaError_t scalar_regalloc_cross(const Prog& P, cudaStream_t s, bool* cross);
+void launch_scalar_ra_free(const Prog& P, unsigned long long* preserve, cudaStream_t s);
+void launch_scalar_ra_serial(const Prog& P, int32_t* regs, SRaStep* steps, unsigned long long* preserve,
+                             cudaStream_t s);
+void launch_scalar_ra_count_scan(const Prog& P, const unsigned long long* preserve, uint32_t* extra,
+                                 const ScanScratch& sc, cudaStream_t s);
+void launch_scalar_ra_emit(const Prog& P, const unsigned long long* preserve, unsigned long long* claim,
+                           cudaStream_t s);
 
 // Two partition rounds as one CUDA graph.  Every launch of a round takes its arguments
 // from the scratch layout (pointers, capacities) and reads its counts on the device, and

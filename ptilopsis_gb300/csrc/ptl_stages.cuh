@@ -49,6 +49,20 @@ PTL_HD void record_error(ErrorWord* e, uint32_t code, uint32_t where, uint32_t d
     if (e->code == 0u) { e->code = code; e->where = where; e->detail = detail; }
 #endif
 }
+PTL_HD void at_add_u32(uint32_t* p, uint32_t v) {
+#if defined(__CUDA_ARCH__)
+    atomicAdd(p, v);
+#else
+    *p += v;
+#endif
+}
+PTL_HD int popcount64(uint64_t v) {
+#if defined(__CUDA_ARCH__)
+    return __popcll(static_cast<unsigned long long>(v));
+#else
+    return __builtin_popcountll(v);
+#endif
+}
 PTL_HD uint32_t ctz64(uint64_t t) {
 #if defined(__CUDA_ARCH__)
     return static_cast<uint32_t>(__ffsll(static_cast<long long>(t)) - 1);
@@ -165,6 +179,8 @@ struct Prog {
     Tab tab;
     ErrorWord* err;
     uint32_t* flags;      // [0] optimize changed, [1] [2] regalloc checks, [3] a node at max_depth
+    uint32_t scalar;      // 1: the scalar generator's semantics (ptl_scalar.cuh)
+    uint32_t pad_;
 };
 
 // Function-argument registers and stack slots, rv_generator_avx.cpp:126-213, on one
@@ -195,6 +211,25 @@ PTL_HD void pre_args(uint32_t& t, uint32_t rt, uint32_t& nd, uint32_t ci) {
         t |= on_stack & 0b10u;
         reg_offset -= 8u & on_stack;
         if (is_int) nd = reg_offset;
+    }
+}
+
+// The scalar generator's argument placement, rv_generator.cpp:231-284, on one node.
+// rt & 0b001 and rt & 0b110: a float or float reference.
+PTL_HD void pre_args_scalar(uint32_t& t, uint32_t rt, uint32_t& nd, uint32_t ci) {
+    if ((t & RV_FUNC_ARG) != RV_FUNC_ARG) return;
+    const bool is_f = (rt & 1u) && (rt & 6u);
+    if (is_f && nd < 8u) return;  // the first eight float arguments stay in float registers
+    const int32_t preceding_integers = is_f ? s32(ci - nd) : s32(nd);
+    const int32_t preceding_floats = s32(ci) - preceding_integers;
+    const int32_t over = preceding_floats - 8;
+    const int32_t ir_idx = preceding_integers + (over > 0 ? over : 0);
+    if (ir_idx < 8) {
+        nd = u32(ir_idx);
+        if (is_f) t |= 0b01u;
+    } else {
+        t |= 0b10u;
+        nd = u32(ir_idx - 8);
     }
 }
 
@@ -229,7 +264,8 @@ PTL_HD bool st_ingest(const Prog& P, uint32_t i) {
     if (bad) record_error(P.err, ST_INVALID_AST, 0, i);
     uint32_t t = ty < kNumPareasTypes ? P.tab.t->pareas_to_rv[ty] : 0u;
     uint32_t nd = data;
-    pre_args(t, rty, nd, u32(c));  // preprocess's first pass, fused
+    if (P.scalar) pre_args_scalar(t, rty, nd, u32(c));  // preprocess's first pass, fused
+    else pre_args(t, rty, nd, u32(c));
     P.nt[i] = t;
     P.rt[i] = rty;
     P.par[i] = p;

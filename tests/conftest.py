@@ -97,3 +97,33 @@ def load_large(name: str):
         _large_cache.clear()  # one large tree at a time
         _large_cache[name] = (ast, entry)
     return _large_cache[name]
+
+
+def manifest_scalar() -> dict:
+    with open(os.path.join(GOLDEN, "manifest_scalar.json")) as f:
+        return json.load(f)
+
+
+def crc32(a) -> int:
+    import zlib
+    return zlib.crc32(np.ascontiguousarray(a, np.uint32).tobytes())
+
+
+def load_scalar_case(entry: dict):
+    """(Ast, golden outputs or None) of a scalar-generator case of manifest_scalar.json:
+    a committed fixture's tree, or a seeded program regenerated and checked against the
+    CRCs of the tree the reference compiled.  Outputs are stored for the fixtures and
+    the c0 seeds; the workload programs keep CRCs only."""
+    if "fixture" in entry:
+        ast, _ = load_fixture(entry["fixture"])
+    else:
+        from ptilopsis_gb300.synth import SynthParams, config_params, generate
+        prm = SynthParams(seed=entry["seed"]) if "seed" in entry else config_params("c3", program=entry["c3_program"])
+        ast = tree_to_ast(generate(prm))
+    got = [crc32(np.asarray(ast.type, np.uint32)), crc32(np.asarray(ast.parent).view(np.uint32)), crc32(ast.data)]
+    assert got == entry["tree_crcs"], f"{entry['name']}: tree differs from the one the reference compiled"
+    z = np.load(os.path.join(GOLDEN, "scalar_words.npz"))
+    key = entry["name"] + ".out_words"
+    if key not in z.files:
+        return ast, None
+    return ast, {k: z[f"{entry['name']}.{k}"] for k in ("out_words", "fn_start", "fn_end", "fn_size", "fn_id")}

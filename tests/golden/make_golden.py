@@ -5,13 +5,17 @@ oracle/ref/Makefile has built it into oracle/_ref:
 
     python tests/golden/make_golden.py            # small fixtures, synthetic seeds, tables
     python tests/golden/make_golden.py --large    # the reference's larger Pareas inputs
+    python tests/golden/make_golden.py --scalar   # the scalar generator (rv_generator_st)
 
 For each fixture it stores the DepthTree the reference front end (pareas-ast) builds
 from one of the reference's own Pareas test inputs, and what the reference generator
 (rv_generator_avx with one worker thread) produces from it: the output words, the
 function table, and a CRC32 of every intermediate array.  Seeded synthetic programs
 store only the outputs (their trees are regenerated from the seed).  The code tables
-are stored as CRC32s of the reference's constexpr arrays.
+are stored as CRC32s of the reference's constexpr arrays.  --scalar runs the reference's
+scalar generator (rv_generator_st, the -s flag) on the same trees and on seeded programs
+of the batched workload's shape, and stores the outputs of the first two kinds in
+scalar_words.npz and the CRCs of every stage array in manifest_scalar.json.
 """
 from __future__ import annotations
 
@@ -139,8 +143,51 @@ def main() -> None:
         json.dump(manifest, f, indent=1, sort_keys=True)
 
 
+# Seeded programs of the batched workload (program k of config c3) for the scalar
+# generator, the ones of at most SCALAR_C3_MAX_NODES nodes among the first SCALAR_C3.
+SCALAR_C3 = 24
+SCALAR_C3_MAX_NODES = 60000
+
+
+def main_scalar() -> None:
+    if not refbind.build(REF):
+        raise SystemExit("the reference could not be built here (needs the reference tree on x86-64)")
+    from ptilopsis_gb300.synth import SynthParams, config_params, generate
+    cases = []
+    for rel in FIXTURES:
+        name = rel.replace("testfiles/", "").replace("/", "_").replace(".", "_")
+        cases.append((name, {"fixture": name}, refbind.parse_file(os.path.join(REF, rel))))
+    for seed in SYNTH_SEEDS:
+        t = generate(SynthParams(seed=seed))
+        cases.append((f"synth_c0_{seed:08x}", {"seed": seed},
+                      refbind.Ast(t.type, t.rtype, t.parent, t.depth, t.child_idx, t.data, t.max_depth)))
+    for k in range(SCALAR_C3):
+        t = generate(config_params("c3", program=k))
+        if t.n > SCALAR_C3_MAX_NODES:
+            continue
+        cases.append((f"c3_program_{k}", {"c3_program": k},
+                      refbind.Ast(t.type, t.rtype, t.parent, t.depth, t.child_idx, t.data, t.max_depth)))
+    words = {}
+    manifest = {"fixtures": []}
+    for name, origin, ast in cases:
+        res = refbind.compile_ast_scalar(ast, snapshots=True)
+        if "c3_program" not in origin:  # the seeded workload programs keep CRCs only
+            for k in ("out_words", "fn_start", "fn_end", "fn_size", "fn_id"):
+                words[f"{name}.{k}"] = res.bufs[k]
+        manifest["fixtures"].append({"name": name, **origin, "n": int(ast.n), "words": int(len(res.bufs["out_words"])),
+                                     "tree_crcs": [crc(np.asarray(ast.type, np.uint32)),
+                                                   crc(np.asarray(ast.parent).view(np.uint32)), crc(ast.data)],
+                                     "snapshots": {k: [int(len(v)), crc(v)] for k, v in res.bufs.items()}})
+        print(f"{name}: {ast.n} nodes -> {len(res.bufs['out_words'])} words (scalar generator)")
+    np.savez_compressed(os.path.join(HERE, "scalar_words.npz"), **words)
+    with open(os.path.join(HERE, "manifest_scalar.json"), "w") as f:
+        json.dump(manifest, f, indent=1, sort_keys=True)
+
+
 if __name__ == "__main__":
     if "--large" in sys.argv[1:]:
         main_large()
+    elif "--scalar" in sys.argv[1:]:
+        main_scalar()
     else:
         main()

@@ -26,8 +26,8 @@ def test_cli_arguments_and_profile_format(tmp_path):
     assert r.returncode == 0 and b"-S" in r.stdout
     r = _run([str(tmp_path / "missing.npz")], tmp_path)
     assert r.returncode == 1 and b"Failed to open file" in r.stderr
-    r = _run(["-s", "x.npz"], tmp_path)
-    assert r.returncode == 1
+    r = _run(["-s", "x.npz"], tmp_path)  # -s (the scalar generator) is accepted
+    assert r.returncode == 1 and b"Failed to open file" in r.stderr
     assert profile_csv(["a", "b", "c"], [1, 22, 333]) == "a,b,c\n1,22,333\n"
     ast, _ = load_fixture(manifest()["fixtures"][0]["name"])
     tree = ast_to_tree(ast)

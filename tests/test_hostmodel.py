@@ -31,6 +31,9 @@ def hostmodel():
         from ptilopsis_gb300 import build as b
         L = ctypes.CDLL(b.build_hostmodel())
         L.ptlhm_compile.restype = ctypes.c_int
+        L.ptlhm_compile_mode.restype = ctypes.c_int
+        L.ptlhm_set_scalar_serial.argtypes = [ctypes.c_int]
+        L.ptlhm_set_scalar_serial.restype = None
         L.ptlhm_depth_sort.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]
         L.ptlhm_depth_sort.restype = None
         _hm = L
