@@ -21,6 +21,9 @@ whole batch).  Prints one JSON line (rank 0):
   cpu_baseline  the oracle's CPU restatement on a bounded sample, on all host cores
   flatten     AST flattening (ptl_flatten) on 16 programs given in random node order,
               host arrays in and out, against the oracle's restatement on one core
+  scalar      the scalar generator's semantics (the reference's -s, rv_generator_st) on
+              the plain pipeline over a sample of the programs, checked against and timed
+              beside the oracle's restatement of that generator on all host cores
 
 --mode single times one large program (config c1, ~4M nodes) per step instead.
 --impl reference times the oracle restatement on the host cores on a sample of the same
@@ -430,6 +433,44 @@ def run_serving(device, args):
     return out
 
 
+def run_scalar(trees, device, sample_n):
+    """The scalar generator (RvGenerator(scalar=True)) one program at a time on a sample
+    of the workload: device time (stage events) and wall time, the words compared with
+    the oracle's scalar restatement, which runs the same sample on all host cores."""
+    from concurrent.futures import ThreadPoolExecutor
+    from oracle import portbind
+    from ptilopsis_gb300 import STAGES, RvGenerator
+    sample = trees[:sample_n]
+    sn = sum(t.n for t in sample)
+    gen = RvGenerator(sample[0], device=device, scalar=True)
+    gen.process()
+    dev, words, stage = 0.0, [], np.zeros(len(STAGES))
+    t0 = time.perf_counter()
+    for t in sample:
+        gen.upload(t)
+        gen.process(profile=True)
+        words.append(gen.get_instructions())
+        ns = np.array(gen.stage_ns(), dtype=np.float64)
+        stage += ns
+        dev += ns.sum() / 1e9
+    wall = time.perf_counter() - t0
+    gen.close()
+    threads = os.cpu_count() or 1
+    asts = [to_ast(t) for t in sample]
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(threads) as ex:
+        outs = list(ex.map(lambda a: portbind.compile_ast(a, scalar=True), asts))
+    cdt = time.perf_counter() - t0
+    equal = sum(bool(np.array_equal(w, o.words)) for w, o in zip(words, outs))
+    return {"value": sn / dev, "e2e_value": sn / wall, "unit": UNIT, "programs": len(sample), "nodes": sn,
+            "sample": f"first {len(sample)} programs of the workload, one scalar generator, one at a time",
+            "stage_ms": {k: round(float(v) / 1e6, 3) for k, v in zip(STAGES, stage)},
+            "bit_exact_vs_oracle": equal == len(sample), "oracle_equal": equal,
+            "cpu_baseline": {"value": sn / cdt, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"the same {len(sample)} programs, {threads} threads",
+                             "seconds": round(cdt, 3)}}
+
+
 def run_flatten(trees, device, reps=3):
     """AST flattening (ptl_flatten, the GPU's DepthTree construction) on the 16 largest of
     the first 256 programs, each given in a seeded random node order, through the public
@@ -610,6 +651,8 @@ def run_batched(args):
             line["serving"] = run_serving(local, args)
         if not args.no_flatten:
             line["flatten"] = run_flatten(trees, local)
+        if not args.no_scalar:
+            line["scalar"] = run_scalar(trees, local, args.scalar_sample)
         if oracle_check is not None:
             line["bit_exact_vs_oracle"] = oracle_check["equal"] == oracle_check["programs"]
             line["oracle_check"] = oracle_check
@@ -760,6 +803,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--no-flatten", action="store_true")
+    ap.add_argument("--no-scalar", action="store_true")
+    ap.add_argument("--scalar-sample", type=int, default=64)
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--tiles", type=int, nargs=2, metavar=("ELEM", "SWEEP"),
                     help="tile sizes of the batched pipeline instead of autotuning them")

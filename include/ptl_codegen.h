@@ -79,7 +79,10 @@ ptl_status ptl_generator_create_scalar(const ptl_ast_view* tree, int device, ptl
  * profile bits: 1 = per-stage device times (ptl_generator_stage_ns); 2 = leave the words
  * on the device (ptl_generator_device_instructions); 4 = the register allocator finds
  * row-0 values through its hash table even when every virtual register has one
- * definition (the general path, normally taken only when one has two; same output). */
+ * definition (the general path, normally taken only when one has two; same output);
+ * 8 = a scalar generator allocates registers in the reference's serial order for every
+ * program (normally only for programs whose functions name each other's words; same
+ * output). */
 ptl_status ptl_generator_process(ptl_generator* gen, int profile);
 
 /* Replaces get_instructions() (rv_generator_avx.cpp:82-84): the encoded RV words, in a

@@ -853,6 +853,583 @@ struct Gen {
     }
 };
 
+// ==================================================================== scalar generator
+// Restatement of the reference's single-threaded proof of concept, rv_generator_st
+// (src/codegen/rv_generator.cpp:227-1736, the -s flag of src/main.cpp), written as its
+// own loops: preprocess, isn_cnt, isn_gen, optimize, regalloc and fix_jumps have their
+// own rules there (fix_jumps differs only in the jump targets it leaves, which no output
+// word reads); postprocess is the AVX generator's.  The reference keeps registers, rd, rs1 and rs2 in
+// int64 built from u32 arithmetic; they are kept here as u32 and read zero-extended.
+struct GenSt : Gen {
+    static bool is_float_like(uint32_t rt) { return (rt & 1u) && (rt & 6u); }
+    uint32_t tsize(uint32_t t, uint32_t rt) const { return size_flat(t * 6u + rt); }
+    uint32_t tab3(const uint32_t* tab, uint32_t t, uint32_t s, uint32_t rt) const { return tab[t * 24u + s * 6u + rt]; }
+
+    // rv_generator.cpp:227-314
+    void preprocess_st() {
+        for (size_t i = 0; i < n; ++i) {  // argument placement, :231-284
+            uint32_t t = node_types[i];
+            if ((t & port::T_FUNC_ARG) != port::T_FUNC_ARG) continue;
+            const uint32_t rt = result_types[i];
+            uint32_t nd = node_data[i];
+            const bool fl = is_float_like(rt);
+            if (fl && nd < 8u) continue;
+            const int32_t ci = child_idx[i];
+            const int32_t ints = fl ? static_cast<int32_t>(static_cast<uint32_t>(ci) - nd) : static_cast<int32_t>(nd);
+            const int32_t floats = ci - ints;
+            const int32_t ir = ints + std::max<int32_t>(floats - 8, 0);
+            if (ir < 8) {
+                nd = static_cast<uint32_t>(ir);
+                if (fl) t |= 0b01u;
+            } else {
+                t |= 0b10u;
+                nd = static_cast<uint32_t>(ir - 8);
+            }
+            node_types[i] = t;
+            node_data[i] = nd;
+        }
+        for (size_t i = 1; i < n; ++i) {  // call argument lists, :287-304
+            if (node_types[i] != port::T_FUNC_CALL_ARG_LIST) continue;
+            const size_t prev = i - 1;
+            int64_t stack_args = 0;
+            if (node_types[prev] == port::T_FUNC_CALL_ARG) {
+                if (result_types[prev] == port::D_FLOAT) {
+                    const int64_t int_args = static_cast<int64_t>(child_idx[prev]) - static_cast<int64_t>(node_data[prev]);
+                    stack_args = std::max<int64_t>(int_args - 8, 0);
+                }
+            } else if (node_types[prev] == port::T_FUNC_CALL_ARG_ON_STACK) {
+                stack_args = static_cast<uint32_t>(node_data[prev] + 1u);
+            }
+            node_data[i] = static_cast<uint32_t>(stack_args);
+        }
+        for (size_t i = 0; i < n; ++i) {  // float comparisons, :306-313
+            const int32_t p = parents[i];
+            if (p >= 0 && (node_types[p] & port::T_EQ) == port::T_EQ && result_types[i] == port::D_FLOAT) {
+                result_types[p] = port::D_FLOAT;
+            }
+        }
+    }
+
+    // rv_generator.cpp:316-446
+    void isn_cnt_st() {
+        for (size_t i = 0; i < n; ++i) {
+            const uint32_t t = node_types[i];
+            uint32_t delta = 0;
+            if (i > 0 && t == port::T_FUNC_CALL_ARG_LIST) {
+                delta = 1;
+                if ((node_types[i - 1] & port::T_FUNC_CALL_ARG) == port::T_FUNC_CALL_ARG) {
+                    delta += static_cast<uint32_t>(child_idx[i - 1]) + 1u;
+                }
+            }
+            const int32_t p = parents[i];
+            if (p != -1) {
+                const uint32_t pt = p >= 0 ? node_types[p] : static_cast<uint32_t>(port::T_STATEMENT_LIST);
+                const int32_t ci = child_idx[i];
+                if (ci == 0 && (pt == port::T_IF || pt == port::T_IF_ELSE)) delta += 1;
+                else if (ci == 1 && (pt == port::T_IF_ELSE || pt == port::T_WHILE)) delta += 1;
+            }
+            node_sizes[i] = tsize(t, result_types[i]) + delta;
+        }
+        uint32_t acc = 0;
+        for (size_t i = 0; i < n; ++i) {
+            node_locations[i] = acc;
+            acc += node_sizes[i];
+        }
+        for (size_t i = 0; i < n; ++i) {
+            if (node_types[i] == port::T_INVALID) node_locations[i] = 0xFFFFFFFFu;
+        }
+        std::vector<int64_t> fix_idx(n, -1);
+        std::vector<uint32_t> fix_val(n, 0);
+        for (size_t i = 0; i < n; ++i) {
+            const int32_t p = parents[i];
+            if (p == -1) continue;
+            const uint32_t pt = node_types[p];
+            if ((pt & port::T_IF) == port::T_IF && child_idx[i] == static_cast<int32_t>(pt & 1u)) {
+                fix_idx[i] = p;
+                fix_val[i] = node_locations[i] + tsize(node_types[i], result_types[i]);
+            } else if ((node_types[i] & port::T_FUNC_CALL_ARG) == port::T_FUNC_CALL_ARG) {
+                fix_idx[i] = static_cast<int64_t>(i);
+                fix_val[i] = node_locations[p] + static_cast<uint32_t>(child_idx[i]) + 1u;
+            }
+        }
+        for (size_t i = 0; i < n; ++i) {
+            if (fix_idx[i] >= 0) node_locations[fix_idx[i]] = fix_val[i];
+        }
+        std::vector<uint32_t> decls;
+        for (size_t i = 0; i < n; ++i) if (node_types[i] == port::T_FUNC_DECL) decls.push_back(static_cast<uint32_t>(i));
+        const size_t F = decls.size();
+        if (F == 0) throw Unsupported("program has no function (the reference takes the max of an empty range)");
+        function_ids.resize(F);
+        func_starts.resize(F);
+        func_ends.resize(F);
+        function_sizes.resize(F);
+        for (size_t f = 0; f < F; ++f) {
+            function_ids[f] = node_data[decls[f]];
+            const uint32_t off = node_locations[decls[f]] + 6u;
+            const uint32_t prev = f == 0 ? 0u : node_locations[decls[f - 1]] + 6u;
+            function_sizes[f] = f == 0 ? off : off - prev;
+            func_starts[f] = prev;
+            func_ends[f] = prev + function_sizes[f];
+        }
+    }
+
+    // rv_generator.cpp:448-809
+    void isn_gen_st() {
+        std::vector<uint32_t> idx_array(n);
+        std::iota(idx_array.begin(), idx_array.end(), 0u);
+        std::sort(idx_array.begin(), idx_array.end(), [this](uint32_t a, uint32_t b) { return depth[a] < depth[b]; });
+        std::vector<uint32_t> depth_starts;
+        for (size_t i = 0; i < n; ++i) {
+            if (i == 0 || depth[idx_array[i]] != depth[idx_array[i - 1]]) depth_starts.push_back(static_cast<uint32_t>(i));
+        }
+        if (depth_starts.size() != max_depth + 1) throw Unsupported("depths 0..max_depth are not all populated");
+        const uint32_t W = node_locations[static_cast<int64_t>(n) - 1];
+        std::vector<int64_t> registers(n * 3, 0);
+        instr.resize(W); rd.resize(W); rs1.resize(W); rs2.resize(W); jt.resize(W);
+        const uint32_t* has_instr = &T.has_instr[0][0][0];
+        const uint32_t* has_output = &T.has_output[0][0][0];
+        const uint32_t* pai_tab = &T.pai[0][0][0];
+        const uint32_t* out_tab = &T.out[0][0][0];
+        const uint32_t* instr_tab = &T.instr[0][0][0];
+        const uint32_t* const_tab = &T.cnst[0][0];
+        const uint32_t* operand_tab = &T.operand[0][0][0][0];
+        const uint32_t* jt_tab = &T.jt[0][0];
+        const size_t F = func_starts.size();
+
+        auto parent_arg_idx = [&](uint32_t node, uint32_t s) -> int64_t {
+            const int64_t pidx = static_cast<int64_t>(parents[node]) * 3 + child_idx[node];
+            auto lookup = [&]() -> int64_t {
+                const uint32_t calc = tab3(pai_tab, node_types[node], s, result_types[node]);
+                if (calc == 1) return pidx;
+                if (calc == 2 && result_types[node] > 1u) return pidx;
+                return -1;
+            };
+            const int32_t p = parents[node];
+            if (p == -1) return lookup();
+            const uint32_t pt = node_types[p];
+            const int32_t ci = child_idx[node];
+            if (ci > 0 && (pt == port::T_IF || pt == port::T_IF_ELSE)) return pidx;
+            if ((ci == 0 || ci == 2) && pt == port::T_WHILE) return pidx;
+            return lookup();
+        };
+        auto prop_value = [&](uint32_t node, int64_t rdv, int64_t off) -> int64_t {
+            const int32_t p = parents[node];
+            if (p == -1) return rdv;
+            const uint32_t pt = node_types[p];
+            const int32_t ci = child_idx[node];
+            const int64_t instr_no = off + tsize(node_types[node], result_types[node]);
+            if (pt == port::T_IF || pt == port::T_IF_ELSE) return (ci == 1 || ci == 2) ? instr_no : rdv;
+            if (pt == port::T_WHILE) return (ci == 0 || ci == 2) ? instr_no : rdv;
+            return rdv;
+        };
+        auto extend12 = [](uint32_t x) { return static_cast<uint32_t>(static_cast<int32_t>(x << 20) >> 20); };
+
+        struct Entry { int64_t at, pidx; uint32_t word, jtv; int64_t rdv, r1, r2, reg; };
+        std::vector<Entry> entries;
+        for (size_t lvl = 0; lvl <= max_depth; ++lvl) {
+            const size_t cur = max_depth - lvl;
+            const uint32_t start = depth_starts[cur];
+            const uint32_t end = cur == max_depth ? static_cast<uint32_t>(n) : depth_starts[cur + 1];
+            entries.clear();
+            for (uint32_t k = start; k < end; ++k) {
+                const uint32_t idx = idx_array[k];
+                const uint32_t t = node_types[idx], rt = result_types[idx], nd = node_data[idx];
+                const int64_t* reg = &registers[static_cast<size_t>(idx) * 3];
+                for (uint32_t s = 0; s < 4; ++s) {
+                    Entry e{-1, -1, 0, 0, 0, 0, 0, 0};
+                    if (tab3(has_instr, t, s, rt)) {
+                        const uint32_t iib = node_locations[idx] + s;
+                        const uint32_t oc = tab3(out_tab, t, s, rt);
+                        int64_t rdv;
+                        if (oc == 1) rdv = static_cast<uint32_t>(nd + 10u);
+                        else if (oc == 2) rdv = static_cast<uint32_t>(nd + 42u);
+                        else if (oc == 3) rdv = 32;
+                        else if (oc == 4) rdv = 10;
+                        else rdv = (parent_arg_idx(idx, s) != -1 || tab3(has_output, t, s, rt)) ? static_cast<uint32_t>(iib + 64u) : 0;
+                        int64_t at;
+                        if (s == 1 && t == port::T_IF_ELSE) at = reg[1];
+                        else if (s == 1 && t == port::T_WHILE) at = reg[2];
+                        else if ((s >= 2 && t == port::T_FUNC_DECL_DUMMY) || t == port::T_FUNC_DECL) at = static_cast<uint32_t>(iib + 2u);
+                        else if (s == 1 && t == port::T_FUNC_CALL_ARG_LIST) {
+                            uint32_t res = iib + 2u;
+                            if (idx != 0) {
+                                const uint32_t pv = node_types[idx - 1];
+                                if (pv == port::T_FUNC_CALL_ARG || pv == port::T_FUNC_CALL_ARG_FLOAT_AS_INT ||
+                                    pv == port::T_FUNC_CALL_ARG_ON_STACK) {
+                                    res += static_cast<uint32_t>(child_idx[idx - 1]);
+                                }
+                            }
+                            at = res;
+                        } else {
+                            at = iib;
+                        }
+                        e.at = static_cast<int32_t>(at);
+                        e.pidx = static_cast<int32_t>(parent_arg_idx(idx, s));
+                        uint32_t w = tab3(instr_tab, t, s, rt);
+                        switch (const_tab[t * 4u + s]) {
+                            case 1: w |= (nd - extend12(nd & 0xFFFu)) & 0xFFFFF000u; break;
+                            case 2: w |= (nd & 0xFFFu) << 20; break;
+                            case 3: w |= static_cast<uint32_t>(-(4 * (static_cast<int64_t>(static_cast<int32_t>(nd)) + 2))) << 20; break;
+                            case 4: w |= (4u * nd) << 20; break;
+                            case 5: w |= static_cast<uint32_t>(-(4 * static_cast<int64_t>(static_cast<int32_t>(nd)))) << 20; break;
+                            default: break;
+                        }
+                        e.word = w;
+                        e.rdv = rdv;
+                        for (uint32_t a = 0; a < 2; ++a) {
+                            int64_t v = 0;
+                            switch (operand_tab[(t * 24u + s * 6u + rt) * 2u + a]) {
+                                case 1: v = reg[a]; break;
+                                case 2: v = static_cast<uint32_t>(nd + 10u); break;
+                                case 3: v = static_cast<uint32_t>(nd + 42u); break;
+                                case 4: v = reg[1]; break;
+                                case 5: v = reg[1 - a]; break;
+                                case 6: v = reg[0]; break;
+                                case 7: v = static_cast<int64_t>(iib) + 64 - 1; break;
+                                default: break;
+                            }
+                            (a == 0 ? e.r1 : e.r2) = v;
+                        }
+                        int64_t j = 0;
+                        switch (jt_tab[t * 4u + s]) {
+                            case 1: j = reg[1]; break;
+                            case 2: j = reg[1] + 1; break;
+                            case 3: j = reg[2]; break;
+                            case 4: j = reg[2] + 1; break;
+                            case 5: j = reg[0]; break;
+                            case 6: if (nd >= F) throw Unsupported("jump to a function past the table"); j = func_ends[nd] - 6u; break;
+                            case 7: if (nd >= F) throw Unsupported("jump to a function past the table"); j = func_starts[nd]; break;
+                            default: break;
+                        }
+                        e.jtv = static_cast<uint32_t>(j);
+                        e.reg = prop_value(idx, rdv, iib);
+                    } else if (s == 0) {
+                        e.pidx = static_cast<int32_t>(parent_arg_idx(idx, 0));
+                        e.reg = prop_value(idx, 0, node_locations[idx]);
+                    } else {
+                        continue;
+                    }
+                    entries.push_back(e);
+                }
+            }
+            for (const Entry& e : entries) {
+                if (e.at >= 0 && e.at < static_cast<int64_t>(W)) {
+                    instr[e.at] = e.word;
+                    rd[e.at] = static_cast<uint32_t>(e.rdv);
+                    rs1[e.at] = static_cast<uint32_t>(e.r1);
+                    rs2[e.at] = static_cast<uint32_t>(e.r2);
+                    jt[e.at] = e.jtv;
+                }
+            }
+            for (const Entry& e : entries) {
+                if (e.pidx >= 0 && e.pidx < static_cast<int64_t>(registers.size())) registers[e.pidx] = e.reg;
+            }
+        }
+    }
+
+    // rv_generator.cpp:811-900 (Jacobi iterations to the fixed point)
+    void optimize_st() {
+        const size_t W = instr.size();
+        std::vector<uint8_t> used(W, 0);
+        auto in_range = [W](int64_t v) { return v >= 0 && v < static_cast<int64_t>(W); };
+        for (size_t i = 0; i < W; ++i) {
+            if (in_range(int64_t(rs1[i]) - 64)) used[rs1[i] - 64] = 1;
+            if (in_range(int64_t(rs2[i]) - 64)) used[rs2[i] - 64] = 1;
+        }
+        for (;;) {
+            const std::vector<uint8_t> before = used;
+            std::vector<uint8_t> next = used;
+            for (size_t i = 0; i < W; ++i) {
+                if (rd[i] < 64u) continue;
+                if (!in_range(int64_t(rd[i]) - 64)) throw Unsupported("rd names a word past the program");
+                if (before[rd[i] - 64]) continue;
+                if (in_range(int64_t(rs1[i]) - 64)) next[rs1[i] - 64] = 0;
+                if (in_range(int64_t(rs2[i]) - 64)) next[rs2[i] - 64] = 0;
+            }
+            for (size_t i = 0; i < W; ++i) {
+                const uint32_t m = instr[i] & 0x707Fu;
+                if (m != 0x2023u && m != 0x2027u) continue;  // sw, fsw
+                if (in_range(int64_t(rs1[i]) - 64)) next[rs1[i] - 64] = 1;
+                if (in_range(int64_t(rs2[i]) - 64)) next[rs2[i] - 64] = 1;
+            }
+            used = next;
+            if (used == before) break;
+        }
+        used_instrs.resize(W);
+        for (size_t i = 0; i < W; ++i) used_instrs[i] = (rd[i] < 64u || used[i]) ? 1u : 0u;
+    }
+
+    // rv_generator.cpp:1619-1720
+    void fix_jumps_st() {
+        const size_t W = instr.size();
+        auto is_jump = [](uint32_t w) { return (w & 0x7Fu) == 0x67u && w != 0x00008067u; };
+        std::vector<int64_t> sizes(W), offs(W);
+        for (size_t i = 0; i < W; ++i) sizes[i] = is_jump(instr[i]) ? 2 : (instr[i] == 0 ? 0 : 1);
+        int64_t acc = 0;
+        for (size_t i = 0; i < W; ++i) { offs[i] = acc; acc += sizes[i]; }
+        const int64_t count = W == 0 ? 0 : sizes[W - 1] + offs[W - 1];
+        PBuf<uint32_t> ni(count), nrd(count), nr1(count), nr2(count), njt(count);
+        for (size_t i = 0; i < W; ++i) {
+            const int64_t at = offs[i];
+            if (at >= count) throw Unsupported("word past the output");
+            ni[at] = instr[i]; nrd[at] = rd[i]; nr1[at] = rs1[i]; nr2[at] = rs2[i]; njt[at] = jt[i];
+        }
+        for (int64_t i = 0; i < count; ++i) {
+            if (njt[i] >= W) throw Unsupported("jump target past the words");
+            njt[i] = static_cast<uint32_t>(offs[njt[i]]);
+        }
+        struct Put { int64_t at; uint32_t w, d, a, b; };
+        std::vector<Put> puts;
+        for (size_t i = 0; i < W; ++i) {
+            const int64_t at = offs[i];
+            const uint32_t w = ni[at];
+            const bool jump = is_jump(w), branch = (w & 0x7Fu) == 0x63u;
+            if (!jump && !branch) continue;
+            const uint32_t delta = static_cast<uint32_t>(static_cast<int64_t>(njt[at]) * 4 - at * 4);
+            if (jump) {
+                const uint32_t upper = ((delta & 0xFFFFF000u) >> 12) + ((delta >> 11) & 1u);
+                puts.push_back({at, 0x97u | (upper << 12), 0, 0, 0});
+                puts.push_back({at + 1, w | ((delta & 0xFFFu) << 20) | (1u << 15), 0, 0, 0});
+            } else {
+                const uint32_t word = w | (((delta >> 12) & 1u) << 31) | (((delta >> 11) & 1u) << 7) |
+                                      (((delta >> 5) & 0x1Fu) << 25) | (((delta >> 1) & 0xFu) << 8);
+                puts.push_back({at, word, nrd[at], nr1[at], nr2[at]});
+            }
+        }
+        for (const Put& p : puts) {
+            if (p.at < 0 || p.at >= count) continue;
+            ni[p.at] = p.w; njt[p.at] = 0; nrd[p.at] = p.d; nr1[p.at] = p.a; nr2[p.at] = p.b;
+        }
+        instr = ni.clone(); rd = nrd.clone(); rs1 = nr1.clone(); rs2 = nr2.clone(); jt = njt.clone();
+        PBuf<uint32_t> o(W);
+        for (size_t i = 0; i < W; ++i) o[i] = static_cast<uint32_t>(offs[i]);
+        fix_func_tab(o, W);
+    }
+
+    // rv_generator.cpp:902-1602
+    void regalloc_st() {
+        const size_t W = instr.size();
+        const size_t F = function_sizes.size();
+        uint32_t S = 0;
+        for (size_t f = 0; f < F; ++f) S = std::max(S, function_sizes[f]);
+        for (size_t f = 0; f < F; ++f) {
+            if (func_starts[f] > W || function_sizes[f] > W - func_starts[f]) throw Unsupported("function past the words");
+        }
+        constexpr uint64_t kPreserved = 0x0FFC03000FFC031Full, kNonscratch = 0x0FFC03000FFC0200ull;
+        std::vector<uint64_t> lifetime(F, 0x1Full), preserve(F, 0);
+        std::vector<uint8_t> sym_reg(W, 0), sym_swp(W, 0);
+        std::vector<int64_t> state(F * 64, -1);
+        auto needs_float = [](uint32_t w, int which) {
+            if (w == 0xC0007053u) return which != 0;
+            if (w == 0xD0007053u) return which == 0;
+            return (w & 0x7Fu) == 0x53u;
+        };
+        auto check_sym = [W](uint32_t r) {
+            if (r >= 64u && r - 64u >= W) throw Unsupported("a register names a word past the program");
+        };
+        struct Step {
+            uint64_t mask = 0;
+            int64_t sym[3] = {-1, -1, -1};  // symbols the step assigns
+            uint8_t phys[3] = {0, 0, 0};
+            uint64_t swapped = 0;           // physical registers whose symbols are swapped out
+            bool act = false, call = false;
+            uint32_t rdv = 0, rd_phys = 0, r1_phys = 0, r2_phys = 0;
+        };
+        std::vector<Step> steps(F);
+        for (uint32_t i = 0; i < S; ++i) {
+            for (size_t f = 0; f < F; ++f) {
+                Step& st = steps[f];
+                st = Step{};
+                st.mask = lifetime[f];
+                if (i >= function_sizes[f]) continue;
+                const uint32_t off = func_starts[f] + i;
+                if (!used_instrs[off]) continue;
+                st.act = true;
+                const uint32_t w = instr[off];
+                const uint32_t start = func_starts[f], end = start + function_sizes[f];
+                if (w == 0x000000EFu && (jt[off] < start || jt[off] >= end)) {  // a call, :967-1000
+                    st.call = true;
+                    st.mask = lifetime[f] & kPreserved;
+                    const uint64_t spilled = lifetime[f] & ~kPreserved;
+                    st.swapped = spilled;
+                    continue;
+                }
+                check_sym(rs1[off]); check_sym(rs2[off]); check_sym(rd[off]);
+                auto sym_of = [&](uint32_t r, uint32_t* reg, bool* sw) {
+                    if (r < 64u) { *reg = r; *sw = false; }
+                    else { *reg = sym_reg[r - 64u]; *sw = sym_swp[r - 64u] != 0; }
+                };
+                uint32_t p1, p2;
+                bool s1, s2;
+                sym_of(rs1[off], &p1, &s1);
+                sym_of(rs2[off], &p2, &s2);
+                if (s1) p1 = needs_float(w, 1) ? 37u : 5u;
+                if (s2) p2 = needs_float(w, 2) ? 38u : 6u;
+                uint64_t cleared = lifetime[f];
+                if (p1 != 0) cleared &= ~(1ull << p1);
+                if (p2 != 0) cleared &= ~(1ull << p2);
+                uint32_t prd = rd[off];
+                if (prd >= 64u) {
+                    const bool fl = needs_float(w, 0);
+                    const uint64_t fixed = cleared | (0xFFFFFFFFull << (fl ? 0 : 32));
+                    const uint32_t low = ~static_cast<uint32_t>(fixed);  // the reference's ffs takes an int
+                    if (low == 0) prd = fl ? 37u : 5u;
+                    else prd = static_cast<uint32_t>(__builtin_ctz(low));
+                }
+                if (prd != 0 && ((cleared >> prd) & 1u)) st.swapped |= 1ull << prd;
+                if (p1 != 0 && ((lifetime[f] >> p1) & 1u)) st.swapped |= 1ull << p1;
+                if (p2 != 0 && ((lifetime[f] >> p2) & 1u)) st.swapped |= 1ull << p2;
+                st.mask = cleared | (1ull << prd);
+                const uint32_t named[3] = {rd[off], rs1[off], rs2[off]};
+                const uint32_t phys[3] = {prd, p1, p2};
+                for (int k = 0; k < 3; ++k) {
+                    st.sym[k] = named[k] >= 64u ? static_cast<int64_t>(named[k]) - 64 : -1;
+                    st.phys[k] = static_cast<uint8_t>(phys[k]);
+                }
+                st.rdv = rd[off];
+                st.rd_phys = prd;
+                st.r1_phys = p1;
+                st.r2_phys = p2;
+            }
+            // swapped symbols keep their register and read as swapped; then the step's
+            // symbols take their registers (later writes win, every swap first)
+            for (size_t f = 0; f < F; ++f) {
+                for (int p = 0; p < 64; ++p) {
+                    if (!((steps[f].swapped >> p) & 1u)) continue;
+                    const int64_t v = state[f * 64 + p];
+                    if (v >= 64 && v - 64 < static_cast<int64_t>(W)) sym_swp[v - 64] = 1;
+                }
+            }
+            for (size_t f = 0; f < F; ++f) {
+                for (int k = 0; k < 3; ++k) {
+                    const int64_t v = steps[f].sym[k];
+                    if (v >= 0 && v < static_cast<int64_t>(W)) { sym_reg[v] = steps[f].phys[k]; sym_swp[v] = 0; }
+                }
+            }
+            for (size_t f = 0; f < F; ++f) {
+                const Step& st = steps[f];
+                lifetime[f] = st.mask;
+                preserve[f] |= lifetime[f];
+                if (!st.act) continue;
+                int64_t* rs = &state[f * 64];
+                if (st.call) {
+                    for (int p = 0; p < 64; ++p) if (!((st.mask >> p) & 1u)) rs[p] = -1;
+                } else {
+                    rs[st.rd_phys] = st.rdv;
+                    if (st.r1_phys != st.rd_phys) rs[st.r1_phys] = -1;
+                    if (st.r2_phys != st.rd_phys) rs[st.r2_phys] = -1;
+                }
+            }
+        }
+        for (size_t f = 0; f < F; ++f) preserve[f] &= kNonscratch;
+
+        // spill slots: the swapped flag of each function's first word, held to the next
+        // function start (:1290-1300)
+        std::vector<uint8_t> is_start(W + 1, 0);
+        for (size_t f = 0; f < F; ++f) if (func_starts[f] < W) is_start[func_starts[f]] = 1;
+        std::vector<uint32_t> spill(W, 0);
+        for (size_t v = 0; v < W; ++v) spill[v] = is_start[v] ? sym_swp[v] : (v > 0 ? spill[v - 1] : 0u);
+
+        // counts, preserve words, offsets (:1302-1340)
+        std::vector<int64_t> counts(W, 0);
+        for (size_t i = 0; i < W; ++i) {
+            if (!used_instrs[i]) continue;
+            int64_t c = 1;
+            for (uint32_t r : {rd[i], rs1[i], rs2[i]}) {
+                check_sym(r);
+                if (r >= 64u && sym_swp[r - 64u]) ++c;
+            }
+            counts[i] = c;
+        }
+        for (size_t f = 0; f < F; ++f) {
+            const int64_t pc = __builtin_popcountll(preserve[f]);
+            const int64_t a = static_cast<int64_t>(func_starts[f]) + 5;
+            const int64_t b = static_cast<int64_t>(func_starts[f]) + function_sizes[f] - 6;
+            if (a < 0 || b < 0 || a >= static_cast<int64_t>(W) || b >= static_cast<int64_t>(W))
+                throw Unsupported("preserve words counted past the program");
+            counts[a] += pc;
+            counts[b] += pc;
+        }
+        PBuf<uint32_t> offs(W);
+        {
+            int64_t acc = 0;
+            for (size_t i = 0; i < W; ++i) { offs[i] = static_cast<uint32_t>(acc); acc += counts[i]; }
+        }
+        const size_t W2 = W == 0 ? 0 : static_cast<size_t>(offs[static_cast<int64_t>(W) - 1]) + 1;
+        PBuf<uint32_t> ni(W2), nrd(W2), nr1(W2), nr2(W2), njt(W2);
+        auto put = [&](int64_t at, uint32_t w, uint32_t d, uint32_t a, uint32_t b, uint32_t j) {
+            if (at < 0 || at >= static_cast<int64_t>(W2)) return;
+            ni[at] = w; nrd[at] = d; nr1[at] = a; nr2[at] = b; njt[at] = j;
+        };
+        for (size_t i = 0; i < W; ++i) {  // :1354-1480
+            if (!used_instrs[i]) continue;
+            const int64_t base = offs[i];
+            const uint32_t a1 = rs1[i], a2 = rs2[i], ad = rd[i];
+            const bool sw1 = a1 >= 64u && sym_swp[a1 - 64u];
+            const bool sw2 = a2 >= 64u && sym_swp[a2 - 64u];
+            const bool swd = ad >= 64u && sym_swp[ad - 64u];
+            const int64_t l1 = sw1 ? base : -1;
+            const int64_t l2 = sw2 ? base + (l1 > 0 ? 1 : 0) : -1;
+            const int64_t mo = base + (l1 > 0 ? 1 : 0) + (l2 > 0 ? 1 : 0);
+            const int64_t so = swd ? mo + 1 : -1;
+            const uint32_t prd = ad >= 64u ? sym_reg[ad - 64u] : ad;
+            uint32_t p1 = a1, p2 = a2;
+            if (a1 >= 64u) p1 = sw1 ? (needs_float(instr[i], 1) ? 37u : 5u) : sym_reg[a1 - 64u];
+            if (a2 >= 64u) p2 = sw2 ? (needs_float(instr[i], 2) ? 38u : 6u) : sym_reg[a2 - 64u];
+            const uint32_t st1 = sw1 ? spill[a1 - 64u] : 0u;
+            const uint32_t st2 = sw2 ? spill[a2 - 64u] : 0u;
+            const uint32_t std_ = swd ? spill[ad - 64u] : 0u;
+            if (l1 >= 0) put(l1, 0x2003u | ((4u * (st1 - 1u)) << 20), 5, 0, 0, 0);
+            if (l2 >= 0) put(l2, 0x2003u | ((4u * (st2 - 1u)) << 20), 6, 0, 0, 0);
+            // the offsets hold W values in a zeroed allocation: just past them reads 0
+            if (jt[i] >= W + 8) throw Unsupported("jump target past the program");
+            put(mo, instr[i], prd, p1, p2, jt[i] < W ? offs[jt[i]] : 0u);
+            if (so >= 0) {
+                const uint32_t imm = 0u - 4u * (std_ - 1u);
+                put(so, 0x2023u | ((imm & 0x1Fu) << 7) | ((imm & 0xFEu) << 19), 0, prd, 0, 0);
+            }
+        }
+        instr = ni.clone(); rd = nrd.clone(); rs1 = nr1.clone(); rs2 = nr2.clone(); jt = njt.clone();
+        fix_func_tab(offs, W);
+        // frame words, preserve stores, preserve loads: one scatter in that order (:1509-1602)
+        std::vector<std::pair<int64_t, uint32_t>> frame;
+        for (size_t f = 0; f < F; ++f) {
+            const uint32_t ss = (static_cast<uint32_t>(__builtin_popcountll(preserve[f])) + 2u) * 4u;
+            const uint32_t lower = (ss & 0xFFFu) << 20;
+            const uint32_t sx = static_cast<uint32_t>(static_cast<int32_t>((ss & 0xFFFu) << 20) >> 20);
+            const uint32_t upper = (ss - sx) & 0xFFFFF000u;
+            const int64_t st = func_starts[f], sz = function_sizes[f];
+            frame.push_back({st + 2, 0x437u | upper});
+            frame.push_back({st + 3, 0x40413u | lower});
+            frame.push_back({st + sz - 6, 0x437u | upper});
+            frame.push_back({st + sz - 5, 0x40413u | lower});
+        }
+        for (int pass = 0; pass < 2; ++pass) {
+            for (size_t f = 0; f < F; ++f) {
+                const uint64_t pm = preserve[f];
+                const int64_t st = func_starts[f], sz = function_sizes[f];
+                for (uint32_t j = 0; j < 64; ++j) {
+                    if (!((pm >> j) & 1u)) continue;
+                    const int64_t lead = __builtin_popcountll(pm & ((1ull << j) - 1));
+                    const int64_t offset = -(8 + lead * 4);
+                    if (pass == 0) {
+                        const uint32_t w = (j >= 32 ? 0x42027u : 0x42023u) | static_cast<uint32_t>((offset & 0xFE0) << 25) |
+                                           static_cast<uint32_t>((offset & 0x1F) << 7) | ((j % 32) << 20);
+                        frame.push_back({st + lead + 6, w});
+                    } else {
+                        const uint32_t w = (j >= 32 ? 0x42007u : 0x42003u) | (static_cast<uint32_t>(offset) << 20) | ((j % 32) << 7);
+                        frame.push_back({st + sz + lead - 7, w});
+                    }
+                }
+            }
+        }
+        for (auto& fw : frame) {
+            if (fw.first < 0 || fw.first >= static_cast<int64_t>(W2)) continue;
+            instr[fw.first] = fw.second; rd[fw.first] = 0; rs1[fw.first] = 0; rs2[fw.first] = 0; jt[fw.first] = 0;
+        }
+    }
+};
+
 template <typename B>
 ptlport_buf copy_out(const B& b) {
     ptlport_buf o{nullptr, b.size()};
@@ -867,10 +1444,11 @@ void set_err(char* err, size_t errlen, const char* msg) {
 
 }  // namespace
 
-extern "C" int ptlport_compile(const uint8_t* type, const uint8_t* rtype, const int32_t* parent,
-                               const int32_t* depth, const int32_t* child_idx, const uint32_t* data,
-                               size_t n, size_t max_depth, int snapshots, ptlport_result* out,
-                               char* err, size_t errlen) {
+namespace {
+
+int compile_impl(const uint8_t* type, const uint8_t* rtype, const int32_t* parent, const int32_t* depth,
+                 const int32_t* child_idx, const uint32_t* data, size_t n, size_t max_depth, int snapshots,
+                 ptlport_result* out, char* err, size_t errlen, bool scalar) {
     std::memset(out, 0, sizeof(*out));
     if (n == 0) { set_err(err, errlen, "empty tree"); return PTLPORT_EINVAL; }
     if (max_depth == 0) { set_err(err, errlen, "max_depth is 0 (the reference divides by it)"); return PTLPORT_EINVAL; }
@@ -878,7 +1456,7 @@ extern "C" int ptlport_compile(const uint8_t* type, const uint8_t* rtype, const 
         if (type[i] >= 44 || rtype[i] > 5) { set_err(err, errlen, "node type or data type out of range"); return PTLPORT_EINVAL; }
     }
     try {
-        Gen g;
+        GenSt g;
         g.n = n;
         g.max_depth = max_depth;
         g.node_types.resize(n); g.result_types.resize(n); g.node_data.resize(n);
@@ -900,13 +1478,13 @@ extern "C" int ptlport_compile(const uint8_t* type, const uint8_t* rtype, const 
             out->stage_ns[idx] = static_cast<uint64_t>(
                 std::chrono::duration_cast<std::chrono::nanoseconds>(clock::now() - t0).count());
         };
-        timed(0, [&] { g.preprocess(); });
+        timed(0, [&] { if (scalar) g.preprocess_st(); else g.preprocess(); });
         if (snapshots) {
             out->bufs[PTLPORT_PRE_TYPE] = copy_out(g.node_types);
             out->bufs[PTLPORT_PRE_RTYPE] = copy_out(g.result_types);
             out->bufs[PTLPORT_PRE_DATA] = copy_out(g.node_data);
         }
-        timed(1, [&] { g.isn_cnt(); });
+        timed(1, [&] { if (scalar) g.isn_cnt_st(); else g.isn_cnt(); });
         if (snapshots) {
             out->bufs[PTLPORT_CNT_SIZE] = copy_out(g.node_sizes);
             out->bufs[PTLPORT_CNT_LOC] = copy_out(g.node_locations);
@@ -915,7 +1493,7 @@ extern "C" int ptlport_compile(const uint8_t* type, const uint8_t* rtype, const 
             out->bufs[PTLPORT_CNT_FN_END] = copy_out(g.func_ends);
             out->bufs[PTLPORT_CNT_FN_SIZE] = copy_out(g.function_sizes);
         }
-        timed(2, [&] { g.isn_gen(); });
+        timed(2, [&] { if (scalar) g.isn_gen_st(); else g.isn_gen(); });
         if (snapshots) {
             out->bufs[PTLPORT_GEN_INSTR] = copy_out(g.instr);
             out->bufs[PTLPORT_GEN_RD] = copy_out(g.rd);
@@ -923,9 +1501,9 @@ extern "C" int ptlport_compile(const uint8_t* type, const uint8_t* rtype, const 
             out->bufs[PTLPORT_GEN_RS2] = copy_out(g.rs2);
             out->bufs[PTLPORT_GEN_JT] = copy_out(g.jt);
         }
-        timed(3, [&] { g.optimize(); });
+        timed(3, [&] { if (scalar) g.optimize_st(); else g.optimize(); });
         if (snapshots) out->bufs[PTLPORT_OPT_USED] = copy_out(g.used_instrs);
-        timed(4, [&] { g.regalloc(); });
+        timed(4, [&] { if (scalar) g.regalloc_st(); else g.regalloc(); });
         if (snapshots) {
             out->bufs[PTLPORT_RA_INSTR] = copy_out(g.instr);
             out->bufs[PTLPORT_RA_RD] = copy_out(g.rd);
@@ -936,7 +1514,7 @@ extern "C" int ptlport_compile(const uint8_t* type, const uint8_t* rtype, const 
             out->bufs[PTLPORT_RA_FN_END] = copy_out(g.func_ends);
             out->bufs[PTLPORT_RA_FN_SIZE] = copy_out(g.function_sizes);
         }
-        timed(5, [&] { g.fix_jumps(); });
+        timed(5, [&] { if (scalar) g.fix_jumps_st(); else g.fix_jumps(); });
         if (snapshots) {
             out->bufs[PTLPORT_FJ_INSTR] = copy_out(g.instr);
             out->bufs[PTLPORT_FJ_RD] = copy_out(g.rd);
@@ -963,6 +1541,24 @@ extern "C" int ptlport_compile(const uint8_t* type, const uint8_t* rtype, const 
         ptlport_free_result(out);
         return PTLPORT_EUNSUPPORTED;
     }
+}
+
+}  // namespace
+
+extern "C" int ptlport_compile(const uint8_t* type, const uint8_t* rtype, const int32_t* parent,
+                               const int32_t* depth, const int32_t* child_idx, const uint32_t* data,
+                               size_t n, size_t max_depth, int snapshots, ptlport_result* out,
+                               char* err, size_t errlen) {
+    return compile_impl(type, rtype, parent, depth, child_idx, data, n, max_depth, snapshots, out, err, errlen,
+                        false);
+}
+
+extern "C" int ptlport_compile_scalar(const uint8_t* type, const uint8_t* rtype, const int32_t* parent,
+                                      const int32_t* depth, const int32_t* child_idx, const uint32_t* data,
+                                      size_t n, size_t max_depth, int snapshots, ptlport_result* out,
+                                      char* err, size_t errlen) {
+    return compile_impl(type, rtype, parent, depth, child_idx, data, n, max_depth, snapshots, out, err, errlen,
+                        true);
 }
 
 extern "C" void ptlport_free_result(ptlport_result* r) {

@@ -3,7 +3,8 @@
  *
  * A scalar CPU restatement of the reference's AVX2 code generator
  * (src/codegen/rv_generator_avx.cpp), run with one worker thread, which is the
- * deterministic configuration whose output the GPU build must reproduce bit for bit.
+ * deterministic configuration whose output the GPU build must reproduce bit for bit,
+ * and of its single-threaded scalar generator (src/codegen/rv_generator.cpp).
  * Parity of this restatement is pinned against the reference itself, compiled from
  * its sources by oracle/ref/Makefile, on the reference's Pareas test inputs and on
  * seeded synthetic programs (tests/test_oracle_pin.py); tests/golden/ carries the
@@ -58,6 +59,13 @@ int ptlport_compile(const uint8_t* type, const uint8_t* rtype, const int32_t* pa
                     size_t n, size_t max_depth, int snapshots, ptlport_result* out,
                     char* err, size_t errlen);
 void ptlport_free_result(ptlport_result* r);
+
+/* The same for the reference's scalar generator rv_generator_st
+ * (src/codegen/rv_generator.cpp:227-1736, the -s flag of src/main.cpp). */
+int ptlport_compile_scalar(const uint8_t* type, const uint8_t* rtype, const int32_t* parent,
+                           const int32_t* depth, const int32_t* child_idx, const uint32_t* data,
+                           size_t n, size_t max_depth, int snapshots, ptlport_result* out,
+                           char* err, size_t errlen);
 
 /* The permutation libstdc++'s std::sort leaves when it sorts iota(n) by key (the
  * reference's isn_gen sort, src/codegen/rv_generator_avx.cpp:539-541), written into

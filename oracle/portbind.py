@@ -60,6 +60,8 @@ def lib():
         L.ptlport_compile.argtypes = [u8p, u8p, i32p, i32p, i32p, u32p, ctypes.c_size_t, ctypes.c_size_t,
                                       ctypes.c_int, ctypes.POINTER(_Result), ctypes.c_char_p, ctypes.c_size_t]
         L.ptlport_compile.restype = ctypes.c_int
+        L.ptlport_compile_scalar.argtypes = L.ptlport_compile.argtypes
+        L.ptlport_compile_scalar.restype = ctypes.c_int
         L.ptlport_free_result.argtypes = [ctypes.POINTER(_Result)]
         L.ptlport_depth_sort.argtypes = [i32p, ctypes.c_size_t, u32p]
         L.ptlport_table.argtypes = [ctypes.c_int, u32p]
@@ -71,7 +73,9 @@ def lib():
     return _lib
 
 
-def compile_ast(ast: Ast, snapshots: bool = False) -> RefResult:
+def compile_ast(ast: Ast, snapshots: bool = False, scalar: bool = False) -> RefResult:
+    """The restatement of rv_generator_avx (one worker thread), or with scalar=True of
+    the scalar generator rv_generator_st (src/codegen/rv_generator.cpp:227-1736)."""
     L = lib()
     a = [np.ascontiguousarray(ast.type, np.uint8), np.ascontiguousarray(ast.rtype, np.uint8),
          np.ascontiguousarray(ast.parent, np.int32), np.ascontiguousarray(ast.depth, np.int32),
@@ -81,7 +85,8 @@ def compile_ast(ast: Ast, snapshots: bool = False) -> RefResult:
             a[4].ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), a[5].ctypes.data_as(ctypes.POINTER(ctypes.c_uint32))]
     r = _Result()
     err = ctypes.create_string_buffer(1024)
-    rc = L.ptlport_compile(*ptrs, ast.n, int(ast.max_depth), int(snapshots), ctypes.byref(r), err, 1024)
+    fn = L.ptlport_compile_scalar if scalar else L.ptlport_compile
+    rc = fn(*ptrs, ast.n, int(ast.max_depth), int(snapshots), ctypes.byref(r), err, 1024)
     if rc != 0:
         raise PortError(rc, "oracle restatement: " + err.value.decode())
     try:

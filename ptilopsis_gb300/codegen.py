@@ -233,10 +233,12 @@ class RvGenerator:
         self._check(self._lib.ptl_generator_upload(self._h, ctypes.byref(view)), "upload")
         self.n = tree.n
 
-    def process(self, profile: bool = False, to_host: bool = True, row0_hash: bool = False) -> None:
+    def process(self, profile: bool = False, to_host: bool = True, row0_hash: bool = False,
+                serial: bool = False) -> None:
         """rv_generator_avx::process.  to_host=False leaves the words on the device;
-        row0_hash=True takes the register allocator's general row-0 lookup (same output)."""
-        flags = (1 if profile else 0) | (0 if to_host else 2) | (4 if row0_hash else 0)
+        row0_hash=True takes the register allocator's general row-0 lookup, serial=True
+        the scalar generator's serial register allocation (both: same output)."""
+        flags = (1 if profile else 0) | (0 if to_host else 2) | (4 if row0_hash else 0) | (8 if serial else 0)
         self._check(self._lib.ptl_generator_process(self._h, flags), "process")
 
     def get_instructions(self) -> np.ndarray:

@@ -270,7 +270,9 @@ struct StageTimer {
     }
 };
 
-ptl_status run_pipeline(ptl_generator* g, bool profile, bool to_host, bool row0_hash) {
+// row0_hash: the AVX allocator's general row-0 lookup; serial: the scalar allocator in
+// the reference's order for every program.  Both leave the output unchanged.
+ptl_status run_pipeline(ptl_generator* g, bool profile, bool to_host, bool row0_hash, bool serial) {
     cudaStream_t s = g->stream;
     const size_t n = g->n;
     const size_t nb8 = r8(n);
@@ -423,7 +425,7 @@ ptl_status run_pipeline(ptl_generator* g, bool profile, bool to_host, bool row0_
             return fail(g, PTL_CUDA_ERROR, "internal: unallocated regalloc state");
         bool cross = false;
         PTL_CU(scalar_regalloc_cross(P, s, &cross));
-        if (cross) {
+        if (cross || serial) {
             PTL_CU(g->sregs.ensure(static_cast<size_t>(g->F) * 64, 4));
             PTL_CU(g->ssteps.ensure(g->F, sizeof(SRaStep)));
             launch_scalar_ra_serial(P, g->sregs.at<int32_t>(), g->ssteps.at<SRaStep>(),
@@ -431,7 +433,7 @@ ptl_status run_pipeline(ptl_generator* g, bool profile, bool to_host, bool row0_
         } else {
             launch_scalar_ra_free(P, g->preserve.at<unsigned long long>(), s);
         }
-        g->ra_serial = cross;
+        g->ra_serial = cross || serial;
         PTL_CU(scan_for(wb8, &sc));
         launch_scalar_ra_count_scan(P, g->preserve.at<unsigned long long>(), g->sextra.at<uint32_t>(), sc, s);
     } else {
@@ -591,7 +593,8 @@ ptl_status ptl_generator_process(ptl_generator* g, int profile) {
     if (!g) return PTL_BAD_ARGUMENT;
     const DeviceScope on_device(g->device);
     if (!on_device.ok()) return fail(g, PTL_CUDA_ERROR, "cudaSetDevice");
-    const ptl_status st = run_pipeline(g, (profile & 1) != 0, (profile & 2) == 0, (profile & 4) != 0);
+    const ptl_status st =
+        run_pipeline(g, (profile & 1) != 0, (profile & 2) == 0, (profile & 4) != 0, (profile & 8) != 0);
     if (st == PTL_OK) g->last_error.clear();
     return st;
 }

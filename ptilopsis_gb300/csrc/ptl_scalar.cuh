@@ -471,7 +471,9 @@ PTL_HD uint32_t st_s_ra_count(const Prog& P, uint32_t i, const uint32_t* extra) 
 PTL_HD void st_s_ra_scatter(const Prog& P, uint32_t i) {
     if (i >= P.W || !P.used_instrs[i]) return;
     const uint32_t r1 = P.rs1[i], r2 = P.rs2[i], r = P.rd[i], ins = P.instr[i];
-    if (!s_sym_ok(P, r1) || !s_sym_ok(P, r2) || !s_sym_ok(P, r) || P.jt[i] >= P.wb8 + 16u) {
+    // the reference's offsets array holds W values in a zeroed allocation: a jump target
+    // just past the words reads 0, one further on is undefined
+    if (!s_sym_ok(P, r1) || !s_sym_ok(P, r2) || !s_sym_ok(P, r) || P.jt[i] >= P.W + 8u) {
         record_error(P.err, ST_UNSUPPORTED, W_RA_SCATTER, i);
         return;
     }
@@ -499,7 +501,7 @@ PTL_HD void st_s_ra_scatter(const Prog& P, uint32_t i) {
     auto load = [](uint32_t stack) { return 0x2003u | ((4u * (stack - 1u)) << 20); };  // lw
     if (sw1) put(l1, load(P.spill[r1 - 64u]), 5u, 0, 0, 0);
     if (sw2) put(l2, load(P.spill[r2 - 64u]), 6u, 0, 0, 0);
-    put(at_main, ins, ard, ar1, ar2, P.roffs[P.jt[i]]);
+    put(at_main, ins, ard, ar1, ar2, P.jt[i] < P.W ? P.roffs[P.jt[i]] : 0u);
     if (swd) {  // sw of the result; the reference keeps imm bits 7:1 in the upper field
         const uint32_t imm = 0u - 4u * (P.spill[r - 64u] - 1u);
         put(so, 0x2023u | ((imm & 0x1Fu) << 7) | ((imm & 0xFEu) << 19), 0, ard, 0, 0);

@@ -355,12 +355,13 @@ PTL_HD uint32_t st_count(const Prog& P, uint32_t i) {
     const uint32_t t = P.nt[i];
     const uint32_t rt = P.rt[i];
     uint32_t v = P.tab.size(t, rt);
-    if (t == RV_FUNC_CALL_ARG_LIST) {
+    if (t == RV_FUNC_CALL_ARG_LIST && (i > 0 || !P.scalar)) {  // the scalar generator skips node 0 (:325)
         v += 1u;
         const int64_t q = static_cast<int64_t>(i) - 1;
         if ((P.nt[q] & RV_FUNC_CALL_ARG) == RV_FUNC_CALL_ARG) v += u32(P.ci[q]) + 1u;
     }
     const int32_t p = P.par[i];
+    if (P.scalar && p == -1) return v;  // and the root's parent (rv_generator.cpp:334)
     const uint32_t pt = P.nt[p != -1 ? p : 0];
     const int32_t ci = P.ci[i];
     const bool if_else = pt == RV_IF_ELSE;
@@ -375,11 +376,17 @@ PTL_HD uint32_t st_count(const Prog& P, uint32_t i) {
 // the other rule, so both run in parallel from the scanned locations: first every node
 // takes its own (or its call-argument) location, then condition children overwrite
 // their parents -- except call arguments, whose list rule comes later in the reference.
+// The scanned location as the fixes read it: the scalar generator first sets the
+// locations of invalid nodes to 0xFFFFFFFF (rv_generator.cpp:364-369).
+PTL_HD uint32_t fix_loc0(const Prog& P, int64_t i) {
+    return (P.scalar && P.nt[i] == RV_INVALID) ? 0xFFFFFFFFu : P.loc0[i];
+}
+
 PTL_HD void st_fix_own(const Prog& P, uint32_t i) {
     if ((P.nt[i] & RV_FUNC_CALL_ARG) == RV_FUNC_CALL_ARG) {
-        P.loc[i] = P.loc0[P.par[i]] + u32(P.ci[i]) + 1u;
+        P.loc[i] = fix_loc0(P, P.par[i]) + u32(P.ci[i]) + 1u;
     } else {
-        P.loc[i] = P.loc0[i];
+        P.loc[i] = fix_loc0(P, i);
     }
 }
 
@@ -393,7 +400,7 @@ PTL_HD void st_fix_cond(const Prog& P, uint32_t i) {
         return;
     }
     if ((pt & RV_FUNC_CALL_ARG) == RV_FUNC_CALL_ARG) return;  // overwritten by the list rule
-    P.loc[p] = P.loc0[i] + P.tab.size(P.nt[i], P.rt[i]);
+    P.loc[p] = fix_loc0(P, i) + P.tab.size(P.nt[i], P.rt[i]);
 }
 
 // Function table, rv_generator_avx.cpp:451-517.  decl[] holds the FUNC_DECL indices in

@@ -6,6 +6,7 @@ oracle/ref/Makefile has built it into oracle/_ref:
     python tests/golden/make_golden.py            # small fixtures, synthetic seeds, tables
     python tests/golden/make_golden.py --large    # the reference's larger Pareas inputs
     python tests/golden/make_golden.py --scalar   # the scalar generator (rv_generator_st)
+    python tests/golden/make_golden.py --scalar-large   # ... on the larger Pareas inputs
 
 For each fixture it stores the DepthTree the reference front end (pareas-ast) builds
 from one of the reference's own Pareas test inputs, and what the reference generator
@@ -184,9 +185,46 @@ def main_scalar() -> None:
         json.dump(manifest, f, indent=1, sort_keys=True)
 
 
+def _scalar_large_one(rel: str) -> dict:
+    import time
+    sys.path.insert(0, HERE)
+    import codec
+    name = "pareas_" + rel.replace("/", "_")
+    with open(os.path.join(HERE, "large", name + ".tree.xz"), "rb") as f:
+        arrs = codec.decode(f.read())
+    entry = next(e for e in json.load(open(os.path.join(HERE, "manifest_large.json")))["fixtures"] if e["name"] == name)
+    ast = refbind.Ast(*arrs, max_depth=entry["max_depth"])
+    t0 = time.time()
+    res = refbind.compile_ast_scalar(ast, snapshots=True)
+    return {"name": name, "words": int(len(res.bufs["out_words"])),
+            "snapshots": {k: [int(len(v)), crc(v)] for k, v in res.bufs.items()},
+            "reference_s": round(time.time() - t0, 1)}
+
+
+def main_scalar_large() -> None:
+    """The scalar generator on the larger Pareas inputs (their trees as committed under
+    large/), as many as finish: its register allocation copies every function's register
+    state at every step, so the reference takes minutes per 100k nodes.  Each result is
+    written as it arrives."""
+    import multiprocessing as mp
+    if not refbind.build(REF):
+        raise SystemExit("the reference could not be built here (needs the reference tree on x86-64)")
+    path = os.path.join(HERE, "manifest_scalar_large.json")
+    out = {"fixtures": []}
+    with mp.get_context("spawn").Pool(max(1, (os.cpu_count() or 2) - 1)) as pool:
+        for e in pool.imap_unordered(_scalar_large_one, LARGE):
+            out["fixtures"].append(e)
+            out["fixtures"].sort(key=lambda x: x["name"])
+            with open(path, "w") as f:
+                json.dump(out, f, indent=1, sort_keys=True)
+            print(f"{e['name']}: {e['words']} words ({e['reference_s']} s)", flush=True)
+
+
 if __name__ == "__main__":
     if "--large" in sys.argv[1:]:
         main_large()
+    elif "--scalar-large" in sys.argv[1:]:
+        main_scalar_large()
     elif "--scalar" in sys.argv[1:]:
         main_scalar()
     else:

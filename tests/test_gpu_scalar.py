@@ -97,3 +97,44 @@ def test_gpu_scalar_rejects_malformed_tree(built_cuda):
         with pytest.raises(PtlError) as e:
             gen.process()
     assert e.value.status == 1
+
+
+@pytest.mark.parametrize("name", [n for n in CASES if not n.startswith("c3_")] + ["c3_program_0", "c3_program_22"])
+def test_gpu_scalar_serial_order_equals_reference(built_cuda, name):
+    """The serial register-allocation kernel (the reference's order over all functions,
+    which programs whose functions name each other's words need) gives the reference's
+    words on every program."""
+    from ptilopsis_gb300 import RvGenerator
+    entry = next(e for e in manifest_scalar()["fixtures"] if e["name"] == name)
+    ast, _ = load_scalar_case(entry)
+    with RvGenerator(ast_to_tree(ast), scalar=True) as gen:
+        gen.process(serial=True)
+        words = gen.get_instructions()
+        for k in ("ra_instr", "ra_rd", "ra_rs1", "ra_rs2", "ra_jt"):
+            assert _crc(k, gen.snapshot(k)) == entry["snapshots"][k], f"{name}: {k}"
+    assert [len(words), crc32(words)] == entry["snapshots"]["out_words"]
+
+
+@pytest.mark.parametrize("case", ["c1_quarter", "c3_large"])
+def test_gpu_scalar_against_oracle_at_scale(built_cuda, case):
+    """Programs larger than the committed cases against the oracle's restatement of the
+    scalar generator: a quarter of the 4.3M-node spilling configuration, and the largest
+    of the first 256 batched-workload programs."""
+    from oracle import portbind
+    from ptilopsis_gb300 import RvGenerator
+    from ptilopsis_gb300.synth import config_params, generate
+    from conftest import tree_to_ast
+    if case == "c1_quarter":
+        tree = generate(config_params("c1", scale=0.25))
+    else:
+        sizes = [(generate(config_params("c3", program=k)).n, k) for k in range(0, 256, 16)]
+        tree = generate(config_params("c3", program=max(sizes)[1]))
+    ref = portbind.compile_ast(tree_to_ast(tree), snapshots=True, scalar=True)
+    with RvGenerator(tree, scalar=True) as gen:
+        gen.process()
+        np.testing.assert_array_equal(gen.get_instructions(), ref.words)
+        t = gen.function_table()
+        np.testing.assert_array_equal(t["starts"], ref.bufs["fn_start"])
+        np.testing.assert_array_equal(t["sizes"], ref.bufs["fn_size"])
+        for k in ("gen_instr", "gen_rd", "ra_instr", "ra_rs1"):
+            np.testing.assert_array_equal(gen.snapshot(k), ref.bufs[k], err_msg=k)

@@ -111,3 +111,41 @@ def test_port_matches_reference_on_large_inputs(built, fx):
     assert len(res.words) == entry["words"]
     for name, (length, c) in entry["snapshots"].items():
         assert len(res.bufs[name]) == length and crc(res.bufs[name]) == c, name
+
+
+# ---------------------------------------------------------------- scalar generator
+@pytest.mark.parametrize("name", [e["name"] for e in __import__("conftest").manifest_scalar()["fixtures"]])
+def test_port_scalar_matches_reference_snapshots(built, name):
+    """The restatement of the scalar generator (rv_generator_st, the -s flag): all 36
+    stage arrays against the CRCs of the reference's scalar run (manifest_scalar.json)."""
+    from conftest import load_scalar_case, manifest_scalar
+    from oracle import portbind
+    entry = next(e for e in manifest_scalar()["fixtures"] if e["name"] == name)
+    ast, gold = load_scalar_case(entry)
+    res = portbind.compile_ast(ast, snapshots=True, scalar=True)
+    for k, (length, c) in entry["snapshots"].items():
+        a = res.bufs[k]
+        if k == "opt_used":  # the reference's flags are bools
+            a = (a != 0).astype(np.uint32)
+        assert len(a) == length and crc(a) == c, k
+    if gold is not None:
+        np.testing.assert_array_equal(res.words, gold["out_words"])
+
+
+@pytest.mark.parametrize("seed", [0x50544C10 + k for k in range(3)])
+def test_port_scalar_matches_reference_on_synthetic(built, seed):
+    if not reference_available():
+        pytest.skip("reference not buildable on this host")
+    from oracle import portbind, refbind
+    from ptilopsis_gb300.synth import SynthParams, generate
+    tree = generate(SynthParams(seed=seed, n_functions=24, median_fn_nodes=600.0, sigma=1.0, spill_frac=0.3,
+                                max_nesting=24, float_frac=0.4))
+    ast = tree_to_ast(tree)
+    ref = refbind.compile_ast_scalar(ast, snapshots=True)
+    port = portbind.compile_ast(ast, snapshots=True, scalar=True)
+    for name in STAGE_BUFS:
+        a = port.bufs[name]
+        b = ref.bufs[name]
+        if name == "opt_used":
+            a, b = (a != 0), (b != 0)
+        np.testing.assert_array_equal(a, b, err_msg=name)
