@@ -223,8 +223,19 @@ struct Model {
             std::vector<SRaStep> steps(F);
             s_ra_serial(P, sregs.data(), steps.data(), preserve.data());
         } else {
+            // the GPU's word tiles (functions by their first word, symbols as bytes)
             int32_t sregs[64];
-            for (uint32_t f = 0; f < F; ++f) s_ra_function(P, f, sregs, preserve.data());
+            constexpr uint32_t T = 4096;
+            std::vector<uint8_t> sym;
+            for (uint32_t b = 0; b <= W / T; ++b) {
+                uint32_t first, last, base;
+                s_ra_tile_functions(P, b, T, &first, &last);
+                const uint32_t count = s_ra_tile_span(P, first, last, &base);
+                sym.assign(count + 1, 0);
+                const SymBytes sy{sym.data(), base, count, P.err};
+                for (uint32_t f = first; f < last; ++f) s_ra_function(P, sy, f, sregs, preserve.data());
+                for (uint32_t k = 0; k < count; ++k) s_ra_tile_writeback(P, sym.data(), base, count, k);
+            }
         }
         g_last_cross = cross != 0;
         if (!check()) return;

@@ -1419,11 +1419,29 @@ __global__ void k_s_pre_float(Prog P) { PTL_FOR(i, P.nb8) st_s_pre_float(P, i); 
 __global__ void k_s_gen_prop(Prog P) { PTL_FOR(x, P.n) st_s_gen_prop(P, x); }
 __global__ void k_s_gen_claim(Prog P) { PTL_FOR(x, P.n) st_s_gen_claim(P, x); }
 __global__ void k_s_gen_write(Prog P) { PTL_FOR(x, P.n) st_s_gen_write(P, x); }
-// One thread per function, its 64-entry register state in local memory.
-constexpr int kScalarRaThreads = 128;
-__global__ void __launch_bounds__(kScalarRaThreads) k_s_ra_free(Prog P, unsigned long long* preserve) {
+// Functions on their own: one warp per tile of the word space (the functions starting in
+// it, one per lane), their symbols as bytes in shared memory (cap bytes; a tile whose
+// words exceed it works on the program's arrays), the 64-entry register state of each
+// function in local memory.
+constexpr int kScalarRaThreads = 32;
+constexpr uint32_t kScalarTileWords = 4096;
+__global__ void __launch_bounds__(kScalarRaThreads) k_s_ra_tiles(Prog P, unsigned long long* preserve, uint32_t cap) {
+    extern __shared__ uint8_t s_sym[];
+    uint32_t first, last, base;
+    s_ra_tile_functions(P, blockIdx.x, kScalarTileWords, &first, &last);
+    const uint32_t count = s_ra_tile_span(P, first, last, &base);
+    if (first >= last) return;
     int32_t regs[64];
-    PTL_FOR(f, P.F) s_ra_function(P, f, regs, preserve);
+    if (count > cap) {
+        for (uint32_t f = first + threadIdx.x; f < last; f += blockDim.x) s_ra_function(P, SymGlobal{P}, f, regs, preserve);
+        return;
+    }
+    for (uint32_t k = threadIdx.x; k < count; k += blockDim.x) s_sym[k] = 0;
+    __syncthreads();
+    const SymBytes sy{s_sym, base, count, P.err};
+    for (uint32_t f = first + threadIdx.x; f < last; f += blockDim.x) s_ra_function(P, sy, f, regs, preserve);
+    __syncthreads();
+    for (uint32_t k = threadIdx.x; k < count; k += blockDim.x) s_ra_tile_writeback(P, s_sym, base, count, k);
 }
 __global__ void k_s_ra_serial(Prog P, int32_t* regs, SRaStep* steps, unsigned long long* preserve) {
     if (blockIdx.x == 0 && threadIdx.x == 0) s_ra_serial(P, regs, steps, preserve);
@@ -1802,8 +1820,18 @@ cudaError_t scalar_regalloc_cross(const Prog& P, cudaStream_t s, bool* cross) {
 }
 
 void launch_scalar_ra_free(const Prog& P, unsigned long long* preserve, cudaStream_t s) {
+    // a tile's words: at most one tile plus the longest function
+    const uint64_t want = (static_cast<uint64_t>(kScalarTileWords) + P.S + 15u) & ~uint64_t(15);
+    const uint32_t cap = static_cast<uint32_t>(std::min<uint64_t>(want, 96u * 1024u));
+    if (allow_dynamic_smem(reinterpret_cast<const void*>(&k_s_ra_tiles), cap) != cudaSuccess) {
+        ErrorWord e{ST_UNSUPPORTED, W_RA1, 0, 0};
+        cudaMemcpyAsync(P.err, &e, sizeof(e), cudaMemcpyHostToDevice, s);
+        cudaStreamSynchronize(s);
+        return;
+    }
+    const uint32_t tiles = P.W / kScalarTileWords + 1u;
     g_launches++;
-    k_s_ra_free<<<grid_for(P.F, kScalarRaThreads), kScalarRaThreads, 0, s>>>(P, preserve);
+    k_s_ra_tiles<<<tiles, kScalarRaThreads, cap, s>>>(P, preserve, cap);
 }
 
 void launch_scalar_ra_serial(const Prog& P, int32_t* regs, SRaStep* steps, unsigned long long* preserve,

@@ -259,10 +259,49 @@ struct SRaStep {
 // names a symbol (word r - 64).
 PTL_HD bool s_sym_ok(const Prog& P, uint32_t r) { return r < 64u || r - 64u < P.W; }
 
-// lifetime_analyze_valid (:959-1145) for function f's word off under lifetime mask; false
+// Where the symbols (register, swapped flag per word) live while the steps run: the
+// program's arrays, or one byte per word of a run of functions (register in bits 0..5,
+// swapped in bit 7) in shared memory -- a function only reads and writes its own words'
+// symbols when it runs on its own.
+struct SymGlobal {
+    const Prog& P;
+    PTL_HD uint32_t reg(uint32_t w) const { return P.symreg[w] & 0xFFu; }
+    PTL_HD bool swapped(uint32_t w) const { return P.symswp[w] != 0; }
+    PTL_HD void mark(uint32_t w) const { P.symswp[w] = 0xFFFFFFFFu; }
+    PTL_HD void assign(uint32_t w, uint32_t r) const {
+        P.symreg[w] = r;
+        P.symswp[w] = 0;
+    }
+};
+struct SymBytes {
+    uint8_t* b;     // byte of word base + k at b[k], k < count
+    uint32_t base, count;
+    ErrorWord* err;
+    // the cross check keeps every access inside the run; one outside is refused
+    PTL_HD bool in(uint32_t w) const {
+        if (w - base < count) return true;
+        record_error(err, ST_UNSUPPORTED, W_RA1, w);
+        return false;
+    }
+    PTL_HD uint32_t reg(uint32_t w) const { return in(w) ? (b[w - base] & 0x3Fu) : 0u; }
+    PTL_HD bool swapped(uint32_t w) const { return in(w) && (b[w - base] & 0x80u) != 0; }
+    PTL_HD void mark(uint32_t w) const { if (in(w)) b[w - base] = static_cast<uint8_t>(b[w - base] | 0x80u); }
+    PTL_HD void assign(uint32_t w, uint32_t r) const { if (in(w)) b[w - base] = static_cast<uint8_t>(r & 0x3Fu); }
+};
+
+// The fields of word off a step reads.
+struct SWord {
+    uint32_t used, ins, r1, r2, rd, jt;
+};
+PTL_HD SWord s_word(const Prog& P, uint32_t off) {
+    return SWord{P.used_instrs[off], P.instr[off], P.rs1[off], P.rs2[off], P.rd[off], P.jt[off]};
+}
+
+// lifetime_analyze_valid (:959-1145) for function f's word wd under lifetime mask; false
 // for an input the reference leaves undefined (a symbol past the words).
-PTL_HD bool s_ra_compute(const Prog& P, uint32_t f, uint32_t off, uint64_t mask, SRaStep& R) {
-    const uint32_t ins = P.instr[off], r1 = P.rs1[off], r2 = P.rs2[off], rdv = P.rd[off], j = P.jt[off];
+template <class Sym>
+PTL_HD bool s_ra_compute(const Prog& P, const Sym& sy, uint32_t f, const SWord& wd, uint64_t mask, SRaStep& R) {
+    const uint32_t ins = wd.ins, r1 = wd.r1, r2 = wd.r2, rdv = wd.rd, j = wd.jt;
     const uint32_t start = P.fn_start0[f];
     if (ins == 0x000000EFu && (j < start || j - start >= P.fn_size0[f])) {
         // a call out of the function: caller-saved registers are freed, the ones in use
@@ -279,8 +318,8 @@ PTL_HD bool s_ra_compute(const Prog& P, uint32_t f, uint32_t off, uint64_t mask,
             *reg = r;
             *sw = false;
         } else {
-            *reg = P.symreg[r - 64u] & 0xFFu;
-            *sw = P.symswp[r - 64u] != 0;
+            *reg = sy.reg(r - 64u);
+            *sw = sy.swapped(r - 64u);
         }
     };
     uint32_t rs1_reg, rs2_reg;
@@ -317,24 +356,25 @@ PTL_HD bool s_ra_compute(const Prog& P, uint32_t f, uint32_t off, uint64_t mask,
 
 // The swap marks: the symbols the swapped registers held before the step (regs, the
 // function's register state, not yet updated) keep their register and read as swapped.
-PTL_HD void s_ra_swaps(const Prog& P, const SRaStep& R, const int32_t* regs) {
+template <class Sym>
+PTL_HD void s_ra_swaps(const Prog& P, const Sym& sy, const SRaStep& R, const int32_t* regs) {
     unsigned long long m = R.swap;
     while (m) {
         const uint32_t j = ctz64(m);
         m &= m - 1ull;
         const int32_t v = regs[j];
-        if (v >= 64 && u32(v) - 64u < P.W) P.symswp[u32(v) - 64u] = 0xFFFFFFFFu;
+        if (v >= 64 && u32(v) - 64u < P.W) sy.mark(u32(v) - 64u);
     }
 }
 
 // The step's symbols take their registers (after every swap mark of the step).
-PTL_HD void s_ra_uses(const Prog& P, const SRaStep& R) {
+template <class Sym>
+PTL_HD void s_ra_uses(const Prog& P, const Sym& sy, const SRaStep& R) {
     if (R.act != 1) return;
     for (int k = 0; k < 3; ++k) {
         const uint32_t v = R.use_v[k];
         if (v >= 64u && v - 64u < P.W) {
-            P.symreg[v - 64u] = R.use_reg[k];
-            P.symswp[v - 64u] = 0;
+            sy.assign(v - 64u, R.use_reg[k]);
         }
     }
 }
@@ -362,8 +402,10 @@ PTL_HD bool s_ra_function_ok(const Prog& P, uint32_t f) {
 
 // One function on its own (no word of another function named): its steps in order.
 // regs: its 64-entry register state (caller's storage).  preserve[f] receives the OR of
-// its lifetime masks, masked to the callee-saved registers.
-PTL_HD void s_ra_function(const Prog& P, uint32_t f, int32_t* regs, unsigned long long* preserve) {
+// its lifetime masks, masked to the callee-saved registers.  The next step's word is
+// loaded while the current one runs.
+template <class Sym>
+PTL_HD void s_ra_function(const Prog& P, const Sym& sy, uint32_t f, int32_t* regs, unsigned long long* preserve) {
     for (int k = 0; k < 64; ++k) regs[k] = -1;
     uint64_t mask = 0x1Full, pm = 0;
     if (!s_ra_function_ok(P, f)) {
@@ -371,22 +413,62 @@ PTL_HD void s_ra_function(const Prog& P, uint32_t f, int32_t* regs, unsigned lon
         return;
     }
     const uint32_t start = P.fn_start0[f], size = P.fn_size0[f];
+    SWord cur = size > 0 ? s_word(P, start) : SWord{};
     for (uint32_t i = 0; i < size; ++i) {
         const uint32_t off = start + i;
-        if (P.used_instrs[off]) {
+        const SWord next = i + 1 < size ? s_word(P, off + 1) : SWord{};
+        if (cur.used) {
             SRaStep R;
-            if (!s_ra_compute(P, f, off, mask, R)) {
+            if (!s_ra_compute(P, sy, f, cur, mask, R)) {
                 record_error(P.err, ST_UNSUPPORTED, W_RA1, off);
                 return;
             }
-            s_ra_swaps(P, R, regs);
-            s_ra_uses(P, R);
+            s_ra_swaps(P, sy, R, regs);
+            s_ra_uses(P, sy, R);
             s_ra_regs(R, regs);
             mask = R.mask;
         }
         pm |= mask;
+        cur = next;
     }
     preserve[f] = pm & kNonscratchRegisters;
+}
+
+// Functions on their own in tiles of the word space: tile b takes the functions whose
+// first word lies in [b * T, (b + 1) * T); their words run from the first one's start to
+// the last one's end, at most T + S bytes (S: the longest function).  Threads of the
+// tile run its functions with their symbols in sym (zeroed by the caller), then copy
+// the bytes back to the program's arrays.  first/last: the tile's function range.
+PTL_HD void s_ra_tile_functions(const Prog& P, uint32_t b, uint32_t T, uint32_t* first, uint32_t* last) {
+    auto lower = [&](uint64_t w) {  // first function starting at or after word w
+        uint32_t lo = 0, hi = P.F;
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi) / 2;
+            if (P.fn_start0[mid] < w) lo = mid + 1; else hi = mid;
+        }
+        return lo;
+    };
+    *first = lower(static_cast<uint64_t>(b) * T);
+    *last = lower(static_cast<uint64_t>(b + 1) * T);
+}
+
+// The tile's words [base, base + count) (clipped to the program).
+PTL_HD uint32_t s_ra_tile_span(const Prog& P, uint32_t first, uint32_t last, uint32_t* base) {
+    if (first >= last) {
+        *base = 0;
+        return 0;
+    }
+    *base = P.fn_start0[first];
+    uint64_t end = static_cast<uint64_t>(P.fn_start0[last - 1]) + P.fn_size0[last - 1];
+    if (end > P.W) end = P.W;
+    return end > *base ? static_cast<uint32_t>(end - *base) : 0u;
+}
+
+PTL_HD void s_ra_tile_writeback(const Prog& P, const uint8_t* sym, uint32_t base, uint32_t count, uint32_t k) {
+    if (k >= count || base + k >= P.W) return;
+    const uint8_t v = sym[k];
+    P.symreg[base + k] = v & 0x3Fu;
+    P.symswp[base + k] = (v & 0x80u) ? 0xFFFFFFFFu : 0u;
 }
 
 // All functions in the reference's order (:1167-1269): per step, every function computes
@@ -411,17 +493,17 @@ PTL_HD void s_ra_serial(const Prog& P, int32_t* regs, SRaStep* steps, unsigned l
             steps[f].act = 0;
             const uint32_t off = P.fn_start0[f] + i;
             if (i < P.fn_size0[f] && P.used_instrs[off]) {
-                if (!s_ra_compute(P, f, off, P.lifetime[f], steps[f])) {
+                if (!s_ra_compute(P, SymGlobal{P}, f, s_word(P, off), P.lifetime[f], steps[f])) {
                     record_error(P.err, ST_UNSUPPORTED, W_RA1, off);
                     return;
                 }
             }
         }
         for (uint32_t f = 0; f < F; ++f)
-            if (steps[f].act) s_ra_swaps(P, steps[f], regs + f * 64u);
+            if (steps[f].act) s_ra_swaps(P, SymGlobal{P}, steps[f], regs + f * 64u);
         for (uint32_t f = 0; f < F; ++f) {
             if (steps[f].act) {
-                s_ra_uses(P, steps[f]);
+                s_ra_uses(P, SymGlobal{P}, steps[f]);
                 s_ra_regs(steps[f], regs + f * 64u);
                 P.lifetime[f] = steps[f].mask;
             }
