@@ -13,7 +13,12 @@
  * that the inherited print(), to_asm() and to_binary() work unchanged.  With profile
  * set it prints the stage CSV of the reference's -p flag (rv_generator.cpp:150-162:
  * the seven stage names, then their times in ns, on stdout), from device times.
- * Errors are thrown as std::runtime_error, as the reference does for its own. */
+ * Errors are thrown as std::runtime_error, as the reference does for its own.
+ *
+ * With scalar set it replaces the reference's scalar generator rv_generator_st instead
+ * (include/codegen/rv_generator.hpp:82-100, picked by -s at src/main.cpp:123-124):
+ *
+ *     gen = std::make_unique<rv_generator_gb300>(depth_tree, 0, simple); */
 #pragma once
 
 #include <algorithm>
@@ -45,16 +50,18 @@ class rv_generator_gb300 : public rv_generator {
     }
 
   public:
-    /* device: the CUDA device to compile on.  The tree is read here (DepthTree getters,
+    /* device: the CUDA device to compile on; scalar: the scalar generator's semantics.
+     * The tree is read here (DepthTree getters,
      * subprojects/pareas-ast/include/codegen/depthtree.hpp:32-58) and copied to the
      * device; the base class keeps its own host copy as the reference's constructor does. */
-    explicit rv_generator_gb300(const DepthTree& tree, int device = 0) : rv_generator(tree) {
+    explicit rv_generator_gb300(const DepthTree& tree, int device = 0, bool scalar = false) : rv_generator(tree) {
         const ptl_ast_view v{tree.filledNodes(),          tree.maxDepth(),
                              tree.getNodeTypes().data(),  tree.getResultingTypes().data(),
                              tree.getParents().data(),    tree.getDepth().data(),
                              tree.getChildren().data(),   tree.getNodeData().data(),
                              /*on_device=*/0};
-        check(ptl_generator_create(&v, device, &gen_), nullptr, "ptl_generator_create");
+        if (scalar) check(ptl_generator_create_scalar(&v, device, &gen_), nullptr, "ptl_generator_create_scalar");
+        else check(ptl_generator_create(&v, device, &gen_), nullptr, "ptl_generator_create");
     }
 
     ~rv_generator_gb300() override { ptl_generator_destroy(gen_); }

@@ -4,13 +4,14 @@
 // front end, flatten it (DepthTree), construct rv_generator_gb300, process, and write
 // the assembly listing (inherited to_asm) and the raw words (inherited to_binary).
 //
-//   binding_check <input.in> <out.S> <out.bin>
+//   binding_check [-s] <input.in> <out.S> <out.bin>     (-s: the scalar generator)
 //
 // Exit status: 0 on success; 3 with the exception text on stderr when the GPU generator
 // throws (for instance on a host without a GPU); 2 when the front end fails.
 #include <fstream>
 #include <iostream>
 #include <memory>
+#include <string>
 
 #include "codegen/astnode.hpp"
 #include "codegen/depthtree.hpp"
@@ -21,8 +22,10 @@
 #include "rv_generator_gb300.hpp"
 
 int main(int argc, char** argv) {
+    const bool scalar = argc == 5 && std::string(argv[1]) == "-s";
+    if (scalar) ++argv, --argc;
     if (argc != 4) {
-        std::cerr << "usage: binding_check <input.in> <out.S> <out.bin>\n";
+        std::cerr << "usage: binding_check [-s] <input.in> <out.S> <out.bin>\n";
         return 1;
     }
     std::unique_ptr<ASTNode> node;
@@ -40,7 +43,7 @@ int main(int argc, char** argv) {
         return 2;
     }
     try {
-        std::unique_ptr<rv_generator> gen = std::make_unique<rv_generator_gb300>(*tree);
+        std::unique_ptr<rv_generator> gen = std::make_unique<rv_generator_gb300>(*tree, 0, scalar);
         gen->process(true);
         std::ofstream asm_out(argv[2]);
         gen->to_asm(asm_out);

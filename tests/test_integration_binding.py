@@ -43,3 +43,12 @@ def test_reference_binding_builds_and_runs(built_cuda, tmp_path):
     else:
         assert run.returncode == 3, run.stdout + run.stderr
         assert "ptl_generator_create: status 6" in run.stderr  # PTL_CUDA_ERROR: no device
+    # the scalar generator through the same binding (the reference's -s)
+    run = subprocess.run([exe, "-s", src, str(out_s), str(out_b)], capture_output=True, text=True, timeout=300)
+    if gpu:
+        assert run.returncode == 0, run.stderr
+        ref = refbind.compile_ast_scalar(refbind.parse_file(src))
+        np.testing.assert_array_equal(np.fromfile(out_b, dtype="<u4"), ref.bufs["out_words"])
+    else:
+        assert run.returncode == 3, run.stdout + run.stderr
+        assert "ptl_generator_create_scalar: status 6" in run.stderr
