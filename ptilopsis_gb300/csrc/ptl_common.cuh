@@ -59,10 +59,29 @@ struct CodeTables {
     uint8_t jt[kTypeRows][4];        // instr_jt_table
     uint8_t opd[kTypeRows][4][6][2]; // operand_table
     uint32_t instr[kTypeRows][4][6]; // instr_table
+    // isn_gen's reads per (row, data type), the four slots side by side so that a node
+    // loads them in one 16-byte read: gdesc packs the slot's fields (gd_* below), gword
+    // its instruction word
+    alignas(16) uint32_t gdesc[kTypeRows][6][4];
+    alignas(16) uint32_t gword[kTypeRows][6][4];
 };
+
+// gdesc fields: has_instr (bit 0), parent_arg_idx calc (1-2), output calc (3-5),
+// has_output (6), instr_constant calc (7-9), instr_jt calc (10-12), the two operand calcs
+// (13-15, 16-18), node_size_mapping (19-22).
+PTL_HD bool gd_has(uint32_t d) { return (d & 1u) != 0; }
+PTL_HD uint32_t gd_pai(uint32_t d) { return (d >> 1) & 3u; }
+PTL_HD uint32_t gd_out(uint32_t d) { return (d >> 3) & 7u; }
+PTL_HD bool gd_has_output(uint32_t d) { return ((d >> 6) & 1u) != 0; }
+PTL_HD uint32_t gd_cnst(uint32_t d) { return (d >> 7) & 7u; }
+PTL_HD uint32_t gd_jt(uint32_t d) { return (d >> 10) & 7u; }
+PTL_HD uint32_t gd_opd(uint32_t d, uint32_t k) { return (d >> (13u + 3u * k)) & 7u; }
+PTL_HD uint32_t gd_size(uint32_t d) { return (d >> 19) & 15u; }
 
 // Builds the tables (ptl_tables.cpp).
 void build_code_tables(CodeTables* t);
+// Whether the packed isn_gen fields decode to the tables (every value fit its field).
+bool gen_desc_ok(const CodeTables* t);
 
 PTL_HD int32_t s32(uint32_t v) { return static_cast<int32_t>(v); }
 PTL_HD uint32_t u32(int32_t v) { return static_cast<uint32_t>(v); }

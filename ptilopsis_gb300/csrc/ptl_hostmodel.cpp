@@ -434,6 +434,13 @@ int ptlhm_compile(const uint8_t* type, const uint8_t* rtype, const int32_t* pare
 }
 
 int ptlhm_last_cross(void) { return g_last_cross ? 1 : 0; }
+
+// Whether isn_gen's packed table fields decode to the code tables.
+int ptlhm_gen_desc_ok(void) {
+    static CodeTables t;
+    build_code_tables(&t);
+    return gen_desc_ok(&t) ? 1 : 0;
+}
 void ptlhm_set_scalar_serial(int on) { g_force_serial = on != 0; }
 
 void ptlhm_set_cache_entries(uint32_t k) { g_cache_k = k; }

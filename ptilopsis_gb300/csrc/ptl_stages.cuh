@@ -103,6 +103,21 @@ struct Tab {
         return tab_ld(&t->opd[row(type)][s][rt][k]);
     }
     PTL_HD uint32_t word(uint32_t type, uint32_t s, uint32_t rt) const { return tab_ld(&t->instr[row(type)][s][rt]); }
+    // the four slots' packed fields / words of (type, rt) in one 16-byte read
+    struct Slots4 {
+        uint32_t v[4];
+    };
+    PTL_HD Slots4 slots4(const uint32_t (*tab)[6][4], uint32_t type, uint32_t rt) const {
+        const uint32_t* p = &tab[row(type)][rt][0];
+#if defined(__CUDA_ARCH__)
+        const uint4 q = __ldg(reinterpret_cast<const uint4*>(p));
+        return Slots4{{q.x, q.y, q.z, q.w}};
+#else
+        return Slots4{{p[0], p[1], p[2], p[3]}};
+#endif
+    }
+    PTL_HD Slots4 gdesc(uint32_t type, uint32_t rt) const { return slots4(t->gdesc, type, rt); }
+    PTL_HD Slots4 gword(uint32_t type, uint32_t rt) const { return slots4(t->gword, type, rt); }
 };
 
 // ------------------------------------------------------------------ program view
@@ -449,11 +464,11 @@ PTL_HD GenNode gen_node(const Prog& P, uint32_t x) {
     return N;
 }
 
-PTL_HD GenLane gen_lane(const Prog& P, const GenNode& N, uint32_t s) {
+// d: the slot's packed table fields (Tab::gdesc).
+PTL_HD GenLane gen_lane(const GenNode& N, uint32_t s, uint32_t d) {
     GenLane L;
-    const uint32_t t = N.t;
     const uint32_t rt = N.rt;
-    L.has = P.tab.has_instr(t, s, rt);
+    L.has = gd_has(d);
     L.prop = L.has || s == 0;
     L.par = L.prop ? N.par : 0u;
     L.nopar = s32(L.par) == -1;
@@ -463,7 +478,7 @@ PTL_HD GenLane gen_lane(const Prog& P, const GenNode& N, uint32_t s) {
     L.nonc = ((L.pt & RV_IF) == RV_IF) && !(L.ci == (L.pt & 1u));
     L.call = L.nonc;
     if ((L.nopar || !L.nonc) && L.prop) {
-        const uint32_t calc = P.tab.pai(t, s, rt);
+        const uint32_t calc = gd_pai(d);
         if (calc == 1) L.call = true;
         if (calc == 2 && s32(rt) > 1) L.call = true;
     }
@@ -471,18 +486,18 @@ PTL_HD GenLane gen_lane(const Prog& P, const GenNode& N, uint32_t s) {
     L.iib = s + (L.prop ? N.loc : 0u);
     uint32_t r = 0;
     if (L.has) {
-        const uint32_t calc = P.tab.out(t, s, rt);
+        const uint32_t calc = gd_out(d);
         if (calc == 3) r |= 32u;
         if (calc == 4) r |= 10u;
         if (calc == 1) r |= N.nd + 10u;
         if (calc == 2) r |= N.nd + 42u;
         bool hov = L.call;
-        if (calc == 0 && P.tab.has_output(t, s, rt)) hov = true;
+        if (calc == 0 && gd_has_output(d)) hov = true;
         if (hov) r |= L.iib + 64u;
     }
     L.rdv = r;
     const bool use_rd = L.nopar || (!L.nonc && L.lfp);
-    const uint32_t instr_no = L.iib + (L.nonc ? P.tab.size(t, rt) : 0u);
+    const uint32_t instr_no = L.iib + (L.nonc ? gd_size(d) : 0u);
     L.dpv = (use_rd ? r : 0u) | (L.nonc ? instr_no : 0u);
     return L;
 }
@@ -493,10 +508,11 @@ PTL_HD GenLane gen_lane(const Prog& P, const GenNode& N, uint32_t s) {
 // wins, as in the reference.
 PTL_HD void st_gen_prop(const Prog& P, uint32_t x) {
     const GenNode N = gen_node(P, x);
+    const Tab::Slots4 D = P.tab.gdesc(N.t, N.rt);
     int32_t target = -1;
     uint32_t value = 0;
     for (uint32_t s = 0; s < 4; ++s) {
-        const GenLane L = gen_lane(P, N, s);
+        const GenLane L = gen_lane(N, s, D.v[s]);
         if (L.pai >= 0) {
             target = L.pai;
             value = L.dpv;
@@ -541,13 +557,15 @@ PTL_HD unsigned long long gen_key(const Prog& P, uint32_t x) {
 }
 
 PTL_HD void st_gen_claim(const Prog& P, uint32_t x) {
+    const Tab::Slots4 D = P.tab.gdesc(P.nt[x], P.rt[x]);
+    if (!((D.v[0] | D.v[1] | D.v[2] | D.v[3]) & 1u)) return;  // no slot has an instruction
     const GenNode N = gen_node(P, x);
     const unsigned long long key = gen_key(P, x);
     const bool loop2 = N.t == RV_IF_ELSE || N.t == RV_WHILE;  // slot 1 goes where a register says
     const uint32_t r1 = loop2 ? P.regs[x * 3u + 1u] : 0u, r2 = loop2 ? P.regs[x * 3u + 2u] : 0u;
     for (uint32_t s = 0; s < 4; ++s) {
-        if (!P.tab.has_instr(N.t, s, N.rt)) continue;  // most slots: no instruction
-        const GenLane L = gen_lane(P, N, s);
+        if (!gd_has(D.v[s])) continue;  // most slots: no instruction
+        const GenLane L = gen_lane(N, s, D.v[s]);
         const uint32_t loc = gen_loc(P, N, s, L, r1, r2);
         if (loc >= P.W) {
             record_error(P.err, ST_UNSUPPORTED, W_GEN, x);
@@ -558,20 +576,24 @@ PTL_HD void st_gen_claim(const Prog& P, uint32_t x) {
 }
 
 PTL_HD void st_gen_write(const Prog& P, uint32_t x) {
+    const Tab::Slots4 D = P.tab.gdesc(P.nt[x], P.rt[x]);
+    if (!((D.v[0] | D.v[1] | D.v[2] | D.v[3]) & 1u)) return;  // no slot has an instruction
     const GenNode N = gen_node(P, x);
     const uint32_t t = N.t;
     const uint32_t rt = N.rt;
     const unsigned long long key = gen_key(P, x);
     const uint32_t reg[3] = {P.regs[x * 3u], P.regs[x * 3u + 1u], P.regs[x * 3u + 2u]};
     const uint32_t nd = N.nd;
+    const Tab::Slots4 Wd = P.tab.gword(t, rt);
     for (uint32_t s = 0; s < 4; ++s) {
-        if (!P.tab.has_instr(t, s, rt)) continue;  // most slots: no instruction
-        const GenLane L = gen_lane(P, N, s);
+        const uint32_t d = D.v[s];
+        if (!gd_has(d)) continue;  // most slots: no instruction
+        const GenLane L = gen_lane(N, s, d);
         const uint32_t loc = gen_loc(P, N, s, L, reg[1], reg[2]);
         if (loc >= P.W || P.owner[loc] != (key | s)) continue;
         // instruction word and constants, :752-779
-        uint32_t w = P.tab.word(t, s, rt);
-        const uint32_t cc = P.tab.cnst(t, s);
+        uint32_t w = Wd.v[s];
+        const uint32_t cc = gd_cnst(d);
         if (cc == 1) w |= nd & 0xFFFFF000u;
         if (cc == 2) w |= (nd & 0xFFFu) << 20;
         const uint32_t m4 = nd * 4u;
@@ -579,7 +601,7 @@ PTL_HD void st_gen_write(const Prog& P, uint32_t x) {
         if (cc == 4) w |= m4 << 20;
         if (cc == 5) w |= (0u - m4) << 20;
         // jump target, :781-814
-        const uint32_t jc = P.tab.jt(t, s);
+        const uint32_t jc = gd_jt(d);
         uint32_t jv = 0;
         if (s32(jc) > 0 && !(s32(jc) > 5)) {
             uint32_t v = s32(jc) > 2 ? reg[2] : reg[1];
@@ -595,7 +617,7 @@ PTL_HD void st_gen_write(const Prog& P, uint32_t x) {
         // operands, :816-850
         uint32_t ops[2];
         for (uint32_t k = 0; k < 2; ++k) {
-            const uint32_t c = P.tab.opd(t, s, rt, k);
+            const uint32_t c = gd_opd(d, k);
             uint32_t a = 0;
             if (c == 1 || c == 4 || c == 5 || c == 6) {
                 uint32_t ri = 0;

@@ -188,6 +188,45 @@ void build_code_tables(CodeTables* t) {
         RV_DECL, RV_ID, RV_WHILE_DUMMY, RV_FUNC_DECL_DUMMY, RV_RETURN,
     };
     for (uint32_t k = 0; k < kNumPareasTypes; ++k) t->pareas_to_rv[k] = static_cast<uint8_t>(pareas[k]);
+
+    // isn_gen's packed per-slot fields; a value that does not fit its field is stored as
+    // all ones there (gen_desc_ok reports it)
+    auto fit = [](uint32_t v, uint32_t bits) { return v < (1u << bits) ? v : (1u << bits) - 1u; };
+    for (uint32_t r = 0; r < kTypeRows; ++r) {
+        for (uint32_t d = 0; d < 6; ++d) {
+            for (uint32_t s = 0; s < 4; ++s) {
+                uint32_t v = (t->has_instr[r][s] >> d) & 1u;
+                v |= fit(t->pai[r][s][d], 2) << 1;
+                v |= fit(t->out[r][s][d], 3) << 3;
+                v |= ((t->has_output[r][s] >> d) & 1u) << 6;
+                v |= fit(t->cnst[r][s], 3) << 7;
+                v |= fit(t->jt[r][s], 3) << 10;
+                v |= fit(t->opd[r][s][d][0], 3) << 13;
+                v |= fit(t->opd[r][s][d][1], 3) << 16;
+                v |= fit(t->size[r][d], 4) << 19;
+                t->gdesc[r][d][s] = v;
+                t->gword[r][d][s] = t->instr[r][s][d];
+            }
+        }
+    }
+}
+
+bool gen_desc_ok(const CodeTables* t) {
+    for (uint32_t r = 0; r < kTypeRows; ++r) {
+        for (uint32_t d = 0; d < 6; ++d) {
+            for (uint32_t s = 0; s < 4; ++s) {
+                const uint32_t v = t->gdesc[r][d][s];
+                const bool ok = gd_has(v) == (((t->has_instr[r][s] >> d) & 1u) != 0) && gd_pai(v) == t->pai[r][s][d] &&
+                                gd_out(v) == t->out[r][s][d] &&
+                                gd_has_output(v) == (((t->has_output[r][s] >> d) & 1u) != 0) &&
+                                gd_cnst(v) == t->cnst[r][s] && gd_jt(v) == t->jt[r][s] &&
+                                gd_opd(v, 0) == t->opd[r][s][d][0] && gd_opd(v, 1) == t->opd[r][s][d][1] &&
+                                gd_size(v) == t->size[r][d] && t->gword[r][d][s] == t->instr[r][s][d];
+                if (!ok) return false;
+            }
+        }
+    }
+    return true;
 }
 
 }  // namespace ptl

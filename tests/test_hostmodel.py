@@ -152,3 +152,9 @@ def test_hostmodel_row0_lookup_modes(built, hashed):
             assert_stages_equal(ast)
     finally:
         L.ptlhm_set_hashed(ctypes.c_int(0))
+
+
+def test_packed_gen_tables_decode_to_the_code_tables(built):
+    """isn_gen reads each node type's four slots from one packed 16-byte record; every
+    field must fit and decode to the table it was packed from."""
+    assert hostmodel().ptlhm_gen_desc_ok() == 1
