@@ -15,6 +15,7 @@
 #include <algorithm>
 #include <atomic>
 #include <chrono>
+#include <map>
 #include <cstdlib>
 #include <cstring>
 #include <mutex>
@@ -979,6 +980,50 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
     return PTL_OK;
 }
 
+// Whether kernels should read the callers' pageable arrays directly rather than take
+// them from pinned memory through the copy engine.  The link that direct reads use
+// differs between hosts (on some the device reads host memory at a few GB/s while the
+// copy engine still moves tens of GB/s), so it is measured once per device: 32 MB read
+// each way; direct unless the copy engine is more than twice as fast, which pays for the
+// host threads' gather into pinned memory.
+bool direct_host_pays(int device, cudaStream_t s) {
+    static std::mutex mu;
+    static std::map<int, bool> known;
+    std::lock_guard<std::mutex> lk(mu);
+    const auto it = known.find(device);
+    if (it != known.end()) return it->second;
+    constexpr size_t kBytes = size_t(32) << 20;
+    bool direct = true;  // if the probe cannot run: the reads it would have compared
+    void* host = std::malloc(kBytes);
+    void* pinned = nullptr;
+    void* dev = nullptr;
+    cudaEvent_t ev[4] = {};
+    bool ok = host && cudaHostAlloc(&pinned, kBytes, cudaHostAllocDefault) == cudaSuccess &&
+              cudaMalloc(&dev, kBytes) == cudaSuccess;
+    for (auto& e : ev) ok = ok && cudaEventCreate(&e) == cudaSuccess;
+    if (ok) {
+        std::memset(host, 1, kBytes);
+        std::memset(pinned, 1, kBytes);
+        for (int rep = 0; rep < 2 && ok; ++rep) {  // the first round warms both paths
+            ok = cudaEventRecord(ev[0], s) == cudaSuccess && read_host(host, dev, kBytes, s) == cudaSuccess &&
+                 cudaEventRecord(ev[1], s) == cudaSuccess &&
+                 cudaMemcpyAsync(dev, pinned, kBytes, cudaMemcpyHostToDevice, s) == cudaSuccess &&
+                 cudaEventRecord(ev[2], s) == cudaSuccess && cudaStreamSynchronize(s) == cudaSuccess;
+        }
+        float t_direct = 0, t_copy = 0;
+        if (ok && cudaEventElapsedTime(&t_direct, ev[0], ev[1]) == cudaSuccess &&
+            cudaEventElapsedTime(&t_copy, ev[1], ev[2]) == cudaSuccess && t_copy > 0)
+            direct = t_direct <= 2.0f * t_copy;
+    }
+    for (auto& e : ev) if (e) cudaEventDestroy(e);
+    if (dev) cudaFree(dev);
+    if (pinned) cudaFreeHost(pinned);
+    std::free(host);
+    cudaGetLastError();  // a failed probe leaves no error behind
+    known[device] = direct;
+    return direct;
+}
+
 }  // namespace
 
 BatchPipeline* BatchPipeline::create(int device, int host_threads, ptl_status* st, bool urgent) {
@@ -1000,7 +1045,7 @@ BatchPipeline* BatchPipeline::create(int device, int host_threads, ptl_status* s
     int pageable = 0;
     if (cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, device) != cudaSuccess) pageable = 0;
     const char* env = std::getenv("PTL_HOST_GATHER");  // "1": gather through pinned memory regardless
-    p->direct_host = pageable == 1 && !(env && env[0] == '1');
+    p->direct_host = pageable == 1 && !(env && env[0] == '1') && direct_host_pays(device, p->s);
     if (st) *st = PTL_OK;
     return p;
 }

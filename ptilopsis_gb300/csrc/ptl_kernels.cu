@@ -2432,6 +2432,20 @@ void batch_sort_keys(const BatchLaunch& bl, uint32_t total, unsigned long long* 
     else batch_launch(bl, total, BSortInit{a, aoff});
 }
 
+// Plain 16-byte copy from host memory the device reads directly (the probe of the host
+// input path, below).
+__global__ void __launch_bounds__(kThreads) k_read_host(const uint4* src, uint4* dst, uint64_t n) {
+    for (uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
+         i += static_cast<uint64_t>(gridDim.x) * blockDim.x)
+        dst[i] = src[i];
+}
+
+cudaError_t read_host(const void* src, void* dst, size_t bytes, cudaStream_t s) {
+    g_launches++;
+    k_read_host<<<152u * 2u, kThreads, 0, s>>>(static_cast<const uint4*>(src), static_cast<uint4*>(dst), bytes / 16u);
+    return cudaGetLastError();
+}
+
 void batch_gather_host(const BatchLaunch& bl, uint32_t total, const HostGather& g) {
     if (total == 0) return;
     g_launches++;
