@@ -143,7 +143,7 @@ struct Prog {
     int32_t* par;
     int32_t* ci;
     int32_t* dep;
-    uint8_t* fflag;   // pass 3: becomes FLOAT
+    uint8_t* fflag;   // pass 3: becomes FLOAT; from isn_gen on, each node's parent type
     uint32_t* sizes;  // node code sizes, kept for stage snapshots (null in a batch)
     uint32_t* loc0;   // scan result
     uint32_t* loc;    // after fix
@@ -451,13 +451,16 @@ struct GenNode {
     uint32_t x, t, rt, par, ntp, ci, loc, nd;
 };
 
-PTL_HD GenNode gen_node(const Prog& P, uint32_t x) {
+// stored_ntp: the parent's type from the byte the propagation pass keeps per node (the
+// AVX passes after it), instead of a read at the parent's index.
+PTL_HD GenNode gen_node(const Prog& P, uint32_t x, bool stored_ntp = false) {
     GenNode N;
     N.x = x;
     N.t = P.nt[x];
     N.rt = P.rt[x];
     N.par = u32(P.par[x]);
-    N.ntp = s32(N.par) == -1 ? 0u : P.nt[s32(N.par)];  // the parent's type
+    if (stored_ntp) N.ntp = P.fflag[x];
+    else N.ntp = s32(N.par) == -1 ? 0u : P.nt[s32(N.par)];  // the parent's type
     N.ci = u32(P.ci[x]);
     N.loc = P.loc[x];
     N.nd = P.nd[x];
@@ -508,6 +511,7 @@ PTL_HD GenLane gen_lane(const GenNode& N, uint32_t s, uint32_t d) {
 // wins, as in the reference.
 PTL_HD void st_gen_prop(const Prog& P, uint32_t x) {
     const GenNode N = gen_node(P, x);
+    P.fflag[x] = static_cast<uint8_t>(N.ntp);  // rv node types fit a byte
     const Tab::Slots4 D = P.tab.gdesc(N.t, N.rt);
     int32_t target = -1;
     uint32_t value = 0;
@@ -559,7 +563,7 @@ PTL_HD unsigned long long gen_key(const Prog& P, uint32_t x) {
 PTL_HD void st_gen_claim(const Prog& P, uint32_t x) {
     const Tab::Slots4 D = P.tab.gdesc(P.nt[x], P.rt[x]);
     if (!((D.v[0] | D.v[1] | D.v[2] | D.v[3]) & 1u)) return;  // no slot has an instruction
-    const GenNode N = gen_node(P, x);
+    const GenNode N = gen_node(P, x, true);
     const unsigned long long key = gen_key(P, x);
     const bool loop2 = N.t == RV_IF_ELSE || N.t == RV_WHILE;  // slot 1 goes where a register says
     const uint32_t r1 = loop2 ? P.regs[x * 3u + 1u] : 0u, r2 = loop2 ? P.regs[x * 3u + 2u] : 0u;
@@ -578,7 +582,7 @@ PTL_HD void st_gen_claim(const Prog& P, uint32_t x) {
 PTL_HD void st_gen_write(const Prog& P, uint32_t x) {
     const Tab::Slots4 D = P.tab.gdesc(P.nt[x], P.rt[x]);
     if (!((D.v[0] | D.v[1] | D.v[2] | D.v[3]) & 1u)) return;  // no slot has an instruction
-    const GenNode N = gen_node(P, x);
+    const GenNode N = gen_node(P, x, true);
     const uint32_t t = N.t;
     const uint32_t rt = N.rt;
     const unsigned long long key = gen_key(P, x);
