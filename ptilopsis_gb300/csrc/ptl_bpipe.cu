@@ -116,6 +116,8 @@ const CodeTables& tables() {
         if (e_ != cudaSuccess) return cuda_fail(e_, #x);             \
     } while (0)
 
+void direct_host_slow(int device);  // later pipelines on the device gather through pinned memory
+
 class Pipeline final : public BatchPipeline {
 public:
     int device = 0;
@@ -142,6 +144,7 @@ public:
     PBuf h_in, h_out, h_fn, h_small, h_gp;
     DBuf d_gp;                 // host-gather parameters (source pointers, offsets, counts)
     bool direct_host = false;  // the device reads pageable host memory coherently
+    uint64_t last_in_bytes = 0;  // input bytes of the last compile
 
     std::vector<uint8_t> active;
     std::vector<ptl_status> status;
@@ -489,6 +492,7 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
             BP_CU(ce);
         }
         h2d += 18 * nodes_in;
+        last_in_bytes = 18 * nodes_in;
         BP_CU(cudaEventRecord(ev[0], s));  // stage times start with the inputs on the device
 
         // node, register and depth families
@@ -974,6 +978,14 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
         }
         ns[6] = 0;  // postprocess is fused into fix_jumps
         if (cudaEventElapsedTime(&ms, ev_in, ev[0]) == cudaSuccess) hns[1] = static_cast<uint64_t>(ms * 1e6);
+        // Direct reads of a large input slower than 40 GB/s (where the host's page
+        // translation, not the link, bounds them): this pipeline and later ones on the
+        // device take the inputs through pinned memory from now on.
+        if (direct_host && last_in_bytes >= (uint64_t(256) << 20) && hns[1] > 0 &&
+            static_cast<double>(last_in_bytes) < 40.0 * static_cast<double>(hns[1])) {
+            direct_host = false;
+            direct_host_slow(device);
+        }
         sort_ns = cudaEventElapsedTime(&ms, ev_sort0, ev_sort1) == cudaSuccess ? static_cast<uint64_t>(ms * 1e6) : 0;
         if (cudaEventElapsedTime(&ms, ev_out0, ev_out1) == cudaSuccess) hns[2] = static_cast<uint64_t>(ms * 1e6);
     }
@@ -986,10 +998,25 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
 // copy engine still moves tens of GB/s), so it is measured once per device: 32 MB read
 // each way; direct unless the copy engine is more than twice as fast, which pays for the
 // host threads' gather into pinned memory.
+struct DirectHostChoice {
+    std::mutex mu;
+    std::map<int, bool> known;
+};
+DirectHostChoice& direct_host_choice() {
+    static DirectHostChoice c;
+    return c;
+}
+
+void direct_host_slow(int device) {
+    DirectHostChoice& c = direct_host_choice();
+    std::lock_guard<std::mutex> lk(c.mu);
+    c.known[device] = false;
+}
+
 bool direct_host_pays(int device, cudaStream_t s) {
-    static std::mutex mu;
-    static std::map<int, bool> known;
-    std::lock_guard<std::mutex> lk(mu);
+    DirectHostChoice& c = direct_host_choice();
+    std::lock_guard<std::mutex> lk(c.mu);
+    std::map<int, bool>& known = c.known;
     const auto it = known.find(device);
     if (it != known.end()) return it->second;
     constexpr size_t kBytes = size_t(32) << 20;
