@@ -127,3 +127,10 @@ def load_scalar_case(entry: dict):
     if key not in z.files:
         return ast, None
     return ast, {k: z[f"{entry['name']}.{k}"] for k in ("out_words", "fn_start", "fn_end", "fn_size", "fn_id")}
+
+
+def manifest_scalar_large() -> dict:
+    """The scalar generator's stage CRCs on the larger Pareas inputs it finished
+    (make_golden.py --scalar-large); their trees are those of manifest_large.json."""
+    with open(os.path.join(GOLDEN, "manifest_scalar_large.json")) as f:
+        return json.load(f)

@@ -138,3 +138,17 @@ def test_gpu_scalar_against_oracle_at_scale(built_cuda, case):
         np.testing.assert_array_equal(t["sizes"], ref.bufs["fn_size"])
         for k in ("gen_instr", "gen_rd", "ra_instr", "ra_rs1"):
             np.testing.assert_array_equal(gen.snapshot(k), ref.bufs[k], err_msg=k)
+
+
+@pytest.mark.parametrize("fx", [e["name"] for e in __import__("conftest").manifest_scalar_large()["fixtures"]])
+def test_gpu_scalar_matches_reference_on_large_inputs(built_cuda, fx):
+    from conftest import load_large, manifest_scalar_large
+    from ptilopsis_gb300 import RvGenerator
+    entry = next(e for e in manifest_scalar_large()["fixtures"] if e["name"] == fx)
+    ast, _ = load_large(fx)
+    with RvGenerator(ast_to_tree(ast), scalar=True) as gen:
+        gen.process()
+        words = gen.get_instructions()
+        for k in ("gen_instr", "gen_rs1", "ra_instr", "ra_rd", "ra_rs1", "ra_rs2", "fn_start", "fn_size"):
+            assert _crc(k, gen.snapshot(k)) == entry["snapshots"][k], f"{fx}: {k}"
+    assert [len(words), crc32(words)] == entry["snapshots"]["out_words"]

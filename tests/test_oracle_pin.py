@@ -149,3 +149,20 @@ def test_port_scalar_matches_reference_on_synthetic(built, seed):
         if name == "opt_used":
             a, b = (a != 0), (b != 0)
         np.testing.assert_array_equal(a, b, err_msg=name)
+
+
+@pytest.mark.parametrize("fx", [e["name"] for e in __import__("conftest").manifest_scalar_large()["fixtures"]])
+def test_port_scalar_matches_reference_on_large_inputs(built, fx):
+    """The scalar restatement on the reference's larger Pareas inputs: every stage array
+    against the CRCs of the reference's scalar run (minutes per input there)."""
+    from conftest import load_large, manifest_scalar_large
+    from oracle import portbind
+    entry = next(e for e in manifest_scalar_large()["fixtures"] if e["name"] == fx)
+    ast, _ = load_large(fx)
+    res = portbind.compile_ast(ast, snapshots=True, scalar=True)
+    assert len(res.words) == entry["words"]
+    for k, (length, c) in entry["snapshots"].items():
+        a = res.bufs[k]
+        if k == "opt_used":
+            a = (a != 0).astype(np.uint32)
+        assert len(a) == length and crc(a) == c, k
