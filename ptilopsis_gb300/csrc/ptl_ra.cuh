@@ -117,41 +117,15 @@ PTL_HD void ra_free_function_cached(const Prog& P, const SymCache& c, uint32_t s
         if (s32(S.ord) > 63) sym_write(P, c, slot, S.ord, S.rdr, false);
         if (s32(S.r1) > 63) sym_write(P, c, slot, S.r1, S.r1r, false);
         if (s32(S.r2) > 63) sym_write(P, c, slot, S.r2, S.r2r, false);
-#if defined(__CUDA_ARCH__)
-        // The lanes of a warp at the same step (its functions belong to one program)
-        // combine their trigger records and chunk counts before the atomics: one min/max
-        // pair per position and one count per chunk for the group, not per function.
-        const unsigned grp = __match_any_sync(__activemask(), i);
-        const uint32_t lane = threadIdx.x & 31u;
-        const uint32_t lo = __reduce_or_sync(grp, static_cast<uint32_t>(S.trig));
-        const uint32_t hi = __reduce_or_sync(grp, static_cast<uint32_t>(S.trig >> 32));
-        for (uint64_t all = (static_cast<uint64_t>(hi) << 32) | lo; all; all &= all - 1) {
-            const uint32_t p = ctz64(all);
-            const bool mine = ((S.trig >> p) & 1ull) != 0;
-            const uint32_t gmin = __reduce_min_sync(grp, mine ? g1 : 0xFFFFFFFFu);
-            const uint32_t gmax = __reduce_max_sync(grp, mine ? g1 : 0u);
-            if (lane == static_cast<uint32_t>(__ffs(static_cast<int>(grp)) - 1)) {
-                atomicMin(&P.trig_min[static_cast<size_t>(i) * 64u + p], gmin);
-                atomicMax(&P.trig_max[static_cast<size_t>(i) * 64u + p], gmax);
-            }
-        }
-        if (done) {
-            const bool last = !have || (i + 1u) % kRaChunk == 0;
-            const unsigned finishing = __ballot_sync(grp, last);
-            if (finishing) {
-                // every lane of the group fences: its atomics above carried other lanes'
-                // records, all of which must be visible before the count
-                __threadfence();
-                __syncwarp(grp);
-                if (lane == static_cast<uint32_t>(__ffs(static_cast<int>(finishing)) - 1))
-                    atomicAdd(&done[i / kRaChunk], static_cast<uint32_t>(__popc(finishing)));
-            }
-        }
-#else
         for (uint64_t t = S.trig; t; t &= t - 1) {
             const uint32_t p = ctz64(t);
             at_min_u32(&P.trig_min[static_cast<size_t>(i) * 64u + p], g1);
             at_max_u32(&P.trig_max[static_cast<size_t>(i) * 64u + p], g1);
+        }
+#if defined(__CUDA_ARCH__)
+        if (done && (!have || (i + 1u) % kRaChunk == 0)) {
+            __threadfence();
+            atomicAdd(&done[i / kRaChunk], 1u);
         }
 #endif
     }
