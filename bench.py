@@ -608,17 +608,21 @@ def run_batched(args):
     gen = RvGenerator(sample[0], device=local)
     gen.process()
     plain_dev, plain_words = 0.0, []
+    plain_stage = np.zeros(len(STAGES))
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for t in sample:
         gen.upload(t)
         gen.process(profile=True)
         plain_words.append(gen.get_instructions())
-        plain_dev += sum(gen.stage_ns()) / 1e9
+        ns = np.array(gen.stage_ns(), dtype=np.float64)
+        plain_stage += ns
+        plain_dev += ns.sum() / 1e9
     plain_wall = time.perf_counter() - t0
     gen.close()
     plain = {"value": sn / plain_dev, "e2e_value": sn / plain_wall, "unit": UNIT, "programs": len(sample),
-             "nodes": sn, "sample": f"first {len(sample)} programs of the workload, one generator, one at a time"}
+             "nodes": sn, "sample": f"first {len(sample)} programs of the workload, one generator, one at a time",
+             "stage_ms": {k: round(float(v) / 1e6, 3) for k, v in zip(STAGES, plain_stage)}}
     same_as_plain = all(np.array_equal(bc.words(k), plain_words[k]) for k in range(len(sample)))
     oracle_check, cpu_line = None, None
     if rank == 0 and not args.no_cpu_baseline:
