@@ -105,6 +105,13 @@ ptl_status ptl_generator_function_table(ptl_generator* gen, const uint32_t** sta
  * reported as 0). */
 ptl_status ptl_generator_stage_ns(ptl_generator* gen, uint64_t ns[7]);
 
+/* isn_gen's depth order on its own: pos[i] = the position of i in the order libstdc++'s
+ * std::sort leaves iota(n) in when it sorts by keys[i] (the reference's isn_gen sort,
+ * src/codegen/rv_generator_avx.cpp:539-541), computed by the GPU's emulation of that
+ * introsort -- the order the generator uses to break ties between writers of a word.
+ * keys are non-negative (depths).  For tests and tools; blocks until done. */
+ptl_status ptl_depth_order(const int32_t* keys, size_t n, uint32_t* pos, int device);
+
 /* Human-readable detail of the last non-OK status. */
 const char* ptl_generator_last_error(const ptl_generator* gen);
 

@@ -7,8 +7,8 @@ rv_generator interface plus the seeded synthetic program generator used by the
 benchmarks.
 """
 from .codegen import (DepthTree, PtlError, RvGenerator, SNAPSHOTS, STAGES, code_table,
-                      compile_tree, device_info, disassemble, flatten, library_path, to_asm,
-                      to_elf)
+                      compile_tree, depth_order, device_info, disassemble, flatten, library_path,
+                      to_asm, to_elf)
 
 __all__ = ["DepthTree", "PtlError", "RvGenerator", "SNAPSHOTS", "STAGES", "code_table", "compile_tree",
-           "device_info", "disassemble", "flatten", "library_path", "to_asm", "to_elf"]
+           "depth_order", "device_info", "disassemble", "flatten", "library_path", "to_asm", "to_elf"]

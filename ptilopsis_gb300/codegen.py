@@ -148,6 +148,8 @@ def lib():
         L.ptl_generator_destroy.restype = None
         L.ptl_generator_snapshot.argtypes = [vp, ctypes.c_int, u32p, sz, ctypes.POINTER(sz)]
         L.ptl_compile.argtypes = [ctypes.POINTER(_AstView), ctypes.c_int, u32p, sz, ctypes.POINTER(sz)]
+        L.ptl_depth_order.argtypes = [ctypes.c_void_p, sz, ctypes.c_void_p, ctypes.c_int]
+        L.ptl_depth_order.restype = ctypes.c_int
         L.ptl_code_table.argtypes = [ctypes.c_int, u32p]
         L.ptl_code_table.restype = ctypes.c_size_t
         L.ptl_device_info.argtypes = [ctypes.c_int, ctypes.c_char_p, sz, ctypes.POINTER(ctypes.c_int),
@@ -317,6 +319,17 @@ def compile_tree(tree: DepthTree, device: int = 0, profile: bool = False, scalar
     with RvGenerator(tree, device, scalar=scalar) as gen:
         gen.process(profile=profile)
         return gen.get_instructions()
+
+
+def depth_order(keys, device: int = 0) -> np.ndarray:
+    """isn_gen's depth order on its own (ptl_depth_order): pos[i] is i's position in
+    libstdc++'s std::sort of iota(n) by keys (non-negative), from the GPU's emulation."""
+    k = np.ascontiguousarray(keys, np.int32)
+    pos = np.empty(k.shape[0], np.uint32)
+    st = lib().ptl_depth_order(k.ctypes.data, k.shape[0], pos.ctypes.data, device)
+    if st != 0:
+        raise PtlError(st, "ptl_depth_order")
+    return pos
 
 
 def kernel_launches() -> int:

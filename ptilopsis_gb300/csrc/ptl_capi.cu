@@ -270,6 +270,47 @@ struct StageTimer {
     }
 };
 
+// The depth sort's scratch for n keys (grown as needed), in ss.
+cudaError_t sort_scratch(ptl_generator* g, size_t n, SortScratch* ss) {
+#define E(expr)                                   \
+    do {                                          \
+        const cudaError_t e_ = (expr);            \
+        if (e_ != cudaSuccess) return e_;         \
+    } while (0)
+    const size_t seg_cap = n / 17 + 16, tile_cap = n / kSortTile + seg_cap + 16, leaf_cap = n / 2 + 16;
+    E(g->sort_a.ensure(n, 8));
+    E(g->sort_apos.ensure(n, 4));
+    E(g->sort_bpos.ensure(n, 4));
+    E(g->sort_seg0.ensure(seg_cap, sizeof(SortSeg)));
+    E(g->sort_seg1.ensure(seg_cap, sizeof(SortSeg)));
+    E(g->sort_tile_seg.ensure(tile_cap, 4));
+    E(g->sort_tile_l.ensure(tile_cap, 4));
+    E(g->sort_tile_r.ensure(tile_cap, 4));
+    E(g->sort_leaf.ensure(2 * leaf_cap, 4));
+    E(g->sort_heap.ensure(2 * leaf_cap, 4));
+    E(g->sort_counters.ensure(8, 4));
+    E(g->sort_local.ensure(3 * seg_cap, 4));
+    E(g->sort_equal.ensure(2 * seg_cap, 4));
+    ss->a = g->sort_a.at<unsigned long long>();
+    ss->apos = g->sort_apos.at<uint32_t>();
+    ss->bpos = g->sort_bpos.at<uint32_t>();
+    ss->seg[0] = g->sort_seg0.at<SortSeg>();
+    ss->seg[1] = g->sort_seg1.at<SortSeg>();
+    ss->seg_cap = static_cast<uint32_t>(seg_cap);
+    ss->tile_seg = g->sort_tile_seg.at<uint32_t>();
+    ss->tile_l = g->sort_tile_l.at<uint32_t>();
+    ss->tile_r = g->sort_tile_r.at<uint32_t>();
+    ss->tile_cap = static_cast<uint32_t>(tile_cap);
+    ss->leaf = g->sort_leaf.at<uint32_t>();
+    ss->heap = g->sort_heap.at<uint32_t>();
+    ss->leaf_cap = static_cast<uint32_t>(leaf_cap);
+    ss->counters = g->sort_counters.at<uint32_t>();
+    ss->local = g->sort_local.at<uint32_t>();
+    ss->equal = g->sort_equal.at<uint32_t>();
+#undef E
+    return cudaSuccess;
+}
+
 // row0_hash: the AVX allocator's general row-0 lookup; serial: the scalar allocator in
 // the reference's order for every program.  Both leave the output unchanged.
 ptl_status run_pipeline(ptl_generator* g, bool profile, bool to_host, bool row0_hash, bool serial) {
@@ -353,37 +394,8 @@ ptl_status run_pipeline(ptl_generator* g, bool profile, bool to_host, bool row0_
     timer.mark();
 
     // ---- isn_gen: depth order, register propagation, instruction writes
-    const size_t seg_cap = n / 17 + 16, tile_cap = n / kSortTile + seg_cap + 16, leaf_cap = n / 2 + 16;
-    PTL_CU(g->sort_a.ensure(n, 8));
-    PTL_CU(g->sort_apos.ensure(n, 4));
-    PTL_CU(g->sort_bpos.ensure(n, 4));
-    PTL_CU(g->sort_seg0.ensure(seg_cap, sizeof(SortSeg)));
-    PTL_CU(g->sort_seg1.ensure(seg_cap, sizeof(SortSeg)));
-    PTL_CU(g->sort_tile_seg.ensure(tile_cap, 4));
-    PTL_CU(g->sort_tile_l.ensure(tile_cap, 4));
-    PTL_CU(g->sort_tile_r.ensure(tile_cap, 4));
-    PTL_CU(g->sort_leaf.ensure(2 * leaf_cap, 4));
-    PTL_CU(g->sort_heap.ensure(2 * leaf_cap, 4));
-    PTL_CU(g->sort_counters.ensure(8, 4));
-    PTL_CU(g->sort_local.ensure(3 * seg_cap, 4));
-    PTL_CU(g->sort_equal.ensure(2 * seg_cap, 4));
     SortScratch ss{};
-    ss.a = g->sort_a.at<unsigned long long>();
-    ss.apos = g->sort_apos.at<uint32_t>();
-    ss.bpos = g->sort_bpos.at<uint32_t>();
-    ss.seg[0] = g->sort_seg0.at<SortSeg>();
-    ss.seg[1] = g->sort_seg1.at<SortSeg>();
-    ss.seg_cap = static_cast<uint32_t>(seg_cap);
-    ss.tile_seg = g->sort_tile_seg.at<uint32_t>();
-    ss.tile_l = g->sort_tile_l.at<uint32_t>();
-    ss.tile_r = g->sort_tile_r.at<uint32_t>();
-    ss.tile_cap = static_cast<uint32_t>(tile_cap);
-    ss.leaf = g->sort_leaf.at<uint32_t>();
-    ss.heap = g->sort_heap.at<uint32_t>();
-    ss.leaf_cap = static_cast<uint32_t>(leaf_cap);
-    ss.counters = g->sort_counters.at<uint32_t>();
-    ss.local = g->sort_local.at<uint32_t>();
-    ss.equal = g->sort_equal.at<uint32_t>();
+    PTL_CU(sort_scratch(g, n, &ss));
 
     const size_t wb8 = r8(g->W);
     for (DevBuf* b : {&g->instr, &g->rd, &g->rs1, &g->rs2, &g->jt, &g->used_instrs, &g->symreg, &g->symswp,
@@ -673,6 +685,34 @@ ptl_status ptl_compile(const ptl_ast_view* tree, int device, uint32_t* words, si
     }
     ptl_generator_destroy(g);
     return st;
+}
+
+ptl_status ptl_depth_order(const int32_t* keys, size_t n, uint32_t* pos, int device) {
+    if (!keys || !pos || n == 0 || n >= (1ull << 31)) return PTL_BAD_ARGUMENT;
+    for (size_t i = 0; i < n; ++i) if (keys[i] < 0) return PTL_BAD_ARGUMENT;
+    const DeviceScope on_device(device);
+    if (!on_device.ok()) return PTL_CUDA_ERROR;
+    ptl_generator g;  // its buffers and stream only
+    g.device = device;
+    g.n = n;
+    cudaError_t e = cudaStreamCreateWithFlags(&g.stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = g.dep.ensure(r8(n), 4);
+    if (e == cudaSuccess) e = g.pos.ensure(r8(n), 4);
+    if (e == cudaSuccess) e = g.errw.ensure(1, sizeof(ErrorWord));
+    if (e == cudaSuccess) e = g.flags.ensure(4, 4);
+    if (e == cudaSuccess) e = g.errw.zero(g.stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(g.dep.at<int32_t>(), keys, n * 4, cudaMemcpyHostToDevice, g.stream);
+    SortScratch ss{};
+    if (e == cudaSuccess) e = sort_scratch(&g, n, &ss);
+    if (e == cudaSuccess) {
+        const Prog P = make_prog(&g);
+        uint32_t rounds = 0;
+        e = run_depth_sort(P, ss, g.stream, &rounds, nullptr);
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(pos, g.pos.at<uint32_t>(), n * 4, cudaMemcpyDeviceToHost, g.stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(g.stream);
+    if (e != cudaSuccess) return e == cudaErrorMemoryAllocation ? PTL_OOM : PTL_CUDA_ERROR;
+    return check_error_word(&g);
 }
 
 ptl_status ptl_generator_snapshot(ptl_generator* g, int which, uint32_t* out, size_t capacity, size_t* count) {

@@ -184,3 +184,42 @@ def test_gpu_depth_order_equals_std_sort(built_cuda, case):
         gen.process()
         got = gen.snapshot("depth_order_pos")
     np.testing.assert_array_equal(got[:tree.n], want)
+
+
+def _adversarial_keys(kind: str, n: int, seed: int) -> np.ndarray:
+    rng = np.random.default_rng(seed)
+    if kind == "all_equal":
+        return np.full(n, 7, np.int32)
+    if kind == "one_low":  # all equal but one smaller key, somewhere
+        k = np.full(n, 9, np.int32)
+        k[rng.integers(n)] = 3
+        return k
+    if kind == "mostly_one":  # 99% one value, the rest spread below and above it
+        k = np.full(n, 20, np.int32)
+        idx = rng.choice(n, size=max(1, n // 100), replace=False)
+        k[idx] = rng.integers(0, 41, size=idx.size)
+        return k
+    if kind == "two_alternating":
+        return (np.arange(n) % 2).astype(np.int32) + 5
+    if kind == "few_sorted":
+        return np.sort(rng.integers(0, 4, size=n)).astype(np.int32)
+    if kind == "few_reversed":
+        return np.sort(rng.integers(0, 4, size=n))[::-1].astype(np.int32).copy()
+    return rng.integers(0, 60, size=n).astype(np.int32)  # "depth_like"
+
+
+@pytest.mark.parametrize("kind", ["all_equal", "one_low", "mostly_one", "two_alternating", "few_sorted",
+                                  "few_reversed", "depth_like"])
+@pytest.mark.parametrize("n", [17, 8192, 8193, 50_000, 300_000])
+def test_gpu_depth_order_adversarial_keys(built_cuda, kind, n):
+    """The depth-order emulation on key sets that stress the partition rounds' pair-count
+    bound and the closed forms (one value, one outlier, a 1% sprinkle, alternation, few
+    values sorted either way), at sizes for one leaf, one block, and rounds then blocks:
+    every position against the oracle's std::sort."""
+    from oracle import portbind
+    from ptilopsis_gb300 import depth_order
+    keys = _adversarial_keys(kind, n, seed=n ^ len(kind))
+    perm = portbind.depth_sort(keys)
+    want = np.empty(n, np.uint32)
+    want[perm] = np.arange(n, dtype=np.uint32)
+    np.testing.assert_array_equal(depth_order(keys), want)
