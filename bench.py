@@ -25,7 +25,8 @@ whole batch).  Prints one JSON line (rank 0):
               the plain pipeline over a sample of the programs, checked against and timed
               beside the oracle's restatement of that generator on all host cores
 
---mode single times one large program (config c1, ~4M nodes) per step instead.
+--mode single times one large program (config c1, ~4M nodes) per step instead; --mode
+scalar runs only the scalar generator's measurement.
 --impl reference times the oracle restatement on the host cores on a sample of the same
 workload (the reference itself is AVX2-only and cannot run on the aarch64 GPU hosts).
 Multi-GPU: every rank compiles its own batch (programs are independent, no collective on
@@ -801,7 +802,7 @@ def main():
     ap.add_argument("--config", default="c1")
     ap.add_argument("--scale", type=float, default=1.0)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--mode", default="batched", choices=["batched", "single"])
+    ap.add_argument("--mode", default="batched", choices=["batched", "single", "scalar"])
     ap.add_argument("--programs", type=int, default=4096)
     ap.add_argument("--plain-sample", type=int, default=64)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -822,6 +823,14 @@ def main():
         run_reference(args)
     elif args.mode == "batched":
         run_batched(args)
+    elif args.mode == "scalar":
+        # the scalar generator alone on the first --scalar-sample programs (the `scalar`
+        # object of the batched line, printed by itself)
+        import torch
+        args.programs = args.scalar_sample
+        trees = make_workload(args, 0)
+        torch.cuda.init()
+        print(json.dumps({"mode": "scalar", **run_scalar(trees, 0, len(trees))}), flush=True)
     else:
         run_gb300(args)
 
