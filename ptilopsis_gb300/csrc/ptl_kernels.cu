@@ -1443,6 +1443,109 @@ __global__ void __launch_bounds__(kScalarRaThreads) k_s_ra_tiles(Prog P, unsigne
     __syncthreads();
     for (uint32_t k = threadIdx.x; k < count; k += blockDim.x) s_ra_tile_writeback(P, s_sym, base, count, k);
 }
+// The same steps (s_ra_function, ptl_scalar.cuh) with one warp per function, for the
+// latency of one program's longest function: every lane runs the step's scalar logic on
+// the same values (no divergence), lane k holds registers k and k + 32 of the register
+// state in registers, a swap reads the register it needs by a shuffle, and the
+// function's symbols are bytes in shared memory (register in bits 0..5, swapped in bit
+// 7).  Every lane performs every symbol write with the same value, so each lane reads
+// back what all wrote without a barrier.  Functions of at most `stride` words.
+constexpr uint32_t kScalarWarpFns = 4;          // functions (warps) per block
+constexpr uint32_t kScalarWarpSymCap = 12288;   // symbol bytes per warp
+__global__ void __launch_bounds__(32 * kScalarWarpFns) k_s_ra_warp(Prog P, unsigned long long* preserve,
+                                                                   uint32_t stride) {
+    extern __shared__ uint8_t s_wsym[];
+    constexpr unsigned kFull = 0xFFFFFFFFu;
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t f = blockIdx.x * kScalarWarpFns + (threadIdx.x >> 5);
+    if (f >= P.F) return;  // the whole warp
+    if (!s_ra_function_ok(P, f) || P.fn_size0[f] > stride) {
+        if (lane == 0) record_error(P.err, ST_UNSUPPORTED, W_RA1, f);
+        return;
+    }
+    const uint32_t start = P.fn_start0[f], size = P.fn_size0[f];
+    uint8_t* sym = s_wsym + (threadIdx.x >> 5) * stride;
+    for (uint32_t k = lane; k < size; k += 32u) sym[k] = 0;
+    __syncwarp();
+    int32_t rlo = -1, rhi = -1;  // regs[lane], regs[lane + 32]
+    unsigned long long mask = 0x1Full, pm = 0;
+    bool bad = false;
+    // a symbol's byte index; the cross check keeps it inside the function
+    auto at = [&](uint32_t r) -> uint32_t {
+        const uint32_t w = r - 64u - start;
+        if (w >= size) bad = true;
+        return w < size ? w : 0u;
+    };
+    auto mark = [&](uint64_t regs_swapped) {
+        for (uint64_t m = regs_swapped; m; m &= m - 1ull) {
+            const uint32_t j = ctz64(m);
+            const int32_t v = __shfl_sync(kFull, j < 32u ? rlo : rhi, j & 31u);
+            if (v >= 64) {
+                const uint32_t w = at(u32(v));
+                sym[w] = static_cast<uint8_t>(sym[w] | 0x80u);
+            }
+        }
+    };
+    SWord cur = size > 0 ? s_word(P, start) : SWord{};
+    for (uint32_t i = 0; i < size && !bad; ++i) {
+        const SWord next = i + 1 < size ? s_word(P, start + i + 1) : SWord{};
+        if (cur.used) {
+            const uint32_t ins = cur.ins;
+            if (ins == 0x000000EFu && cur.jt - start >= size) {  // a call out of the function
+                mark(mask & ~kPreservedRegisterMask);
+                mask &= kPreservedRegisterMask;
+                if (!((mask >> lane) & 1ull)) rlo = -1;
+                if (!((mask >> (lane + 32u)) & 1ull)) rhi = -1;
+            } else {
+                const uint32_t r1 = cur.r1, r2 = cur.r2, rdv = cur.rd;
+                uint32_t rs1 = r1, rs2 = r2;
+                if (r1 >= 64u) {
+                    const uint32_t b = sym[at(r1)];
+                    rs1 = (b & 0x80u) ? (s_needs_float(ins, 1) ? 37u : 5u) : (b & 0x3Fu);
+                }
+                if (r2 >= 64u) {
+                    const uint32_t b = sym[at(r2)];
+                    rs2 = (b & 0x80u) ? (s_needs_float(ins, 2) ? 38u : 6u) : (b & 0x3Fu);
+                }
+                unsigned long long cleared = mask;
+                if (rs1 != 0) cleared &= ~(1ull << rs1);
+                if (rs2 != 0) cleared &= ~(1ull << rs2);
+                uint32_t rdr = rdv;
+                if (rdv >= 64u) {
+                    const bool fl = s_needs_float(ins, 0);
+                    const uint32_t r = ffz_low32(cleared | (fl ? 0x00000000FFFFFFFFull : 0xFFFFFFFF00000000ull));
+                    rdr = r == 64u ? (fl ? 37u : 5u) : r;
+                }
+                unsigned long long swap = 0;
+                if (rdr != 0 && ((cleared >> rdr) & 1ull)) swap |= 1ull << rdr;
+                if (rs1 != 0 && ((mask >> rs1) & 1ull)) swap |= 1ull << rs1;
+                if (rs2 != 0 && ((mask >> rs2) & 1ull)) swap |= 1ull << rs2;
+                mark(swap);  // from the register state before the step
+                if (rdv >= 64u) sym[at(rdv)] = static_cast<uint8_t>(rdr);  // rd, rs1, rs2: a later write wins
+                if (r1 >= 64u) sym[at(r1)] = static_cast<uint8_t>(rs1);
+                if (r2 >= 64u) sym[at(r2)] = static_cast<uint8_t>(rs2);
+                if ((rdr & 31u) == lane) (rdr < 32u ? rlo : rhi) = s32(rdv);
+                if (rs1 != rdr && (rs1 & 31u) == lane) (rs1 < 32u ? rlo : rhi) = -1;
+                if (rs2 != rdr && (rs2 & 31u) == lane) (rs2 < 32u ? rlo : rhi) = -1;
+                mask = cleared | (1ull << rdr);
+            }
+        }
+        pm |= mask;
+        cur = next;
+    }
+    if (bad) {
+        if (lane == 0) record_error(P.err, ST_UNSUPPORTED, W_RA1, f);
+        return;
+    }
+    if (lane == 0) preserve[f] = pm & kNonscratchRegisters;
+    __syncwarp();
+    for (uint32_t k = lane; k < size; k += 32u) {
+        const uint32_t b = sym[k];
+        P.symreg[start + k] = b & 0x3Fu;
+        P.symswp[start + k] = (b & 0x80u) ? 0xFFFFFFFFu : 0u;
+    }
+}
+
 __global__ void k_s_ra_serial(Prog P, int32_t* regs, SRaStep* steps, unsigned long long* preserve) {
     if (blockIdx.x == 0 && threadIdx.x == 0) s_ra_serial(P, regs, steps, preserve);
 }
@@ -1820,6 +1923,16 @@ cudaError_t scalar_regalloc_cross(const Prog& P, cudaStream_t s, bool* cross) {
 }
 
 void launch_scalar_ra_free(const Prog& P, unsigned long long* preserve, cudaStream_t s) {
+    if (P.S <= kScalarWarpSymCap) {  // one warp per function
+        const uint32_t stride = (std::max<uint32_t>(P.S, 1u) + 15u) & ~15u;
+        const size_t bytes = static_cast<size_t>(stride) * kScalarWarpFns;
+        if (allow_dynamic_smem(reinterpret_cast<const void*>(&k_s_ra_warp), bytes) == cudaSuccess) {
+            g_launches++;
+            k_s_ra_warp<<<(P.F + kScalarWarpFns - 1u) / kScalarWarpFns, 32u * kScalarWarpFns, bytes, s>>>(P, preserve,
+                                                                                                     stride);
+            return;
+        }
+    }
     // a tile's words: at most one tile plus the longest function
     const uint64_t want = (static_cast<uint64_t>(kScalarTileWords) + P.S + 15u) & ~uint64_t(15);
     const uint32_t cap = static_cast<uint32_t>(std::min<uint64_t>(want, 96u * 1024u));
