@@ -63,11 +63,11 @@ STAGE_BYTES = {
 }
 
 
-# DRAM bytes the isn_gen stage's kernels (the depth sort and the instruction writes)
-# moved per node in one ncu capture of a batched compile of the workload's first 256
-# programs (profiles/isn_gen_traffic_256_programs.md); the batch's traffic is estimated as
-# this times its nodes.
-ISN_GEN_DRAM_BYTES_PER_NODE = 371.1
+# DRAM bytes each stage's kernels moved per node in one ncu capture of a batched compile
+# of the workload's first 256 programs (profiles/stage_traffic_256_programs.md); a
+# batch's traffic is estimated as this times its nodes.
+STAGE_DRAM_BYTES_PER_NODE = {"preprocess": 67.2, "isn_cnt": 53.7, "isn_gen": 371.0, "optimize": 55.6,
+                             "regalloc": 177.2, "fix_jumps": 26.3}
 
 
 def stage_rooflines(stage_ms, tot, peak):
@@ -82,8 +82,10 @@ def stage_rooflines(stage_ms, tot, peak):
             continue
         b = STAGE_BYTES[s](tot["n"], tot["W"], tot["W2"], tot["W3"])
         gbs = b / (ms / 1000.0) / 1e9
+        traffic = STAGE_DRAM_BYTES_PER_NODE[s] * tot["n"]
         out[s] = {"ms": round(float(ms), 3), "algorithmic_bytes": int(b), "achieved_gbs": round(gbs, 1),
-                  "frac": round(gbs / peak, 4)}
+                  "frac": round(gbs / peak, 4), "traffic_bytes_est": int(traffic),
+                  "traffic_over_algorithmic": round(traffic / b, 2)}
         if s in ("isn_cnt", "isn_gen", "optimize"):
             grp_b += b
             grp_ms += ms
@@ -592,7 +594,7 @@ def run_batched(args):
     alg = STAGE_BYTES[name](tot["n"], tot["W"], tot["W2"], tot["W3"])
     achieved = alg / (stage_ms[dom] / 1000.0) / 1e9
     peak, peak_kind = peaks()
-    traffic = ISN_GEN_DRAM_BYTES_PER_NODE * tot["n"] if name == "isn_gen" else None
+    traffic = STAGE_DRAM_BYTES_PER_NODE[name] * tot["n"]
     roofline = {"bound": "hbm", "kernel": f"{name} stage (all programs)", "achieved": achieved, "peak": peak,
                 "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
                 "traffic_source": ("ncu dram__bytes_read.sum + dram__bytes_write.sum of the stage's kernels on the "
