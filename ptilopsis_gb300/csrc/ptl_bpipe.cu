@@ -499,8 +499,8 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
         Layout Ln, Lr;
         Ln.build(nb8, active);
         Lr.build(n3, active);
-        BP_CU(family_written(Ln, {&nt, &rt, &nd1, &nd, &par, &ci, &dep, &loc0, &loc}, 4));
-        BP_CU(family_written(Ln, {&fflag}, 1));
+        BP_CU(family_written(Ln, {&nd1, &nd, &par, &ci, &dep, &loc0, &loc}, 4));
+        BP_CU(family_written(Ln, {&nt, &rt, &fflag}, 1));
         BP_CU(family(Ln, {&pos, &decl}, 4));
         BP_CU(family(Lr, {&regs}, 4));
         hp.assign(B, Prog{});
@@ -516,8 +516,8 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
             P.in_child = in_child.at<int32_t>(din[p]);
             P.in_data = in_data.at<uint32_t>(din[p]);
             const uint64_t e = Ln.elem(p);
-            P.nt = nt.at<uint32_t>(e);
-            P.rt = rt.at<uint32_t>(e);
+            P.nt = nt.at<uint8_t>(e);
+            P.rt = rt.at<uint8_t>(e);
             P.nd1 = nd1.at<uint32_t>(e);
             P.nd = nd.at<uint32_t>(e);
             P.par = par.at<int32_t>(e);

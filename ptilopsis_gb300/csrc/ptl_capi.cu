@@ -164,8 +164,8 @@ Prog make_prog(ptl_generator* g) {
     P.in_depth = g->in_depth.at<int32_t>();
     P.in_child = g->in_child.at<int32_t>();
     P.in_data = g->in_data.at<uint32_t>();
-    P.nt = g->nt.at<uint32_t>();
-    P.rt = g->rt.at<uint32_t>();
+    P.nt = g->nt.at<uint8_t>();
+    P.rt = g->rt.at<uint8_t>();
     P.nd1 = g->nd1.at<uint32_t>();
     P.nd = g->nd.at<uint32_t>();
     P.par = g->par.at<int32_t>();
@@ -326,7 +326,11 @@ ptl_status run_pipeline(ptl_generator* g, bool profile, bool to_host, bool row0_
     PTL_CU(g->errw.zero(s));
     PTL_CU(g->meta.zero(s));
     // node arrays
-    for (DevBuf* b : {&g->nt, &g->rt, &g->nd1, &g->nd, &g->par, &g->ci, &g->dep, &g->sizes, &g->loc0, &g->loc, &g->pos}) {
+    for (DevBuf* b : {&g->nt, &g->rt}) {
+        PTL_CU(b->ensure(nb8, 1));
+        PTL_CU(b->zero(s));
+    }
+    for (DevBuf* b : {&g->nd1, &g->nd, &g->par, &g->ci, &g->dep, &g->sizes, &g->loc0, &g->loc, &g->pos}) {
         PTL_CU(b->ensure(nb8, 4));
         PTL_CU(b->zero(s));
     }
@@ -757,7 +761,13 @@ ptl_status ptl_generator_snapshot(ptl_generator* g, int which, uint32_t* out, si
     *count = len;
     if (!out) return PTL_OK;
     if (capacity < len) return PTL_BAD_ARGUMENT;
-    if (len) {
+    if (len && b->elem == 1) {  // byte arrays (node and data types), widened
+        std::vector<uint8_t> bytes(len);
+        cudaError_t e = cudaMemcpyAsync(bytes.data(), b->at<uint8_t>(), len, cudaMemcpyDeviceToHost, g->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+        if (e != cudaSuccess) return cuda_fail(g, e, "snapshot");
+        for (size_t k = 0; k < len; ++k) out[k] = bytes[k];
+    } else if (len) {
         cudaError_t e = cudaMemcpyAsync(out, b->at<uint32_t>(), len * 4, cudaMemcpyDeviceToHost, g->stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
         if (e != cudaSuccess) return cuda_fail(g, e, "snapshot");

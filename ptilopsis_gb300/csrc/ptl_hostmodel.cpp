@@ -47,9 +47,9 @@ struct Model {
     CodeTables tab;
     ErrorWord err{};
     uint32_t flags[4] = {0, 0, 0, 0};
-    HBuf<uint8_t> in_type, in_rtype, fflag, used, smark, defpos;
+    HBuf<uint8_t> in_type, in_rtype, fflag, used, smark, defpos, nt, rt;
     HBuf<int32_t> in_parent, in_depth, in_child, par, ci, dep;
-    HBuf<uint32_t> in_data, nt, rt, nd1, nd, sizes, loc0, loc, regs, pos, decl, fn_id, fn_start, fn_size,
+    HBuf<uint32_t> in_data, nd1, nd, sizes, loc0, loc, regs, pos, decl, fn_id, fn_start, fn_size,
         fn_end, fn_start0, fn_size0, fn_end0, fn_ra_start, fn_ra_end, fn_ra_size, instr, rd, rs1, rs2, jt,
         used_instrs, symreg, symswp, stamp, trig_min, trig_max, spill, roffs, ni, nrd, nr1, nr2, njt, fsz,
         joffs, out;
@@ -265,7 +265,9 @@ struct Model {
         std::memcpy(in_type.p, type, n); std::memcpy(in_rtype.p, rtype, n);
         std::memcpy(in_parent.p, parent, 4ull * n); std::memcpy(in_depth.p, depth, 4ull * n);
         std::memcpy(in_child.p, child, 4ull * n); std::memcpy(in_data.p, data, 4ull * n);
-        for (auto* b : {&nt, &rt, &nd1, &nd, &sizes, &loc0, &loc, &pos, &decl}) b->ensure(nb8);
+        for (auto* b : {&nd1, &nd, &sizes, &loc0, &loc, &pos, &decl}) b->ensure(nb8);
+        nt.ensure(nb8);
+        rt.ensure(nb8);
         for (auto* b : {&par, &ci, &dep}) b->ensure(nb8);
         fflag.ensure(nb8);
         regs.ensure(3ull * n);
@@ -414,7 +416,14 @@ int ptlhm_compile_mode(const uint8_t* type, const uint8_t* rtype, const int32_t*
         const Prog& P = m->P;
         put(0, P.out, P.W3);
         put(1, P.fn_start, P.F); put(2, P.fn_end, P.F); put(3, P.fn_size, P.F); put(4, P.fn_id, P.F);
-        put(5, P.nt, P.n); put(6, P.rt, P.n); put(7, P.nd, P.n);
+        {
+            std::vector<uint32_t> wide(P.n);
+            for (uint32_t i = 0; i < P.n; ++i) wide[i] = P.nt[i];
+            put(5, wide.data(), P.n);
+            for (uint32_t i = 0; i < P.n; ++i) wide[i] = P.rt[i];
+            put(6, wide.data(), P.n);
+        }
+        put(7, P.nd, P.n);
         put(8, P.sizes, P.n); put(9, P.loc, P.n);
         put(10, P.fn_id, P.F); put(11, P.fn_start0, P.F); put(12, m->fn_end0.p, P.F); put(13, P.fn_size0, P.F);
         put(14, P.instr, P.W); put(15, P.rd, P.W); put(16, P.rs1, P.W); put(17, P.rs2, P.W); put(18, P.jt, P.W);

@@ -136,8 +136,8 @@ struct Prog {
     const int32_t* in_child;
     const uint32_t* in_data;
     // node arrays (padded)
-    uint32_t* nt;     // rv node type
-    uint32_t* rt;     // data type (final after preprocess)
+    uint8_t* nt;      // rv node type (every type fits a byte)
+    uint8_t* rt;      // data type (final after preprocess)
     uint32_t* nd1;    // node data after pass 1
     uint32_t* nd;     // node data after pass 2 (final)
     int32_t* par;
