@@ -627,6 +627,13 @@ def run_batched(args):
              "nodes": sn, "sample": f"first {len(sample)} programs of the workload, one generator, one at a time",
              "stage_ms": {k: round(float(v) / 1e6, 3) for k, v in zip(STAGES, plain_stage)}}
     same_as_plain = all(np.array_equal(bc.words(k), plain_words[k]) for k in range(len(sample)))
+    if rank == 0 and not args.no_cpu_baseline:
+        # what one caller with one program at a time gets on the CPU: the oracle's
+        # restatement on one core over the same sample, beside the plain pipeline
+        rate1, dt1, _ = port_parallel(sample, 1)
+        plain["cpu_one_program_at_a_time"] = {"value": rate1, "unit": UNIT, "cores": 1, "kind": "port",
+                                              "seconds": round(dt1, 3),
+                                              "plain_over_cpu": plain["value"] / rate1}
     oracle_check, cpu_line = None, None
     if rank == 0 and not args.no_cpu_baseline:
         # the oracle on every program of the batch, on all host cores (outside the timed
