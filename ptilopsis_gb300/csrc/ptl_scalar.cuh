@@ -4,11 +4,12 @@
 // comparison pass, isn_gen's parent-slot and jump-target rules, the lui constant, and a
 // register allocator with one register state per function and real preserve masks.
 //
-// Stages that compute the same thing in both generators (isn_cnt with its fix-ups and
-// function table, the depth order, optimize's fixed point, fix_jumps, postprocess) run
-// the AVX stage functions of ptl_stages.cuh; the functions here replace the others.  Each
-// is one thread's share, shared by the CUDA kernels and the host model, as in
-// ptl_stages.cuh.
+// Stages that compute the same thing in both generators (the depth order, optimize's
+// fixed point, fix_jumps, postprocess) run the AVX stage functions of ptl_stages.cuh, and
+// so does isn_cnt, whose three scalar differences are branches there (st_count,
+// fix_loc0); the functions here replace the others.  Each is one thread's share, shared
+// by the CUDA kernels and the host model, as in ptl_stages.cuh (the warp-per-function
+// register allocation kernel restates s_ra_function's steps in ptl_kernels.cu).
 #pragma once
 
 #include "ptl_stages.cuh"
