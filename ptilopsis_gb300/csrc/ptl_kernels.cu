@@ -594,6 +594,8 @@ struct BlockSortSmem {
     uint32_t bst_f[kSortStack], bst_l[kSortStack], bst_d[kSortStack];
     uint32_t cntL[kSortBlockSweeps * kSortBlockWarps], cntR[kSortBlockSweeps * kSortBlockWarps];
     int32_t wmin[kSortBlockWarps], wmax[kSortBlockWarps];
+    int32_t kmin, kmax;
+    uint32_t nL, nR, K, cut;
     uint32_t n_sm, n_fin, next_sm, n_bst, bad;
     uint32_t cur_f, cur_l, cur_d, have;
 };
@@ -641,24 +643,14 @@ __device__ __forceinline__ int32_t warp_max_i32(int32_t v) {
     return v;
 }
 
-// One block-wide split of [f, l): the partition's cut and the part's least and greatest
-// key (w.bad on a broken invariant).  Every thread calls it and gets the same result;
-// it ends with a barrier.  The caller has moved the median to f (thread 0, before the
-// barrier that publishes the part).  Three barriers: after the stop counts, after the
-// stop positions, after the swaps -- between them every warp computes the scan of the
-// counts and the pair count K for itself (a few shuffles and broadcast reads) instead of
-// one warp computing them for all behind two more barriers.
-struct BSplit {
-    uint32_t cut;
-    int32_t kmin, kmax;
-};
-
-__device__ BSplit bsort_split_block(BlockSortSmem& w, uint32_t f, uint32_t l) {
+// One block-wide split of [f, l); sets w.K / w.cut / w.kmin / w.kmax (w.bad on a broken
+// invariant).  Every thread calls it; it ends with a barrier.
+// The caller has moved the median to f (thread 0, before the barrier that publishes the
+// part).
+__device__ void bsort_split_block(BlockSortSmem& w, uint32_t f, uint32_t l) {
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
     const unsigned full = 0xFFFFFFFFu, lt = (1u << lane) - 1u;
     constexpr uint32_t T = kSortBlockThreads;
-    constexpr uint32_t E = kSortBlockSweeps * kSortBlockWarps, per = E / 32;
-    static_assert(kSortBlockWarps % per == 0, "a warp's count entries sit at one lane position");
     const int32_t pivot = skey(w.buf[f]);
     const uint32_t sweeps = (l - f - 1u + T - 1u) / T;
     uint32_t fl = 0, fr = 0;
@@ -682,72 +674,88 @@ __device__ BSplit bsort_split_block(BlockSortSmem& w, uint32_t f, uint32_t l) {
     mx = warp_max_i32(mx);
     if (lane == 0) { w.wmin[warp] = mn; w.wmax[warp] = mx; }
     __syncthreads();
-    // the exclusive scan of the (sweep, warp) counts in that order, 8 entries per lane:
-    // this warp's entry of sweep k is entry k * warps + warp, at lane position warp % per
-    const uint32_t used = sweeps * kSortBlockWarps, q0 = warp % per;
-    uint32_t sl = 0, sr = 0, bl = 0, br = 0;
+    if (warp == 0) {
+        // exclusive scan of the (sweep, warp) counts in that order, 8 entries per lane
+        constexpr uint32_t E = kSortBlockSweeps * kSortBlockWarps, per = E / 32;
+        const uint32_t used = sweeps * kSortBlockWarps;
+        uint32_t vl[per], vr[per], sl = 0, sr = 0;
 #pragma unroll
-    for (uint32_t q = 0; q < per; ++q) {
-        const uint32_t e = lane * per + q;
-        if (q == q0) { bl = sl; br = sr; }
-        sl += e < used ? w.cntL[e] : 0u;
-        sr += e < used ? w.cntR[e] : 0u;
-    }
-    uint32_t il = sl, ir = sr;
+        for (uint32_t q = 0; q < per; ++q) {
+            const uint32_t e = lane * per + q;
+            vl[q] = e < used ? w.cntL[e] : 0u;
+            vr[q] = e < used ? w.cntR[e] : 0u;
+            sl += vl[q];
+            sr += vr[q];
+        }
+        uint32_t il = sl, ir = sr;
 #pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-        const uint32_t al = __shfl_up_sync(full, il, d), ar = __shfl_up_sync(full, ir, d);
-        if (lane >= static_cast<uint32_t>(d)) { il += al; ir += ar; }
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t al = __shfl_up_sync(full, il, d), ar = __shfl_up_sync(full, ir, d);
+            if (lane >= static_cast<uint32_t>(d)) { il += al; ir += ar; }
+        }
+        uint32_t ol = il - sl, orr = ir - sr;
+#pragma unroll
+        for (uint32_t q = 0; q < per; ++q) {
+            const uint32_t e = lane * per + q;
+            if (e < used) { w.cntL[e] = ol; w.cntR[e] = orr; }
+            ol += vl[q];
+            orr += vr[q];
+        }
+        int32_t a = lane < kSortBlockWarps ? w.wmin[lane] : pivot, b = lane < kSortBlockWarps ? w.wmax[lane] : pivot;
+        a = warp_min_i32(a);
+        b = warp_max_i32(b);
+        if (lane == 31) { w.nL = il; w.nR = ir; }
+        if (lane == 0) { w.kmin = a; w.kmax = b; }
     }
-    const uint32_t offl = il - sl + bl, offr = ir - sr + br;  // of entry lane * per + q0
-    const uint32_t nL = __shfl_sync(full, il, 31), nR = __shfl_sync(full, ir, 31);
-    BSplit out;
-    out.kmin = warp_min_i32(lane < static_cast<uint32_t>(kSortBlockWarps) ? w.wmin[lane] : pivot);
-    out.kmax = warp_max_i32(lane < static_cast<uint32_t>(kSortBlockWarps) ? w.wmax[lane] : pivot);
+    __syncthreads();
     for (uint32_t k = 0; k < sweeps; ++k) {
-        const uint32_t src = (k * kSortBlockWarps + warp) / per;
-        const uint32_t ol = __shfl_sync(full, offl, src), orr = __shfl_sync(full, offr, src);
         const bool isL = (fl >> k) & 1u, isR = (fr >> k) & 1u;
         const unsigned bL = __ballot_sync(full, isL), bR = __ballot_sync(full, isR);
         const uint32_t p = f + 1u + k * T + tid;
-        if (isL) w.A[f + ol + __popc(bL & lt)] = static_cast<uint16_t>(p);
-        if (isR) w.R[f + orr + __popc(bR & lt)] = static_cast<uint16_t>(p);
+        if (isL) w.A[f + w.cntL[k * kSortBlockWarps + warp] + __popc(bL & lt)] = static_cast<uint16_t>(p);
+        if (isR) w.R[f + w.cntR[k * kSortBlockWarps + warp] + __popc(bR & lt)] = static_cast<uint16_t>(p);
     }
     __syncthreads();
-    uint32_t K = 0, cut = 0;
-    const bool lead = tid == 0;
-    if (nL == 0 || nR == 0) {  // the median move guarantees both kinds of stop
-        if (lead) w.bad = 1;
-    } else {
-        // K: A[k] < B[k] holds on a prefix of k, and K is in [lo, hi].  32 probes per round
-        // narrow the range to one of 33 slices; the last round tests each index.
-        uint32_t lo = 0, hi = nL < nR ? nL : nR;
-        while (hi - lo > 32u) {
-            const uint64_t span = hi - lo;
-            const uint32_t q = lo + static_cast<uint32_t>(span * (lane + 1u) / 33u);
-            const uint32_t c = __popc(__ballot_sync(full, w.A[f + q] < w.R[f + nR - 1u - q]));
-            const uint32_t nlo = c == 0 ? lo : lo + static_cast<uint32_t>(span * c / 33u) + 1u;
-            const uint32_t nhi = c == 32 ? hi : lo + static_cast<uint32_t>(span * (c + 1u) / 33u);
-            lo = nlo;
-            hi = nhi;
-        }
-        const uint32_t q = lo + lane;
-        K = lo + __popc(__ballot_sync(full, q < hi && w.A[f + q] < w.R[f + nR - 1u - q]));
-        if (K == 0) {
-            cut = w.A[f];
+    if (warp == 0) {
+        const uint32_t nL = w.nL, nR = w.nR;
+        uint32_t K = 0, cut = 0;
+        if (nL == 0 || nR == 0) {  // the median move guarantees both kinds of stop
+            if (lane == 0) w.bad = 1;
         } else {
-            const uint32_t bk = w.R[f + nR - K];  // B[K-1]
-            cut = (K < nL && w.A[f + K] < bk) ? w.A[f + K] : bk;
+            // K: A[k] < B[k] holds on a prefix of k, and K is in [lo, hi].  32 probes per
+            // round narrow the range to one of 33 slices; the last round tests each index.
+            uint32_t lo = 0, hi = nL < nR ? nL : nR;
+            while (hi - lo > 32u) {
+                const uint64_t span = hi - lo;
+                const uint32_t q = lo + static_cast<uint32_t>(span * (lane + 1u) / 33u);
+                const uint32_t c = __popc(__ballot_sync(full, w.A[f + q] < w.R[f + nR - 1u - q]));
+                const uint32_t nlo = c == 0 ? lo : lo + static_cast<uint32_t>(span * c / 33u) + 1u;
+                const uint32_t nhi = c == 32 ? hi : lo + static_cast<uint32_t>(span * (c + 1u) / 33u);
+                lo = nlo;
+                hi = nhi;
+            }
+            const uint32_t q = lo + lane;
+            K = lo + __popc(__ballot_sync(full, q < hi && w.A[f + q] < w.R[f + nR - 1u - q]));
+            if (K == 0) {
+                cut = w.A[f];
+            } else {
+                const uint32_t bk = w.R[f + nR - K];  // B[K-1]
+                cut = (K < nL && w.A[f + K] < bk) ? w.A[f + K] : bk;
+            }
+            if (cut <= f || cut >= l) {
+                if (lane == 0) w.bad = 1;
+                K = 0;
+            }
         }
-        if (cut <= f || cut >= l) {
-            if (lead) w.bad = 1;
-            K = 0;
+        if (lane == 0) {
+            w.K = K;
+            w.cut = cut;
         }
     }
-    out.cut = cut;
+    __syncthreads();
+    const uint32_t K = w.K, nR = w.nR;
     for (uint32_t k = tid; k < K; k += T) sswap(w.buf, w.A[f + k], w.R[f + nR - 1u - k]);
     __syncthreads();
-    return out;
 }
 
 // One warp finishes part [f, l) (more than 16 keys, depth budget d > 0) and every part
@@ -876,14 +884,14 @@ __global__ void __launch_bounds__(kSortBlockThreads) k_sort_block(SortScratch ss
         // parts longer than kSortLocal: the whole block
         while (w.have) {
             const uint32_t f = w.cur_f, l = w.cur_l, d = w.cur_d;
-            const BSplit sp = bsort_split_block(w, f, l);
+            bsort_split_block(w, f, l);
             if (tid == 0) {
                 w.have = 0;
                 if (!w.bad) {
-                    const uint32_t cut = sp.cut;
+                    const uint32_t cut = w.cut;
                     const int32_t pivot = skey(w.buf[f]);
-                    const bool gl = bsort_route(w, f, cut, d - 1, sp.kmin == pivot);
-                    const bool gr = bsort_route(w, cut, l, d - 1, sp.kmax == pivot);
+                    const bool gl = bsort_route(w, f, cut, d - 1, w.kmin == pivot);
+                    const bool gr = bsort_route(w, cut, l, d - 1, w.kmax == pivot);
                     // warp-sized parts are listed; of two block-sized parts the larger waits
                     const bool bl = gl && cut - f > kSortLocal, br = gr && l - cut > kSortLocal;
                     if (gl && !bl) bsort_push_small(w, f, cut, d - 1);
