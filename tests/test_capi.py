@@ -8,6 +8,7 @@ import re
 import zlib
 
 import numpy as np
+import pytest
 
 from conftest import ROOT, manifest
 
@@ -43,3 +44,18 @@ def test_no_cpu_fallback_without_library(monkeypatch, built_cuda):
     monkeypatch.setattr(codegen, "LIB_PATH", "/nonexistent/libptl_gb300.so")
     with pytest.raises(RuntimeError, match="no CPU fallback"):
         codegen.lib()
+
+
+def test_argument_checks_need_no_device(built_cuda):
+    """Arguments the C ABI refuses before touching a device: status BAD_ARGUMENT (7)."""
+    import ctypes
+    import numpy as np
+    from ptilopsis_gb300 import PtlError, depth_order
+    from ptilopsis_gb300.codegen import lib
+    with pytest.raises(PtlError) as e:
+        depth_order(np.array([3, -1, 2], np.int32))  # keys are depths, never negative
+    assert e.value.status == 7
+    L = lib()
+    assert L.ptl_depth_order(None, 4, None, 0) == 7
+    count = ctypes.c_size_t()
+    assert L.ptl_compile(None, 0, None, 0, ctypes.byref(count)) == 7
