@@ -604,6 +604,14 @@ def run_batched(args):
                 "stage_ms": {s: round(float(v), 3) for s, v in zip(STAGES, stage_ms)},
                 "depth_sort_ms": round(float(np.mean(sort_ms)), 3),  # part of isn_gen
                 **stage_rooflines(stage_ms, tot, peak)}
+    # isn_gen's generation passes alone: its algorithmic bytes (inputs, registers, words;
+    # the depth order moves none of them) over the stage's time less the depth sort's
+    gen_ms = float(stage_ms[STAGES.index("isn_gen")]) - float(np.mean(sort_ms))
+    if gen_ms > 0:
+        gb = STAGE_BYTES["isn_gen"](tot["n"], tot["W"], tot["W2"], tot["W3"])
+        roofline["isn_gen_generation_passes"] = {"ms": round(gen_ms, 3), "algorithmic_bytes": int(gb),
+                                                 "achieved_gbs": round(gb / (gen_ms / 1000.0) / 1e9, 1),
+                                                 "frac": round(gb / (gen_ms / 1000.0) / 1e9 / peak, 4)}
 
     # the plain pipeline on a sample of the same programs, one at a time
     sample = trees[:args.plain_sample]
