@@ -139,8 +139,8 @@ public:
     DBuf trig_min, trig_max, ra_chunks;
     DBuf ni, nrd, nr1, nr2, njt, joffs, out;
     DBuf errw, flags, meta, progs, tabs, lists, changed, sort_err, a_off, dirty, ra_sync;
-    DBuf sa, sapos, sbpos, seg0, seg1, tile_seg, tile_l, tile_r, leaf, heap, counters, scan_status, scan_counter,
-        sort_local, sort_equal;
+    DBuf sa, sapos, sbpos, seg0, seg1, tile_seg, tile_l, tile_r, sort_stops, leaf, heap, counters, scan_status,
+        scan_counter, sort_local, sort_equal;
     PBuf h_in, h_out, h_fn, h_small, h_gp;
     DBuf d_gp;                 // host-gather parameters (source pointers, offsets, counts)
     bool direct_host = false;  // the device reads pageable host memory coherently
@@ -170,7 +170,7 @@ public:
                 &symswp, &stamp, &spill, &roffs, &owner, &used, &smark, &defpos, &trig_min, &trig_max, &ra_chunks, &ni, &nrd,
                 &nr1, &nr2, &njt, &joffs, &out, &errw, &flags, &meta, &progs, &tabs, &lists, &changed,
                 &sort_err, &a_off, &dirty, &ra_sync, &sa, &sapos, &sbpos, &seg0, &seg1, &tile_seg, &tile_l, &tile_r,
-                &leaf, &heap, &counters, &scan_status, &scan_counter, &sort_local, &sort_equal};
+                &sort_stops, &leaf, &heap, &counters, &scan_status, &scan_counter, &sort_local, &sort_equal};
     }
 
     ptl_status cuda_fail(cudaError_t e, const char* what) {
@@ -665,7 +665,9 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
             if (!active[p]) continue;
             const uint64_t np = n[p];
             seg_cap += np / 17 + 16;
-            tile_cap += np / 2048 + np / 17 + 16;
+            // a round's segments are disjoint and longer than kSortBlock: at most
+            // np / kSortBlock of them, each with one partial tile
+            tile_cap += np / kSortTile + np / kSortBlock + 16;
             leaf_cap += np / 2 + 16;
             if (np > kSortBlock) {
                 SortSeg g{};
@@ -695,6 +697,7 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
         BP_CU(tile_seg.ensure(tile_cap * 4));
         BP_CU(tile_l.ensure(tile_cap * 4));
         BP_CU(tile_r.ensure(tile_cap * 4));
+        BP_CU(sort_stops.ensure(tile_cap * 2 * (kSortTile / 32) * 4));
         BP_CU(leaf.ensure(2 * leaf_cap * 4));
         BP_CU(heap.ensure(2 * leaf_cap * 4));
         BP_CU(counters.ensure(64));
@@ -714,6 +717,7 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
         ss.tile_seg = tile_seg.at<uint32_t>();
         ss.tile_l = tile_l.at<uint32_t>();
         ss.tile_r = tile_r.at<uint32_t>();
+        ss.stops = sort_stops.at<uint32_t>();
         ss.tile_cap = static_cast<uint32_t>(tile_cap);
         ss.leaf = leaf.at<uint32_t>();
         ss.heap = heap.at<uint32_t>();

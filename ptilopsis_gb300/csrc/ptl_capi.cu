@@ -88,7 +88,7 @@ struct ptl_generator {
     DevBuf instr, rd, rs1, rs2, jt, owner, used, smark, used_instrs;
     DevBuf symreg, symswp, stamp, defpos, lifetime, trig_min, trig_max, ra_chunks, spill, roffs;
     DevBuf ni, nrd, nr1, nr2, njt, fsz, joffs, out;
-    DevBuf sort_a, sort_apos, sort_bpos, sort_seg0, sort_seg1, sort_tile_seg, sort_tile_l, sort_tile_r,
+    DevBuf sort_a, sort_apos, sort_bpos, sort_seg0, sort_seg1, sort_tile_seg, sort_tile_l, sort_tile_r, sort_stops,
         sort_leaf, sort_heap, sort_counters, sort_local, sort_equal;
     DevBuf scan_status, scan_counter, meta, flags, errw, tables;
     DevBuf preserve, sregs, ssteps, sextra, sclaim;  // scalar register allocation
@@ -113,7 +113,7 @@ struct ptl_generator {
                 &fn_size, &fn_end, &fn_start0, &fn_size0, &fn_end0, &fn_ra_start, &fn_ra_end, &fn_ra_size,
                 &instr, &rd, &rs1, &rs2, &jt, &owner, &used, &smark, &used_instrs, &symreg, &symswp,
                 &stamp, &defpos, &lifetime, &trig_min, &trig_max, &ra_chunks, &spill, &roffs, &ni, &nrd, &nr1, &nr2, &njt,
-                &fsz, &joffs, &out, &sort_a, &sort_apos, &sort_bpos, &sort_seg0, &sort_seg1,
+                &fsz, &joffs, &out, &sort_a, &sort_apos, &sort_bpos, &sort_seg0, &sort_seg1, &sort_stops,
                 &sort_tile_seg, &sort_tile_l, &sort_tile_r, &sort_leaf, &sort_heap, &sort_counters, &sort_local, &sort_equal,
                 &scan_status, &scan_counter, &meta, &flags, &errw, &tables, &preserve, &sregs, &ssteps,
                 &sextra, &sclaim};
@@ -277,7 +277,8 @@ cudaError_t sort_scratch(ptl_generator* g, size_t n, SortScratch* ss) {
         const cudaError_t e_ = (expr);            \
         if (e_ != cudaSuccess) return e_;         \
     } while (0)
-    const size_t seg_cap = n / 17 + 16, tile_cap = n / kSortTile + seg_cap + 16, leaf_cap = n / 2 + 16;
+    // a round's segments are disjoint and longer than kSortBlock, each with one partial tile
+    const size_t seg_cap = n / 17 + 16, tile_cap = n / kSortTile + n / kSortBlock + 16, leaf_cap = n / 2 + 16;
     E(g->sort_a.ensure(n, 8));
     E(g->sort_apos.ensure(n, 4));
     E(g->sort_bpos.ensure(n, 4));
@@ -286,6 +287,7 @@ cudaError_t sort_scratch(ptl_generator* g, size_t n, SortScratch* ss) {
     E(g->sort_tile_seg.ensure(tile_cap, 4));
     E(g->sort_tile_l.ensure(tile_cap, 4));
     E(g->sort_tile_r.ensure(tile_cap, 4));
+    E(g->sort_stops.ensure(tile_cap * 2 * (kSortTile / 32), 4));
     E(g->sort_leaf.ensure(2 * leaf_cap, 4));
     E(g->sort_heap.ensure(2 * leaf_cap, 4));
     E(g->sort_counters.ensure(8, 4));
@@ -300,6 +302,7 @@ cudaError_t sort_scratch(ptl_generator* g, size_t n, SortScratch* ss) {
     ss->tile_seg = g->sort_tile_seg.at<uint32_t>();
     ss->tile_l = g->sort_tile_l.at<uint32_t>();
     ss->tile_r = g->sort_tile_r.at<uint32_t>();
+    ss->stops = g->sort_stops.at<uint32_t>();
     ss->tile_cap = static_cast<uint32_t>(tile_cap);
     ss->leaf = g->sort_leaf.at<uint32_t>();
     ss->heap = g->sort_heap.at<uint32_t>();

@@ -328,7 +328,10 @@ __device__ __forceinline__ void block_excl_scan2(uint32_t a, uint32_t b, uint32_
 
 // Stop counts per tile, and the least and greatest key of each segment (atomics on the
 // segment record; a part of the next split is known to hold one key when its bound on
-// the pivot's side meets the pivot).
+// the pivot's side meets the pivot).  The tile's stop bits go to ss.stops (tile-local
+// key j at word j / 32, bit j % 32), so the position pass reads 2 bits per key, not 8
+// bytes.
+constexpr uint32_t kStopWords = kSortTile / 32;  // per kind and tile
 __global__ void __launch_bounds__(kThreads) k_sort_count(SortScratch ss, SortSeg* cur) {
     __shared__ uint32_t sm[kThreads / 32];
     __shared__ int32_t smn[kThreads / 32], smx[kThreads / 32];
@@ -347,6 +350,17 @@ __global__ void __launch_bounds__(kThreads) k_sort_count(SortScratch ss, SortSeg
         for (uint32_t u = 0; u < kSortItems; ++u) {
             const uint32_t p = lo + threadIdx.x + u * kThreads;
             key[u] = p < hi ? skey(ss.a[p]) : g.pivot;
+        }
+        uint32_t* bits = ss.stops + static_cast<size_t>(t) * 2u * kStopWords;
+#pragma unroll
+        for (uint32_t u = 0; u < kSortItems; ++u) {  // tile-local j = warp * 32 + lane + u * kThreads
+            const bool in = lo + threadIdx.x + u * kThreads < hi;
+            const unsigned bl = __ballot_sync(0xFFFFFFFFu, in && is_lstop(key[u], g.pivot));
+            const unsigned br = __ballot_sync(0xFFFFFFFFu, in && is_rstop(key[u], g.pivot));
+            if (lane == 0) {
+                bits[warp + u * (kThreads / 32)] = bl;
+                bits[kStopWords + warp + u * (kThreads / 32)] = br;
+            }
         }
 #pragma unroll
         for (uint32_t u = 0; u < kSortItems; ++u) {
@@ -433,16 +447,15 @@ __global__ void __launch_bounds__(kThreads) k_sort_pos(SortScratch ss, const Sor
         const uint32_t lo = g.first + 1 + (t - g.tbase) * kSortTile;
         const uint32_t hi = min(g.last, lo + kSortTile);
         const uint32_t p0 = lo + threadIdx.x * kSortItems;
-        uint32_t fl = 0, fr = 0, cl = 0, cr = 0;
-#pragma unroll
-        for (uint32_t k = 0; k < kSortItems; ++k) {
-            const uint32_t p = p0 + k;
-            if (p < hi) {
-                const int32_t key = skey(ss.a[p]);
-                if (is_lstop(key, g.pivot)) { fl |= 1u << k; ++cl; }
-                if (is_rstop(key, g.pivot)) { fr |= 1u << k; ++cr; }
-            }
-        }
+        // this thread's kSortItems keys: tile-local j = threadIdx.x * 8 .. + 7, one byte of
+        // a stop word (bits past the tile's end are clear)
+        static_assert(kSortItems == 8, "a thread's stop bits are one byte of a word");
+        const uint32_t* bits = ss.stops + static_cast<size_t>(t) * 2u * kStopWords;
+        const uint32_t sh = (threadIdx.x & 3u) * 8u;
+        const uint32_t fl = (bits[threadIdx.x >> 2] >> sh) & 0xFFu;
+        const uint32_t fr = (bits[kStopWords + (threadIdx.x >> 2)] >> sh) & 0xFFu;
+        const uint32_t cl = __popc(fl), cr = __popc(fr);
+        (void)hi;
         uint32_t el, er, tot[2];
         block_excl_scan2(cl, cr, sm, &el, &er, tot);
         uint32_t rl = ss.tile_l[t] + el;
@@ -1629,6 +1642,7 @@ void launch_sort_round(const SortScratch& ss, SortSeg* segs, SortSeg* next, Erro
 bool same_layout(const SortScratch& a, const SortScratch& b) {
     return a.a == b.a && a.apos == b.apos && a.bpos == b.bpos && a.seg[0] == b.seg[0] && a.seg[1] == b.seg[1] &&
            a.seg_cap == b.seg_cap && a.tile_seg == b.tile_seg && a.tile_l == b.tile_l && a.tile_r == b.tile_r &&
+           a.stops == b.stops &&
            a.tile_cap == b.tile_cap && a.leaf == b.leaf && a.heap == b.heap && a.leaf_cap == b.leaf_cap &&
            a.local == b.local && a.equal == b.equal && a.counters == b.counters;
 }

@@ -20,6 +20,8 @@ struct SortScratch {
     uint32_t* tile_seg;        // tile -> segment
     uint32_t* tile_l;          // L-stop count per tile, then its exclusive offset
     uint32_t* tile_r;
+    uint32_t* stops;           // per tile: its keys' L-stop bits, then their R-stop bits
+                               // (kSortTile / 32 words each), written by the count pass
     uint32_t tile_cap;
     uint32_t* leaf;            // leaf ranges (first, last)
     uint32_t* heap;            // heap-sorted ranges
