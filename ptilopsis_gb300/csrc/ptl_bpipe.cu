@@ -825,7 +825,7 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
         uint32_t* hfl = reinterpret_cast<uint32_t*>(h_small.at<uint8_t>(small_meta_off));
         BP_CU(cudaMemcpyAsync(hfl, flags.p, B * 16, cudaMemcpyDeviceToHost, s));
         BP_CU(collect_errors());
-        std::vector<uint32_t> lane0_list, serial_list, active_list;
+        std::vector<uint32_t> lane0_list, serial_list, active_list, wide_list;
         std::vector<uint8_t> lane0(B, 0);
         std::vector<uint64_t> nfree(B, 0);
         uint32_t max_g0 = 1;
@@ -838,6 +838,10 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
                 continue;
             }
             if (hfl[4 * p + 2]) hp[p].defpos = nullptr;  // a register with two definitions: hash row 0
+            if (g0 > kRaClusterMin && ra_cluster_fits(static_cast<uint32_t>(g0))) {
+                wide_list.push_back(static_cast<uint32_t>(p));  // its own launches, on a cluster
+                continue;
+            }
             lane0[p] = 1;
             lane0_list.push_back(static_cast<uint32_t>(p));
             nfree[p] = F[p] - g0;
@@ -868,6 +872,13 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
                              ra_items, max_g0, ra_sync.at<uint32_t>(), s, ra_share));
         const uint32_t* d_serial = upload_list(1, serial_list);
         batch_serial(progs.at<Prog>(), d_serial, static_cast<uint32_t>(serial_list.size()), s);
+        for (const uint32_t p : wide_list) {
+            Prog Pfree = hp[p];
+            Pfree.defpos = nullptr;  // the independent functions never need definition positions
+            bool launched = false;
+            BP_CU(launch_ra_wide(hp[p], Pfree, static_cast<uint32_t>((F[p] + 7) / 8), s, &launched));
+            if (!launched) return cuda_fail(cudaErrorLaunchFailure, "lane-0 cluster pass");
+        }
         const uint32_t t_w_sp = tiles(13, W, elem_tile);
         batch_stage(BatchStage::Spill, bl(13), t_w_sp, nullptr);
         const uint32_t st_wb8 = tiles(9, wb8, batch_scan_tile());

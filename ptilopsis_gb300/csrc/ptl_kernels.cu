@@ -2,6 +2,7 @@
 // ptl_sort.cuh; this file holds the launch shapes, the cross-thread primitives (scans,
 // the depth-order rounds, the lock-step register allocator of lane-0 functions) and
 // their bounded waits.
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -1407,6 +1408,167 @@ __global__ void __launch_bounds__(1024) k_ra_steps(Prog P, uint32_t S, uint32_t 
     ra_lane0_block<Q>(P, S, K, chunks, smem);
 }
 
+// ------------------------------------------------------- the lane-0 pass on a cluster
+// A program with more lane-0 groups than one block runs at one slot per thread (above
+// 1,024) spreads its slots over the CTAs of a thread-block cluster: one per thread (Q
+// per thread above 8 x 512).  Row 0 and the step state (Ra2Shared) live in CTA 0's
+// shared memory, which every CTA reaches through distributed shared memory; each CTA
+// keeps its own slots' step records and symbol caches, which the row-0 phases (CTA 0,
+// one thread per physical register) read and mark remotely.  Cluster barriers take the
+// place of the block's.  A barrier that ORs a flag adds to a word in CTA 0: three words
+// in rotation, the one the next such barrier uses cleared before this one (its last
+// readers passed the barrier in between).  The independent functions ran before, so
+// every trigger record is complete and nothing waits.
+namespace cg = cooperative_groups;
+constexpr uint32_t kRaClusterThreads = 512;
+constexpr uint32_t kRaClusterMax = 8;  // the portable cluster size
+
+struct ClusterSlots {
+    uint32_t* cur;  // this CTA's records and caches: the same offsets in every CTA
+    uint32_t* tag;
+    uint32_t* val;
+    uint32_t K;
+    uint32_t per_cta;  // slots per CTA: group j is slot j % per_cta of CTA j / per_cta
+    __device__ const uint32_t* rec(uint32_t slot) const {
+        return cg::this_cluster().map_shared_rank(cur, slot / per_cta) + 4u * (slot % per_cta);
+    }
+    __device__ void mark(const Prog& P, uint32_t owner, uint32_t v) const {
+        P.symswp[v - 64u] = 0xFFFFFFFFu;
+        if (owner == 0xFFFFFFFFu) return;
+        const uint32_t r = owner / per_cta, e = (owner % per_cta) * K + ((v - 64u) & (K - 1u));
+        const uint32_t* t = cg::this_cluster().map_shared_rank(tag, r);
+        uint32_t* x = cg::this_cluster().map_shared_rank(val, r);
+        if (t[e] == v) x[e] |= 0x100u;
+    }
+};
+
+template <int Q>
+__global__ void __launch_bounds__(kRaClusterThreads, 1)
+    k_ra_lane0_cluster(Prog P, uint32_t S, uint32_t K, uint32_t per_cta) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ uint32_t s_s0, s_or[3];
+    cg::cluster_group cl = cg::this_cluster();
+    const uint32_t rank = cl.block_rank(), tid = threadIdx.x, T = blockDim.x;
+    const uint32_t G0 = (P.F + 7u) / 8u;
+    uint32_t* cur = reinterpret_cast<uint32_t*>(smem + sizeof(Ra2Shared));
+    uint32_t* ctag = cur + 4u * per_cta;
+    uint32_t* cval = ctag + per_cta * K;
+    const SymCache c{ctag, cval, K};  // this CTA's slots, by local index
+    const ClusterSlots cs{cur, ctag, cval, K, per_cta};
+    const bool row = rank == 0 && tid < 64u;  // a row-0 thread (T >= 64)
+    const bool hashed = P.defpos == nullptr;
+    if (tid == 0) {
+        s_s0 = 0;
+        s_or[0] = s_or[1] = s_or[2] = 0;
+    }
+    cl.sync();  // every CTA has started (its shared memory exists) before remote accesses
+    Ra2Shared& sh = *cl.map_shared_rank(reinterpret_cast<Ra2Shared*>(smem), 0);
+    uint32_t* s0p = cl.map_shared_rank(&s_s0, 0);
+    uint32_t* orp = cl.map_shared_rank(s_or, 0);
+    uint32_t nbar = 0;  // OR barriers so far (the same count in every thread)
+    auto cluster_or = [&](bool v) -> bool {
+        const uint32_t k = nbar % 3u;
+        if (rank == 0 && tid == 0) orp[(k + 1u) % 3u] = 0;
+        if (__any_sync(0xFFFFFFFFu, v) && (tid & 31u) == 0) atomicOr(&orp[k], 1u);
+        cl.sync();
+        ++nbar;
+        return *reinterpret_cast<volatile uint32_t*>(&orp[k]) != 0;
+    };
+    Ra2Slot L[Q];
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        const uint32_t l = tid + static_cast<uint32_t>(q) * T;
+        L[q].act = false;
+        L[q].have_next = false;
+        if (l < per_cta && rank * per_cta + l < G0) {
+            ra2_slot_init(P, c, L[q], l, rank * per_cta + l);
+            atomicMax(s0p, ra2_lane0_size(L[q]));
+        }
+    }
+    if (row) {
+        sh.R0[tid] = 0xFFFFFFFFu;
+        sh.R0own[tid] = 0xFFFFFFFFu;
+    }
+    if (rank == 0) {
+        for (uint32_t k = tid; k < kSnapHash; k += T) {
+            sh.hkey[0][k] = sh.hkey[1][k] = 0;
+            sh.hmask[0][k] = sh.hmask[1][k] = 0;
+        }
+    }
+    cl.sync();
+    uint32_t tmin = 0xFFFFFFFFu, tmax = 0;  // a row-0 thread's trigger records, one step ahead
+    if (row && S > 0) {
+        ra2_begin_p(sh, 0, tid, __ldcg(&P.trig_min[tid]), __ldcg(&P.trig_max[tid]), hashed);
+        if (S > 1) {
+            tmin = __ldcg(&P.trig_min[64u + tid]);
+            tmax = __ldcg(&P.trig_max[64u + tid]);
+        }
+    }
+    cl.sync();
+    const uint32_t s0 = min(*reinterpret_cast<volatile uint32_t*>(s0p), S);
+    // the block's phases per step (ra_lane0_block), with cluster barriers
+    for (uint32_t i = 0; i < s0; ++i) {
+        bool in_row0 = false;
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+            const uint32_t l = tid + static_cast<uint32_t>(q) * T;
+            if (l < per_cta && rank * per_cta + l < G0) {
+                ra2_load(P, L[q], i, cur + 4u * l);
+                in_row0 |= ra2_compute0(P, c, sh, L[q], l, i);
+            }
+        }
+        const bool any_row0 = cluster_or(in_row0);
+        bool flag = false;
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+            const uint32_t l = tid + static_cast<uint32_t>(q) * T;
+            if (l < per_cta && rank * per_cta + l < G0) {
+                if (any_row0) flag |= ra2_check(sh, L[q]);
+                ra2_apply(P, c, sh, L[q], l, i, cur + 4u * l);
+            }
+        }
+        if (hashed && row) snap_clear_next(sh, i, tid);
+        if (cluster_or(flag)) {
+            if (row) sh.r0grp[tid] = 0;
+            for (uint32_t round = 0;; ++round) {
+#pragma unroll
+                for (int q = 0; q < Q; ++q) {
+                    const uint32_t l = tid + static_cast<uint32_t>(q) * T;
+                    if (l < per_cta && rank * per_cta + l < G0) ra2_round(sh, L[q]);
+                }
+                cl.sync();
+                const bool changed = row && ra2_round_p(sh, tid);
+                if (!cluster_or(changed)) break;
+                if (round > G0 + 2u) {
+                    if (rank == 0 && tid == 0) record_error(P.err, ST_DEVICE_TIMEOUT, W_RA2, i);
+                    break;
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < Q; ++q) {
+                const uint32_t l = tid + static_cast<uint32_t>(q) * T;
+                if (l < per_cta && rank * per_cta + l < G0) ra2_apply(P, c, sh, L[q], l, i, cur + 4u * l);
+            }
+            cl.sync();
+        }
+        if (row) {
+            ra2_end_p_at(P, cs, sh, tid);
+            if (i + 1 < S) {
+                ra2_begin_p(sh, i + 1, tid, tmin, tmax, hashed);
+                if (i + 2 < S) {
+                    tmin = __ldcg(&P.trig_min[static_cast<size_t>(i + 2) * 64u + tid]);
+                    tmax = __ldcg(&P.trig_max[static_cast<size_t>(i + 2) * 64u + tid]);
+                }
+            }
+        }
+        cl.sync();
+    }
+    // After the last cluster barrier no CTA touches another's shared memory: CTA 0 reads
+    // only its own row 0 (the marks of the tail end the pass; no cache needs them).
+    if (s0 >= S) return;
+    if (row && ra2_tail_hit(P, sh, tid, s0, S)) P.symswp[sh.R0[tid] - 64u] = 0xFFFFFFFFu;
+}
+
 // flags[1]: functions share symbols; flags[2]: a lane-0 virtual register has two
 // definitions.  stamp counts the definitions (zeroed before).
 __global__ void k_ra_cross(Prog P) {
@@ -1849,7 +2011,77 @@ cudaError_t launch_ra_steps_q(const Prog& P0, const Prog& Pfree, uint32_t G0, ui
     return cudaGetLastError();
 }
 
+// The independent functions, then the lane-0 pass on a cluster of C CTAs
+// (k_ra_lane0_cluster) -- when the device can place such a cluster; *launched tells
+// (nothing is launched otherwise; with dry set, nothing is launched either way).
+template <int Q>
+cudaError_t launch_ra_cluster_q(const Prog& P0, const Prog& Pfree, uint32_t G0, cudaStream_t s, bool* launched,
+                                bool dry = false) {
+    *launched = false;
+    const uint32_t C = std::min(kRaClusterMax, (G0 + kRaClusterThreads * Q - 1u) / (kRaClusterThreads * Q));
+    const uint32_t per_cta = (G0 + C - 1u) / C;
+    const uint32_t T = std::max(64u, ((per_cta + Q - 1u) / Q + 31u) & ~31u);
+    constexpr size_t kBudget = 160u * 1024u;
+    const size_t fixed = sizeof(Ra2Shared) + 16ull * per_cta;
+    uint32_t K = 64;
+    while (K > 1 && fixed + static_cast<size_t>(per_cta) * K * 8u > kBudget) K >>= 1;
+    const size_t smem = fixed + static_cast<size_t>(per_cta) * K * 8u + 16;
+    const void* fn = reinterpret_cast<const void*>(k_ra_lane0_cluster<Q>);
+    cudaError_t ce = allow_dynamic_smem(fn, smem);
+    if (ce != cudaSuccess) return ce;
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(C);
+    cfg.blockDim = dim3(T);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = C;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    int clusters = 0;
+    if (cudaOccupancyMaxActiveClusters(&clusters, fn, &cfg) != cudaSuccess || clusters < 1) {
+        cudaGetLastError();  // not placeable here: the caller takes the one-block pass
+        return cudaSuccess;
+    }
+    if (dry) {
+        *launched = true;
+        return cudaSuccess;
+    }
+    const uint32_t free_fns = P0.F - G0;
+    if (free_fns) {
+        g_launches++;
+        k_ra_free_cached<<<(free_fns + kRaFreeThreads - 1) / kRaFreeThreads, kRaFreeThreads, 0, s>>>(Pfree);
+    }
+    g_launches++;
+    ce = cudaLaunchKernelEx(&cfg, k_ra_lane0_cluster<Q>, P0, P0.S, K, per_cta);
+    *launched = true;
+    return ce;
+}
+
+cudaError_t launch_ra_wide(const Prog& P0, const Prog& Pfree, uint32_t G0, cudaStream_t s, bool* launched) {
+    *launched = false;
+    if (G0 <= kRaClusterMin || G0 > 2u * kRaClusterThreads * kRaClusterMax) return cudaSuccess;
+    return G0 <= kRaClusterThreads * kRaClusterMax ? launch_ra_cluster_q<1>(P0, Pfree, G0, s, launched)
+                                                   : launch_ra_cluster_q<2>(P0, Pfree, G0, s, launched);
+}
+
+bool ra_cluster_fits(uint32_t G0) {
+    if (G0 <= kRaClusterMin || G0 > 2u * kRaClusterThreads * kRaClusterMax) return false;
+    Prog none{};
+    bool fits = false;
+    const cudaError_t ce = G0 <= kRaClusterThreads * kRaClusterMax
+                               ? launch_ra_cluster_q<1>(none, none, G0, nullptr, &fits, true)
+                               : launch_ra_cluster_q<2>(none, none, G0, nullptr, &fits, true);
+    return ce == cudaSuccess && fits;
+}
+
 cudaError_t launch_ra_steps(const Prog& P0, const Prog& Pfree, uint32_t G0, cudaStream_t s) {
+    bool launched = false;
+    const cudaError_t ce = launch_ra_wide(P0, Pfree, G0, s, &launched);
+    if (ce != cudaSuccess || launched) return ce;
     const uint32_t T = G0 <= 1024u ? std::max(32u, (G0 + 31u) & ~31u) : 1024u;
     const uint32_t Q = (G0 + T - 1u) / T;
     switch (Q) {

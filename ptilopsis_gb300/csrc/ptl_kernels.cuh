@@ -56,6 +56,14 @@ void launch_functab(const Prog& P, uint32_t* meta, cudaStream_t s);
 void launch_gen(const Prog& P, cudaStream_t s);
 cudaError_t run_optimize(const Prog& P, cudaStream_t s, uint32_t* sweeps_out);
 cudaError_t run_regalloc_steps(const Prog& P, cudaStream_t s, bool* serial_out, bool row0_hash);
+// Lane-0 passes too wide for one block: programs with more than kRaClusterMin lane-0
+// groups (at most 8,192) run theirs on a thread-block cluster when the device can place
+// it.  ra_cluster_fits tells whether it can; launch_ra_wide launches the program's
+// independent functions (Pfree: no definition positions), then the cluster pass (P0),
+// and sets *launched, or launches nothing.
+constexpr uint32_t kRaClusterMin = 1024;
+bool ra_cluster_fits(uint32_t G0);
+cudaError_t launch_ra_wide(const Prog& P0, const Prog& Pfree, uint32_t G0, cudaStream_t s, bool* launched);
 void launch_regalloc_count_scan(const Prog& P, const ScanScratch& sc, cudaStream_t s);
 void launch_regalloc_emit(const Prog& P, cudaStream_t s);
 void launch_fixjumps_scan(const Prog& P, const ScanScratch& sc, cudaStream_t s);

@@ -385,27 +385,41 @@ PTL_HD void ra2_apply(const Prog& P, const SymCache& c, Ra2Shared& sh, Ra2Slot& 
     if (S.r2r != S.rdr && s32(S.r2r) >= 0 && S.r2r < 64u) at_max_u32(&sh.r0grp[S.r2r], g1);
 }
 
+// The slots' step records (cur[0..3] of ra2_load / ra2_apply) and symbol caches, seen
+// by slot index (== group index) from the row-0 phases.  One block holds them all; a
+// thread-block cluster spreads them over its CTAs (k_ra_lane0_cluster has its own view).
+struct BlockSlots {
+    const uint32_t* cur;
+    SymCache c;
+    PTL_HD const uint32_t* rec(uint32_t slot) const { return cur + 4u * slot; }
+    PTL_HD void mark(const Prog& P, uint32_t owner, uint32_t v) const { sym_mark(P, c, owner, v); }
+};
+
 // Step end for row-0 position p: marks on symbols their owner did not update this step,
-// then row 0 takes the highest group's write.  cur[4*slot..] are the slots' records
-// (slot index == group index).
-PTL_HD void ra2_end_p(const Prog& P, const SymCache& c, Ra2Shared& sh, uint32_t p, const uint32_t* cur) {
+// then row 0 takes the highest group's write.
+template <class Slots>
+PTL_HD void ra2_end_p_at(const Prog& P, const Slots& sl, Ra2Shared& sh, uint32_t p) {
     const bool triggered = sh.omin[p] != 0xFFFFFFFFu || sh.lcur[p] != 0xFFFFFFFFu;
     const uint32_t v = sh.snap[p];
     if (triggered && s32(v - 64u) >= 0) {
         const uint32_t own = sh.snapown[p];
         bool updated = false;
         if (own != 0xFFFFFFFFu) {
-            const uint32_t* u = cur + 4u * own;
+            const uint32_t* u = sl.rec(own);
             updated = (s32(u[0]) > 63 && u[0] == v) || (s32(u[1]) > 63 && u[1] == v) || (s32(u[2]) > 63 && u[2] == v);
         }
-        if (!updated) sym_mark(P, c, own, v);
+        if (!updated) sl.mark(P, own, v);
     }
     const uint32_t g = sh.r0grp[p];
     if (g != 0) {
-        const uint32_t* w = cur + 4u * (g - 1u);
+        const uint32_t* w = sl.rec(g - 1u);
         sh.R0[p] = (w[0] != 0 && w[3] == p) ? w[0] : 0xFFFFFFFFu;
         sh.R0own[p] = g - 1u;
     }
+}
+// cur[4*slot..] are the slots' records (slot index == group index).
+PTL_HD void ra2_end_p(const Prog& P, const SymCache& c, Ra2Shared& sh, uint32_t p, const uint32_t* cur) {
+    ra2_end_p_at(P, BlockSlots{cur, c}, sh, p);
 }
 
 // ---------------------------------------------------------------- the tail of the pass
@@ -424,18 +438,21 @@ PTL_HD uint32_t ld_records(const uint32_t* p) {
 #endif
 }
 
-// Position p after step s0-1: its symbol is marked when any step in [s0, S) has another
-// function's trigger record there.
-PTL_HD void ra2_tail_p(const Prog& P, const SymCache& c, const Ra2Shared& sh, uint32_t p, uint32_t s0, uint32_t S) {
+// Position p after step s0-1: whether its symbol is marked in a step of [s0, S), i.e.
+// another function has a trigger record there.
+PTL_HD bool ra2_tail_hit(const Prog& P, const Ra2Shared& sh, uint32_t p, uint32_t s0, uint32_t S) {
     const uint32_t v = sh.R0[p];
-    if (s32(v - 64u) < 0) return;
+    if (s32(v - 64u) < 0) return false;
     bool hit = false;
     for (uint32_t i = s0; i < S && !hit; i += 8) {
 #pragma unroll
         for (uint32_t k = 0; k < 8; ++k)
             if (i + k < S) hit |= ld_records(&P.trig_min[static_cast<size_t>(i + k) * 64u + p]) != 0xFFFFFFFFu;
     }
-    if (hit) sym_mark(P, c, sh.R0own[p], v);
+    return hit;
+}
+PTL_HD void ra2_tail_p(const Prog& P, const SymCache& c, const Ra2Shared& sh, uint32_t p, uint32_t s0, uint32_t S) {
+    if (ra2_tail_hit(P, sh, p, s0, S)) sym_mark(P, c, sh.R0own[p], sh.R0[p]);
 }
 
 }  // namespace ptl

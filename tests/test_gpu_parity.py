@@ -89,6 +89,34 @@ def test_gpu_many_functions(built_cuda):
                                                sigma=1.0, max_nesting=8)))
 
 
+@pytest.mark.parametrize("n_functions", [9000, 32768, 33000])
+def test_gpu_cluster_lane0_pass(built_cuda, n_functions):
+    """More than 1,024 lane-0 groups: the lane-0 pass runs on a thread-block cluster
+    (one slot per thread up to 4,096 groups -- 32,768 functions fill 8 CTAs of 512 --
+    two per thread above).  Plain pipeline with both row-0 lookups, and the batched
+    pipeline with a small program beside it, all against the oracle."""
+    from oracle import portbind
+    from ptilopsis_gb300 import RvGenerator
+    from ptilopsis_gb300.batch import BatchCompiler
+    from ptilopsis_gb300.synth import SynthParams, generate
+    tree = generate(SynthParams(seed=0x50544C60 + n_functions, n_functions=n_functions, median_fn_nodes=40.0,
+                                sigma=1.0, max_nesting=6, spill_frac=0.25))
+    small = generate(SynthParams(seed=0x50544C44))
+    ref = portbind.compile_ast(tree_to_ast(tree))
+    ref_small = portbind.compile_ast(tree_to_ast(small))
+    with RvGenerator(tree) as gen:
+        gen.process()
+        np.testing.assert_array_equal(gen.get_instructions(), ref.words)
+        np.testing.assert_array_equal(gen.function_table()["starts"], ref.bufs["fn_start"])
+        gen.process(row0_hash=True)
+        np.testing.assert_array_equal(gen.get_instructions(), ref.words)
+    with BatchCompiler(workers=8) as b:
+        b.compile([small, tree])
+        np.testing.assert_array_equal(b.result(0).words, ref_small.words)
+        np.testing.assert_array_equal(b.result(1).words, ref.words)
+        np.testing.assert_array_equal(b.result(1).table["starts"], ref.bufs["fn_start"])
+
+
 def test_gpu_float_heavy_deep_expressions(built_cuda):
     from ptilopsis_gb300.synth import config_params, generate
     assert_matches_oracle(generate(config_params("c2", scale=64 / 32768)))
