@@ -833,7 +833,7 @@ def main():
     ap.add_argument("--serve-requests", type=int, default=1000, help="distinct serving requests (the pool)")
     ap.add_argument("--serve-seconds", type=float, default=5.0, help="arrival window per rate")
     ap.add_argument("--serve-drain", type=float, default=10.0, help="seconds after the window before the rest is dropped")
-    ap.add_argument("--serve-slots", type=int, default=2)
+    ap.add_argument("--serve-slots", type=int, default=3, help="server lanes: slots // 2 for small requests, the rest large")
     ap.add_argument("--serve-rates", type=float, nargs="+", default=[1000.0, 10000.0, 50000.0])
     args = ap.parse_args()
     if args.impl == "reference":

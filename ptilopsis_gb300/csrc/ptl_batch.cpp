@@ -210,6 +210,8 @@ struct ptl_server {
         return t;
     }
     uint64_t max_batch_nodes = 64ull << 20;
+    static constexpr size_t kCopyThreads = 6;                 // result copies of one batch
+    static constexpr uint64_t kCopyWordsPerThread = 4u << 20;  // (16 MB of words a thread at least)
     static constexpr size_t kLookAhead = 4096;  // queued requests examined per batch formed
     // Requests below small_nodes are "small"; lanes w < small_lanes take only those, so a
     // small request never waits behind a large one whose register allocation chain sets a
@@ -317,22 +319,41 @@ struct ptl_server {
             }
             const ptl_status st = pipes[w]->compile(views.data(), views.size(), res);
             uint64_t held = pipes[w]->device_bytes();
-            for (size_t k = 0; k < batch.size(); ++k) {
+            // The results leave the pipeline's output buffers before the lane's next compile
+            // overwrites them; a large batch's (hundreds of MB) on several threads, since
+            // the lane takes no new batch meanwhile.
+            auto copy_out = [&](size_t k) {
                 Result& out = batch[k]->result;
                 if (st != PTL_OK) {
                     out.status = st;
                     const char* why = pipes[w]->last_error();
                     out.error = why ? why : "";
-                    continue;
+                    return;
                 }
                 const ptl::BatchResult& r = res[k];
                 out.status = r.status;
-                if (r.status != PTL_OK) continue;
+                if (r.status != PTL_OK) return;
                 out.words.assign(r.words, r.words + r.count);
                 out.starts.assign(r.starts, r.starts + r.functions);
                 out.ends.assign(r.ends, r.ends + r.functions);
                 out.sizes.assign(r.sizes, r.sizes + r.functions);
                 out.ids.assign(r.ids, r.ids + r.functions);
+            };
+            uint64_t words = 0;
+            if (st == PTL_OK)
+                for (size_t k = 0; k < batch.size(); ++k) words += res[k].status == PTL_OK ? res[k].count : 0;
+            const size_t helpers = std::min<size_t>({kCopyThreads - 1, batch.size() - 1, words / kCopyWordsPerThread});
+            if (helpers == 0) {
+                for (size_t k = 0; k < batch.size(); ++k) copy_out(k);
+            } else {
+                std::atomic<size_t> next{0};
+                auto drain = [&] {
+                    for (size_t k = next.fetch_add(1); k < batch.size(); k = next.fetch_add(1)) copy_out(k);
+                };
+                std::vector<std::thread> th;
+                for (size_t h = 0; h < helpers; ++h) th.emplace_back(drain);
+                drain();
+                for (auto& t : th) t.join();
             }
             bool give_back = false;
             {
