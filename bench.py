@@ -634,6 +634,39 @@ def run_batched(args):
     plain = {"value": sn / plain_dev, "e2e_value": sn / plain_wall, "unit": UNIT, "programs": len(sample),
              "nodes": sn, "sample": f"first {len(sample)} programs of the workload, one generator, one at a time",
              "stage_ms": {k: round(float(v) / 1e6, 3) for k, v in zip(STAGES, plain_stage)}}
+    # the same programs through 16 generators on 16 host threads at once (each its own
+    # stream; host arrays in and out): what a caller compiling many programs through the
+    # one-program API gets
+    n_conc = 16
+    gens = [RvGenerator(sample[0], device=local) for _ in range(min(n_conc, len(sample)))]
+    conc_words = [None] * len(sample)
+
+    def conc_worker(g, ks):
+        for k in ks:
+            g.upload(sample[k])
+            g.process()
+            conc_words[k] = g.get_instructions()
+
+    import threading
+    largest = max(range(len(sample)), key=lambda k: sample[k].n)
+    for g in gens:  # arenas sized by the largest program, as a long-running caller's would be
+        g.upload(sample[largest])
+        g.process()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ths = [threading.Thread(target=conc_worker, args=(g, range(j, len(sample), len(gens)))) for j, g in enumerate(gens)]
+    for t in ths:
+        t.start()
+    for t in ths:
+        t.join()
+    conc_wall = time.perf_counter() - t0
+    for g in gens:
+        g.close()
+    plain["concurrent_generators"] = {
+        "value": sn / conc_wall, "unit": UNIT, "generators": len(gens), "host_threads": len(gens),
+        "sample": "the same programs, host arrays in and out, generator j taking programs j, j+16, ...; "
+                  "each generator first compiled the largest of them (arenas sized)",
+        "bit_exact_vs_one_at_a_time": all(np.array_equal(conc_words[k], plain_words[k]) for k in range(len(sample)))}
     same_as_plain = all(np.array_equal(bc.words(k), plain_words[k]) for k in range(len(sample)))
     if rank == 0 and not args.no_cpu_baseline:
         # what one caller with one program at a time gets on the CPU: the oracle's
@@ -642,6 +675,12 @@ def run_batched(args):
         plain["cpu_one_program_at_a_time"] = {"value": rate1, "unit": UNIT, "cores": 1, "kind": "port",
                                               "seconds": round(dt1, 3),
                                               "plain_over_cpu": plain["value"] / rate1}
+        # beside the concurrent generators: the oracle on every host core over the same programs
+        cores = os.cpu_count() or 1
+        rate_all, dt_all, _ = port_parallel(sample, cores)
+        plain["concurrent_generators"]["cpu_all_cores"] = {
+            "value": rate_all, "unit": UNIT, "cores": cores, "kind": "port", "seconds": round(dt_all, 3),
+            "concurrent_over_cpu": plain["concurrent_generators"]["value"] / rate_all}
     oracle_check, cpu_line = None, None
     if rank == 0 and not args.no_cpu_baseline:
         # the oracle on every program of the batch, on all host cores (outside the timed

@@ -713,15 +713,21 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
         ss.bpos = sbpos.at<uint32_t>();
         ss.seg[0] = seg0.at<SortSeg>();
         ss.seg[1] = seg1.at<SortSeg>();
-        ss.seg_cap = static_cast<uint32_t>(seg_cap);
+        // capacities as allocated: the captured round graph bakes them in, and they change
+        // only when a buffer is reallocated, not with each batch's sizes
+        ss.seg_cap = static_cast<uint32_t>(std::min<uint64_t>(
+            {seg0.bytes / sizeof(SortSeg), seg1.bytes / sizeof(SortSeg), sort_local.bytes / 12, sort_equal.bytes / 8,
+             UINT32_MAX}));
         ss.tile_seg = tile_seg.at<uint32_t>();
         ss.tile_l = tile_l.at<uint32_t>();
         ss.tile_r = tile_r.at<uint32_t>();
         ss.stops = sort_stops.at<uint32_t>();
-        ss.tile_cap = static_cast<uint32_t>(tile_cap);
+        ss.tile_cap = static_cast<uint32_t>(std::min<uint64_t>(
+            {tile_seg.bytes / 4, tile_l.bytes / 4, tile_r.bytes / 4, sort_stops.bytes / (8 * (kSortTile / 32)),
+             UINT32_MAX}));
         ss.leaf = leaf.at<uint32_t>();
         ss.heap = heap.at<uint32_t>();
-        ss.leaf_cap = static_cast<uint32_t>(leaf_cap);
+        ss.leaf_cap = static_cast<uint32_t>(std::min<uint64_t>({leaf.bytes / 8, heap.bytes / 8, UINT32_MAX}));
         ss.counters = counters.at<uint32_t>();
         ss.local = sort_local.at<uint32_t>();
         ss.equal = sort_equal.at<uint32_t>();

@@ -50,6 +50,8 @@ struct DevBuf {
     cudaError_t zero(cudaStream_t s) const { return base ? cudaMemsetAsync(base, 0, (count + kFrontPad + kBackPad) * elem, s) : cudaSuccess; }
     cudaError_t fill(cudaStream_t s, int byte) const { return base ? cudaMemsetAsync(base, byte, (count + kFrontPad + kBackPad) * elem, s) : cudaSuccess; }
     void release() { if (base) cudaFree(base); base = nullptr; bytes = 0; }
+    // elements the allocation holds (at least the last ensure's n)
+    size_t capacity() const { return base ? bytes / elem - kFrontPad - kBackPad : 0; }
 };
 
 const CodeTables& host_tables() {
@@ -298,15 +300,22 @@ cudaError_t sort_scratch(ptl_generator* g, size_t n, SortScratch* ss) {
     ss->bpos = g->sort_bpos.at<uint32_t>();
     ss->seg[0] = g->sort_seg0.at<SortSeg>();
     ss->seg[1] = g->sort_seg1.at<SortSeg>();
-    ss->seg_cap = static_cast<uint32_t>(seg_cap);
+    // The capacities are what the allocations hold, so that they (and the captured round
+    // graph that bakes them in) change only when a buffer is reallocated, not with n.
+    const size_t seg_room = std::min({g->sort_seg0.capacity(), g->sort_seg1.capacity(), g->sort_local.capacity() / 3,
+                                      g->sort_equal.capacity() / 2});
+    const size_t tile_room = std::min({g->sort_tile_seg.capacity(), g->sort_tile_l.capacity(),
+                                       g->sort_tile_r.capacity(), g->sort_stops.capacity() / (2 * (kSortTile / 32))});
+    const size_t leaf_room = std::min(g->sort_leaf.capacity(), g->sort_heap.capacity()) / 2;
+    ss->seg_cap = static_cast<uint32_t>(std::min<size_t>(seg_room, UINT32_MAX));
     ss->tile_seg = g->sort_tile_seg.at<uint32_t>();
     ss->tile_l = g->sort_tile_l.at<uint32_t>();
     ss->tile_r = g->sort_tile_r.at<uint32_t>();
     ss->stops = g->sort_stops.at<uint32_t>();
-    ss->tile_cap = static_cast<uint32_t>(tile_cap);
+    ss->tile_cap = static_cast<uint32_t>(std::min<size_t>(tile_room, UINT32_MAX));
     ss->leaf = g->sort_leaf.at<uint32_t>();
     ss->heap = g->sort_heap.at<uint32_t>();
-    ss->leaf_cap = static_cast<uint32_t>(leaf_cap);
+    ss->leaf_cap = static_cast<uint32_t>(std::min<size_t>(leaf_room, UINT32_MAX));
     ss->counters = g->sort_counters.at<uint32_t>();
     ss->local = g->sort_local.at<uint32_t>();
     ss->equal = g->sort_equal.at<uint32_t>();
