@@ -20,12 +20,15 @@ namespace {
 constexpr size_t kFrontPad = 16;  // elements before index 0 (the reference reads [-1])
 constexpr size_t kBackPad = 80;   // elements after the last 8-lane block
 
-// A device buffer with the reference's padding around it.
+// A device buffer with the reference's padding around it.  Allocated and freed in the
+// order of its generator's stream (cudaMallocAsync / cudaFreeAsync): growing or freeing
+// it does not wait for the whole device, so generators on other threads keep running.
 struct DevBuf {
     void* base = nullptr;
     size_t bytes = 0;
     size_t elem = 4;
     size_t count = 0;  // logical capacity in elements (without pads)
+    cudaStream_t s = nullptr;  // the owner's stream
 
     template <typename T>
     T* at() const { return base ? reinterpret_cast<T*>(static_cast<char*>(base) + kFrontPad * elem) : nullptr; }
@@ -36,11 +39,11 @@ struct DevBuf {
             count = n;
             return cudaSuccess;
         }
-        if (base) cudaFree(base);
+        if (base) cudaFreeAsync(base, s);
         base = nullptr;
         bytes = 0;
         const size_t grow = need + need / 4;  // room to grow without reallocating
-        cudaError_t e = cudaMalloc(&base, grow);
+        cudaError_t e = cudaMallocAsync(&base, grow, s);
         if (e != cudaSuccess) { base = nullptr; return e; }
         bytes = grow;
         elem = esize;
@@ -49,7 +52,7 @@ struct DevBuf {
     }
     cudaError_t zero(cudaStream_t s) const { return base ? cudaMemsetAsync(base, 0, (count + kFrontPad + kBackPad) * elem, s) : cudaSuccess; }
     cudaError_t fill(cudaStream_t s, int byte) const { return base ? cudaMemsetAsync(base, byte, (count + kFrontPad + kBackPad) * elem, s) : cudaSuccess; }
-    void release() { if (base) cudaFree(base); base = nullptr; bytes = 0; }
+    void release() { if (base) cudaFreeAsync(base, s); base = nullptr; bytes = 0; }
     // elements the allocation holds (at least the last ensure's n)
     size_t capacity() const { return base ? bytes / elem - kFrontPad - kBackPad : 0; }
 };
@@ -108,6 +111,10 @@ struct ptl_generator {
     ~ptl_generator() {
         for (DevBuf* b : all()) b->release();
         if (stream) cudaStreamDestroy(stream);
+    }
+    // The buffers allocate and free in this generator's stream order (after it exists).
+    void bind_stream() {
+        for (DevBuf* b : all()) b->s = stream;
     }
     std::vector<DevBuf*> all() {
         return {&in_type, &in_rtype, &in_parent, &in_depth, &in_child, &in_data, &nt, &rt, &nd1, &nd,
@@ -596,6 +603,7 @@ ptl_status ptl_generator_create(const ptl_ast_view* tree, int device, ptl_genera
     const DeviceScope on_device(device);
     cudaError_t e = on_device.err;
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) g->bind_stream();
     if (e == cudaSuccess) e = upload_inputs(g, tree);
     if (e == cudaSuccess) e = g->tables.ensure(sizeof(CodeTables), 1);
     if (e == cudaSuccess) e = cudaMemcpyAsync(g->tables.at<char>(), &host_tables(), sizeof(CodeTables), cudaMemcpyHostToDevice, g->stream);
@@ -712,6 +720,7 @@ ptl_status ptl_depth_order(const int32_t* keys, size_t n, uint32_t* pos, int dev
     g.device = device;
     g.n = n;
     cudaError_t e = cudaStreamCreateWithFlags(&g.stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) g.bind_stream();
     if (e == cudaSuccess) e = g.dep.ensure(r8(n), 4);
     if (e == cudaSuccess) e = g.pos.ensure(r8(n), 4);
     if (e == cudaSuccess) e = g.errw.ensure(1, sizeof(ErrorWord));
