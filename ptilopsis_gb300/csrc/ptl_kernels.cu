@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <atomic>
 #include <map>
 #include <mutex>
@@ -2061,15 +2062,25 @@ cudaError_t launch_ra_cluster_q(const Prog& P0, const Prog& Pfree, uint32_t G0, 
     return ce;
 }
 
+// PTL_RA_ONE_BLOCK=1 in the environment keeps every lane-0 pass in one block (the pass a
+// device that cannot place the cluster takes), so that both paths can be compared.
+bool ra_cluster_disabled() {
+    static const bool off = [] {
+        const char* v = std::getenv("PTL_RA_ONE_BLOCK");
+        return v && v[0] == '1';
+    }();
+    return off;
+}
+
 cudaError_t launch_ra_wide(const Prog& P0, const Prog& Pfree, uint32_t G0, cudaStream_t s, bool* launched) {
     *launched = false;
-    if (G0 <= kRaClusterMin || G0 > 2u * kRaClusterThreads * kRaClusterMax) return cudaSuccess;
+    if (G0 <= kRaClusterMin || G0 > 2u * kRaClusterThreads * kRaClusterMax || ra_cluster_disabled()) return cudaSuccess;
     return G0 <= kRaClusterThreads * kRaClusterMax ? launch_ra_cluster_q<1>(P0, Pfree, G0, s, launched)
                                                    : launch_ra_cluster_q<2>(P0, Pfree, G0, s, launched);
 }
 
 bool ra_cluster_fits(uint32_t G0) {
-    if (G0 <= kRaClusterMin || G0 > 2u * kRaClusterThreads * kRaClusterMax) return false;
+    if (G0 <= kRaClusterMin || G0 > 2u * kRaClusterThreads * kRaClusterMax || ra_cluster_disabled()) return false;
     Prog none{};
     bool fits = false;
     const cudaError_t ce = G0 <= kRaClusterThreads * kRaClusterMax

@@ -117,6 +117,46 @@ def test_gpu_cluster_lane0_pass(built_cuda, n_functions):
         np.testing.assert_array_equal(b.result(1).table["starts"], ref.bufs["fn_start"])
 
 
+def test_gpu_cluster_and_one_block_lane0_passes_agree(built_cuda):
+    """The lane-0 pass of a program with 1,125 lane-0 groups on a cluster (the default)
+    and in one block of 1,024 threads (PTL_RA_ONE_BLOCK=1, the pass a device that cannot
+    place the cluster takes) give the same words, plain and batched.  The environment is
+    read once per process, so the one-block run is a child process."""
+    import json
+    import os
+    import subprocess
+    import sys
+    from ptilopsis_gb300 import RvGenerator
+    from ptilopsis_gb300.synth import SynthParams, generate
+    params = dict(seed=0x50544C60 + 9000, n_functions=9000, median_fn_nodes=40.0, sigma=1.0, max_nesting=6,
+                  spill_frac=0.25)
+    with RvGenerator(generate(SynthParams(**params))) as gen:
+        gen.process()
+        want = gen.get_instructions()
+    code = f"""
+import json, sys, zlib
+sys.path.insert(0, {os.path.dirname(os.path.dirname(os.path.abspath(__file__)))!r})
+from ptilopsis_gb300 import RvGenerator
+from ptilopsis_gb300.batch import BatchCompiler
+from ptilopsis_gb300.synth import SynthParams, generate
+t = generate(SynthParams(**{params!r}))
+with RvGenerator(t) as g:
+    g.process()
+    w = g.get_instructions()
+with BatchCompiler(workers=4) as b:
+    b.compile([t])
+    wb = b.result(0).words
+print(json.dumps([len(w), zlib.crc32(w.tobytes()), len(wb), zlib.crc32(wb.tobytes())]))
+"""
+    env = dict(os.environ, PTL_RA_ONE_BLOCK="1")
+    out = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True, timeout=600)
+    assert out.returncode == 0, out.stderr[-2000:]
+    import zlib
+    n, c, nb, cb = json.loads(out.stdout.strip().splitlines()[-1])
+    assert (n, c) == (len(want), zlib.crc32(want.tobytes())), "plain, one block"
+    assert (nb, cb) == (len(want), zlib.crc32(want.tobytes())), "batched, one block"
+
+
 def test_gpu_float_heavy_deep_expressions(built_cuda):
     from ptilopsis_gb300.synth import config_params, generate
     assert_matches_oracle(generate(config_params("c2", scale=64 / 32768)))
