@@ -209,6 +209,10 @@ ptl_status ptl_batch_tiles(const ptl_batch* batch, uint32_t tiles[2]);
  * launch may take (default 1).  Batches compiled at the same time on other handles of the
  * same device run beside it when it takes less. */
 ptl_status ptl_batch_set_regalloc_share(ptl_batch* batch, double share);
+/* scalar != 0: the following compiles give every program the scalar generator's output
+ * (rv_generator_st, the reference's -s; ptl_generator_create_scalar one program at a
+ * time); 0 (the default): the AVX generator's. */
+ptl_status ptl_batch_set_scalar(ptl_batch* batch, int scalar);
 void ptl_batch_destroy(ptl_batch* batch);
 
 /* ---- AST flattening.  ptl_flatten replaces DepthTree::DepthTree(ASTNode*)

@@ -42,6 +42,7 @@ def _bind(L):
     L.ptl_batch_set_tiles.argtypes = [vp, ctypes.c_uint32, ctypes.c_uint32]
     L.ptl_batch_tiles.argtypes = [vp, ctypes.POINTER(ctypes.c_uint32)]
     L.ptl_batch_set_regalloc_share.argtypes = [vp, ctypes.c_double]
+    L.ptl_batch_set_scalar.argtypes = [vp, ctypes.c_int]
     L.ptl_batch_device_ns.argtypes = [vp]
     L.ptl_batch_device_ns.restype = u64
     L.ptl_batch_depth_sort_ns.argtypes = [vp]
@@ -66,7 +67,7 @@ def _bind(L):
     L.ptl_clock_ns.restype = u64
     for fn in ("ptl_batch_create", "ptl_batch_compile", "ptl_batch_status", "ptl_batch_words", "ptl_batch_stage_ns",
                "ptl_batch_copied_bytes", "ptl_batch_sizes", "ptl_batch_host_ns", "ptl_batch_set_tiles", "ptl_batch_tiles",
-               "ptl_batch_set_regalloc_share",
+               "ptl_batch_set_regalloc_share", "ptl_batch_set_scalar",
                "ptl_batch_function_table", "ptl_server_create", "ptl_server_submit", "ptl_server_submit_flags", "ptl_server_poll",
                "ptl_server_result", "ptl_server_times", "ptl_server_release", "ptl_server_stats", "ptl_server_memory"):
         getattr(L, fn).restype = ctypes.c_int
@@ -159,12 +160,14 @@ class BatchCompiler:
     applies this device's autotuned tile sizes when there are some, None keeps the
     defaults, a pair (element tile, sweep tile) sets them."""
 
-    def __init__(self, device: int = 0, workers: int = 8, tiles="cached"):
+    def __init__(self, device: int = 0, workers: int = 8, tiles="cached", scalar: bool = False):
         self._lib = _bind(lib())
         self._h = ctypes.c_void_p()
         st = self._lib.ptl_batch_create(device, workers, ctypes.byref(self._h))
         if st != 0:
             raise PtlError(st, "ptl_batch_create")
+        if scalar:
+            self.set_scalar(True)
         choice = cached_tiles(device) if isinstance(tiles, str) and tiles == "cached" else tiles
         if choice:
             self.set_tiles(*choice)
@@ -173,6 +176,13 @@ class BatchCompiler:
         st = self._lib.ptl_batch_set_tiles(self._h, elem_tile, sweep_tile)
         if st != 0:
             raise PtlError(st, f"ptl_batch_set_tiles({elem_tile}, {sweep_tile})")
+
+    def set_scalar(self, on: bool) -> None:
+        """True: the following compiles give the scalar generator's output (the
+        reference's -s, RvGenerator(scalar=True) one program at a time)."""
+        st = self._lib.ptl_batch_set_scalar(self._h, 1 if on else 0)
+        if st != 0:
+            raise PtlError(st, "ptl_batch_set_scalar")
 
     def set_regalloc_share(self, share: float) -> None:
         """Part of the device's resident blocks the persistent register-allocation launch

@@ -157,6 +157,12 @@ extern "C" ptl_status ptl_batch_set_regalloc_share(ptl_batch* b, double share) {
     return PTL_OK;
 }
 
+extern "C" ptl_status ptl_batch_set_scalar(ptl_batch* b, int scalar) {
+    if (!b) return PTL_BAD_ARGUMENT;
+    b->pipe->set_scalar(scalar != 0);
+    return PTL_OK;
+}
+
 extern "C" ptl_status ptl_batch_tiles(const ptl_batch* b, uint32_t tiles[2]) {
     if (!b || !tiles) return PTL_BAD_ARGUMENT;
     b->pipe->tiles(tiles);

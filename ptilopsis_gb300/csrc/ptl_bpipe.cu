@@ -141,6 +141,8 @@ public:
     DBuf errw, flags, meta, progs, tabs, lists, changed, sort_err, a_off, dirty, ra_sync;
     DBuf sa, sapos, sbpos, seg0, seg1, tile_seg, tile_l, tile_r, sort_stops, leaf, heap, counters, scan_status,
         scan_counter, sort_local, sort_equal;
+    DBuf s_preserve, s_extra, s_claim, s_sregs, s_ssteps;  // the scalar generator's allocation
+    bool scalar_mode = false;  // rv_generator_st's semantics for the whole batch
     PBuf h_in, h_out, h_fn, h_small, h_gp;
     DBuf d_gp;                 // host-gather parameters (source pointers, offsets, counts)
     bool direct_host = false;  // the device reads pageable host memory coherently
@@ -170,7 +172,8 @@ public:
                 &symswp, &stamp, &spill, &roffs, &owner, &used, &smark, &defpos, &trig_min, &trig_max, &ra_chunks, &ni, &nrd,
                 &nr1, &nr2, &njt, &joffs, &out, &errw, &flags, &meta, &progs, &tabs, &lists, &changed,
                 &sort_err, &a_off, &dirty, &ra_sync, &sa, &sapos, &sbpos, &seg0, &seg1, &tile_seg, &tile_l, &tile_r,
-                &sort_stops, &leaf, &heap, &counters, &scan_status, &scan_counter, &sort_local, &sort_equal};
+                &sort_stops, &leaf, &heap, &counters, &scan_status, &scan_counter, &sort_local, &sort_equal,
+                &s_preserve, &s_extra, &s_claim, &s_sregs, &s_ssteps};
     }
 
     ptl_status cuda_fail(cudaError_t e, const char* what) {
@@ -197,6 +200,10 @@ public:
         d_gp.release();
     }
     void set_regalloc_share(double share) override { ra_share = std::min(1.0, std::max(0.05, share)); }
+    void set_scalar(bool on) override { scalar_mode = on; }
+    ptl_status scalar_regalloc(const std::vector<uint64_t>& F, const std::vector<uint64_t>& W,
+                               const std::vector<uint64_t>& S, const Layout& Lf, const Layout& Lw, uint32_t* hfl,
+                               std::vector<uint32_t>& active_list);
     bool set_tiles(uint32_t e, uint32_t w) override {
         if (!batch_tile_ok(e) || !batch_sweep_tile_ok(w)) return false;
         elem_tile = e;
@@ -307,6 +314,54 @@ public:
     }
 };
 
+// The scalar generator's register allocation (rv_generator.cpp:1213-1335) of every active
+// program: each function on its own, with its preserve mask.  Programs whose functions
+// share symbols take the serial order, one launch each; the others run one warp per
+// function in one launch for the batch, except a program with a function longer than a
+// warp's symbol bytes, which takes the tile form on its own.
+ptl_status Pipeline::scalar_regalloc(const std::vector<uint64_t>& F, const std::vector<uint64_t>& W,
+                                     const std::vector<uint64_t>& S, const Layout& Lf, const Layout& Lw,
+                                     uint32_t* hfl, std::vector<uint32_t>& active_list) {
+    BP_CU(family(Lf, {&s_preserve}, 8));
+    BP_CU(family(Lw, {&s_extra}, 4));
+    for (size_t p = 0; p < B; ++p) {
+        hp[p].s_preserve = s_preserve.at<unsigned long long>(Lf.elem(p));
+        hp[p].s_extra = s_extra.at<uint32_t>(Lw.elem(p));
+    }
+    upload_progs();
+    const uint32_t t_w = tiles(7, W, elem_tile);
+    batch_stage(BatchStage::Cross, bl(7), t_w, nullptr);  // flags[1]: functions share symbols
+    BP_CU(cudaMemcpyAsync(hfl, flags.p, B * 16, cudaMemcpyDeviceToHost, s));
+    BP_CU(collect_errors());
+    std::vector<uint8_t> on_warp(B, 0);
+    std::vector<uint32_t> serial, alone;
+    uint64_t longest = 1, serial_f = 1;
+    for (size_t p = 0; p < B; ++p) {
+        if (!active[p]) continue;
+        active_list.push_back(static_cast<uint32_t>(p));
+        if (hfl[4 * p + 1]) {
+            serial.push_back(static_cast<uint32_t>(p));
+            serial_f = std::max(serial_f, F[p]);
+        } else if (S[p] <= scalar_warp_cap()) {
+            on_warp[p] = 1;
+            longest = std::max(longest, S[p]);
+        } else {
+            alone.push_back(static_cast<uint32_t>(p));
+        }
+    }
+    const uint32_t t_sw = tiles(16, F, scalar_warp_fns(), &on_warp);
+    batch_scalar_ra_warp(bl(16), t_sw, static_cast<uint32_t>((longest + 15) & ~uint64_t(15)));
+    if (!serial.empty()) {  // per program, one after another: they share the scratch
+        BP_CU(s_sregs.ensure(serial_f * 64 * 4));
+        BP_CU(s_ssteps.ensure(serial_f * sizeof(SRaStep)));
+        for (const uint32_t p : serial)
+            launch_scalar_ra_serial(hp[p], s_sregs.at<int32_t>(), s_ssteps.at<SRaStep>(), hp[p].s_preserve, s);
+    }
+    for (const uint32_t p : alone) launch_scalar_ra_free(hp[p], hp[p].s_preserve, s);
+    BP_CU(cudaGetLastError());
+    return PTL_OK;
+}
+
 ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vector<BatchResult>& res) {
     res.assign(count, BatchResult{});
     err_text.clear();
@@ -347,7 +402,7 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
     for (auto& x : hns) x = 0;
 
     // ---- small per-program state and the pinned small area
-    constexpr int kTables = 22, kLists = 4;  // table slots 0..21 are used
+    constexpr int kTables = 23, kLists = 4;  // table slots 0..22 are used
     small_progs_off = static_cast<size_t>(kTables) * (B + 1) * 4;
     small_meta_off = small_progs_off + B * sizeof(Prog);
     small_err_off = small_meta_off + B * 16;
@@ -532,6 +587,7 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
             P.tab.t = tab.at<CodeTables>();
             P.err = errw.at<ErrorWord>(p);
             P.flags = flags.at<uint32_t>(4 * p);
+            P.scalar = scalar_mode ? 1u : 0u;
         }
         upload_progs();
 
@@ -556,7 +612,7 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
             }
         }
         const uint32_t t_nb8 = tiles(1, nb8, elem_tile);
-        batch_stage(BatchStage::Preprocess, bl(1), t_nb8, nullptr);
+        batch_stage(scalar_mode ? BatchStage::PreprocessScalar : BatchStage::Preprocess, bl(1), t_nb8, nullptr);
         BP_CU(cudaEventRecord(ev[1], s));
 
         // ---- isn_cnt
@@ -762,7 +818,7 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
                               sort_err.at<ErrorWord>(), s, &rounds, &sort_graph));
         batch_sort_keys(bl(4), t_n2, sa.at<unsigned long long>(), a_off.at<uint64_t>(), true);
         BP_CU(cudaEventRecord(ev_sort1, s));
-        batch_stage(BatchStage::Gen, bl(4), t_n2, nullptr);
+        batch_stage(scalar_mode ? BatchStage::GenScalar : BatchStage::Gen, bl(4), t_n2, nullptr);
         {
             ErrorWord se{};
             BP_CU(cudaMemcpyAsync(&se, sort_err.p, sizeof(se), cudaMemcpyDeviceToHost, s));
@@ -808,6 +864,12 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
         BP_CU(cudaEventRecord(ev[4], s));
 
         // ---- regalloc
+        std::vector<uint32_t> active_list;
+        uint32_t* hfl = reinterpret_cast<uint32_t*>(h_small.at<uint8_t>(small_meta_off));
+        if (scalar_mode) {
+            const ptl_status sr = scalar_regalloc(F, W, S, Lf, Lw, hfl, active_list);
+            if (sr != PTL_OK) return sr;
+        } else {
         const uint32_t t_f = tiles(6, F, elem_tile);
         batch_stage(BatchStage::InitLifetime, bl(6), t_f, nullptr);
         Layout Lt, Lc;
@@ -828,10 +890,9 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
         upload_progs();
         const uint32_t t_w = tiles(7, W, elem_tile);
         batch_stage(BatchStage::Cross, bl(7), t_w, nullptr);
-        uint32_t* hfl = reinterpret_cast<uint32_t*>(h_small.at<uint8_t>(small_meta_off));
         BP_CU(cudaMemcpyAsync(hfl, flags.p, B * 16, cudaMemcpyDeviceToHost, s));
         BP_CU(collect_errors());
-        std::vector<uint32_t> lane0_list, serial_list, active_list, wide_list;
+        std::vector<uint32_t> lane0_list, serial_list, wide_list;
         std::vector<uint8_t> lane0(B, 0);
         std::vector<uint64_t> nfree(B, 0);
         uint32_t max_g0 = 1;
@@ -885,12 +946,17 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
             BP_CU(launch_ra_wide(hp[p], Pfree, static_cast<uint32_t>((F[p] + 7) / 8), s, &launched));
             if (!launched) return cuda_fail(cudaErrorLaunchFailure, "lane-0 cluster pass");
         }
+        }  // the AVX generator's allocation
         const uint32_t t_w_sp = tiles(13, W, elem_tile);
         batch_stage(BatchStage::Spill, bl(13), t_w_sp, nullptr);
+        if (scalar_mode) {  // preserve counts at each function's two preserve positions
+            const uint32_t t_fp = tiles(6, F, elem_tile);
+            batch_stage(BatchStage::SPreserveCounts, bl(6), t_fp, nullptr);
+        }
         const uint32_t st_wb8 = tiles(9, wb8, batch_scan_tile());
         BP_CU(scan_status.ensure((static_cast<size_t>(st_wb8) + 8) * 8));
         sc = ScanScratch{scan_status.at<unsigned long long>(), scan_counter.at<uint32_t>(), st_wb8 + 8};
-        batch_scan(BatchScan::RaCount, bl(9), st_wb8, sc, nullptr);
+        batch_scan(scalar_mode ? BatchScan::SRaCount : BatchScan::RaCount, bl(9), st_wb8, sc, nullptr);
         const uint32_t* d_active = upload_list(2, active_list);
         batch_sizes(false, progs.at<Prog>(), d_active, static_cast<uint32_t>(active_list.size()), meta.at<uint32_t>(), s);
         hm = read_meta();
@@ -906,6 +972,7 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
         L2.build(w2r, active);
         BP_CU(family(L2, {&ni, &nrd, &nr1, &nr2, &njt}, 4));
         BP_CU(family_written(L2, {&joffs}, 4));
+        if (scalar_mode) BP_CU(family(L2, {&s_claim}, 8));  // the frame writes' claims, zeroed
         for (size_t p = 0; p < B; ++p) {
             Prog& P = hp[p];
             P.W2 = static_cast<uint32_t>(W2[p]);
@@ -917,6 +984,7 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
             P.nr2 = nr2.at<uint32_t>(e);
             P.njt = njt.at<uint32_t>(e);
             P.joffs = joffs.at<uint32_t>(e);
+            if (scalar_mode) P.s_claim = s_claim.at<unsigned long long>(e);
         }
         upload_progs();
         {
@@ -926,9 +994,18 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
             batch_guards(ArenaGuard::Words2, bl(21), t_g);
         }
         const uint32_t t_wb8_sc = tiles(14, wb8, elem_tile);
-        batch_stage(BatchStage::Scatter, bl(14), t_wb8_sc, nullptr);
-        const uint32_t t_f2 = tiles(10, F, elem_tile);
-        batch_stage(BatchStage::RaFunctab, bl(10), t_f2, nullptr);
+        batch_stage(scalar_mode ? BatchStage::SScatter : BatchStage::Scatter, bl(14), t_wb8_sc, nullptr);
+        if (scalar_mode) {
+            const uint32_t t_f2 = tiles(10, F, elem_tile);
+            batch_stage(BatchStage::SFunctab, bl(10), t_f2, nullptr);
+            std::vector<uint64_t> f3(B);
+            for (size_t p = 0; p < B; ++p) f3[p] = 3 * F[p];
+            const uint32_t t_f3 = tiles(22, f3, elem_tile);
+            batch_stage(BatchStage::SFrames, bl(22), t_f3, nullptr);
+        } else {
+            const uint32_t t_f2 = tiles(10, F, elem_tile);
+            batch_stage(BatchStage::RaFunctab, bl(10), t_f2, nullptr);
+        }
         BP_CU(cudaEventRecord(ev[5], s));
 
         // ---- fix_jumps (+ postprocess)

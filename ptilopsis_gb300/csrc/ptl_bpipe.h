@@ -48,6 +48,8 @@ public:
     // The part of the device's resident blocks the persistent regalloc launch may take
     // (default 1); less leaves SMs to pipelines on other streams.
     virtual void set_regalloc_share(double share) = 0;
+    // The scalar generator's semantics (rv_generator_st) for the following compiles.
+    virtual void set_scalar(bool on) = 0;
     virtual void tiles(uint32_t out[2]) const = 0;
     // Detail of the last failure.
     virtual const char* last_error() const = 0;

@@ -1628,19 +1628,16 @@ __global__ void __launch_bounds__(kScalarRaThreads) k_s_ra_tiles(Prog P, unsigne
 // back what all wrote without a barrier.  Functions of at most `stride` words.
 constexpr uint32_t kScalarWarpFns = 4;          // functions (warps) per block
 constexpr uint32_t kScalarWarpSymCap = 12288;   // symbol bytes per warp
-__global__ void __launch_bounds__(32 * kScalarWarpFns) k_s_ra_warp(Prog P, unsigned long long* preserve,
-                                                                   uint32_t stride) {
-    extern __shared__ uint8_t s_wsym[];
+// Function f of P by the calling warp; sym: the warp's `stride` symbol bytes.
+__device__ void s_ra_warp_function(const Prog& P, uint32_t f, unsigned long long* preserve, uint32_t stride,
+                                   uint8_t* sym) {
     constexpr unsigned kFull = 0xFFFFFFFFu;
     const uint32_t lane = threadIdx.x & 31u;
-    const uint32_t f = blockIdx.x * kScalarWarpFns + (threadIdx.x >> 5);
-    if (f >= P.F) return;  // the whole warp
     if (!s_ra_function_ok(P, f) || P.fn_size0[f] > stride) {
         if (lane == 0) record_error(P.err, ST_UNSUPPORTED, W_RA1, f);
         return;
     }
     const uint32_t start = P.fn_start0[f], size = P.fn_size0[f];
-    uint8_t* sym = s_wsym + (threadIdx.x >> 5) * stride;
     for (uint32_t k = lane; k < size; k += 32u) sym[k] = 0;
     __syncwarp();
     int32_t rlo = -1, rhi = -1;  // regs[lane], regs[lane + 32]
@@ -1719,6 +1716,27 @@ __global__ void __launch_bounds__(32 * kScalarWarpFns) k_s_ra_warp(Prog P, unsig
         const uint32_t b = sym[k];
         P.symreg[start + k] = b & 0x3Fu;
         P.symswp[start + k] = (b & 0x80u) ? 0xFFFFFFFFu : 0u;
+    }
+}
+__global__ void __launch_bounds__(32 * kScalarWarpFns) k_s_ra_warp(Prog P, unsigned long long* preserve,
+                                                                   uint32_t stride) {
+    extern __shared__ uint8_t s_wsym[];
+    const uint32_t f = blockIdx.x * kScalarWarpFns + (threadIdx.x >> 5);
+    if (f >= P.F) return;  // the whole warp
+    s_ra_warp_function(P, f, preserve, stride, s_wsym + (threadIdx.x >> 5) * stride);
+}
+__device__ __forceinline__ uint32_t batch_program(const uint32_t* off, uint32_t B, uint32_t t);
+// The same for the listed programs of a batch: a tile is kScalarWarpFns functions of one
+// program (off: the per-program tile table over F), one warp each.
+__global__ void __launch_bounds__(32 * kScalarWarpFns) k_batch_s_ra_warp(const Prog* progs, const uint32_t* off,
+                                                                         uint32_t B, uint32_t total, uint32_t stride) {
+    extern __shared__ uint8_t s_wsym[];
+    for (uint32_t t = blockIdx.x; t < total; t += gridDim.x) {
+        const uint32_t p = batch_program(off, B, t);
+        const Prog& P = progs[p];
+        const uint32_t f = (t - off[p]) * kScalarWarpFns + (threadIdx.x >> 5);
+        if (f < P.F) s_ra_warp_function(P, f, P.s_preserve, stride, s_wsym + (threadIdx.x >> 5) * stride);
+        __syncthreads();  // the warps' symbol bytes are reused by the next tile
     }
 }
 
@@ -2324,6 +2342,22 @@ PTL_BATCH_OP(BFunctab, P.fb8, st_functab(P, i))
 PTL_BATCH_OP(BGenProp, P.n, st_gen_prop(P, i))
 PTL_BATCH_OP(BGenClaim, P.n, st_gen_claim(P, i))
 PTL_BATCH_OP(BGenWrite, P.n, st_gen_write(P, i))
+// the scalar generator's stages where they differ (ptl_scalar.cuh)
+PTL_BATCH_OP_V(BSPreLists, false, P.nb8, st_s_pre_lists(P, i))
+PTL_BATCH_OP_V(BSPreFloat, false, P.nb8, st_s_pre_float(P, i))
+PTL_BATCH_OP(BSGenProp, P.n, st_s_gen_prop(P, i))
+PTL_BATCH_OP(BSGenClaim, P.n, st_s_gen_claim(P, i))
+PTL_BATCH_OP(BSGenWrite, P.n, st_s_gen_write(P, i))
+PTL_BATCH_OP(BSPreserveCounts, P.F, st_s_preserve_counts(P, i, P.s_preserve, P.s_extra))
+PTL_BATCH_OP(BSRaScatter, P.wb8, st_s_ra_scatter(P, i))
+struct BSFrame {
+    static constexpr bool kViewInShared = true;
+    int mode;
+    __device__ static uint32_t count(const Prog& P) { return 3u * P.F; }
+    __device__ void operator()(const Prog& P, uint32_t t, uint32_t) const {
+        st_s_frame(P, t % P.F, t / P.F, P.s_preserve, mode, P.s_claim);
+    }
+};
 // Pads of the families the stages write in full (ArenaGuard): guard element j of a
 // program is j - kArenaFront before its first element, then written + (j - kArenaFront).
 __device__ __forceinline__ int64_t guard_index(uint32_t j, uint32_t written) {
@@ -2587,6 +2621,12 @@ struct BScanRaCount {
     __device__ uint32_t load(const Prog& P, uint32_t i) const { return st_ra_count(P, i); }
     __device__ void store(const Prog& P, uint32_t i, uint32_t v, uint32_t) const { P.roffs[i] = v; }
 };
+struct BScanSRaCount {
+    static constexpr bool kBlocked = true;
+    __device__ static uint32_t count(const Prog& P) { return P.wb8; }
+    __device__ uint32_t load(const Prog& P, uint32_t i) const { return st_s_ra_count(P, i, P.s_extra); }
+    __device__ void store(const Prog& P, uint32_t i, uint32_t v, uint32_t) const { P.roffs[i] = v; }
+};
 struct BScanFjSize {
     static constexpr bool kBlocked = true;
     __device__ static uint32_t count(const Prog& P) { return P.w2b8; }
@@ -2781,6 +2821,23 @@ void batch_stage(BatchStage st, const BatchLaunch& bl, uint32_t total, uint32_t*
             batch_launch(bl, total, BGenClaim{});
             batch_launch(bl, total, BGenWrite{});
             break;
+        case BatchStage::PreprocessScalar:
+            batch_launch(bl, total, BSPreLists{});
+            batch_launch(bl, total, BSPreFloat{});
+            batch_launch(bl, total, BPreFloatApply{});
+            break;
+        case BatchStage::GenScalar:
+            batch_launch(bl, total, BSGenProp{});
+            batch_launch(bl, total, BSGenClaim{});
+            batch_launch(bl, total, BSGenWrite{});
+            break;
+        case BatchStage::SPreserveCounts: batch_launch(bl, total, BSPreserveCounts{}); break;
+        case BatchStage::SScatter: batch_launch(bl, total, BSRaScatter{}); break;
+        case BatchStage::SFunctab: batch_launch(bl, total, BRaFunctab{}); break;
+        case BatchStage::SFrames:  // the frame words, then the preserve stores and loads over them
+            batch_launch(bl, total, BSFrame{1});
+            batch_launch(bl, total, BSFrame{2});
+            break;
         case BatchStage::OptMark: batch_launch(bl, total, BOptMark{meta}); break;  // meta: the odd flag
         case BatchStage::OptFinal: batch_launch(bl, total, BOptFinal{}); break;
         case BatchStage::InitLifetime: batch_launch(bl, total, BInitLifetime{}); break;
@@ -2796,6 +2853,17 @@ void batch_stage(BatchStage st, const BatchLaunch& bl, uint32_t total, uint32_t*
         case BatchStage::FjFunctab: batch_launch(bl, total, BFjFunctab{}); break;
     }
 }
+
+void batch_scalar_ra_warp(const BatchLaunch& bl, uint32_t total, uint32_t stride) {
+    if (total == 0) return;
+    const size_t bytes = static_cast<size_t>(stride) * kScalarWarpFns;
+    if (allow_dynamic_smem(reinterpret_cast<const void*>(&k_batch_s_ra_warp), bytes) != cudaSuccess) return;
+    g_launches++;
+    const uint32_t grid = std::min<uint32_t>(total, 152u * 16u);
+    k_batch_s_ra_warp<<<grid, 32u * kScalarWarpFns, bytes, bl.s>>>(bl.progs, bl.off, bl.B, total, stride);
+}
+uint32_t scalar_warp_fns() { return kScalarWarpFns; }
+uint32_t scalar_warp_cap() { return kScalarWarpSymCap; }
 
 void batch_sort_keys(const BatchLaunch& bl, uint32_t total, unsigned long long* a, const uint64_t* aoff, bool out) {
     if (out) batch_launch(bl, total, BSortOut{a, aoff});
@@ -2845,6 +2913,7 @@ void batch_scan(BatchScan which, const BatchLaunch& bl, uint32_t tiles, const Sc
         case BatchScan::Count: k_bscan<<<tiles, kScanThreads, 0, bl.s>>>(bl.progs, bl.off, bl.B, BScanCount{}, sc); break;
         case BatchScan::Decl: k_bscan<<<tiles, kScanThreads, 0, bl.s>>>(bl.progs, bl.off, bl.B, BScanDecl{meta}, sc); break;
         case BatchScan::RaCount: k_bscan<<<tiles, kScanThreads, 0, bl.s>>>(bl.progs, bl.off, bl.B, BScanRaCount{}, sc); break;
+        case BatchScan::SRaCount: k_bscan<<<tiles, kScanThreads, 0, bl.s>>>(bl.progs, bl.off, bl.B, BScanSRaCount{}, sc); break;
         case BatchScan::FjSize: k_bscan<<<tiles, kScanThreads, 0, bl.s>>>(bl.progs, bl.off, bl.B, BScanFjSize{}, sc); break;
     }
 }

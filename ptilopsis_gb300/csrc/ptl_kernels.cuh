@@ -121,9 +121,13 @@ struct BatchLaunch {
 };
 enum class BatchStage {
     Ingest, Preprocess, Fix, Functab, Gen, OptMark, OptFinal, InitLifetime, Cross, RaHist, Spill,
-    Scatter, RaFunctab, FjEmit, FjFunctab
+    Scatter, RaFunctab, FjEmit, FjFunctab,
+    // the scalar generator's (ptl_scalar.cuh): preprocess, isn_gen, preserve counts
+    // (per function), scatter (per word), the function table after regalloc (per
+    // function), the frame words and preserve stores (3 items per function)
+    PreprocessScalar, GenScalar, SPreserveCounts, SScatter, SFunctab, SFrames
 };
-enum class BatchScan { Count, Decl, RaCount, FjSize };
+enum class BatchScan { Count, Decl, RaCount, FjSize, SRaCount };
 uint32_t batch_tile();       // default elements per tile of the element-wise stages
 // Tile sizes the element-wise kernels and the optimize sweeps accept (powers of two).
 bool batch_tile_ok(uint32_t tile);
@@ -177,6 +181,14 @@ void batch_serial(const Prog* progs, const uint32_t* list, uint32_t count, cudaS
 // batch_ra_threads(max_g0), then its lane-0 pass, which follows their progress through
 // the program's ra_chunks record: histogram (BatchStage::RaHist) then zeroed counts).
 uint32_t batch_ra_threads(uint32_t max_g0);
+// The scalar generator's register allocation of the listed programs' functions, one warp
+// per function (a tile: scalar_warp_fns() functions of one program; the tile table over
+// F in bl), each warp with `stride` symbol bytes (at least the listed programs' longest
+// function, at most scalar_warp_cap()).  The serial and tile forms run per program
+// through launch_scalar_ra_serial / launch_scalar_ra_free.
+void batch_scalar_ra_warp(const BatchLaunch& bl, uint32_t total, uint32_t stride);
+uint32_t scalar_warp_fns();
+uint32_t scalar_warp_cap();
 // share: the part of the device's resident blocks the persistent launch may take (1 =
 // all; less leaves room for other streams' kernels, e.g. a compile server's other lanes).
 cudaError_t batch_regalloc(const Prog* progs, const uint32_t* item_off, const uint32_t* order, uint32_t n,

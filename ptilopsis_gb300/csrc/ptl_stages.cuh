@@ -196,6 +196,12 @@ struct Prog {
     uint32_t* flags;      // [0] optimize changed, [1] [2] regalloc checks, [3] a node at max_depth
     uint32_t scalar;      // 1: the scalar generator's semantics (ptl_scalar.cuh)
     uint32_t pad_;
+    // the scalar generator's register allocation in a batch (null otherwise): per
+    // function the preserve mask, per word the preserve counts, per word after
+    // regalloc the frame writes' claims
+    unsigned long long* s_preserve;
+    uint32_t* s_extra;
+    unsigned long long* s_claim;
 };
 
 // Function-argument registers and stack slots, rv_generator_avx.cpp:126-213, on one

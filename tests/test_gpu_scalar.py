@@ -152,3 +152,69 @@ def test_gpu_scalar_matches_reference_on_large_inputs(built_cuda, fx):
         for k in ("gen_instr", "gen_rs1", "ra_instr", "ra_rd", "ra_rs1", "ra_rs2", "fn_start", "fn_size"):
             assert _crc(k, gen.snapshot(k)) == entry["snapshots"][k], f"{fx}: {k}"
     assert [len(words), crc32(words)] == entry["snapshots"]["out_words"]
+
+
+def test_gpu_scalar_batch_matches_reference(built_cuda):
+    """Every committed scalar case (fixtures, c0 seeds, batched-workload programs) in one
+    batch with the scalar switch on: each program's words and function table equal the
+    reference's scalar run (CRCs), the same as through the one-program API."""
+    from ptilopsis_gb300.batch import BatchCompiler
+    entries = manifest_scalar()["fixtures"]
+    trees = [ast_to_tree(load_scalar_case(e)[0]) for e in entries]
+    with BatchCompiler(workers=4, scalar=True) as b:
+        b.compile(trees)
+        for k, e in enumerate(entries):
+            res = b.result(k)
+            assert [len(res.words), crc32(res.words)] == e["snapshots"]["out_words"], e["name"]
+            for key, snap in (("starts", "fn_start"), ("ends", "fn_end"), ("sizes", "fn_size"), ("ids", "fn_id")):
+                assert [len(res.table[key]), crc32(res.table[key])] == e["snapshots"][snap], (e["name"], key)
+
+
+def test_gpu_scalar_batch_large_inputs(built_cuda):
+    """The reference's larger Pareas inputs with scalar goldens, all in one scalar batch."""
+    from conftest import load_large, manifest_scalar_large
+    from ptilopsis_gb300.batch import BatchCompiler
+    entries = manifest_scalar_large()["fixtures"]
+    trees = [ast_to_tree(load_large(e["name"])[0]) for e in entries]
+    with BatchCompiler(workers=8, scalar=True) as b:
+        b.compile(trees)
+        for k, e in enumerate(entries):
+            w = b.result(k).words
+            assert [len(w), crc32(w)] == e["snapshots"]["out_words"], e["name"]
+
+
+def test_gpu_scalar_batch_equals_plain_and_switches(built_cuda):
+    """Synthetic programs (spilling ones, one with a function too long for a warp's
+    symbol bytes, which takes the tile form on its own) in one scalar batch equal the
+    plain scalar generator; the same compiler then compiles them with the AVX
+    generator's semantics and back, each equal to the matching plain generator."""
+    from ptilopsis_gb300 import RvGenerator
+    from ptilopsis_gb300.batch import BatchCompiler
+    from ptilopsis_gb300.synth import SynthParams, config_params, generate
+    rng = np.random.default_rng(0x50544C70)
+    trees = [generate(SynthParams(seed=0x50544C70 + k, n_functions=int(rng.integers(1, 40)),
+                                  median_fn_nodes=float(rng.integers(40, 900)), sigma=0.8,
+                                  max_nesting=int(rng.integers(2, 12)), spill_frac=0.25 if k % 3 == 0 else 0.0))
+             for k in range(24)]
+    trees.append(generate(SynthParams(seed=0x50544C90, n_functions=2, median_fn_nodes=16000.0, max_nesting=4)))
+    trees += [generate(config_params("c3", program=k)) for k in (3, 8)]
+
+    def plain(t, scalar):
+        with RvGenerator(t, scalar=scalar) as g:
+            g.process()
+            return g.get_instructions(), g.function_table()
+
+    want_s = [plain(t, True) for t in trees]
+    want_a = [plain(t, False) for t in trees]
+    with RvGenerator(trees[24], scalar=True) as g:  # its longest function passes the warp form's cap
+        g.process(profile=True)
+        assert int(np.max(g.snapshot("cnt_fn_size"))) > 12288
+    with BatchCompiler(workers=6) as b:
+        for mode, want in ((True, want_s), (False, want_a), (True, want_s)):
+            b.set_scalar(mode)
+            b.compile(trees)
+            for k, (w, tab) in enumerate(want):
+                res = b.result(k)
+                np.testing.assert_array_equal(res.words, w, err_msg=f"scalar={mode} program {k}")
+                for key in ("starts", "ends", "sizes", "ids"):
+                    np.testing.assert_array_equal(res.table[key], tab[key], err_msg=f"scalar={mode} {k} {key}")
