@@ -296,6 +296,9 @@ ptl_status ptl_server_submit(ptl_server* server, const ptl_ast_view* tree, uint6
  * instead of copying them (submit costs O(1)), and the caller keeps them alive and
  * unchanged until ptl_server_release of the ticket. */
 #define PTL_SUBMIT_BORROW 1u
+/* The request gets the scalar generator's output (rv_generator_st, the reference's -s);
+ * a batch holds requests of one kind only. */
+#define PTL_SUBMIT_SCALAR 2u
 ptl_status ptl_server_submit_flags(ptl_server* server, const ptl_ast_view* tree, uint32_t flags, uint64_t* ticket);
 /* *done = 1 once the request finished (wait != 0 blocks until then); returns its status. */
 ptl_status ptl_server_poll(ptl_server* server, uint64_t ticket, int wait, int* done);

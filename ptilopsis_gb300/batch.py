@@ -303,13 +303,15 @@ class CompileServer:
         if st != 0:
             raise PtlError(st, "ptl_server_create")
 
-    def submit(self, tree: DepthTree, copy: bool = True) -> int:
+    def submit(self, tree: DepthTree, copy: bool = True, scalar: bool = False) -> int:
         """Queues a host tree.  copy=False lends the tree's arrays to the server instead of
-        copying them (the server keeps a reference until release(ticket))."""
+        copying them (the server keeps a reference until release(ticket)); scalar=True asks
+        for the scalar generator's output (the reference's -s)."""
         keep: list = []
         view = _view(tree, keep)
         t = ctypes.c_uint64()
-        st = self._lib.ptl_server_submit_flags(self._h, ctypes.byref(view), 0 if copy else 1, ctypes.byref(t))
+        flags = (0 if copy else 1) | (2 if scalar else 0)
+        st = self._lib.ptl_server_submit_flags(self._h, ctypes.byref(view), flags, ctypes.byref(t))
         if st != 0:
             raise PtlError(st, "ptl_server_submit")
         if not copy:

@@ -183,6 +183,7 @@ struct Request {
     std::vector<int32_t> parent, depth, child;
     std::vector<uint32_t> data;
     bool borrowed = false;
+    bool scalar = false;  // the scalar generator's semantics (PTL_SUBMIT_SCALAR)
     ptl_ast_view borrowed_view{};
     uint64_t bytes = 0;        // admission estimate
     uint64_t t_submit = 0, t_start = 0, t_done = 0;
@@ -227,10 +228,17 @@ struct ptl_server {
     size_t small_lanes = 1;
     std::mutex mu;
     std::condition_variable cv_work, cv_done;
-    // queued requests by size class (0: small, 1: large), each in arrival order; a lane
-    // takes from the front, so a batch leaves its queue in O(1) per request however long
-    // the queue has grown
-    std::deque<std::shared_ptr<Request>> queue[2];
+    // queued requests by size class (0: small, 1: large), each in arrival order, for the
+    // AVX generator's semantics (mode 0) and the scalar generator's (mode 1); a lane takes
+    // from the front, so a batch leaves its queue in O(1) per request however long the
+    // queue has grown
+    std::deque<std::shared_ptr<Request>> queue[2][2];
+    // The mode whose queue of class c has the earliest request at its front.
+    int mode_for(int c) const {
+        if (queue[1][c].empty()) return 0;
+        if (queue[0][c].empty()) return 1;
+        return queue[1][c].front()->t_submit < queue[0][c].front()->t_submit ? 1 : 0;
+    }
     std::unordered_map<uint64_t, std::shared_ptr<Request>> all;
     std::vector<std::thread> lanes;
     std::vector<std::unique_ptr<ptl::BatchPipeline>> pipes;
@@ -246,6 +254,7 @@ struct ptl_server {
     // while the other lanes keep taking the requests that arrive meanwhile.
     void run(size_t w) {
         std::vector<std::shared_ptr<Request>> batch;
+        bool batch_scalar = false;
         std::vector<ptl_ast_view> views;
         std::vector<ptl::BatchResult> res;
         const bool prefer_small = w < small_lanes;
@@ -270,7 +279,9 @@ struct ptl_server {
                     for (int pass = 0; pass < (prefer_small ? 1 : 2) && batch.empty(); ++pass) {
                         const bool want_small = (pass == 0) == prefer_small;
                         uint64_t nodes = 0;
-                        std::deque<std::shared_ptr<Request>>& q = queue[want_small ? 0 : 1];
+                        const int c = want_small ? 0 : 1;
+                        batch_scalar = mode_for(c) == 1;
+                        std::deque<std::shared_ptr<Request>>& q = queue[batch_scalar ? 1 : 0][c];
                         // a request that does not fit may be passed by later ones that do, within a
                         // bounded look-ahead (the lock is held while a batch is formed)
                         size_t looked = 0;
@@ -323,6 +334,7 @@ struct ptl_server {
                 r->t_start = t0;
                 views.push_back(r->view());
             }
+            pipes[w]->set_scalar(batch_scalar);
             const ptl_status st = pipes[w]->compile(views.data(), views.size(), res);
             uint64_t held = pipes[w]->device_bytes();
             // The results leave the pipeline's output buffers before the lane's next compile
@@ -426,12 +438,14 @@ extern "C" ptl_status ptl_server_submit(ptl_server* s, const ptl_ast_view* tree,
 
 extern "C" ptl_status ptl_server_submit_flags(ptl_server* s, const ptl_ast_view* tree, uint32_t flags,
                                               uint64_t* ticket) {
-    if (!s || !tree || !ticket || tree->on_device || (flags & ~PTL_SUBMIT_BORROW)) return PTL_BAD_ARGUMENT;
+    if (!s || !tree || !ticket || tree->on_device || (flags & ~(PTL_SUBMIT_BORROW | PTL_SUBMIT_SCALAR)))
+        return PTL_BAD_ARGUMENT;
     auto req = std::make_shared<Request>();
     const size_t n = tree->n;
     req->n = n;
     req->max_depth = tree->max_depth;
     req->bytes = footprint(n);
+    req->scalar = (flags & PTL_SUBMIT_SCALAR) != 0;
     if (req->bytes > s->budget) return PTL_ADMISSION_DENIED;  // could never be admitted
     if (n && (!tree->type || !tree->rtype || !tree->parent || !tree->depth || !tree->child_idx || !tree->data))
         return PTL_BAD_ARGUMENT;
@@ -451,7 +465,7 @@ extern "C" ptl_status ptl_server_submit_flags(ptl_server* s, const ptl_ast_view*
         req->ticket = s->next_ticket++;
         req->t_submit = now_ns();
         s->all[req->ticket] = req;
-        s->queue[n < s->small_nodes ? 0 : 1].push_back(req);
+        s->queue[req->scalar ? 1 : 0][n < s->small_nodes ? 0 : 1].push_back(req);
         *ticket = req->ticket;
     }
     s->cv_work.notify_one();
@@ -527,7 +541,7 @@ extern "C" ptl_status ptl_server_stats(ptl_server* s, uint64_t stats[5]) {
     std::lock_guard<std::mutex> lk(s->mu);
     stats[0] = s->completed;
     stats[1] = s->nodes_done;
-    stats[2] = s->queue[0].size() + s->queue[1].size();
+    stats[2] = s->queue[0][0].size() + s->queue[0][1].size() + s->queue[1][0].size() + s->queue[1][1].size();
     stats[3] = s->in_use;
     stats[4] = s->batches;
     return PTL_OK;

@@ -288,3 +288,22 @@ def test_batch_regalloc_share_and_device_window(built_cuda):
             assert 0 < b.device_ns() <= b.elapsed_ns()
         with pytest.raises(PtlError):
             b.set_regalloc_share(0.0)
+
+
+def test_server_scalar_and_avx_requests_in_the_mix(built_cuda):
+    """Requests for the scalar generator (PTL_SUBMIT_SCALAR) and for the AVX generator
+    submitted interleaved to one server: batches hold one kind each, and every result
+    equals the plain generator of its kind."""
+    from ptilopsis_gb300 import RvGenerator
+    from ptilopsis_gb300.batch import CompileServer
+    trees = _programs(24, seed0=0x50544DE0)
+    kinds = [k % 3 == 1 for k in range(len(trees))]
+    with CompileServer(device=0, slots=3, memory_budget=8 << 30) as srv:
+        tickets = [srv.submit(t, scalar=sc) for t, sc in zip(trees, kinds)]
+        outs = [srv.result(t) for t in tickets]
+        for t in tickets:
+            srv.release(t)
+    for k, (t, sc) in enumerate(zip(trees, kinds)):
+        with RvGenerator(t, scalar=sc) as g:
+            g.process()
+            _assert_same(outs[k], g.get_instructions(), g.function_table(), f"request {k} scalar={sc}")
