@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdint>
 #include <initializer_list>
 #include <cstdio>
 #include <cstring>
@@ -130,6 +131,25 @@ struct ptl_generator {
 };
 
 namespace {
+
+// Whether the device reads and writes pageable host memory coherently (the
+// cudaDevAttrPageableMemoryAccess attribute), per device, asked once.
+bool pageable_access(int device) {
+    static std::mutex mu;
+    static std::vector<int> known;  // -1 unknown, 0 no, 1 yes
+    std::lock_guard<std::mutex> lk(mu);
+    if (device < 0) return false;
+    if (known.size() <= static_cast<size_t>(device)) known.resize(static_cast<size_t>(device) + 1, -1);
+    if (known[device] < 0) {
+        int v = 0;
+        if (cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccess, device) != cudaSuccess) {
+            cudaGetLastError();
+            v = 0;
+        }
+        known[device] = v ? 1 : 0;
+    }
+    return known[device] == 1;
+}
 
 ptl_status fail(ptl_generator* g, ptl_status st, const std::string& msg) {
     if (g) g->last_error = msg;
@@ -536,7 +556,14 @@ ptl_status run_pipeline(ptl_generator* g, bool profile, bool to_host, bool row0_
         g->fn_end_h.resize(g->F);
         g->fn_size_h.resize(g->F);
         g->fn_id_h.resize(g->F);
-        if (g->W3) PTL_CU(cudaMemcpyAsync(g->words.data(), P.out, g->W3 * 4ull, cudaMemcpyDeviceToHost, s));
+        if (g->W3) {
+            // Where the device accesses pageable memory coherently (ATS), kernel stores put
+            // the words straight into the vector; otherwise the copy engine stages them.
+            if (pageable_access(g->device) && (reinterpret_cast<uintptr_t>(g->words.data()) & 15u) == 0)
+                PTL_CU(write_host(P.out, g->words.data(), g->W3 * 4ull, s));
+            else
+                PTL_CU(cudaMemcpyAsync(g->words.data(), P.out, g->W3 * 4ull, cudaMemcpyDeviceToHost, s));
+        }
         PTL_CU(cudaMemcpyAsync(g->fn_start_h.data(), P.fn_start, g->F * 4ull, cudaMemcpyDeviceToHost, s));
         PTL_CU(cudaMemcpyAsync(g->fn_end_h.data(), P.fn_end, g->F * 4ull, cudaMemcpyDeviceToHost, s));
         PTL_CU(cudaMemcpyAsync(g->fn_size_h.data(), P.fn_size, g->F * 4ull, cudaMemcpyDeviceToHost, s));

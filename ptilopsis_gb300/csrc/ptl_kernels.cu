@@ -2884,6 +2884,35 @@ cudaError_t read_host(const void* src, void* dst, size_t bytes, cudaStream_t s) 
     return cudaGetLastError();
 }
 
+// Device memory into pinned host memory by stores over the host link (the pinned
+// buffer's address is valid on the device): 16-byte stores, four in flight per thread,
+// the last bytes one at a time.
+__global__ void __launch_bounds__(kThreads) k_write_host(const uint4* src, uint4* dst, uint64_t n16,
+                                                         const uint8_t* tsrc, uint8_t* tdst, uint32_t tail) {
+    const uint64_t stride = static_cast<uint64_t>(gridDim.x) * blockDim.x;
+    uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    for (; i + 3 * stride < n16; i += 4 * stride) {
+        const uint4 a = src[i], b = src[i + stride], c = src[i + 2 * stride], d = src[i + 3 * stride];
+        dst[i] = a;
+        dst[i + stride] = b;
+        dst[i + 2 * stride] = c;
+        dst[i + 3 * stride] = d;
+    }
+    for (; i < n16; i += stride) dst[i] = src[i];
+    if (blockIdx.x == 0 && threadIdx.x < tail) tdst[threadIdx.x] = tsrc[threadIdx.x];
+}
+
+cudaError_t write_host(const void* src, void* dst, size_t bytes, cudaStream_t s) {
+    if (bytes == 0) return cudaSuccess;
+    const uint64_t n16 = bytes / 16u;
+    const uint32_t tail = static_cast<uint32_t>(bytes - n16 * 16u);
+    g_launches++;
+    k_write_host<<<152u * 4u, kThreads, 0, s>>>(static_cast<const uint4*>(src), static_cast<uint4*>(dst), n16,
+                                                static_cast<const uint8_t*>(src) + n16 * 16u,
+                                                static_cast<uint8_t*>(dst) + n16 * 16u, tail);
+    return cudaGetLastError();
+}
+
 void batch_gather_host(const BatchLaunch& bl, uint32_t total, const HostGather& g) {
     if (total == 0) return;
     g_launches++;
