@@ -1050,7 +1050,7 @@ ptl_status Pipeline::compile(const ptl_ast_view* trees, size_t count, std::vecto
             // against 9-10 ms through the copy engine
             void* dout = nullptr;  // the pinned output buffer's address on the device
             if (cudaHostGetDevicePointer(&dout, h_out.p, 0) == cudaSuccess && dout) {
-                BP_CU(write_host(out.p, dout, Lo.total * 4, s));
+                BP_CU(kernel_copy(out.p, dout, Lo.total * 4, s));
             } else {
                 cudaGetLastError();
                 BP_CU(cudaMemcpyAsync(h_out.p, out.p, Lo.total * 4, cudaMemcpyDeviceToHost, s));

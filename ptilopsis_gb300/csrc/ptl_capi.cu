@@ -560,7 +560,7 @@ ptl_status run_pipeline(ptl_generator* g, bool profile, bool to_host, bool row0_
             // Where the device accesses pageable memory coherently (ATS), kernel stores put
             // the words straight into the vector; otherwise the copy engine stages them.
             if (pageable_access(g->device) && (reinterpret_cast<uintptr_t>(g->words.data()) & 15u) == 0)
-                PTL_CU(write_host(P.out, g->words.data(), g->W3 * 4ull, s));
+                PTL_CU(kernel_copy(P.out, g->words.data(), g->W3 * 4ull, s));
             else
                 PTL_CU(cudaMemcpyAsync(g->words.data(), P.out, g->W3 * 4ull, cudaMemcpyDeviceToHost, s));
         }
@@ -586,10 +586,23 @@ cudaError_t upload_inputs(ptl_generator* g, const ptl_ast_view* tree) {
     struct { DevBuf* b; const void* src; size_t es; } in[] = {
         {&g->in_type, tree->type, 1}, {&g->in_rtype, tree->rtype, 1}, {&g->in_parent, tree->parent, 4},
         {&g->in_depth, tree->depth, 4}, {&g->in_child, tree->child_idx, 4}, {&g->in_data, tree->data, 4}};
+    // Where the device reads pageable memory coherently (ATS), a kernel reads the caller's
+    // arrays in place (about 200 GB/s, against the staged copies of pageable memory); the
+    // call then waits for it, so that the caller may reuse the arrays on return, as after
+    // a staged copy.
+    bool direct = !tree->on_device && pageable_access(g->device);
+    for (auto& x : in) direct = direct && (reinterpret_cast<uintptr_t>(x.src) & 15u) == 0;
     cudaError_t e = cudaSuccess;
     for (auto& x : in) {
         e = x.b->ensure(n, x.es);
-        if (e == cudaSuccess) e = cudaMemcpyAsync(x.b->at<char>(), x.src, n * x.es, kind, g->stream);
+        if (e == cudaSuccess) {
+            e = direct ? kernel_copy(x.src, x.b->at<char>(), n * x.es, g->stream)
+                       : cudaMemcpyAsync(x.b->at<char>(), x.src, n * x.es, kind, g->stream);
+        }
+        if (e != cudaSuccess) return e;
+    }
+    if (direct) {
+        e = cudaStreamSynchronize(g->stream);
         if (e != cudaSuccess) return e;
     }
     g->n = tree->n;

@@ -2884,10 +2884,9 @@ cudaError_t read_host(const void* src, void* dst, size_t bytes, cudaStream_t s) 
     return cudaGetLastError();
 }
 
-// Device memory into pinned host memory by stores over the host link (the pinned
-// buffer's address is valid on the device): 16-byte stores, four in flight per thread,
-// the last bytes one at a time.
-__global__ void __launch_bounds__(kThreads) k_write_host(const uint4* src, uint4* dst, uint64_t n16,
+// A copy by kernel loads and stores (kernel_copy): 16-byte elements, four in flight per
+// thread, the last bytes one at a time.
+__global__ void __launch_bounds__(kThreads) k_copy16(const uint4* src, uint4* dst, uint64_t n16,
                                                          const uint8_t* tsrc, uint8_t* tdst, uint32_t tail) {
     const uint64_t stride = static_cast<uint64_t>(gridDim.x) * blockDim.x;
     uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -2902,12 +2901,12 @@ __global__ void __launch_bounds__(kThreads) k_write_host(const uint4* src, uint4
     if (blockIdx.x == 0 && threadIdx.x < tail) tdst[threadIdx.x] = tsrc[threadIdx.x];
 }
 
-cudaError_t write_host(const void* src, void* dst, size_t bytes, cudaStream_t s) {
+cudaError_t kernel_copy(const void* src, void* dst, size_t bytes, cudaStream_t s) {
     if (bytes == 0) return cudaSuccess;
     const uint64_t n16 = bytes / 16u;
     const uint32_t tail = static_cast<uint32_t>(bytes - n16 * 16u);
     g_launches++;
-    k_write_host<<<152u * 4u, kThreads, 0, s>>>(static_cast<const uint4*>(src), static_cast<uint4*>(dst), n16,
+    k_copy16<<<152u * 4u, kThreads, 0, s>>>(static_cast<const uint4*>(src), static_cast<uint4*>(dst), n16,
                                                 static_cast<const uint8_t*>(src) + n16 * 16u,
                                                 static_cast<uint8_t*>(dst) + n16 * 16u, tail);
     return cudaGetLastError();

@@ -171,9 +171,10 @@ void batch_gather_host(const BatchLaunch& bl, uint32_t total, const HostGather& 
 // A kernel copying bytes (a multiple of 16, both 16-byte aligned) from host memory it
 // reads directly into device memory.
 cudaError_t read_host(const void* src, void* dst, size_t bytes, cudaStream_t s);
-// Copies bytes from device memory into pinned host memory (both 16-byte aligned) with
-// kernel stores over the host link.
-cudaError_t write_host(const void* src, void* dst, size_t bytes, cudaStream_t s);
+// Copies bytes between memories a kernel can address (device memory, pinned host memory,
+// pageable host memory where the device accesses it coherently), both 16-byte aligned,
+// with kernel loads and stores: over the host link faster than the copy engine here.
+cudaError_t kernel_copy(const void* src, void* dst, size_t bytes, cudaStream_t s);
 void batch_scan(BatchScan which, const BatchLaunch& bl, uint32_t tiles, const ScanScratch& sc, uint32_t* meta);
 void batch_sizes(bool w3, const Prog* progs, const uint32_t* list, uint32_t count, uint32_t* meta, cudaStream_t s);
 // ra_order of each listed program: its independent functions, longest first.
