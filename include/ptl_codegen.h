@@ -89,6 +89,13 @@ ptl_status ptl_generator_process(ptl_generator* gen, int profile);
  * host buffer owned by the generator, valid until the next process or destroy. */
 ptl_status ptl_generator_instructions(ptl_generator* gen, const uint32_t** words, size_t* count);
 
+/* The same words copied into the caller's buffer: dst null (or capacity too small, then
+ * PTL_BAD_ARGUMENT) only sets *count.  After a process that left the words on the device
+ * (flag 2) they go straight from the device into dst, without the generator's own copy;
+ * into pageable memory whose pages the host has not touched yet that is slower than the
+ * generator's copy, whose buffer keeps its pages from call to call. */
+ptl_status ptl_generator_copy_instructions(ptl_generator* gen, uint32_t* dst, size_t capacity, size_t* count);
+
 /* The same words as a device pointer (no copy). */
 ptl_status ptl_generator_device_instructions(ptl_generator* gen, const uint32_t** words, size_t* count);
 

@@ -138,6 +138,7 @@ def lib():
         L.ptl_kernel_launches.argtypes = []
         L.ptl_kernel_launches.restype = ctypes.c_uint64
         L.ptl_generator_instructions.argtypes = [vp, ctypes.POINTER(u32p), ctypes.POINTER(sz)]
+        L.ptl_generator_copy_instructions.argtypes = [vp, u32p, sz, ctypes.POINTER(sz)]
         L.ptl_generator_device_instructions.argtypes = [vp, ctypes.POINTER(vp), ctypes.POINTER(sz)]
         L.ptl_generator_function_table.argtypes = [vp, ctypes.POINTER(u32p), ctypes.POINTER(u32p),
                                                    ctypes.POINTER(u32p), ctypes.POINTER(u32p), ctypes.POINTER(sz)]
@@ -154,7 +155,7 @@ def lib():
         L.ptl_code_table.restype = ctypes.c_size_t
         L.ptl_device_info.argtypes = [ctypes.c_int, ctypes.c_char_p, sz, ctypes.POINTER(ctypes.c_int),
                                       ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
-        for fn in ("ptl_generator_create", "ptl_generator_create_scalar", "ptl_generator_process", "ptl_generator_upload", "ptl_generator_instructions",
+        for fn in ("ptl_generator_create", "ptl_generator_create_scalar", "ptl_generator_process", "ptl_generator_upload", "ptl_generator_instructions", "ptl_generator_copy_instructions",
                    "ptl_generator_device_instructions", "ptl_generator_function_table",
                    "ptl_generator_stage_ns", "ptl_generator_snapshot", "ptl_compile", "ptl_device_info"):
             getattr(L, fn).restype = ctypes.c_int
@@ -244,6 +245,9 @@ class RvGenerator:
         self._check(self._lib.ptl_generator_process(self._h, flags), "process")
 
     def get_instructions(self) -> np.ndarray:
+        # A copy of the generator's host words.  (Fetching from the device straight into a
+        # new array was slower: the device's stores fault the new array's pages in one by
+        # one, while the generator's buffer keeps its pages from call to call.)
         p = ctypes.POINTER(ctypes.c_uint32)()
         n = ctypes.c_size_t()
         self._check(self._lib.ptl_generator_instructions(self._h, ctypes.byref(p), ctypes.byref(n)), "instructions")

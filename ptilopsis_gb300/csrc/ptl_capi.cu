@@ -103,7 +103,7 @@ struct ptl_generator {
     // results
     uint32_t F = 0, W = 0, W2 = 0, W3 = 0, S = 0;
     std::vector<uint32_t> words, fn_start_h, fn_end_h, fn_size_h, fn_id_h;
-    bool host_valid = false;
+    bool words_valid = false, table_valid = false;  // the last result's host copies are current
     uint64_t stage_ns[7] = {0, 0, 0, 0, 0, 0, 0};
     uint32_t sort_rounds = 0, opt_sweeps = 0;
     SortRoundGraph sort_graph;  // a pair of depth-sort rounds, replayed
@@ -356,7 +356,7 @@ ptl_status run_pipeline(ptl_generator* g, bool profile, bool to_host, bool row0_
     cudaStream_t s = g->stream;
     const size_t n = g->n;
     const size_t nb8 = r8(n);
-    g->host_valid = false;
+    g->words_valid = g->table_valid = false;
     StageTimer timer(g, profile);
 
     // fixed-size scratch first, so every Prog view below sees it
@@ -569,7 +569,7 @@ ptl_status run_pipeline(ptl_generator* g, bool profile, bool to_host, bool row0_
         PTL_CU(cudaMemcpyAsync(g->fn_size_h.data(), P.fn_size, g->F * 4ull, cudaMemcpyDeviceToHost, s));
         PTL_CU(cudaMemcpyAsync(g->fn_id_h.data(), P.fn_id, g->F * 4ull, cudaMemcpyDeviceToHost, s));
         PTL_CU(cudaStreamSynchronize(s));
-        g->host_valid = true;
+        g->words_valid = g->table_valid = true;
     }
     return PTL_OK;
 }
@@ -607,7 +607,7 @@ cudaError_t upload_inputs(ptl_generator* g, const ptl_ast_view* tree) {
     }
     g->n = tree->n;
     g->max_depth = tree->max_depth;
-    g->host_valid = false;
+    g->words_valid = g->table_valid = false;
     return cudaSuccess;
 }
 
@@ -675,18 +675,44 @@ ptl_status ptl_generator_process(ptl_generator* g, int profile) {
     return st;
 }
 
+namespace {
+// The last result's words from the device into dst (count words), by kernel stores where
+// the device writes pageable memory coherently and dst is 16-byte aligned.
+cudaError_t fetch_words(ptl_generator* g, uint32_t* dst, size_t count) {
+    if (count == 0) return cudaSuccess;
+    const DeviceScope on_device(g->device);
+    if (!on_device.ok()) return on_device.err;
+    cudaError_t e = (pageable_access(g->device) && (reinterpret_cast<uintptr_t>(dst) & 15u) == 0)
+                        ? kernel_copy(g->out.at<uint32_t>(), dst, count * 4ull, g->stream)
+                        : cudaMemcpyAsync(dst, g->out.at<uint32_t>(), count * 4ull, cudaMemcpyDeviceToHost, g->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+    return e;
+}
+}  // namespace
+
 ptl_status ptl_generator_instructions(ptl_generator* g, const uint32_t** words, size_t* count) {
     if (!g || !words || !count) return PTL_BAD_ARGUMENT;
-    if (!g->host_valid) {
+    if (!g->words_valid) {
         g->words.resize(g->W3);
-        if (g->W3) {
-            cudaError_t e = cudaMemcpyAsync(g->words.data(), g->out.at<uint32_t>(), g->W3 * 4ull, cudaMemcpyDeviceToHost, g->stream);
-            if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
-            if (e != cudaSuccess) return cuda_fail(g, e, "instructions");
-        }
+        if (const cudaError_t e = fetch_words(g, g->words.data(), g->W3); e != cudaSuccess)
+            return cuda_fail(g, e, "instructions");
+        g->words_valid = true;
     }
     *words = g->words.data();
     *count = g->W3;
+    return PTL_OK;
+}
+
+ptl_status ptl_generator_copy_instructions(ptl_generator* g, uint32_t* dst, size_t capacity, size_t* count) {
+    if (!g || !count) return PTL_BAD_ARGUMENT;
+    *count = g->W3;
+    if (!dst) return PTL_OK;
+    if (capacity < g->W3) return PTL_BAD_ARGUMENT;
+    if (g->words_valid) {
+        if (g->W3) std::memcpy(dst, g->words.data(), g->W3 * 4ull);
+        return PTL_OK;
+    }
+    if (const cudaError_t e = fetch_words(g, dst, g->W3); e != cudaSuccess) return cuda_fail(g, e, "instructions");
     return PTL_OK;
 }
 
@@ -700,10 +726,9 @@ ptl_status ptl_generator_device_instructions(ptl_generator* g, const uint32_t** 
 ptl_status ptl_generator_function_table(ptl_generator* g, const uint32_t** starts, const uint32_t** ends,
                                         const uint32_t** sizes, const uint32_t** ids, size_t* count) {
     if (!g || !count) return PTL_BAD_ARGUMENT;
-    if (!g->host_valid) {
-        const uint32_t* w;
-        size_t c;
-        if (ptl_status st = ptl_generator_instructions(g, &w, &c); st != PTL_OK) return st;
+    if (!g->table_valid) {
+        const DeviceScope on_device(g->device);
+        if (!on_device.ok()) return fail(g, PTL_CUDA_ERROR, "cudaSetDevice");
         g->fn_start_h.resize(g->F);
         g->fn_end_h.resize(g->F);
         g->fn_size_h.resize(g->F);
@@ -714,7 +739,7 @@ ptl_status ptl_generator_function_table(ptl_generator* g, const uint32_t** start
         cudaMemcpyAsync(g->fn_id_h.data(), g->fn_id.at<uint32_t>(), g->F * 4ull, cudaMemcpyDeviceToHost, g->stream);
         const cudaError_t e = cudaStreamSynchronize(g->stream);
         if (e != cudaSuccess) return cuda_fail(g, e, "function table");
-        g->host_valid = true;
+        g->table_valid = true;
     }
     if (starts) *starts = g->fn_start_h.data();
     if (ends) *ends = g->fn_end_h.data();
