@@ -291,3 +291,25 @@ def test_gpu_depth_order_adversarial_keys(built_cuda, kind, n):
     want = np.empty(n, np.uint32)
     want[perm] = np.arange(n, dtype=np.uint32)
     np.testing.assert_array_equal(depth_order(keys), want)
+
+
+def test_gpu_copy_instructions_into_caller_buffer(built_cuda):
+    """ptl_generator_copy_instructions: a null buffer sets the count, a short one is
+    refused, and after a process that left the words on the device (and after one that
+    brought them to the host) the copy equals get_instructions."""
+    import ctypes
+    from ptilopsis_gb300 import RvGenerator
+    from ptilopsis_gb300.synth import SynthParams, generate
+    tree = generate(SynthParams(seed=0x50544C45))
+    with RvGenerator(tree) as gen:
+        L, h = gen._lib, gen._h
+        for to_host in (False, True):
+            gen.process(to_host=to_host)
+            n = ctypes.c_size_t()
+            assert L.ptl_generator_copy_instructions(h, None, 0, ctypes.byref(n)) == 0
+            assert n.value > 0
+            buf = np.zeros(n.value, np.uint32)
+            ptr = buf.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32))
+            assert L.ptl_generator_copy_instructions(h, ptr, n.value - 1, ctypes.byref(n)) != 0
+            assert L.ptl_generator_copy_instructions(h, ptr, n.value, ctypes.byref(n)) == 0
+            np.testing.assert_array_equal(buf, gen.get_instructions(), err_msg=f"to_host={to_host}")
