@@ -1412,36 +1412,152 @@ __global__ void __launch_bounds__(1024) k_ra_steps(Prog P, uint32_t S, uint32_t 
 // ------------------------------------------------------- the lane-0 pass on a cluster
 // A program with more lane-0 groups than one block runs at one slot per thread (above
 // 1,024) spreads its slots over the CTAs of a thread-block cluster: one per thread (Q
-// per thread above 8 x 512).  Row 0 and the step state (Ra2Shared) live in CTA 0's
-// shared memory, which every CTA reaches through distributed shared memory; each CTA
-// keeps its own slots' step records and symbol caches, which the row-0 phases (CTA 0,
-// one thread per physical register) read and mark remotely.  Cluster barriers take the
-// place of the block's.  A barrier that ORs a flag adds to a word in CTA 0: three words
-// in rotation, the one the next such barrier uses cleared before this one (its last
-// readers passed the barrier in between).  The independent functions ran before, so
-// every trigger record is complete and nothing waits.
+// per thread above 8 x 512).  Each CTA keeps its own copy of row 0 and of the step
+// state the slots read (Ra2Shared) and runs the end-of-step phase on it itself (one
+// thread per physical register), so that phase needs no cluster barrier after it: the
+// copies stay equal because they are computed from the same values.  What all slots add
+// to in a step -- lane-0 triggers and the highest group writing each position (Ra2Agg)
+// -- lives in CTA 0's shared memory, reached through distributed shared memory, one set
+// per step parity; the slots' step records are kept per parity too, so a CTA that has
+// gone on to the next step never overwrites what a slower CTA's end phase still reads
+// (no CTA gets two steps ahead: each step starts with a cluster barrier).  A CTA marks
+// only the symbols of its own slots (cache and global memory); the others see the marks
+// of their own.  A barrier that ORs a flag adds to a word in CTA 0: three words in
+// rotation, the one the next such barrier uses cleared before this one.  The
+// independent functions ran before, so every trigger record is complete and nothing
+// waits.
 namespace cg = cooperative_groups;
 constexpr uint32_t kRaClusterThreads = 512;
 constexpr uint32_t kRaClusterMax = 8;  // the portable cluster size
 
-struct ClusterSlots {
-    uint32_t* cur;  // this CTA's records and caches: the same offsets in every CTA
-    uint32_t* tag;
-    uint32_t* val;
-    uint32_t K;
-    uint32_t per_cta;  // slots per CTA: group j is slot j % per_cta of CTA j / per_cta
-    __device__ const uint32_t* rec(uint32_t slot) const {
-        return cg::this_cluster().map_shared_rank(cur, slot / per_cta) + 4u * (slot % per_cta);
-    }
-    __device__ void mark(const Prog& P, uint32_t owner, uint32_t v) const {
-        P.symswp[v - 64u] = 0xFFFFFFFFu;
-        if (owner == 0xFFFFFFFFu) return;
-        const uint32_t r = owner / per_cta, e = (owner % per_cta) * K + ((v - 64u) & (K - 1u));
-        const uint32_t* t = cg::this_cluster().map_shared_rank(tag, r);
-        uint32_t* x = cg::this_cluster().map_shared_rank(val, r);
-        if (t[e] == v) x[e] |= 0x100u;
-    }
+struct Ra2Agg {
+    uint32_t lcur[64], lmax[64];       // lane-0 triggers of the current round
+    uint32_t lnew[64], lmaxnew[64];    // of the next Jacobi round
+    uint32_t r0grp[64];                // highest group (+1) writing each position
 };
+
+__device__ bool c_marked_before(const Ra2Shared& loc, const Ra2Agg& ag, uint64_t m, uint32_t j, bool with_lane0) {
+    for (; m; m &= m - 1) {
+        const uint32_t p = ctz64(m);
+        uint32_t g = loc.omin[p];
+        if (with_lane0 && ag.lcur[p] < g) g = ag.lcur[p];
+        if (g <= j) return true;
+    }
+    return false;
+}
+__device__ void c_add_triggers(Ra2Agg& ag, uint64_t trig, uint32_t g1, bool into_new) {
+    for (uint64_t t = trig; t; t &= t - 1) {
+        const uint32_t p = ctz64(t);
+        if (into_new) {
+            atomicMin(&ag.lnew[p], g1);
+            atomicMax(&ag.lmaxnew[p], g1);
+        } else {
+            atomicMin(&ag.lcur[p], g1);
+            atomicMax(&ag.lmax[p], g1);
+        }
+    }
+}
+// ra2_compute0, ra2_check, ra2_round, ra2_round_p and ra2_apply (ptl_ra.cuh) with the
+// aggregates apart from the CTA's copy of the step state.
+__device__ bool c_compute0(const Prog& P, const SymCache& c, const Ra2Shared& loc, Ra2Agg& ag, Ra2Slot& L,
+                           uint32_t slot, uint32_t i) {
+    if (!L.act) return false;
+    RaStep& S = L.S;
+    L.r1reg = L.r2reg = 0;
+    L.r1stored = L.r2stored = false;
+    L.m1 = L.m2 = 0;
+    if (s32(S.r1) > 63) {
+        uint32_t d;
+        sym_read(P, c, slot, S.r1, &L.r1reg, &L.r1stored, &d);
+        L.m1 = snap_positions(P, loc, i, S.r1, d);
+    }
+    if (s32(S.r2) > 63) {
+        uint32_t d;
+        sym_read(P, c, slot, S.r2, &L.r2reg, &L.r2stored, &d);
+        L.m2 = snap_positions(P, loc, i, S.r2, d);
+    }
+    L.r1m = c_marked_before(loc, ag, L.m1, L.j, false);
+    L.r2m = c_marked_before(loc, ag, L.m2, L.j, false);
+    ra_compute(S, L.lifetime, L.r1reg, L.r1stored || L.r1m, L.r2reg, L.r2stored || L.r2m);
+    c_add_triggers(ag, S.trig, L.j + 1u, false);
+    return (L.m1 | L.m2) != 0;
+}
+__device__ bool c_check(const Ra2Shared& loc, const Ra2Agg& ag, const Ra2Slot& L) {
+    if (!L.act || (L.m1 | L.m2) == 0) return false;
+    return c_marked_before(loc, ag, L.m1, L.j, true) != L.r1m || c_marked_before(loc, ag, L.m2, L.j, true) != L.r2m;
+}
+__device__ void c_round(const Ra2Shared& loc, Ra2Agg& ag, Ra2Slot& L) {
+    if (!L.act) return;
+    if (L.m1 | L.m2) {
+        L.r1m = c_marked_before(loc, ag, L.m1, L.j, true);
+        L.r2m = c_marked_before(loc, ag, L.m2, L.j, true);
+        ra_compute(L.S, L.lifetime, L.r1reg, L.r1stored || L.r1m, L.r2reg, L.r2stored || L.r2m);
+    }
+    c_add_triggers(ag, L.S.trig, L.j + 1u, true);
+}
+__device__ bool c_round_p(Ra2Agg& ag, uint32_t p) {
+    const bool changed = ag.lnew[p] != ag.lcur[p];
+    ag.lcur[p] = ag.lnew[p];
+    ag.lmax[p] = ag.lmaxnew[p];
+    ag.lnew[p] = 0xFFFFFFFFu;
+    ag.lmaxnew[p] = 0;
+    return changed;
+}
+__device__ void c_apply(const Prog& P, const SymCache& c, const Ra2Shared& loc, Ra2Agg& ag, Ra2Slot& L, uint32_t slot,
+                        uint32_t i, uint32_t* cur) {
+    if (!L.act) return;
+    const RaStep& S = L.S;
+    L.lt_new = S.cleared | S.rdm;
+    const uint32_t g1 = L.j + 1u;
+    auto later = [&](uint64_t m) {
+        for (; m; m &= m - 1) {
+            const uint32_t p = ctz64(m);
+            const uint32_t g = loc.omax[p] > ag.lmax[p] ? loc.omax[p] : ag.lmax[p];
+            if (g > g1) return true;
+        }
+        return false;
+    };
+    const bool l_ord = !P.defpos && s32(S.ord) > 63 && later(snap_positions_hashed(loc, i, S.ord));
+    const bool l_r1 = s32(S.r1) > 63 && later(L.m1);
+    const bool l_r2 = s32(S.r2) > 63 && later(L.m2);
+    if (s32(S.ord) > 63) sym_write(P, c, slot, S.ord, S.rdr, false, (S.rdr & 63u) + 1u);
+    if (s32(S.r1) > 63) sym_write(P, c, slot, S.r1, S.r1r, false);
+    if (s32(S.r2) > 63) sym_write(P, c, slot, S.r2, S.r2r, false);
+    const bool r2v = s32(S.r2) > 63, r1v = s32(S.r1) > 63;
+    if (l_ord) sym_write(P, c, slot, S.ord, (r2v && S.r2 == S.ord) ? S.r2r : ((r1v && S.r1 == S.ord) ? S.r1r : S.rdr), true);
+    if (l_r1) sym_write(P, c, slot, S.r1, (r2v && S.r2 == S.r1) ? S.r2r : S.r1r, true);
+    if (l_r2) sym_write(P, c, slot, S.r2, S.r2r, true);
+    cur[3] = S.rdr & 63u;
+    if (S.ord != 0) atomicMax(&ag.r0grp[S.rdr & 63u], g1);
+    if (S.r1r != S.rdr && s32(S.r1r) >= 0 && S.r1r < 64u) atomicMax(&ag.r0grp[S.r1r], g1);
+    if (S.r2r != S.rdr && s32(S.r2r) >= 0 && S.r2r < 64u) atomicMax(&ag.r0grp[S.r2r], g1);
+}
+// ra2_end_p on this CTA's copy of row 0: the marks of the symbols of its own slots (the
+// owner's record is local), then row 0 takes the highest group's write, whose record
+// may sit in any CTA.  cur: this CTA's records of the step (parity); recs(slot): any
+// slot's, through distributed shared memory.
+__device__ void c_end_p(const Prog& P, const SymCache& c, Ra2Shared& loc, const Ra2Agg& ag, uint32_t p, uint32_t rank,
+                        uint32_t per_cta, const uint32_t* cur) {
+    const bool triggered = loc.omin[p] != 0xFFFFFFFFu || ag.lcur[p] != 0xFFFFFFFFu;
+    const uint32_t v = loc.snap[p];
+    const uint32_t own = loc.snapown[p];
+    const bool mine = own == 0xFFFFFFFFu ? rank == 0 : own / per_cta == rank;
+    if (triggered && s32(v - 64u) >= 0 && mine) {
+        bool updated = false;
+        if (own != 0xFFFFFFFFu) {
+            const uint32_t* u = cur + 4u * (own % per_cta);
+            updated = (s32(u[0]) > 63 && u[0] == v) || (s32(u[1]) > 63 && u[1] == v) || (s32(u[2]) > 63 && u[2] == v);
+        }
+        if (!updated) sym_mark(P, c, own == 0xFFFFFFFFu ? 0xFFFFFFFFu : own % per_cta, v);
+    }
+    const uint32_t g = ag.r0grp[p];
+    if (g != 0) {
+        const uint32_t w = g - 1u;
+        const uint32_t* r = cg::this_cluster().map_shared_rank(const_cast<uint32_t*>(cur), w / per_cta) + 4u * (w % per_cta);
+        loc.R0[p] = (r[0] != 0 && r[3] == p) ? r[0] : 0xFFFFFFFFu;
+        loc.R0own[p] = w;
+    }
+}
 
 template <int Q>
 __global__ void __launch_bounds__(kRaClusterThreads, 1)
@@ -1451,19 +1567,20 @@ __global__ void __launch_bounds__(kRaClusterThreads, 1)
     cg::cluster_group cl = cg::this_cluster();
     const uint32_t rank = cl.block_rank(), tid = threadIdx.x, T = blockDim.x;
     const uint32_t G0 = (P.F + 7u) / 8u;
-    uint32_t* cur = reinterpret_cast<uint32_t*>(smem + sizeof(Ra2Shared));
-    uint32_t* ctag = cur + 4u * per_cta;
+    Ra2Shared& loc = *reinterpret_cast<Ra2Shared*>(smem);  // this CTA's copy of row 0 and the step state
+    Ra2Agg* agl = reinterpret_cast<Ra2Agg*>(smem + sizeof(Ra2Shared));  // [2]: used in CTA 0
+    uint32_t* cur = reinterpret_cast<uint32_t*>(smem + sizeof(Ra2Shared) + 2 * sizeof(Ra2Agg));  // [2][per_cta][4]
+    uint32_t* ctag = cur + 8u * per_cta;
     uint32_t* cval = ctag + per_cta * K;
     const SymCache c{ctag, cval, K};  // this CTA's slots, by local index
-    const ClusterSlots cs{cur, ctag, cval, K, per_cta};
-    const bool row = rank == 0 && tid < 64u;  // a row-0 thread (T >= 64)
+    const bool row = tid < 64u;       // the CTA's row-0 threads (T >= 64)
     const bool hashed = P.defpos == nullptr;
     if (tid == 0) {
         s_s0 = 0;
         s_or[0] = s_or[1] = s_or[2] = 0;
     }
     cl.sync();  // every CTA has started (its shared memory exists) before remote accesses
-    Ra2Shared& sh = *cl.map_shared_rank(reinterpret_cast<Ra2Shared*>(smem), 0);
+    Ra2Agg* ag = cl.map_shared_rank(agl, 0);
     uint32_t* s0p = cl.map_shared_rank(&s_s0, 0);
     uint32_t* orp = cl.map_shared_rank(s_or, 0);
     uint32_t nbar = 0;  // OR barriers so far (the same count in every thread)
@@ -1474,6 +1591,13 @@ __global__ void __launch_bounds__(kRaClusterThreads, 1)
         cl.sync();
         ++nbar;
         return *reinterpret_cast<volatile uint32_t*>(&orp[k]) != 0;
+    };
+    auto reset_agg = [&](Ra2Agg& a, uint32_t p) {
+        a.lcur[p] = 0xFFFFFFFFu;
+        a.lmax[p] = 0;
+        a.lnew[p] = 0xFFFFFFFFu;
+        a.lmaxnew[p] = 0;
+        a.r0grp[p] = 0;
     };
     Ra2Slot L[Q];
 #pragma unroll
@@ -1487,58 +1611,66 @@ __global__ void __launch_bounds__(kRaClusterThreads, 1)
         }
     }
     if (row) {
-        sh.R0[tid] = 0xFFFFFFFFu;
-        sh.R0own[tid] = 0xFFFFFFFFu;
-    }
-    if (rank == 0) {
-        for (uint32_t k = tid; k < kSnapHash; k += T) {
-            sh.hkey[0][k] = sh.hkey[1][k] = 0;
-            sh.hmask[0][k] = sh.hmask[1][k] = 0;
+        loc.R0[tid] = 0xFFFFFFFFu;
+        loc.R0own[tid] = 0xFFFFFFFFu;
+        if (rank == 0) {
+            reset_agg(agl[0], tid);
+            reset_agg(agl[1], tid);
         }
     }
-    cl.sync();
+    for (uint32_t k = tid; k < kSnapHash; k += T) {
+        loc.hkey[0][k] = loc.hkey[1][k] = 0;
+        loc.hmask[0][k] = loc.hmask[1][k] = 0;
+    }
+    __syncthreads();
     uint32_t tmin = 0xFFFFFFFFu, tmax = 0;  // a row-0 thread's trigger records, one step ahead
     if (row && S > 0) {
-        ra2_begin_p(sh, 0, tid, __ldcg(&P.trig_min[tid]), __ldcg(&P.trig_max[tid]), hashed);
+        ra2_begin_p(loc, 0, tid, __ldcg(&P.trig_min[tid]), __ldcg(&P.trig_max[tid]), hashed);
         if (S > 1) {
             tmin = __ldcg(&P.trig_min[64u + tid]);
             tmax = __ldcg(&P.trig_max[64u + tid]);
         }
     }
-    cl.sync();
+    cl.sync();  // the slots' step lengths and CTA 0's aggregates, for every CTA
     const uint32_t s0 = min(*reinterpret_cast<volatile uint32_t*>(s0p), S);
-    // the block's phases per step (ra_lane0_block), with cluster barriers
     for (uint32_t i = 0; i < s0; ++i) {
+        const uint32_t par = i & 1u;
+        Ra2Agg& a = ag[par];
+        uint32_t* curp = cur + par * 4u * per_cta;
         bool in_row0 = false;
 #pragma unroll
         for (int q = 0; q < Q; ++q) {
             const uint32_t l = tid + static_cast<uint32_t>(q) * T;
             if (l < per_cta && rank * per_cta + l < G0) {
-                ra2_load(P, L[q], i, cur + 4u * l);
-                in_row0 |= ra2_compute0(P, c, sh, L[q], l, i);
+                ra2_load(P, L[q], i, curp + 4u * l);
+                in_row0 |= c_compute0(P, c, loc, a, L[q], l, i);
             }
         }
         const bool any_row0 = cluster_or(in_row0);
+        // the other parity's aggregates: every CTA read them last in the previous step's
+        // end phase, before the barrier above; the next step's first writes come after the
+        // barrier below
+        if (rank == 0 && row) reset_agg(ag[par ^ 1u], tid);
         bool flag = false;
 #pragma unroll
         for (int q = 0; q < Q; ++q) {
             const uint32_t l = tid + static_cast<uint32_t>(q) * T;
             if (l < per_cta && rank * per_cta + l < G0) {
-                if (any_row0) flag |= ra2_check(sh, L[q]);
-                ra2_apply(P, c, sh, L[q], l, i, cur + 4u * l);
+                if (any_row0) flag |= c_check(loc, a, L[q]);
+                c_apply(P, c, loc, a, L[q], l, i, curp + 4u * l);
             }
         }
-        if (hashed && row) snap_clear_next(sh, i, tid);
+        if (hashed && row) snap_clear_next(loc, i, tid);
         if (cluster_or(flag)) {
-            if (row) sh.r0grp[tid] = 0;
+            if (rank == 0 && row) a.r0grp[tid] = 0;
             for (uint32_t round = 0;; ++round) {
 #pragma unroll
                 for (int q = 0; q < Q; ++q) {
                     const uint32_t l = tid + static_cast<uint32_t>(q) * T;
-                    if (l < per_cta && rank * per_cta + l < G0) ra2_round(sh, L[q]);
+                    if (l < per_cta && rank * per_cta + l < G0) c_round(loc, a, L[q]);
                 }
                 cl.sync();
-                const bool changed = row && ra2_round_p(sh, tid);
+                const bool changed = rank == 0 && row && c_round_p(a, tid);
                 if (!cluster_or(changed)) break;
                 if (round > G0 + 2u) {
                     if (rank == 0 && tid == 0) record_error(P.err, ST_DEVICE_TIMEOUT, W_RA2, i);
@@ -1548,26 +1680,26 @@ __global__ void __launch_bounds__(kRaClusterThreads, 1)
 #pragma unroll
             for (int q = 0; q < Q; ++q) {
                 const uint32_t l = tid + static_cast<uint32_t>(q) * T;
-                if (l < per_cta && rank * per_cta + l < G0) ra2_apply(P, c, sh, L[q], l, i, cur + 4u * l);
+                if (l < per_cta && rank * per_cta + l < G0) c_apply(P, c, loc, a, L[q], l, i, curp + 4u * l);
             }
             cl.sync();
         }
         if (row) {
-            ra2_end_p_at(P, cs, sh, tid);
+            c_end_p(P, c, loc, a, tid, rank, per_cta, curp);
             if (i + 1 < S) {
-                ra2_begin_p(sh, i + 1, tid, tmin, tmax, hashed);
+                ra2_begin_p(loc, i + 1, tid, tmin, tmax, hashed);
                 if (i + 2 < S) {
                     tmin = __ldcg(&P.trig_min[static_cast<size_t>(i + 2) * 64u + tid]);
                     tmax = __ldcg(&P.trig_max[static_cast<size_t>(i + 2) * 64u + tid]);
                 }
             }
         }
-        cl.sync();
+        __syncthreads();  // this CTA's copy of row 0 is ready for the next step
     }
-    // After the last cluster barrier no CTA touches another's shared memory: CTA 0 reads
-    // only its own row 0 (the marks of the tail end the pass; no cache needs them).
+    cl.sync();  // every end phase has read the other CTAs' records: none exits before
     if (s0 >= S) return;
-    if (row && ra2_tail_hit(P, sh, tid, s0, S)) P.symswp[sh.R0[tid] - 64u] = 0xFFFFFFFFu;
+    // the steps after the last lane-0 one only mark row 0's symbols (global memory)
+    if (rank == 0 && row && ra2_tail_hit(P, loc, tid, s0, S)) P.symswp[loc.R0[tid] - 64u] = 0xFFFFFFFFu;
 }
 
 // flags[1]: functions share symbols; flags[2]: a lane-0 virtual register has two
@@ -2041,7 +2173,7 @@ cudaError_t launch_ra_cluster_q(const Prog& P0, const Prog& Pfree, uint32_t G0, 
     const uint32_t per_cta = (G0 + C - 1u) / C;
     const uint32_t T = std::max(64u, ((per_cta + Q - 1u) / Q + 31u) & ~31u);
     constexpr size_t kBudget = 160u * 1024u;
-    const size_t fixed = sizeof(Ra2Shared) + 16ull * per_cta;
+    const size_t fixed = sizeof(Ra2Shared) + 2 * sizeof(Ra2Agg) + 32ull * per_cta;  // records per step parity
     uint32_t K = 64;
     while (K > 1 && fixed + static_cast<size_t>(per_cta) * K * 8u > kBudget) K >>= 1;
     const size_t smem = fixed + static_cast<size_t>(per_cta) * K * 8u + 16;
