@@ -502,6 +502,47 @@ def run_scalar(trees, device, sample_n):
     return out
 
 
+def run_huge_program(device, steps=3, check=True):
+    """The huge-program configuration (one 64M-node program, 32,768 functions) through the
+    plain pipeline: device time per compile (stage events, median of `steps`), the call
+    with host arrays in and out, and the words against the oracle's restatement (one
+    core, outside the timings)."""
+    from ptilopsis_gb300 import STAGES, RvGenerator
+    from ptilopsis_gb300.synth import config_tree
+    tree = config_tree("c2")
+    n = tree.n
+    with RvGenerator(tree, device=device) as gen:
+        gen.process()
+        dev, stage = [], []
+        for _ in range(steps):
+            gen.process(profile=True, to_host=False)
+            ns = np.array(gen.stage_ns(), dtype=np.float64)
+            dev.append(ns.sum() / 1e9)
+            stage.append(ns)
+        walls = []
+        for _ in range(steps):
+            t0 = time.perf_counter()
+            gen.upload(tree)
+            gen.process()
+            words = gen.get_instructions()
+            table = gen.function_table()
+            walls.append(time.perf_counter() - t0)
+    k = int(np.argsort(dev)[len(dev) // 2])
+    out = {"value": n / dev[k], "e2e_value": n / float(np.median(walls)), "unit": UNIT, "nodes": n,
+           "functions": int(len(table["starts"])), "words": int(len(words)),
+           "sample": f"one program of {n} nodes (configuration c2), median of {steps} compiles",
+           "stage_ms": {s: round(float(v) / 1e6, 3) for s, v in zip(STAGES, stage[k])}}
+    if check:
+        from oracle import portbind
+        t0 = time.perf_counter()
+        ref = portbind.compile_ast(to_ast(tree))
+        out["bit_exact_vs_oracle"] = bool(np.array_equal(words, ref.words)) and bool(
+            np.array_equal(table["starts"], ref.bufs["fn_start"]))
+        out["cpu_baseline"] = {"value": n / (time.perf_counter() - t0), "unit": UNIT, "cores": 1, "kind": "port",
+                               "sample": "the same program, one thread"}
+    return out
+
+
 def run_flatten(trees, device, reps=3):
     """AST flattening (ptl_flatten, the GPU's DepthTree construction) on the 16 largest of
     the first 256 programs, each given in a seeded random node order, through the public
@@ -739,6 +780,8 @@ def run_batched(args):
             line["flatten"] = run_flatten(trees, local)
         if not args.no_scalar:
             line["scalar"] = run_scalar(trees, local, args.scalar_sample)
+        if not args.no_huge:
+            line["huge_program"] = run_huge_program(local, check=not args.no_cpu_baseline)
         if oracle_check is not None:
             line["bit_exact_vs_oracle"] = oracle_check["equal"] == oracle_check["programs"]
             line["oracle_check"] = oracle_check
@@ -890,6 +933,7 @@ def main():
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--no-flatten", action="store_true")
     ap.add_argument("--no-scalar", action="store_true")
+    ap.add_argument("--no-huge", action="store_true", help="skip the 64M-node program (configuration c2)")
     ap.add_argument("--scalar-sample", type=int, default=64)
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--tiles", type=int, nargs=2, metavar=("ELEM", "SWEEP"),
