@@ -502,14 +502,14 @@ def run_scalar(trees, device, sample_n):
     return out
 
 
-def run_huge_program(device, steps=3, check=True):
-    """The huge-program configuration (one 64M-node program, 32,768 functions) through the
-    plain pipeline: device time per compile (stage events, median of `steps`), the call
-    with host arrays in and out, and the words against the oracle's restatement (one
-    core, outside the timings)."""
+def run_single_program(device, config, steps=3, check=True):
+    """One configuration's single program (c1: 4.3M nodes, 2,048 functions, a quarter of
+    them spilling; c2: 64M nodes, 32,768 functions) through the plain pipeline: device
+    time per compile (stage events, median of `steps`), the call with host arrays in and
+    out, and the words against the oracle's restatement (one core, outside the timings)."""
     from ptilopsis_gb300 import STAGES, RvGenerator
     from ptilopsis_gb300.synth import config_tree
-    tree = config_tree("c2")
+    tree = config_tree(config)
     n = tree.n
     with RvGenerator(tree, device=device) as gen:
         gen.process()
@@ -530,7 +530,7 @@ def run_huge_program(device, steps=3, check=True):
     k = int(np.argsort(dev)[len(dev) // 2])
     out = {"value": n / dev[k], "e2e_value": n / float(np.median(walls)), "unit": UNIT, "nodes": n,
            "functions": int(len(table["starts"])), "words": int(len(words)),
-           "sample": f"one program of {n} nodes (configuration c2), median of {steps} compiles",
+           "sample": f"one program of {n} nodes (configuration {config}), median of {steps} compiles",
            "stage_ms": {s: round(float(v) / 1e6, 3) for s, v in zip(STAGES, stage[k])}}
     if check:
         from oracle import portbind
@@ -781,7 +781,8 @@ def run_batched(args):
         if not args.no_scalar:
             line["scalar"] = run_scalar(trees, local, args.scalar_sample)
         if not args.no_huge:
-            line["huge_program"] = run_huge_program(local, check=not args.no_cpu_baseline)
+            line["large_program"] = run_single_program(local, "c1", check=not args.no_cpu_baseline)
+            line["huge_program"] = run_single_program(local, "c2", check=not args.no_cpu_baseline)
         if oracle_check is not None:
             line["bit_exact_vs_oracle"] = oracle_check["equal"] == oracle_check["programs"]
             line["oracle_check"] = oracle_check
@@ -933,7 +934,7 @@ def main():
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--no-flatten", action="store_true")
     ap.add_argument("--no-scalar", action="store_true")
-    ap.add_argument("--no-huge", action="store_true", help="skip the 64M-node program (configuration c2)")
+    ap.add_argument("--no-huge", action="store_true", help="skip the single large and huge programs (c1, c2)")
     ap.add_argument("--scalar-sample", type=int, default=64)
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--tiles", type=int, nargs=2, metavar=("ELEM", "SWEEP"),
