@@ -8,6 +8,8 @@
 #include <cstdio>
 #include <cstring>
 #include <mutex>
+#include <cstdlib>
+#include <map>
 #include <new>
 #include <string>
 #include <vector>
@@ -132,23 +134,65 @@ struct ptl_generator {
 
 namespace {
 
-// Whether the device reads and writes pageable host memory coherently (the
-// cudaDevAttrPageableMemoryAccess attribute), per device, asked once.
-bool pageable_access(int device) {
-    static std::mutex mu;
-    static std::vector<int> known;  // -1 unknown, 0 no, 1 yes
-    std::lock_guard<std::mutex> lk(mu);
-    if (device < 0) return false;
-    if (known.size() <= static_cast<size_t>(device)) known.resize(static_cast<size_t>(device) + 1, -1);
-    if (known[device] < 0) {
-        int v = 0;
-        if (cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccess, device) != cudaSuccess) {
-            cudaGetLastError();
-            v = 0;
-        }
-        known[device] = v ? 1 : 0;
+// How the plain pipeline moves the caller's arrays, per device, decided once: by a copy
+// kernel that reads (writes) pageable host memory in place, where the device accesses
+// it coherently (cudaDevAttrPageableMemoryAccess) and a 32 MB probe of each direction
+// shows that faster than the copy engine's staged copy of pageable memory; else staged.
+// (On some hosts in-place access to pageable memory runs far below the link.)
+struct PageablePaths {
+    bool read = false, write = false;
+};
+PageablePaths probe_pageable(int device) {
+    PageablePaths out;
+    int v = 0;
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccess, device) != cudaSuccess || !v) {
+        cudaGetLastError();
+        return out;
     }
-    return known[device] == 1;
+    constexpr size_t kBytes = size_t(32) << 20;
+    void* host = std::malloc(kBytes);
+    void* dev = nullptr;
+    cudaStream_t s = nullptr;
+    cudaEvent_t ev[5] = {};
+    bool ok = host && cudaMalloc(&dev, kBytes) == cudaSuccess &&
+              cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) == cudaSuccess;
+    for (auto& e : ev) ok = ok && cudaEventCreate(&e) == cudaSuccess;
+    float t[4] = {0, 0, 0, 0};
+    if (ok) {
+        std::memset(host, 1, kBytes);
+        for (int rep = 0; rep < 2 && ok; ++rep) {  // the first round warms every path
+            ok = cudaEventRecord(ev[0], s) == cudaSuccess && kernel_copy(host, dev, kBytes, s) == cudaSuccess &&
+                 cudaEventRecord(ev[1], s) == cudaSuccess &&
+                 cudaMemcpyAsync(dev, host, kBytes, cudaMemcpyHostToDevice, s) == cudaSuccess &&
+                 cudaEventRecord(ev[2], s) == cudaSuccess && kernel_copy(dev, host, kBytes, s) == cudaSuccess &&
+                 cudaEventRecord(ev[3], s) == cudaSuccess &&
+                 cudaMemcpyAsync(host, dev, kBytes, cudaMemcpyDeviceToHost, s) == cudaSuccess &&
+                 cudaEventRecord(ev[4], s) == cudaSuccess && cudaStreamSynchronize(s) == cudaSuccess;
+        }
+        for (int k = 0; k < 4 && ok; ++k) ok = cudaEventElapsedTime(&t[k], ev[k], ev[k + 1]) == cudaSuccess;
+        if (ok) {
+            out.read = t[0] <= t[1];
+            out.write = t[2] <= t[3];
+        }
+    }
+    for (auto& e : ev)
+        if (e) cudaEventDestroy(e);
+    if (s) cudaStreamDestroy(s);
+    if (dev) cudaFree(dev);
+    std::free(host);
+    cudaGetLastError();  // a failed probe leaves no error behind
+    return out;
+}
+const PageablePaths& pageable_paths(int device) {
+    static std::mutex mu;
+    static std::map<int, PageablePaths> known;
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = known.find(device);
+    if (it == known.end()) {
+        const DeviceScope on_device(device);
+        it = known.emplace(device, on_device.ok() ? probe_pageable(device) : PageablePaths{}).first;
+    }
+    return it->second;
 }
 
 ptl_status fail(ptl_generator* g, ptl_status st, const std::string& msg) {
@@ -559,7 +603,7 @@ ptl_status run_pipeline(ptl_generator* g, bool profile, bool to_host, bool row0_
         if (g->W3) {
             // Where the device accesses pageable memory coherently (ATS), kernel stores put
             // the words straight into the vector; otherwise the copy engine stages them.
-            if (pageable_access(g->device) && (reinterpret_cast<uintptr_t>(g->words.data()) & 15u) == 0)
+            if (pageable_paths(g->device).write && (reinterpret_cast<uintptr_t>(g->words.data()) & 15u) == 0)
                 PTL_CU(kernel_copy(P.out, g->words.data(), g->W3 * 4ull, s));
             else
                 PTL_CU(cudaMemcpyAsync(g->words.data(), P.out, g->W3 * 4ull, cudaMemcpyDeviceToHost, s));
@@ -590,7 +634,7 @@ cudaError_t upload_inputs(ptl_generator* g, const ptl_ast_view* tree) {
     // arrays in place (about 200 GB/s, against the staged copies of pageable memory); the
     // call then waits for it, so that the caller may reuse the arrays on return, as after
     // a staged copy.
-    bool direct = !tree->on_device && pageable_access(g->device);
+    bool direct = !tree->on_device && pageable_paths(g->device).read;
     for (auto& x : in) direct = direct && (reinterpret_cast<uintptr_t>(x.src) & 15u) == 0;
     cudaError_t e = cudaSuccess;
     for (auto& x : in) {
@@ -682,7 +726,7 @@ cudaError_t fetch_words(ptl_generator* g, uint32_t* dst, size_t count) {
     if (count == 0) return cudaSuccess;
     const DeviceScope on_device(g->device);
     if (!on_device.ok()) return on_device.err;
-    cudaError_t e = (pageable_access(g->device) && (reinterpret_cast<uintptr_t>(dst) & 15u) == 0)
+    cudaError_t e = (pageable_paths(g->device).write && (reinterpret_cast<uintptr_t>(dst) & 15u) == 0)
                         ? kernel_copy(g->out.at<uint32_t>(), dst, count * 4ull, g->stream)
                         : cudaMemcpyAsync(dst, g->out.at<uint32_t>(), count * 4ull, cudaMemcpyDeviceToHost, g->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
