@@ -762,9 +762,9 @@ def run_batched(args):
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "u32", "data": "synthetic (seeded grammar, no datasets)",
-            "config": batched_config(trees, tot["W3"]),
-            "l2": "working set (~60 GB) > L2; no flush needed",
-            "parallelism": f"replicas x{world} (each GPU its own batch)",
+            "config": {**batched_config(trees, tot["W3"]),
+                       "l2": "inputs and working set (~60 GB) larger than L2; no flush between steps",
+                       "parallelism": f"replicas x{world} (each GPU its own batch)"},
             "tiles": {"elem": bc.tiles()[0], "sweep": bc.tiles()[1],
                       "chosen_by": "defaults" if tiles is None else "--tiles" if args.tiles else
                       "autotune on 512 other programs of the same distribution"},
