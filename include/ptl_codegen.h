@@ -60,8 +60,9 @@ typedef struct ptl_generator ptl_generator;
 ptl_status ptl_generator_create(const ptl_ast_view* tree, int device, ptl_generator** out);
 
 /* Replaces the generator's input with another tree of any size, reusing the device
- * memory of earlier compiles (the reference builds a new generator per tree).  Host
- * trees are copied on the generator's stream. */
+ * memory of earlier compiles (the reference builds a new generator per tree).  A host
+ * tree is on the device when the call returns, so its arrays may be reused; a device
+ * tree is copied on the generator's stream. */
 ptl_status ptl_generator_upload(ptl_generator* gen, const ptl_ast_view* tree);
 
 /* Replaces the scalar generator's constructor, rv_generator_st(const DepthTree&)

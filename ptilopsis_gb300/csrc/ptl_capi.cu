@@ -630,10 +630,9 @@ cudaError_t upload_inputs(ptl_generator* g, const ptl_ast_view* tree) {
     struct { DevBuf* b; const void* src; size_t es; } in[] = {
         {&g->in_type, tree->type, 1}, {&g->in_rtype, tree->rtype, 1}, {&g->in_parent, tree->parent, 4},
         {&g->in_depth, tree->depth, 4}, {&g->in_child, tree->child_idx, 4}, {&g->in_data, tree->data, 4}};
-    // Where the device reads pageable memory coherently (ATS), a kernel reads the caller's
-    // arrays in place (about 200 GB/s, against the staged copies of pageable memory); the
-    // call then waits for it, so that the caller may reuse the arrays on return, as after
-    // a staged copy.
+    // Where the device reads pageable memory coherently (ATS) and that is faster here, a
+    // kernel reads the caller's arrays in place, else the copy engine copies them; either
+    // way the call waits, so that the caller may reuse host arrays on return.
     bool direct = !tree->on_device && pageable_paths(g->device).read;
     for (auto& x : in) direct = direct && (reinterpret_cast<uintptr_t>(x.src) & 15u) == 0;
     cudaError_t e = cudaSuccess;
@@ -645,7 +644,7 @@ cudaError_t upload_inputs(ptl_generator* g, const ptl_ast_view* tree) {
         }
         if (e != cudaSuccess) return e;
     }
-    if (direct) {
+    if (!tree->on_device) {  // the caller may reuse host arrays once this returns
         e = cudaStreamSynchronize(g->stream);
         if (e != cudaSuccess) return e;
     }
