@@ -1867,8 +1867,9 @@ __global__ void __launch_bounds__(32 * kScalarWarpFns) k_batch_s_ra_warp(const P
         const uint32_t p = batch_program(off, B, t);
         const Prog& P = progs[p];
         const uint32_t f = (t - off[p]) * kScalarWarpFns + (threadIdx.x >> 5);
+        // each warp's symbol bytes are its own, reused only by its next function: the warps
+        // of a block go on to their next tiles without waiting for one another
         if (f < P.F) s_ra_warp_function(P, f, P.s_preserve, stride, s_wsym + (threadIdx.x >> 5) * stride);
-        __syncthreads();  // the warps' symbol bytes are reused by the next tile
     }
 }
 
